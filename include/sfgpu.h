@@ -1,0 +1,253 @@
+/*
+ * sfgpu.h - C ABI of the GB300-native Levenberg-Marquardt back end for SymForce's sym::Optimizer.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, never throws, and returns an
+ * int32 status (SFG_OK == 0).  sfg_last_error() returns a thread-local message for the last
+ * failure on the calling thread.  Device memory is owned by the handle; host arrays passed in are
+ * borrowed for the duration of the call only (the reference Optimizer copies factors in and updates
+ * Values in place: symforce/opt/optimizer.tcc:20-40, symforce/opt/internal/optimizer_utils.h:69).
+ *
+ * One handle = one CUDA stream; a handle is not thread safe, handles on different threads are
+ * independent (symforce/opt/optimizer.h:23 "Not thread safe! Create one per thread.").
+ */
+#ifndef SFGPU_H_
+#define SFGPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SFG_ABI_VERSION 1
+
+/* ---------------------------------------------------------------------------------------------
+ * Status codes.  Solver outcomes (SUCCESS / HIT_ITERATION_LIMIT / FAILED) are not errors: they are
+ * reported in sfg_stats_t exactly like the reference reports them in OptimizationStats
+ * (symforce/opt/internal/optimizer_utils.h:45-64).  Errors are what the reference raises with
+ * SYM_ASSERT (symforce/opt/assert.h:41-47).
+ * ------------------------------------------------------------------------------------------- */
+enum {
+  SFG_OK = 0,
+  SFG_ERR_INVALID_ARGUMENT = 1, /* bad sizes, bad key/factor kinds, null pointers */
+  SFG_ERR_CUDA = 2,             /* a CUDA runtime call failed (message in sfg_last_error) */
+  SFG_ERR_NO_DEVICE = 3,        /* no CUDA device visible: there is no CPU fallback */
+  SFG_ERR_STRUCTURE = 4,        /* structure not supported (e.g. Schur block C not block diagonal) */
+  SFG_ERR_DEVICE_STATUS = 5,    /* a device loop hit its hard cap or saw non-finite values */
+  SFG_ERR_OUT_OF_MEMORY = 6,
+  SFG_ERR_CAPACITY = 7          /* a caller-provided output buffer is too small */
+};
+
+/* Optimization status and LM failure reasons: same integer values as the reference LCM enums
+ * optimization_status_t / levenberg_marquardt_solver_failure_reason_t
+ * (lcmtypes/symforce.lcm:279-300). */
+enum { SFG_STATUS_INVALID = 0, SFG_STATUS_SUCCESS = 1, SFG_STATUS_HIT_ITERATION_LIMIT = 2,
+       SFG_STATUS_FAILED = 3 };
+enum { SFG_FAILURE_INVALID = 0, SFG_FAILURE_LAMBDA_OUT_OF_BOUNDS = 1,
+       SFG_FAILURE_INITIAL_ERROR_NOT_FINITE = 2 };
+
+/* lambda_update_type_t (lcmtypes/symforce.lcm:117-131). */
+enum { SFG_LAMBDA_UPDATE_INVALID = 0, SFG_LAMBDA_UPDATE_STATIC = 1, SFG_LAMBDA_UPDATE_DYNAMIC = 2 };
+
+/* ---------------------------------------------------------------------------------------------
+ * Variable (key) types.  Storage / tangent layouts are the reference's:
+ *   VEC1..VEC3: storage = tangent = n scalars, Retract is +=   (symforce/opt/values.cc:303-309)
+ *   POSE2: storage [re, im, x, y], tangent [theta, x, y]        (gen/cpp/sym/ops/pose2/lie_group_ops.cc:58-82)
+ *   POSE3: storage [qx, qy, qz, qw, x, y, z], tangent [w(3), t(3)]
+ *          Retract q <- q * exp(w) with eps-regularised norm, t <- t + dt
+ *                                                               (gen/cpp/sym/ops/pose3/lie_group_ops.cc:69-102)
+ * ------------------------------------------------------------------------------------------- */
+enum { SFG_KEY_VEC1 = 1, SFG_KEY_VEC2 = 2, SFG_KEY_VEC3 = 3, SFG_KEY_POSE2 = 4, SFG_KEY_POSE3 = 5 };
+
+/* ---------------------------------------------------------------------------------------------
+ * Typed factor kinds.  The reference stores a factor as a type-erased std::function
+ * (symforce/opt/factor.h:99-119) that a GPU cannot call, so each factor batch names one of these
+ * kinds, its keys (indices into the key table) and its constants.  Residual conventions follow the
+ * reference's generated factors; consts are laid out per factor, factor-major.
+ *
+ *  BEARING_POSE2      keys [pose2]                consts [lx, ly, angle, epsilon, sqrt_info]
+ *      r = sqrt_info * wrap_angle(atan2(tb.y, tb.x + copysign(eps, tb.x)) - angle),
+ *      tb = pose^-1 * landmark   (symforce/examples/robot_2d_localization/gen/bearing_factor.h:21-97)
+ *  ODOMETRY_POSE2     keys [pose2 a, pose2 b]     consts [dist, epsilon, sqrt_info]
+ *      r = sqrt_info * (sqrt(|tb - ta|^2 + eps) - dist)
+ *                                (symforce/examples/robot_2d_localization/gen/odometry_factor.h:21-98)
+ *  SNAVELY_REPROJECTION keys [pose3 cam_T_world, vec3 (f,k1,k2), vec3 point]
+ *                     consts [px, py, epsilon, cauchy_delta]
+ *      e = f*(1 + k1 |p|^2 + k2 |p|^4) * p - pixel, p = pc.xy / -pc.z, pc = cam_T_world * point
+ *      (symforce/examples/bundle_adjustment_in_the_large/bundle_adjustment_in_the_large.py:18-63);
+ *      cauchy_delta > 0 whitens the norm with the Cauchy loss (Barron alpha=0 limit,
+ *      symforce/opt/noise_models.py:318-428 whiten_norm): r = sqrt(2 rho(n)) / n * e,
+ *      n = sqrt(|e|^2 + eps), rho(n) = delta^2 log(1 + n^2 / (2 delta^2)).  0 = no loss.
+ *  BETWEEN_POSE3      keys [pose3 a, pose3 b]     consts [a_T_b (7 storage), sqrt_info_diag (6), epsilon]
+ *      r = diag(s) * local_coordinates(a_T_b, a^-1 * b)     (gen/cpp/sym/factors/between_factor_pose3.h)
+ *  PRIOR_POSE3        keys [pose3]                consts [prior (7 storage), sqrt_info_diag (6), epsilon]
+ *      r = diag(s) * local_coordinates(prior, value)        (gen/cpp/sym/factors/prior_factor_pose3.h)
+ *  RANGE_POSE3        keys [pose3]                consts [lx, ly, lz, range, sqrt_info, epsilon]
+ *      r = sqrt_info * (sqrt(|t - l|^2 + eps) - range)   (no reference counterpart; written in the
+ *      same style as the odometry factor)
+ * ------------------------------------------------------------------------------------------- */
+enum {
+  SFG_FACTOR_BEARING_POSE2 = 1,
+  SFG_FACTOR_ODOMETRY_POSE2 = 2,
+  SFG_FACTOR_SNAVELY_REPROJECTION = 3,
+  SFG_FACTOR_BETWEEN_POSE3 = 4,
+  SFG_FACTOR_PRIOR_POSE3 = 5,
+  SFG_FACTOR_RANGE_POSE3 = 6
+};
+
+typedef struct sfg_factor_batch_t {
+  int32_t kind;          /* SFG_FACTOR_* */
+  int32_t count;         /* number of factors in the batch (may be 0) */
+  const int32_t* keys;   /* [count * num_keys(kind)] indices into the problem's key table */
+  const double* consts;  /* [count * num_consts(kind)] */
+} sfg_factor_batch_t;
+
+/* A problem: the keys to optimize, in state-vector order (the reference's Linearizer key order,
+ * symforce/opt/linearizer.cc:148-158), plus factor batches.  Residual rows are laid out batch by
+ * batch, factor by factor.  If num_schur_keys > 0, the last num_schur_keys keys (all VEC3 and not
+ * sharing a factor with each other) are eliminated by a Schur complement, as SparseSchurSolver
+ * does for a block-diagonal C (symforce/opt/sparse_schur_solver.tcc:15-97). */
+typedef struct sfg_problem_t {
+  int32_t num_keys;
+  const int32_t* key_types;          /* [num_keys] SFG_KEY_* */
+  int32_t num_batches;
+  const sfg_factor_batch_t* batches; /* [num_batches] */
+  int32_t num_schur_keys;
+} sfg_problem_t;
+
+/* Plain-old-data mirror of optimizer_params_t (lcmtypes/symforce.lcm:134-200); defaults are
+ * sfg_default_optimizer_params(), matching sym::DefaultOptimizerParams (symforce/opt/optimizer.cc:8-56).
+ * verbose / check_derivatives / include_jacobians / debug_checks are accepted and ignored by the
+ * device path (no per-iteration host logging; derivative checks live in the tests). */
+typedef struct sfg_optimizer_params_t {
+  int32_t verbose;
+  int32_t debug_stats;
+  int32_t check_derivatives;
+  int32_t include_jacobians;
+  int32_t debug_checks;
+  double initial_lambda;
+  double lambda_lower_bound;
+  double lambda_upper_bound;
+  int32_t lambda_update_type;
+  double lambda_up_factor;
+  double lambda_down_factor;
+  double dynamic_lambda_update_beta;
+  double dynamic_lambda_update_gamma;
+  int32_t dynamic_lambda_update_p;
+  int32_t use_diagonal_damping;
+  int32_t use_unit_damping;
+  int32_t keep_max_diagonal_damping;
+  double diagonal_damping_min;
+  int32_t iterations;
+  double early_exit_min_reduction;
+  double early_exit_min_absolute_error;
+  int32_t enable_bold_updates;
+} sfg_optimizer_params_t;
+
+/* One record of optimization_iteration_t (lcmtypes/symforce.lcm:229-262) plus the device time
+ * (ms since the start of the optimize call, read from the GPU global timer when the record was
+ * written).  The update/values/residual debug vectors are not recorded. */
+typedef struct sfg_iteration_t {
+  int32_t iteration;
+  int32_t update_accepted;
+  double current_lambda;
+  double new_error_linear;
+  double new_error;
+  double relative_reduction;
+  double update_angle_change;
+  double best_error;    /* error of the best state after this iteration */
+  double elapsed_ms;    /* device time since the optimize call started */
+} sfg_iteration_t;
+
+/* optimization_stats_t (lcmtypes/symforce.lcm:302-336).  `iterations` is caller-owned with room
+ * for `capacity` records (params.iterations + 1 suffices). */
+typedef struct sfg_stats_t {
+  sfg_iteration_t* iterations;
+  int32_t capacity;
+  int32_t num_iterations;
+  int32_t best_index;
+  int32_t status;
+  int32_t failure_reason;
+  int32_t _pad;
+} sfg_stats_t;
+
+/* Forms of the solver (besides the plain FP64 drop-in). */
+enum { SFG_PRECISION_FP64 = 0, SFG_PRECISION_MIXED = 1 };
+enum { SFG_LINEAR_SOLVER_SPARSE_LDLT = 0, SFG_LINEAR_SOLVER_SCHUR = 1 };
+enum { SFG_ORDERING_NESTED_DISSECTION = 0, SFG_ORDERING_NATURAL = 1, SFG_ORDERING_MIN_DEGREE = 2 };
+
+typedef struct sfg_form_params_t {
+  int32_t precision;      /* SFG_PRECISION_* */
+  int32_t linear_solver;  /* SFG_LINEAR_SOLVER_*; SCHUR requires problem.num_schur_keys > 0 */
+  int32_t ordering;       /* SFG_ORDERING_* (block level) */
+  int32_t device;         /* CUDA device ordinal */
+  double epsilon;         /* the Optimizer's epsilon (symforce/opt/optimizer.h:90-94); default 10 * DBL_EPSILON */
+  int32_t refine_steps;   /* MIXED: max FP64 iterative-refinement steps on the reduced system */
+  int32_t _pad;
+  double refine_tol;      /* MIXED: relative residual at which refinement stops */
+} sfg_form_params_t;
+
+typedef struct sfg_handle sfg_handle;
+
+/* -------------------------------- library --------------------------------------------------- */
+int32_t sfg_abi_version(void);
+const char* sfg_last_error(void);
+void sfg_default_optimizer_params(sfg_optimizer_params_t* out);
+void sfg_default_form_params(sfg_form_params_t* out);
+int32_t sfg_key_dims(int32_t key_type, int32_t* storage_dim, int32_t* tangent_dim);
+int32_t sfg_factor_dims(int32_t kind, int32_t* num_keys, int32_t* num_consts, int32_t* residual_dim);
+
+/* -------------------------------- sym::Optimizer --------------------------------------------
+ * Replaces sym::Optimizer<double> construction (symforce/opt/optimizer.h:86-111) plus the first
+ * Linearizer / LinearSolver analysis: uploads the structure, builds the block-sparse Hessian
+ * layout, the Schur pair lists and the supernodal symbolic factorization.                      */
+int32_t sfg_create(const sfg_problem_t* problem, const sfg_form_params_t* form, sfg_handle** out);
+int32_t sfg_destroy(sfg_handle* h);
+/* Values: the storage of every key of the problem, concatenated in key order. */
+int32_t sfg_storage_dim(const sfg_handle* h, int64_t* storage_dim, int64_t* tangent_dim,
+                        int64_t* residual_dim);
+int32_t sfg_set_values(sfg_handle* h, const double* storage, int64_t n);
+/* Optimizer::Optimize(values, num_iterations, populate_best_linearization, stats)
+ * (symforce/opt/optimizer.tcc:79-89): runs the whole LM loop on the device; num_iterations < 0
+ * means params->iterations.  Values stay on the device until sfg_get_values. */
+int32_t sfg_optimize(sfg_handle* h, const sfg_optimizer_params_t* params, int32_t num_iterations,
+                     sfg_stats_t* stats);
+/* GetBestValues (symforce/opt/levenberg_marquardt_solver.h:178-182). */
+int32_t sfg_get_values(sfg_handle* h, double* storage, int64_t n);
+/* Linearize the problem at the current values and return residual (M), rhs (N) and error; the
+ * Hessian is returned in the reference's CSC lower layout (symforce/opt/linearizer.cc:148-356):
+ * pass null arrays to query nnz. */
+int32_t sfg_linearize(sfg_handle* h, double* residual, double* rhs, double* error);
+int32_t sfg_hessian_lower(sfg_handle* h, int64_t* nnz, int32_t* col_ptr, int32_t* row_idx,
+                          double* values);
+/* The block ordering used by the linear solver, as new position of every state scalar. */
+int32_t sfg_permutation(sfg_handle* h, int32_t* perm, int64_t n);
+
+/* -------------------------------- SparseCholeskySolver -------------------------------------
+ * The LinearSolver concept on a user CSC lower matrix (symforce/opt/sparse_cholesky/
+ * sparse_cholesky_solver.h:28-163): AnalyzeSparsityPattern -> sfg_ldlt_create, Factorize ->
+ * sfg_ldlt_factorize, Solve/SolveInPlace -> sfg_ldlt_solve.  LDL^T with unit L, no pivoting.    */
+typedef struct sfg_ldlt sfg_ldlt;
+int32_t sfg_ldlt_create(int32_t n, const int32_t* col_ptr, const int32_t* row_idx,
+                        int32_t ordering, int32_t device, sfg_ldlt** out);
+int32_t sfg_ldlt_factorize(sfg_ldlt* s, const double* values);
+int32_t sfg_ldlt_solve(sfg_ldlt* s, const double* b, double* x, int32_t nrhs);
+int32_t sfg_ldlt_diagonal(sfg_ldlt* s, double* d);        /* D() in the solver's ordering */
+int32_t sfg_ldlt_permutation(sfg_ldlt* s, int32_t* perm);  /* Permutation(): new index of old i */
+int32_t sfg_ldlt_destroy(sfg_ldlt* s);
+
+/* -------------------------------- SparseSchurSolver ----------------------------------------
+ * symforce/opt/sparse_schur_solver.h:62-135: A (CSC lower) = [[B, E^T],[E, C]] with C block
+ * diagonal and dense blocks; ComputeSymbolicSparsity(A, C_dim) -> sfg_schur_create,
+ * Factorize -> sfg_schur_factorize, Solve -> sfg_schur_solve.                                  */
+typedef struct sfg_schur sfg_schur;
+int32_t sfg_schur_create(int32_t n, const int32_t* col_ptr, const int32_t* row_idx, int32_t c_dim,
+                         int32_t device, sfg_schur** out);
+int32_t sfg_schur_factorize(sfg_schur* s, const double* values);
+int32_t sfg_schur_solve(sfg_schur* s, const double* b, double* x, int32_t nrhs);
+int32_t sfg_schur_destroy(sfg_schur* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SFGPU_H_ */

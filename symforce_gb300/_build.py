@@ -1,0 +1,83 @@
+"""Build the in-tree CUDA library libsfgpu.so for sm_103a (nvcc, no cmake).
+
+Translation units compile in parallel; the shared library lands in symforce_gb300/lib/ (git-ignored).
+Rebuilds only when a source is newer than the library.
+"""
+
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+INCLUDE = PKG.parent / "include"
+OUT_DIR = PKG / "lib"
+BUILD_DIR = PKG / "_build"
+LIB = OUT_DIR / "libsfgpu.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CUDA_SOURCES = ["kernels_lin.cu", "kernels_lm.cu", "kernels_solve.cu", "api.cu", "api_solvers.cu"]
+HOST_SOURCES = ["host_structure.cpp", "host_layout.cpp"]
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _sources():
+    return [CSRC / s for s in CUDA_SOURCES + HOST_SOURCES]
+
+
+def _deps():
+    return list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
+
+
+def _stale() -> bool:
+    if not LIB.exists():
+        return True
+    t = LIB.stat().st_mtime
+    return any(p.stat().st_mtime > t for p in _sources() + _deps() + [Path(__file__)])
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    if not force and not _stale():
+        return LIB
+    nvcc = _nvcc()
+    BUILD_DIR.mkdir(exist_ok=True)
+    OUT_DIR.mkdir(exist_ok=True)
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo", f"-I{INCLUDE}", f"-I{CSRC}"]
+
+    def compile_one(src: Path) -> Path:
+        obj = BUILD_DIR / (src.name + ".o")
+        if src.suffix == ".cu":
+            cmd = [nvcc, *ARCH, *common, "-c", str(src), "-o", str(obj)]
+        else:
+            cmd = [nvcc, *common, "-x", "c++", "-c", str(src), "-o", str(obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        if verbose and r.stderr:
+            print(r.stderr)
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(compile_one, _sources()))
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart_static", "-lrt",
+           "-lpthread", "-ldl"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

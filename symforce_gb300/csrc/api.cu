@@ -1,0 +1,731 @@
+// The C ABI (include/sfgpu.h): handle lifetime, device buffers, and the CUDA graph that runs the
+// whole Levenberg-Marquardt loop on the device (a prologue, then a conditional while node whose
+// body is one LevenbergMarquardtSolver::Iterate).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "layout.h"
+
+namespace sfg {
+
+thread_local std::string g_last_error;
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------
+// device memory helpers
+// ---------------------------------------------------------------------------------------------
+struct DeviceArena {
+  std::vector<void*> ptrs;
+  ~DeviceArena() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  void* Alloc(size_t bytes) {
+    void* p = nullptr;
+    if (bytes == 0) bytes = 16;
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess)
+      throw Error(e == cudaErrorMemoryAllocation ? SFG_ERR_OUT_OF_MEMORY : SFG_ERR_CUDA,
+                  std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+    ptrs.push_back(p);
+    return p;
+  }
+  template <typename T>
+  T* Upload(const std::vector<T>& v) {
+    T* p = static_cast<T*>(Alloc(v.size() * sizeof(T)));
+    if (!v.empty()) SFG_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return p;
+  }
+  template <typename T>
+  T* Zeros(size_t n) {
+    T* p = static_cast<T*>(Alloc(n * sizeof(T)));
+    SFG_CUDA(cudaMemset(p, 0, n * sizeof(T)));
+    return p;
+  }
+};
+
+void CheckDevice(int device) {
+  int n = 0;
+  const cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    throw Error(SFG_ERR_NO_DEVICE, "no CUDA device is visible; this library has no CPU fallback");
+  if (device < 0 || device >= n) throw Error(SFG_ERR_INVALID_ARGUMENT, "bad device ordinal");
+  SFG_CUDA(cudaSetDevice(device));
+}
+
+// Device copy of a symbolic factorization + task plan.
+struct FactorPlan {
+  Symbolic sym;
+  TaskPlan plan;
+  FactorDev f{};
+  int grid_factor = 0, grid_solve = 0;
+  size_t elem = 8;
+  void* F = nullptr;       // front pool
+  void* ycon = nullptr;
+  void* ysave = nullptr;
+  void* xperm = nullptr;
+  int nflags = 0;
+};
+
+void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, int ordering,
+                     size_t elem, int* error_word, const LmState* st, int64_t a_stride,
+                     int64_t b_stride, int num_sms) {
+  fp.elem = elem;
+  fp.sym = Analyze(pat, ordering);
+  const Symbolic& S = fp.sym;
+  fp.plan = PlanTasks(S, elem == 8 ? 16 : 32);
+  const TaskPlan& T = fp.plan;
+  // device arrays
+  FactorDev& f = fp.f;
+  f.ns = S.ns;
+  f.ntasks = int(T.tasks.size());
+  f.tile = T.tile;
+  f.tasks = A.Upload(T.tasks);
+  f.sn_w = A.Upload(S.sn_w);
+  f.sn_m = A.Upload(S.sn_m);
+  f.sn_foff = A.Upload(S.sn_foff);
+  f.tile_base = A.Upload(T.tile_base);
+  f.npiv = A.Upload(T.npiv);
+  f.ntiles = A.Upload(T.ntiles);
+  f.asm_off = A.Upload(S.asm_off);
+  std::vector<AsmDev> asms(S.asms.size());
+  for (size_t q = 0; q < S.asms.size(); ++q) {
+    const auto& a = S.asms[q];
+    AsmDev d;
+    d.src = a.src;
+    d.dscal = 0;
+    d.row0 = a.row0;
+    d.col0 = a.col0;
+    d.di = a.di;
+    d.dj = a.dj;
+    d.transpose = a.transpose;
+    d.diag = a.diag;
+    asms[q] = d;
+  }
+  // diagonal blocks: original scalar offset of the block (for damping)
+  {
+    // map each diagonal assembly entry back to its original block: src offset -> block
+    std::vector<int64_t> src_to_block_scalar;
+    for (int j = 0; j < pat.nb; ++j)
+      for (int64_t q = pat.colptr[j]; q < pat.colptr[j + 1]; ++q)
+        if (pat.rows[q] == j) {
+          for (auto& a : asms)
+            if (a.diag && a.src == pat.boff[q]) a.dscal = pat.off[j];
+        }
+  }
+  f.asms = A.Upload(asms);
+  f.rel_off = A.Upload(S.rel_off);
+  f.rel = A.Upload(S.rel);
+  std::vector<int32_t> cptr(S.ns + 1, 0), clist;
+  for (int s = 0; s < S.ns; ++s) {
+    for (int c : S.sn_children[s]) clist.push_back(c);
+    cptr[s + 1] = int32_t(clist.size());
+  }
+  f.child_ptr = A.Upload(cptr);
+  f.child_list = A.Upload(clist);
+  f.parent = A.Upload(S.sn_parent);
+  f.idx_off = A.Upload(S.idx_off);
+  f.idx = A.Upload(S.idx);
+  std::vector<int32_t> scalar_old(S.n);
+  for (int q = 0; q < S.nb; ++q) {
+    const int old = S.border[q];
+    for (int t = 0; t < pat.dim[old]; ++t) scalar_old[S.pstart[q] + t] = int32_t(pat.off[old] + t);
+  }
+  f.scalar_old = A.Upload(scalar_old);
+  f.tile_state = A.Zeros<int>(std::max(T.nstates, 1));
+  f.counters = A.Zeros<int>(2);
+  fp.nflags = 2 * S.ns;
+  f.front_flags = A.Zeros<int>(std::max(fp.nflags, 1));
+  f.error = error_word;
+  int maxm = 1;
+  for (int s = 0; s < S.ns; ++s) maxm = std::max(maxm, S.sn_m[s]);
+  f.max_m = maxm;
+  f.st = st;
+  f.a_stride = a_stride;
+  f.b_stride = b_stride;
+  fp.F = A.Alloc(size_t(S.front_pool) * elem);
+  fp.ycon = A.Alloc(size_t(std::max<int64_t>(S.rel_off[S.ns], 1)) * elem);
+  fp.ysave = A.Alloc(size_t(std::max<int64_t>(S.idx_off[S.ns], 1)) * elem);
+  fp.xperm = A.Alloc(size_t(std::max<int64_t>(S.n, 1)) * elem);
+  const int per_sm = 8;
+  fp.grid_factor = std::max(1, std::min<int>(f.ntasks, num_sms * per_sm));
+  fp.grid_solve = std::max(1, std::min<int>(2 * S.ns, num_sms * per_sm));
+  if (elem == 8) ConfigureSolve<double>(maxm);
+  else ConfigureSolve<float>(maxm);
+}
+
+template <typename T>
+void RunFactorAndSolve(const FactorPlan& fp, const void* A, const double* damping, const void* b,
+                       void* x, cudaStream_t s) {
+  LaunchResetFactorState(fp.f.tile_state, fp.plan.nstates, fp.f.front_flags, fp.nflags,
+                         fp.f.counters, s);
+  LaunchFactor<T>(fp.f, A, damping, fp.F, fp.grid_factor, s);
+  LaunchSolve<T>(fp.f, fp.F, b, fp.ycon, fp.ysave, fp.xperm, x, fp.grid_solve, s);
+}
+
+}  // namespace
+}  // namespace sfg
+
+// =============================================================================================
+// Handle
+// =============================================================================================
+struct sfg_handle {
+  sfg::DeviceArena arena;
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  sfg::HostProblem P;
+  sfg::LinLayout L;
+  bool schur = false;
+  sfg::SchurLayout SL;
+  int precision = SFG_PRECISION_FP64;
+  size_t elem = 8;
+  double epsilon = 10 * DBL_EPSILON;
+  sfg::FactorPlan fp;
+  // buffers
+  double* values = nullptr;     // [3][S]
+  double* values_in = nullptr;  // [S]
+  double* residual = nullptr;   // [3][M]
+  void* hess = nullptr;         // [3][nvals]
+  void* rhs = nullptr;          // [3][N]
+  void* stage = nullptr;
+  double* cost_partials = nullptr;
+  int ncost = 0;
+  int64_t* key_soff = nullptr;
+  int64_t* key_toff = nullptr;
+  int32_t* key_type = nullptr;
+  std::vector<sfg::BatchDev> batches;
+  std::vector<int> batch_kind;
+  sfg::ReduceDev red{};
+  sfg::DampDev damp{};
+  double* update = nullptr;
+  double* last_update = nullptr;
+  double* delta_partials = nullptr;
+  sfg::LmState* st = nullptr;
+  sfg::LmParams* params = nullptr;
+  sfg_iteration_t* records = nullptr;
+  int records_cap = 0;
+  // schur
+  sfg::SchurDev sd{};
+  void *cinv = nullptr, *W = nullptr, *tp = nullptr, *S = nullptr, *v = nullptr, *y = nullptr;
+  void* xsol = nullptr;
+  // graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool have_graph = false;
+  bool values_set = false;
+  int last_linearized_block = -1;
+
+  ~sfg_handle() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace sfg {
+namespace {
+
+LinOut MakeLinOut(sfg_handle* h, int which) {
+  LinOut o;
+  o.values = h->values;
+  o.key_soff = h->key_soff;
+  o.residual = h->residual;
+  o.hess = h->hess;
+  o.rhs = h->rhs;
+  o.stage = h->stage;
+  o.cost_partials = h->cost_partials;
+  o.S = h->P.S;
+  o.M = h->P.M;
+  o.N = h->P.N;
+  o.nvals = h->L.nvals;
+  o.st = h->st;
+  o.which = which;
+  return o;
+}
+
+template <typename T>
+void EnqueueLinearize(sfg_handle* h, int which, cudaStream_t s) {
+  const LinOut o = MakeLinOut(h, which);
+  for (size_t b = 0; b < h->batches.size(); ++b) LaunchLinearize<T>(h->batch_kind[b], o, h->batches[b], s);
+  LaunchReduceStage<T>(h->red, o, s);
+  LaunchFinishCost(h->cost_partials, h->ncost, h->st, which, s);
+}
+
+template <typename T>
+void EnqueueIterationBody(sfg_handle* h, cudaGraphConditionalHandle cond, cudaStream_t s) {
+  const int64_t N = h->P.N;
+  LaunchDamping<T>(h->damp, h->hess, h->L.nvals, h->params, h->st, s);
+  if (h->schur) {
+    LaunchSchurPoints<T>(h->sd, h->hess, h->rhs, h->L.nvals, N, h->damp.damping, h->cinv, h->W, h->tp,
+                         h->st, s);
+    LaunchSchurBuildS<T>(h->sd, h->hess, h->L.nvals, h->damp.damping, h->W, h->S, h->st, s);
+    LaunchSchurRhs<T>(h->sd, h->hess, h->L.nvals, h->rhs, N, h->tp, h->v, h->st, s);
+    RunFactorAndSolve<T>(h->fp, h->S, nullptr, h->v, h->y, s);
+    LaunchSchurBackSub<T>(h->sd, h->y, h->W, h->tp, h->update, s);
+  } else {
+    RunFactorAndSolve<T>(h->fp, h->hess, h->damp.damping, h->rhs, h->xsol, s);
+    LaunchNegate<T>(h->xsol, h->update, N, s);
+  }
+  RetractDev r;
+  r.nkeys = h->P.nkeys;
+  r.key_type = h->key_type;
+  r.soff = h->key_soff;
+  r.toff = h->key_toff;
+  r.values = h->values;
+  r.S = h->P.S;
+  r.update = h->update;
+  LaunchRetract(r, h->params, h->st, s);
+  EnqueueLinearize<T>(h, 1, s);
+  LaunchLinearDelta<T>(h->update, h->rhs, h->damp.damping, h->last_update, N, h->delta_partials,
+                       h->st, 1, s);
+  LaunchDecide(h->params, h->st, h->records, h->update, h->last_update, N, h->delta_partials,
+               DeltaPartials(), cond, s);
+}
+
+template <typename T>
+void BuildGraph(sfg_handle* h) {
+  if (h->exec) {
+    cudaGraphExecDestroy(h->exec);
+    h->exec = nullptr;
+  }
+  if (h->graph) {
+    cudaGraphDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  cudaGraph_t g;
+  SFG_CUDA(cudaGraphCreate(&g, 0));
+  h->graph = g;
+  cudaGraphConditionalHandle cond;
+  SFG_CUDA(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
+  cudaStream_t s = h->stream;
+  SFG_CUDA(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  // prologue: Reset, Step, relinearize Init, initial record
+  LaunchCopyValues(h->values_in, h->values, h->P.S, h->st, 1, s);
+  LaunchBegin(h->params, h->st, 0, s);
+  EnqueueLinearize<T>(h, 0, s);
+  LaunchFirstRecord(h->params, h->st, h->records, cond, s);
+  // conditional while node
+  cudaStreamCaptureStatus status;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  SFG_CUDA(cudaStreamGetCaptureInfo(s, &status, nullptr, nullptr, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = cond;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cnode;
+  std::vector<cudaGraphNode_t> dv(deps, deps + ndeps);
+  SFG_CUDA(cudaGraphAddNode(&cnode, g, dv.data(), nullptr, dv.size(), &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  SFG_CUDA(cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+  // epilogue: best values back into the input buffer
+  LaunchCopyBest(h->values, h->values_in, h->P.S, h->st, s);
+  SFG_CUDA(cudaStreamEndCapture(s, &g));
+  // body
+  cudaStream_t bs;
+  SFG_CUDA(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
+  SFG_CUDA(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  EnqueueIterationBody<T>(h, cond, bs);
+  cudaGraph_t body_out;
+  SFG_CUDA(cudaStreamEndCapture(bs, &body_out));
+  cudaStreamDestroy(bs);
+  SFG_CUDA(cudaGraphInstantiate(&h->exec, g, 0));
+  h->have_graph = true;
+}
+
+void ToLmParams(const sfg_optimizer_params_t& p, int iterations, double eps, LmParams* o) {
+  o->initial_lambda = p.initial_lambda;
+  o->lambda_lower_bound = p.lambda_lower_bound;
+  o->lambda_upper_bound = p.lambda_upper_bound;
+  o->lambda_up_factor = p.lambda_up_factor;
+  o->lambda_down_factor = p.lambda_down_factor;
+  o->dynamic_beta = p.dynamic_lambda_update_beta;
+  o->dynamic_gamma = p.dynamic_lambda_update_gamma;
+  o->diagonal_damping_min = p.diagonal_damping_min;
+  o->early_exit_min_reduction = p.early_exit_min_reduction;
+  o->early_exit_min_absolute_error = p.early_exit_min_absolute_error;
+  o->epsilon = eps;
+  o->lambda_update_type = p.lambda_update_type;
+  o->dynamic_p = p.dynamic_lambda_update_p;
+  o->use_diagonal_damping = p.use_diagonal_damping;
+  o->use_unit_damping = p.use_unit_damping;
+  o->keep_max_diagonal_damping = p.keep_max_diagonal_damping;
+  o->enable_bold_updates = p.enable_bold_updates;
+  o->iterations = iterations;
+}
+
+template <typename F>
+int32_t Guard(F&& fn) {
+  try {
+    fn();
+    return SFG_OK;
+  } catch (const Error& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host out of memory";
+    return SFG_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return SFG_ERR_INVALID_ARGUMENT;
+  }
+}
+
+void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, sfg_handle* h) {
+  sfg_form_params_t fm;
+  sfg_default_form_params(&fm);
+  if (form) fm = *form;
+  if (fm.precision != SFG_PRECISION_FP64 && fm.precision != SFG_PRECISION_MIXED)
+    throw Error(SFG_ERR_INVALID_ARGUMENT, "unknown precision");
+  CheckDevice(fm.device);
+  h->device = fm.device;
+  SFG_CUDA(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, fm.device));
+  h->P = ParseProblem(problem);
+  h->precision = fm.precision;
+  if (fm.precision == SFG_PRECISION_MIXED)
+    throw Error(SFG_ERR_INVALID_ARGUMENT, "mixed precision form is not available in this build");
+  h->elem = 8;
+  h->epsilon = fm.epsilon;
+  h->schur = fm.linear_solver == SFG_LINEAR_SOLVER_SCHUR;
+  if (h->schur && h->P.num_schur == 0)
+    throw Error(SFG_ERR_INVALID_ARGUMENT, "Schur solver requires num_schur_keys > 0");
+  h->L = BuildLinLayout(h->P);
+  if (h->schur) h->SL = BuildSchurLayout(h->P, h->L);
+  SFG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  DeviceArena& A = h->arena;
+  const HostProblem& P = h->P;
+  const size_t E = h->elem;
+  h->values = A.Zeros<double>(3 * size_t(P.S));
+  h->values_in = A.Zeros<double>(size_t(P.S));
+  h->residual = A.Zeros<double>(3 * size_t(std::max<int64_t>(P.M, 1)));
+  h->hess = A.Alloc(3 * size_t(h->L.nvals) * E);
+  SFG_CUDA(cudaMemset(h->hess, 0, 3 * size_t(h->L.nvals) * E));
+  h->rhs = A.Alloc(3 * size_t(P.N) * E);
+  h->stage = A.Alloc(size_t(std::max<int64_t>(h->L.nstage, 1)) * E);
+  std::vector<int64_t> soff(P.soff.begin(), P.soff.begin() + P.nkeys);
+  std::vector<int64_t> toff(P.toff.begin(), P.toff.begin() + P.nkeys);
+  h->key_soff = A.Upload(soff);
+  h->key_toff = A.Upload(toff);
+  h->key_type = A.Upload(std::vector<int32_t>(P.key_type.begin(), P.key_type.end()));
+  // batches
+  int partial = 0;
+  const int lb = LinearizeBlockSize();
+  for (size_t b = 0; b < P.batches.size(); ++b) {
+    const HostBatch& B = P.batches[b];
+    BatchDev d{};
+    d.count = B.count;
+    d.nent = h->L.maps[b].nent;
+    std::vector<int32_t> keys(size_t(B.count) * B.nk);
+    for (int f = 0; f < B.count; ++f)
+      for (int k = 0; k < B.nk; ++k) keys[size_t(k) * B.count + f] = B.keys[size_t(f) * B.nk + k];
+    std::vector<double> consts(size_t(B.count) * B.nc);
+    for (int f = 0; f < B.count; ++f)
+      for (int c = 0; c < B.nc; ++c) consts[size_t(c) * B.count + f] = B.consts[size_t(f) * B.nc + c];
+    d.keys = A.Upload(keys);
+    d.consts = A.Upload(consts);
+    d.dest = A.Upload(h->L.maps[b].dest);
+    d.roff = B.roff;
+    d.partial_base = partial;
+    partial += (B.count + lb - 1) / lb;
+    h->batches.push_back(d);
+    h->batch_kind.push_back(B.kind);
+  }
+  h->ncost = std::max(partial, 1);
+  h->cost_partials = A.Zeros<double>(h->ncost);
+  h->red.ngroups = int(h->L.red_dst.size());
+  h->red.dst = A.Upload(h->L.red_dst);
+  h->red.ptr = A.Upload(h->L.red_ptr);
+  h->damp.N = P.N;
+  h->damp.diag_off = A.Upload(h->L.diag_off);
+  h->damp.damping = A.Zeros<double>(size_t(P.N));
+  h->damp.max_diagonal = A.Zeros<double>(size_t(P.N));
+  h->update = A.Zeros<double>(size_t(P.N));
+  h->last_update = A.Zeros<double>(size_t(P.N));
+  h->delta_partials = A.Zeros<double>(4 * size_t(DeltaPartials()));
+  h->st = static_cast<LmState*>(A.Alloc(sizeof(LmState)));
+  {
+    LmState s0{};
+    s0.init_idx = 0;
+    s0.new_idx = 1;
+    s0.best_idx = 0;
+    s0.free_idx = 2;
+    s0.iteration = -1;
+    SFG_CUDA(cudaMemcpy(h->st, &s0, sizeof(LmState), cudaMemcpyHostToDevice));
+  }
+  h->params = static_cast<LmParams*>(A.Alloc(sizeof(LmParams)));
+  int* err_word = &h->st->device_error;
+  if (h->schur) {
+    const SchurLayout& S = h->SL;
+    SchurDev& d = h->sd;
+    d.npoints = S.npoints;
+    d.nB = int(S.nB);
+    d.c_toff = S.c_toff;
+    d.pt_diag = A.Upload(S.pt_diag);
+    d.pt_eptr = A.Upload(S.pt_eptr);
+    d.pt_ekey_toff = A.Upload(S.pt_ekey_toff);
+    d.pt_ekey_dim = A.Upload(S.pt_ekey_dim);
+    d.pt_eoff = A.Upload(S.pt_eoff);
+    d.pt_woff = A.Upload(S.pt_woff);
+    d.nsblocks = int(S.Spat.nblocks());
+    d.sb_ptr = A.Upload(S.sb_ptr);
+    d.sb_eoff = A.Upload(S.sb_eoff);
+    d.sb_woff = A.Upload(S.sb_woff);
+    d.sb_hoff = A.Upload(S.sb_hoff);
+    d.sb_soff = A.Upload(S.sb_soff);
+    d.sb_dk = A.Upload(S.sb_dk);
+    d.sb_dl = A.Upload(S.sb_dl);
+    d.sb_diag_toff = A.Upload(S.sb_diag_toff);
+    d.r_ptr = A.Upload(S.r_ptr);
+    d.r_eoff = A.Upload(S.r_eoff);
+    d.r_ecol = A.Upload(S.r_ecol);
+    d.r_dk = A.Upload(S.r_dk);
+    d.r_pt = A.Upload(S.r_pt);
+    h->cinv = A.Alloc(9 * size_t(std::max(S.npoints, 1)) * E);
+    h->W = A.Alloc(size_t(std::max<int64_t>(S.nW, 1)) * E);
+    h->tp = A.Alloc(3 * size_t(std::max(S.npoints, 1)) * E);
+    h->S = A.Alloc(size_t(std::max<int64_t>(S.Spat.nvals(), 1)) * E);
+    h->v = A.Alloc(size_t(std::max<int64_t>(S.nB, 1)) * E);
+    h->y = A.Alloc(size_t(std::max<int64_t>(S.nB, 1)) * E);
+    BuildFactorPlan(A, h->fp, S.Spat, fm.ordering, E, err_word, h->st, 0, 0, h->num_sms);
+  } else {
+    h->xsol = A.Alloc(size_t(P.N) * E);
+    BuildFactorPlan(A, h->fp, h->L.H, fm.ordering, E, err_word, h->st, h->L.nvals, P.N, h->num_sms);
+  }
+  SFG_CUDA(cudaDeviceSynchronize());
+}
+
+void EnsureRecords(sfg_handle* h, int cap) {
+  if (cap <= h->records_cap) return;
+  int c = std::max(cap, 64);
+  h->records = static_cast<sfg_iteration_t*>(h->arena.Alloc(size_t(c) * sizeof(sfg_iteration_t)));
+  h->records_cap = c;
+  h->have_graph = false;
+}
+
+}  // namespace
+}  // namespace sfg
+
+// =============================================================================================
+// extern "C"
+// =============================================================================================
+using sfg::Error;
+using sfg::Guard;
+
+extern "C" {
+
+int32_t sfg_abi_version(void) { return SFG_ABI_VERSION; }
+
+const char* sfg_last_error(void) { return sfg::g_last_error.c_str(); }
+
+void sfg_default_optimizer_params(sfg_optimizer_params_t* o) {
+  // sym::DefaultOptimizerParams (symforce/opt/optimizer.cc:8-56)
+  std::memset(o, 0, sizeof(*o));
+  o->initial_lambda = 1.0;
+  o->lambda_lower_bound = 0.0;
+  o->lambda_upper_bound = 1000000.0;
+  o->lambda_update_type = SFG_LAMBDA_UPDATE_STATIC;
+  o->lambda_up_factor = 4.0;
+  o->lambda_down_factor = 1 / 4.0;
+  o->dynamic_lambda_update_beta = 2.0;
+  o->dynamic_lambda_update_gamma = 3.0;
+  o->dynamic_lambda_update_p = 3;
+  o->use_diagonal_damping = 0;
+  o->use_unit_damping = 1;
+  o->keep_max_diagonal_damping = 0;
+  o->diagonal_damping_min = 1e-6;
+  o->iterations = 50;
+  o->early_exit_min_reduction = 1e-6;
+  o->early_exit_min_absolute_error = 0.0;
+  o->enable_bold_updates = 0;
+}
+
+void sfg_default_form_params(sfg_form_params_t* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->precision = SFG_PRECISION_FP64;
+  o->linear_solver = SFG_LINEAR_SOLVER_SPARSE_LDLT;
+  o->ordering = SFG_ORDERING_NESTED_DISSECTION;
+  o->device = 0;
+  o->epsilon = 10 * DBL_EPSILON;
+  o->refine_steps = 10;
+  o->refine_tol = 1e-12;
+}
+
+int32_t sfg_key_dims(int32_t key_type, int32_t* storage_dim, int32_t* tangent_dim) {
+  return Guard([&] {
+    int s, t;
+    sfg::KeyDims(key_type, &s, &t);
+    if (storage_dim) *storage_dim = s;
+    if (tangent_dim) *tangent_dim = t;
+  });
+}
+
+int32_t sfg_factor_dims(int32_t kind, int32_t* num_keys, int32_t* num_consts, int32_t* residual_dim) {
+  return Guard([&] {
+    const sfg::FactorSpec s = sfg::Spec(kind);
+    if (num_keys) *num_keys = s.nkeys;
+    if (num_consts) *num_consts = s.nconsts;
+    if (residual_dim) *residual_dim = s.rdim;
+  });
+}
+
+int32_t sfg_create(const sfg_problem_t* problem, const sfg_form_params_t* form, sfg_handle** out) {
+  if (!out) {
+    sfg::g_last_error = "out is null";
+    return SFG_ERR_INVALID_ARGUMENT;
+  }
+  *out = nullptr;
+  auto h = std::make_unique<sfg_handle>();
+  const int32_t rc = Guard([&] { sfg::CreateHandle(problem, form, h.get()); });
+  if (rc == SFG_OK) *out = h.release();
+  return rc;
+}
+
+int32_t sfg_destroy(sfg_handle* h) {
+  if (!h) return SFG_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  delete h;
+  return SFG_OK;
+}
+
+int32_t sfg_storage_dim(const sfg_handle* h, int64_t* storage_dim, int64_t* tangent_dim,
+                        int64_t* residual_dim) {
+  if (!h) return SFG_ERR_INVALID_ARGUMENT;
+  if (storage_dim) *storage_dim = h->P.S;
+  if (tangent_dim) *tangent_dim = h->P.N;
+  if (residual_dim) *residual_dim = h->P.M;
+  return SFG_OK;
+}
+
+int32_t sfg_set_values(sfg_handle* h, const double* storage, int64_t n) {
+  return Guard([&] {
+    if (!h || !storage) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (n != h->P.S) throw Error(SFG_ERR_INVALID_ARGUMENT, "values size mismatch");
+    SFG_CUDA(cudaSetDevice(h->device));
+    SFG_CUDA(cudaMemcpyAsync(h->values_in, storage, size_t(n) * sizeof(double), cudaMemcpyHostToDevice,
+                             h->stream));
+    SFG_CUDA(cudaStreamSynchronize(h->stream));
+    h->values_set = true;
+  });
+}
+
+int32_t sfg_optimize(sfg_handle* h, const sfg_optimizer_params_t* params, int32_t num_iterations,
+                     sfg_stats_t* stats) {
+  return Guard([&] {
+    if (!h || !params) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (!h->values_set) throw Error(SFG_ERR_INVALID_ARGUMENT, "sfg_set_values was not called");
+    if (params->lambda_update_type != SFG_LAMBDA_UPDATE_STATIC &&
+        params->lambda_update_type != SFG_LAMBDA_UPDATE_DYNAMIC)
+      throw Error(SFG_ERR_INVALID_ARGUMENT, "Invalid lambda update type");
+    const int iters = num_iterations < 0 ? params->iterations : num_iterations;
+    if (iters <= 0) throw Error(SFG_ERR_INVALID_ARGUMENT, "num_iterations must be positive");
+    SFG_CUDA(cudaSetDevice(h->device));
+    sfg::EnsureRecords(h, iters + 1);
+    if (!h->have_graph) sfg::BuildGraph<double>(h);
+    sfg::LmParams lp;
+    sfg::ToLmParams(*params, iters, h->epsilon, &lp);
+    SFG_CUDA(cudaMemcpyAsync(h->params, &lp, sizeof(lp), cudaMemcpyHostToDevice, h->stream));
+    SFG_CUDA(cudaGraphLaunch(h->exec, h->stream));
+    SFG_CUDA(cudaStreamSynchronize(h->stream));
+    sfg::LmState st;
+    SFG_CUDA(cudaMemcpy(&st, h->st, sizeof(st), cudaMemcpyDeviceToHost));
+    if (st.device_error)
+      throw Error(SFG_ERR_DEVICE_STATUS, "device loop hit its cap (code " + std::to_string(st.device_error) + ")");
+    if (stats) {
+      stats->num_iterations = st.num_records;
+      stats->best_index = st.best_index;
+      stats->status = st.status;
+      stats->failure_reason = st.failure_reason;
+      if (stats->iterations) {
+        if (stats->capacity < st.num_records)
+          throw Error(SFG_ERR_CAPACITY, "stats->iterations too small");
+        SFG_CUDA(cudaMemcpy(stats->iterations, h->records, sizeof(sfg_iteration_t) * st.num_records,
+                            cudaMemcpyDeviceToHost));
+      }
+    }
+  });
+}
+
+int32_t sfg_get_values(sfg_handle* h, double* storage, int64_t n) {
+  return Guard([&] {
+    if (!h || !storage) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (n != h->P.S) throw Error(SFG_ERR_INVALID_ARGUMENT, "values size mismatch");
+    SFG_CUDA(cudaSetDevice(h->device));
+    SFG_CUDA(cudaMemcpyAsync(storage, h->values_in, size_t(n) * sizeof(double), cudaMemcpyDeviceToHost,
+                             h->stream));
+    SFG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int32_t sfg_linearize(sfg_handle* h, double* residual, double* rhs, double* error) {
+  return Guard([&] {
+    if (!h) throw Error(SFG_ERR_INVALID_ARGUMENT, "null handle");
+    if (!h->values_set) throw Error(SFG_ERR_INVALID_ARGUMENT, "sfg_set_values was not called");
+    SFG_CUDA(cudaSetDevice(h->device));
+    sfg::LmState st;
+    SFG_CUDA(cudaMemcpy(&st, h->st, sizeof(st), cudaMemcpyDeviceToHost));
+    const int blk = st.best_idx == 2 ? 1 : 2;  // any block that does not hold the best values
+    const int which = 2 + blk;
+    cudaStream_t s = h->stream;
+    sfg::LaunchCopyValues(h->values_in, h->values, h->P.S, h->st, which, s);
+    sfg::EnqueueLinearize<double>(h, which, s);
+    SFG_CUDA(cudaStreamSynchronize(s));
+    SFG_CUDA(cudaGetLastError());
+    h->last_linearized_block = blk;
+    if (residual)
+      SFG_CUDA(cudaMemcpy(residual, h->residual + size_t(blk) * h->P.M, sizeof(double) * h->P.M,
+                          cudaMemcpyDeviceToHost));
+    if (rhs)
+      SFG_CUDA(cudaMemcpy(rhs, static_cast<double*>(h->rhs) + size_t(blk) * h->P.N,
+                          sizeof(double) * h->P.N, cudaMemcpyDeviceToHost));
+    if (error) {
+      SFG_CUDA(cudaMemcpy(&st, h->st, sizeof(st), cudaMemcpyDeviceToHost));
+      *error = st.error[blk];
+    }
+  });
+}
+
+int32_t sfg_hessian_lower(sfg_handle* h, int64_t* nnz, int32_t* col_ptr, int32_t* row_idx,
+                          double* values) {
+  return Guard([&] {
+    if (!h || !nnz) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    const auto& L = h->L;
+    *nnz = int64_t(L.csc_rowidx.size());
+    if (col_ptr) std::copy(L.csc_colptr.begin(), L.csc_colptr.end(), col_ptr);
+    if (row_idx) std::copy(L.csc_rowidx.begin(), L.csc_rowidx.end(), row_idx);
+    if (values) {
+      if (h->last_linearized_block < 0) throw Error(SFG_ERR_INVALID_ARGUMENT, "call sfg_linearize first");
+      std::vector<double> hv(L.nvals);
+      SFG_CUDA(cudaSetDevice(h->device));
+      SFG_CUDA(cudaMemcpy(hv.data(), static_cast<double*>(h->hess) + size_t(h->last_linearized_block) * L.nvals,
+                          sizeof(double) * L.nvals, cudaMemcpyDeviceToHost));
+      for (size_t q = 0; q < L.csc_src.size(); ++q) values[q] = hv[L.csc_src[q]];
+    }
+  });
+}
+
+int32_t sfg_permutation(sfg_handle* h, int32_t* perm, int64_t n) {
+  return Guard([&] {
+    if (!h || !perm) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    const sfg::Symbolic& S = h->fp.sym;
+    if (n != S.n) throw Error(SFG_ERR_INVALID_ARGUMENT, "size mismatch");
+    const sfg::BlockPattern& pat = h->schur ? h->SL.Spat : h->L.H;
+    for (int q = 0; q < S.nb; ++q) {
+      const int old = S.border[q];
+      for (int t = 0; t < pat.dim[old]; ++t) perm[pat.off[old] + t] = int32_t(S.pstart[q] + t);
+    }
+  });
+}
+
+// ---- standalone SparseCholeskySolver / SparseSchurSolver: provided by api_solvers.cu
+}  // extern "C"

@@ -1,0 +1,453 @@
+// Standalone linear solvers of the C ABI: the LinearSolver concept on a user CSC matrix
+// (SparseCholeskySolver, symforce/opt/sparse_cholesky/sparse_cholesky_solver.h:28-163) and the
+// Schur-complement solver (SparseSchurSolver, symforce/opt/sparse_schur_solver.h:62-135), both
+// running the same device kernels as the optimizer.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "layout.h"
+
+namespace sfg {
+extern thread_local std::string g_last_error;
+}
+
+namespace {
+
+using sfg::Error;
+
+struct Arena {
+  std::vector<void*> ptrs;
+  ~Arena() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  void* Alloc(size_t bytes) {
+    void* p = nullptr;
+    if (bytes == 0) bytes = 16;
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess)
+      throw Error(e == cudaErrorMemoryAllocation ? SFG_ERR_OUT_OF_MEMORY : SFG_ERR_CUDA,
+                  std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    ptrs.push_back(p);
+    return p;
+  }
+  template <typename T>
+  T* Upload(const std::vector<T>& v) {
+    T* p = static_cast<T*>(Alloc(v.size() * sizeof(T)));
+    if (!v.empty()) SFG_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return p;
+  }
+  template <typename T>
+  T* Zeros(size_t n) {
+    T* p = static_cast<T*>(Alloc(std::max<size_t>(n, 1) * sizeof(T)));
+    SFG_CUDA(cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T)));
+    return p;
+  }
+};
+
+template <typename F>
+int32_t Guard(F&& fn) {
+  try {
+    fn();
+    return SFG_OK;
+  } catch (const Error& e) {
+    sfg::g_last_error = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    sfg::g_last_error = e.what();
+    return SFG_ERR_INVALID_ARGUMENT;
+  }
+}
+
+void SelectDevice(int device) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+    throw Error(SFG_ERR_NO_DEVICE, "no CUDA device is visible; this library has no CPU fallback");
+  if (device < 0 || device >= n) throw Error(SFG_ERR_INVALID_ARGUMENT, "bad device ordinal");
+  SFG_CUDA(cudaSetDevice(device));
+}
+
+// Device plan of one LDL^T (shared by both standalone solvers).
+struct Plan {
+  sfg::Symbolic sym;
+  sfg::TaskPlan tp;
+  sfg::FactorDev f{};
+  void *F = nullptr, *ycon = nullptr, *ysave = nullptr, *xperm = nullptr;
+  int nflags = 0, grid_factor = 1, grid_solve = 1;
+};
+
+void MakePlan(Arena& A, Plan& p, const sfg::BlockPattern& pat, int ordering, int* err,
+              const sfg::LmState* st, int num_sms) {
+  p.sym = sfg::Analyze(pat, ordering);
+  p.tp = sfg::PlanTasks(p.sym, 16);
+  const auto& S = p.sym;
+  const auto& T = p.tp;
+  sfg::FactorDev& f = p.f;
+  f.ns = S.ns;
+  f.ntasks = int(T.tasks.size());
+  f.tile = T.tile;
+  f.tasks = A.Upload(T.tasks);
+  f.sn_w = A.Upload(S.sn_w);
+  f.sn_m = A.Upload(S.sn_m);
+  f.sn_foff = A.Upload(S.sn_foff);
+  f.tile_base = A.Upload(T.tile_base);
+  f.npiv = A.Upload(T.npiv);
+  f.ntiles = A.Upload(T.ntiles);
+  f.asm_off = A.Upload(S.asm_off);
+  std::vector<sfg::AsmDev> asms(S.asms.size());
+  for (size_t q = 0; q < S.asms.size(); ++q) {
+    const auto& a = S.asms[q];
+    asms[q] = sfg::AsmDev{a.src, 0, a.row0, a.col0, a.di, a.dj, a.transpose, a.diag};
+  }
+  f.asms = A.Upload(asms);
+  f.rel_off = A.Upload(S.rel_off);
+  f.rel = A.Upload(S.rel);
+  std::vector<int32_t> cptr(S.ns + 1, 0), clist;
+  for (int s = 0; s < S.ns; ++s) {
+    for (int c : S.sn_children[s]) clist.push_back(c);
+    cptr[s + 1] = int32_t(clist.size());
+  }
+  f.child_ptr = A.Upload(cptr);
+  f.child_list = A.Upload(clist);
+  f.parent = A.Upload(S.sn_parent);
+  f.idx_off = A.Upload(S.idx_off);
+  f.idx = A.Upload(S.idx);
+  std::vector<int32_t> scalar_old(S.n);
+  for (int q = 0; q < S.nb; ++q) {
+    const int old = S.border[q];
+    for (int t = 0; t < pat.dim[old]; ++t) scalar_old[S.pstart[q] + t] = int32_t(pat.off[old] + t);
+  }
+  f.scalar_old = A.Upload(scalar_old);
+  f.tile_state = A.Zeros<int>(T.nstates);
+  f.counters = A.Zeros<int>(2);
+  p.nflags = 2 * S.ns;
+  f.front_flags = A.Zeros<int>(p.nflags);
+  f.error = err;
+  int maxm = 1;
+  for (int s = 0; s < S.ns; ++s) maxm = std::max(maxm, S.sn_m[s]);
+  f.max_m = maxm;
+  f.st = st;
+  f.a_stride = 0;
+  f.b_stride = 0;
+  p.F = A.Alloc(size_t(S.front_pool) * sizeof(double));
+  p.ycon = A.Alloc(size_t(std::max<int64_t>(S.rel_off[S.ns], 1)) * sizeof(double));
+  p.ysave = A.Alloc(size_t(std::max<int64_t>(S.idx_off[S.ns], 1)) * sizeof(double));
+  p.xperm = A.Alloc(size_t(std::max<int64_t>(S.n, 1)) * sizeof(double));
+  p.grid_factor = std::max(1, std::min(f.ntasks, num_sms * 8));
+  p.grid_solve = std::max(1, std::min(2 * S.ns, num_sms * 8));
+  sfg::ConfigureSolve<double>(maxm);
+}
+
+void CheckError(const sfg::LmState* st) {
+  int e = 0;
+  SFG_CUDA(cudaMemcpy(&e, &st->device_error, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) throw Error(SFG_ERR_DEVICE_STATUS, "device factorization hit its wait cap");
+}
+
+sfg::LmState* MakeState(Arena& A) {
+  sfg::LmState s0{};
+  auto* st = static_cast<sfg::LmState*>(A.Alloc(sizeof(sfg::LmState)));
+  SFG_CUDA(cudaMemcpy(st, &s0, sizeof(s0), cudaMemcpyHostToDevice));
+  return st;
+}
+
+// Validate a lower CSC structure.
+void CheckCsc(int32_t n, const int32_t* col_ptr, const int32_t* row_idx) {
+  if (n <= 0 || !col_ptr || !row_idx) throw Error(SFG_ERR_INVALID_ARGUMENT, "bad CSC arguments");
+  if (col_ptr[0] != 0) throw Error(SFG_ERR_INVALID_ARGUMENT, "col_ptr[0] must be 0");
+  for (int c = 0; c < n; ++c) {
+    if (col_ptr[c + 1] < col_ptr[c]) throw Error(SFG_ERR_INVALID_ARGUMENT, "col_ptr not monotone");
+    for (int32_t q = col_ptr[c]; q < col_ptr[c + 1]; ++q)
+      if (row_idx[q] < c || row_idx[q] >= n)
+        throw Error(SFG_ERR_INVALID_ARGUMENT, "CSC must hold the lower triangle only");
+  }
+}
+
+}  // namespace
+
+struct sfg_ldlt {
+  Arena A;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int32_t n = 0;
+  sfg::BlockPattern pat;
+  Plan plan;
+  sfg::LmState* st = nullptr;
+  std::vector<int64_t> csc_to_val;
+  double* vals = nullptr;
+  double* b = nullptr;
+  double* x = nullptr;
+  bool factored = false;
+  ~sfg_ldlt() {
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+struct sfg_schur {
+  Arena A;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int32_t n = 0, c_dim = 0;
+  sfg::HostProblem P;
+  sfg::LinLayout L;
+  sfg::SchurLayout SL;
+  sfg::SchurDev sd{};
+  Plan plan;
+  sfg::LmState* st = nullptr;
+  std::vector<int64_t> csc_to_val;
+  double *hess = nullptr, *rhs = nullptr, *damping = nullptr, *cinv = nullptr, *W = nullptr,
+         *tp = nullptr, *S = nullptr, *v = nullptr, *y = nullptr, *update = nullptr;
+  bool factored = false;
+  ~sfg_schur() {
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+extern "C" {
+
+int32_t sfg_ldlt_create(int32_t n, const int32_t* col_ptr, const int32_t* row_idx, int32_t ordering,
+                        int32_t device, sfg_ldlt** out) {
+  if (!out) return SFG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  auto s = std::make_unique<sfg_ldlt>();
+  const int32_t rc = Guard([&] {
+    CheckCsc(n, col_ptr, row_idx);
+    SelectDevice(device);
+    s->device = device;
+    s->n = n;
+    std::vector<std::pair<int, int>> pairs;
+    for (int c = 0; c < n; ++c)
+      for (int32_t q = col_ptr[c]; q < col_ptr[c + 1]; ++q) pairs.push_back({row_idx[q], c});
+    s->pat = sfg::MakePattern(std::vector<int>(n, 1), pairs);
+    s->csc_to_val.resize(col_ptr[n]);
+    for (int c = 0; c < n; ++c)
+      for (int32_t q = col_ptr[c]; q < col_ptr[c + 1]; ++q)
+        s->csc_to_val[q] = s->pat.boff[s->pat.Find(row_idx[q], c)];
+    SFG_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    s->st = MakeState(s->A);
+    int sms = 0;
+    SFG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    MakePlan(s->A, s->plan, s->pat, ordering, &s->st->device_error, s->st, sms);
+    s->vals = s->A.Zeros<double>(size_t(s->pat.nvals()));
+    s->b = s->A.Zeros<double>(size_t(n));
+    s->x = s->A.Zeros<double>(size_t(n));
+  });
+  if (rc == SFG_OK) *out = s.release();
+  return rc;
+}
+
+int32_t sfg_ldlt_factorize(sfg_ldlt* s, const double* values) {
+  return Guard([&] {
+    if (!s || !values) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    SFG_CUDA(cudaSetDevice(s->device));
+    std::vector<double> v(s->pat.nvals(), 0.0);
+    for (size_t q = 0; q < s->csc_to_val.size(); ++q) v[s->csc_to_val[q]] += values[q];
+    SFG_CUDA(cudaMemcpy(s->vals, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice));
+    const Plan& p = s->plan;
+    sfg::LaunchResetFactorState(p.f.tile_state, p.tp.nstates, p.f.front_flags, p.nflags,
+                                p.f.counters, s->stream);
+    sfg::LaunchFactor<double>(p.f, s->vals, nullptr, p.F, p.grid_factor, s->stream);
+    SFG_CUDA(cudaStreamSynchronize(s->stream));
+    SFG_CUDA(cudaGetLastError());
+    CheckError(s->st);
+    s->factored = true;
+  });
+}
+
+int32_t sfg_ldlt_solve(sfg_ldlt* s, const double* b, double* x, int32_t nrhs) {
+  return Guard([&] {
+    if (!s || !b || !x || nrhs < 1) throw Error(SFG_ERR_INVALID_ARGUMENT, "bad argument");
+    if (!s->factored) throw Error(SFG_ERR_INVALID_ARGUMENT, "factorize first");
+    SFG_CUDA(cudaSetDevice(s->device));
+    const Plan& p = s->plan;
+    for (int r = 0; r < nrhs; ++r) {
+      SFG_CUDA(cudaMemcpyAsync(s->b, b + size_t(r) * s->n, sizeof(double) * s->n, cudaMemcpyHostToDevice,
+                               s->stream));
+      sfg::LaunchResetFactorState(p.f.tile_state, 0, p.f.front_flags, p.nflags, p.f.counters, s->stream);
+      sfg::LaunchSolve<double>(p.f, p.F, s->b, p.ycon, p.ysave, p.xperm, s->x, p.grid_solve, s->stream);
+      SFG_CUDA(cudaMemcpyAsync(x + size_t(r) * s->n, s->x, sizeof(double) * s->n, cudaMemcpyDeviceToHost,
+                               s->stream));
+      SFG_CUDA(cudaStreamSynchronize(s->stream));
+      CheckError(s->st);
+    }
+  });
+}
+
+int32_t sfg_ldlt_diagonal(sfg_ldlt* s, double* d) {
+  return Guard([&] {
+    if (!s || !d) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (!s->factored) throw Error(SFG_ERR_INVALID_ARGUMENT, "factorize first");
+    const auto& S = s->plan.sym;
+    std::vector<double> F(S.front_pool);
+    SFG_CUDA(cudaMemcpy(F.data(), s->plan.F, sizeof(double) * F.size(), cudaMemcpyDeviceToHost));
+    for (int q = 0; q < S.ns; ++q)
+      for (int c = 0; c < S.sn_w[q]; ++c)
+        d[S.idx[S.idx_off[q] + c]] = F[S.sn_foff[q] + int64_t(c) * (S.sn_m[q] + 1)];
+  });
+}
+
+int32_t sfg_ldlt_permutation(sfg_ldlt* s, int32_t* perm) {
+  return Guard([&] {
+    if (!s || !perm) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    const auto& S = s->plan.sym;
+    for (int q = 0; q < S.nb; ++q) perm[S.border[q]] = int32_t(S.pstart[q]);
+  });
+}
+
+int32_t sfg_ldlt_destroy(sfg_ldlt* s) {
+  if (s) {
+    cudaSetDevice(s->device);
+    delete s;
+  }
+  return SFG_OK;
+}
+
+int32_t sfg_schur_create(int32_t n, const int32_t* col_ptr, const int32_t* row_idx, int32_t c_dim,
+                         int32_t device, sfg_schur** out) {
+  if (!out) return SFG_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  auto s = std::make_unique<sfg_schur>();
+  const int32_t rc = Guard([&] {
+    CheckCsc(n, col_ptr, row_idx);
+    if (c_dim <= 0 || c_dim >= n || c_dim % 3 != 0)
+      throw Error(SFG_ERR_STRUCTURE, "C must be made of 3x3 diagonal blocks");
+    SelectDevice(device);
+    s->device = device;
+    s->n = n;
+    s->c_dim = c_dim;
+    const int nb = n - c_dim, npts = c_dim / 3;
+    sfg::HostProblem& P = s->P;
+    P.nkeys = nb + npts;
+    P.tdim.assign(nb, 1);
+    P.tdim.insert(P.tdim.end(), npts, 3);
+    P.sdim = P.tdim;
+    P.key_type.assign(P.nkeys, SFG_KEY_VEC1);
+    for (int k = nb; k < P.nkeys; ++k) P.key_type[k] = SFG_KEY_VEC3;
+    P.toff.assign(P.nkeys + 1, 0);
+    for (int k = 0; k < P.nkeys; ++k) P.toff[k + 1] = P.toff[k] + P.tdim[k];
+    P.soff = P.toff;
+    P.N = P.S = n;
+    P.num_schur = npts;
+    auto key_of = [&](int i) { return i < nb ? i : nb + (i - nb) / 3; };
+    std::vector<std::pair<int, int>> pairs;
+    for (int c = 0; c < n; ++c)
+      for (int32_t q = col_ptr[c]; q < col_ptr[c + 1]; ++q) pairs.push_back({key_of(row_idx[q]), key_of(c)});
+    s->L.H = sfg::MakePattern(P.tdim, pairs);
+    s->L.nvals = s->L.H.nvals();
+    s->L.N = n;
+    s->csc_to_val.resize(col_ptr[n]);
+    for (int c = 0; c < n; ++c)
+      for (int32_t q = col_ptr[c]; q < col_ptr[c + 1]; ++q) {
+        const int r = row_idx[q];
+        const int kr = key_of(r), kc = key_of(c);
+        const int64_t blk = s->L.H.Find(kr, kc);
+        s->csc_to_val[q] = s->L.H.boff[blk] + int64_t(r - P.toff[kr]) * P.tdim[kc] + (c - P.toff[kc]);
+      }
+    s->SL = sfg::BuildSchurLayout(P, s->L);
+    SFG_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    Arena& A = s->A;
+    s->st = MakeState(A);
+    const auto& S = s->SL;
+    sfg::SchurDev& d = s->sd;
+    d.npoints = S.npoints;
+    d.nB = int(S.nB);
+    d.c_toff = S.c_toff;
+    d.pt_diag = A.Upload(S.pt_diag);
+    d.pt_eptr = A.Upload(S.pt_eptr);
+    d.pt_ekey_toff = A.Upload(S.pt_ekey_toff);
+    d.pt_ekey_dim = A.Upload(S.pt_ekey_dim);
+    d.pt_eoff = A.Upload(S.pt_eoff);
+    d.pt_woff = A.Upload(S.pt_woff);
+    d.nsblocks = int(S.Spat.nblocks());
+    d.sb_ptr = A.Upload(S.sb_ptr);
+    d.sb_eoff = A.Upload(S.sb_eoff);
+    d.sb_woff = A.Upload(S.sb_woff);
+    d.sb_hoff = A.Upload(S.sb_hoff);
+    d.sb_soff = A.Upload(S.sb_soff);
+    d.sb_dk = A.Upload(S.sb_dk);
+    d.sb_dl = A.Upload(S.sb_dl);
+    d.sb_diag_toff = A.Upload(S.sb_diag_toff);
+    d.r_ptr = A.Upload(S.r_ptr);
+    d.r_eoff = A.Upload(S.r_eoff);
+    d.r_ecol = A.Upload(S.r_ecol);
+    d.r_dk = A.Upload(S.r_dk);
+    d.r_pt = A.Upload(S.r_pt);
+    s->hess = A.Zeros<double>(size_t(s->L.nvals));
+    s->rhs = A.Zeros<double>(size_t(n));
+    s->damping = A.Zeros<double>(size_t(n));
+    s->cinv = A.Zeros<double>(9 * size_t(npts));
+    s->W = A.Zeros<double>(size_t(S.nW));
+    s->tp = A.Zeros<double>(3 * size_t(npts));
+    s->S = A.Zeros<double>(size_t(S.Spat.nvals()));
+    s->v = A.Zeros<double>(size_t(S.nB));
+    s->y = A.Zeros<double>(size_t(S.nB));
+    s->update = A.Zeros<double>(size_t(n));
+    int sms = 0;
+    SFG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    MakePlan(A, s->plan, S.Spat, SFG_ORDERING_NESTED_DISSECTION, &s->st->device_error, s->st, sms);
+  });
+  if (rc == SFG_OK) *out = s.release();
+  return rc;
+}
+
+int32_t sfg_schur_factorize(sfg_schur* s, const double* values) {
+  return Guard([&] {
+    if (!s || !values) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    SFG_CUDA(cudaSetDevice(s->device));
+    std::vector<double> v(s->L.nvals, 0.0);
+    for (size_t q = 0; q < s->csc_to_val.size(); ++q) v[s->csc_to_val[q]] += values[q];
+    SFG_CUDA(cudaMemcpy(s->hess, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice));
+    cudaStream_t st = s->stream;
+    // C^-1 and W only depend on the matrix; the rhs-dependent t_p is recomputed in solve
+    sfg::LaunchSchurPoints<double>(s->sd, s->hess, s->rhs, s->L.nvals, s->n, s->damping, s->cinv, s->W,
+                                   s->tp, s->st, st);
+    sfg::LaunchSchurBuildS<double>(s->sd, s->hess, s->L.nvals, s->damping, s->W, s->S, s->st, st);
+    const Plan& p = s->plan;
+    sfg::LaunchResetFactorState(p.f.tile_state, p.tp.nstates, p.f.front_flags, p.nflags, p.f.counters, st);
+    sfg::LaunchFactor<double>(p.f, s->S, nullptr, p.F, p.grid_factor, st);
+    SFG_CUDA(cudaStreamSynchronize(st));
+    SFG_CUDA(cudaGetLastError());
+    CheckError(s->st);
+    s->factored = true;
+  });
+}
+
+int32_t sfg_schur_solve(sfg_schur* s, const double* b, double* x, int32_t nrhs) {
+  return Guard([&] {
+    if (!s || !b || !x || nrhs < 1) throw Error(SFG_ERR_INVALID_ARGUMENT, "bad argument");
+    if (!s->factored) throw Error(SFG_ERR_INVALID_ARGUMENT, "factorize first");
+    SFG_CUDA(cudaSetDevice(s->device));
+    cudaStream_t st = s->stream;
+    const Plan& p = s->plan;
+    std::vector<double> u(s->n);
+    for (int r = 0; r < nrhs; ++r) {
+      SFG_CUDA(cudaMemcpyAsync(s->rhs, b + size_t(r) * s->n, sizeof(double) * s->n, cudaMemcpyHostToDevice, st));
+      sfg::LaunchSchurPoints<double>(s->sd, s->hess, s->rhs, s->L.nvals, s->n, s->damping, s->cinv, s->W,
+                                     s->tp, s->st, st);
+      sfg::LaunchSchurRhs<double>(s->sd, s->hess, s->L.nvals, s->rhs, s->n, s->tp, s->v, s->st, st);
+      sfg::LaunchResetFactorState(p.f.tile_state, 0, p.f.front_flags, p.nflags, p.f.counters, st);
+      sfg::LaunchSolve<double>(p.f, p.F, s->v, p.ycon, p.ysave, p.xperm, s->y, p.grid_solve, st);
+      sfg::LaunchSchurBackSub<double>(s->sd, s->y, s->W, s->tp, s->update, st);
+      SFG_CUDA(cudaMemcpyAsync(u.data(), s->update, sizeof(double) * s->n, cudaMemcpyDeviceToHost, st));
+      SFG_CUDA(cudaStreamSynchronize(st));
+      CheckError(s->st);
+      for (int i = 0; i < s->n; ++i) x[size_t(r) * s->n + i] = -u[i];
+    }
+  });
+}
+
+int32_t sfg_schur_destroy(sfg_schur* s) {
+  if (s) {
+    cudaSetDevice(s->device);
+    delete s;
+  }
+  return SFG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,170 @@
+// Host-callable launchers of the device kernels (one definition per .cu file).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/sfgpu.h"
+#include "device.cuh"
+
+namespace sfg {
+
+// ---------------------------------------------------------------- linearization (kernels_lin.cu)
+// Evaluate every factor of a batch at the Init or New values, writing residual rows, packed
+// Gauss-Newton Hessian / rhs entries (directly, or into staging when shared), and per-CTA cost
+// partial sums.  T = double (plain form) or float (mixed form).
+template <typename T>
+void LaunchLinearize(int kind, const LinOut& out, const BatchDev& b, cudaStream_t s);
+int LinearizeBlockSize();
+
+// Sum staged contributions into shared Hessian / rhs destinations in a fixed order.
+struct ReduceDev {
+  int ngroups;
+  const int32_t* dst;   // sink index (< nvals + N) of each group
+  const int64_t* ptr;   // [ngroups + 1] range of the group's staging slots
+};
+template <typename T>
+void LaunchReduceStage(const ReduceDev& r, const LinOut& out, cudaStream_t s);
+
+// Cost of a state block: 0.5 * sum of the cost partials (fixed order, deterministic).
+void LaunchFinishCost(const double* partials, int npartials, LmState* st, int which,
+                      cudaStream_t s);
+
+// ---------------------------------------------------------------- LM bookkeeping (kernels_lm.cu)
+struct DampDev {
+  int64_t N;
+  const int64_t* diag_off;  // value offset of each tangent scalar's diagonal entry in H
+  double* damping;          // [N]
+  double* max_diagonal;     // [N]
+};
+template <typename T>
+void LaunchDamping(const DampDev& d, const void* hess, int64_t nvals, const LmParams* p,
+                   LmState* st, cudaStream_t s);
+
+struct RetractDev {
+  int nkeys;
+  const int32_t* key_type;
+  const int64_t* soff;
+  const int64_t* toff;
+  double* values;   // [3][S]
+  int64_t S;
+  const double* update;  // [N]
+};
+void LaunchRetract(const RetractDev& r, const LmParams* p, LmState* st, cudaStream_t s);
+
+// Per-CTA partial sums of u.(rhs - d.u) (rhs of the Init block) and, for bold updates, of u.last,
+// u.u and last.last; the decide kernel adds the partials in a fixed order.
+template <typename T>
+void LaunchLinearDelta(const double* update, const void* rhs, const double* damping,
+                       const double* last_update, int64_t N, double* partials, LmState* st,
+                       int bold, cudaStream_t s);
+int DeltaPartials();
+
+// The end of LevenbergMarquardtSolver::Iterate: stats record, accept / reject, lambda update,
+// best tracking, state-index juggling, early exit; sets the graph's loop condition.
+void LaunchDecide(const LmParams* p, LmState* st, sfg_iteration_t* records, const double* update,
+                  double* last_update, int64_t N, const double* delta_partials, int nparts,
+                  cudaGraphConditionalHandle h, cudaStream_t s);
+// Start of an optimize call: Reset + the first half of the first Iterate (Step).
+void LaunchBegin(const LmParams* p, LmState* st, int reset_indices, cudaStream_t s);
+// After the Init block has been linearized for the first time: initial record and the
+// non-finite check (INITIAL_ERROR_NOT_FINITE).
+void LaunchFirstRecord(const LmParams* p, LmState* st, sfg_iteration_t* records,
+                       cudaGraphConditionalHandle h, cudaStream_t s);
+void LaunchCopyValues(const double* src, double* values, int64_t S, const LmState* st, int which,
+                      cudaStream_t s);
+void LaunchCopyBest(const double* values, double* dst, int64_t S, const LmState* st, cudaStream_t s);
+
+// ---------------------------------------------------------------- Schur + LDL^T (kernels_solve.cu)
+struct SchurDev {
+  int npoints;
+  int nB;                       // scalar dimension of the reduced system
+  int64_t c_toff;               // tangent offset of the first point
+  const int64_t* pt_diag;       // H value offset of each point's 3x3 block
+  const int64_t* pt_eptr;       // [np + 1] E blocks of each point
+  const int32_t* pt_ekey_toff;  // tangent offset of the B key of each E block
+  const int32_t* pt_ekey_dim;   // dim of that key
+  const int64_t* pt_eoff;       // H value offset of E block (3 x d_k, row-major)
+  const int64_t* pt_woff;       // W value offset (3 x d_k)
+  int nsblocks;
+  const int64_t* sb_ptr;        // [nsblocks + 1] terms of each S block
+  const int64_t* sb_eoff;       // E_pk offset per term
+  const int64_t* sb_woff;       // W_pl offset per term
+  const int64_t* sb_hoff;       // H value offset of the B block (-1: none)
+  const int64_t* sb_soff;       // S value offset of the block
+  const int32_t* sb_dk;         // rows of the block
+  const int32_t* sb_dl;         // cols
+  const int32_t* sb_diag_toff;  // tangent offset of the key if diagonal block, else -1
+  const int64_t* r_ptr;         // [nB + 1] points of each B scalar
+  const int64_t* r_eoff;        // E block offset per entry (column of the scalar inside E)
+  const int32_t* r_ecol;        // column inside the E block
+  const int32_t* r_dk;          // E block column count
+  const int32_t* r_pt;          // point index
+};
+template <typename T>
+void LaunchSchurPoints(const SchurDev& d, const void* hess, const void* rhs, int64_t nvals,
+                       int64_t N, const double* damping, void* cinv, void* W, void* tp,
+                       const LmState* st, cudaStream_t s);
+template <typename T>
+void LaunchSchurBuildS(const SchurDev& d, const void* hess, int64_t nvals, const double* damping,
+                       const void* W, void* S, const LmState* st, cudaStream_t s);
+template <typename T>
+void LaunchSchurRhs(const SchurDev& d, const void* hess, int64_t nvals, const void* rhs, int64_t N,
+                    const void* tp, void* v, const LmState* st, cudaStream_t s);
+template <typename T>
+void LaunchSchurBackSub(const SchurDev& d, const void* y, const void* W, const void* tp,
+                        double* update, cudaStream_t s);
+
+struct AsmDev {
+  int64_t src;          // block value offset
+  int64_t dscal;        // original scalar offset of the block row (diagonal blocks: damping)
+  int32_t row0, col0;
+  int16_t di, dj, transpose, diag;
+};
+
+struct FactorDev {
+  int ns, ntasks, tile;
+  const int4* tasks;
+  const int32_t* sn_w;
+  const int32_t* sn_m;
+  const int64_t* sn_foff;
+  const int32_t* tile_base;
+  const int32_t* npiv;
+  const int32_t* ntiles;
+  const int64_t* asm_off;
+  const AsmDev* asms;
+  const int64_t* rel_off;
+  const int32_t* rel;
+  const int32_t* child_ptr;
+  const int32_t* child_list;
+  const int32_t* parent;
+  const int64_t* idx_off;
+  const int32_t* idx;         // new scalar indices of each front
+  const int32_t* scalar_old;  // new scalar -> old scalar
+  int* tile_state;
+  int* counters;              // [0]: factor task counter, [1]: solve task counter
+  int* front_flags;           // [2 * ns]: forward done, backward done
+  int* error;                 // device error word
+  int max_m;                  // largest front (solve kernel shared memory)
+  const LmState* st;          // state whose Init block the matrix / rhs are read from
+  int64_t a_stride;           // per-state-block stride of the matrix values (0: fixed)
+  int64_t b_stride;           // per-state-block stride of the rhs (0: fixed)
+};
+template <typename T>
+void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F,
+                  int grid, cudaStream_t s);
+// Solve (L D L^T) x = b for b in the original scalar order; x in the original order.
+template <typename T>
+void LaunchSolve(const FactorDev& f, const void* F, const void* b, void* ycon, void* ysave,
+                 void* xperm, void* x, int grid, cudaStream_t s);
+int FactorThreads();
+void LaunchResetFactorState(int* tile_state, int nstates, int* front_flags, int nflags,
+                            int* counters, cudaStream_t s);
+template <typename T>
+void LaunchNegate(const void* x, double* u, int64_t n, cudaStream_t s);
+// Opt the solve kernel into the shared memory its largest front needs (call once per device).
+template <typename T>
+void ConfigureSolve(int max_m);
+
+}  // namespace sfg

@@ -1,0 +1,648 @@
+// Linear solve of the damped Gauss-Newton system on the device.
+//
+//  - Schur complement over the trailing 3x3 point blocks (the SparseSchurSolver math,
+//    symforce/opt/sparse_schur_solver.tcc:99-162): per point C^-1 (LL^T), W = C^-1 E, the
+//    reduced system S = B - E^T W accumulated per S block in a fixed order, the reduced rhs, and
+//    the point back-substitution.
+//  - Multifrontal LDL^T (unit L, diagonal D, no pivoting: the factorization the reference computes
+//    with its up-looking SparseCholeskySolver, symforce/opt/sparse_cholesky/
+//    sparse_cholesky_solver.tcc:108-219) over a host-computed supernodal structure.  One
+//    persistent kernel executes a topologically ordered list of tile tasks (front assembly,
+//    diagonal-tile LDL^T, panel triangular solve, trailing update); dependencies are tile version
+//    counters in global memory.  A CTA only waits on tasks that precede its own in the list, all
+//    of which are held by running CTAs, so progress is guaranteed; every wait is capped and a cap
+//    hit sets the error word and drains the kernel.
+//  - The triangular solves, one task per front, forward in postorder and backward in reverse.
+#include "factor_math.cuh"
+#include <algorithm>
+
+#include "kernels.h"
+
+namespace sfg {
+
+namespace {
+
+constexpr int kFactorThreads = 128;
+constexpr unsigned kSpinLimit = 1u << 22;
+constexpr int kFinal = 1 << 30;
+
+__device__ __forceinline__ int LoadVolatile(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
+// Thread 0 only.  Returns false if the wait gave up (error set by us or by another CTA).
+__device__ bool WaitAtLeast(const int* addr, int v, int* err) {
+  unsigned it = 0;
+  while (LoadVolatile(addr) < v) {
+    if (LoadVolatile(err) != 0) return false;
+    if (++it > kSpinLimit) {
+      atomicExch(err, kDevSpinTimeout);
+      return false;
+    }
+    __nanosleep(100);
+  }
+  __threadfence();
+  return true;
+}
+
+template <typename T>
+__device__ __forceinline__ T Ld(const T* p) { return __ldcg(p); }
+template <typename T>
+__device__ __forceinline__ void St(T* p, T v) { __stcg(p, v); }
+
+// ---------------------------------------------------------------------------------------------
+// Schur complement kernels
+// ---------------------------------------------------------------------------------------------
+template <typename T>
+__global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_all, int64_t nvals,
+                                  int64_t N, const double* damping, T* cinv, T* W, T* tp,
+                                  const LmState* st) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.npoints) return;
+  const T* H = hess_all + int64_t(st->init_idx) * nvals;
+  const T* g = rhs_all + int64_t(st->init_idx) * N;
+  const T* C = H + d.pt_diag[p];
+  const int64_t toff = d.c_toff + 3 * int64_t(p);
+  const T a00 = C[0] + T(damping[toff]);
+  const T a10 = C[3];
+  const T a11 = C[4] + T(damping[toff + 1]);
+  const T a20 = C[6];
+  const T a21 = C[7];
+  const T a22 = C[8] + T(damping[toff + 2]);
+  const T l00 = sqrt(a00);
+  const T l10 = a10 / l00, l20 = a20 / l00;
+  const T l11 = sqrt(a11 - l10 * l10);
+  const T l21 = (a21 - l20 * l10) / l11;
+  const T l22 = sqrt(a22 - l20 * l20 - l21 * l21);
+  const T i00 = T(1) / l00, i11 = T(1) / l11, i22 = T(1) / l22;
+  const T i10 = -l10 * i00 * i11;
+  const T i21 = -l21 * i11 * i22;
+  const T i20 = -(l20 * i00 + l21 * i10) * i22;
+  const T c00 = i00 * i00 + i10 * i10 + i20 * i20;
+  const T c10 = i11 * i10 + i21 * i20;
+  const T c20 = i22 * i20;
+  const T c11 = i11 * i11 + i21 * i21;
+  const T c21 = i22 * i21;
+  const T c22 = i22 * i22;
+  T* ci = cinv + 9 * int64_t(p);
+  ci[0] = c00; ci[1] = c10; ci[2] = c20;
+  ci[3] = c10; ci[4] = c11; ci[5] = c21;
+  ci[6] = c20; ci[7] = c21; ci[8] = c22;
+  const T g0 = g[toff], g1 = g[toff + 1], g2 = g[toff + 2];
+  T* t = tp + 3 * int64_t(p);
+  t[0] = c00 * g0 + c10 * g1 + c20 * g2;
+  t[1] = c10 * g0 + c11 * g1 + c21 * g2;
+  t[2] = c20 * g0 + c21 * g1 + c22 * g2;
+  for (int64_t e = d.pt_eptr[p]; e < d.pt_eptr[p + 1]; ++e) {
+    const int dk = d.pt_ekey_dim[e];
+    const T* E = H + d.pt_eoff[e];
+    T* Wp = W + d.pt_woff[e];
+    for (int c = 0; c < dk; ++c) {
+      const T e0 = E[c], e1 = E[dk + c], e2 = E[2 * dk + c];
+      Wp[c] = c00 * e0 + c10 * e1 + c20 * e2;
+      Wp[dk + c] = c10 * e0 + c11 * e1 + c21 * e2;
+      Wp[2 * dk + c] = c20 * e0 + c21 * e1 + c22 * e2;
+    }
+  }
+}
+
+// One CTA per S block, one thread per block entry, terms summed in a fixed order.
+template <typename T>
+__global__ void SchurBuildSKernel(SchurDev d, const T* hess_all, int64_t nvals,
+                                  const double* damping, const T* W, T* S, const LmState* st) {
+  const int sb = blockIdx.x;
+  const T* H = hess_all + int64_t(st->init_idx) * nvals;
+  const int dk = d.sb_dk[sb], dl = d.sb_dl[sb];
+  const int64_t hoff = d.sb_hoff[sb];
+  const int diag_toff = d.sb_diag_toff[sb];
+  const int64_t t0 = d.sb_ptr[sb], t1 = d.sb_ptr[sb + 1];
+  for (int ent = threadIdx.x; ent < dk * dl; ent += blockDim.x) {
+    const int r = ent / dl, c = ent - r * dl;
+    T acc = hoff >= 0 ? H[hoff + ent] : T(0);
+    if (diag_toff >= 0 && r == c) acc += T(damping[diag_toff + r]);
+    for (int64_t t = t0; t < t1; ++t) {
+      const T* E = H + d.sb_eoff[t];
+      const T* Wl = W + d.sb_woff[t];
+      acc -= E[r] * Wl[c] + E[dk + r] * Wl[dl + c] + E[2 * dk + r] * Wl[2 * dl + c];
+    }
+    S[d.sb_soff[sb] + ent] = acc;
+  }
+}
+
+// One warp per reduced-system scalar: v_i = g_i - sum_p (E_p^T t_p)_i, fixed shuffle tree.
+template <typename T>
+__global__ void SchurRhsKernel(SchurDev d, const T* hess_all, int64_t nvals, const T* rhs_all,
+                               int64_t N, const T* tp, T* v, const LmState* st) {
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= d.nB) return;
+  const T* H = hess_all + int64_t(st->init_idx) * nvals;
+  const T* g = rhs_all + int64_t(st->init_idx) * N;
+  T acc = T(0);
+  for (int64_t q = d.r_ptr[i] + lane; q < d.r_ptr[i + 1]; q += 32) {
+    const int dk = d.r_dk[q];
+    const T* E = H + d.r_eoff[q] + d.r_ecol[q];
+    const T* t = tp + 3 * int64_t(d.r_pt[q]);
+    acc += E[0] * t[0] + E[dk] * t[1] + E[2 * dk] * t[2];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) v[i] = g[i] - acc;
+}
+
+// Point back-substitution z_p = t_p - sum_k W_pk y_k, and update = -[y; z].
+template <typename T>
+__global__ void SchurBackSubKernel(SchurDev d, const T* y, const T* W, const T* tp,
+                                   double* update) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < d.npoints) {
+    const int p = t;
+    T z0 = tp[3 * int64_t(p)], z1 = tp[3 * int64_t(p) + 1], z2 = tp[3 * int64_t(p) + 2];
+    for (int64_t e = d.pt_eptr[p]; e < d.pt_eptr[p + 1]; ++e) {
+      const int dk = d.pt_ekey_dim[e];
+      const T* Wp = W + d.pt_woff[e];
+      const T* yk = y + d.pt_ekey_toff[e];
+      T s0 = T(0), s1 = T(0), s2 = T(0);
+      for (int c = 0; c < dk; ++c) {
+        const T yc = yk[c];
+        s0 += Wp[c] * yc;
+        s1 += Wp[dk + c] * yc;
+        s2 += Wp[2 * dk + c] * yc;
+      }
+      z0 -= s0;
+      z1 -= s1;
+      z2 -= s2;
+    }
+    double* u = update + d.c_toff + 3 * int64_t(p);
+    u[0] = -double(z0);
+    u[1] = -double(z1);
+    u[2] = -double(z2);
+  } else if (t < d.npoints + d.nB) {
+    const int i = t - d.npoints;
+    update[i] = -double(y[i]);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Multifrontal LDL^T: persistent tile-task kernel
+// ---------------------------------------------------------------------------------------------
+struct Geom {
+  int w, m, np, nt, base;
+  int64_t foff;
+};
+
+__device__ __forceinline__ Geom FrontGeom(const FactorDev& f, int s) {
+  Geom g;
+  g.w = f.sn_w[s];
+  g.m = f.sn_m[s];
+  g.np = f.npiv[s];
+  g.nt = f.ntiles[s];
+  g.base = f.tile_base[s];
+  g.foff = f.sn_foff[s];
+  return g;
+}
+__device__ __forceinline__ int TileStart(const Geom& g, int t, int tile) {
+  return t < g.np ? t * tile : g.w + (t - g.np) * tile;
+}
+__device__ __forceinline__ int TileSize(const Geom& g, int t, int tile) {
+  return t < g.np ? min(tile, g.w - t * tile) : min(tile, g.m - TileStart(g, t, tile));
+}
+__device__ __forceinline__ int StateIdx(const Geom& g, int i, int j) { return g.base + i * (i + 1) / 2 + j; }
+
+template <typename T, int TILE>
+struct TileSmem {
+  T a[TILE * TILE];
+  T b[TILE * TILE];
+  T d[TILE];
+};
+
+// Broadcast of thread 0's wait result.
+__device__ __forceinline__ bool CtaWait(bool ok_thread0, int* s_flag) {
+  if (threadIdx.x == 0) *s_flag = ok_thread0 ? 1 : 0;
+  __syncthreads();
+  const bool ok = *s_flag != 0;
+  __syncthreads();
+  return ok;
+}
+
+__device__ __forceinline__ void Signal(int* addr, int v) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) atomicExch(addr, v);
+}
+
+template <typename T, int TILE>
+__device__ void TaskAssemble(const FactorDev& f, int s, const T* A, const double* damping, T* F,
+                             int* s_flag) {
+  const Geom g = FrontGeom(f, s);
+  bool ok = true;
+  if (threadIdx.x == 0) {
+    for (int q = f.child_ptr[s]; q < f.child_ptr[s + 1] && ok; ++q) {
+      const int c = f.child_list[q];
+      const Geom gc = FrontGeom(f, c);
+      for (int i = gc.np; i < gc.nt && ok; ++i)
+        for (int j = gc.np; j <= i && ok; ++j)
+          ok = WaitAtLeast(f.tile_state + StateIdx(gc, i, j), 1 + gc.np, f.error);
+    }
+  }
+  if (!CtaWait(ok, s_flag)) return;
+  T* Fs = F + g.foff;
+  const int m = g.m;
+  for (int64_t e = threadIdx.x; e < int64_t(m) * m; e += blockDim.x) {
+    const int r = int(e % m), c = int(e / m);
+    if (r >= c) St(Fs + e, T(0));
+  }
+  __syncthreads();
+  for (int64_t a = f.asm_off[s]; a < f.asm_off[s + 1]; ++a) {
+    const AsmDev as = f.asms[a];
+    const int nent = int(as.di) * int(as.dj);
+    for (int e = threadIdx.x; e < nent; e += blockDim.x) {
+      const int r = e / as.dj, c = e - r * as.dj;
+      if (as.diag && r < c) continue;
+      T v = A[as.src + e];
+      if (as.diag && r == c && damping) v += T(damping[as.dscal + r]);
+      int64_t pos;
+      if (as.transpose) {
+        pos = int64_t(as.row0 + c) + int64_t(as.col0 + r) * m;
+      } else {
+        pos = int64_t(as.row0 + r) + int64_t(as.col0 + c) * m;
+      }
+      St(Fs + pos, v);
+    }
+  }
+  __syncthreads();
+  for (int q = f.child_ptr[s]; q < f.child_ptr[s + 1]; ++q) {
+    const int c = f.child_list[q];
+    const Geom gc = FrontGeom(f, c);
+    const int hc = gc.m - gc.w;
+    const int32_t* rel = f.rel + f.rel_off[c];
+    const T* Fc = F + gc.foff;
+    for (int64_t e = threadIdx.x; e < int64_t(hc) * hc; e += blockDim.x) {
+      const int r = int(e % hc), cc = int(e / hc);
+      if (r < cc) continue;
+      const T u = Ld(Fc + int64_t(gc.w + r) + int64_t(gc.w + cc) * gc.m);
+      T* dst = Fs + int64_t(rel[r]) + int64_t(rel[cc]) * m;
+      St(dst, Ld(dst) + u);
+    }
+    __syncthreads();
+  }
+  __threadfence();
+  __syncthreads();
+  const int ntile_states = g.nt * (g.nt + 1) / 2;
+  for (int q = threadIdx.x; q < ntile_states; q += blockDim.x) atomicExch(f.tile_state + g.base + q, 1);
+}
+
+template <typename T, int TILE>
+__device__ void TaskDiag(const FactorDev& f, int s, int k, T* F, TileSmem<T, TILE>& sm,
+                         int* s_flag) {
+  const Geom g = FrontGeom(f, s);
+  bool ok = true;
+  if (threadIdx.x == 0) ok = WaitAtLeast(f.tile_state + StateIdx(g, k, k), 1 + k, f.error);
+  if (!CtaWait(ok, s_flag)) return;
+  const int b = TileSize(g, k, TILE), r0 = TileStart(g, k, TILE);
+  T* Fs = F + g.foff;
+  for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+    const int r = e % b, c = e / b;
+    if (r >= c) sm.a[r * TILE + c] = Ld(Fs + int64_t(r0 + r) + int64_t(r0 + c) * g.m);
+  }
+  __syncthreads();
+  for (int j = 0; j < b; ++j) {
+    const T dj = sm.a[j * TILE + j];
+    const int rem = b - j - 1;
+    for (int e = threadIdx.x; e < rem * rem; e += blockDim.x) {
+      const int r = j + 1 + e % rem, c = j + 1 + e / rem;
+      if (r >= c) sm.a[r * TILE + c] -= sm.a[r * TILE + j] * sm.a[c * TILE + j] / dj;
+    }
+    __syncthreads();
+    for (int r = j + 1 + threadIdx.x; r < b; r += blockDim.x) sm.a[r * TILE + j] /= dj;
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
+    const int r = e % b, c = e / b;
+    if (r >= c) St(Fs + int64_t(r0 + r) + int64_t(r0 + c) * g.m, sm.a[r * TILE + c]);
+  }
+  Signal(f.tile_state + StateIdx(g, k, k), kFinal);
+}
+
+template <typename T, int TILE>
+__device__ void TaskTrsm(const FactorDev& f, int s, int i, int k, T* F, TileSmem<T, TILE>& sm,
+                         int* s_flag) {
+  const Geom g = FrontGeom(f, s);
+  bool ok = true;
+  if (threadIdx.x == 0) {
+    ok = WaitAtLeast(f.tile_state + StateIdx(g, k, k), kFinal, f.error) &&
+         WaitAtLeast(f.tile_state + StateIdx(g, i, k), 1 + k, f.error);
+  }
+  if (!CtaWait(ok, s_flag)) return;
+  const int bk = TileSize(g, k, TILE), ck = TileStart(g, k, TILE);
+  const int bi = TileSize(g, i, TILE), ri = TileStart(g, i, TILE);
+  T* Fs = F + g.foff;
+  for (int e = threadIdx.x; e < bk * bk; e += blockDim.x) {
+    const int r = e % bk, c = e / bk;
+    if (r >= c) sm.a[r * TILE + c] = Ld(Fs + int64_t(ck + r) + int64_t(ck + c) * g.m);
+  }
+  for (int e = threadIdx.x; e < bi * bk; e += blockDim.x) {
+    const int r = e % bi, c = e / bi;
+    sm.b[r * TILE + c] = Ld(Fs + int64_t(ri + r) + int64_t(ck + c) * g.m);
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < bi; r += blockDim.x) {
+    T* row = sm.b + r * TILE;
+    for (int c = 0; c < bk; ++c) {
+      T x = row[c];
+      for (int q = 0; q < c; ++q) x -= row[q] * sm.a[c * TILE + q];
+      row[c] = x;  // W = L_ik D
+    }
+    for (int c = 0; c < bk; ++c) row[c] /= sm.a[c * TILE + c];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < bi * bk; e += blockDim.x) {
+    const int r = e % bi, c = e / bi;
+    St(Fs + int64_t(ri + r) + int64_t(ck + c) * g.m, sm.b[r * TILE + c]);
+  }
+  Signal(f.tile_state + StateIdx(g, i, k), kFinal);
+}
+
+template <typename T, int TILE>
+__device__ void TaskUpdate(const FactorDev& f, int s, int i, int j, int k, T* F,
+                           TileSmem<T, TILE>& sm, int* s_flag) {
+  const Geom g = FrontGeom(f, s);
+  bool ok = true;
+  if (threadIdx.x == 0) {
+    ok = WaitAtLeast(f.tile_state + StateIdx(g, i, k), kFinal, f.error) &&
+         WaitAtLeast(f.tile_state + StateIdx(g, j, k), kFinal, f.error) &&
+         WaitAtLeast(f.tile_state + StateIdx(g, i, j), 1 + k, f.error);
+  }
+  if (!CtaWait(ok, s_flag)) return;
+  const int bk = TileSize(g, k, TILE), ck = TileStart(g, k, TILE);
+  const int bi = TileSize(g, i, TILE), ri = TileStart(g, i, TILE);
+  const int bj = TileSize(g, j, TILE), rj = TileStart(g, j, TILE);
+  T* Fs = F + g.foff;
+  for (int e = threadIdx.x; e < bi * bk; e += blockDim.x) {
+    const int r = e % bi, c = e / bi;
+    sm.a[r * TILE + c] = Ld(Fs + int64_t(ri + r) + int64_t(ck + c) * g.m);
+  }
+  for (int e = threadIdx.x; e < bj * bk; e += blockDim.x) {
+    const int r = e % bj, c = e / bj;
+    sm.b[r * TILE + c] = Ld(Fs + int64_t(rj + r) + int64_t(ck + c) * g.m);
+  }
+  for (int c = threadIdx.x; c < bk; c += blockDim.x) sm.d[c] = Ld(Fs + int64_t(ck + c) * (g.m + 1));
+  __syncthreads();
+  for (int c = threadIdx.x; c < bk; c += blockDim.x) {
+    // scale L_jk by D once: b <- L_jk D
+    for (int r = 0; r < bj; ++r) sm.b[r * TILE + c] *= sm.d[c];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < bi * bj; e += blockDim.x) {
+    const int r = e % bi, c = e / bi;
+    if (i == j && r < c) continue;
+    T acc = T(0);
+    for (int q = 0; q < bk; ++q) acc += sm.a[r * TILE + q] * sm.b[c * TILE + q];
+    T* dst = Fs + int64_t(ri + r) + int64_t(rj + c) * g.m;
+    St(dst, Ld(dst) - acc);
+  }
+  Signal(f.tile_state + StateIdx(g, i, j), 2 + k);
+}
+
+template <typename T, int TILE>
+__global__ void __launch_bounds__(kFactorThreads) FactorKernel(FactorDev f, const T* A,
+                                                               const double* damping, T* F) {
+  __shared__ TileSmem<T, TILE> sm;
+  A += int64_t(f.st->init_idx) * f.a_stride;
+  __shared__ int s_task, s_ok, s_flag;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_ok = LoadVolatile(f.error) == 0;
+      s_task = s_ok ? atomicAdd(f.counters, 1) : f.ntasks;
+    }
+    __syncthreads();
+    const int t = s_task;
+    if (t >= f.ntasks) return;
+    const int4 task = f.tasks[t];
+    const int i = task.z >> 16, j = task.z & 0xffff, k = task.w;
+    switch (task.x) {
+      case kTaskAssemble: TaskAssemble<T, TILE>(f, task.y, A, damping, F, &s_flag); break;
+      case kTaskDiag: TaskDiag<T, TILE>(f, task.y, k, F, sm, &s_flag); break;
+      case kTaskTrsm: TaskTrsm<T, TILE>(f, task.y, i, k, F, sm, &s_flag); break;
+      case kTaskUpdate: TaskUpdate<T, TILE>(f, task.y, i, j, k, F, sm, &s_flag); break;
+      default:
+        if (threadIdx.x == 0) atomicExch(f.error, kDevBadTask);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Triangular solves: task t < ns is the forward solve of front t (postorder), task ns + q the
+// backward solve of front ns - 1 - q (reverse postorder).  Dynamic shared memory: 2 * max_m.
+// ---------------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kFactorThreads) SolveKernel(FactorDev f, const T* F, const T* b,
+                                                              T* ycon, T* ysave, T* xperm, T* x) {
+  extern __shared__ unsigned char smem_raw[];
+  T* xs = reinterpret_cast<T*>(smem_raw);
+  __shared__ int s_task, s_ok, s_flag;
+  int* fwd_done = f.front_flags;
+  int* bwd_done = f.front_flags + f.ns;
+  b += int64_t(f.st->init_idx) * f.b_stride;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_ok = LoadVolatile(f.error) == 0;
+      s_task = s_ok ? atomicAdd(f.counters + 1, 1) : 2 * f.ns;
+    }
+    __syncthreads();
+    const int t = s_task;
+    if (t >= 2 * f.ns) return;
+    if (t < f.ns) {
+      const int s = t;
+      const Geom g = FrontGeom(f, s);
+      bool ok = true;
+      if (threadIdx.x == 0)
+        for (int q = f.child_ptr[s]; q < f.child_ptr[s + 1] && ok; ++q)
+          ok = WaitAtLeast(fwd_done + f.child_list[q], 1, f.error);
+      if (CtaWait(ok, &s_flag)) {
+        const int32_t* idx = f.idx + f.idx_off[s];
+        const T* Fs = F + g.foff;
+        for (int q = threadIdx.x; q < g.m; q += blockDim.x)
+          xs[q] = q < g.w ? b[f.scalar_old[idx[q]]] : T(0);
+        __syncthreads();
+        for (int q = f.child_ptr[s]; q < f.child_ptr[s + 1]; ++q) {
+          const int c = f.child_list[q];
+          const int hc = f.sn_m[c] - f.sn_w[c];
+          const int32_t* rel = f.rel + f.rel_off[c];
+          for (int r = threadIdx.x; r < hc; r += blockDim.x) xs[rel[r]] += Ld(ycon + f.rel_off[c] + r);
+          __syncthreads();
+        }
+        for (int c = 0; c < g.w; ++c) {
+          const T xc = xs[c];
+          for (int r = c + 1 + threadIdx.x; r < g.m; r += blockDim.x)
+            xs[r] -= Ld(Fs + int64_t(r) + int64_t(c) * g.m) * xc;
+          __syncthreads();
+        }
+        for (int q = threadIdx.x; q < g.w; q += blockDim.x) St(ysave + f.idx_off[s] + q, xs[q]);
+        for (int r = threadIdx.x; r < g.m - g.w; r += blockDim.x) St(ycon + f.rel_off[s] + r, xs[g.w + r]);
+        Signal(fwd_done + s, 1);
+      }
+    } else {
+      const int s = f.ns - 1 - (t - f.ns);
+      const Geom g = FrontGeom(f, s);
+      bool ok = true;
+      if (threadIdx.x == 0) {
+        const int p = f.parent[s];
+        ok = p >= 0 ? WaitAtLeast(bwd_done + p, 1, f.error) : WaitAtLeast(fwd_done + s, 1, f.error);
+      }
+      if (CtaWait(ok, &s_flag)) {
+        const int32_t* idx = f.idx + f.idx_off[s];
+        const T* Fs = F + g.foff;
+        const int h = g.m - g.w;
+        T* xa = xs + g.w;
+        for (int r = threadIdx.x; r < h; r += blockDim.x) xa[r] = Ld(xperm + idx[g.w + r]);
+        __syncthreads();
+        for (int q = threadIdx.x; q < g.w; q += blockDim.x) {
+          T z = Ld(ysave + f.idx_off[s] + q) / Ld(Fs + int64_t(q) * (g.m + 1));
+          for (int r = 0; r < h; ++r) z -= Ld(Fs + int64_t(g.w + r) + int64_t(q) * g.m) * xa[r];
+          xs[q] = z;
+        }
+        __syncthreads();
+        for (int c = g.w - 1; c >= 0; --c) {
+          const T xc = xs[c];
+          for (int r = threadIdx.x; r < c; r += blockDim.x) xs[r] -= Ld(Fs + int64_t(c) + int64_t(r) * g.m) * xc;
+          __syncthreads();
+        }
+        for (int q = threadIdx.x; q < g.w; q += blockDim.x) {
+          St(xperm + idx[q], xs[q]);
+          x[f.scalar_old[idx[q]]] = xs[q];
+        }
+        Signal(bwd_done + s, 1);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void ResetFactorStateKernel(int* tile_state, int nstates, int* front_flags, int nflags,
+                                       int* counters) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nstates; i += gridDim.x * blockDim.x)
+    tile_state[i] = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nflags; i += gridDim.x * blockDim.x)
+    front_flags[i] = 0;
+  if (blockIdx.x == 0 && threadIdx.x < 2) counters[threadIdx.x] = 0;
+}
+
+template <typename T>
+__global__ void NegateKernel(const T* x, double* u, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    u[i] = -double(x[i]);
+}
+
+}  // namespace
+
+void LaunchResetFactorState(int* tile_state, int nstates, int* front_flags, int nflags,
+                            int* counters, cudaStream_t s) {
+  const int threads = 256;
+  int grid = (std::max(nstates, nflags) + threads - 1) / threads;
+  grid = std::min(std::max(grid, 1), 1024);
+  ResetFactorStateKernel<<<grid, threads, 0, s>>>(tile_state, nstates, front_flags, nflags, counters);
+}
+
+template <typename T>
+void LaunchNegate(const void* x, double* u, int64_t n, cudaStream_t s) {
+  const int threads = 256;
+  int grid = int(std::min<int64_t>((n + threads - 1) / threads, 1024));
+  NegateKernel<T><<<std::max(grid, 1), threads, 0, s>>>(static_cast<const T*>(x), u, n);
+}
+template void LaunchNegate<double>(const void*, double*, int64_t, cudaStream_t);
+template void LaunchNegate<float>(const void*, double*, int64_t, cudaStream_t);
+
+int FactorThreads() { return kFactorThreads; }
+
+template <typename T>
+void ConfigureSolve(int max_m) {
+  const size_t smem = size_t(max_m) * sizeof(T);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(SolveKernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+}
+template void ConfigureSolve<double>(int);
+template void ConfigureSolve<float>(int);
+
+template <typename T>
+void LaunchSchurPoints(const SchurDev& d, const void* hess, const void* rhs, int64_t nvals,
+                       int64_t N, const double* damping, void* cinv, void* W, void* tp,
+                       const LmState* st, cudaStream_t s) {
+  if (d.npoints == 0) return;
+  const int threads = 128;
+  SchurPointsKernel<T><<<(d.npoints + threads - 1) / threads, threads, 0, s>>>(
+      d, static_cast<const T*>(hess), static_cast<const T*>(rhs), nvals, N, damping,
+      static_cast<T*>(cinv), static_cast<T*>(W), static_cast<T*>(tp), st);
+}
+
+template <typename T>
+void LaunchSchurBuildS(const SchurDev& d, const void* hess, int64_t nvals, const double* damping,
+                       const void* W, void* S, const LmState* st, cudaStream_t s) {
+  if (d.nsblocks == 0) return;
+  SchurBuildSKernel<T><<<d.nsblocks, 96, 0, s>>>(d, static_cast<const T*>(hess), nvals, damping,
+                                                 static_cast<const T*>(W), static_cast<T*>(S), st);
+}
+
+template <typename T>
+void LaunchSchurRhs(const SchurDev& d, const void* hess, int64_t nvals, const void* rhs, int64_t N,
+                    const void* tp, void* v, const LmState* st, cudaStream_t s) {
+  if (d.nB == 0) return;
+  const int warps = 4;
+  SchurRhsKernel<T><<<(d.nB + warps - 1) / warps, 32 * warps, 0, s>>>(
+      d, static_cast<const T*>(hess), nvals, static_cast<const T*>(rhs), N,
+      static_cast<const T*>(tp), static_cast<T*>(v), st);
+}
+
+template <typename T>
+void LaunchSchurBackSub(const SchurDev& d, const void* y, const void* W, const void* tp,
+                        double* update, cudaStream_t s) {
+  const int n = d.npoints + d.nB;
+  const int threads = 128;
+  SchurBackSubKernel<T><<<(n + threads - 1) / threads, threads, 0, s>>>(
+      d, static_cast<const T*>(y), static_cast<const T*>(W), static_cast<const T*>(tp), update);
+}
+
+template <typename T>
+void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F, int grid,
+                  cudaStream_t s) {
+  constexpr int kTile = sizeof(T) == 8 ? 16 : 32;
+  FactorKernel<T, kTile><<<grid, kFactorThreads, 0, s>>>(f, static_cast<const T*>(A), damping,
+                                                         static_cast<T*>(F));
+}
+
+template <typename T>
+void LaunchSolve(const FactorDev& f, const void* F, const void* b, void* ycon, void* ysave,
+                 void* xperm, void* x, int grid, cudaStream_t s) {
+  // dynamic shared memory: the largest front's scalars
+  const size_t smem = size_t(f.max_m) * sizeof(T);
+  SolveKernel<T><<<grid, kFactorThreads, smem, s>>>(
+      f, static_cast<const T*>(F), static_cast<const T*>(b), static_cast<T*>(ycon),
+      static_cast<T*>(ysave), static_cast<T*>(xperm), static_cast<T*>(x));
+}
+
+template void LaunchSchurPoints<double>(const SchurDev&, const void*, const void*, int64_t, int64_t,
+                                        const double*, void*, void*, void*, const LmState*, cudaStream_t);
+template void LaunchSchurPoints<float>(const SchurDev&, const void*, const void*, int64_t, int64_t,
+                                       const double*, void*, void*, void*, const LmState*, cudaStream_t);
+template void LaunchSchurBuildS<double>(const SchurDev&, const void*, int64_t, const double*,
+                                        const void*, void*, const LmState*, cudaStream_t);
+template void LaunchSchurBuildS<float>(const SchurDev&, const void*, int64_t, const double*,
+                                       const void*, void*, const LmState*, cudaStream_t);
+template void LaunchSchurRhs<double>(const SchurDev&, const void*, int64_t, const void*, int64_t,
+                                     const void*, void*, const LmState*, cudaStream_t);
+template void LaunchSchurRhs<float>(const SchurDev&, const void*, int64_t, const void*, int64_t,
+                                    const void*, void*, const LmState*, cudaStream_t);
+template void LaunchSchurBackSub<double>(const SchurDev&, const void*, const void*, const void*,
+                                         double*, cudaStream_t);
+template void LaunchSchurBackSub<float>(const SchurDev&, const void*, const void*, const void*,
+                                        double*, cudaStream_t);
+template void LaunchFactor<double>(const FactorDev&, const void*, const double*, void*, int,
+                                   cudaStream_t);
+template void LaunchFactor<float>(const FactorDev&, const void*, const double*, void*, int,
+                                  cudaStream_t);
+template void LaunchSolve<double>(const FactorDev&, const void*, const void*, void*, void*, void*,
+                                  void*, int, cudaStream_t);
+template void LaunchSolve<float>(const FactorDev&, const void*, const void*, void*, void*, void*,
+                                 void*, int, cudaStream_t);
+
+}  // namespace sfg

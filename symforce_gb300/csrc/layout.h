@@ -1,0 +1,46 @@
+// Host-computed layouts: where every factor's linearization lands in the block-sparse Hessian,
+// the Schur complement term lists, and the reference CSC export map.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "common.h"
+
+namespace sfg {
+
+struct LinLayout {
+  BlockPattern H;                  // key blocks of hessian_lower (tangent dims)
+  std::vector<int64_t> diag_off;   // [N] value offset of each diagonal scalar
+  struct BatchMap {
+    int nent = 0;                  // packed H entries + rhs entries per factor
+    std::vector<int32_t> dest;     // [nent][count] sink index
+  };
+  std::vector<BatchMap> maps;
+  int64_t nvals = 0, N = 0, nstage = 0;
+  // groups of staged contributions: destination and [ptr, ptr+1) range of staging slots
+  std::vector<int32_t> red_dst;
+  std::vector<int64_t> red_ptr;
+  // reference CSC lower layout (symforce/opt/linearizer.cc:324-353): values come from csc_src
+  std::vector<int32_t> csc_colptr, csc_rowidx;
+  std::vector<int64_t> csc_src;
+};
+
+LinLayout BuildLinLayout(const HostProblem& P);
+
+struct SchurLayout {
+  int nB_keys = 0, npoints = 0;
+  int64_t nB = 0, c_toff = 0;
+  std::vector<int64_t> pt_diag, pt_eptr, pt_eoff, pt_woff;
+  std::vector<int32_t> pt_ekey_toff, pt_ekey_dim;
+  int64_t nW = 0;
+  BlockPattern Spat;               // pattern of the reduced system over B keys
+  std::vector<int64_t> sb_ptr, sb_eoff, sb_woff, sb_hoff, sb_soff;
+  std::vector<int32_t> sb_dk, sb_dl, sb_diag_toff;
+  std::vector<int64_t> r_ptr, r_eoff;
+  std::vector<int32_t> r_ecol, r_dk, r_pt;
+};
+
+SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L);
+
+}  // namespace sfg

@@ -1,0 +1,227 @@
+"""Python mirror of the sym::Optimizer interface over the C ABI of libsfgpu.so.
+
+`Optimizer(params, problem, form)` corresponds to `sym::Optimizer<double>(params, factors, ...)`
+(symforce/opt/optimizer.h:86-111) and `optimize()` to `Optimizer::Optimize(values, num_iterations,
+populate_best_linearization, stats)` (symforce/opt/optimizer.tcc:79-89): it runs the whole
+Levenberg-Marquardt loop on the GPU and returns `OptimizationStats` with the same per-iteration
+records, best index, status and failure reason.  `LinearSolver`-concept objects `SparseLdlt` and
+`SparseSchur` mirror SparseCholeskySolver / SparseSchurSolver.
+
+There is no CPU fallback: constructing any of these without a CUDA device raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _build
+from . import _cabi as A
+
+_lib = None
+
+
+class SfgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"sfgpu error {code}: {msg}")
+        self.code = code
+
+
+def lib() -> C.CDLL:
+    """Load (building first if needed) the in-tree libsfgpu.so."""
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(str(path))
+        L.sfg_last_error.restype = C.c_char_p
+        L.sfg_create.argtypes = [C.POINTER(A.ProblemC), C.POINTER(A.FormParams), C.POINTER(C.c_void_p)]
+        L.sfg_destroy.argtypes = [C.c_void_p]
+        L.sfg_set_values.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int64]
+        L.sfg_get_values.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int64]
+        L.sfg_optimize.argtypes = [C.c_void_p, C.POINTER(A.OptimizerParams), C.c_int32, C.POINTER(A.StatsC)]
+        L.sfg_linearize.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double)]
+        L.sfg_hessian_lower.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                        C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        L.sfg_permutation.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_int64]
+        L.sfg_storage_dim.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_int64)]
+        L.sfg_ldlt_create.argtypes = [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
+                                      C.c_int32, C.POINTER(C.c_void_p)]
+        L.sfg_ldlt_factorize.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.sfg_ldlt_solve.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32]
+        L.sfg_ldlt_diagonal.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.sfg_ldlt_permutation.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+        L.sfg_ldlt_destroy.argtypes = [C.c_void_p]
+        L.sfg_schur_create.argtypes = [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
+                                       C.c_int32, C.POINTER(C.c_void_p)]
+        L.sfg_schur_factorize.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.sfg_schur_solve.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32]
+        L.sfg_schur_destroy.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise SfgError(rc, lib().sfg_last_error().decode())
+
+
+@dataclass
+class OptimizationStats:
+    """optimization_stats_t (lcmtypes/symforce.lcm:302-336) plus per-iteration device times."""
+
+    iterations: list = field(default_factory=list)
+    best_index: int = 0
+    status: int = 0
+    failure_reason: int = 0
+
+    @property
+    def best_error(self) -> float:
+        return self.iterations[self.best_index].new_error
+
+
+class Optimizer:
+    """GPU Levenberg-Marquardt optimizer for one problem structure (create once, optimize many)."""
+
+    def __init__(self, problem: A.ProblemArrays, params: A.OptimizerParams | None = None,
+                 form: A.FormParams | None = None):
+        self.problem = problem
+        self.params = params or A.default_optimizer_params()
+        self.form = form or A.default_form_params()
+        self._h = C.c_void_p()
+        pc = problem.to_c()
+        _check(lib().sfg_create(C.byref(pc), C.byref(self.form), C.byref(self._h)))
+        S, N, M = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(lib().sfg_storage_dim(self._h, C.byref(S), C.byref(N), C.byref(M)))
+        self.storage_dim, self.tangent_dim, self.residual_dim = S.value, N.value, M.value
+
+    def close(self) -> None:
+        if self._h:
+            lib().sfg_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_values(self, values: np.ndarray) -> None:
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        _check(lib().sfg_set_values(self._h, A.dptr(v), v.size))
+
+    def get_values(self) -> np.ndarray:
+        out = np.zeros(self.storage_dim)
+        _check(lib().sfg_get_values(self._h, A.dptr(out), out.size))
+        return out
+
+    def optimize(self, values: np.ndarray | None = None, num_iterations: int = -1,
+                 params: A.OptimizerParams | None = None) -> tuple[np.ndarray, OptimizationStats]:
+        """Optimizer::Optimize: returns (best values, stats)."""
+        if values is not None:
+            self.set_values(values)
+        p = params or self.params
+        cap = (p.iterations if num_iterations < 0 else num_iterations) + 1
+        recs = (A.IterationC * cap)()
+        st = A.StatsC(recs, cap, 0, 0, 0, 0, 0)
+        _check(lib().sfg_optimize(self._h, C.byref(p), num_iterations, C.byref(st)))
+        stats = OptimizationStats([recs[i] for i in range(st.num_iterations)], st.best_index,
+                                  st.status, st.failure_reason)
+        return self.get_values(), stats
+
+    def linearize(self, values: np.ndarray | None = None):
+        """Linearization at the given (or current) values: residual, rhs, error, CSC hessian_lower."""
+        if values is not None:
+            self.set_values(values)
+        res = np.zeros(self.residual_dim)
+        rhs = np.zeros(self.tangent_dim)
+        err = C.c_double()
+        _check(lib().sfg_linearize(self._h, A.dptr(res), A.dptr(rhs), C.byref(err)))
+        nnz = C.c_int64()
+        _check(lib().sfg_hessian_lower(self._h, C.byref(nnz), None, None, None))
+        colptr = np.zeros(self.tangent_dim + 1, dtype=np.int32)
+        rowidx = np.zeros(nnz.value, dtype=np.int32)
+        hv = np.zeros(nnz.value)
+        _check(lib().sfg_hessian_lower(self._h, C.byref(nnz), A.iptr(colptr), A.iptr(rowidx), A.dptr(hv)))
+        return dict(residual=res, rhs=rhs, error=err.value, colptr=colptr, rowidx=rowidx, hvals=hv)
+
+    def permutation(self) -> np.ndarray:
+        n = self.form.linear_solver == A.SFG_LINEAR_SOLVER_SCHUR
+        size = self.tangent_dim - (3 * self.problem.num_schur_keys if n else 0)
+        perm = np.zeros(size, dtype=np.int32)
+        _check(lib().sfg_permutation(self._h, A.iptr(perm), size))
+        return perm
+
+
+class SparseLdlt:
+    """SparseCholeskySolver concept on a CSC lower matrix: factorize(values), solve(b)."""
+
+    def __init__(self, n: int, colptr, rowidx, ordering: int = A.SFG_ORDERING_NESTED_DISSECTION,
+                 device: int = 0):
+        self.n = n
+        self._colptr = np.ascontiguousarray(colptr, dtype=np.int32)
+        self._rowidx = np.ascontiguousarray(rowidx, dtype=np.int32)
+        self._h = C.c_void_p()
+        _check(lib().sfg_ldlt_create(n, A.iptr(self._colptr), A.iptr(self._rowidx), ordering, device,
+                                     C.byref(self._h)))
+
+    def factorize(self, values) -> None:
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        _check(lib().sfg_ldlt_factorize(self._h, A.dptr(v)))
+
+    def solve(self, b) -> np.ndarray:
+        b = np.ascontiguousarray(np.asarray(b, dtype=np.float64).T)  # column-major rhs
+        nrhs = 1 if b.ndim == 1 else b.shape[0]
+        x = np.zeros_like(b)
+        _check(lib().sfg_ldlt_solve(self._h, A.dptr(b), A.dptr(x), nrhs))
+        return x.T if b.ndim > 1 else x
+
+    def diagonal(self) -> np.ndarray:
+        d = np.zeros(self.n)
+        _check(lib().sfg_ldlt_diagonal(self._h, A.dptr(d)))
+        return d
+
+    def permutation(self) -> np.ndarray:
+        p = np.zeros(self.n, dtype=np.int32)
+        _check(lib().sfg_ldlt_permutation(self._h, A.iptr(p)))
+        return p
+
+    def __del__(self) -> None:
+        try:
+            if self._h:
+                lib().sfg_ldlt_destroy(self._h)
+        except Exception:
+            pass
+
+
+class SparseSchur:
+    """SparseSchurSolver concept: A = [[B, E^T], [E, C]] with 3x3 block-diagonal C."""
+
+    def __init__(self, n: int, colptr, rowidx, c_dim: int, device: int = 0):
+        self.n = n
+        self._colptr = np.ascontiguousarray(colptr, dtype=np.int32)
+        self._rowidx = np.ascontiguousarray(rowidx, dtype=np.int32)
+        self._h = C.c_void_p()
+        _check(lib().sfg_schur_create(n, A.iptr(self._colptr), A.iptr(self._rowidx), c_dim, device,
+                                      C.byref(self._h)))
+
+    def factorize(self, values) -> None:
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        _check(lib().sfg_schur_factorize(self._h, A.dptr(v)))
+
+    def solve(self, b) -> np.ndarray:
+        b = np.ascontiguousarray(np.asarray(b, dtype=np.float64).T)
+        nrhs = 1 if b.ndim == 1 else b.shape[0]
+        x = np.zeros_like(b)
+        _check(lib().sfg_schur_solve(self._h, A.dptr(b), A.dptr(x), nrhs))
+        return x.T if b.ndim > 1 else x
+
+    def __del__(self) -> None:
+        try:
+            if self._h:
+                lib().sfg_schur_destroy(self._h)
+        except Exception:
+            pass

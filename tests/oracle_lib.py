@@ -1,0 +1,138 @@
+"""ctypes loader for the CPU oracle (oracle/_build/liboracle.so).
+
+Test infrastructure: the oracle is the checker, never the thing measured or shipped.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+from symforce_gb300 import _cabi as A
+
+ROOT = Path(__file__).resolve().parents[1]
+ORACLE_DIR = ROOT / "oracle"
+LIB_PATH = ORACLE_DIR / "_build" / "liboracle.so"
+
+_lib = None
+
+
+def build() -> Path:
+    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], check=True)
+    return LIB_PATH
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists() or os.environ.get("SFG_REBUILD_ORACLE"):
+            build()
+        L = C.CDLL(str(LIB_PATH))
+        L.orc_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise RuntimeError("oracle: " + lib().orc_last_error().decode())
+
+
+def factor_linearize(kind: int, key_types, storage, consts, epsilon=A.DEFAULT_EPSILON):
+    nk, nc, rdim, _ = A.FACTOR_DIMS[kind]
+    kt = np.ascontiguousarray(key_types, dtype=np.int32)
+    st = np.ascontiguousarray(storage, dtype=np.float64)
+    cs = np.ascontiguousarray(consts, dtype=np.float64)
+    tdim = sum(A.KEY_DIMS[int(t)][1] for t in kt)
+    res = np.zeros(rdim)
+    J = np.zeros((rdim, tdim))
+    _check(lib().orc_factor_linearize(C.c_int32(kind), A.iptr(kt), A.dptr(st), A.dptr(cs),
+                                      C.c_double(epsilon), A.dptr(res), A.dptr(J)))
+    return res, J
+
+
+def linearize(problem: A.ProblemArrays, values=None, epsilon=A.DEFAULT_EPSILON):
+    pc = problem.to_c()
+    v = problem.values if values is None else np.ascontiguousarray(values, dtype=np.float64)
+    M, N, nnz = C.c_int64(), C.c_int64(), C.c_int64()
+    null = C.POINTER(C.c_double)()
+    _check(lib().orc_linearize(C.byref(pc), A.dptr(v), C.c_double(epsilon), C.byref(M), C.byref(N),
+                               C.byref(nnz), null, null, C.POINTER(C.c_int64)(),
+                               C.POINTER(C.c_int32)(), null))
+    res = np.zeros(M.value)
+    rhs = np.zeros(N.value)
+    colptr = np.zeros(N.value + 1, dtype=np.int64)
+    rowidx = np.zeros(nnz.value, dtype=np.int32)
+    hv = np.zeros(nnz.value)
+    _check(lib().orc_linearize(C.byref(pc), A.dptr(v), C.c_double(epsilon), C.byref(M), C.byref(N),
+                               C.byref(nnz), A.dptr(res), A.dptr(rhs), A.lptr(colptr),
+                               A.iptr(rowidx), A.dptr(hv)))
+    return dict(residual=res, rhs=rhs, colptr=colptr, rowidx=rowidx, hvals=hv)
+
+
+def optimize(problem: A.ProblemArrays, params=None, num_iterations=-1, epsilon=A.DEFAULT_EPSILON,
+             linear_solver=A.SFG_LINEAR_SOLVER_SPARSE_LDLT, ordering=A.SFG_ORDERING_MIN_DEGREE,
+             values=None):
+    params = params or A.default_optimizer_params()
+    pc = problem.to_c()
+    v = problem.values if values is None else np.ascontiguousarray(values, dtype=np.float64)
+    out = np.zeros_like(v)
+    cap = max(params.iterations, num_iterations) + 2
+    iters = (A.IterationC * cap)()
+    n, best, status, reason = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+    secs = np.zeros(3)
+    _check(lib().orc_optimize(C.byref(pc), A.dptr(v), C.byref(params), C.c_int32(num_iterations),
+                              C.c_double(epsilon), C.c_int32(linear_solver), C.c_int32(ordering),
+                              A.dptr(out), iters, C.c_int32(cap), C.byref(n), C.byref(best),
+                              C.byref(status), C.byref(reason), A.dptr(secs)))
+    recs = [iters[i] for i in range(n.value)]
+    return dict(values=out, iterations=recs, best_index=best.value, status=status.value,
+                failure_reason=reason.value, seconds=float(secs[0]),
+                seconds_linearize=float(secs[1]), seconds_solve=float(secs[2]))
+
+
+def ldlt_solve(n, colptr, rowidx, vals, b, ordering=A.SFG_ORDERING_MIN_DEGREE, order=None):
+    colptr = np.ascontiguousarray(colptr, dtype=np.int64)
+    rowidx = np.ascontiguousarray(rowidx, dtype=np.int32)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(n)
+    D = np.zeros(n)
+    perm = np.zeros(n, dtype=np.int32)
+    ordp = A.iptr(np.ascontiguousarray(order, dtype=np.int32)) if order is not None else C.POINTER(C.c_int32)()
+    _check(lib().orc_ldlt_solve(C.c_int64(n), A.lptr(colptr), A.iptr(rowidx), A.dptr(vals),
+                                C.c_int32(ordering), ordp, A.dptr(b), A.dptr(x), A.dptr(D),
+                                A.iptr(perm)))
+    return x, D, perm
+
+
+def schur_solve(n, colptr, rowidx, vals, c_dim, b):
+    colptr = np.ascontiguousarray(colptr, dtype=np.int64)
+    rowidx = np.ascontiguousarray(rowidx, dtype=np.int32)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(n)
+    _check(lib().orc_schur_solve(C.c_int64(n), A.lptr(colptr), A.iptr(rowidx), A.dptr(vals),
+                                 C.c_int64(c_dim), A.dptr(b), A.dptr(x)))
+    return x
+
+
+def retract(key_type, storage, delta, epsilon=A.DEFAULT_EPSILON):
+    sd, _ = A.KEY_DIMS[key_type]
+    out = np.zeros(sd)
+    st = np.ascontiguousarray(storage, dtype=np.float64)
+    d = np.ascontiguousarray(delta, dtype=np.float64)
+    _check(lib().orc_retract(C.c_int32(key_type), A.dptr(st), A.dptr(d), C.c_double(epsilon),
+                             A.dptr(out)))
+    return out
+
+
+def pose_smoothing_initial_values(num_keys=10, epsilon=A.DEFAULT_EPSILON):
+    out = np.zeros(7 * num_keys)
+    _check(lib().orc_pose_smoothing_initial_values(C.c_int32(num_keys), C.c_double(epsilon),
+                                                   A.dptr(out)))
+    return out

@@ -1,0 +1,89 @@
+"""GPU parity of the full Levenberg-Marquardt loop against the CPU oracle and the reference's own
+known answers (all through the C ABI)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+import reference_cases as R
+from symforce_gb300 import _cabi as A
+from symforce_gb300 import synth
+from symforce_gb300.optimizer import Optimizer
+
+pytestmark = pytest.mark.gpu
+
+
+def _records(stats_iters):
+    return [(r.iteration, r.current_lambda, r.new_error, r.update_accepted) for r in stats_iters]
+
+
+def test_robot_2d_example_known_answers():
+    p = R.robot_2d_localization()
+    opt = Optimizer(p, form=A.default_form_params(ordering=A.SFG_ORDERING_NESTED_DISSECTION))
+    values, stats = opt.optimize(p.values)
+    E = R.ROBOT_2D_EXPECTED
+    assert len(stats.iterations) == E["num_iterations"]
+    assert E["first_error_range"][0] < stats.iterations[0].new_error < E["first_error_range"][1]
+    assert stats.iterations[0].new_error == pytest.approx(E["first_error_python"], rel=1e-14)
+    assert stats.best_error < E["best_error_below"]
+    assert stats.status == A.SFG_STATUS_SUCCESS
+    np.testing.assert_allclose(values.reshape(-1, 4), E["poses"], atol=1e-6)
+    ref = O.optimize(p)
+    for g, o in zip(stats.iterations, ref["iterations"]):
+        assert g.iteration == o.iteration and g.update_accepted == o.update_accepted
+        assert g.current_lambda == pytest.approx(o.current_lambda, rel=1e-12)
+        assert g.new_error == pytest.approx(o.new_error, rel=1e-9, abs=1e-14)
+
+
+def test_pose_smoothing_known_answers():
+    v0 = O.pose_smoothing_initial_values()
+    p = R.pose_smoothing(v0)
+    params = A.default_optimizer_params(**R.POSE_SMOOTHING_PARAMS)
+    opt = Optimizer(p, params)
+    values, stats = opt.optimize(p.values)
+    last = stats.iterations[-1]
+    assert last.iteration == R.POSE_SMOOTHING_EXPECTED["last_iteration"]
+    lam, tol = R.POSE_SMOOTHING_EXPECTED["lambda_approx"]
+    assert last.current_lambda == pytest.approx(lam, rel=tol)
+    err, tol = R.POSE_SMOOTHING_EXPECTED["error_approx"]
+    assert last.new_error == pytest.approx(err, rel=tol)
+    assert stats.status == A.SFG_STATUS_SUCCESS
+
+
+def test_linearization_matches_oracle_ba_small():
+    p = synth.bundle_adjustment(num_cameras=8, num_points=120, num_observations=500, seed=3)
+    opt = Optimizer(p, form=A.default_form_params(linear_solver=A.SFG_LINEAR_SOLVER_SCHUR))
+    g = opt.linearize(p.values)
+    o = O.linearize(p)
+    np.testing.assert_allclose(g["residual"], o["residual"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_array_equal(g["colptr"], o["colptr"])
+    np.testing.assert_array_equal(g["rowidx"], o["rowidx"])
+    scale = np.abs(o["hvals"]).max()
+    np.testing.assert_allclose(g["hvals"], o["hvals"], rtol=1e-9, atol=1e-12 * scale)
+    np.testing.assert_allclose(g["rhs"], o["rhs"], rtol=1e-9, atol=1e-12 * np.abs(o["rhs"]).max())
+
+
+@pytest.mark.parametrize("solver", [A.SFG_LINEAR_SOLVER_SCHUR, A.SFG_LINEAR_SOLVER_SPARSE_LDLT])
+def test_ba_small_matches_oracle(solver):
+    p = synth.bundle_adjustment(num_cameras=10, num_points=300, num_observations=1300, seed=1)
+    params = A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC, iterations=20)
+    opt = Optimizer(p, params, A.default_form_params(linear_solver=solver))
+    values, stats = opt.optimize(p.values)
+    ref = O.optimize(p, params, linear_solver=A.SFG_LINEAR_SOLVER_SPARSE_LDLT)
+    assert len(stats.iterations) == len(ref["iterations"])
+    for g, o in zip(stats.iterations, ref["iterations"]):
+        assert g.update_accepted == o.update_accepted
+        assert g.new_error == pytest.approx(o.new_error, rel=1e-9)
+    assert stats.best_error == pytest.approx(ref["iterations"][ref["best_index"]].new_error, rel=1e-9)
+    assert stats.status == ref["status"]
+
+
+def test_robot_2d_config_matches_oracle():
+    p = synth.robot_2d(200, seed=2)
+    params = A.default_optimizer_params(iterations=30)
+    opt = Optimizer(p, params)
+    values, stats = opt.optimize(p.values)
+    ref = O.optimize(p, params)
+    assert stats.best_error == pytest.approx(ref["iterations"][ref["best_index"]].new_error, rel=1e-9)
