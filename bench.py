@@ -1,0 +1,318 @@
+#!/usr/bin/env python3
+"""Benchmark: bundle-adjustment time to the FP64-oracle cost on one GB300 (plain FP64 form).
+
+Workload (one step = one full Optimizer::Optimize call): the 50-camera / 7,800-point / ~32k
+observation synthetic bundle adjustment with Cauchy-whitened Snavely reprojection factors, Schur
+elimination of the points and a device multifrontal LDL^T of the reduced camera system, DYNAMIC
+lambda, 50 iterations.  Metric: milliseconds until the best cost is within 1e-6 (relative) of the
+CPU oracle's final cost (committed in tests/golden/oracle_costs.json), read from the per-iteration
+device timestamps of the run; lower is better.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`--impl reference` times the CPU restatement of the reference's sym::Optimizer (the reference
+itself cannot be compiled here: its Eigen / METIS dependencies are absent) on the host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+from symforce_gb300 import _cabi as A  # noqa: E402
+from symforce_gb300 import workloads  # noqa: E402
+
+METRIC = "BA time to FP64-oracle cost (rel 1e-6): plain vs mixed/learned; linearize GB/s"
+WORKLOAD = "ba_50_7800"
+TOL = 1e-6
+
+
+def _oracle_cost(name: str) -> dict:
+    return json.loads((ROOT / "tests" / "golden" / "oracle_costs.json").read_text())[name]
+
+
+def _measured_peaks() -> tuple[dict, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self) -> None:
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self) -> None:
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def _allreduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _cpu_solve(problem, params, max_iterations: int) -> dict:
+    """The oracle port (CPU restatement of the reference optimizer), single-threaded."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib as O
+    p = A.default_optimizer_params()
+    for f, _ in A.OptimizerParams._fields_:
+        setattr(p, f, getattr(params, f))
+    p.iterations = max_iterations
+    r = O.optimize(problem, p, linear_solver=A.SFG_LINEAR_SOLVER_SPARSE_LDLT,
+                   ordering=A.SFG_ORDERING_MIN_DEGREE)
+    return r
+
+
+def run_reference(args) -> None:
+    world, rank, _ = _dist_init()
+    if rank != 0:
+        return
+    w = workloads.get(WORKLOAD)
+    problem = w.problem()
+    params = w.params()
+    oracle = _oracle_cost(WORKLOAD)
+    target = oracle["best_error"] * (1 + TOL)
+    # bounded sample: the full 50-iteration solve takes ~10-15 s on one core; cap the whole run
+    budget_s = float(os.environ.get("SFG_REFERENCE_BUDGET_S", "200"))
+    t0 = time.perf_counter()
+    probe = _cpu_solve(problem, params, params.iterations)
+    est = time.perf_counter() - t0
+    total_steps = args.warmup + args.steps
+    iters = params.iterations
+    if est * total_steps > budget_s:
+        iters = max(5, int(params.iterations * budget_s / (est * total_steps)))
+    times = []
+    for k in range(total_steps):
+        t0 = time.perf_counter()
+        r = _cpu_solve(problem, params, iters)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt * params.iterations / iters)
+    ttc_iters = next((i for i, e in enumerate(probe["iterations"]) if e.best_error <= target),
+                     len(probe["iterations"]) - 1)
+    frac = ttc_iters / max(len(probe["iterations"]) - 1, 1)
+    ms_step = 1e3 * statistics.median(times)
+    value = ms_step * frac
+    sample = (f"{iters} of {params.iterations} LM iterations per step, scaled to the full solve"
+              if iters < params.iterations else "full 50-iteration solve per step")
+    line = {
+        "metric": METRIC, "impl": "reference", "value": round(value, 3), "unit": "ms",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
+        "config": {"workload": WORKLOAD, "form": "plain FP64, CPU restatement of sym::Optimizer "
+                   "(up-looking sparse LDL^T on the full Hessian, block minimum-degree ordering)",
+                   "cores": 1},
+        "cpu_baseline": {"value": round(value, 3), "unit": "ms", "cores": 1, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "ms", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "time_to_cost_fraction_of_solve": round(frac, 4),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args) -> None:
+    world, rank, local = _dist_init()
+    import torch
+    torch.cuda.set_device(local)
+    from symforce_gb300.optimizer import Optimizer
+    w = workloads.get(WORKLOAD)
+    problem = w.problem()
+    params = w.params()
+    oracle = _oracle_cost(WORKLOAD)
+    target = oracle["best_error"] * (1 + TOL)
+    target9 = oracle["best_error"] * (1 + 1e-9)
+    form = w.form()
+    form.device = local
+    opt = Optimizer(problem, params, form)
+    S = problem.storage_dim
+    vin = torch.from_numpy(problem.values.copy()).pin_memory()
+    vout = torch.empty(S, dtype=torch.float64).pin_memory()
+    vin_np, vout_np = vin.numpy(), vout.numpy()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    def step():
+        flush.zero_()  # L2 flush: 256 MB > 129 MB L2
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, stats = opt.optimize(vin_np, out=vout_np)
+        t1 = time.perf_counter()
+        recs = stats.iterations
+        ttc = next((r.elapsed_ms for r in recs if r.best_error <= target), None)
+        ttc9 = next((r.elapsed_ms for r in recs if r.best_error <= target9), None)
+        return (t1 - t0) * 1e3, stats, ttc, ttc9
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    if clocks:
+        clocks.start()
+    _barrier(world)
+    torch.cuda.synchronize()
+    e2e, dev, ttcs, ttc9s, launches, last = [], [], [], [], [], None
+    for _ in range(args.steps):
+        e, stats, ttc, ttc9 = step()
+        e2e.append(e)
+        dev.append(stats.device_ms)
+        ttcs.append(ttc if ttc is not None else float("nan"))
+        ttc9s.append(ttc9 if ttc9 is not None else float("nan"))
+        launches.append(stats.kernel_launches)
+        last = stats
+    torch.cuda.synchronize()
+    _barrier(world)
+    clk = clocks.stop() if clocks else None
+    value = _allreduce_max(statistics.median(ttcs), world)
+    ms_step = _allreduce_max(statistics.median(dev), world)
+    e2e_ms = _allreduce_max(statistics.median(e2e), world)
+    # live roofline of the linearization stage (CUDA events on the library's stream)
+    lin = opt.time_stage(A.SFG_STAGE_LINEARIZE, reps=50)
+    stages = {}
+    for name, sid in [("linearize", A.SFG_STAGE_LINEARIZE), ("schur", A.SFG_STAGE_SCHUR),
+                      ("factor", A.SFG_STAGE_FACTOR), ("solve", A.SFG_STAGE_SOLVE)]:
+        t = opt.time_stage(sid, reps=20)
+        stages[name] = {"ms": round(t["ms"], 5), "fp64_gfma_s": round(t["fmas"] / t["ms"] / 1e6, 2)}
+    peaks, peak_kind = _measured_peaks()
+    achieved = lin["bytes"] / (lin["ms"] * 1e-3) / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "traffic.json"
+    if tp.exists():
+        traffic = json.loads(tp.read_text()).get(f"linearize_{WORKLOAD}")
+    final_rel = abs(last.best_error - oracle["best_error"]) / oracle["best_error"]
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        r = _cpu_solve(problem, params, params.iterations)
+        cpu_s = time.perf_counter() - t0
+        frac = next((i for i, e in enumerate(r["iterations"]) if e.best_error <= target),
+                    len(r["iterations"]) - 1) / max(len(r["iterations"]) - 1, 1)
+        cpu = {"value": round(cpu_s * 1e3 * frac, 3), "unit": "ms", "cores": 1, "kind": "port",
+               "sample": "one full 50-iteration solve of the same workload on one host core "
+                         "(CPU restatement of sym::Optimizer, full-Hessian sparse LDL^T)"}
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": "ms", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded PCG64, no dataset)",
+        "config": {"workload": WORKLOAD, "form": "plain FP64 (Schur over points + multifrontal "
+                   "LDL^T of the reduced camera system)", "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "l2": "flushed (256 MB write) before every step",
+                   "num_cameras": problem.meta["num_cameras"], "num_points": problem.meta["num_points"],
+                   "num_observations": problem.meta["num_observations"],
+                   "lm_iterations": len(last.iterations) - 1},
+        "roofline": {"kernel": "linearize (Snavely FP64 factor kernel + staged reduction + cost)",
+                     "bound": "hbm", "achieved": round(achieved, 2),
+                     "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": round(achieved / peaks.get("hbm_gbs"), 5),
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes": lin["bytes"], "ms_per_launch": round(lin["ms"], 5)},
+        "stages_ms_per_launch": stages,
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": 8 * S + 8 * 24,
+                "d2h_bytes_per_step": 8 * S + 64 * len(last.iterations)},
+        "gpu_launches": int(sum(launches)),
+        "clocks": clk,
+        "time_to_cost_1e-9_ms": round(statistics.median(ttc9s), 4),
+        "final_cost_rel_err_vs_oracle": final_rel,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -168,7 +168,8 @@ typedef struct sfg_stats_t {
   int32_t best_index;
   int32_t status;
   int32_t failure_reason;
-  int32_t _pad;
+  int32_t kernel_launches;  /* device kernels the optimize call launched (graph nodes executed) */
+  double device_ms;         /* CUDA-event time of the device work of the optimize call */
 } sfg_stats_t;
 
 /* Forms of the solver (besides the plain FP64 drop-in). */
@@ -222,6 +223,14 @@ int32_t sfg_hessian_lower(sfg_handle* h, int64_t* nnz, int32_t* col_ptr, int32_t
                           double* values);
 /* The block ordering used by the linear solver, as new position of every state scalar. */
 int32_t sfg_permutation(sfg_handle* h, int32_t* perm, int64_t n);
+/* Time `reps` back-to-back launches of one stage of the iteration on the handle's stream with CUDA
+ * events (after one warm-up launch) at the current values: SFG_STAGE_LINEARIZE (all factor
+ * batches + staged reduction + cost), SFG_STAGE_SCHUR (point inverses, reduced system and rhs),
+ * SFG_STAGE_FACTOR (numeric LDL^T), SFG_STAGE_SOLVE (triangular solves).  Requires a prior
+ * sfg_optimize on the handle.  Also returns the stage's algorithmic bytes and multiply-adds. */
+enum { SFG_STAGE_LINEARIZE = 0, SFG_STAGE_SCHUR = 1, SFG_STAGE_FACTOR = 2, SFG_STAGE_SOLVE = 3 };
+int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_per_launch,
+                       double* algorithmic_bytes, double* fmas);
 
 /* -------------------------------- SparseCholeskySolver -------------------------------------
  * The LinearSolver concept on a user CSC lower matrix (symforce/opt/sparse_cholesky/

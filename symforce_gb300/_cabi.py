@@ -151,8 +151,12 @@ class StatsC(C.Structure):
         ("best_index", C.c_int32),
         ("status", C.c_int32),
         ("failure_reason", C.c_int32),
-        ("_pad", C.c_int32),
+        ("kernel_launches", C.c_int32),
+        ("device_ms", C.c_double),
     ]
+
+
+SFG_STAGE_LINEARIZE, SFG_STAGE_SCHUR, SFG_STAGE_FACTOR, SFG_STAGE_SOLVE = 0, 1, 2, 3
 
 
 class FormParams(C.Structure):

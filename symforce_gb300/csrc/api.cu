@@ -5,12 +5,16 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
 
+#include "device_plan.h"
 #include "kernels.h"
 #include "layout.h"
 
@@ -20,37 +24,10 @@ thread_local std::string g_last_error;
 
 namespace {
 
-// ---------------------------------------------------------------------------------------------
-// device memory helpers
-// ---------------------------------------------------------------------------------------------
-struct DeviceArena {
-  std::vector<void*> ptrs;
-  ~DeviceArena() {
-    for (void* p : ptrs) cudaFree(p);
-  }
-  void* Alloc(size_t bytes) {
-    void* p = nullptr;
-    if (bytes == 0) bytes = 16;
-    const cudaError_t e = cudaMalloc(&p, bytes);
-    if (e != cudaSuccess)
-      throw Error(e == cudaErrorMemoryAllocation ? SFG_ERR_OUT_OF_MEMORY : SFG_ERR_CUDA,
-                  std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
-    ptrs.push_back(p);
-    return p;
-  }
-  template <typename T>
-  T* Upload(const std::vector<T>& v) {
-    T* p = static_cast<T*>(Alloc(v.size() * sizeof(T)));
-    if (!v.empty()) SFG_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
-    return p;
-  }
-  template <typename T>
-  T* Zeros(size_t n) {
-    T* p = static_cast<T*>(Alloc(n * sizeof(T)));
-    SFG_CUDA(cudaMemset(p, 0, n * sizeof(T)));
-    return p;
-  }
-};
+bool TraceOn() {
+  const char* tr = std::getenv("SFG_TRACE_FACTOR");
+  return tr && tr[0] == '1';
+}
 
 void CheckDevice(int device) {
   int n = 0;
@@ -59,116 +36,6 @@ void CheckDevice(int device) {
     throw Error(SFG_ERR_NO_DEVICE, "no CUDA device is visible; this library has no CPU fallback");
   if (device < 0 || device >= n) throw Error(SFG_ERR_INVALID_ARGUMENT, "bad device ordinal");
   SFG_CUDA(cudaSetDevice(device));
-}
-
-// Device copy of a symbolic factorization + task plan.
-struct FactorPlan {
-  Symbolic sym;
-  TaskPlan plan;
-  FactorDev f{};
-  int grid_factor = 0, grid_solve = 0;
-  size_t elem = 8;
-  void* F = nullptr;       // front pool
-  void* ycon = nullptr;
-  void* ysave = nullptr;
-  void* xperm = nullptr;
-  int nflags = 0;
-};
-
-void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, int ordering,
-                     size_t elem, int* error_word, const LmState* st, int64_t a_stride,
-                     int64_t b_stride, int num_sms) {
-  fp.elem = elem;
-  fp.sym = Analyze(pat, ordering);
-  const Symbolic& S = fp.sym;
-  fp.plan = PlanTasks(S, elem == 8 ? 16 : 32);
-  const TaskPlan& T = fp.plan;
-  // device arrays
-  FactorDev& f = fp.f;
-  f.ns = S.ns;
-  f.ntasks = int(T.tasks.size());
-  f.tile = T.tile;
-  f.tasks = A.Upload(T.tasks);
-  f.sn_w = A.Upload(S.sn_w);
-  f.sn_m = A.Upload(S.sn_m);
-  f.sn_foff = A.Upload(S.sn_foff);
-  f.tile_base = A.Upload(T.tile_base);
-  f.npiv = A.Upload(T.npiv);
-  f.ntiles = A.Upload(T.ntiles);
-  f.asm_off = A.Upload(S.asm_off);
-  std::vector<AsmDev> asms(S.asms.size());
-  for (size_t q = 0; q < S.asms.size(); ++q) {
-    const auto& a = S.asms[q];
-    AsmDev d;
-    d.src = a.src;
-    d.dscal = 0;
-    d.row0 = a.row0;
-    d.col0 = a.col0;
-    d.di = a.di;
-    d.dj = a.dj;
-    d.transpose = a.transpose;
-    d.diag = a.diag;
-    asms[q] = d;
-  }
-  // diagonal blocks: original scalar offset of the block (for damping)
-  {
-    // map each diagonal assembly entry back to its original block: src offset -> block
-    std::vector<int64_t> src_to_block_scalar;
-    for (int j = 0; j < pat.nb; ++j)
-      for (int64_t q = pat.colptr[j]; q < pat.colptr[j + 1]; ++q)
-        if (pat.rows[q] == j) {
-          for (auto& a : asms)
-            if (a.diag && a.src == pat.boff[q]) a.dscal = pat.off[j];
-        }
-  }
-  f.asms = A.Upload(asms);
-  f.rel_off = A.Upload(S.rel_off);
-  f.rel = A.Upload(S.rel);
-  std::vector<int32_t> cptr(S.ns + 1, 0), clist;
-  for (int s = 0; s < S.ns; ++s) {
-    for (int c : S.sn_children[s]) clist.push_back(c);
-    cptr[s + 1] = int32_t(clist.size());
-  }
-  f.child_ptr = A.Upload(cptr);
-  f.child_list = A.Upload(clist);
-  f.parent = A.Upload(S.sn_parent);
-  f.idx_off = A.Upload(S.idx_off);
-  f.idx = A.Upload(S.idx);
-  std::vector<int32_t> scalar_old(S.n);
-  for (int q = 0; q < S.nb; ++q) {
-    const int old = S.border[q];
-    for (int t = 0; t < pat.dim[old]; ++t) scalar_old[S.pstart[q] + t] = int32_t(pat.off[old] + t);
-  }
-  f.scalar_old = A.Upload(scalar_old);
-  f.tile_state = A.Zeros<int>(std::max(T.nstates, 1));
-  f.counters = A.Zeros<int>(2);
-  fp.nflags = 2 * S.ns;
-  f.front_flags = A.Zeros<int>(std::max(fp.nflags, 1));
-  f.error = error_word;
-  int maxm = 1;
-  for (int s = 0; s < S.ns; ++s) maxm = std::max(maxm, S.sn_m[s]);
-  f.max_m = maxm;
-  f.st = st;
-  f.a_stride = a_stride;
-  f.b_stride = b_stride;
-  fp.F = A.Alloc(size_t(S.front_pool) * elem);
-  fp.ycon = A.Alloc(size_t(std::max<int64_t>(S.rel_off[S.ns], 1)) * elem);
-  fp.ysave = A.Alloc(size_t(std::max<int64_t>(S.idx_off[S.ns], 1)) * elem);
-  fp.xperm = A.Alloc(size_t(std::max<int64_t>(S.n, 1)) * elem);
-  const int per_sm = 8;
-  fp.grid_factor = std::max(1, std::min<int>(f.ntasks, num_sms * per_sm));
-  fp.grid_solve = std::max(1, std::min<int>(2 * S.ns, num_sms * per_sm));
-  if (elem == 8) ConfigureSolve<double>(maxm);
-  else ConfigureSolve<float>(maxm);
-}
-
-template <typename T>
-void RunFactorAndSolve(const FactorPlan& fp, const void* A, const double* damping, const void* b,
-                       void* x, cudaStream_t s) {
-  LaunchResetFactorState(fp.f.tile_state, fp.plan.nstates, fp.f.front_flags, fp.nflags,
-                         fp.f.counters, s);
-  LaunchFactor<T>(fp.f, A, damping, fp.F, fp.grid_factor, s);
-  LaunchSolve<T>(fp.f, fp.F, b, fp.ycon, fp.ysave, fp.xperm, x, fp.grid_solve, s);
 }
 
 }  // namespace
@@ -261,7 +128,8 @@ void EnqueueLinearize(sfg_handle* h, int which, cudaStream_t s) {
 }
 
 template <typename T>
-void EnqueueIterationBody(sfg_handle* h, cudaGraphConditionalHandle cond, cudaStream_t s) {
+void EnqueueIterationBody(sfg_handle* h, cudaGraphConditionalHandle cond, int use_cond,
+                          cudaStream_t s) {
   const int64_t N = h->P.N;
   LaunchDamping<T>(h->damp, h->hess, h->L.nvals, h->params, h->st, s);
   if (h->schur) {
@@ -269,10 +137,12 @@ void EnqueueIterationBody(sfg_handle* h, cudaGraphConditionalHandle cond, cudaSt
                          h->st, s);
     LaunchSchurBuildS<T>(h->sd, h->hess, h->L.nvals, h->damp.damping, h->W, h->S, h->st, s);
     LaunchSchurRhs<T>(h->sd, h->hess, h->L.nvals, h->rhs, N, h->tp, h->v, h->st, s);
-    RunFactorAndSolve<T>(h->fp, h->S, nullptr, h->v, h->y, s);
+    EnqueueFactor<T>(h->fp, h->S, nullptr, s);
+    EnqueueSolve<T>(h->fp, h->v, h->y, s);
     LaunchSchurBackSub<T>(h->sd, h->y, h->W, h->tp, h->update, s);
   } else {
-    RunFactorAndSolve<T>(h->fp, h->hess, h->damp.damping, h->rhs, h->xsol, s);
+    EnqueueFactor<T>(h->fp, h->hess, h->damp.damping, s);
+    EnqueueSolve<T>(h->fp, h->rhs, h->xsol, s);
     LaunchNegate<T>(h->xsol, h->update, N, s);
   }
   RetractDev r;
@@ -288,7 +158,7 @@ void EnqueueIterationBody(sfg_handle* h, cudaGraphConditionalHandle cond, cudaSt
   LaunchLinearDelta<T>(h->update, h->rhs, h->damp.damping, h->last_update, N, h->delta_partials,
                        h->st, 1, s);
   LaunchDecide(h->params, h->st, h->records, h->update, h->last_update, N, h->delta_partials,
-               DeltaPartials(), cond, s);
+               DeltaPartials(), cond, use_cond, s);
 }
 
 template <typename T>
@@ -312,7 +182,7 @@ void BuildGraph(sfg_handle* h) {
   LaunchCopyValues(h->values_in, h->values, h->P.S, h->st, 1, s);
   LaunchBegin(h->params, h->st, 0, s);
   EnqueueLinearize<T>(h, 0, s);
-  LaunchFirstRecord(h->params, h->st, h->records, cond, s);
+  LaunchFirstRecord(h->params, h->st, h->records, cond, 1, s);
   // conditional while node
   cudaStreamCaptureStatus status;
   const cudaGraphNode_t* deps = nullptr;
@@ -335,12 +205,32 @@ void BuildGraph(sfg_handle* h) {
   cudaStream_t bs;
   SFG_CUDA(cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking));
   SFG_CUDA(cudaStreamBeginCaptureToGraph(bs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  EnqueueIterationBody<T>(h, cond, bs);
+  EnqueueIterationBody<T>(h, cond, 1, bs);
   cudaGraph_t body_out;
   SFG_CUDA(cudaStreamEndCapture(bs, &body_out));
   cudaStreamDestroy(bs);
   SFG_CUDA(cudaGraphInstantiate(&h->exec, g, 0));
   h->have_graph = true;
+}
+
+// The same work as the graph, launched one kernel at a time from the host (the loop condition is
+// read back after every iteration).  Used for per-kernel profiling, since profilers do not
+// attribute kernels inside graphs that contain conditional nodes.
+template <typename T>
+void RunEager(sfg_handle* h) {
+  cudaStream_t s = h->stream;
+  LaunchCopyValues(h->values_in, h->values, h->P.S, h->st, 1, s);
+  LaunchBegin(h->params, h->st, 0, s);
+  EnqueueLinearize<T>(h, 0, s);
+  LaunchFirstRecord(h->params, h->st, h->records, 0, 0, s);
+  for (;;) {
+    int done = 0;
+    SFG_CUDA(cudaMemcpyAsync(&done, &h->st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SFG_CUDA(cudaStreamSynchronize(s));
+    if (done) break;
+    EnqueueIterationBody<T>(h, 0, 0, s);
+  }
+  LaunchCopyBest(h->values, h->values_in, h->P.S, h->st, s);
 }
 
 void ToLmParams(const sfg_optimizer_params_t& p, int iterations, double eps, LmParams* o) {
@@ -496,12 +386,30 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
     h->S = A.Alloc(size_t(std::max<int64_t>(S.Spat.nvals(), 1)) * E);
     h->v = A.Alloc(size_t(std::max<int64_t>(S.nB, 1)) * E);
     h->y = A.Alloc(size_t(std::max<int64_t>(S.nB, 1)) * E);
-    BuildFactorPlan(A, h->fp, S.Spat, fm.ordering, E, err_word, h->st, 0, 0, h->num_sms);
+    BuildFactorPlan(A, h->fp, S.Spat, fm.ordering, E, err_word, h->st, 0, 0, h->num_sms, TraceOn());
   } else {
     h->xsol = A.Alloc(size_t(P.N) * E);
-    BuildFactorPlan(A, h->fp, h->L.H, fm.ordering, E, err_word, h->st, h->L.nvals, P.N, h->num_sms);
+    BuildFactorPlan(A, h->fp, h->L.H, fm.ordering, E, err_word, h->st, h->L.nvals, P.N, h->num_sms,
+                    TraceOn());
   }
   SFG_CUDA(cudaDeviceSynchronize());
+}
+
+int PrologueKernels(const sfg_handle* h) {
+  int n = 0;
+  for (const auto& b : h->batches) n += b.count > 0 ? 1 : 0;
+  n += h->red.ngroups > 0 ? 1 : 0;
+  return n + 1 /*cost*/ + 1 /*copy*/ + 1 /*begin*/ + 1 /*first record*/ + 1 /*copy best*/;
+}
+
+int BodyKernels(const sfg_handle* h) {
+  int n = 0;
+  for (const auto& b : h->batches) n += b.count > 0 ? 1 : 0;
+  n += h->red.ngroups > 0 ? 1 : 0;
+  n += 1;  // cost
+  n += 1 /*damping*/ + 1 /*retract*/ + 1 /*delta*/ + 1 /*decide*/ + 3 /*reset, factor, solve*/;
+  n += h->schur ? 4 /*points, S, rhs, back-substitution*/ : 1 /*negate*/;
+  return n;
 }
 
 void EnsureRecords(sfg_handle* h, int cap) {
@@ -635,13 +543,30 @@ int32_t sfg_optimize(sfg_handle* h, const sfg_optimizer_params_t* params, int32_
     sfg::LmParams lp;
     sfg::ToLmParams(*params, iters, h->epsilon, &lp);
     SFG_CUDA(cudaMemcpyAsync(h->params, &lp, sizeof(lp), cudaMemcpyHostToDevice, h->stream));
-    SFG_CUDA(cudaGraphLaunch(h->exec, h->stream));
+    cudaEvent_t e0, e1;
+    SFG_CUDA(cudaEventCreate(&e0));
+    SFG_CUDA(cudaEventCreate(&e1));
+    SFG_CUDA(cudaEventRecord(e0, h->stream));
+    const char* eager = std::getenv("SFG_EAGER");
+    if (eager && eager[0] == '1') {
+      sfg::RunEager<double>(h);
+    } else {
+      SFG_CUDA(cudaGraphLaunch(h->exec, h->stream));
+    }
+    SFG_CUDA(cudaEventRecord(e1, h->stream));
     SFG_CUDA(cudaStreamSynchronize(h->stream));
+    float ms = 0.f;
+    SFG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
     sfg::LmState st;
     SFG_CUDA(cudaMemcpy(&st, h->st, sizeof(st), cudaMemcpyDeviceToHost));
     if (st.device_error)
       throw Error(SFG_ERR_DEVICE_STATUS, "device loop hit its cap (code " + std::to_string(st.device_error) + ")");
     if (stats) {
+      stats->device_ms = double(ms);
+      stats->kernel_launches =
+          sfg::PrologueKernels(h) + std::max(st.num_records - 1, 0) * sfg::BodyKernels(h);
       stats->num_iterations = st.num_records;
       stats->best_index = st.best_index;
       stats->status = st.status;
@@ -724,6 +649,104 @@ int32_t sfg_permutation(sfg_handle* h, int32_t* perm, int64_t n) {
       const int old = S.border[q];
       for (int t = 0; t < pat.dim[old]; ++t) perm[pat.off[old] + t] = int32_t(S.pstart[q] + t);
     }
+  });
+}
+
+int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_per_launch,
+                       double* algorithmic_bytes, double* fmas) {
+  return Guard([&] {
+    if (!h || reps < 1) throw Error(SFG_ERR_INVALID_ARGUMENT, "bad argument");
+    if (!h->have_graph) throw Error(SFG_ERR_INVALID_ARGUMENT, "call sfg_optimize first");
+    SFG_CUDA(cudaSetDevice(h->device));
+    cudaStream_t s = h->stream;
+    const auto& P = h->P;
+    double bytes = 0, fma = 0;
+    std::function<void()> launch;
+    switch (stage) {
+      case SFG_STAGE_LINEARIZE: {
+        launch = [&] { sfg::EnqueueLinearize<double>(h, 1, s); };
+        int64_t consts = 0;
+        for (const auto& b : P.batches) consts += int64_t(b.count) * b.nc;
+        bytes = 8.0 * double(P.S + consts + P.M + int64_t(h->L.csc_rowidx.size()) + P.N);
+        for (const auto& b : P.batches) {
+          const double td = b.tdim, rd = b.rdim;
+          fma += double(b.count) * (rd * td * (td + 1) / 2 + rd * td);
+        }
+        break;
+      }
+      case SFG_STAGE_SCHUR: {
+        if (!h->schur) throw Error(SFG_ERR_INVALID_ARGUMENT, "handle has no Schur stage");
+        const auto& S = h->SL;
+        launch = [&] {
+          sfg::LaunchSchurPoints<double>(h->sd, h->hess, h->rhs, h->L.nvals, P.N, h->damp.damping,
+                                         h->cinv, h->W, h->tp, h->st, s);
+          sfg::LaunchSchurBuildS<double>(h->sd, h->hess, h->L.nvals, h->damp.damping, h->W, h->S,
+                                         h->st, s);
+          sfg::LaunchSchurRhs<double>(h->sd, h->hess, h->L.nvals, h->rhs, P.N, h->tp, h->v, h->st, s);
+        };
+        // read E and C blocks + rhs, write W and S; E is re-read for the rhs
+        int64_t ne = 0;
+        for (size_t e = 0; e < S.pt_eoff.size(); ++e) ne += 3 * S.pt_ekey_dim[e];
+        bytes = 8.0 * double(2 * ne + 2 * ne + 9 * S.npoints + S.Spat.nvals() + P.N);
+        for (size_t b = 0; b + 1 < S.sb_ptr.size(); ++b)
+          fma += 3.0 * S.sb_dk[b] * S.sb_dl[b] * double(S.sb_ptr[b + 1] - S.sb_ptr[b]);
+        fma += 9.0 * double(ne) / 3.0 * 3.0;
+        break;
+      }
+      case SFG_STAGE_FACTOR: {
+        const sfg::FactorPlan& fp = h->fp;
+        const void* A = h->schur ? h->S : h->hess;
+        const double* damping = h->schur ? nullptr : h->damp.damping;
+        launch = [&, A, damping] { sfg::EnqueueFactor<double>(fp, A, damping, s); };
+        bytes = 8.0 * 2.0 * double(fp.sym.front_pool);
+        fma = fp.sym.flops;
+        break;
+      }
+      case SFG_STAGE_SOLVE: {
+        const sfg::FactorPlan& fp = h->fp;
+        const void* b = h->schur ? h->v : h->rhs;
+        void* x = h->schur ? h->y : h->xsol;
+        launch = [&, b, x] { sfg::EnqueueSolve<double>(fp, b, x, s); };
+        bytes = 8.0 * double(fp.sym.nnz_L + fp.sym.n) * 2.0;
+        fma = 2.0 * double(fp.sym.nnz_L);
+        break;
+      }
+      default:
+        throw Error(SFG_ERR_INVALID_ARGUMENT, "unknown stage");
+    }
+    launch();
+    cudaEvent_t e0, e1;
+    SFG_CUDA(cudaEventCreate(&e0));
+    SFG_CUDA(cudaEventCreate(&e1));
+    SFG_CUDA(cudaEventRecord(e0, s));
+    for (int r = 0; r < reps; ++r) launch();
+    SFG_CUDA(cudaEventRecord(e1, s));
+    SFG_CUDA(cudaStreamSynchronize(s));
+    SFG_CUDA(cudaGetLastError());
+    float ms = 0.f;
+    SFG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    sfg::LmState st;
+    SFG_CUDA(cudaMemcpy(&st, h->st, sizeof(st), cudaMemcpyDeviceToHost));
+    if (st.device_error) throw Error(SFG_ERR_DEVICE_STATUS, "device loop hit its cap");
+    if (stage == SFG_STAGE_FACTOR && h->fp.f.trace) {
+      if (const char* path = std::getenv("SFG_TRACE_FACTOR_FILE")) {
+        const auto& tasks = h->fp.plan.tasks;
+        std::vector<unsigned long long> tr(4 * tasks.size());
+        SFG_CUDA(cudaMemcpy(tr.data(), h->fp.f.trace, tr.size() * 8, cudaMemcpyDeviceToHost));
+        if (FILE* fo = std::fopen(path, "wb")) {
+          const int64_t n = int64_t(tasks.size());
+          std::fwrite(&n, 8, 1, fo);
+          std::fwrite(tasks.data(), sizeof(int4), tasks.size(), fo);
+          std::fwrite(tr.data(), 8, tr.size(), fo);
+          std::fclose(fo);
+        }
+      }
+    }
+    if (ms_per_launch) *ms_per_launch = double(ms) / reps;
+    if (algorithmic_bytes) *algorithmic_bytes = bytes;
+    if (fmas) *fmas = fma;
   });
 }
 

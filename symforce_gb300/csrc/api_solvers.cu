@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "device_plan.h"
 #include "kernels.h"
 #include "layout.h"
 
@@ -22,34 +23,7 @@ namespace {
 
 using sfg::Error;
 
-struct Arena {
-  std::vector<void*> ptrs;
-  ~Arena() {
-    for (void* p : ptrs) cudaFree(p);
-  }
-  void* Alloc(size_t bytes) {
-    void* p = nullptr;
-    if (bytes == 0) bytes = 16;
-    const cudaError_t e = cudaMalloc(&p, bytes);
-    if (e != cudaSuccess)
-      throw Error(e == cudaErrorMemoryAllocation ? SFG_ERR_OUT_OF_MEMORY : SFG_ERR_CUDA,
-                  std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    ptrs.push_back(p);
-    return p;
-  }
-  template <typename T>
-  T* Upload(const std::vector<T>& v) {
-    T* p = static_cast<T*>(Alloc(v.size() * sizeof(T)));
-    if (!v.empty()) SFG_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
-    return p;
-  }
-  template <typename T>
-  T* Zeros(size_t n) {
-    T* p = static_cast<T*>(Alloc(std::max<size_t>(n, 1) * sizeof(T)));
-    SFG_CUDA(cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T)));
-    return p;
-  }
-};
+using Arena = sfg::DeviceArena;
 
 template <typename F>
 int32_t Guard(F&& fn) {
@@ -73,76 +47,7 @@ void SelectDevice(int device) {
   SFG_CUDA(cudaSetDevice(device));
 }
 
-// Device plan of one LDL^T (shared by both standalone solvers).
-struct Plan {
-  sfg::Symbolic sym;
-  sfg::TaskPlan tp;
-  sfg::FactorDev f{};
-  void *F = nullptr, *ycon = nullptr, *ysave = nullptr, *xperm = nullptr;
-  int nflags = 0, grid_factor = 1, grid_solve = 1;
-};
-
-void MakePlan(Arena& A, Plan& p, const sfg::BlockPattern& pat, int ordering, int* err,
-              const sfg::LmState* st, int num_sms) {
-  p.sym = sfg::Analyze(pat, ordering);
-  p.tp = sfg::PlanTasks(p.sym, 16);
-  const auto& S = p.sym;
-  const auto& T = p.tp;
-  sfg::FactorDev& f = p.f;
-  f.ns = S.ns;
-  f.ntasks = int(T.tasks.size());
-  f.tile = T.tile;
-  f.tasks = A.Upload(T.tasks);
-  f.sn_w = A.Upload(S.sn_w);
-  f.sn_m = A.Upload(S.sn_m);
-  f.sn_foff = A.Upload(S.sn_foff);
-  f.tile_base = A.Upload(T.tile_base);
-  f.npiv = A.Upload(T.npiv);
-  f.ntiles = A.Upload(T.ntiles);
-  f.asm_off = A.Upload(S.asm_off);
-  std::vector<sfg::AsmDev> asms(S.asms.size());
-  for (size_t q = 0; q < S.asms.size(); ++q) {
-    const auto& a = S.asms[q];
-    asms[q] = sfg::AsmDev{a.src, 0, a.row0, a.col0, a.di, a.dj, a.transpose, a.diag};
-  }
-  f.asms = A.Upload(asms);
-  f.rel_off = A.Upload(S.rel_off);
-  f.rel = A.Upload(S.rel);
-  std::vector<int32_t> cptr(S.ns + 1, 0), clist;
-  for (int s = 0; s < S.ns; ++s) {
-    for (int c : S.sn_children[s]) clist.push_back(c);
-    cptr[s + 1] = int32_t(clist.size());
-  }
-  f.child_ptr = A.Upload(cptr);
-  f.child_list = A.Upload(clist);
-  f.parent = A.Upload(S.sn_parent);
-  f.idx_off = A.Upload(S.idx_off);
-  f.idx = A.Upload(S.idx);
-  std::vector<int32_t> scalar_old(S.n);
-  for (int q = 0; q < S.nb; ++q) {
-    const int old = S.border[q];
-    for (int t = 0; t < pat.dim[old]; ++t) scalar_old[S.pstart[q] + t] = int32_t(pat.off[old] + t);
-  }
-  f.scalar_old = A.Upload(scalar_old);
-  f.tile_state = A.Zeros<int>(T.nstates);
-  f.counters = A.Zeros<int>(2);
-  p.nflags = 2 * S.ns;
-  f.front_flags = A.Zeros<int>(p.nflags);
-  f.error = err;
-  int maxm = 1;
-  for (int s = 0; s < S.ns; ++s) maxm = std::max(maxm, S.sn_m[s]);
-  f.max_m = maxm;
-  f.st = st;
-  f.a_stride = 0;
-  f.b_stride = 0;
-  p.F = A.Alloc(size_t(S.front_pool) * sizeof(double));
-  p.ycon = A.Alloc(size_t(std::max<int64_t>(S.rel_off[S.ns], 1)) * sizeof(double));
-  p.ysave = A.Alloc(size_t(std::max<int64_t>(S.idx_off[S.ns], 1)) * sizeof(double));
-  p.xperm = A.Alloc(size_t(std::max<int64_t>(S.n, 1)) * sizeof(double));
-  p.grid_factor = std::max(1, std::min(f.ntasks, num_sms * 8));
-  p.grid_solve = std::max(1, std::min(2 * S.ns, num_sms * 8));
-  sfg::ConfigureSolve<double>(maxm);
-}
+using Plan = sfg::FactorPlan;
 
 void CheckError(const sfg::LmState* st) {
   int e = 0;
@@ -233,7 +138,8 @@ int32_t sfg_ldlt_create(int32_t n, const int32_t* col_ptr, const int32_t* row_id
     s->st = MakeState(s->A);
     int sms = 0;
     SFG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    MakePlan(s->A, s->plan, s->pat, ordering, &s->st->device_error, s->st, sms);
+    sfg::BuildFactorPlan(s->A, s->plan, s->pat, ordering, 8, &s->st->device_error, s->st, 0, 0, sms,
+                         false);
     s->vals = s->A.Zeros<double>(size_t(s->pat.nvals()));
     s->b = s->A.Zeros<double>(size_t(n));
     s->x = s->A.Zeros<double>(size_t(n));
@@ -249,10 +155,7 @@ int32_t sfg_ldlt_factorize(sfg_ldlt* s, const double* values) {
     std::vector<double> v(s->pat.nvals(), 0.0);
     for (size_t q = 0; q < s->csc_to_val.size(); ++q) v[s->csc_to_val[q]] += values[q];
     SFG_CUDA(cudaMemcpy(s->vals, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice));
-    const Plan& p = s->plan;
-    sfg::LaunchResetFactorState(p.f.tile_state, p.tp.nstates, p.f.front_flags, p.nflags,
-                                p.f.counters, s->stream);
-    sfg::LaunchFactor<double>(p.f, s->vals, nullptr, p.F, p.grid_factor, s->stream);
+    sfg::EnqueueFactor<double>(s->plan, s->vals, nullptr, s->stream);
     SFG_CUDA(cudaStreamSynchronize(s->stream));
     SFG_CUDA(cudaGetLastError());
     CheckError(s->st);
@@ -269,8 +172,7 @@ int32_t sfg_ldlt_solve(sfg_ldlt* s, const double* b, double* x, int32_t nrhs) {
     for (int r = 0; r < nrhs; ++r) {
       SFG_CUDA(cudaMemcpyAsync(s->b, b + size_t(r) * s->n, sizeof(double) * s->n, cudaMemcpyHostToDevice,
                                s->stream));
-      sfg::LaunchResetFactorState(p.f.tile_state, 0, p.f.front_flags, p.nflags, p.f.counters, s->stream);
-      sfg::LaunchSolve<double>(p.f, p.F, s->b, p.ycon, p.ysave, p.xperm, s->x, p.grid_solve, s->stream);
+      sfg::EnqueueSolve<double>(p, s->b, s->x, s->stream);
       SFG_CUDA(cudaMemcpyAsync(x + size_t(r) * s->n, s->x, sizeof(double) * s->n, cudaMemcpyDeviceToHost,
                                s->stream));
       SFG_CUDA(cudaStreamSynchronize(s->stream));
@@ -390,7 +292,8 @@ int32_t sfg_schur_create(int32_t n, const int32_t* col_ptr, const int32_t* row_i
     s->update = A.Zeros<double>(size_t(n));
     int sms = 0;
     SFG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    MakePlan(A, s->plan, S.Spat, SFG_ORDERING_NESTED_DISSECTION, &s->st->device_error, s->st, sms);
+    sfg::BuildFactorPlan(A, s->plan, S.Spat, SFG_ORDERING_NESTED_DISSECTION, 8, &s->st->device_error,
+                         s->st, 0, 0, sms, false);
   });
   if (rc == SFG_OK) *out = s.release();
   return rc;
@@ -408,9 +311,7 @@ int32_t sfg_schur_factorize(sfg_schur* s, const double* values) {
     sfg::LaunchSchurPoints<double>(s->sd, s->hess, s->rhs, s->L.nvals, s->n, s->damping, s->cinv, s->W,
                                    s->tp, s->st, st);
     sfg::LaunchSchurBuildS<double>(s->sd, s->hess, s->L.nvals, s->damping, s->W, s->S, s->st, st);
-    const Plan& p = s->plan;
-    sfg::LaunchResetFactorState(p.f.tile_state, p.tp.nstates, p.f.front_flags, p.nflags, p.f.counters, st);
-    sfg::LaunchFactor<double>(p.f, s->S, nullptr, p.F, p.grid_factor, st);
+    sfg::EnqueueFactor<double>(s->plan, s->S, nullptr, st);
     SFG_CUDA(cudaStreamSynchronize(st));
     SFG_CUDA(cudaGetLastError());
     CheckError(s->st);
@@ -431,8 +332,7 @@ int32_t sfg_schur_solve(sfg_schur* s, const double* b, double* x, int32_t nrhs) 
       sfg::LaunchSchurPoints<double>(s->sd, s->hess, s->rhs, s->L.nvals, s->n, s->damping, s->cinv, s->W,
                                      s->tp, s->st, st);
       sfg::LaunchSchurRhs<double>(s->sd, s->hess, s->L.nvals, s->rhs, s->n, s->tp, s->v, s->st, st);
-      sfg::LaunchResetFactorState(p.f.tile_state, 0, p.f.front_flags, p.nflags, p.f.counters, st);
-      sfg::LaunchSolve<double>(p.f, p.F, s->v, p.ycon, p.ysave, p.xperm, s->y, p.grid_solve, st);
+      sfg::EnqueueSolve<double>(p, s->v, s->y, st);
       sfg::LaunchSchurBackSub<double>(s->sd, s->y, s->W, s->tp, s->update, st);
       SFG_CUDA(cudaMemcpyAsync(u.data(), s->update, sizeof(double) * s->n, cudaMemcpyDeviceToHost, st));
       SFG_CUDA(cudaStreamSynchronize(st));

@@ -131,6 +131,7 @@ struct Symbolic {
     int16_t di, dj;      // stored block dims (rows, cols) as stored
     int16_t transpose;   // 1: place block^T (stored block is above the diagonal after ordering)
     int16_t diag;        // 1: diagonal block (lower triangle only)
+    int32_t oi, oj;      // original block row / column
   };
   std::vector<int64_t> asm_off;        // [ns + 1]
   std::vector<Asm> asms;
@@ -146,8 +147,11 @@ struct TaskPlan {
   std::vector<int32_t> tile_base;   // [ns + 1] first tile-state index of each front
   std::vector<int32_t> ntiles;      // tiles per front dimension
   std::vector<int32_t> npiv;        // pivot tiles per front
-  std::vector<int4> tasks;          // {type, front, i, j | k<<16}
+  std::vector<int4> tasks;          // {type, front, i << 16 | j, k}
   int32_t nstates = 0;
+  std::vector<int32_t> asm_col_base;  // [ns + 1]
+  std::vector<int64_t> asm_col_off;   // per (front, tile column)
+  std::vector<int32_t> asm_col_list;
 };
 TaskPlan PlanTasks(const Symbolic& sym, int tile);
 

@@ -1,0 +1,65 @@
+// Device-side resources shared by the optimizer handle and the standalone solvers: a simple
+// device allocation arena and the device copy of a multifrontal factorization plan.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "kernels.h"
+
+namespace sfg {
+
+struct DeviceArena {
+  std::vector<void*> ptrs;
+  DeviceArena() = default;
+  DeviceArena(const DeviceArena&) = delete;
+  DeviceArena& operator=(const DeviceArena&) = delete;
+  ~DeviceArena() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  void* Alloc(size_t bytes);
+  template <typename T>
+  T* Upload(const std::vector<T>& v) {
+    T* p = static_cast<T*>(Alloc(v.size() * sizeof(T)));
+    if (!v.empty()) SFG_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return p;
+  }
+  template <typename T>
+  T* Zeros(size_t n) {
+    if (n == 0) n = 1;
+    T* p = static_cast<T*>(Alloc(n * sizeof(T)));
+    SFG_CUDA(cudaMemset(p, 0, n * sizeof(T)));
+    return p;
+  }
+};
+
+// Device copy of a symbolic factorization and its task plan, plus the numeric buffers.
+struct FactorPlan {
+  Symbolic sym;
+  TaskPlan plan;
+  FactorDev f{};
+  int grid_factor = 1, grid_solve = 1;
+  size_t elem = 8;
+  void* F = nullptr;       // front pool
+  void* Linv = nullptr;    // inverses of the diagonal tiles
+  void* ycon = nullptr;
+  void* ysave = nullptr;
+  void* xperm = nullptr;
+  int nflags = 0;
+};
+
+// Analyze `pat` with the given ordering and upload everything the factor / solve kernels need.
+// `damping_by_scalar`: diagonal entries get damping[original scalar index] added at assembly.
+void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, int ordering,
+                     size_t elem, int* error_word, const LmState* st, int64_t a_stride,
+                     int64_t b_stride, int num_sms, bool trace);
+
+template <typename T>
+void EnqueueFactor(const FactorPlan& fp, const void* A, const double* damping, cudaStream_t s);
+template <typename T>
+void EnqueueSolve(const FactorPlan& fp, const void* b, void* x, cudaStream_t s);
+
+}  // namespace sfg

@@ -589,6 +589,8 @@ Symbolic Analyze(const BlockPattern& A, int ordering) {
       a.dj = int16_t(A.dim[oj]);
       a.transpose = int16_t(ni < nj ? 1 : 0);
       a.diag = int16_t(oi == oj ? 1 : 0);
+      a.oi = oi;
+      a.oj = oj;
       asml[q].push_back(a);
     }
   S.asm_off.assign(ns + 1, 0);
@@ -621,9 +623,33 @@ TaskPlan PlanTasks(const Symbolic& sym, int tile) {
     T.tile_base[s + 1] = T.tile_base[s] + nt * (nt + 1) / 2;
   }
   T.nstates = T.tile_base[sym.ns];
+  // assembly entries per (front, tile column)
+  T.asm_col_base.assign(sym.ns + 1, 0);
+  for (int s = 0; s < sym.ns; ++s) T.asm_col_base[s + 1] = T.asm_col_base[s] + T.ntiles[s];
+  std::vector<std::vector<int32_t>> percol(T.asm_col_base[sym.ns]);
+  for (int s = 0; s < sym.ns; ++s) {
+    const int np = T.npiv[s], w = sym.sn_w[s], m = sym.sn_m[s];
+    auto col_tile = [&](int c) { return c < w ? c / tile : np + (c - w) / tile; };
+    (void)m;
+    for (int64_t a = sym.asm_off[s]; a < sym.asm_off[s + 1]; ++a) {
+      const auto& as = sym.asms[a];
+      const int ncols = as.transpose ? as.di : as.dj;
+      int last = -1;
+      for (int c = as.col0; c < as.col0 + ncols; ++c) {
+        const int t = col_tile(c);
+        if (t != last) percol[T.asm_col_base[s] + t].push_back(int32_t(a));
+        last = t;
+      }
+    }
+  }
+  T.asm_col_off.assign(percol.size() + 1, 0);
+  for (size_t q = 0; q < percol.size(); ++q) {
+    T.asm_col_off[q + 1] = T.asm_col_off[q] + int64_t(percol[q].size());
+    T.asm_col_list.insert(T.asm_col_list.end(), percol[q].begin(), percol[q].end());
+  }
   for (int s = 0; s < sym.ns; ++s) {
     const int nt = T.ntiles[s], np = T.npiv[s];
-    T.tasks.push_back(make_int4(kTaskAssemble, s, 0, 0));
+    for (int j = 0; j < nt; ++j) T.tasks.push_back(make_int4(kTaskAssemble, s, j, 0));
     for (int k = 0; k < np; ++k) {
       T.tasks.push_back(make_int4(kTaskDiag, s, k * 65536 + k, k));
       for (int i = k + 1; i < nt; ++i) T.tasks.push_back(make_int4(kTaskTrsm, s, i * 65536 + k, k));

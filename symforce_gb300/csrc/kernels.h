@@ -62,16 +62,17 @@ void LaunchLinearDelta(const double* update, const void* rhs, const double* damp
 int DeltaPartials();
 
 // The end of LevenbergMarquardtSolver::Iterate: stats record, accept / reject, lambda update,
-// best tracking, state-index juggling, early exit; sets the graph's loop condition.
+// best tracking, state-index juggling, early exit; sets the graph's loop condition when use_cond
+// (launched inside the optimize graph) and only the state's done flag otherwise.
 void LaunchDecide(const LmParams* p, LmState* st, sfg_iteration_t* records, const double* update,
                   double* last_update, int64_t N, const double* delta_partials, int nparts,
-                  cudaGraphConditionalHandle h, cudaStream_t s);
+                  cudaGraphConditionalHandle h, int use_cond, cudaStream_t s);
 // Start of an optimize call: Reset + the first half of the first Iterate (Step).
 void LaunchBegin(const LmParams* p, LmState* st, int reset_indices, cudaStream_t s);
 // After the Init block has been linearized for the first time: initial record and the
 // non-finite check (INITIAL_ERROR_NOT_FINITE).
 void LaunchFirstRecord(const LmParams* p, LmState* st, sfg_iteration_t* records,
-                       cudaGraphConditionalHandle h, cudaStream_t s);
+                       cudaGraphConditionalHandle h, int use_cond, cudaStream_t s);
 void LaunchCopyValues(const double* src, double* values, int64_t S, const LmState* st, int which,
                       cudaStream_t s);
 void LaunchCopyBest(const double* values, double* dst, int64_t S, const LmState* st, cudaStream_t s);
@@ -116,13 +117,6 @@ template <typename T>
 void LaunchSchurBackSub(const SchurDev& d, const void* y, const void* W, const void* tp,
                         double* update, cudaStream_t s);
 
-struct AsmDev {
-  int64_t src;          // block value offset
-  int64_t dscal;        // original scalar offset of the block row (diagonal blocks: damping)
-  int32_t row0, col0;
-  int16_t di, dj, transpose, diag;
-};
-
 struct FactorDev {
   int ns, ntasks, tile;
   const int4* tasks;
@@ -132,8 +126,18 @@ struct FactorDev {
   const int32_t* tile_base;
   const int32_t* npiv;
   const int32_t* ntiles;
-  const int64_t* asm_off;
-  const AsmDev* asms;
+  // assembly, flattened per (front, tile column) slot; slot = col_base[front] + tile column
+  const int32_t* col_base;       // [ns + 1]
+  const int64_t* a_ptr;          // [nslots + 1] original entries of each slot
+  const int64_t* a_src;          // value index in the assembled matrix
+  const int32_t* a_dst;          // position inside the front (row + col * m)
+  const int32_t* a_damp;         // scalar index into the damping vector, or -1
+  const int64_t* e_rptr;         // [nslots + 1] rounds of child update entries of each slot
+  const int64_t* e_round;        // round boundaries (entry indices), one past per slot's last
+  const int64_t* e_src;          // absolute index into the front pool (child update entry)
+  const int32_t* e_dst;          // position inside the front
+  const int64_t* linv_base;      // [ns] offset of the front's pivot-tile inverses
+  unsigned long long* trace;     // optional per-task timestamps (null: off)
   const int64_t* rel_off;
   const int32_t* rel;
   const int32_t* child_ptr;
@@ -152,7 +156,7 @@ struct FactorDev {
   int64_t b_stride;           // per-state-block stride of the rhs (0: fixed)
 };
 template <typename T>
-void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F,
+void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F, void* Linv,
                   int grid, cudaStream_t s);
 // Solve (L D L^T) x = b for b in the original scalar order; x in the original order.
 template <typename T>

@@ -170,7 +170,7 @@ __global__ void BeginKernel(const LmParams* p, LmState* st, int reset_indices) {
 // First Iterate after relinearizing Init: SetBestToInit, the iteration -1 record, and the
 // INITIAL_ERROR_NOT_FINITE check (symforce/opt/levenberg_marquardt_solver.tcc:151-186).
 __global__ void FirstRecordKernel(const LmParams* p, LmState* st, sfg_iteration_t* rec,
-                                  cudaGraphConditionalHandle h) {
+                                  cudaGraphConditionalHandle h, int use_cond) {
   if (st->best_idx != st->init_idx) {
     if (st->best_idx != st->new_idx) st->free_idx = st->best_idx;
     st->best_idx = st->init_idx;
@@ -194,12 +194,13 @@ __global__ void FirstRecordKernel(const LmParams* p, LmState* st, sfg_iteration_
     st->done = 1;
     go = 0;
   }
-  cudaGraphSetConditional(h, go);
+  if (use_cond) cudaGraphSetConditional(h, go);
 }
 
 __global__ void DecideKernel(const LmParams* p, LmState* st, sfg_iteration_t* records,
                              const double* update, double* last_update, int64_t N,
-                             const double* partials, int nparts, cudaGraphConditionalHandle h) {
+                             const double* partials, int nparts, cudaGraphConditionalHandle h,
+                             int use_cond) {
   __shared__ int s_copy;
   if (threadIdx.x == 0) {
     double sums[4] = {0, 0, 0, 0};
@@ -292,7 +293,7 @@ __global__ void DecideKernel(const LmParams* p, LmState* st, sfg_iteration_t* re
       st->new_idx = t;
       st->iteration += 1;
     }
-    cudaGraphSetConditional(h, done ? 0 : 1);
+    if (use_cond) cudaGraphSetConditional(h, done ? 0 : 1);
     s_copy = (accept && p->enable_bold_updates) ? 1 : 0;
   }
   __syncthreads();
@@ -343,9 +344,9 @@ void LaunchLinearDelta(const double* update, const void* rhs, const double* damp
 
 void LaunchDecide(const LmParams* p, LmState* st, sfg_iteration_t* records, const double* update,
                   double* last_update, int64_t N, const double* delta_partials, int nparts,
-                  cudaGraphConditionalHandle h, cudaStream_t s) {
+                  cudaGraphConditionalHandle h, int use_cond, cudaStream_t s) {
   DecideKernel<<<1, 256, 0, s>>>(p, st, records, update, last_update, N, delta_partials, nparts,
-                                 h);
+                                 h, use_cond);
 }
 
 void LaunchBegin(const LmParams* p, LmState* st, int reset_indices, cudaStream_t s) {
@@ -353,8 +354,8 @@ void LaunchBegin(const LmParams* p, LmState* st, int reset_indices, cudaStream_t
 }
 
 void LaunchFirstRecord(const LmParams* p, LmState* st, sfg_iteration_t* records,
-                       cudaGraphConditionalHandle h, cudaStream_t s) {
-  FirstRecordKernel<<<1, 1, 0, s>>>(p, st, records, h);
+                       cudaGraphConditionalHandle h, int use_cond, cudaStream_t s) {
+  FirstRecordKernel<<<1, 1, 0, s>>>(p, st, records, h, use_cond);
 }
 
 void LaunchCopyValues(const double* src, double* values, int64_t S, const LmState* st, int which,

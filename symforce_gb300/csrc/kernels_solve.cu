@@ -37,10 +37,22 @@ __device__ bool WaitAtLeast(const int* addr, int v, int* err) {
       atomicExch(err, kDevSpinTimeout);
       return false;
     }
-    __nanosleep(100);
+    if (it > 64) __nanosleep(64);  // poll tightly first: most waits end within a few microseconds
   }
   __threadfence();
   return true;
+}
+
+__device__ __forceinline__ unsigned long long Clock64Global() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned SmId() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+  return r;
 }
 
 template <typename T>
@@ -207,6 +219,8 @@ __device__ __forceinline__ int TileSize(const Geom& g, int t, int tile) {
 }
 __device__ __forceinline__ int StateIdx(const Geom& g, int i, int j) { return g.base + i * (i + 1) / 2 + j; }
 
+// Shared tiles are stored transposed (column index major, row index minor) so that the lanes of a
+// warp, which walk consecutive rows, read consecutive words.
 template <typename T, int TILE>
 struct TileSmem {
   T a[TILE * TILE];
@@ -214,24 +228,59 @@ struct TileSmem {
   T d[TILE];
 };
 
+// Reciprocal for the pivot chain.  FP64 division is a long dependent instruction sequence on this
+// GPU (FP64 issues at a small fraction of the FP32 rate), so doubles use the Newton-Raphson
+// iteration y <- y + y (1 - x y) from an FP32 seed: two steps take the seed's ~24 correct bits to
+// full double precision (the error squares at each step).
+template <typename T>
+__device__ __forceinline__ T PivotReciprocal(T x) { return T(1) / x; }
+template <>
+__device__ __forceinline__ double PivotReciprocal<double>(double x) {
+  const float xf = float(x);
+  if (!(fabsf(xf) > 1e-30f && fabsf(xf) < 1e30f)) return 1.0 / x;  // seed out of FP32 range
+  double y = double(1.0f / xf);
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+
 // Broadcast of thread 0's wait result.
-__device__ __forceinline__ bool CtaWait(bool ok_thread0, int* s_flag) {
+__device__ __forceinline__ bool CtaWait(bool ok_thread0, int* s_flag,
+                                        unsigned long long* ready = nullptr) {
   if (threadIdx.x == 0) *s_flag = ok_thread0 ? 1 : 0;
+  if (threadIdx.x == 0 && ready) *ready = Clock64Global();
   __syncthreads();
   const bool ok = *s_flag != 0;
   __syncthreads();
   return ok;
 }
 
+// Publish a tile version: the CTA barrier orders every thread's writes before thread 0's fence,
+// and the fence (cumulative) before the flag store that other CTAs acquire.
 __device__ __forceinline__ void Signal(int* addr, int v) {
-  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) atomicExch(addr, v);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicExch(addr, v);
+  }
 }
 
+// Load a b_r x b_c tile at (r0, c0) of a column-major front into smem, transposed: dst[c*TILE + r].
 template <typename T, int TILE>
-__device__ void TaskAssemble(const FactorDev& f, int s, const T* A, const double* damping, T* F,
-                             int* s_flag) {
+__device__ __forceinline__ void LoadTileT(const T* Fs, int m, int r0, int c0, int br, int bc, T* dst) {
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+    const int r = e % TILE, c = e / TILE;
+    if (r < br && c < bc) dst[c * TILE + r] = Ld(Fs + (r0 + r) + int64_t(c0 + c) * m);
+  }
+}
+
+// Assemble one tile column of a front from host-flattened lists: zero it, write the original
+// entries (+ damping on the diagonal), then add the children's update entries round by round
+// (within a round every destination is distinct).
+template <typename T, int TILE>
+__device__ void TaskAssemble(const FactorDev& f, int s, int tj, const T* A, const double* damping,
+                             T* F, int* s_flag, unsigned long long* ready) {
   const Geom g = FrontGeom(f, s);
   bool ok = true;
   if (threadIdx.x == 0) {
@@ -243,127 +292,123 @@ __device__ void TaskAssemble(const FactorDev& f, int s, const T* A, const double
           ok = WaitAtLeast(f.tile_state + StateIdx(gc, i, j), 1 + gc.np, f.error);
     }
   }
-  if (!CtaWait(ok, s_flag)) return;
+  if (!CtaWait(ok, s_flag, ready)) return;
   T* Fs = F + g.foff;
   const int m = g.m;
-  for (int64_t e = threadIdx.x; e < int64_t(m) * m; e += blockDim.x) {
-    const int r = int(e % m), c = int(e / m);
-    if (r >= c) St(Fs + e, T(0));
-  }
+  const int c0 = TileStart(g, tj, TILE), c1 = c0 + TileSize(g, tj, TILE);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int c = c0 + warp; c < c1; c += nwarp)
+    for (int r = c + lane; r < m; r += 32) St(Fs + r + int64_t(c) * m, T(0));
   __syncthreads();
-  for (int64_t a = f.asm_off[s]; a < f.asm_off[s + 1]; ++a) {
-    const AsmDev as = f.asms[a];
-    const int nent = int(as.di) * int(as.dj);
-    for (int e = threadIdx.x; e < nent; e += blockDim.x) {
-      const int r = e / as.dj, c = e - r * as.dj;
-      if (as.diag && r < c) continue;
-      T v = A[as.src + e];
-      if (as.diag && r == c && damping) v += T(damping[as.dscal + r]);
-      int64_t pos;
-      if (as.transpose) {
-        pos = int64_t(as.row0 + c) + int64_t(as.col0 + r) * m;
-      } else {
-        pos = int64_t(as.row0 + r) + int64_t(as.col0 + c) * m;
-      }
-      St(Fs + pos, v);
-    }
+  const int slot = f.col_base[s] + tj;
+  for (int64_t e = f.a_ptr[slot] + threadIdx.x; e < f.a_ptr[slot + 1]; e += blockDim.x) {
+    T v = A[f.a_src[e]];
+    const int dmp = f.a_damp[e];
+    if (dmp >= 0 && damping) v += T(damping[dmp]);
+    St(Fs + f.a_dst[e], v);
   }
-  __syncthreads();
-  for (int q = f.child_ptr[s]; q < f.child_ptr[s + 1]; ++q) {
-    const int c = f.child_list[q];
-    const Geom gc = FrontGeom(f, c);
-    const int hc = gc.m - gc.w;
-    const int32_t* rel = f.rel + f.rel_off[c];
-    const T* Fc = F + gc.foff;
-    for (int64_t e = threadIdx.x; e < int64_t(hc) * hc; e += blockDim.x) {
-      const int r = int(e % hc), cc = int(e / hc);
-      if (r < cc) continue;
-      const T u = Ld(Fc + int64_t(gc.w + r) + int64_t(gc.w + cc) * gc.m);
-      T* dst = Fs + int64_t(rel[r]) + int64_t(rel[cc]) * m;
-      St(dst, Ld(dst) + u);
-    }
+  for (int64_t rb = f.e_rptr[slot]; rb < f.e_rptr[slot + 1]; ++rb) {
     __syncthreads();
+    for (int64_t e = f.e_round[rb] + threadIdx.x; e < f.e_round[rb + 1]; e += blockDim.x) {
+      T* dst = Fs + f.e_dst[e];
+      St(dst, Ld(dst) + Ld(F + f.e_src[e]));
+    }
   }
-  __threadfence();
   __syncthreads();
-  const int ntile_states = g.nt * (g.nt + 1) / 2;
-  for (int q = threadIdx.x; q < ntile_states; q += blockDim.x) atomicExch(f.tile_state + g.base + q, 1);
+  if (threadIdx.x == 0) __threadfence();
+  __syncthreads();
+  for (int i = tj + threadIdx.x; i < g.nt; i += blockDim.x) atomicExch(f.tile_state + StateIdx(g, i, tj), 1);
 }
 
+// LDL^T of the diagonal tile, plus the explicit inverse of its unit lower factor (kept for the
+// panel solves, which then become small matrix products).
 template <typename T, int TILE>
-__device__ void TaskDiag(const FactorDev& f, int s, int k, T* F, TileSmem<T, TILE>& sm,
-                         int* s_flag) {
+__device__ void TaskDiag(const FactorDev& f, int s, int k, T* F, T* Linv, TileSmem<T, TILE>& sm,
+                         int* s_flag, unsigned long long* ready) {
   const Geom g = FrontGeom(f, s);
   bool ok = true;
   if (threadIdx.x == 0) ok = WaitAtLeast(f.tile_state + StateIdx(g, k, k), 1 + k, f.error);
-  if (!CtaWait(ok, s_flag)) return;
+  if (!CtaWait(ok, s_flag, ready)) return;
   const int b = TileSize(g, k, TILE), r0 = TileStart(g, k, TILE);
   T* Fs = F + g.foff;
-  for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
-    const int r = e % b, c = e / b;
-    if (r >= c) sm.a[r * TILE + c] = Ld(Fs + int64_t(r0 + r) + int64_t(r0 + c) * g.m);
-  }
+  T* a = sm.a;  // a[c * TILE + r] = tile(r, c), lower part
+  LoadTileT<T, TILE>(Fs, g.m, r0, r0, b, b, a);
   __syncthreads();
+  // Right-looking LDL^T in shared memory.  One thread forms each pivot's reciprocal (an FP64
+  // division is a long instruction sequence); column j is scaled during step j + 1, which does
+  // not read it.
   for (int j = 0; j < b; ++j) {
-    const T dj = sm.a[j * TILE + j];
-    const int rem = b - j - 1;
-    for (int e = threadIdx.x; e < rem * rem; e += blockDim.x) {
-      const int r = j + 1 + e % rem, c = j + 1 + e / rem;
-      if (r >= c) sm.a[r * TILE + c] -= sm.a[r * TILE + j] * sm.a[c * TILE + j] / dj;
+    if (threadIdx.x == 0) sm.d[j] = PivotReciprocal<T>(a[j * TILE + j]);
+    __syncthreads();
+    const T inv = sm.d[j];
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+      const int r = e % TILE, c = e / TILE;
+      if (c > j && r >= c && r < b) a[c * TILE + r] -= a[j * TILE + r] * (a[j * TILE + c] * inv);
+      if (j > 0 && c == j - 1 && r > c && r < b) a[c * TILE + r] *= sm.d[j - 1];
     }
     __syncthreads();
-    for (int r = j + 1 + threadIdx.x; r < b; r += blockDim.x) sm.a[r * TILE + j] /= dj;
-    __syncthreads();
   }
-  for (int e = threadIdx.x; e < b * b; e += blockDim.x) {
-    const int r = e % b, c = e / b;
-    if (r >= c) St(Fs + int64_t(r0 + r) + int64_t(r0 + c) * g.m, sm.a[r * TILE + c]);
+  // unit lower inverse, one column per thread: Li(r, c) = -sum_{q=c}^{r-1} L(r, q) Li(q, c)
+  T* li = sm.b;
+  for (int c = threadIdx.x; c < TILE; c += blockDim.x) {
+    for (int r = 0; r < TILE; ++r) li[c * TILE + r] = T(r == c ? 1 : 0);
+    if (c < b)
+      for (int r = c + 1; r < b; ++r) {
+        T acc = T(0);
+        for (int q = c; q < r; ++q) acc += a[q * TILE + r] * li[c * TILE + q];
+        li[c * TILE + r] = -acc;
+      }
+  }
+  __syncthreads();
+  T* Lk = Linv + f.linv_base[s] + int64_t(k) * TILE * TILE;
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+    const int r = e % TILE, c = e / TILE;
+    St(Lk + e, li[e]);  // stored transposed like the shared tiles
+    if (r < b && c < b && r >= c) St(Fs + (r0 + r) + int64_t(r0 + c) * g.m, a[c * TILE + r]);
   }
   Signal(f.tile_state + StateIdx(g, k, k), kFinal);
 }
 
+// Panel solve L_ik = F_ik L_kk^-T D_k^-1 as a product with the stored inverse.
 template <typename T, int TILE>
-__device__ void TaskTrsm(const FactorDev& f, int s, int i, int k, T* F, TileSmem<T, TILE>& sm,
-                         int* s_flag) {
+__device__ void TaskTrsm(const FactorDev& f, int s, int i, int k, T* F, const T* Linv,
+                         TileSmem<T, TILE>& sm, int* s_flag, unsigned long long* ready) {
   const Geom g = FrontGeom(f, s);
   bool ok = true;
   if (threadIdx.x == 0) {
     ok = WaitAtLeast(f.tile_state + StateIdx(g, k, k), kFinal, f.error) &&
          WaitAtLeast(f.tile_state + StateIdx(g, i, k), 1 + k, f.error);
   }
-  if (!CtaWait(ok, s_flag)) return;
+  if (!CtaWait(ok, s_flag, ready)) return;
   const int bk = TileSize(g, k, TILE), ck = TileStart(g, k, TILE);
   const int bi = TileSize(g, i, TILE), ri = TileStart(g, i, TILE);
   T* Fs = F + g.foff;
-  for (int e = threadIdx.x; e < bk * bk; e += blockDim.x) {
-    const int r = e % bk, c = e / bk;
-    if (r >= c) sm.a[r * TILE + c] = Ld(Fs + int64_t(ck + r) + int64_t(ck + c) * g.m);
-  }
-  for (int e = threadIdx.x; e < bi * bk; e += blockDim.x) {
-    const int r = e % bi, c = e / bi;
-    sm.b[r * TILE + c] = Ld(Fs + int64_t(ri + r) + int64_t(ck + c) * g.m);
-  }
+  LoadTileT<T, TILE>(Fs, g.m, ri, ck, bi, bk, sm.a);  // F_ik
+  const T* Lk = Linv + f.linv_base[s] + int64_t(k) * TILE * TILE;
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) sm.b[e] = Ld(Lk + e);
+  for (int c = threadIdx.x; c < bk; c += blockDim.x)
+    sm.d[c] = PivotReciprocal<T>(Ld(Fs + int64_t(ck + c) * (g.m + 1)));
   __syncthreads();
-  for (int r = threadIdx.x; r < bi; r += blockDim.x) {
-    T* row = sm.b + r * TILE;
-    for (int c = 0; c < bk; ++c) {
-      T x = row[c];
-      for (int q = 0; q < c; ++q) x -= row[q] * sm.a[c * TILE + q];
-      row[c] = x;  // W = L_ik D
-    }
-    for (int c = 0; c < bk; ++c) row[c] /= sm.a[c * TILE + c];
+  // W(r, c) = sum_{q <= c} F(r, q) Li(c, q);  Li(c, q) = b[q * TILE + c]
+  T out[TILE * TILE / 32];
+  int n = 0;
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x, ++n) {
+    const int r = e % TILE, c = e / TILE;
+    T acc = T(0);
+    for (int q = 0; q <= c && q < bk; ++q) acc += sm.a[q * TILE + r] * sm.b[q * TILE + c];
+    out[n] = acc * sm.d[c < bk ? c : 0];
   }
-  __syncthreads();
-  for (int e = threadIdx.x; e < bi * bk; e += blockDim.x) {
-    const int r = e % bi, c = e / bi;
-    St(Fs + int64_t(ri + r) + int64_t(ck + c) * g.m, sm.b[r * TILE + c]);
+  n = 0;
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x, ++n) {
+    const int r = e % TILE, c = e / TILE;
+    if (r < bi && c < bk) St(Fs + (ri + r) + int64_t(ck + c) * g.m, out[n]);
   }
   Signal(f.tile_state + StateIdx(g, i, k), kFinal);
 }
 
 template <typename T, int TILE>
 __device__ void TaskUpdate(const FactorDev& f, int s, int i, int j, int k, T* F,
-                           TileSmem<T, TILE>& sm, int* s_flag) {
+                           TileSmem<T, TILE>& sm, int* s_flag, unsigned long long* ready) {
   const Geom g = FrontGeom(f, s);
   bool ok = true;
   if (threadIdx.x == 0) {
@@ -371,69 +416,152 @@ __device__ void TaskUpdate(const FactorDev& f, int s, int i, int j, int k, T* F,
          WaitAtLeast(f.tile_state + StateIdx(g, j, k), kFinal, f.error) &&
          WaitAtLeast(f.tile_state + StateIdx(g, i, j), 1 + k, f.error);
   }
-  if (!CtaWait(ok, s_flag)) return;
+  if (!CtaWait(ok, s_flag, ready)) return;
   const int bk = TileSize(g, k, TILE), ck = TileStart(g, k, TILE);
   const int bi = TileSize(g, i, TILE), ri = TileStart(g, i, TILE);
   const int bj = TileSize(g, j, TILE), rj = TileStart(g, j, TILE);
   T* Fs = F + g.foff;
-  for (int e = threadIdx.x; e < bi * bk; e += blockDim.x) {
-    const int r = e % bi, c = e / bi;
-    sm.a[r * TILE + c] = Ld(Fs + int64_t(ri + r) + int64_t(ck + c) * g.m);
+  constexpr int kPer = TILE * TILE / kFactorThreads;
+  T cdst[kPer];
+  {
+    int n = 0;
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x, ++n) {
+      const int r = e % TILE, c = e / TILE;
+      cdst[n] = (r < bi && c < bj) ? Ld(Fs + (ri + r) + int64_t(rj + c) * g.m) : T(0);
+    }
   }
-  for (int e = threadIdx.x; e < bj * bk; e += blockDim.x) {
-    const int r = e % bj, c = e / bj;
-    sm.b[r * TILE + c] = Ld(Fs + int64_t(rj + r) + int64_t(ck + c) * g.m);
-  }
+  LoadTileT<T, TILE>(Fs, g.m, ri, ck, bi, bk, sm.a);  // L_ik
+  LoadTileT<T, TILE>(Fs, g.m, rj, ck, bj, bk, sm.b);  // L_jk
   for (int c = threadIdx.x; c < bk; c += blockDim.x) sm.d[c] = Ld(Fs + int64_t(ck + c) * (g.m + 1));
   __syncthreads();
-  for (int c = threadIdx.x; c < bk; c += blockDim.x) {
-    // scale L_jk by D once: b <- L_jk D
-    for (int r = 0; r < bj; ++r) sm.b[r * TILE + c] *= sm.d[c];
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+    const int c = e / TILE;
+    if (c < bk) sm.b[e] *= sm.d[c];  // L_jk D
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < bi * bj; e += blockDim.x) {
-    const int r = e % bi, c = e / bi;
-    if (i == j && r < c) continue;
-    T acc = T(0);
-    for (int q = 0; q < bk; ++q) acc += sm.a[r * TILE + q] * sm.b[c * TILE + q];
-    T* dst = Fs + int64_t(ri + r) + int64_t(rj + c) * g.m;
-    St(dst, Ld(dst) - acc);
+  {
+    int n = 0;
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x, ++n) {
+      const int r = e % TILE, c = e / TILE;
+      if (r >= bi || c >= bj || (i == j && r < c)) continue;
+      T acc = T(0);
+#pragma unroll 8
+      for (int q = 0; q < bk; ++q) acc += sm.a[q * TILE + r] * sm.b[q * TILE + c];
+      St(Fs + (ri + r) + int64_t(rj + c) * g.m, cdst[n] - acc);
+    }
   }
   Signal(f.tile_state + StateIdx(g, i, j), 2 + k);
 }
 
 template <typename T, int TILE>
 __global__ void __launch_bounds__(kFactorThreads) FactorKernel(FactorDev f, const T* A,
-                                                               const double* damping, T* F) {
+                                                               const double* damping, T* F,
+                                                               T* Linv) {
   __shared__ TileSmem<T, TILE> sm;
+  __shared__ int s_task, s_next, s_ok, s_flag;
   A += int64_t(f.st->init_idx) * f.a_stride;
-  __shared__ int s_task, s_ok, s_flag;
+  if (threadIdx.x == 0) s_next = atomicAdd(f.counters, 1);
   for (;;) {
     if (threadIdx.x == 0) {
       s_ok = LoadVolatile(f.error) == 0;
-      s_task = s_ok ? atomicAdd(f.counters, 1) : f.ntasks;
+      s_task = s_ok ? s_next : f.ntasks;
+      // fetch the following task now so that the atomic's latency overlaps this task
+      if (s_task < f.ntasks) s_next = atomicAdd(f.counters, 1);
     }
     __syncthreads();
     const int t = s_task;
     if (t >= f.ntasks) return;
     const int4 task = f.tasks[t];
     const int i = task.z >> 16, j = task.z & 0xffff, k = task.w;
+    unsigned long long* ready = f.trace ? f.trace + 4 * int64_t(t) + 1 : nullptr;
+    if (f.trace && threadIdx.x == 0) {
+      f.trace[4 * int64_t(t)] = Clock64Global();
+      f.trace[4 * int64_t(t) + 3] = SmId();
+    }
     switch (task.x) {
-      case kTaskAssemble: TaskAssemble<T, TILE>(f, task.y, A, damping, F, &s_flag); break;
-      case kTaskDiag: TaskDiag<T, TILE>(f, task.y, k, F, sm, &s_flag); break;
-      case kTaskTrsm: TaskTrsm<T, TILE>(f, task.y, i, k, F, sm, &s_flag); break;
-      case kTaskUpdate: TaskUpdate<T, TILE>(f, task.y, i, j, k, F, sm, &s_flag); break;
+      case kTaskAssemble: TaskAssemble<T, TILE>(f, task.y, j, A, damping, F, &s_flag, ready); break;
+      case kTaskDiag: TaskDiag<T, TILE>(f, task.y, k, F, Linv, sm, &s_flag, ready); break;
+      case kTaskTrsm: TaskTrsm<T, TILE>(f, task.y, i, k, F, Linv, sm, &s_flag, ready); break;
+      case kTaskUpdate: TaskUpdate<T, TILE>(f, task.y, i, j, k, F, sm, &s_flag, ready); break;
       default:
         if (threadIdx.x == 0) atomicExch(f.error, kDevBadTask);
     }
     __syncthreads();
+    if (f.trace && threadIdx.x == 0) f.trace[4 * int64_t(t) + 2] = Clock64Global();
   }
 }
 
 // ---------------------------------------------------------------------------------------------
 // Triangular solves: task t < ns is the forward solve of front t (postorder), task ns + q the
-// backward solve of front ns - 1 - q (reverse postorder).  Dynamic shared memory: 2 * max_m.
+// backward solve of front ns - 1 - q (reverse postorder).  Dynamic shared memory: max_m scalars.
+// The pivot columns are processed in panels of kSolvePanel: warp 0 solves the panel's triangle
+// from registers, then every thread updates its rows with the whole panel (independent loads), so
+// a front costs one synchronization per panel rather than one per column.
 // ---------------------------------------------------------------------------------------------
+constexpr int kSolvePanel = 32;
+
+template <typename T>
+__device__ void ForwardFront(const FactorDev& f, const Geom& g, const T* Fs, T* xs) {
+  const int m = g.m;
+  const int lane = threadIdx.x & 31;
+  for (int p0 = 0; p0 < g.w; p0 += kSolvePanel) {
+    const int p1 = min(p0 + kSolvePanel, g.w);
+    if (threadIdx.x < 32) {
+      const int r = p0 + lane;
+      T lrow[kSolvePanel];
+#pragma unroll
+      for (int c = 0; c < kSolvePanel; ++c)
+        lrow[c] = (r < p1 && p0 + c < r) ? Ld(Fs + r + int64_t(p0 + c) * m) : T(0);
+      T xr = r < p1 ? xs[r] : T(0);
+#pragma unroll
+      for (int c = 0; c < kSolvePanel; ++c) {
+        const T xc = __shfl_sync(0xffffffffu, xr, c);
+        if (p0 + c < r) xr -= lrow[c] * xc;
+      }
+      if (r < p1) xs[r] = xr;
+    }
+    __syncthreads();
+    for (int r = p1 + threadIdx.x; r < m; r += blockDim.x) {
+      T acc = T(0);
+      for (int c = p0; c < p1; ++c) acc += Ld(Fs + r + int64_t(c) * m) * xs[c];
+      xs[r] -= acc;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__device__ void BackwardFront(const FactorDev& f, const Geom& g, const T* Fs, T* xs) {
+  const int m = g.m;
+  const int lane = threadIdx.x & 31;
+  const int npan = (g.w + kSolvePanel - 1) / kSolvePanel;
+  for (int pp = npan - 1; pp >= 0; --pp) {
+    const int p0 = pp * kSolvePanel, p1 = min(p0 + kSolvePanel, g.w);
+    if (threadIdx.x < 32) {
+      const int r = p0 + lane;  // row of L^T = column of L
+      T lcol[kSolvePanel];      // L[c][r] for c in (r, p1)
+#pragma unroll
+      for (int c = 0; c < kSolvePanel; ++c)
+        lcol[c] = (r < p1 && p0 + c > r && p0 + c < p1) ? Ld(Fs + (p0 + c) + int64_t(r) * m) : T(0);
+      T xr = r < p1 ? xs[r] : T(0);
+#pragma unroll
+      for (int c = kSolvePanel - 1; c >= 0; --c) {
+        const T xc = __shfl_sync(0xffffffffu, xr, c);
+        if (p0 + c > r) xr -= lcol[c] * xc;
+      }
+      if (r < p1) xs[r] = xr;
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < p0; r += blockDim.x) {
+      T acc = T(0);
+      const T* col = Fs + int64_t(r) * m;
+      for (int c = p0; c < p1; ++c) acc += Ld(col + c) * xs[c];
+      xs[r] -= acc;
+    }
+    __syncthreads();
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kFactorThreads) SolveKernel(FactorDev f, const T* F, const T* b,
                                                               T* ycon, T* ysave, T* xperm, T* x) {
@@ -471,12 +599,7 @@ __global__ void __launch_bounds__(kFactorThreads) SolveKernel(FactorDev f, const
           for (int r = threadIdx.x; r < hc; r += blockDim.x) xs[rel[r]] += Ld(ycon + f.rel_off[c] + r);
           __syncthreads();
         }
-        for (int c = 0; c < g.w; ++c) {
-          const T xc = xs[c];
-          for (int r = c + 1 + threadIdx.x; r < g.m; r += blockDim.x)
-            xs[r] -= Ld(Fs + int64_t(r) + int64_t(c) * g.m) * xc;
-          __syncthreads();
-        }
+        ForwardFront<T>(f, g, Fs, xs);
         for (int q = threadIdx.x; q < g.w; q += blockDim.x) St(ysave + f.idx_off[s] + q, xs[q]);
         for (int r = threadIdx.x; r < g.m - g.w; r += blockDim.x) St(ycon + f.rel_off[s] + r, xs[g.w + r]);
         Signal(fwd_done + s, 1);
@@ -498,15 +621,12 @@ __global__ void __launch_bounds__(kFactorThreads) SolveKernel(FactorDev f, const
         __syncthreads();
         for (int q = threadIdx.x; q < g.w; q += blockDim.x) {
           T z = Ld(ysave + f.idx_off[s] + q) / Ld(Fs + int64_t(q) * (g.m + 1));
-          for (int r = 0; r < h; ++r) z -= Ld(Fs + int64_t(g.w + r) + int64_t(q) * g.m) * xa[r];
+          const T* col = Fs + int64_t(q) * g.m + g.w;
+          for (int r = 0; r < h; ++r) z -= Ld(col + r) * xa[r];
           xs[q] = z;
         }
         __syncthreads();
-        for (int c = g.w - 1; c >= 0; --c) {
-          const T xc = xs[c];
-          for (int r = threadIdx.x; r < c; r += blockDim.x) xs[r] -= Ld(Fs + int64_t(c) + int64_t(r) * g.m) * xc;
-          __syncthreads();
-        }
+        BackwardFront<T>(f, g, Fs, xs);
         for (int q = threadIdx.x; q < g.w; q += blockDim.x) {
           St(xperm + idx[q], xs[q]);
           x[f.scalar_old[idx[q]]] = xs[q];
@@ -603,11 +723,11 @@ void LaunchSchurBackSub(const SchurDev& d, const void* y, const void* W, const v
 }
 
 template <typename T>
-void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F, int grid,
-                  cudaStream_t s) {
+void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F, void* Linv,
+                  int grid, cudaStream_t s) {
   constexpr int kTile = sizeof(T) == 8 ? 16 : 32;
   FactorKernel<T, kTile><<<grid, kFactorThreads, 0, s>>>(f, static_cast<const T*>(A), damping,
-                                                         static_cast<T*>(F));
+                                                         static_cast<T*>(F), static_cast<T*>(Linv));
 }
 
 template <typename T>
@@ -636,9 +756,9 @@ template void LaunchSchurBackSub<double>(const SchurDev&, const void*, const voi
                                          double*, cudaStream_t);
 template void LaunchSchurBackSub<float>(const SchurDev&, const void*, const void*, const void*,
                                         double*, cudaStream_t);
-template void LaunchFactor<double>(const FactorDev&, const void*, const double*, void*, int,
+template void LaunchFactor<double>(const FactorDev&, const void*, const double*, void*, void*, int,
                                    cudaStream_t);
-template void LaunchFactor<float>(const FactorDev&, const void*, const double*, void*, int,
+template void LaunchFactor<float>(const FactorDev&, const void*, const double*, void*, void*, int,
                                   cudaStream_t);
 template void LaunchSolve<double>(const FactorDev&, const void*, const void*, void*, void*, void*,
                                   void*, int, cudaStream_t);

@@ -46,6 +46,8 @@ def lib() -> C.CDLL:
         L.sfg_hessian_lower.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                         C.POINTER(C.c_int32), C.POINTER(C.c_double)]
         L.sfg_permutation.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_int64]
+        L.sfg_time_stage.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.sfg_storage_dim.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                       C.POINTER(C.c_int64)]
         L.sfg_ldlt_create.argtypes = [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
@@ -77,6 +79,8 @@ class OptimizationStats:
     best_index: int = 0
     status: int = 0
     failure_reason: int = 0
+    kernel_launches: int = 0
+    device_ms: float = 0.0
 
     @property
     def best_error(self) -> float:
@@ -119,18 +123,29 @@ class Optimizer:
         return out
 
     def optimize(self, values: np.ndarray | None = None, num_iterations: int = -1,
-                 params: A.OptimizerParams | None = None) -> tuple[np.ndarray, OptimizationStats]:
-        """Optimizer::Optimize: returns (best values, stats)."""
+                 params: A.OptimizerParams | None = None,
+                 out: np.ndarray | None = None) -> tuple[np.ndarray, OptimizationStats]:
+        """Optimizer::Optimize: returns (best values, stats).  `out` (float64, storage size), if
+        given, receives the best values (e.g. a pinned buffer)."""
         if values is not None:
             self.set_values(values)
         p = params or self.params
         cap = (p.iterations if num_iterations < 0 else num_iterations) + 1
         recs = (A.IterationC * cap)()
-        st = A.StatsC(recs, cap, 0, 0, 0, 0, 0)
+        st = A.StatsC(recs, cap, 0, 0, 0, 0, 0, 0.0)
         _check(lib().sfg_optimize(self._h, C.byref(p), num_iterations, C.byref(st)))
         stats = OptimizationStats([recs[i] for i in range(st.num_iterations)], st.best_index,
-                                  st.status, st.failure_reason)
-        return self.get_values(), stats
+                                  st.status, st.failure_reason, st.kernel_launches, st.device_ms)
+        if out is None:
+            out = np.zeros(self.storage_dim)
+        _check(lib().sfg_get_values(self._h, A.dptr(out), out.size))
+        return out, stats
+
+    def time_stage(self, stage: int, reps: int = 20) -> dict:
+        """CUDA-event time of one stage of the LM iteration (after an optimize call)."""
+        ms, by, fm = C.c_double(), C.c_double(), C.c_double()
+        _check(lib().sfg_time_stage(self._h, stage, reps, C.byref(ms), C.byref(by), C.byref(fm)))
+        return dict(ms=ms.value, bytes=by.value, fmas=fm.value)
 
     def linearize(self, values: np.ndarray | None = None):
         """Linearization at the given (or current) values: residual, rhs, error, CSC hessian_lower."""

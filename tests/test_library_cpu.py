@@ -1,0 +1,82 @@
+"""Host-side checks of the GPU library that run without a GPU: it builds, loads, exports every
+symbol include/sfgpu.h declares, reports the reference defaults, and refuses to run without a
+device (there is no CPU fallback)."""
+
+from __future__ import annotations
+
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from symforce_gb300 import _build
+from symforce_gb300 import _cabi as A
+from symforce_gb300 import synth
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _lib():
+    return C.CDLL(str(_build.build()))
+
+
+def _gpu_present() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def test_exports_every_declared_symbol():
+    header = (ROOT / "include" / "sfgpu.h").read_text()
+    declared = set(re.findall(r"\b(sfg_[a-z_]+)\s*\(", header))
+    out = subprocess.run(["nm", "-D", "--defined-only", str(_build.build())], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    assert declared, "no declarations parsed"
+    missing = declared - exported
+    assert not missing, f"declared but not exported: {sorted(missing)}"
+    L = _lib()
+    for name in declared:
+        getattr(L, name)
+
+
+def test_default_params_match_reference():
+    L = _lib()
+    p = A.OptimizerParams()
+    L.sfg_default_optimizer_params(C.byref(p))
+    ref = A.default_optimizer_params()
+    for f, _ in A.OptimizerParams._fields_:
+        assert getattr(p, f) == getattr(ref, f), f
+    assert L.sfg_abi_version() == 1
+
+
+def test_dims_tables():
+    L = _lib()
+    s, t = C.c_int32(), C.c_int32()
+    for kt, (sd, td) in A.KEY_DIMS.items():
+        assert L.sfg_key_dims(kt, C.byref(s), C.byref(t)) == 0
+        assert (s.value, t.value) == (sd, td)
+    nk, nc, rd = C.c_int32(), C.c_int32(), C.c_int32()
+    for kind, (k, c, r, _) in A.FACTOR_DIMS.items():
+        assert L.sfg_factor_dims(kind, C.byref(nk), C.byref(nc), C.byref(rd)) == 0
+        assert (nk.value, nc.value, rd.value) == (k, c, r)
+    assert L.sfg_factor_dims(99, None, None, None) == 1
+
+
+@pytest.mark.skipif(_gpu_present(), reason="checks the no-device path")
+def test_create_without_device_fails_loudly():
+    from symforce_gb300.optimizer import Optimizer, SfgError
+    p = synth.bundle_adjustment(num_cameras=4, num_points=20, num_observations=80, seed=0)
+    with pytest.raises(SfgError) as e:
+        Optimizer(p)
+    assert e.value.code == 3  # SFG_ERR_NO_DEVICE
+
+
+def test_graft_entry_build_imports():
+    import __graft_entry__ as g
+    g.build()

@@ -1,0 +1,148 @@
+"""The CPU oracle pinned against the reference's own known answers and symbolic definitions."""
+
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+import reference_cases as R
+from symforce_gb300 import _cabi as A
+from symforce_gb300 import synth
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def test_robot_2d_example_known_answers():
+    """symforce/examples/robot_2d_localization/run_localization.cc:85-96 and
+    test/symforce_examples_robot_2d_localization_test.py:48-50."""
+    r = O.optimize(R.robot_2d_localization())
+    E = R.ROBOT_2D_EXPECTED
+    assert len(r["iterations"]) == E["num_iterations"]
+    first = r["iterations"][0].new_error
+    assert E["first_error_range"][0] < first < E["first_error_range"][1]
+    assert first == pytest.approx(E["first_error_python"], rel=1e-15)
+    assert r["iterations"][r["best_index"]].new_error < E["best_error_below"]
+    assert r["status"] == A.SFG_STATUS_SUCCESS
+    np.testing.assert_allclose(r["values"].reshape(-1, 4), E["poses"], atol=1e-6)
+
+
+def test_pose_smoothing_known_answers():
+    """test/symforce_optimizer_test.cc:142-176."""
+    p = R.pose_smoothing(O.pose_smoothing_initial_values())
+    r = O.optimize(p, A.default_optimizer_params(**R.POSE_SMOOTHING_PARAMS))
+    last = r["iterations"][-1]
+    assert last.iteration == R.POSE_SMOOTHING_EXPECTED["last_iteration"]
+    lam, tol = R.POSE_SMOOTHING_EXPECTED["lambda_approx"]
+    assert last.current_lambda == pytest.approx(lam, rel=tol)
+    err, tol = R.POSE_SMOOTHING_EXPECTED["error_approx"]
+    assert last.new_error == pytest.approx(err, rel=tol)
+    assert r["status"] == A.SFG_STATUS_SUCCESS
+
+
+def test_pose_smoothing_hessian_is_jtj():
+    """H == lower(J^T J) (test/symforce_optimizer_test.cc:170-175), built from per-factor jets."""
+    p = R.pose_smoothing(O.pose_smoothing_initial_values())
+    lin = O.linearize(p)
+    N = p.tangent_dim
+    J = np.zeros((p.residual_dim, N))
+    row = 0
+    offs = np.cumsum([0] + [A.KEY_DIMS[int(t)][1] for t in p.key_types])
+    soffs = p.key_storage_offsets()
+    for b in p.batches:
+        for f in range(b.count):
+            keys = b.keys[f]
+            st = np.concatenate([p.values[soffs[k]:soffs[k + 1]] for k in keys])
+            res, Jf = O.factor_linearize(b.kind, [p.key_types[k] for k in keys], st, b.consts[f])
+            c = 0
+            for k in keys:
+                d = A.KEY_DIMS[int(p.key_types[k])][1]
+                J[row:row + len(res), offs[k]:offs[k] + d] = Jf[:, c:c + d]
+                c += d
+            row += len(res)
+    H = np.zeros((N, N))
+    for col in range(N):
+        for q in range(lin["colptr"][col], lin["colptr"][col + 1]):
+            H[lin["rowidx"][q], col] = lin["hvals"][q]
+    np.testing.assert_allclose(np.tril(H), np.tril(J.T @ J), rtol=1e-12, atol=1e-10)
+    np.testing.assert_allclose(lin["rhs"], J.T @ lin["residual"], rtol=1e-12, atol=1e-10)
+
+
+def _golden_vectors():
+    return json.loads((GOLDEN / "factor_vectors.json").read_text())["vectors"]
+
+
+@pytest.mark.parametrize("vec", _golden_vectors(), ids=lambda v: f"kind{v['kind']}")
+def test_factor_matches_symforce_symbolic(vec):
+    """Residual and tangent Jacobian against the reference's symbolic factor definitions
+    (fixtures made by tests/golden/make_symforce_factor_vectors.py)."""
+    res, J = O.factor_linearize(vec["kind"], vec["key_types"], vec["storage"], vec["consts"])
+    np.testing.assert_allclose(res, vec["residual"], rtol=1e-10, atol=1e-12)
+    Jg = np.array(vec["jacobian"])
+    np.testing.assert_allclose(J, Jg, rtol=1e-8, atol=1e-9 * max(1.0, np.abs(Jg).max()))
+
+
+def _random_spd_csc(n, density, seed):
+    rng = np.random.default_rng(seed)
+    M = rng.normal(size=(n, n)) * (rng.uniform(size=(n, n)) < density)
+    A_ = M @ M.T + n * np.eye(n)
+    L = np.tril(A_)
+    colptr, rowidx, vals = [0], [], []
+    for c in range(n):
+        rows = np.nonzero(L[:, c])[0]
+        rows = rows[rows >= c]
+        rowidx += list(rows)
+        vals += list(L[rows, c])
+        colptr.append(len(rowidx))
+    return A_, np.array(colptr, np.int64), np.array(rowidx, np.int32), np.array(vals)
+
+
+@pytest.mark.parametrize("ordering", [A.SFG_ORDERING_NATURAL, A.SFG_ORDERING_MIN_DEGREE])
+def test_ldlt_matches_dense(ordering):
+    """Random SPD systems (test/sparse_cholesky_solver_test.cc:59-131)."""
+    for seed in range(3):
+        A_, cp, ri, v = _random_spd_csc(40, 0.1, seed)
+        b = np.random.default_rng(seed + 10).normal(size=40)
+        x, D, perm = O.ldlt_solve(40, cp, ri, v, b, ordering=ordering)
+        np.testing.assert_allclose(x, np.linalg.solve(A_, b), rtol=1e-10, atol=1e-12)
+        assert sorted(perm) == list(range(40))
+
+
+def test_schur_matches_ldlt():
+    """Schur vs full LDL^T on a BA Hessian (test/sparse_schur_solver_test.cc:105-250)."""
+    p = synth.bundle_adjustment(num_cameras=5, num_points=40, num_observations=160, seed=2)
+    lin = O.linearize(p)
+    N = p.tangent_dim
+    vals = lin["hvals"].copy()
+    for c in range(N):  # damp to make it SPD
+        q = lin["colptr"][c] + np.searchsorted(lin["rowidx"][lin["colptr"][c]:lin["colptr"][c + 1]], c)
+        vals[q] += 1.0
+    b = lin["rhs"]
+    x1, _, _ = O.ldlt_solve(N, lin["colptr"], lin["rowidx"], vals, b)
+    x2 = O.schur_solve(N, lin["colptr"], lin["rowidx"], vals, 3 * p.num_schur_keys, b)
+    np.testing.assert_allclose(x2, x1, rtol=1e-8, atol=1e-10 * np.abs(x1).max())
+
+
+def test_retract_pose3_matches_reference_formula():
+    q = np.array([0.1, -0.2, 0.3, 0.9])
+    q /= np.linalg.norm(q)
+    st = np.concatenate([q, [1.0, 2.0, 3.0]])
+    d = np.array([0.01, -0.02, 0.03, 0.1, 0.2, 0.3])
+    out = O.retract(A.SFG_KEY_POSE3, st, d)
+    th = np.linalg.norm(d[:3])
+    dq = np.concatenate([np.sin(th / 2) / th * d[:3], [np.cos(th / 2)]])
+    expect = synth.quat_mul(q, dq)
+    np.testing.assert_allclose(out[:4], expect, atol=1e-14)
+    np.testing.assert_allclose(out[4:], st[4:] + d[3:], atol=1e-15)
+
+
+def test_ba_oracle_fixture_is_reproducible():
+    """The committed oracle cost of the benchmark workload is what the oracle computes now."""
+    from symforce_gb300 import workloads
+    fx = json.loads((GOLDEN / "oracle_costs.json").read_text())
+    w = workloads.get("robot2d_1000")
+    r = O.optimize(w.problem(), w.params())
+    assert r["iterations"][r["best_index"]].new_error == pytest.approx(fx["robot2d_1000"]["best_error"], rel=1e-12)
