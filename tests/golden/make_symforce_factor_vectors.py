@@ -34,6 +34,7 @@ symforce.set_symbolic_api("sympy")
 symforce.set_epsilon_to_symbol()
 import ast  # noqa: E402
 
+import mpmath  # noqa: E402
 import sympy  # noqa: E402
 
 import symforce.symbolic as sf  # noqa: E402
@@ -73,22 +74,25 @@ def rand_quat() -> list:
     return list(q)
 
 
-def _num(e, subs):
-    # inputs are substituted as exact rationals so that the 40-digit evaluation is not limited by
-    # the 53-bit precision of the float inputs
-    subs = {k: sympy.Rational(float(v)) for k, v in subs.items()}
-    v = sympy.N(sympy.sympify(e).xreplace(subs), DIGITS)
-    re, im = v.as_real_imag()
-    if abs(float(im)) > 1e-30 * max(1.0, abs(float(re))):
-        raise ValueError(f"complex value {v}")
-    return float(re)
-
-
 def evaluate(res, args, subs):
+    """Residual and tangent Jacobian at `subs`, evaluated with mpmath at DIGITS significant digits
+    (inputs converted exactly from their double values)."""
     J = jacobian_helpers.tangent_jacobians(res, args)
     Jfull = sf.Matrix.block_matrix([J]) if len(J) > 1 else J[0]
-    r = [_num(e, subs) for e in res.to_flat_list()]
-    Jv = [[_num(Jfull[i, j], subs) for j in range(Jfull.shape[1])] for i in range(Jfull.shape[0])]
+    syms = list(subs.keys())
+    mpmath.mp.dps = DIGITS
+    vals = [mpmath.mpf(float(subs[k])) for k in syms]
+    # symforce's sign helpers (symforce/internal/symbolic.py: SignNoZero, CopysignNoZero)
+    custom = {"SignNoZero": lambda x: 1 if x >= 0 else -1,
+              "CopysignNoZero": lambda x, y: abs(x) * (1 if y >= 0 else -1)}
+    mods = [custom, "mpmath"]
+    fr = sympy.lambdify(syms, sympy.Matrix(res.to_flat_list()), modules=mods)
+    Jm = sympy.Matrix([[Jfull[i, j] for j in range(Jfull.shape[1])] for i in range(Jfull.shape[0])])
+    fj = sympy.lambdify(syms, Jm, modules=mods)
+    R = fr(*vals)
+    JJ = fj(*vals)
+    r = [float(mpmath.re(R[i])) for i in range(len(res.to_flat_list()))]
+    Jv = [[float(mpmath.re(JJ[i, j])) for j in range(Jfull.shape[1])] for i in range(Jfull.shape[0])]
     return r, Jv
 
 
