@@ -256,6 +256,23 @@ int32_t sfg_schur_factorize(sfg_schur* s, const double* values);
 int32_t sfg_schur_solve(sfg_schur* s, const double* b, double* x, int32_t nrhs);
 int32_t sfg_schur_destroy(sfg_schur* s);
 
+/* -------------------------------- dense solve without allocation ----------------------------
+ * No counterpart in the reference.  Solves A x = b for a dense symmetric positive definite n x n
+ * matrix (LDL^T, unit L, no pivoting; only the lower triangle of A is read) for callers that
+ * cannot allocate device memory when they need the solve: code under an allocator that forbids
+ * cudaMalloc / cudaFree (they allocate from and may synchronize the whole device), and plugins that
+ * only receive device pointers from their host application.  A (column-major, leading dimension
+ * lda), b and x are device pointers owned by the caller; `stream` is a cudaStream_t (null: the
+ * default stream).  All working memory is a fixed set of file-scope device arrays (about 2.2 MB,
+ * held on every GPU that loads the library until the process exits): n may be at most 512, larger
+ * n is rejected with SFG_ERR_INVALID_ARGUMENT.  The call allocates nothing.  Its first call on a
+ * device looks up the arrays' device addresses (cudaGetSymbolAddress), so make that first call
+ * before any stream capture.  The call returns when the solve has finished on `stream`.  Every
+ * call shares the same arrays, so calls that overlap on the GPU (other threads, other streams)
+ * race; each call reinitializes everything it reads. */
+int32_t sfg_dense_ldlt_solve_noalloc(int32_t n, const double* A, int64_t lda, const double* b,
+                                     double* x, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

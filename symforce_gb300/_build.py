@@ -20,7 +20,8 @@ BUILD_DIR = PKG / "_build"
 LIB = OUT_DIR / "libsfgpu.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["kernels_lin.cu", "kernels_lm.cu", "kernels_solve.cu", "api.cu", "api_solvers.cu"]
+CUDA_SOURCES = ["kernels_lin.cu", "kernels_lm.cu", "kernels_solve.cu", "api.cu", "api_solvers.cu",
+                "api_noalloc.cu"]
 HOST_SOURCES = ["host_structure.cpp", "host_layout.cpp", "device_plan.cpp"]
 
 
