@@ -183,9 +183,9 @@ typedef struct sfg_form_params_t {
   int32_t ordering;       /* SFG_ORDERING_* (block level) */
   int32_t device;         /* CUDA device ordinal */
   double epsilon;         /* the Optimizer's epsilon (symforce/opt/optimizer.h:90-94); default 10 * DBL_EPSILON */
-  int32_t refine_steps;   /* MIXED: max FP64 iterative-refinement steps on the reduced system */
+  int32_t refine_steps;   /* MIXED: FP64 iterative-refinement steps per linear solve (default 2) */
   int32_t _pad;
-  double refine_tol;      /* MIXED: relative residual at which refinement stops */
+  double refine_tol;      /* reserved (0) */
 } sfg_form_params_t;
 
 typedef struct sfg_handle sfg_handle;

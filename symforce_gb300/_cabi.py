@@ -179,9 +179,9 @@ def default_form_params(**overrides) -> FormParams:
         ordering=SFG_ORDERING_NESTED_DISSECTION,
         device=0,
         epsilon=DEFAULT_EPSILON,
-        refine_steps=10,
+        refine_steps=2,
         _pad=0,
-        refine_tol=1e-12,
+        refine_tol=0.0,
     )
     for k, v in overrides.items():
         setattr(f, k, v)

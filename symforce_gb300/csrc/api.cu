@@ -84,6 +84,13 @@ struct sfg_handle {
   sfg::SchurDev sd{};
   void *cinv = nullptr, *W = nullptr, *tp = nullptr, *S = nullptr, *v = nullptr, *y = nullptr;
   void* xsol = nullptr;
+  // FP64 refinement of a low-precision solve (mixed form)
+  int refine_steps = 0;
+  sfg::SpmvDev spmv{};
+  double* ydbl = nullptr;
+  double* rres = nullptr;
+  void* rlo = nullptr;
+  void* dy = nullptr;
   // graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -127,6 +134,21 @@ void EnqueueLinearize(sfg_handle* h, int which, cudaStream_t s) {
   LaunchFinishCost(h->cost_partials, h->ncost, h->st, which, s);
 }
 
+// Mixed form: widen the low-precision solution and refine it in FP64 a fixed number of times
+// against the matrix that was factored (r = b - A y in FP64, correction solved with the factors).
+template <typename T>
+void EnqueueRefinement(sfg_handle* h, const void* A, const double* damping, const void* b,
+                       const void* x_lo, cudaStream_t s) {
+  if (sizeof(T) == 8) return;
+  const int64_t n = h->spmv.n;
+  LaunchWiden<T>(x_lo, h->ydbl, n, s);
+  for (int k = 0; k < h->refine_steps; ++k) {
+    LaunchRefineResidual<T>(h->spmv, A, damping, b, h->ydbl, h->rres, h->rlo, h->st, s);
+    EnqueueSolve<T>(h->fp, h->rlo, h->dy, s, /*fixed_b=*/true);
+    LaunchAccumulate<T>(h->dy, h->ydbl, n, s);
+  }
+}
+
 template <typename T>
 void EnqueueIterationBody(sfg_handle* h, cudaGraphConditionalHandle cond, int use_cond,
                           cudaStream_t s) {
@@ -139,11 +161,14 @@ void EnqueueIterationBody(sfg_handle* h, cudaGraphConditionalHandle cond, int us
     LaunchSchurRhs<T>(h->sd, h->hess, h->L.nvals, h->rhs, N, h->tp, h->v, h->st, s);
     EnqueueFactor<T>(h->fp, h->S, nullptr, s);
     EnqueueSolve<T>(h->fp, h->v, h->y, s);
-    LaunchSchurBackSub<T>(h->sd, h->y, h->W, h->tp, h->update, s);
+    EnqueueRefinement<T>(h, h->S, nullptr, h->v, h->y, s);
+    LaunchSchurBackSub<T>(h->sd, sizeof(T) == 8 ? h->y : h->ydbl, h->W, h->tp, h->update, s);
   } else {
     EnqueueFactor<T>(h->fp, h->hess, h->damp.damping, s);
     EnqueueSolve<T>(h->fp, h->rhs, h->xsol, s);
-    LaunchNegate<T>(h->xsol, h->update, N, s);
+    EnqueueRefinement<T>(h, h->hess, h->damp.damping, h->rhs, h->xsol, s);
+    if (sizeof(T) == 8) LaunchNegate<T>(h->xsol, h->update, N, s);
+    else LaunchNegate<double>(h->ydbl, h->update, N, s);
   }
   RetractDev r;
   r.nkeys = h->P.nkeys;
@@ -282,9 +307,10 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
   SFG_CUDA(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, fm.device));
   h->P = ParseProblem(problem);
   h->precision = fm.precision;
-  if (fm.precision == SFG_PRECISION_MIXED)
-    throw Error(SFG_ERR_INVALID_ARGUMENT, "mixed precision form is not available in this build");
-  h->elem = 8;
+  h->elem = fm.precision == SFG_PRECISION_MIXED ? 4 : 8;
+  if (fm.refine_steps < 0 || fm.refine_steps > 64)
+    throw Error(SFG_ERR_INVALID_ARGUMENT, "refine_steps must be in 0..64");
+  h->refine_steps = fm.precision == SFG_PRECISION_MIXED ? fm.refine_steps : 0;
   h->epsilon = fm.epsilon;
   h->schur = fm.linear_solver == SFG_LINEAR_SOLVER_SCHUR;
   if (h->schur && h->P.num_schur == 0)
@@ -387,10 +413,21 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
     h->v = A.Alloc(size_t(std::max<int64_t>(S.nB, 1)) * E);
     h->y = A.Alloc(size_t(std::max<int64_t>(S.nB, 1)) * E);
     BuildFactorPlan(A, h->fp, S.Spat, fm.ordering, E, err_word, h->st, 0, 0, h->num_sms, TraceOn());
+    if (h->elem == 4) h->spmv = BuildSpmv(A, S.Spat, 0, 0);
   } else {
     h->xsol = A.Alloc(size_t(P.N) * E);
     BuildFactorPlan(A, h->fp, h->L.H, fm.ordering, E, err_word, h->st, h->L.nvals, P.N, h->num_sms,
                     TraceOn());
+    if (h->elem == 4) h->spmv = BuildSpmv(A, h->L.H, h->L.nvals, P.N);
+  }
+  if (h->elem == 4) {
+    const size_t n = size_t(std::max(h->spmv.n, 1));
+    h->ydbl = A.Zeros<double>(n);
+    h->rres = A.Zeros<double>(n);
+    h->rlo = A.Alloc(n * E);
+    h->dy = A.Alloc(n * E);
+    if (!h->ydbl || !h->rres || !h->rlo || !h->dy || !h->spmv.row_ptr)
+      throw Error(SFG_ERR_OUT_OF_MEMORY, "refinement buffers were not allocated");
   }
   SFG_CUDA(cudaDeviceSynchronize());
 }
@@ -409,6 +446,7 @@ int BodyKernels(const sfg_handle* h) {
   n += 1;  // cost
   n += 1 /*damping*/ + 1 /*retract*/ + 1 /*delta*/ + 1 /*decide*/ + 3 /*reset, factor, solve*/;
   n += h->schur ? 4 /*points, S, rhs, back-substitution*/ : 1 /*negate*/;
+  if (h->elem == 4) n += 1 + 4 * h->refine_steps;  // widen; residual, reset, solve, accumulate
   return n;
 }
 
@@ -464,8 +502,8 @@ void sfg_default_form_params(sfg_form_params_t* o) {
   o->ordering = SFG_ORDERING_NESTED_DISSECTION;
   o->device = 0;
   o->epsilon = 10 * DBL_EPSILON;
-  o->refine_steps = 10;
-  o->refine_tol = 1e-12;
+  o->refine_steps = 2;
+  o->refine_tol = 0.0;
 }
 
 int32_t sfg_key_dims(int32_t key_type, int32_t* storage_dim, int32_t* tangent_dim) {
@@ -539,7 +577,10 @@ int32_t sfg_optimize(sfg_handle* h, const sfg_optimizer_params_t* params, int32_
     if (iters <= 0) throw Error(SFG_ERR_INVALID_ARGUMENT, "num_iterations must be positive");
     SFG_CUDA(cudaSetDevice(h->device));
     sfg::EnsureRecords(h, iters + 1);
-    if (!h->have_graph) sfg::BuildGraph<double>(h);
+    if (!h->have_graph) {
+      if (h->elem == 8) sfg::BuildGraph<double>(h);
+      else sfg::BuildGraph<float>(h);
+    }
     sfg::LmParams lp;
     sfg::ToLmParams(*params, iters, h->epsilon, &lp);
     SFG_CUDA(cudaMemcpyAsync(h->params, &lp, sizeof(lp), cudaMemcpyHostToDevice, h->stream));
@@ -549,7 +590,8 @@ int32_t sfg_optimize(sfg_handle* h, const sfg_optimizer_params_t* params, int32_
     SFG_CUDA(cudaEventRecord(e0, h->stream));
     const char* eager = std::getenv("SFG_EAGER");
     if (eager && eager[0] == '1') {
-      sfg::RunEager<double>(h);
+      if (h->elem == 8) sfg::RunEager<double>(h);
+      else sfg::RunEager<float>(h);
     } else {
       SFG_CUDA(cudaGraphLaunch(h->exec, h->stream));
     }
@@ -603,16 +645,25 @@ int32_t sfg_linearize(sfg_handle* h, double* residual, double* rhs, double* erro
     const int which = 2 + blk;
     cudaStream_t s = h->stream;
     sfg::LaunchCopyValues(h->values_in, h->values, h->P.S, h->st, which, s);
-    sfg::EnqueueLinearize<double>(h, which, s);
+    if (h->elem == 8) sfg::EnqueueLinearize<double>(h, which, s);
+    else sfg::EnqueueLinearize<float>(h, which, s);
     SFG_CUDA(cudaStreamSynchronize(s));
     SFG_CUDA(cudaGetLastError());
     h->last_linearized_block = blk;
     if (residual)
       SFG_CUDA(cudaMemcpy(residual, h->residual + size_t(blk) * h->P.M, sizeof(double) * h->P.M,
                           cudaMemcpyDeviceToHost));
-    if (rhs)
-      SFG_CUDA(cudaMemcpy(rhs, static_cast<double*>(h->rhs) + size_t(blk) * h->P.N,
-                          sizeof(double) * h->P.N, cudaMemcpyDeviceToHost));
+    if (rhs) {
+      if (h->elem == 8) {
+        SFG_CUDA(cudaMemcpy(rhs, static_cast<double*>(h->rhs) + size_t(blk) * h->P.N,
+                            sizeof(double) * h->P.N, cudaMemcpyDeviceToHost));
+      } else {
+        std::vector<float> tmp(h->P.N);
+        SFG_CUDA(cudaMemcpy(tmp.data(), static_cast<float*>(h->rhs) + size_t(blk) * h->P.N,
+                            sizeof(float) * h->P.N, cudaMemcpyDeviceToHost));
+        std::copy(tmp.begin(), tmp.end(), rhs);
+      }
+    }
     if (error) {
       SFG_CUDA(cudaMemcpy(&st, h->st, sizeof(st), cudaMemcpyDeviceToHost));
       *error = st.error[blk];
@@ -632,8 +683,15 @@ int32_t sfg_hessian_lower(sfg_handle* h, int64_t* nnz, int32_t* col_ptr, int32_t
       if (h->last_linearized_block < 0) throw Error(SFG_ERR_INVALID_ARGUMENT, "call sfg_linearize first");
       std::vector<double> hv(L.nvals);
       SFG_CUDA(cudaSetDevice(h->device));
-      SFG_CUDA(cudaMemcpy(hv.data(), static_cast<double*>(h->hess) + size_t(h->last_linearized_block) * L.nvals,
-                          sizeof(double) * L.nvals, cudaMemcpyDeviceToHost));
+      if (h->elem == 8) {
+        SFG_CUDA(cudaMemcpy(hv.data(), static_cast<double*>(h->hess) + size_t(h->last_linearized_block) * L.nvals,
+                            sizeof(double) * L.nvals, cudaMemcpyDeviceToHost));
+      } else {
+        std::vector<float> tmp(L.nvals);
+        SFG_CUDA(cudaMemcpy(tmp.data(), static_cast<float*>(h->hess) + size_t(h->last_linearized_block) * L.nvals,
+                            sizeof(float) * L.nvals, cudaMemcpyDeviceToHost));
+        std::copy(tmp.begin(), tmp.end(), hv.begin());
+      }
       for (size_t q = 0; q < L.csc_src.size(); ++q) values[q] = hv[L.csc_src[q]];
     }
   });
@@ -664,7 +722,10 @@ int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_pe
     std::function<void()> launch;
     switch (stage) {
       case SFG_STAGE_LINEARIZE: {
-        launch = [&] { sfg::EnqueueLinearize<double>(h, 1, s); };
+        launch = [&] {
+          if (h->elem == 8) sfg::EnqueueLinearize<double>(h, 1, s);
+          else sfg::EnqueueLinearize<float>(h, 1, s);
+        };
         int64_t consts = 0;
         for (const auto& b : P.batches) consts += int64_t(b.count) * b.nc;
         bytes = 8.0 * double(P.S + consts + P.M + int64_t(h->L.csc_rowidx.size()) + P.N);
@@ -678,11 +739,19 @@ int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_pe
         if (!h->schur) throw Error(SFG_ERR_INVALID_ARGUMENT, "handle has no Schur stage");
         const auto& S = h->SL;
         launch = [&] {
-          sfg::LaunchSchurPoints<double>(h->sd, h->hess, h->rhs, h->L.nvals, P.N, h->damp.damping,
-                                         h->cinv, h->W, h->tp, h->st, s);
-          sfg::LaunchSchurBuildS<double>(h->sd, h->hess, h->L.nvals, h->damp.damping, h->W, h->S,
-                                         h->st, s);
-          sfg::LaunchSchurRhs<double>(h->sd, h->hess, h->L.nvals, h->rhs, P.N, h->tp, h->v, h->st, s);
+          if (h->elem == 8) {
+            sfg::LaunchSchurPoints<double>(h->sd, h->hess, h->rhs, h->L.nvals, P.N, h->damp.damping,
+                                           h->cinv, h->W, h->tp, h->st, s);
+            sfg::LaunchSchurBuildS<double>(h->sd, h->hess, h->L.nvals, h->damp.damping, h->W, h->S,
+                                           h->st, s);
+            sfg::LaunchSchurRhs<double>(h->sd, h->hess, h->L.nvals, h->rhs, P.N, h->tp, h->v, h->st, s);
+          } else {
+            sfg::LaunchSchurPoints<float>(h->sd, h->hess, h->rhs, h->L.nvals, P.N, h->damp.damping,
+                                          h->cinv, h->W, h->tp, h->st, s);
+            sfg::LaunchSchurBuildS<float>(h->sd, h->hess, h->L.nvals, h->damp.damping, h->W, h->S,
+                                          h->st, s);
+            sfg::LaunchSchurRhs<float>(h->sd, h->hess, h->L.nvals, h->rhs, P.N, h->tp, h->v, h->st, s);
+          }
         };
         // read E and C blocks + rhs, write W and S; E is re-read for the rhs
         int64_t ne = 0;
@@ -697,7 +766,10 @@ int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_pe
         const sfg::FactorPlan& fp = h->fp;
         const void* A = h->schur ? h->S : h->hess;
         const double* damping = h->schur ? nullptr : h->damp.damping;
-        launch = [&, A, damping] { sfg::EnqueueFactor<double>(fp, A, damping, s); };
+        launch = [&, A, damping] {
+          if (h->elem == 8) sfg::EnqueueFactor<double>(fp, A, damping, s);
+          else sfg::EnqueueFactor<float>(fp, A, damping, s);
+        };
         bytes = 8.0 * 2.0 * double(fp.sym.front_pool);
         fma = fp.sym.flops;
         break;
@@ -706,7 +778,10 @@ int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_pe
         const sfg::FactorPlan& fp = h->fp;
         const void* b = h->schur ? h->v : h->rhs;
         void* x = h->schur ? h->y : h->xsol;
-        launch = [&, b, x] { sfg::EnqueueSolve<double>(fp, b, x, s); };
+        launch = [&, b, x] {
+          if (h->elem == 8) sfg::EnqueueSolve<double>(fp, b, x, s);
+          else sfg::EnqueueSolve<float>(fp, b, x, s);
+        };
         bytes = 8.0 * double(fp.sym.nnz_L + fp.sym.n) * 2.0;
         fma = 2.0 * double(fp.sym.nnz_L);
         break;

@@ -3,6 +3,7 @@
 #include "device_plan.h"
 
 #include <algorithm>
+#include <array>
 #include <unordered_map>
 
 namespace sfg {
@@ -154,6 +155,48 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   else ConfigureSolve<float>(maxm);
 }
 
+SpmvDev BuildSpmv(DeviceArena& A, const BlockPattern& pat, int64_t a_stride, int64_t b_stride) {
+  const int64_t n = pat.off[pat.nb];
+  std::vector<std::vector<std::array<int64_t, 4>>> rows(n);  // base, stride, len, x
+  for (int j = 0; j < pat.nb; ++j)
+    for (int64_t q = pat.colptr[j]; q < pat.colptr[j + 1]; ++q) {
+      const int i = pat.rows[q];
+      const int di = pat.dim[i], dj = pat.dim[j];
+      const int64_t b = pat.boff[q];
+      if (i == j) {
+        for (int r = 0; r < di; ++r) {
+          rows[pat.off[i] + r].push_back({b + int64_t(r) * dj, 1, r + 1, pat.off[j]});
+          if (r + 1 < di)
+            rows[pat.off[i] + r].push_back({b + int64_t(r + 1) * dj + r, dj, di - r - 1, pat.off[j] + r + 1});
+        }
+      } else {
+        for (int r = 0; r < di; ++r) rows[pat.off[i] + r].push_back({b + int64_t(r) * dj, 1, dj, pat.off[j]});
+        for (int c = 0; c < dj; ++c) rows[pat.off[j] + c].push_back({b + c, dj, di, pat.off[i]});
+      }
+    }
+  std::vector<int64_t> ptr(n + 1, 0), base;
+  std::vector<int32_t> stride, len, x;
+  for (int64_t r = 0; r < n; ++r) {
+    for (auto& sg : rows[r]) {
+      base.push_back(sg[0]);
+      stride.push_back(int32_t(sg[1]));
+      len.push_back(int32_t(sg[2]));
+      x.push_back(int32_t(sg[3]));
+    }
+    ptr[r + 1] = int64_t(base.size());
+  }
+  SpmvDev m{};
+  m.n = int(n);
+  m.row_ptr = A.Upload(ptr);
+  m.seg_base = A.Upload(base);
+  m.seg_stride = A.Upload(stride);
+  m.seg_len = A.Upload(len);
+  m.seg_x = A.Upload(x);
+  m.a_stride = a_stride;
+  m.b_stride = b_stride;
+  return m;
+}
+
 template <typename T>
 void EnqueueFactor(const FactorPlan& fp, const void* A, const double* damping, cudaStream_t s) {
   LaunchResetFactorState(fp.f.tile_state, fp.plan.nstates, fp.f.front_flags, fp.nflags,
@@ -162,14 +205,16 @@ void EnqueueFactor(const FactorPlan& fp, const void* A, const double* damping, c
 }
 
 template <typename T>
-void EnqueueSolve(const FactorPlan& fp, const void* b, void* x, cudaStream_t s) {
+void EnqueueSolve(const FactorPlan& fp, const void* b, void* x, cudaStream_t s, bool fixed_b) {
   LaunchResetFactorState(fp.f.tile_state, 0, fp.f.front_flags, fp.nflags, fp.f.counters, s);
-  LaunchSolve<T>(fp.f, fp.F, b, fp.ycon, fp.ysave, fp.xperm, x, fp.grid_solve, s);
+  FactorDev f = fp.f;
+  if (fixed_b) f.b_stride = 0;
+  LaunchSolve<T>(f, fp.F, b, fp.ycon, fp.ysave, fp.xperm, x, fp.grid_solve, s);
 }
 
 template void EnqueueFactor<double>(const FactorPlan&, const void*, const double*, cudaStream_t);
 template void EnqueueFactor<float>(const FactorPlan&, const void*, const double*, cudaStream_t);
-template void EnqueueSolve<double>(const FactorPlan&, const void*, void*, cudaStream_t);
-template void EnqueueSolve<float>(const FactorPlan&, const void*, void*, cudaStream_t);
+template void EnqueueSolve<double>(const FactorPlan&, const void*, void*, cudaStream_t, bool);
+template void EnqueueSolve<float>(const FactorPlan&, const void*, void*, cudaStream_t, bool);
 
 }  // namespace sfg

@@ -113,9 +113,29 @@ void LaunchSchurBuildS(const SchurDev& d, const void* hess, int64_t nvals, const
 template <typename T>
 void LaunchSchurRhs(const SchurDev& d, const void* hess, int64_t nvals, const void* rhs, int64_t N,
                     const void* tp, void* v, const LmState* st, cudaStream_t s);
+// y: the reduced-system solution in FP64.
 template <typename T>
 void LaunchSchurBackSub(const SchurDev& d, const void* y, const void* W, const void* tp,
                         double* update, cudaStream_t s);
+
+// Symmetric block-sparse matrix-vector product layout (per scalar row: segments of a stored block
+// row, or of a stored block column for the mirrored upper part).
+struct SpmvDev {
+  int n;
+  const int64_t* row_ptr;     // [n + 1]
+  const int64_t* seg_base;    // value offset of the segment's first entry
+  const int32_t* seg_stride;  // distance between consecutive entries (1: along a row)
+  const int32_t* seg_len;
+  const int32_t* seg_x;       // x index of the segment's first entry
+  int64_t a_stride, b_stride; // per-state-block strides of the matrix / rhs (0: fixed buffers)
+};
+template <typename T>
+void LaunchRefineResidual(const SpmvDev& m, const void* A, const double* damping, const void* b,
+                          const double* y, double* r, void* r_lo, const LmState* st, cudaStream_t s);
+template <typename T>
+void LaunchWiden(const void* x, double* y, int64_t n, cudaStream_t s);
+template <typename T>
+void LaunchAccumulate(const void* dx, double* y, int64_t n, cudaStream_t s);
 
 struct FactorDev {
   int ns, ntasks, tile;

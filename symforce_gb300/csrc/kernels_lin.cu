@@ -97,15 +97,21 @@ __global__ void __launch_bounds__(kLinBlock) LinearizeKernel(LinOut o, BatchDev 
   }
 }
 
+// One warp per shared destination: lanes stride over its staged contributions (a camera block
+// collects hundreds) and a fixed shuffle tree adds them, so the order is the same on every run.
 template <typename T>
 __global__ void ReduceStageKernel(ReduceDev r, LinOut o) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
   if (g >= r.ngroups) return;
   const int state = o.which == 0 ? o.st->init_idx : (o.which == 1 ? o.st->new_idx : o.which - 2);
   const T* stage = static_cast<const T*>(o.stage);
   T acc = T(0);
   const int64_t p1 = r.ptr[g + 1];
-  for (int64_t q = r.ptr[g]; q < p1; ++q) acc += stage[q];
+  for (int64_t q = r.ptr[g] + lane; q < p1; q += 32) acc += stage[q];
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, d);
+  if (lane != 0) return;
   const int32_t d = r.dst[g];
   if (d < o.nvals) {
     static_cast<T*>(o.hess)[int64_t(state) * o.nvals + d] = acc;
@@ -159,8 +165,8 @@ void LaunchLinearize(int kind, const LinOut& out, const BatchDev& b, cudaStream_
 template <typename T>
 void LaunchReduceStage(const ReduceDev& r, const LinOut& out, cudaStream_t s) {
   if (r.ngroups == 0) return;
-  const int threads = 128;
-  ReduceStageKernel<T><<<(r.ngroups + threads - 1) / threads, threads, 0, s>>>(r, out);
+  const int warps = 8;
+  ReduceStageKernel<T><<<(r.ngroups + warps - 1) / warps, 32 * warps, 0, s>>>(r, out);
 }
 
 void LaunchFinishCost(const double* partials, int npartials, LmState* st, int which,

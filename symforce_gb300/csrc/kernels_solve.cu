@@ -116,7 +116,9 @@ __global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_al
   }
 }
 
-// One CTA per S block, one thread per block entry, terms summed in a fixed order.
+// One CTA per S block; each warp takes block entries in turn, its lanes stride over the block's
+// terms (one FP64 dependent chain per lane is ~1/32 of the terms) and a fixed shuffle tree adds
+// the lanes, so the sum order is the same on every run.
 template <typename T>
 __global__ void SchurBuildSKernel(SchurDev d, const T* hess_all, int64_t nvals,
                                   const double* damping, const T* W, T* S, const LmState* st) {
@@ -126,16 +128,22 @@ __global__ void SchurBuildSKernel(SchurDev d, const T* hess_all, int64_t nvals,
   const int64_t hoff = d.sb_hoff[sb];
   const int diag_toff = d.sb_diag_toff[sb];
   const int64_t t0 = d.sb_ptr[sb], t1 = d.sb_ptr[sb + 1];
-  for (int ent = threadIdx.x; ent < dk * dl; ent += blockDim.x) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
+  for (int ent = warp; ent < dk * dl; ent += nwarp) {
     const int r = ent / dl, c = ent - r * dl;
-    T acc = hoff >= 0 ? H[hoff + ent] : T(0);
-    if (diag_toff >= 0 && r == c) acc += T(damping[diag_toff + r]);
-    for (int64_t t = t0; t < t1; ++t) {
+    T acc = T(0);
+    for (int64_t t = t0 + lane; t < t1; t += 32) {
       const T* E = H + d.sb_eoff[t];
       const T* Wl = W + d.sb_woff[t];
-      acc -= E[r] * Wl[c] + E[dk + r] * Wl[dl + c] + E[2 * dk + r] * Wl[2 * dl + c];
+      acc += E[r] * Wl[c] + E[dk + r] * Wl[dl + c] + E[2 * dk + r] * Wl[2 * dl + c];
     }
-    S[d.sb_soff[sb] + ent] = acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      T v = hoff >= 0 ? H[hoff + ent] : T(0);
+      if (diag_toff >= 0 && r == c) v += T(damping[diag_toff + r]);
+      S[d.sb_soff[sb] + ent] = v - acc;
+    }
   }
 }
 
@@ -162,7 +170,7 @@ __global__ void SchurRhsKernel(SchurDev d, const T* hess_all, int64_t nvals, con
 
 // Point back-substitution z_p = t_p - sum_k W_pk y_k, and update = -[y; z].
 template <typename T>
-__global__ void SchurBackSubKernel(SchurDev d, const T* y, const T* W, const T* tp,
+__global__ void SchurBackSubKernel(SchurDev d, const double* y, const T* W, const T* tp,
                                    double* update) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < d.npoints) {
@@ -171,10 +179,10 @@ __global__ void SchurBackSubKernel(SchurDev d, const T* y, const T* W, const T* 
     for (int64_t e = d.pt_eptr[p]; e < d.pt_eptr[p + 1]; ++e) {
       const int dk = d.pt_ekey_dim[e];
       const T* Wp = W + d.pt_woff[e];
-      const T* yk = y + d.pt_ekey_toff[e];
+      const double* yk = y + d.pt_ekey_toff[e];
       T s0 = T(0), s1 = T(0), s2 = T(0);
       for (int c = 0; c < dk; ++c) {
-        const T yc = yk[c];
+        const T yc = T(yk[c]);
         s0 += Wp[c] * yc;
         s1 += Wp[dk + c] * yc;
         s2 += Wp[2 * dk + c] * yc;
@@ -638,6 +646,49 @@ __global__ void __launch_bounds__(kFactorThreads) SolveKernel(FactorDev f, const
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// FP64 iterative refinement of a low-precision factorization: r = b - (A + diag(damping)) y with
+// A the matrix that was factored (block-sparse lower, used symmetrically) in its stored precision
+// and every product and sum in FP64.  One warp per scalar row; lanes take row segments in turn
+// and a fixed shuffle tree adds them.
+// ---------------------------------------------------------------------------------------------
+template <typename T>
+__global__ void RefineResidualKernel(SpmvDev m, const T* A_all, const double* damping, const T* b_all,
+                                     const double* y, double* r, T* r_lo, const LmState* st) {
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= m.n) return;
+  const T* A = A_all + int64_t(st->init_idx) * m.a_stride;
+  const T* b = b_all + int64_t(st->init_idx) * m.b_stride;
+  double acc = 0.0;
+  for (int64_t q = m.row_ptr[row] + lane; q < m.row_ptr[row + 1]; q += 32) {
+    const T* a = A + m.seg_base[q];
+    const int stride = m.seg_stride[q], n = m.seg_len[q];
+    const double* x = y + m.seg_x[q];
+    for (int c = 0; c < n; ++c) acc += double(a[int64_t(c) * stride]) * x[c];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) {
+    if (damping) acc += damping[row] * y[row];
+    const double res = double(b[row]) - acc;
+    r[row] = res;
+    r_lo[row] = T(res);
+  }
+}
+
+template <typename T>
+__global__ void WidenKernel(const T* x, double* y, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    y[i] = double(x[i]);
+}
+
+template <typename T>
+__global__ void AccumulateKernel(const T* dx, double* y, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    y[i] += double(dx[i]);
+}
+
 __global__ void ResetFactorStateKernel(int* tile_state, int nstates, int* front_flags, int nflags,
                                        int* counters) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nstates; i += gridDim.x * blockDim.x)
@@ -673,6 +724,34 @@ void LaunchNegate(const void* x, double* u, int64_t n, cudaStream_t s) {
 template void LaunchNegate<double>(const void*, double*, int64_t, cudaStream_t);
 template void LaunchNegate<float>(const void*, double*, int64_t, cudaStream_t);
 
+template <typename T>
+void LaunchRefineResidual(const SpmvDev& m, const void* A, const double* damping, const void* b,
+                          const double* y, double* r, void* r_lo, const LmState* st, cudaStream_t s) {
+  const int warps = 8;
+  RefineResidualKernel<T><<<(m.n + warps - 1) / warps, 32 * warps, 0, s>>>(
+      m, static_cast<const T*>(A), damping, static_cast<const T*>(b), y, r, static_cast<T*>(r_lo), st);
+}
+template <typename T>
+void LaunchWiden(const void* x, double* y, int64_t n, cudaStream_t s) {
+  const int threads = 256;
+  const int grid = int(std::min<int64_t>(std::max<int64_t>((n + threads - 1) / threads, 1), 1024));
+  WidenKernel<T><<<grid, threads, 0, s>>>(static_cast<const T*>(x), y, n);
+}
+template <typename T>
+void LaunchAccumulate(const void* dx, double* y, int64_t n, cudaStream_t s) {
+  const int threads = 256;
+  const int grid = int(std::min<int64_t>(std::max<int64_t>((n + threads - 1) / threads, 1), 1024));
+  AccumulateKernel<T><<<grid, threads, 0, s>>>(static_cast<const T*>(dx), y, n);
+}
+template void LaunchRefineResidual<double>(const SpmvDev&, const void*, const double*, const void*,
+                                           const double*, double*, void*, const LmState*, cudaStream_t);
+template void LaunchRefineResidual<float>(const SpmvDev&, const void*, const double*, const void*,
+                                          const double*, double*, void*, const LmState*, cudaStream_t);
+template void LaunchWiden<double>(const void*, double*, int64_t, cudaStream_t);
+template void LaunchWiden<float>(const void*, double*, int64_t, cudaStream_t);
+template void LaunchAccumulate<double>(const void*, double*, int64_t, cudaStream_t);
+template void LaunchAccumulate<float>(const void*, double*, int64_t, cudaStream_t);
+
 int FactorThreads() { return kFactorThreads; }
 
 template <typename T>
@@ -699,7 +778,7 @@ template <typename T>
 void LaunchSchurBuildS(const SchurDev& d, const void* hess, int64_t nvals, const double* damping,
                        const void* W, void* S, const LmState* st, cudaStream_t s) {
   if (d.nsblocks == 0) return;
-  SchurBuildSKernel<T><<<d.nsblocks, 96, 0, s>>>(d, static_cast<const T*>(hess), nvals, damping,
+  SchurBuildSKernel<T><<<d.nsblocks, 128, 0, s>>>(d, static_cast<const T*>(hess), nvals, damping,
                                                  static_cast<const T*>(W), static_cast<T*>(S), st);
 }
 
@@ -719,7 +798,7 @@ void LaunchSchurBackSub(const SchurDev& d, const void* y, const void* W, const v
   const int n = d.npoints + d.nB;
   const int threads = 128;
   SchurBackSubKernel<T><<<(n + threads - 1) / threads, threads, 0, s>>>(
-      d, static_cast<const T*>(y), static_cast<const T*>(W), static_cast<const T*>(tp), update);
+      d, static_cast<const double*>(y), static_cast<const T*>(W), static_cast<const T*>(tp), update);
 }
 
 template <typename T>

@@ -1,0 +1,35 @@
+"""Run a few optimize calls of a named workload, for profilers.
+
+    python -m symforce_gb300.profile_run --workload ba_50_7800 --form plain --runs 2
+
+Set SFG_EAGER=1 so that each kernel is an individual launch (profilers do not attribute kernels
+inside graphs with conditional nodes).
+"""
+
+from __future__ import annotations
+
+import argparse
+
+from . import _cabi as A
+from . import workloads
+from .optimizer import Optimizer
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="ba_50_7800")
+    ap.add_argument("--form", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--runs", type=int, default=2)
+    args = ap.parse_args()
+    w = workloads.get(args.workload)
+    p = w.problem()
+    prec = A.SFG_PRECISION_FP64 if args.form == "plain" else A.SFG_PRECISION_MIXED
+    opt = Optimizer(p, w.params(), w.form(prec))
+    for _ in range(args.runs):
+        _, stats = opt.optimize(p.values)
+        print(f"{args.workload} {args.form}: {len(stats.iterations)} records, best {stats.best_error:.10g}, "
+              f"{stats.device_ms:.3f} ms, {stats.kernel_launches} kernels", flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -21,7 +21,10 @@ class Workload:
         if self.name.startswith("ba_"):
             # the reference's bundle-adjustment example uses DYNAMIC lambda updates
             # (symforce/examples/bundle_adjustment_in_the_large/bundle_adjustment_in_the_large.cc:131-133)
-            return A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC)
+            # cap of 100 iterations: the optimizer stops at convergence (relative reduction < 1e-6),
+            # which the FP64 oracle reaches after 58 on the 50-camera workload
+            return A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC,
+                                              iterations=100)
         return A.default_optimizer_params()
 
     def form(self, precision: int = A.SFG_PRECISION_FP64) -> A.FormParams:

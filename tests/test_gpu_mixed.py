@@ -1,0 +1,53 @@
+"""The mixed-precision form (FP32 Jacobians / Hessian / Schur / factorization, FP64 cost, gain ratio
+and iterative refinement) reaches the FP64 oracle's cost within 1e-6 relative."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from symforce_gb300 import _cabi as A
+from symforce_gb300 import synth
+from symforce_gb300.optimizer import Optimizer
+
+pytestmark = pytest.mark.gpu
+
+
+def _best(r):
+    return r["iterations"][r["best_index"]].new_error
+
+
+@pytest.mark.parametrize("solver", [A.SFG_LINEAR_SOLVER_SCHUR, A.SFG_LINEAR_SOLVER_SPARSE_LDLT])
+def test_mixed_ba_reaches_oracle_cost(solver):
+    p = synth.bundle_adjustment(num_cameras=12, num_points=400, num_observations=1700, seed=4)
+    params = A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC, iterations=30)
+    ref = O.optimize(p, params)
+    opt = Optimizer(p, params, A.default_form_params(precision=A.SFG_PRECISION_MIXED, linear_solver=solver))
+    _, stats = opt.optimize(p.values)
+    best = min(r.best_error for r in stats.iterations)
+    assert best <= _best(ref) * (1 + 1e-6), (best, _best(ref))
+
+
+def test_mixed_linearization_is_fp32_accurate():
+    p = synth.bundle_adjustment(num_cameras=6, num_points=100, num_observations=400, seed=7)
+    g = Optimizer(p, form=A.default_form_params(precision=A.SFG_PRECISION_MIXED,
+                                                linear_solver=A.SFG_LINEAR_SOLVER_SCHUR)).linearize(p.values)
+    o = O.linearize(p)
+    np.testing.assert_allclose(g["residual"], o["residual"], rtol=1e-12, atol=1e-12)  # residual stays FP64
+    scale = np.abs(o["hvals"]).max()
+    np.testing.assert_allclose(g["hvals"], o["hvals"], rtol=1e-4, atol=1e-5 * scale)
+
+
+def test_mixed_converged_problems_reach_oracle_cost():
+    """Problems that converge (SUCCESS) reach the same minimum in the mixed form."""
+    import reference_cases as R
+    for p, params in [(R.robot_2d_localization(), A.default_optimizer_params()),
+                      (R.pose_smoothing(O.pose_smoothing_initial_values()),
+                       A.default_optimizer_params(**R.POSE_SMOOTHING_PARAMS))]:
+        ref = O.optimize(p, params)
+        opt = Optimizer(p, params, A.default_form_params(precision=A.SFG_PRECISION_MIXED))
+        _, stats = opt.optimize(p.values)
+        assert stats.status == A.SFG_STATUS_SUCCESS
+        best = min(r.best_error for r in stats.iterations)
+        assert best <= _best(ref) * (1 + 1e-6) + 1e-12, (p.name, best, _best(ref))
