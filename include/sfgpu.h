@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define SFG_ABI_VERSION 1
+#define SFG_ABI_VERSION 2
 
 /* ---------------------------------------------------------------------------------------------
  * Status codes.  Solver outcomes (SUCCESS / HIT_ITERATION_LIMIT / FAILED) are not errors: they are
@@ -174,7 +174,15 @@ typedef struct sfg_stats_t {
 
 /* Forms of the solver (besides the plain FP64 drop-in). */
 enum { SFG_PRECISION_FP64 = 0, SFG_PRECISION_MIXED = 1 };
-enum { SFG_LINEAR_SOLVER_SPARSE_LDLT = 0, SFG_LINEAR_SOLVER_SCHUR = 1 };
+/* PCG_BLOCK_JACOBI / PCG_LEARNED: Schur complement over the points, then preconditioned conjugate
+ * gradients on the reduced camera system with one 9 x 9 preconditioner block per camera (the keys
+ * that share a factor with each other, e.g. pose + intrinsics).  BLOCK_JACOBI uses the inverse of
+ * the reduced system's diagonal block; LEARNED corrects that block with a small network (see
+ * "learned preconditioner" below).  The exact LDL^T of the reduced system is the fallback for every
+ * solve whose FP64 relative residual |v - S y| / |v| is still above pcg_tol after pcg_max_iters
+ * iterations.  Both require problem.num_schur_keys > 0. */
+enum { SFG_LINEAR_SOLVER_SPARSE_LDLT = 0, SFG_LINEAR_SOLVER_SCHUR = 1,
+       SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI = 2, SFG_LINEAR_SOLVER_PCG_LEARNED = 3 };
 enum { SFG_ORDERING_NESTED_DISSECTION = 0, SFG_ORDERING_NATURAL = 1, SFG_ORDERING_MIN_DEGREE = 2 };
 
 typedef struct sfg_form_params_t {
@@ -184,8 +192,8 @@ typedef struct sfg_form_params_t {
   int32_t device;         /* CUDA device ordinal */
   double epsilon;         /* the Optimizer's epsilon (symforce/opt/optimizer.h:90-94); default 10 * DBL_EPSILON */
   int32_t refine_steps;   /* MIXED: FP64 iterative-refinement steps per linear solve (default 2) */
-  int32_t _pad;
-  double refine_tol;      /* reserved (0) */
+  int32_t pcg_max_iters;  /* PCG forms: iteration cap of one reduced-system solve (default 500) */
+  double pcg_tol;         /* PCG forms: FP64 relative residual target (default 1e-8) */
 } sfg_form_params_t;
 
 typedef struct sfg_handle sfg_handle;
@@ -231,6 +239,73 @@ int32_t sfg_permutation(sfg_handle* h, int32_t* perm, int64_t n);
 enum { SFG_STAGE_LINEARIZE = 0, SFG_STAGE_SCHUR = 1, SFG_STAGE_FACTOR = 2, SFG_STAGE_SOLVE = 3 };
 int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_per_launch,
                        double* algorithmic_bytes, double* fmas);
+
+/* -------------------------------- PCG forms -------------------------------------------------
+ * Statistics of the reduced-system PCG solves of the last sfg_optimize call. */
+typedef struct sfg_pcg_stats_t {
+  int32_t solves;            /* reduced-system solves */
+  int32_t fallbacks;         /* solves that missed pcg_tol and ran the exact LDL^T instead */
+  int64_t iterations;        /* PCG iterations summed over the solves */
+  int32_t max_iterations;    /* most iterations in one solve */
+  int32_t last_iterations;
+  double max_rel_residual;   /* largest final FP64 |v - S y| / |v| of a PCG solve */
+  double last_rel_residual;
+} sfg_pcg_stats_t;
+int32_t sfg_get_pcg_stats(sfg_handle* h, sfg_pcg_stats_t* out);
+/* The exact factorization as judge of a PCG step: at the values of the last accepted state and
+ * the current lambda, solve the reduced system once with PCG and once with the exact LDL^T and
+ * return |y_pcg - y_exact| / |y_exact|, the PCG iterations and its FP64 relative residual.
+ * Requires a prior sfg_optimize on a PCG-form handle. */
+int32_t sfg_pcg_step_error(sfg_handle* h, double* rel_step_error, int32_t* iterations,
+                           double* rel_residual);
+
+/* -------------------------------- learned preconditioner -------------------------------------
+ * No counterpart in the reference.  One network per camera block: input = the camera's 9 x 9
+ * reduced-system block scaled to unit diagonal (81 values, row-major), log(1 + rho_r) for its 9
+ * rows (rho_r = sum over the row's entries outside the block of S_rc^2 / (S_rr S_cc)), the number
+ * of neighbouring camera blocks / 16, and zero padding (96 inputs); two ReLU layers of 256; 45
+ * outputs z, the row-major lower triangle of a 9 x 9 factor L with L_ii = softplus(z_ii + ln(e-1))
+ * (zero outputs give L = I).  With D the block's diagonal and C C^T = D^-1/2 S_gg D^-1/2, the
+ * preconditioner block is P_g = D^-1/2 C^-T L L^T C^-1 D^-1/2 (L = I: block Jacobi).
+ * Weights are float32, packed as W1[96][256], b1[256], W2[256][256], b2[256], W3[256][45], b3[45]
+ * (row = input).
+ * A training sample is 114 floats: the 96 inputs, g_hat = C^-1 D^-1/2 v_g and
+ * x_hat = C^T D^1/2 y_g for the block's part v_g of the reduced rhs and y_g of the exact solution;
+ * its loss is |L L^T g_hat - x_hat|^2 / (|x_hat|^2 + 1e-30) (the error of P_g v_g against y_g
+ * in the S_gg norm, relative), averaged over samples. */
+#define SFG_PRECOND_BLOCK 9
+#define SFG_PRECOND_FEATURES 96
+#define SFG_PRECOND_HIDDEN 256
+#define SFG_PRECOND_OUTPUTS 45
+#define SFG_PRECOND_SAMPLE_FLOATS 114
+#define SFG_PRECOND_NET_PARAMS (96 * 256 + 256 + 256 * 256 + 256 + 256 * 45 + 45)
+int32_t sfg_set_preconditioner_weights(sfg_handle* h, const float* weights, int64_t n);
+/* Record training samples of every camera block at every LM iteration of later sfg_optimize calls
+ * (reduced system and its exact solution; any Schur-form handle), up to max_systems systems. */
+int32_t sfg_collect_samples(sfg_handle* h, int32_t max_systems);
+/* Copy the recorded samples out (count = blocks x systems recorded); cap in samples. */
+int32_t sfg_get_samples(sfg_handle* h, float* samples, int64_t cap, int64_t* count);
+typedef struct sfg_train_params_t {
+  int32_t steps;        /* optimizer steps */
+  int32_t batch;        /* samples per step (drawn without replacement, reshuffled per epoch) */
+  float lr;             /* Adam learning rate (cosine decay to lr / 10) */
+  float beta1, beta2, eps;
+  uint64_t seed;        /* shuffling seed */
+  int32_t device;
+  int32_t _pad;
+} sfg_train_params_t;
+/* Train the network on the GPU (Adam, hand-written forward / backward kernels).  weights holds the
+ * initial weights and receives the trained ones; loss_curve (optional) receives the batch loss of
+ * every step. */
+int32_t sfg_precond_train(const float* samples, int64_t n, const sfg_train_params_t* params,
+                          float* weights, float* loss_curve);
+/* Mean loss over n samples and its gradient with respect to the weights (one forward + backward on
+ * the GPU). */
+int32_t sfg_precond_loss_grad(const float* samples, int64_t n, const float* weights, double* loss,
+                              float* grad, int32_t device);
+/* Network outputs z (45 per input row of 96 features). */
+int32_t sfg_precond_infer(const float* features, int64_t n, const float* weights, float* out,
+                          int32_t device);
 
 /* -------------------------------- SparseCholeskySolver -------------------------------------
  * The LinearSolver concept on a user CSC lower matrix (symforce/opt/sparse_cholesky/

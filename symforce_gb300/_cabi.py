@@ -43,6 +43,14 @@ FACTOR_DIMS = {  # num_keys, num_consts, residual_dim, key types
 
 SFG_PRECISION_FP64, SFG_PRECISION_MIXED = 0, 1
 SFG_LINEAR_SOLVER_SPARSE_LDLT, SFG_LINEAR_SOLVER_SCHUR = 0, 1
+SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI, SFG_LINEAR_SOLVER_PCG_LEARNED = 2, 3
+SCHUR_SOLVERS = (SFG_LINEAR_SOLVER_SCHUR, SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI, SFG_LINEAR_SOLVER_PCG_LEARNED)
+
+# learned preconditioner network (include/sfgpu.h)
+PRECOND_BLOCK, PRECOND_FEATURES, PRECOND_HIDDEN, PRECOND_OUTPUTS = 9, 96, 256, 45
+PRECOND_SAMPLE_FLOATS = PRECOND_FEATURES + 2 * PRECOND_BLOCK
+PRECOND_NET_PARAMS = (PRECOND_FEATURES * PRECOND_HIDDEN + PRECOND_HIDDEN + PRECOND_HIDDEN * PRECOND_HIDDEN
+                      + PRECOND_HIDDEN + PRECOND_HIDDEN * PRECOND_OUTPUTS + PRECOND_OUTPUTS)
 SFG_ORDERING_NESTED_DISSECTION, SFG_ORDERING_NATURAL, SFG_ORDERING_MIN_DEGREE = 0, 1, 2
 
 DEFAULT_EPSILON = 10.0 * np.finfo(np.float64).eps  # sym::kDefaultEpsilon<double>
@@ -167,8 +175,34 @@ class FormParams(C.Structure):
         ("device", C.c_int32),
         ("epsilon", C.c_double),
         ("refine_steps", C.c_int32),
+        ("pcg_max_iters", C.c_int32),
+        ("pcg_tol", C.c_double),
+    ]
+
+
+class PcgStatsC(C.Structure):
+    _fields_ = [
+        ("solves", C.c_int32),
+        ("fallbacks", C.c_int32),
+        ("iterations", C.c_int64),
+        ("max_iterations", C.c_int32),
+        ("last_iterations", C.c_int32),
+        ("max_rel_residual", C.c_double),
+        ("last_rel_residual", C.c_double),
+    ]
+
+
+class TrainParamsC(C.Structure):
+    _fields_ = [
+        ("steps", C.c_int32),
+        ("batch", C.c_int32),
+        ("lr", C.c_float),
+        ("beta1", C.c_float),
+        ("beta2", C.c_float),
+        ("eps", C.c_float),
+        ("seed", C.c_uint64),
+        ("device", C.c_int32),
         ("_pad", C.c_int32),
-        ("refine_tol", C.c_double),
     ]
 
 
@@ -180,8 +214,8 @@ def default_form_params(**overrides) -> FormParams:
         device=0,
         epsilon=DEFAULT_EPSILON,
         refine_steps=2,
-        _pad=0,
-        refine_tol=0.0,
+        pcg_max_iters=500,
+        pcg_tol=1e-8,
     )
     for k, v in overrides.items():
         setattr(f, k, v)
@@ -196,6 +230,11 @@ def dptr(a: np.ndarray) -> C.POINTER(C.c_double):
 def iptr(a: np.ndarray) -> C.POINTER(C.c_int32):
     assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def fptr(a: np.ndarray) -> C.POINTER(C.c_float):
+    assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(C.c_float))
 
 
 def lptr(a: np.ndarray) -> C.POINTER(C.c_int64):

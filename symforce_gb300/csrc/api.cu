@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -91,6 +92,22 @@ struct sfg_handle {
   double* rres = nullptr;
   void* rlo = nullptr;
   void* dy = nullptr;
+  // PCG forms and training-sample collection
+  int pcg_mode = 0;  // 0: exact solve, 1: block-Jacobi PCG, 2: learned PCG
+  bool have_precond = false;
+  sfg::PrecondLayout PL;
+  sfg::PrecondDev pd{};
+  float* rho = nullptr;
+  float* feats = nullptr;
+  float* fac = nullptr;
+  float* zout = nullptr;
+  void* Pblk = nullptr;
+  float* net = nullptr;
+  sfg::PcgState* ps = nullptr;
+  sfg::PcgDev pcg{};
+  int pcg_grid = 1, pcg_threads = 32;
+  int collect_cap = 0;
+  float* samples = nullptr;
   // graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -138,15 +155,36 @@ void EnqueueLinearize(sfg_handle* h, int which, cudaStream_t s) {
 // against the matrix that was factored (r = b - A y in FP64, correction solved with the factors).
 template <typename T>
 void EnqueueRefinement(sfg_handle* h, const void* A, const double* damping, const void* b,
-                       const void* x_lo, cudaStream_t s) {
+                       const void* x_lo, cudaStream_t s, const int* gate = nullptr) {
   if (sizeof(T) == 8) return;
   const int64_t n = h->spmv.n;
-  LaunchWiden<T>(x_lo, h->ydbl, n, s);
+  LaunchWiden<T>(x_lo, h->ydbl, n, s, gate);
   for (int k = 0; k < h->refine_steps; ++k) {
-    LaunchRefineResidual<T>(h->spmv, A, damping, b, h->ydbl, h->rres, h->rlo, h->st, s);
-    EnqueueSolve<T>(h->fp, h->rlo, h->dy, s, /*fixed_b=*/true);
-    LaunchAccumulate<T>(h->dy, h->ydbl, n, s);
+    LaunchRefineResidual<T>(h->spmv, A, damping, b, h->ydbl, h->rres, h->rlo, h->st, s, gate);
+    EnqueueSolve<T>(h->fp, h->rlo, h->dy, s, /*fixed_b=*/true, gate);
+    LaunchAccumulate<T>(h->dy, h->ydbl, n, s, gate);
   }
+}
+
+// Preconditioner blocks of the current reduced system (features, network, assembly).
+template <typename T>
+void EnqueuePrecond(sfg_handle* h, cudaStream_t s) {
+  LaunchPrecondFeatures<T>(h->pd, h->spmv, h->S, h->rho, h->feats, h->fac, s);
+  if (h->pcg_mode == 2) LaunchMlpInfer(h->feats, kPrecondFeatures, h->pd.ng, h->net, h->zout, s);
+  LaunchPrecondAssemble<T>(h->pd.ng, h->fac, h->pcg_mode == 2 ? h->zout : nullptr, h->Pblk, s);
+}
+
+// Reduced-system solve of the PCG forms: PCG into ydbl; the exact factorization and solve (with
+// FP64 refinement in the mixed form) run only when the PCG missed its tolerance.
+template <typename T>
+void EnqueuePcgSolve(sfg_handle* h, cudaStream_t s, bool gated) {
+  EnqueuePrecond<T>(h, s);
+  SFG_CUDA(LaunchPcg<T>(h->pcg, h->pcg_grid, h->pcg_threads, s));
+  const int* gate = gated ? &h->ps->need_fallback : nullptr;
+  EnqueueFactor<T>(h->fp, h->S, nullptr, s, gate);
+  EnqueueSolve<T>(h->fp, h->v, h->y, s, false, gate);
+  if (sizeof(T) == 8) LaunchWiden<double>(h->y, h->ydbl, h->sd.nB, s, gate);
+  else EnqueueRefinement<T>(h, h->S, nullptr, h->v, h->y, s, gate);
 }
 
 template <typename T>
@@ -159,10 +197,22 @@ void EnqueueIterationBody(sfg_handle* h, cudaGraphConditionalHandle cond, int us
                          h->st, s);
     LaunchSchurBuildS<T>(h->sd, h->hess, h->L.nvals, h->damp.damping, h->W, h->S, h->st, s);
     LaunchSchurRhs<T>(h->sd, h->hess, h->L.nvals, h->rhs, N, h->tp, h->v, h->st, s);
-    EnqueueFactor<T>(h->fp, h->S, nullptr, s);
-    EnqueueSolve<T>(h->fp, h->v, h->y, s);
-    EnqueueRefinement<T>(h, h->S, nullptr, h->v, h->y, s);
-    LaunchSchurBackSub<T>(h->sd, sizeof(T) == 8 ? h->y : h->ydbl, h->W, h->tp, h->update, s);
+    const double* ysol;
+    if (h->pcg_mode) {
+      EnqueuePcgSolve<T>(h, s, /*gated=*/true);
+      ysol = h->ydbl;
+    } else {
+      EnqueueFactor<T>(h->fp, h->S, nullptr, s);
+      EnqueueSolve<T>(h->fp, h->v, h->y, s);
+      EnqueueRefinement<T>(h, h->S, nullptr, h->v, h->y, s);
+      ysol = sizeof(T) == 8 ? static_cast<const double*>(h->y) : h->ydbl;
+    }
+    if (h->collect_cap > 0) {
+      if (!h->pcg_mode) LaunchPrecondFeatures<T>(h->pd, h->spmv, h->S, h->rho, h->feats, h->fac, s);
+      LaunchCollectSamples<T>(h->pd, h->feats, h->fac, h->v, ysol, h->samples, h->collect_cap, h->ps,
+                              h->st, s);
+    }
+    LaunchSchurBackSub<T>(h->sd, ysol, h->W, h->tp, h->update, s);
   } else {
     EnqueueFactor<T>(h->fp, h->hess, h->damp.damping, s);
     EnqueueSolve<T>(h->fp, h->rhs, h->xsol, s);
@@ -206,6 +256,7 @@ void BuildGraph(sfg_handle* h) {
   // prologue: Reset, Step, relinearize Init, initial record
   LaunchCopyValues(h->values_in, h->values, h->P.S, h->st, 1, s);
   LaunchBegin(h->params, h->st, 0, s);
+  if (h->ps) LaunchPcgBegin(h->ps, s);
   EnqueueLinearize<T>(h, 0, s);
   LaunchFirstRecord(h->params, h->st, h->records, cond, 1, s);
   // conditional while node
@@ -246,6 +297,7 @@ void RunEager(sfg_handle* h) {
   cudaStream_t s = h->stream;
   LaunchCopyValues(h->values_in, h->values, h->P.S, h->st, 1, s);
   LaunchBegin(h->params, h->st, 0, s);
+  if (h->ps) LaunchPcgBegin(h->ps, s);
   EnqueueLinearize<T>(h, 0, s);
   LaunchFirstRecord(h->params, h->st, h->records, 0, 0, s);
   for (;;) {
@@ -296,6 +348,32 @@ int32_t Guard(F&& fn) {
   }
 }
 
+// Camera blocks, feature buffers and the PCG state (PCG forms, sample collection).
+void EnsurePrecond(sfg_handle* h) {
+  if (h->have_precond) return;
+  if (!h->schur) throw Error(SFG_ERR_INVALID_ARGUMENT, "camera blocks need a Schur-form handle");
+  DeviceArena& A = h->arena;
+  h->PL = BuildPrecondLayout(h->P, h->SL);
+  const PrecondLayout& L = h->PL;
+  PrecondDev& d = h->pd;
+  d.ng = L.ng;
+  d.nB = int(h->SL.nB);
+  d.gidx = A.Upload(L.gidx);
+  d.goff = A.Upload(L.goff);
+  d.degree = A.Upload(L.degree);
+  d.scalar_group = A.Upload(L.scalar_group);
+  d.sdiag_off = A.Upload(L.sdiag_off);
+  if (!h->spmv.row_ptr) h->spmv = BuildSpmv(A, h->SL.Spat, 0, 0);
+  const size_t ng = size_t(std::max(L.ng, 1));
+  h->rho = A.Zeros<float>(size_t(std::max<int64_t>(h->SL.nB, 1)));
+  h->feats = A.Zeros<float>(ng * kPrecondFeatures);
+  h->fac = A.Zeros<float>(ng * kPrecondFac);
+  h->zout = A.Zeros<float>(ng * kPrecondTri);
+  h->Pblk = A.Alloc(ng * kPrecondBlock * kPrecondBlock * h->elem);
+  if (!h->ps) h->ps = A.Zeros<PcgState>(1);
+  h->have_precond = true;
+}
+
 void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, sfg_handle* h) {
   sfg_form_params_t fm;
   sfg_default_form_params(&fm);
@@ -312,9 +390,14 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
     throw Error(SFG_ERR_INVALID_ARGUMENT, "refine_steps must be in 0..64");
   h->refine_steps = fm.precision == SFG_PRECISION_MIXED ? fm.refine_steps : 0;
   h->epsilon = fm.epsilon;
-  h->schur = fm.linear_solver == SFG_LINEAR_SOLVER_SCHUR;
+  if (fm.linear_solver < SFG_LINEAR_SOLVER_SPARSE_LDLT || fm.linear_solver > SFG_LINEAR_SOLVER_PCG_LEARNED)
+    throw Error(SFG_ERR_INVALID_ARGUMENT, "unknown linear solver");
+  h->pcg_mode = fm.linear_solver == SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI ? 1
+                : fm.linear_solver == SFG_LINEAR_SOLVER_PCG_LEARNED  ? 2
+                                                                     : 0;
+  h->schur = fm.linear_solver != SFG_LINEAR_SOLVER_SPARSE_LDLT;
   if (h->schur && h->P.num_schur == 0)
-    throw Error(SFG_ERR_INVALID_ARGUMENT, "Schur solver requires num_schur_keys > 0");
+    throw Error(SFG_ERR_INVALID_ARGUMENT, "Schur and PCG solvers require num_schur_keys > 0");
   h->L = BuildLinLayout(h->P);
   if (h->schur) h->SL = BuildSchurLayout(h->P, h->L);
   SFG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
@@ -413,7 +496,7 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
     h->v = A.Alloc(size_t(std::max<int64_t>(S.nB, 1)) * E);
     h->y = A.Alloc(size_t(std::max<int64_t>(S.nB, 1)) * E);
     BuildFactorPlan(A, h->fp, S.Spat, fm.ordering, E, err_word, h->st, 0, 0, h->num_sms, TraceOn());
-    if (h->elem == 4) h->spmv = BuildSpmv(A, S.Spat, 0, 0);
+    if (h->elem == 4 || h->pcg_mode) h->spmv = BuildSpmv(A, S.Spat, 0, 0);
   } else {
     h->xsol = A.Alloc(size_t(P.N) * E);
     BuildFactorPlan(A, h->fp, h->L.H, fm.ordering, E, err_word, h->st, h->L.nvals, P.N, h->num_sms,
@@ -428,6 +511,37 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
     h->dy = A.Alloc(n * E);
     if (!h->ydbl || !h->rres || !h->rlo || !h->dy || !h->spmv.row_ptr)
       throw Error(SFG_ERR_OUT_OF_MEMORY, "refinement buffers were not allocated");
+  }
+  if (h->pcg_mode) {
+    const int64_t nB = std::max<int64_t>(h->SL.nB, 1);
+    if (!h->ydbl) h->ydbl = A.Zeros<double>(size_t(nB));
+    EnsurePrecond(h);
+    h->net = A.Zeros<float>(kPrecondParams);  // zero weights: L = I, block Jacobi
+    PcgShape(h->pd.ng, h->num_sms, &h->pcg_grid, &h->pcg_threads);
+    if (h->pcg_grid > 1) {
+      const int cap = E == 8 ? PcgMaxResidentCtas<double>(h->pcg_threads, h->num_sms)
+                             : PcgMaxResidentCtas<float>(h->pcg_threads, h->num_sms);
+      if (h->pcg_grid > cap)
+        throw Error(SFG_ERR_STRUCTURE, "the reduced system has " + std::to_string(h->pd.ng) +
+                                           " camera blocks, more than one PCG launch can hold (" +
+                                           std::to_string(cap) + " CTAs)");
+    }
+    PcgDev& c = h->pcg;
+    c.pd = h->pd;
+    c.m = h->spmv;
+    c.S = h->S;
+    c.v = h->v;
+    c.P = h->Pblk;
+    c.y = h->ydbl;
+    c.z = A.Alloc(size_t(nB) * E);
+    c.partials = A.Zeros<double>(4 * size_t(h->pcg_grid));
+    c.bar = A.Zeros<unsigned>(2);
+    c.ps = h->ps;
+    c.err = err_word;
+    c.tol = fm.pcg_tol > 0 ? fm.pcg_tol : 1e-8;
+    c.inner_floor = E == 4 ? 1e-5 : 0.0;
+    c.max_iters = fm.pcg_max_iters > 0 ? fm.pcg_max_iters : 500;
+    c.max_outer = E == 4 ? 8 : 4;
   }
   SFG_CUDA(cudaDeviceSynchronize());
 }
@@ -447,6 +561,11 @@ int BodyKernels(const sfg_handle* h) {
   n += 1 /*damping*/ + 1 /*retract*/ + 1 /*delta*/ + 1 /*decide*/ + 3 /*reset, factor, solve*/;
   n += h->schur ? 4 /*points, S, rhs, back-substitution*/ : 1 /*negate*/;
   if (h->elem == 4) n += 1 + 4 * h->refine_steps;  // widen; residual, reset, solve, accumulate
+  if (h->pcg_mode) {
+    n += 2 /*row coupling, features*/ + (h->pcg_mode == 2 ? 1 : 0) + 1 /*assemble*/ + 1 /*PCG*/;
+    if (h->elem == 8) n += 1;  // widen of the fallback solution
+  }
+  if (h->collect_cap > 0) n += (h->pcg_mode ? 0 : 2) + 1;
   return n;
 }
 
@@ -503,7 +622,8 @@ void sfg_default_form_params(sfg_form_params_t* o) {
   o->device = 0;
   o->epsilon = 10 * DBL_EPSILON;
   o->refine_steps = 2;
-  o->refine_tol = 0.0;
+  o->pcg_max_iters = 500;
+  o->pcg_tol = 1e-8;
 }
 
 int32_t sfg_key_dims(int32_t key_type, int32_t* storage_dim, int32_t* tangent_dim) {
@@ -822,6 +942,127 @@ int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_pe
     if (ms_per_launch) *ms_per_launch = double(ms) / reps;
     if (algorithmic_bytes) *algorithmic_bytes = bytes;
     if (fmas) *fmas = fma;
+  });
+}
+
+int32_t sfg_get_pcg_stats(sfg_handle* h, sfg_pcg_stats_t* out) {
+  return Guard([&] {
+    if (!h || !out) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    if (!h->ps) return;
+    SFG_CUDA(cudaSetDevice(h->device));
+    sfg::PcgState ps;
+    SFG_CUDA(cudaMemcpy(&ps, h->ps, sizeof(ps), cudaMemcpyDeviceToHost));
+    out->solves = ps.solves;
+    out->fallbacks = ps.fallbacks;
+    out->iterations = ps.total_iterations;
+    out->max_iterations = ps.max_iterations;
+    out->last_iterations = ps.iterations;
+    out->max_rel_residual = ps.max_rel_residual;
+    out->last_rel_residual = ps.rel_residual;
+  });
+}
+
+}  // extern "C"
+
+namespace sfg {
+namespace {
+template <typename T>
+void StepError(sfg_handle* h, double* rel_step_error, int32_t* iterations, double* rel_residual) {
+  cudaStream_t s = h->stream;
+  const int64_t N = h->P.N, nB = h->SL.nB;
+  PcgState saved;
+  SFG_CUDA(cudaMemcpy(&saved, h->ps, sizeof(saved), cudaMemcpyDeviceToHost));
+  LaunchDamping<T>(h->damp, h->hess, h->L.nvals, h->params, h->st, s);
+  LaunchSchurPoints<T>(h->sd, h->hess, h->rhs, h->L.nvals, N, h->damp.damping, h->cinv, h->W, h->tp,
+                       h->st, s);
+  LaunchSchurBuildS<T>(h->sd, h->hess, h->L.nvals, h->damp.damping, h->W, h->S, h->st, s);
+  LaunchSchurRhs<T>(h->sd, h->hess, h->L.nvals, h->rhs, N, h->tp, h->v, h->st, s);
+  EnqueuePrecond<T>(h, s);
+  SFG_CUDA(LaunchPcg<T>(h->pcg, h->pcg_grid, h->pcg_threads, s));
+  std::vector<double> ypcg(nB), yex(nB);
+  SFG_CUDA(cudaMemcpyAsync(ypcg.data(), h->ydbl, nB * 8, cudaMemcpyDeviceToHost, s));
+  PcgState ps;
+  SFG_CUDA(cudaMemcpyAsync(&ps, h->ps, sizeof(ps), cudaMemcpyDeviceToHost, s));
+  SFG_CUDA(cudaStreamSynchronize(s));
+  EnqueueFactor<T>(h->fp, h->S, nullptr, s);
+  EnqueueSolve<T>(h->fp, h->v, h->y, s);
+  if (sizeof(T) == 8) LaunchWiden<double>(h->y, h->ydbl, nB, s);
+  else EnqueueRefinement<T>(h, h->S, nullptr, h->v, h->y, s);
+  SFG_CUDA(cudaMemcpyAsync(yex.data(), h->ydbl, nB * 8, cudaMemcpyDeviceToHost, s));
+  SFG_CUDA(cudaMemcpyAsync(h->ps, &saved, sizeof(saved), cudaMemcpyHostToDevice, s));
+  SFG_CUDA(cudaStreamSynchronize(s));
+  SFG_CUDA(cudaGetLastError());
+  LmState st;
+  SFG_CUDA(cudaMemcpy(&st, h->st, sizeof(st), cudaMemcpyDeviceToHost));
+  if (st.device_error) throw Error(SFG_ERR_DEVICE_STATUS, "device loop hit its cap");
+  double num = 0, den = 0;
+  for (int64_t i = 0; i < nB; ++i) {
+    num += (ypcg[i] - yex[i]) * (ypcg[i] - yex[i]);
+    den += yex[i] * yex[i];
+  }
+  if (rel_step_error) *rel_step_error = den > 0 ? std::sqrt(num / den) : std::sqrt(num);
+  if (iterations) *iterations = ps.iterations;
+  if (rel_residual) *rel_residual = ps.rel_residual;
+}
+}  // namespace
+}  // namespace sfg
+
+extern "C" {
+
+int32_t sfg_pcg_step_error(sfg_handle* h, double* rel_step_error, int32_t* iterations,
+                           double* rel_residual) {
+  return Guard([&] {
+    if (!h) throw Error(SFG_ERR_INVALID_ARGUMENT, "null handle");
+    if (!h->pcg_mode) throw Error(SFG_ERR_INVALID_ARGUMENT, "handle is not a PCG form");
+    if (!h->have_graph) throw Error(SFG_ERR_INVALID_ARGUMENT, "call sfg_optimize first");
+    SFG_CUDA(cudaSetDevice(h->device));
+    if (h->elem == 8) sfg::StepError<double>(h, rel_step_error, iterations, rel_residual);
+    else sfg::StepError<float>(h, rel_step_error, iterations, rel_residual);
+  });
+}
+
+int32_t sfg_set_preconditioner_weights(sfg_handle* h, const float* weights, int64_t n) {
+  return Guard([&] {
+    if (!h || !weights) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (n != sfg::kPrecondParams)
+      throw Error(SFG_ERR_INVALID_ARGUMENT, "expected " + std::to_string(sfg::kPrecondParams) + " weights");
+    if (h->pcg_mode != 2) throw Error(SFG_ERR_INVALID_ARGUMENT, "handle is not the learned PCG form");
+    SFG_CUDA(cudaSetDevice(h->device));
+    SFG_CUDA(cudaMemcpyAsync(h->net, weights, size_t(n) * 4, cudaMemcpyHostToDevice, h->stream));
+    SFG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+int32_t sfg_collect_samples(sfg_handle* h, int32_t max_systems) {
+  return Guard([&] {
+    if (!h) throw Error(SFG_ERR_INVALID_ARGUMENT, "null handle");
+    if (max_systems < 0) throw Error(SFG_ERR_INVALID_ARGUMENT, "max_systems must be >= 0");
+    SFG_CUDA(cudaSetDevice(h->device));
+    if (max_systems > h->collect_cap) {
+      sfg::EnsurePrecond(h);
+      h->samples = static_cast<float*>(h->arena.Alloc(size_t(max_systems) * std::max(h->pd.ng, 1) *
+                                                      sfg::kSampleFloats * 4));
+    }
+    h->collect_cap = max_systems;
+    h->have_graph = false;
+  });
+}
+
+int32_t sfg_get_samples(sfg_handle* h, float* samples, int64_t cap, int64_t* count) {
+  return Guard([&] {
+    if (!h || !count) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    *count = 0;
+    if (h->collect_cap == 0) return;
+    SFG_CUDA(cudaSetDevice(h->device));
+    sfg::LmState st;
+    SFG_CUDA(cudaMemcpy(&st, h->st, sizeof(st), cudaMemcpyDeviceToHost));
+    const int systems = std::min(std::max(st.num_records - 1, 0), h->collect_cap);
+    const int64_t n = int64_t(systems) * h->pd.ng;
+    *count = n;
+    if (!samples) return;
+    if (cap < n) throw Error(SFG_ERR_CAPACITY, "samples buffer too small");
+    SFG_CUDA(cudaMemcpy(samples, h->samples, size_t(n) * sfg::kSampleFloats * 4, cudaMemcpyDeviceToHost));
   });
 }
 

@@ -30,6 +30,20 @@ struct LmState {
   unsigned long long t_start;  // globaltimer at the start of the optimize call
 };
 
+// Outcome of the reduced-system PCG solves (PCG forms).  The per-solve fields describe the last
+// solve; need_fallback gates the exact factorization kernels that follow it.  The running totals
+// are cleared at the start of every optimize call.
+struct PcgState {
+  int need_fallback;     // 1: the last solve missed its tolerance, the exact LDL^T runs
+  int converged;
+  int iterations;        // inner iterations of the last solve
+  int outer;             // FP64 residual passes of the last solve
+  double rel_residual;   // FP64 |v - S y| / |v| after the last solve
+  long long total_iterations;
+  int solves, fallbacks, max_iterations, pad;
+  double max_rel_residual;
+};
+
 // Task kinds of the persistent factorization kernel.
 enum TaskType { kTaskAssemble = 0, kTaskDiag = 1, kTaskTrsm = 2, kTaskUpdate = 3 };
 

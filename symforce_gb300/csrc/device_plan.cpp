@@ -198,23 +198,30 @@ SpmvDev BuildSpmv(DeviceArena& A, const BlockPattern& pat, int64_t a_stride, int
 }
 
 template <typename T>
-void EnqueueFactor(const FactorPlan& fp, const void* A, const double* damping, cudaStream_t s) {
+void EnqueueFactor(const FactorPlan& fp, const void* A, const double* damping, cudaStream_t s,
+                   const int* gate) {
   LaunchResetFactorState(fp.f.tile_state, fp.plan.nstates, fp.f.front_flags, fp.nflags,
-                         fp.f.counters, s);
-  LaunchFactor<T>(fp.f, A, damping, fp.F, fp.Linv, fp.grid_factor, s);
+                         fp.f.counters, s, gate);
+  FactorDev f = fp.f;
+  f.gate = gate;
+  LaunchFactor<T>(f, A, damping, fp.F, fp.Linv, fp.grid_factor, s);
 }
 
 template <typename T>
-void EnqueueSolve(const FactorPlan& fp, const void* b, void* x, cudaStream_t s, bool fixed_b) {
-  LaunchResetFactorState(fp.f.tile_state, 0, fp.f.front_flags, fp.nflags, fp.f.counters, s);
+void EnqueueSolve(const FactorPlan& fp, const void* b, void* x, cudaStream_t s, bool fixed_b,
+                  const int* gate) {
+  LaunchResetFactorState(fp.f.tile_state, 0, fp.f.front_flags, fp.nflags, fp.f.counters, s, gate);
   FactorDev f = fp.f;
+  f.gate = gate;
   if (fixed_b) f.b_stride = 0;
   LaunchSolve<T>(f, fp.F, b, fp.ycon, fp.ysave, fp.xperm, x, fp.grid_solve, s);
 }
 
-template void EnqueueFactor<double>(const FactorPlan&, const void*, const double*, cudaStream_t);
-template void EnqueueFactor<float>(const FactorPlan&, const void*, const double*, cudaStream_t);
-template void EnqueueSolve<double>(const FactorPlan&, const void*, void*, cudaStream_t, bool);
-template void EnqueueSolve<float>(const FactorPlan&, const void*, void*, cudaStream_t, bool);
+template void EnqueueFactor<double>(const FactorPlan&, const void*, const double*, cudaStream_t,
+                                    const int*);
+template void EnqueueFactor<float>(const FactorPlan&, const void*, const double*, cudaStream_t,
+                                   const int*);
+template void EnqueueSolve<double>(const FactorPlan&, const void*, void*, cudaStream_t, bool, const int*);
+template void EnqueueSolve<float>(const FactorPlan&, const void*, void*, cudaStream_t, bool, const int*);
 
 }  // namespace sfg

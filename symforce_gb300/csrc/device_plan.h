@@ -60,11 +60,14 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
 // Per-row segments of the symmetric product with a block pattern (lower blocks stored row-major).
 SpmvDev BuildSpmv(DeviceArena& A, const BlockPattern& pat, int64_t a_stride, int64_t b_stride);
 
+// `gate` (optional): the launched kernels do nothing unless *gate != 0.
 template <typename T>
-void EnqueueFactor(const FactorPlan& fp, const void* A, const double* damping, cudaStream_t s);
+void EnqueueFactor(const FactorPlan& fp, const void* A, const double* damping, cudaStream_t s,
+                   const int* gate = nullptr);
 // b is read at the Init block's offset (b + init_idx * b_stride) unless fixed_b, which the
 // refinement's correction solves use for their single right-hand-side buffer.
 template <typename T>
-void EnqueueSolve(const FactorPlan& fp, const void* b, void* x, cudaStream_t s, bool fixed_b = false);
+void EnqueueSolve(const FactorPlan& fp, const void* b, void* x, cudaStream_t s, bool fixed_b = false,
+                  const int* gate = nullptr);
 
 }  // namespace sfg

@@ -1,0 +1,101 @@
+// Camera blocks of the reduced camera system for the PCG forms (host, once per structure).
+#include <algorithm>
+#include <numeric>
+#include <set>
+
+#include "kernels.h"
+#include "layout.h"
+
+namespace sfg {
+
+namespace {
+int Find(std::vector<int>& parent, int a) {
+  while (parent[a] != a) a = parent[a] = parent[parent[a]];
+  return a;
+}
+}  // namespace
+
+PrecondLayout BuildPrecondLayout(const HostProblem& P, const SchurLayout& SL) {
+  constexpr int kB = kPrecondBlock;
+  const int nbk = SL.nB_keys;
+  std::vector<int> parent(nbk);
+  std::iota(parent.begin(), parent.end(), 0);
+  for (const HostBatch& b : P.batches)
+    for (int f = 0; f < b.count; ++f) {
+      int first = -1;
+      for (int k = 0; k < b.nk; ++k) {
+        const int key = b.keys[size_t(f) * b.nk + k];
+        if (key >= nbk) continue;
+        if (first < 0) {
+          first = key;
+        } else {
+          const int ra = Find(parent, first), rb = Find(parent, key);
+          if (ra != rb) parent[std::max(ra, rb)] = std::min(ra, rb);
+        }
+      }
+    }
+  // blocks in order of their first key; keys inside a block in key order
+  std::vector<int> group_of_root(nbk, -1), key_group(nbk);
+  std::vector<std::vector<int>> members;
+  for (int k = 0; k < nbk; ++k) {
+    const int r = Find(parent, k);
+    if (group_of_root[r] < 0) {
+      group_of_root[r] = int(members.size());
+      members.emplace_back();
+    }
+    key_group[k] = group_of_root[r];
+    members[key_group[k]].push_back(k);
+  }
+  PrecondLayout L;
+  L.ng = int(members.size());
+  L.gidx.assign(size_t(L.ng) * kB, -1);
+  L.goff.assign(size_t(L.ng) * kB * kB, -1);
+  L.degree.assign(L.ng, 0.f);
+  L.scalar_group.assign(SL.nB, -1);
+  L.sdiag_off.assign(SL.nB, -1);
+  const BlockPattern& S = SL.Spat;
+  auto entry_offset = [&](int ka, int ta, int kb, int tb) -> int64_t {
+    if (ka < kb) {
+      std::swap(ka, kb);
+      std::swap(ta, tb);
+    }
+    const int64_t q = S.Find(ka, kb);
+    if (q < 0) return -1;
+    return S.boff[q] + int64_t(ta) * S.dim[kb] + tb;
+  };
+  for (int g = 0; g < L.ng; ++g) {
+    std::vector<std::pair<int, int>> dims;  // (key, tangent index)
+    for (int k : members[g])
+      for (int t = 0; t < S.dim[k]; ++t) dims.push_back({k, t});
+    if (int(dims.size()) > kB)
+      throw Error(SFG_ERR_STRUCTURE, "a camera block of the reduced system has " +
+                                         std::to_string(dims.size()) +
+                                         " scalars; the PCG forms support at most 9");
+    for (size_t a = 0; a < dims.size(); ++a) {
+      const int64_t s = S.off[dims[a].first] + dims[a].second;
+      L.gidx[size_t(g) * kB + a] = int32_t(s);
+      L.scalar_group[s] = g;
+      for (size_t b = 0; b < dims.size(); ++b) {
+        const int64_t o = entry_offset(dims[a].first, dims[a].second, dims[b].first, dims[b].second);
+        L.goff[(size_t(g) * kB + a) * kB + b] = o < 0 ? -2 : o;  // -2: structurally zero
+      }
+    }
+  }
+  for (int k = 0; k < nbk; ++k) {
+    const int64_t q = S.Find(k, k);
+    for (int t = 0; t < S.dim[k]; ++t) L.sdiag_off[S.off[k] + t] = S.boff[q] + int64_t(t) * S.dim[k] + t;
+  }
+  std::vector<std::set<int>> nbr(L.ng);
+  for (int j = 0; j < nbk; ++j)
+    for (int64_t q = S.colptr[j]; q < S.colptr[j + 1]; ++q) {
+      const int gi = key_group[S.rows[q]], gj = key_group[j];
+      if (gi != gj) {
+        nbr[gi].insert(gj);
+        nbr[gj].insert(gi);
+      }
+    }
+  for (int g = 0; g < L.ng; ++g) L.degree[g] = float(nbr[g].size());
+  return L;
+}
+
+}  // namespace sfg

@@ -129,13 +129,16 @@ struct SpmvDev {
   const int32_t* seg_x;       // x index of the segment's first entry
   int64_t a_stride, b_stride; // per-state-block strides of the matrix / rhs (0: fixed buffers)
 };
+// `gate` (optional): the kernels do nothing unless *gate != 0 (the PCG forms run the exact
+// solve only as a fallback).
 template <typename T>
 void LaunchRefineResidual(const SpmvDev& m, const void* A, const double* damping, const void* b,
-                          const double* y, double* r, void* r_lo, const LmState* st, cudaStream_t s);
+                          const double* y, double* r, void* r_lo, const LmState* st, cudaStream_t s,
+                          const int* gate = nullptr);
 template <typename T>
-void LaunchWiden(const void* x, double* y, int64_t n, cudaStream_t s);
+void LaunchWiden(const void* x, double* y, int64_t n, cudaStream_t s, const int* gate = nullptr);
 template <typename T>
-void LaunchAccumulate(const void* dx, double* y, int64_t n, cudaStream_t s);
+void LaunchAccumulate(const void* dx, double* y, int64_t n, cudaStream_t s, const int* gate = nullptr);
 
 struct FactorDev {
   int ns, ntasks, tile;
@@ -174,6 +177,7 @@ struct FactorDev {
   const LmState* st;          // state whose Init block the matrix / rhs are read from
   int64_t a_stride;           // per-state-block stride of the matrix values (0: fixed)
   int64_t b_stride;           // per-state-block stride of the rhs (0: fixed)
+  const int* gate;            // optional: the kernels return at once unless *gate != 0
 };
 template <typename T>
 void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F, void* Linv,
@@ -184,11 +188,92 @@ void LaunchSolve(const FactorDev& f, const void* F, const void* b, void* ycon, v
                  void* xperm, void* x, int grid, cudaStream_t s);
 int FactorThreads();
 void LaunchResetFactorState(int* tile_state, int nstates, int* front_flags, int nflags,
-                            int* counters, cudaStream_t s);
+                            int* counters, cudaStream_t s, const int* gate = nullptr);
 template <typename T>
 void LaunchNegate(const void* x, double* u, int64_t n, cudaStream_t s);
 // Opt the solve kernel into the shared memory its largest front needs (call once per device).
 template <typename T>
 void ConfigureSolve(int max_m);
+
+// ---------------------------------------------------------------- PCG forms (kernels_pcg.cu)
+constexpr int kPrecondBlock = 9;
+constexpr int kPrecondFeatures = 96;
+constexpr int kPrecondHidden = 256;
+constexpr int kPrecondTri = 45;
+constexpr int kPrecondFac = kPrecondTri + kPrecondBlock;   // C (lower, packed) + D^-1/2
+constexpr int kSampleFloats = kPrecondFeatures + 2 * kPrecondBlock;
+constexpr int kPrecondParams = kPrecondFeatures * kPrecondHidden + kPrecondHidden +
+                               kPrecondHidden * kPrecondHidden + kPrecondHidden +
+                               kPrecondHidden * kPrecondTri + kPrecondTri;
+
+// Camera blocks of the reduced system (groups of B keys that share factors).
+struct PrecondDev {
+  int ng;                       // blocks
+  int nB;                       // scalar dimension of the reduced system
+  const int32_t* gidx;          // [ng][9] reduced-system scalar of each block row, -1: padding
+  const int64_t* goff;          // [ng][81] S value offset of (a, b); -1 padding, -2 not stored
+  const float* degree;          // [ng] neighbouring blocks
+  const int32_t* scalar_group;  // [nB] block of each scalar
+  const int64_t* sdiag_off;     // [nB] S value offset of each diagonal entry
+};
+// Features of every block (and its scaled Cholesky factor); `rho` is scratch [nB].
+template <typename T>
+void LaunchPrecondFeatures(const PrecondDev& pd, const SpmvDev& m, const void* S, float* rho,
+                           float* feats, float* fac, cudaStream_t s);
+// Preconditioner blocks P_g (T, [ng][81]) from the factors and the network outputs (null: L = I).
+template <typename T>
+void LaunchPrecondAssemble(int ng, const float* fac, const float* z, void* P, cudaStream_t s);
+// Network forward pass for inference: z[n][45] from x[n][96] (row stride ldx floats).
+void LaunchMlpInfer(const float* x, int64_t ldx, int64_t n, const float* weights, float* z,
+                    cudaStream_t s);
+// Training samples of one system: [ng][114] at samples + slot * ng * 114, slot = the LM record
+// index of the iteration, skipped when slot >= max_systems.
+template <typename T>
+void LaunchCollectSamples(const PrecondDev& pd, const float* feats, const float* fac, const void* v,
+                          const double* y, float* samples, int max_systems, PcgState* ps,
+                          const LmState* st, cudaStream_t s);
+
+struct PcgDev {
+  PrecondDev pd;
+  SpmvDev m;                // symmetric rows of S
+  const void* S;            // T [nvals(S)]
+  const void* v;            // T [nB] rhs
+  const void* P;            // T [ng][81]
+  double* y;                // [nB] FP64 solution
+  void* z;                  // T [nB] preconditioned residual (read by the product)
+  double* partials;         // [2][grid][2] per-CTA partial sums (double buffered)
+  unsigned* bar;            // [2] grid barrier count / generation (zero before launch)
+  PcgState* ps;
+  int* err;                 // device error word
+  double tol;               // FP64 relative residual target
+  double inner_floor;       // smallest relative reduction asked of one inner solve
+  int max_iters, max_outer;
+};
+// Grid shape of the PCG kernel for ng blocks (cooperative when grid > 1).
+void PcgShape(int ng, int num_sms, int* grid, int* threads);
+// CTAs of the PCG kernel that fit on the device at once (a cooperative launch needs all of them).
+template <typename T>
+int PcgMaxResidentCtas(int threads, int num_sms);
+template <typename T>
+cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s);
+void LaunchPcgBegin(PcgState* ps, cudaStream_t s);
+
+// ---------------------------------------------------------------- network training (kernels_mlp.cu)
+// C[m][n] = sum_k A(m, k) B(k, n) (+ bias[n]) then ReLU, or times (mask[m][n] > 0); A(m, k) at
+// A[m * a_rs + k * a_cs], B(k, n) at B[k * b_rs + n * b_cs], C row-major with leading dim ldc.
+enum GemmEpilogue { kEpiNone = 0, kEpiBiasRelu = 1, kEpiBias = 2, kEpiMask = 3 };
+void LaunchGemm(int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs, const float* B,
+                int64_t b_rs, int64_t b_cs, float* C, int64_t ldc, int epilogue, const float* bias,
+                const float* mask, int64_t ldmask, cudaStream_t s);
+// out[n] = sum_m A[m][n] (fixed order).
+void LaunchColSum(int M, int N, const float* A, int64_t lda, float* out, cudaStream_t s);
+// Loss head: per sample (row of z, g_hat / x_hat at sample + 96 / + 105 with row stride lds)
+// the loss and d loss / d z scaled by `scale`; loss_sum receives scale * sum of the losses.
+void LaunchHead(int n, const float* z, const float* samples, int64_t lds, float scale, float* dz,
+                float* loss, double* loss_sum, cudaStream_t s);
+// rows[i] = samples[idx[i]] (kSampleFloats floats each).
+void LaunchGather(int n, const float* samples, const int32_t* idx, float* rows, cudaStream_t s);
+void LaunchAdam(int64_t n, float* w, const float* g, float* m, float* v, float lr, float beta1,
+                float beta2, float eps, float c1, float c2, cudaStream_t s);
 
 }  // namespace sfg

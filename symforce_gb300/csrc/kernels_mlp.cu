@@ -1,0 +1,220 @@
+// Training kernels of the camera-block preconditioner network: a tiled FP32 GEMM with fused
+// bias / ReLU / ReLU-mask epilogues, column sums for bias gradients, the loss head (factor L from
+// the outputs, P = L L^T applied to g_hat against x_hat) with its analytic gradient, batch gather
+// and Adam.  Every reduction runs in a fixed order, so training is bit-reproducible.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "kernels.h"
+
+namespace sfg {
+
+namespace {
+
+constexpr int kTileM = 64, kTileN = 64, kTileK = 16;
+constexpr float kDiagShift = 0.54132485f;  // ln(e - 1)
+
+__device__ __forceinline__ int Tri(int i, int j) { return i * (i + 1) / 2 + j; }
+
+__global__ void __launch_bounds__(256) GemmKernel(int M, int N, int K, const float* A, int64_t a_rs,
+                                                  int64_t a_cs, const float* B, int64_t b_rs,
+                                                  int64_t b_cs, float* C, int64_t ldc, int epi,
+                                                  const float* bias, const float* mask,
+                                                  int64_t ldmask) {
+  __shared__ float As[kTileK][kTileM + 4];
+  __shared__ float Bs[kTileK][kTileN + 4];
+  const int tid = threadIdx.x;
+  const int ty = tid / 16, tx = tid % 16;
+  const int m0 = blockIdx.y * kTileM, n0 = blockIdx.x * kTileN;
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += kTileK) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int idx = tid + e * 256;  // 0..1023
+      // A tile: 64 rows x 16 k
+      const int am = idx / kTileK, ak = idx % kTileK;
+      const int gm = m0 + am, gk = k0 + ak;
+      As[ak][am] = (gm < M && gk < K) ? A[int64_t(gm) * a_rs + int64_t(gk) * a_cs] : 0.f;
+      // B tile: 16 k x 64 cols
+      const int bk = idx / kTileN, bn = idx % kTileN;
+      const int gk2 = k0 + bk, gn = n0 + bn;
+      Bs[bk][bn] = (gk2 < K && gn < N) ? B[int64_t(gk2) * b_rs + int64_t(gn) * b_cs] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kTileK; ++k) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[k][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[k][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + ty * 4 + i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gn = n0 + tx * 4 + j;
+      if (gn >= N) continue;
+      float v = acc[i][j];
+      if (epi == kEpiBiasRelu) v = fmaxf(v + bias[gn], 0.f);
+      else if (epi == kEpiBias) v += bias[gn];
+      else if (epi == kEpiMask) v = mask[int64_t(gm) * ldmask + gn] > 0.f ? v : 0.f;
+      C[int64_t(gm) * ldc + gn] = v;
+    }
+  }
+}
+
+__global__ void ColSumKernel(int M, int N, const float* A, int64_t lda, float* out) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  float s = 0.f;
+  for (int m = 0; m < M; ++m) s += A[int64_t(m) * lda + n];
+  out[n] = s;
+}
+
+__global__ void HeadKernel(int n, const float* z, const float* samples, int64_t lds, float scale,
+                           float* dz, float* loss) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  constexpr int kB = kPrecondBlock;
+  const float* zi = z + int64_t(i) * kPrecondTri;
+  const float* gh = samples + int64_t(i) * lds + kPrecondFeatures;
+  const float* xh = gh + kB;
+  float L[kPrecondTri], sig[kB];
+#pragma unroll
+  for (int r = 0; r < kB; ++r)
+#pragma unroll
+    for (int c = 0; c <= r; ++c) {
+      const float zz = zi[Tri(r, c)];
+      if (r == c) {
+        const float x = zz + kDiagShift;
+        L[Tri(r, r)] = x > 20.f ? x : log1pf(expf(x));
+        sig[r] = 1.f / (1.f + expf(-x));
+      } else {
+        L[Tri(r, c)] = zz;
+      }
+    }
+  // t = L^T g_hat, u = L t - x_hat
+  float t[kB], u[kB], g[kB];
+#pragma unroll
+  for (int r = 0; r < kB; ++r) g[r] = gh[r];
+#pragma unroll
+  for (int c = 0; c < kB; ++c) {
+    float s = 0.f;
+#pragma unroll
+    for (int r = c; r < kB; ++r) s += L[Tri(r, c)] * g[r];
+    t[c] = s;
+  }
+  float xx = 0.f, uu = 0.f;
+#pragma unroll
+  for (int r = 0; r < kB; ++r) {
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c <= r; ++c) s += L[Tri(r, c)] * t[c];
+    u[r] = s - xh[r];
+    xx += xh[r] * xh[r];
+    uu += u[r] * u[r];
+  }
+  const float inv = 1.f / (xx + 1e-30f);
+  loss[i] = uu * inv;
+  // d loss / d L = (G + G^T) L with G = 2 u g^T / s, lower triangle
+  const float f = 2.f * inv * scale;
+  float* dzi = dz + int64_t(i) * kPrecondTri;
+#pragma unroll
+  for (int r = 0; r < kB; ++r)
+#pragma unroll
+    for (int c = 0; c <= r; ++c) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = c; k < kB; ++k) s += (u[r] * g[k] + g[r] * u[k]) * L[Tri(k, c)];
+      s *= f;
+      dzi[Tri(r, c)] = r == c ? s * sig[r] : s;
+    }
+}
+
+__global__ void SumKernel(int n, const float* loss, float scale, double* out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += double(loss[i]);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = double(scale) * red[0];
+}
+
+__global__ void GatherKernel(int n, const float* samples, const int32_t* idx, float* rows) {
+  const int64_t total = int64_t(n) * kSampleFloats;
+  for (int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < total;
+       e += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = e / kSampleFloats, c = e - r * kSampleFloats;
+    rows[e] = samples[int64_t(idx[r]) * kSampleFloats + c];
+  }
+}
+
+__global__ void AdamKernel(int64_t n, float* w, const float* g, float* m, float* v, float lr,
+                           float beta1, float beta2, float eps, float c1, float c2) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const float gi = g[i];
+    const float mi = beta1 * m[i] + (1.f - beta1) * gi;
+    const float vi = beta2 * v[i] + (1.f - beta2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+}  // namespace
+
+void LaunchGemm(int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs, const float* B,
+                int64_t b_rs, int64_t b_cs, float* C, int64_t ldc, int epilogue, const float* bias,
+                const float* mask, int64_t ldmask, cudaStream_t s) {
+  if (M == 0 || N == 0) return;
+  const dim3 grid((N + kTileN - 1) / kTileN, (M + kTileM - 1) / kTileM);
+  GemmKernel<<<grid, 256, 0, s>>>(M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, epilogue, bias,
+                                  mask, ldmask);
+}
+
+void LaunchColSum(int M, int N, const float* A, int64_t lda, float* out, cudaStream_t s) {
+  const int threads = 128;
+  ColSumKernel<<<(N + threads - 1) / threads, threads, 0, s>>>(M, N, A, lda, out);
+}
+
+void LaunchHead(int n, const float* z, const float* samples, int64_t lds, float scale, float* dz,
+                float* loss, double* loss_sum, cudaStream_t s) {
+  const int threads = 128;
+  HeadKernel<<<(n + threads - 1) / threads, threads, 0, s>>>(n, z, samples, lds, scale, dz, loss);
+  SumKernel<<<1, 256, 0, s>>>(n, loss, scale, loss_sum);
+}
+
+void LaunchGather(int n, const float* samples, const int32_t* idx, float* rows, cudaStream_t s) {
+  const int threads = 256;
+  const int64_t total = int64_t(n) * kSampleFloats;
+  const int grid = int(std::min<int64_t>((total + threads - 1) / threads, 4096));
+  GatherKernel<<<std::max(grid, 1), threads, 0, s>>>(n, samples, idx, rows);
+}
+
+void LaunchAdam(int64_t n, float* w, const float* g, float* m, float* v, float lr, float beta1,
+                float beta2, float eps, float c1, float c2, cudaStream_t s) {
+  const int threads = 256;
+  const int grid = int(std::min<int64_t>((n + threads - 1) / threads, 1024));
+  AdamKernel<<<grid, threads, 0, s>>>(n, w, g, m, v, lr, beta1, beta2, eps, c1, c2);
+}
+
+}  // namespace sfg

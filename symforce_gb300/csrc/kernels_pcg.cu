@@ -1,0 +1,566 @@
+// Preconditioned conjugate gradients on the reduced camera system (the PCG forms).
+//
+//  - Camera-block features: each camera's 9 x 9 block of S scaled to unit diagonal, the rows'
+//    coupling to other blocks, the block degree; and the block's scaled Cholesky factor.
+//  - Preconditioner blocks P_g = D^-1/2 C^-T L L^T C^-1 D^-1/2 with L from the network (or I:
+//    block Jacobi).
+//  - One persistent kernel per reduced-system solve: FP64 residual passes r = v - S y around
+//    inner PCG solves in the matrix precision, until |r| <= tol |v| or the iteration cap.  Three
+//    lanes-groups of nine lanes per warp own the nine rows of one camera block each, so applying
+//    P_g is a warp-shuffle product and every thread keeps its row of P_g in registers.  Dot
+//    products are reduced in FP64 in a fixed order (warp tree, CTA order, then the same fixed
+//    order over CTAs in every CTA), so every CTA takes the same branch and runs are reproducible.
+//    Multi-CTA solves use a grid barrier (cooperative launch: all CTAs resident) whose waits are
+//    capped; a cap hit sets the device error word.
+//  - The network's inference pass (96 -> 256 -> 256 -> 45, ReLU) for all camera blocks.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "kernels.h"
+
+namespace sfg {
+
+namespace {
+
+constexpr int kB = kPrecondBlock;
+constexpr unsigned kSpinLimit = 1u << 22;
+constexpr float kDiagShift = 0.54132485f;  // ln(e - 1): softplus(kDiagShift) = 1
+constexpr int kPcgMultiThreads = 256;
+
+__device__ __forceinline__ float Softplus(float x) { return x > 20.f ? x : log1pf(expf(x)); }
+
+__device__ __forceinline__ int Tri(int i, int j) { return i * (i + 1) / 2 + j; }
+
+// ---------------------------------------------------------------------------------------------
+// Features
+// ---------------------------------------------------------------------------------------------
+// One warp per reduced-system row: rho = sum over entries outside the row's block of
+// S_rc^2 / (S_rr S_cc).
+template <typename T>
+__global__ void PrecondRowKernel(PrecondDev pd, SpmvDev m, const T* S, float* rho) {
+  const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (row >= m.n) return;
+  const int grow = pd.scalar_group[row];
+  const float drow = float(S[pd.sdiag_off[row]]);
+  float acc = 0.f;
+  for (int64_t q = m.row_ptr[row] + lane; q < m.row_ptr[row + 1]; q += 32) {
+    const T* a = S + m.seg_base[q];
+    const int stride = m.seg_stride[q], n = m.seg_len[q], x0 = m.seg_x[q];
+    for (int c = 0; c < n; ++c) {
+      const int col = x0 + c;
+      if (pd.scalar_group[col] == grow) continue;
+      const float v = float(a[int64_t(c) * stride]);
+      const float dc = float(S[pd.sdiag_off[col]]);
+      acc += v * v / fmaxf(drow * dc, 1e-30f);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) rho[row] = acc;
+}
+
+// One thread per camera block: inputs of the network and the block's scaled Cholesky factor.
+template <typename T>
+__global__ void PrecondFeatureKernel(PrecondDev pd, const T* S, const float* rho, float* feats,
+                                     float* fac) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= pd.ng) return;
+  const int32_t* gi = pd.gidx + size_t(g) * kB;
+  const int64_t* go = pd.goff + size_t(g) * kB * kB;
+  float dis[kB];
+#pragma unroll
+  for (int a = 0; a < kB; ++a) {
+    const int64_t o = go[a * kB + a];
+    const float d = o >= 0 ? float(S[o]) : 1.f;
+    dis[a] = d > 0.f ? rsqrtf(d) : 1.f;
+  }
+  float A[kB * kB];
+#pragma unroll
+  for (int a = 0; a < kB; ++a)
+#pragma unroll
+    for (int b = 0; b < kB; ++b) {
+      const int64_t o = go[a * kB + b];
+      float v;
+      if (o >= 0) v = float(S[o]) * dis[a] * dis[b];
+      else v = (o == -1 && a == b) ? 1.f : 0.f;
+      A[a * kB + b] = v;
+    }
+  float* fo = feats + size_t(g) * kPrecondFeatures;
+#pragma unroll
+  for (int i = 0; i < kB * kB; ++i) fo[i] = A[i];
+#pragma unroll
+  for (int a = 0; a < kB; ++a) fo[kB * kB + a] = gi[a] >= 0 ? log1pf(rho[gi[a]]) : 0.f;
+  fo[kB * kB + kB] = pd.degree[g] * (1.f / 16.f);
+#pragma unroll
+  for (int i = kB * kB + kB + 1; i < kPrecondFeatures; ++i) fo[i] = 0.f;
+  // C C^T = A (lower, packed); identity if A is not numerically positive definite
+  float C[kPrecondTri];
+  bool ok = true;
+#pragma unroll
+  for (int i = 0; i < kB; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      float s = A[i * kB + j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) s -= C[Tri(i, k)] * C[Tri(j, k)];
+      if (i == j) {
+        if (!(s > 1e-12f)) {
+          ok = false;
+          s = 1.f;
+        }
+        C[Tri(i, i)] = sqrtf(s);
+      } else {
+        C[Tri(i, j)] = s / C[Tri(j, j)];
+      }
+    }
+  float* fc = fac + size_t(g) * kPrecondFac;
+#pragma unroll
+  for (int i = 0; i < kB; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) fc[Tri(i, j)] = ok ? C[Tri(i, j)] : (i == j ? 1.f : 0.f);
+#pragma unroll
+  for (int a = 0; a < kB; ++a) fc[kPrecondTri + a] = dis[a];
+}
+
+// P_g = Q Q^T, Q = D^-1/2 C^-T L.
+template <typename T>
+__global__ void PrecondAssembleKernel(int ng, const float* fac, const float* z, T* P) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ng) return;
+  const float* fc = fac + size_t(g) * kPrecondFac;
+  float C[kPrecondTri], L[kPrecondTri];
+#pragma unroll
+  for (int i = 0; i < kPrecondTri; ++i) C[i] = fc[i];
+  if (z) {
+    const float* zg = z + size_t(g) * kPrecondTri;
+#pragma unroll
+    for (int i = 0; i < kB; ++i)
+#pragma unroll
+      for (int j = 0; j <= i; ++j) L[Tri(i, j)] = i == j ? Softplus(zg[Tri(i, i)] + kDiagShift) : zg[Tri(i, j)];
+  } else {
+#pragma unroll
+    for (int i = 0; i < kB; ++i)
+#pragma unroll
+      for (int j = 0; j <= i; ++j) L[Tri(i, j)] = i == j ? 1.f : 0.f;
+  }
+  // M = C^-T L: back substitution with the upper triangle C^T, column by column
+  float Q[kB * kB];
+#pragma unroll
+  for (int j = 0; j < kB; ++j)
+#pragma unroll
+    for (int i = kB - 1; i >= 0; --i) {
+      float s = i >= j ? L[Tri(i, j)] : 0.f;
+#pragma unroll
+      for (int k = i + 1; k < kB; ++k) s -= C[Tri(k, i)] * Q[k * kB + j];
+      Q[i * kB + j] = s / C[Tri(i, i)];
+    }
+#pragma unroll
+  for (int i = 0; i < kB; ++i) {
+    const float d = fc[kPrecondTri + i];
+#pragma unroll
+    for (int j = 0; j < kB; ++j) Q[i * kB + j] *= d;
+  }
+  T* Pg = P + size_t(g) * kB * kB;
+#pragma unroll
+  for (int a = 0; a < kB; ++a)
+#pragma unroll
+    for (int b = 0; b <= a; ++b) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < kB; ++k) s += Q[a * kB + k] * Q[b * kB + k];
+      Pg[a * kB + b] = T(s);
+      Pg[b * kB + a] = T(s);
+    }
+}
+
+// Training samples of the current system: inputs, g_hat = C^-1 D^-1/2 v_g, x_hat = C^T D^1/2 y_g.
+template <typename T>
+__global__ void CollectSamplesKernel(PrecondDev pd, const float* feats, const float* fac,
+                                     const T* v, const double* y, float* samples, int max_systems,
+                                     const LmState* st) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int slot = st->num_records - 1;
+  if (g >= pd.ng || slot < 0 || slot >= max_systems) return;
+  const int32_t* gi = pd.gidx + size_t(g) * kB;
+  const float* fc = fac + size_t(g) * kPrecondFac;
+  float* out = samples + (size_t(slot) * pd.ng + g) * kSampleFloats;
+  const float* fi = feats + size_t(g) * kPrecondFeatures;
+  for (int i = 0; i < kPrecondFeatures; ++i) out[i] = fi[i];
+  float gh[kB];
+#pragma unroll
+  for (int i = 0; i < kB; ++i) {
+    float s = gi[i] >= 0 ? float(v[gi[i]]) * fc[kPrecondTri + i] : 0.f;
+#pragma unroll
+    for (int k = 0; k < i; ++k) s -= fc[Tri(i, k)] * gh[k];
+    gh[i] = s / fc[Tri(i, i)];
+  }
+  float yd[kB];
+#pragma unroll
+  for (int i = 0; i < kB; ++i) yd[i] = gi[i] >= 0 ? float(y[gi[i]]) / fc[kPrecondTri + i] : 0.f;
+#pragma unroll
+  for (int i = 0; i < kB; ++i) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = i; k < kB; ++k) s += fc[Tri(k, i)] * yd[k];
+    out[kPrecondFeatures + i] = gh[i];
+    out[kPrecondFeatures + kB + i] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Network inference: 16 blocks per CTA, one hidden unit per thread.
+// ---------------------------------------------------------------------------------------------
+constexpr int kMlpRows = 16;
+
+__global__ void __launch_bounds__(kPrecondHidden) MlpInferKernel(const float* x, int64_t ldx, int64_t n,
+                                                               const float* W, float* z) {
+  __shared__ float xs[kMlpRows][kPrecondFeatures];
+  __shared__ float h1[kMlpRows][kPrecondHidden];
+  __shared__ float h2[kMlpRows][kPrecondHidden];
+  const int64_t row0 = int64_t(blockIdx.x) * kMlpRows;
+  const int t = threadIdx.x;
+  for (int i = t; i < kMlpRows * kPrecondFeatures; i += blockDim.x) {
+    const int r = i / kPrecondFeatures, c = i - r * kPrecondFeatures;
+    xs[r][c] = row0 + r < n ? x[(row0 + r) * ldx + c] : 0.f;
+  }
+  __syncthreads();
+  const float* W1 = W;
+  const float* b1 = W1 + kPrecondFeatures * kPrecondHidden;
+  const float* W2 = b1 + kPrecondHidden;
+  const float* b2 = W2 + kPrecondHidden * kPrecondHidden;
+  const float* W3 = b2 + kPrecondHidden;
+  const float* b3 = W3 + kPrecondHidden * kPrecondTri;
+  float acc[kMlpRows];
+#pragma unroll
+  for (int r = 0; r < kMlpRows; ++r) acc[r] = b1[t];
+  for (int k = 0; k < kPrecondFeatures; ++k) {
+    const float w = __ldg(W1 + k * kPrecondHidden + t);
+#pragma unroll
+    for (int r = 0; r < kMlpRows; ++r) acc[r] = fmaf(xs[r][k], w, acc[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < kMlpRows; ++r) h1[r][t] = fmaxf(acc[r], 0.f);
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kMlpRows; ++r) acc[r] = b2[t];
+  for (int k = 0; k < kPrecondHidden; ++k) {
+    const float w = __ldg(W2 + k * kPrecondHidden + t);
+#pragma unroll
+    for (int r = 0; r < kMlpRows; ++r) acc[r] = fmaf(h1[r][k], w, acc[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < kMlpRows; ++r) h2[r][t] = fmaxf(acc[r], 0.f);
+  __syncthreads();
+  constexpr int kGroups = kMlpRows / 4;
+  if (t < kPrecondTri * kGroups) {
+    const int o = t % kPrecondTri, rg = t / kPrecondTri;
+    float a4[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a4[i] = b3[o];
+    for (int k = 0; k < kPrecondHidden; ++k) {
+      const float w = __ldg(W3 + k * kPrecondTri + o);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a4[i] = fmaf(h2[rg * 4 + i][k], w, a4[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int64_t r = row0 + rg * 4 + i;
+      if (r < n) z[r * kPrecondTri + o] = a4[i];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// PCG
+// ---------------------------------------------------------------------------------------------
+__device__ void GridBarrier(unsigned* bar, unsigned nblocks, int* err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* vgen = bar + 1;
+    const unsigned gen = *vgen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned it = 0;
+      while (*vgen == gen) {
+        if (*reinterpret_cast<volatile int*>(err) != 0) break;
+        if (++it > kSpinLimit) {
+          atomicExch(err, kDevSpinTimeout);
+          break;
+        }
+        if (it > 32) __nanosleep(32);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+struct PcgSmem {
+  double2 red[32];
+  double2 out;
+};
+
+// Sum of (a, b) over every thread of the grid, the same bits in every thread.
+__device__ double2 GridSum2(double a, double b, const PcgDev& d, int& seq, PcgSmem& sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int grid = gridDim.x;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  __syncthreads();  // readers of the previous result are done
+  if (lane == 0) sm.red[warp] = make_double2(a, b);
+  __syncthreads();
+  double2* part = reinterpret_cast<double2*>(d.partials) + size_t(seq & 1) * grid;
+  if (threadIdx.x == 0) {
+    double2 t = make_double2(0.0, 0.0);
+    for (int w = 0; w < nwarp; ++w) {
+      t.x += sm.red[w].x;
+      t.y += sm.red[w].y;
+    }
+    if (grid == 1) sm.out = t;
+    else __stcg(part + blockIdx.x, t);
+  }
+  if (grid > 1) {
+    GridBarrier(d.bar, grid, d.err);
+    if (warp == 0) {
+      double2 t = make_double2(0.0, 0.0);
+      for (int q = lane; q < grid; q += 32) {
+        const double2 v = __ldcg(part + q);
+        t.x += v.x;
+        t.y += v.y;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        t.x += __shfl_down_sync(0xffffffffu, t.x, o);
+        t.y += __shfl_down_sync(0xffffffffu, t.y, o);
+      }
+      if (lane == 0) sm.out = t;
+    }
+  }
+  __syncthreads();
+  ++seq;
+  return sm.out;
+}
+
+template <typename T>
+__device__ __forceinline__ T ApplyBlock(const T (&prow)[kB], T r, int gbase) {
+  T acc = T(0);
+#pragma unroll
+  for (int b = 0; b < kB; ++b) acc += prow[b] * __shfl_sync(0xffffffffu, r, gbase + b);
+  return acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
+  __shared__ PcgSmem sm;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / kB;  // 0..2: camera block of the lane; 3: idle lanes 27..31
+  const int a = lane - sub * kB;
+  const int g = (blockIdx.x * (blockDim.x >> 5) + warp) * 3 + sub;
+  const bool in_group = sub < 3 && g < d.pd.ng;
+  const int s = in_group ? d.pd.gidx[size_t(g) * kB + a] : -1;
+  const bool own = s >= 0;
+  const int gbase = sub < 3 ? sub * kB : 0;
+  const T* S = static_cast<const T*>(d.S);
+  const T* v = static_cast<const T*>(d.v);
+  const T* P = static_cast<const T*>(d.P);
+  T* zg = static_cast<T*>(d.z);
+  T prow[kB];
+#pragma unroll
+  for (int b = 0; b < kB; ++b) prow[b] = own ? P[(size_t(g) * kB + a) * kB + b] : T(0);
+  const int64_t q0 = own ? d.m.row_ptr[s] : 0, q1 = own ? d.m.row_ptr[s + 1] : 0;
+  int seq = 0;
+  const double vs = own ? double(v[s]) : 0.0;
+  const double vnorm = sqrt(GridSum2(vs * vs, 0.0, d, seq, sm).x);
+  bool converged = !(vnorm > 0.0);  // zero rhs: y = 0
+  double rel = 0.0;
+  double y64 = 0.0;
+  int iters = 0, outer = 0;
+  bool broke = false;
+  while (!converged) {
+    double r64 = vs;
+    if (outer > 0 && own) {
+      double acc = 0.0;
+      for (int64_t q = q0; q < q1; ++q) {
+        const T* aa = S + d.m.seg_base[q];
+        const int stride = d.m.seg_stride[q], n = d.m.seg_len[q];
+        const double* yy = d.y + d.m.seg_x[q];
+        for (int c = 0; c < n; ++c) acc += double(aa[int64_t(c) * stride]) * __ldcg(yy + c);
+      }
+      r64 = vs - acc;
+    }
+    const double rr64 = GridSum2(r64 * r64, 0.0, d, seq, sm).x;
+    rel = sqrt(rr64) / vnorm;
+    if (rel <= d.tol) {
+      converged = true;
+      break;
+    }
+    if (outer >= d.max_outer || iters >= d.max_iters || broke || !(rel == rel)) break;
+    ++outer;
+    // inner PCG on S dx = r (x0 = 0), in the matrix precision; the product uses w = S z and
+    // q = w + beta q so that one grid reduction separates the product from the update
+    T r = T(r64);
+    T zz = ApplyBlock(prow, r, gbase);
+    if (own) __stcg(zg + s, zz);
+    double rz = GridSum2(double(r) * double(zz), 0.0, d, seq, sm).x;
+    const double target = fmax(0.5 * d.tol * vnorm, d.inner_floor * sqrt(rr64));
+    T p = T(0), qv = T(0), dx = T(0);
+    double beta = 0.0;
+    for (;;) {
+      T w = T(0);
+      for (int64_t q = q0; q < q1; ++q) {
+        const T* aa = S + d.m.seg_base[q];
+        const int stride = d.m.seg_stride[q], n = d.m.seg_len[q];
+        const T* zz_in = zg + d.m.seg_x[q];
+        for (int c = 0; c < n; ++c) w += aa[int64_t(c) * stride] * __ldcg(zz_in + c);
+      }
+      p = zz + T(beta) * p;
+      qv = w + T(beta) * qv;
+      const double pq = GridSum2(double(p) * double(qv), 0.0, d, seq, sm).x;
+      if (!(pq > 0.0) || !(pq < 1e300) || !(fabs(rz) < 1e300)) {
+        broke = true;
+        break;
+      }
+      const double alpha = rz / pq;
+      dx += T(alpha) * p;
+      r -= T(alpha) * qv;
+      zz = ApplyBlock(prow, r, gbase);
+      if (own) __stcg(zg + s, zz);
+      const double2 sums = GridSum2(double(r) * double(zz), double(r) * double(r), d, seq, sm);
+      ++iters;
+      if (sqrt(sums.y) <= target || iters >= d.max_iters) break;
+      beta = sums.x / rz;
+      rz = sums.x;
+    }
+    y64 += double(dx);
+    if (own) __stcg(d.y + s, y64);
+    if (gridDim.x > 1) GridBarrier(d.bar, gridDim.x, d.err);
+    else __syncthreads();
+  }
+  if (own) __stcg(d.y + s, y64);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    PcgState* ps = d.ps;
+    ps->converged = converged ? 1 : 0;
+    ps->need_fallback = converged ? 0 : 1;
+    ps->iterations = iters;
+    ps->outer = outer;
+    ps->rel_residual = rel;
+    ps->total_iterations += iters;
+    ps->solves += 1;
+    ps->fallbacks += converged ? 0 : 1;
+    ps->max_iterations = max(ps->max_iterations, iters);
+    ps->max_rel_residual = fmax(ps->max_rel_residual, rel);
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------------------------
+template <typename T>
+void LaunchPrecondFeatures(const PrecondDev& pd, const SpmvDev& m, const void* S, float* rho,
+                           float* feats, float* fac, cudaStream_t s) {
+  if (pd.ng == 0) return;
+  const int warps = 8;
+  PrecondRowKernel<T><<<(m.n + warps - 1) / warps, 32 * warps, 0, s>>>(pd, m, static_cast<const T*>(S), rho);
+  const int threads = 64;
+  PrecondFeatureKernel<T><<<(pd.ng + threads - 1) / threads, threads, 0, s>>>(
+      pd, static_cast<const T*>(S), rho, feats, fac);
+}
+
+template <typename T>
+void LaunchPrecondAssemble(int ng, const float* fac, const float* z, void* P, cudaStream_t s) {
+  if (ng == 0) return;
+  const int threads = 64;
+  PrecondAssembleKernel<T><<<(ng + threads - 1) / threads, threads, 0, s>>>(ng, fac, z, static_cast<T*>(P));
+}
+
+void LaunchMlpInfer(const float* x, int64_t ldx, int64_t n, const float* weights, float* z,
+                    cudaStream_t s) {
+  if (n == 0) return;
+  const int64_t grid = (n + kMlpRows - 1) / kMlpRows;
+  MlpInferKernel<<<unsigned(grid), kPrecondHidden, 0, s>>>(x, ldx, n, weights, z);
+}
+
+template <typename T>
+void LaunchCollectSamples(const PrecondDev& pd, const float* feats, const float* fac, const void* v,
+                          const double* y, float* samples, int max_systems, PcgState* ps,
+                          const LmState* st, cudaStream_t s) {
+  (void)ps;
+  if (pd.ng == 0) return;
+  const int threads = 64;
+  CollectSamplesKernel<T><<<(pd.ng + threads - 1) / threads, threads, 0, s>>>(
+      pd, feats, fac, static_cast<const T*>(v), y, samples, max_systems, st);
+}
+
+void PcgShape(int ng, int num_sms, int* grid, int* threads) {
+  (void)num_sms;
+  const int warps = std::max(1, (ng + 2) / 3);
+  if (warps <= 32) {
+    *grid = 1;
+    *threads = 32 * warps;
+  } else {
+    *threads = kPcgMultiThreads;
+    const int per_cta = 3 * (kPcgMultiThreads / 32);
+    *grid = (ng + per_cta - 1) / per_cta;
+  }
+}
+
+template <typename T>
+int PcgMaxResidentCtas(int threads, int num_sms) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, PcgKernel<T>, threads, 0) != cudaSuccess)
+    return 0;
+  return per_sm * num_sms;
+}
+template int PcgMaxResidentCtas<double>(int, int);
+template int PcgMaxResidentCtas<float>(int, int);
+
+template <typename T>
+cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s) {
+  if (grid == 1) {
+    PcgKernel<T><<<1, threads, 0, s>>>(d);
+    return cudaGetLastError();
+  }
+  const cudaError_t e = cudaMemsetAsync(d.bar, 0, 2 * sizeof(unsigned), s);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, PcgKernel<T>, d);
+}
+
+void LaunchPcgBegin(PcgState* ps, cudaStream_t s) { cudaMemsetAsync(ps, 0, sizeof(PcgState), s); }
+
+template void LaunchPrecondFeatures<double>(const PrecondDev&, const SpmvDev&, const void*, float*,
+                                            float*, float*, cudaStream_t);
+template void LaunchPrecondFeatures<float>(const PrecondDev&, const SpmvDev&, const void*, float*,
+                                           float*, float*, cudaStream_t);
+template void LaunchPrecondAssemble<double>(int, const float*, const float*, void*, cudaStream_t);
+template void LaunchPrecondAssemble<float>(int, const float*, const float*, void*, cudaStream_t);
+template void LaunchCollectSamples<double>(const PrecondDev&, const float*, const float*, const void*,
+                                           const double*, float*, int, PcgState*, const LmState*,
+                                           cudaStream_t);
+template void LaunchCollectSamples<float>(const PrecondDev&, const float*, const float*, const void*,
+                                          const double*, float*, int, PcgState*, const LmState*,
+                                          cudaStream_t);
+template cudaError_t LaunchPcg<double>(const PcgDev&, int, int, cudaStream_t);
+template cudaError_t LaunchPcg<float>(const PcgDev&, int, int, cudaStream_t);
+
+}  // namespace sfg

@@ -467,6 +467,7 @@ __global__ void __launch_bounds__(kFactorThreads) FactorKernel(FactorDev f, cons
                                                                T* Linv) {
   __shared__ TileSmem<T, TILE> sm;
   __shared__ int s_task, s_next, s_ok, s_flag;
+  if (f.gate && *f.gate == 0) return;
   A += int64_t(f.st->init_idx) * f.a_stride;
   if (threadIdx.x == 0) s_next = atomicAdd(f.counters, 1);
   for (;;) {
@@ -578,6 +579,7 @@ __global__ void __launch_bounds__(kFactorThreads) SolveKernel(FactorDev f, const
   __shared__ int s_task, s_ok, s_flag;
   int* fwd_done = f.front_flags;
   int* bwd_done = f.front_flags + f.ns;
+  if (f.gate && *f.gate == 0) return;
   b += int64_t(f.st->init_idx) * f.b_stride;
   for (;;) {
     if (threadIdx.x == 0) {
@@ -654,10 +656,11 @@ __global__ void __launch_bounds__(kFactorThreads) SolveKernel(FactorDev f, const
 // ---------------------------------------------------------------------------------------------
 template <typename T>
 __global__ void RefineResidualKernel(SpmvDev m, const T* A_all, const double* damping, const T* b_all,
-                                     const double* y, double* r, T* r_lo, const LmState* st) {
+                                     const double* y, double* r, T* r_lo, const LmState* st,
+                                     const int* gate) {
   const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (row >= m.n) return;
+  if (row >= m.n || (gate && *gate == 0)) return;
   const T* A = A_all + int64_t(st->init_idx) * m.a_stride;
   const T* b = b_all + int64_t(st->init_idx) * m.b_stride;
   double acc = 0.0;
@@ -678,19 +681,22 @@ __global__ void RefineResidualKernel(SpmvDev m, const T* A_all, const double* da
 }
 
 template <typename T>
-__global__ void WidenKernel(const T* x, double* y, int64_t n) {
+__global__ void WidenKernel(const T* x, double* y, int64_t n, const int* gate) {
+  if (gate && *gate == 0) return;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
     y[i] = double(x[i]);
 }
 
 template <typename T>
-__global__ void AccumulateKernel(const T* dx, double* y, int64_t n) {
+__global__ void AccumulateKernel(const T* dx, double* y, int64_t n, const int* gate) {
+  if (gate && *gate == 0) return;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
     y[i] += double(dx[i]);
 }
 
 __global__ void ResetFactorStateKernel(int* tile_state, int nstates, int* front_flags, int nflags,
-                                       int* counters) {
+                                       int* counters, const int* gate) {
+  if (gate && *gate == 0) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nstates; i += gridDim.x * blockDim.x)
     tile_state[i] = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nflags; i += gridDim.x * blockDim.x)
@@ -708,11 +714,12 @@ __global__ void NegateKernel(const T* x, double* u, int64_t n) {
 }  // namespace
 
 void LaunchResetFactorState(int* tile_state, int nstates, int* front_flags, int nflags,
-                            int* counters, cudaStream_t s) {
+                            int* counters, cudaStream_t s, const int* gate) {
   const int threads = 256;
   int grid = (std::max(nstates, nflags) + threads - 1) / threads;
   grid = std::min(std::max(grid, 1), 1024);
-  ResetFactorStateKernel<<<grid, threads, 0, s>>>(tile_state, nstates, front_flags, nflags, counters);
+  ResetFactorStateKernel<<<grid, threads, 0, s>>>(tile_state, nstates, front_flags, nflags, counters,
+                                                  gate);
 }
 
 template <typename T>
@@ -726,31 +733,35 @@ template void LaunchNegate<float>(const void*, double*, int64_t, cudaStream_t);
 
 template <typename T>
 void LaunchRefineResidual(const SpmvDev& m, const void* A, const double* damping, const void* b,
-                          const double* y, double* r, void* r_lo, const LmState* st, cudaStream_t s) {
+                          const double* y, double* r, void* r_lo, const LmState* st, cudaStream_t s,
+                          const int* gate) {
   const int warps = 8;
   RefineResidualKernel<T><<<(m.n + warps - 1) / warps, 32 * warps, 0, s>>>(
-      m, static_cast<const T*>(A), damping, static_cast<const T*>(b), y, r, static_cast<T*>(r_lo), st);
+      m, static_cast<const T*>(A), damping, static_cast<const T*>(b), y, r, static_cast<T*>(r_lo), st,
+      gate);
 }
 template <typename T>
-void LaunchWiden(const void* x, double* y, int64_t n, cudaStream_t s) {
+void LaunchWiden(const void* x, double* y, int64_t n, cudaStream_t s, const int* gate) {
   const int threads = 256;
   const int grid = int(std::min<int64_t>(std::max<int64_t>((n + threads - 1) / threads, 1), 1024));
-  WidenKernel<T><<<grid, threads, 0, s>>>(static_cast<const T*>(x), y, n);
+  WidenKernel<T><<<grid, threads, 0, s>>>(static_cast<const T*>(x), y, n, gate);
 }
 template <typename T>
-void LaunchAccumulate(const void* dx, double* y, int64_t n, cudaStream_t s) {
+void LaunchAccumulate(const void* dx, double* y, int64_t n, cudaStream_t s, const int* gate) {
   const int threads = 256;
   const int grid = int(std::min<int64_t>(std::max<int64_t>((n + threads - 1) / threads, 1), 1024));
-  AccumulateKernel<T><<<grid, threads, 0, s>>>(static_cast<const T*>(dx), y, n);
+  AccumulateKernel<T><<<grid, threads, 0, s>>>(static_cast<const T*>(dx), y, n, gate);
 }
 template void LaunchRefineResidual<double>(const SpmvDev&, const void*, const double*, const void*,
-                                           const double*, double*, void*, const LmState*, cudaStream_t);
+                                           const double*, double*, void*, const LmState*, cudaStream_t,
+                                           const int*);
 template void LaunchRefineResidual<float>(const SpmvDev&, const void*, const double*, const void*,
-                                          const double*, double*, void*, const LmState*, cudaStream_t);
-template void LaunchWiden<double>(const void*, double*, int64_t, cudaStream_t);
-template void LaunchWiden<float>(const void*, double*, int64_t, cudaStream_t);
-template void LaunchAccumulate<double>(const void*, double*, int64_t, cudaStream_t);
-template void LaunchAccumulate<float>(const void*, double*, int64_t, cudaStream_t);
+                                          const double*, double*, void*, const LmState*, cudaStream_t,
+                                          const int*);
+template void LaunchWiden<double>(const void*, double*, int64_t, cudaStream_t, const int*);
+template void LaunchWiden<float>(const void*, double*, int64_t, cudaStream_t, const int*);
+template void LaunchAccumulate<double>(const void*, double*, int64_t, cudaStream_t, const int*);
+template void LaunchAccumulate<float>(const void*, double*, int64_t, cudaStream_t, const int*);
 
 int FactorThreads() { return kFactorThreads; }
 

@@ -43,4 +43,16 @@ struct SchurLayout {
 
 SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L);
 
+// Camera blocks of the reduced system for the PCG forms: B keys joined when they share a factor
+// (pose + intrinsics of a camera), at most 9 scalars per block, ordered by their first key.
+struct PrecondLayout {
+  int ng = 0;
+  std::vector<int32_t> gidx;          // [ng][9] reduced-system scalar, -1 padding
+  std::vector<int64_t> goff;          // [ng][81] S value offset of (a, b); -1 padding, -2 zero
+  std::vector<float> degree;          // [ng] neighbouring blocks
+  std::vector<int32_t> scalar_group;  // [nB]
+  std::vector<int64_t> sdiag_off;     // [nB]
+};
+PrecondLayout BuildPrecondLayout(const HostProblem& P, const SchurLayout& SL);
+
 }  // namespace sfg

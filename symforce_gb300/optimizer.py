@@ -62,6 +62,18 @@ def lib() -> C.CDLL:
         L.sfg_schur_factorize.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.sfg_schur_solve.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int32]
         L.sfg_schur_destroy.argtypes = [C.c_void_p]
+        L.sfg_get_pcg_stats.argtypes = [C.c_void_p, C.POINTER(A.PcgStatsC)]
+        L.sfg_pcg_step_error.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32),
+                                         C.POINTER(C.c_double)]
+        L.sfg_set_preconditioner_weights.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int64]
+        L.sfg_collect_samples.argtypes = [C.c_void_p, C.c_int32]
+        L.sfg_get_samples.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_int64)]
+        L.sfg_precond_train.argtypes = [C.POINTER(C.c_float), C.c_int64, C.POINTER(A.TrainParamsC),
+                                        C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.sfg_precond_loss_grad.argtypes = [C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float),
+                                            C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_int32]
+        L.sfg_precond_infer.argtypes = [C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float),
+                                        C.POINTER(C.c_float), C.c_int32]
         _lib = L
     return _lib
 
@@ -91,7 +103,9 @@ class Optimizer:
     """GPU Levenberg-Marquardt optimizer for one problem structure (create once, optimize many)."""
 
     def __init__(self, problem: A.ProblemArrays, params: A.OptimizerParams | None = None,
-                 form: A.FormParams | None = None):
+                 form: A.FormParams | None = None, weights: np.ndarray | None = None):
+        """`weights`: preconditioner network weights of the learned PCG form (default: the trained
+        weights shipped with the package)."""
         self.problem = problem
         self.params = params or A.default_optimizer_params()
         self.form = form or A.default_form_params()
@@ -101,6 +115,39 @@ class Optimizer:
         S, N, M = C.c_int64(), C.c_int64(), C.c_int64()
         _check(lib().sfg_storage_dim(self._h, C.byref(S), C.byref(N), C.byref(M)))
         self.storage_dim, self.tangent_dim, self.residual_dim = S.value, N.value, M.value
+        if self.form.linear_solver == A.SFG_LINEAR_SOLVER_PCG_LEARNED:
+            if weights is None:
+                from . import learned
+                weights = learned.load_weights()
+            self.set_preconditioner_weights(weights)
+
+    def set_preconditioner_weights(self, weights: np.ndarray) -> None:
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        _check(lib().sfg_set_preconditioner_weights(self._h, A.fptr(w), w.size))
+
+    def pcg_stats(self) -> dict:
+        """Reduced-system PCG solves of the last optimize call (PCG forms)."""
+        s = A.PcgStatsC()
+        _check(lib().sfg_get_pcg_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in A.PcgStatsC._fields_}
+
+    def pcg_step_error(self) -> dict:
+        """The exact LDL^T as judge of one PCG step at the last accepted state."""
+        e, it, res = C.c_double(), C.c_int32(), C.c_double()
+        _check(lib().sfg_pcg_step_error(self._h, C.byref(e), C.byref(it), C.byref(res)))
+        return dict(rel_step_error=e.value, iterations=it.value, rel_residual=res.value)
+
+    def collect_samples(self, max_systems: int) -> None:
+        """Record preconditioner training samples during the following optimize calls."""
+        _check(lib().sfg_collect_samples(self._h, max_systems))
+
+    def samples(self) -> np.ndarray:
+        n = C.c_int64()
+        _check(lib().sfg_get_samples(self._h, None, 0, C.byref(n)))
+        out = np.zeros((n.value, A.PRECOND_SAMPLE_FLOATS), dtype=np.float32)
+        if n.value:
+            _check(lib().sfg_get_samples(self._h, A.fptr(out), n.value, C.byref(n)))
+        return out
 
     def close(self) -> None:
         if self._h:
@@ -164,7 +211,7 @@ class Optimizer:
         return dict(residual=res, rhs=rhs, error=err.value, colptr=colptr, rowidx=rowidx, hvals=hv)
 
     def permutation(self) -> np.ndarray:
-        n = self.form.linear_solver == A.SFG_LINEAR_SOLVER_SCHUR
+        n = self.form.linear_solver in A.SCHUR_SOLVERS
         size = self.tangent_dim - (3 * self.problem.num_schur_keys if n else 0)
         perm = np.zeros(size, dtype=np.int32)
         _check(lib().sfg_permutation(self._h, A.iptr(perm), size))

@@ -1,0 +1,76 @@
+"""The learned-preconditioner oracle pinned on the CPU: finite-difference gradient of the loss,
+zero weights = block Jacobi, the block assembly identity P_g S_gg = I, and the PCG restatement."""
+
+from __future__ import annotations
+
+import numpy as np
+
+import precond_cases as PC
+from oracle import precond_net as PN
+
+
+def test_loss_gradient_matches_finite_differences():
+    rng = np.random.Generator(np.random.PCG64(1))
+    samples = PC.oracle_samples((3,))[:12].astype(np.float64)
+    w = PC.random_weights(2, out_scale=0.2).astype(np.float64)
+    loss, grad = PN.loss_grad(w, samples)
+    assert np.isfinite(loss) and loss > 0
+    # directional derivatives along random directions and along single coordinates of each layer
+    for _ in range(4):
+        d = rng.normal(size=w.size)
+        h = 1e-6
+        fd = (PN.loss_grad(w + h * d, samples)[0] - PN.loss_grad(w - h * d, samples)[0]) / (2 * h)
+        assert abs(fd - grad @ d) <= 1e-5 * max(1.0, abs(fd)), (fd, grad @ d)
+    offs = np.cumsum([0, 96 * 256, 256, 256 * 256, 256, 256 * 45, 45])
+    for a, b in zip(offs[:-1], offs[1:]):
+        i = int(a + np.argmax(np.abs(grad[a:b])))
+        e = np.zeros(w.size)
+        e[i] = 1.0
+        h = 1e-6
+        fd = (PN.loss_grad(w + h * e, samples)[0] - PN.loss_grad(w - h * e, samples)[0]) / (2 * h)
+        assert abs(fd - grad[i]) <= 1e-5 * max(1e-3, abs(fd)), (i, fd, grad[i])
+
+
+def test_zero_output_layer_is_block_jacobi():
+    p = PC.small_ba(3)
+    S, v = PC.reduced_system(p)
+    gidx, degree = PC.camera_blocks(p)
+    feats, (C, dis) = PN.block_features(S, gidx, degree)
+    w = PC.random_weights(0)
+    w[-(256 * 45 + 45):] = 0.0
+    z = PN.forward(w.astype(np.float64), feats)
+    assert np.abs(z).max() == 0.0
+    P = PN.assemble(C, dis, z)
+    for g in range(gidx.shape[0]):
+        Sgg = S[np.ix_(gidx[g], gidx[g])]
+        np.testing.assert_allclose(P[g] @ Sgg, np.eye(9), atol=1e-9)
+    # features: unit diagonal of the scaled block, symmetric
+    A = feats[:, :81].reshape(-1, 9, 9)
+    np.testing.assert_allclose(np.diagonal(A, axis1=1, axis2=2), 1.0, atol=1e-12)
+    np.testing.assert_allclose(A, np.transpose(A, (0, 2, 1)), atol=1e-12)
+
+
+def test_samples_whitening_identities():
+    p = PC.small_ba(5)
+    S, v = PC.reduced_system(p)
+    gidx, degree = PC.camera_blocks(p)
+    s = PN.samples_of_system(S, v, gidx, degree)
+    _, (C, dis) = PN.block_features(S, gidx, degree)
+    y = np.linalg.solve(S, v)
+    for g in range(gidx.shape[0]):
+        # L = I: P_g v_g - y_g in the S_gg norm equals |g_hat - x_hat|
+        Sgg = S[np.ix_(gidx[g], gidx[g])]
+        e = np.linalg.solve(Sgg, v[gidx[g]]) - y[gidx[g]]
+        gh, xh = s[g, 96:105], s[g, 105:]
+        assert np.isclose(e @ Sgg @ e, np.sum((gh - xh) ** 2), rtol=1e-8)
+
+
+def test_oracle_pcg_solves_reduced_system():
+    p = PC.small_ba(3)
+    S, v = PC.reduced_system(p)
+    gidx, degree = PC.camera_blocks(p)
+    _, (C, dis) = PN.block_features(S, gidx, degree)
+    P = PN.assemble(C, dis, None)
+    x, it, rel = PN.pcg(S, v, P, gidx, tol=1e-10)
+    assert rel <= 1e-10 and it < S.shape[0]
+    np.testing.assert_allclose(x, np.linalg.solve(S, v), rtol=1e-7, atol=1e-9 * np.abs(x).max())
