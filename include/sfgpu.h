@@ -307,6 +307,42 @@ int32_t sfg_precond_loss_grad(const float* samples, int64_t n, const float* weig
 int32_t sfg_precond_infer(const float* features, int64_t n, const float* weights, float* out,
                           int32_t device);
 
+/* -------------------------------- batched small problems -----------------------------------
+ * Many independent problems of uneven size solved by one persistent kernel launch (captured in a
+ * CUDA graph): each warp runs the whole LM loop of one problem at a time (the reference would run
+ * one sym::Optimizer<double> per problem, symforce/opt/optimizer.h:72-94), taking problems
+ * largest first from a device queue.  Supported structure: every key POSE3; unary PRIOR_POSE3 /
+ * RANGE_POSE3 factors and BETWEEN_POSE3 factors between consecutive keys, so each Hessian is block
+ * tridiagonal in key order (6 x 6 blocks) and is factored by a block Cholesky recursion, in FP64.
+ * Values of all problems are concatenated in problem order.  No reference counterpart for the
+ * batching itself. */
+typedef struct sfg_batch sfg_batch;
+typedef struct sfg_batch_result_t {
+  int32_t num_iterations;   /* records, as optimization_stats_t.iterations.size() */
+  int32_t best_index;
+  int32_t status;
+  int32_t failure_reason;
+  double initial_error;
+  double best_error;
+} sfg_batch_result_t;
+int32_t sfg_batch_create(const sfg_problem_t* problems, int32_t num_problems,
+                         const sfg_form_params_t* form, sfg_batch** out);
+int32_t sfg_batch_destroy(sfg_batch* b);
+int32_t sfg_batch_storage_dim(const sfg_batch* b, int64_t* storage_dim);
+int32_t sfg_batch_set_values(sfg_batch* b, const double* storage, int64_t n);
+int32_t sfg_batch_get_values(sfg_batch* b, double* storage, int64_t n);
+/* Optimize every problem (results: one entry per problem, may be null); device_ms: CUDA-event time
+ * of the launch. */
+int32_t sfg_batch_optimize(sfg_batch* b, const sfg_optimizer_params_t* params, int32_t num_iterations,
+                           sfg_batch_result_t* results, double* device_ms);
+/* The LM records of one problem from the last optimize call. */
+int32_t sfg_batch_records(sfg_batch* b, int32_t problem, sfg_iteration_t* records, int32_t capacity,
+                          int32_t* count);
+/* Launch-shape autotuner: times one optimize per candidate (warps per CTA x CTAs per SM) on the
+ * handle's own problems and keeps the fastest; returns the chosen warps per CTA and CTAs. */
+int32_t sfg_batch_autotune(sfg_batch* b, const sfg_optimizer_params_t* params, int32_t* warps_per_cta,
+                           int32_t* ctas);
+
 /* -------------------------------- SparseCholeskySolver -------------------------------------
  * The LinearSolver concept on a user CSC lower matrix (symforce/opt/sparse_cholesky/
  * sparse_cholesky_solver.h:28-163): AnalyzeSparsityPattern -> sfg_ldlt_create, Factorize ->

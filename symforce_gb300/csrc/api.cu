@@ -102,6 +102,8 @@ struct sfg_handle {
   float* fac = nullptr;
   float* zout = nullptr;
   void* Pblk = nullptr;
+  int64_t* blk_off = nullptr;  // [nbl][81] S offsets of the group blocks
+  void* Sb = nullptr;          // [nbl][81] group blocks of S
   float* net = nullptr;
   sfg::PcgState* ps = nullptr;
   sfg::PcgDev pcg{};
@@ -169,6 +171,7 @@ void EnqueueRefinement(sfg_handle* h, const void* A, const double* damping, cons
 // Preconditioner blocks of the current reduced system (features, network, assembly).
 template <typename T>
 void EnqueuePrecond(sfg_handle* h, cudaStream_t s) {
+  LaunchGroupBlocks<T>(h->blk_off, int64_t(h->pcg.nbl) * kPrecondBlock * kPrecondBlock, h->S, h->Sb, s);
   LaunchPrecondFeatures<T>(h->pd, h->spmv, h->S, h->rho, h->feats, h->fac, s);
   if (h->pcg_mode == 2) LaunchMlpInfer(h->feats, kPrecondFeatures, h->pd.ng, h->net, h->zout, s);
   LaunchPrecondAssemble<T>(h->pd.ng, h->fac, h->pcg_mode == 2 ? h->zout : nullptr, h->Pblk, s);
@@ -527,13 +530,30 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
                                            std::to_string(cap) + " CTAs)");
     }
     PcgDev& c = h->pcg;
+    const PrecondLayout& PL = h->PL;
     c.pd = h->pd;
-    c.m = h->spmv;
-    c.S = h->S;
+    c.gptr = A.Upload(PL.gptr);
+    c.gent = reinterpret_cast<const int2*>(A.Upload(PL.gent));
+    c.nbl = int(PL.blk_row.size());
+    h->blk_off = A.Upload(PL.blk_off);
+    h->Sb = A.Alloc(PL.blk_off.size() * E);
+    c.Sb = h->Sb;
     c.v = h->v;
     c.P = h->Pblk;
     c.y = h->ydbl;
-    c.z = A.Alloc(size_t(nB) * E);
+    c.yg = A.Zeros<double>(size_t(std::max(h->pd.ng, 1)) * kPrecondBlock);
+    c.z = A.Zeros<char>(size_t(std::max(h->pd.ng, 1)) * kPrecondBlock * E);
+    c.staged = 0;
+    if (h->pcg_grid == 1) {
+      const int nent = PL.gptr.back();
+      const size_t smem = E == 8 ? PcgStagedSmem<double>(h->pd.ng, c.nbl, nent)
+                                 : PcgStagedSmem<float>(h->pd.ng, c.nbl, nent);
+      if (smem > 0) {
+        if (E == 8) ConfigurePcg<double>();
+        else ConfigurePcg<float>();
+        c.staged = int(smem);
+      }
+    }
     c.partials = A.Zeros<double>(4 * size_t(h->pcg_grid));
     c.bar = A.Zeros<unsigned>(2);
     c.ps = h->ps;
@@ -562,7 +582,8 @@ int BodyKernels(const sfg_handle* h) {
   n += h->schur ? 4 /*points, S, rhs, back-substitution*/ : 1 /*negate*/;
   if (h->elem == 4) n += 1 + 4 * h->refine_steps;  // widen; residual, reset, solve, accumulate
   if (h->pcg_mode) {
-    n += 2 /*row coupling, features*/ + (h->pcg_mode == 2 ? 1 : 0) + 1 /*assemble*/ + 1 /*PCG*/;
+    n += 1 /*group blocks*/ + 2 /*row coupling, features*/ + (h->pcg_mode == 2 ? 1 : 0) +
+         1 /*assemble*/ + 1 /*PCG*/;
     if (h->elem == 8) n += 1;  // widen of the fallback solution
   }
   if (h->collect_cap > 0) n += (h->pcg_mode ? 0 : 2) + 1;

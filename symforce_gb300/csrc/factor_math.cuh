@@ -125,6 +125,23 @@ SFG_HD void QuatLogWithJacobian(const T* q, double eps, T* w, T* dw) {
   }
 }
 
+// Pose3 retraction (gen/cpp/sym/ops/pose3/lie_group_ops.cc:69-102): q <- q * exp(w) with the
+// eps-regularised norm, t <- t + dt.  a, o: storage [qx, qy, qz, qw, x, y, z]; d: tangent [w, dt].
+SFG_HD void RetractPose3(const double* a, const double* d, double eps, double* o) {
+  const double n = sqrt(eps * eps + d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  const double c = cos(0.5 * n);
+  const double s = sin(0.5 * n) / n;
+  const double vx = s * d[0], vy = s * d[1], vz = s * d[2];
+  const double a0 = a[0], a1 = a[1], a2 = a[2], a3 = a[3];
+  o[0] = a3 * vx + a0 * c + a1 * vz - a2 * vy;
+  o[1] = a3 * vy - a0 * vz + a1 * c + a2 * vx;
+  o[2] = a3 * vz + a0 * vy - a1 * vx + a2 * c;
+  o[3] = a3 * c - a0 * vx - a1 * vy - a2 * vz;
+  o[4] = a[4] + d[3];
+  o[5] = a[5] + d[4];
+  o[6] = a[6] + d[5];
+}
+
 // ---------------------------------------------------------------------------------------------
 // Factor evaluation: x[slot] points at the key storage, c at the constants (already loaded).
 // r: residual (double), J: RD x TD row-major (T).
@@ -346,18 +363,36 @@ struct FactorEval<SFG_FACTOR_PRIOR_POSE3, T> {
   }
 };
 
+// 1 / sqrt(x) in FP64: on the device an FP32 seed refined by two Newton steps
+// y <- y (3 - x y^2) / 2 (each roughly doubles the correct digits: ~1e-7 -> ~1e-14 -> rounding),
+// which avoids the long FP64 square-root and divide sequences.
+SFG_HD double RsqrtD(double x) {
+#ifdef __CUDA_ARCH__
+  if (!(x > 1e-30 && x < 1e30)) return 1.0 / sqrt(x);
+  double r = double(rsqrtf(float(x)));
+  r = r * (1.5 - 0.5 * x * r * r);
+  r = r * (1.5 - 0.5 * x * r * r);
+  return r;
+#else
+  return 1.0 / sqrt(x);
+#endif
+}
+
 // Range from the Pose3 position to a fixed landmark.
 template <typename T>
 struct FactorEval<SFG_FACTOR_RANGE_POSE3, T> {
   static SFG_HD void Run(const double* const* x, const double* c, double* r, T* J) {
     const double* v = x[0];
     const double dx = v[4] - c[0], dy = v[5] - c[1], dz = v[6] - c[2];
-    const double n = sqrt(dx * dx + dy * dy + dz * dz + c[5]);
+    const double q = dx * dx + dy * dy + dz * dz + c[5];
+    const double inv = RsqrtD(q);
+    const double n = q * inv;
     r[0] = c[4] * (n - c[3]);
     J[0] = J[1] = J[2] = T(0);
-    J[3] = T(c[4] * dx / n);
-    J[4] = T(c[4] * dy / n);
-    J[5] = T(c[4] * dz / n);
+    const double s = c[4] * inv;
+    J[3] = T(s * dx);
+    J[4] = T(s * dy);
+    J[5] = T(s * dz);
   }
 };
 

@@ -54,8 +54,9 @@ PrecondLayout BuildPrecondLayout(const HostProblem& P, const SchurLayout& SL) {
   L.scalar_group.assign(SL.nB, -1);
   L.sdiag_off.assign(SL.nB, -1);
   const BlockPattern& S = SL.Spat;
+  // the reduced system keeps only the lower triangle of its diagonal key blocks up to date
   auto entry_offset = [&](int ka, int ta, int kb, int tb) -> int64_t {
-    if (ka < kb) {
+    if (ka < kb || (ka == kb && ta < tb)) {
       std::swap(ka, kb);
       std::swap(ta, tb);
     }
@@ -95,6 +96,45 @@ PrecondLayout BuildPrecondLayout(const HostProblem& P, const SchurLayout& SL) {
       }
     }
   for (int g = 0; g < L.ng; ++g) L.degree[g] = float(nbr[g].size());
+  // 9 x 9 group blocks of S: stored lower blocks (g, h <= g) with the S offset of each entry, and
+  // per group row its entries (stored block, neighbour, transposed) in neighbour order
+  std::vector<std::vector<int>> lower(L.ng);
+  for (int g = 0; g < L.ng; ++g) {
+    lower[g].push_back(g);
+    for (int h : nbr[g])
+      if (h < g) lower[g].push_back(h);
+    std::sort(lower[g].begin(), lower[g].end());
+  }
+  std::vector<std::vector<std::pair<int, int>>> row_entries(L.ng);  // (neighbour, block)
+  for (int g = 0; g < L.ng; ++g)
+    for (int h : lower[g]) {
+      const int q = int(L.blk_row.size());
+      L.blk_row.push_back(g);
+      L.blk_col.push_back(h);
+      for (int a = 0; a < kB; ++a)
+        for (int b = 0; b < kB; ++b) {
+          const int32_t sa = L.gidx[size_t(g) * kB + a], sb = L.gidx[size_t(h) * kB + b];
+          int64_t o = -1;
+          if (sa >= 0 && sb >= 0) {
+            const int ka = int(std::upper_bound(S.off.begin(), S.off.end(), int64_t(sa)) - S.off.begin()) - 1;
+            const int kb2 = int(std::upper_bound(S.off.begin(), S.off.end(), int64_t(sb)) - S.off.begin()) - 1;
+            o = entry_offset(ka, int(sa - S.off[ka]), kb2, int(sb - S.off[kb2]));
+            if (o < 0) o = -2;
+          }
+          L.blk_off.push_back(o);
+        }
+      row_entries[g].push_back({h, q});
+      if (h != g) row_entries[h].push_back({g, q});
+    }
+  L.gptr.assign(L.ng + 1, 0);
+  for (int g = 0; g < L.ng; ++g) {
+    std::sort(row_entries[g].begin(), row_entries[g].end());
+    for (auto& e : row_entries[g]) {
+      L.gent.push_back(e.second);
+      L.gent.push_back((e.first << 1) | (e.first > g ? 1 : 0));
+    }
+    L.gptr[g + 1] = int32_t(L.gent.size() / 2);
+  }
   return L;
 }
 

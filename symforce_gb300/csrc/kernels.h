@@ -235,20 +235,34 @@ void LaunchCollectSamples(const PrecondDev& pd, const float* feats, const float*
 
 struct PcgDev {
   PrecondDev pd;
-  SpmvDev m;                // symmetric rows of S
-  const void* S;            // T [nvals(S)]
-  const void* v;            // T [nB] rhs
+  const int32_t* gptr;      // [ng + 1] entries of each group row
+  const int2* gent;         // {stored group block, neighbour << 1 | transposed}
+  int nbl;                  // stored (lower) 9 x 9 group blocks
+  const void* Sb;           // T [nbl][81] group blocks of S, row-major
+  const void* v;            // T [nB] rhs (reduced-system order)
   const void* P;            // T [ng][81]
-  double* y;                // [nB] FP64 solution
-  void* z;                  // T [nB] preconditioned residual (read by the product)
+  double* y;                // [nB] FP64 solution (reduced-system order)
+  double* yg;               // [ng][9] FP64 solution by group (read by the residual passes)
+  void* z;                  // T [ng][9] preconditioned residual by group (read by the product)
+  int staged;               // one CTA holding blocks, entries, z and y in shared memory: its
+                            // dynamic shared memory bytes (0: blocks read from L2)
   double* partials;         // [2][grid][2] per-CTA partial sums (double buffered)
-  unsigned* bar;            // [2] grid barrier count / generation (zero before launch)
+  unsigned* bar;            // [2] grid barrier count / generation
   PcgState* ps;
   int* err;                 // device error word
   double tol;               // FP64 relative residual target
   double inner_floor;       // smallest relative reduction asked of one inner solve
   int max_iters, max_outer;
 };
+// Gather the 9 x 9 group blocks of S: Sb[q][e] = S[off[q][e]] (0 where off < 0).
+template <typename T>
+void LaunchGroupBlocks(const int64_t* off, int64_t n, const void* S, void* Sb, cudaStream_t s);
+// Shared memory of a staged (one CTA) PCG launch; 0 if the blocks do not fit.
+template <typename T>
+size_t PcgStagedSmem(int ng, int nbl, int nent);
+// Opt the staged PCG kernel into its shared memory (once per device).
+template <typename T>
+void ConfigurePcg();
 // Grid shape of the PCG kernel for ng blocks (cooperative when grid > 1).
 void PcgShape(int ng, int num_sms, int* grid, int* threads);
 // CTAs of the PCG kernel that fit on the device at once (a cooperative launch needs all of them).
@@ -257,6 +271,37 @@ int PcgMaxResidentCtas(int threads, int num_sms);
 template <typename T>
 cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s);
 void LaunchPcgBegin(PcgState* ps, cudaStream_t s);
+
+// ---------------------------------------------------------------- batched problems (kernels_batch.cu)
+// Doubles of one warp slot's workspace per pose of the largest problem.
+constexpr int kBatchWsPerPose = 3 * 7 + 3 * 36 + 3 * 36 + 3 * 6 + 27 + 27 + 6 + 6 + 6 + 6 + 36 + 36 + 6;
+
+struct BatchLmDev {
+  int nprob;
+  int nmax;                    // poses of the largest problem
+  const int32_t* order;        // problems, largest first
+  const int32_t* n;            // poses per problem
+  const int64_t* pose0;        // first pose (global index) of each problem
+  const int64_t* un_ptr;       // [total poses + 1] unary factors of each pose
+  const int8_t* un_kind;       // SFG_FACTOR_PRIOR_POSE3 / SFG_FACTOR_RANGE_POSE3
+  const int64_t* un_coff;      // offset of the factor's constants
+  const int64_t* bw_ptr;       // [total poses + 1] between factors from pose k to k + 1
+  const int8_t* bw_rev;        // 1: the factor's keys are (k + 1, k)
+  const int64_t* bw_coff;
+  const double* consts;
+  const double* values_in;     // [total poses][7]
+  double* values_out;          // best values
+  LmState* st;                 // [nprob]
+  sfg_iteration_t* records;    // [nprob][rec_cap] (null: none)
+  int rec_cap;
+  double* ws;                  // [slots][kBatchWsPerPose * nmax]
+  int* counter;                // problem queue head (zero before launch)
+};
+// Launch shapes (kernel instantiations): warps per CTA x register budget.
+int BatchShapes();
+int BatchShapeWarps(int shape);
+int BatchMaxCtasPerSm(int shape);
+void LaunchBatchLm(const BatchLmDev& d, const LmParams* p, int ctas, int shape, cudaStream_t s);
 
 // ---------------------------------------------------------------- network training (kernels_mlp.cu)
 // C[m][n] = sum_k A(m, k) B(k, n) (+ bias[n]) then ReLU, or times (mask[m][n] > 0); A(m, k) at

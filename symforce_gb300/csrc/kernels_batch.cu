@@ -1,0 +1,410 @@
+// Thousands of independent small problems in one persistent launch.
+//
+// Each warp takes a problem from a device queue (largest first) and runs its entire
+// Levenberg-Marquardt loop (symforce/opt/levenberg_marquardt_solver.tcc:138-343, through the same
+// lm_logic.cuh bookkeeping as the single-problem graph) before taking the next one, so uneven
+// problem sizes balance across the GPU without any host round trip.  Supported problems are Pose3
+// chains: unary prior / range factors and between factors on consecutive poses, so the Hessian is
+// block tridiagonal (6 x 6 blocks) in key order.  Per iteration the warp
+//   - linearizes: lane k accumulates pose k's unary factors and the between factor (k, k+1), whose
+//     pose-(k+1) part is handed over through the workspace (fixed order, no atomics);
+//   - factors H + D block by block, C_k C_k^T = A_kk + D_k - B_k B_k^T with B_k = A_k,k-1 C_k-1^-T,
+//     keeping C_k^-1 so that both triangular solves are small matrix-vector products;
+//   - retracts, relinearizes the new state and decides.
+// Everything is FP64; reciprocal square roots start from an FP32 seed refined by two Newton steps
+// (y <- y (3 - x y^2) / 2), which reach FP64 accuracy without the FP64 divide / square-root
+// sequences, whose latency dominates these short dependent chains on GB300.
+#include "factor_math.cuh"
+#include <algorithm>
+
+#include "kernels.h"
+#include "lm_logic.cuh"
+
+namespace sfg {
+
+namespace {
+
+constexpr int kScratch = 6 * 36 + 3 * 6;  // per-warp shared scratch (doubles)
+
+struct Ws {
+  double *vals, *Hd, *Ho, *g, *carry, *bwa, *damp, *maxd, *upd, *last, *Ci, *B, *y;
+};
+
+__device__ __forceinline__ Ws SlotWs(const BatchLmDev& d, int slot) {
+  const size_t n = size_t(d.nmax);
+  double* w = d.ws + size_t(slot) * kBatchWsPerPose * n;
+  Ws s;
+  s.vals = w;  w += 3 * 7 * n;
+  s.Hd = w;    w += 3 * 36 * n;
+  s.Ho = w;    w += 3 * 36 * n;
+  s.g = w;     w += 3 * 6 * n;
+  s.carry = w; w += 27 * n;
+  s.bwa = w;   w += 27 * n;
+  s.damp = w;  w += 6 * n;
+  s.maxd = w;  w += 6 * n;
+  s.upd = w;   w += 6 * n;
+  s.last = w;  w += 6 * n;
+  s.Ci = w;    w += 36 * n;
+  s.B = w;     w += 36 * n;
+  s.y = w;     w += 6 * n;
+  return s;
+}
+
+__device__ __forceinline__ int Tri(int i, int j) { return i * (i + 1) / 2 + j; }
+
+// Butterfly sum: every lane gets the same bits (IEEE addition is commutative).
+__device__ __forceinline__ double WarpSum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Linearize state block s: H (full diagonal blocks, sub-diagonal blocks), rhs, and 0.5 |r|^2.
+// Two passes keep few values live per lane: the between factors (lane per pose k, factor (k, k+1))
+// write their three blocks and two rhs parts to the workspace; the unary factors (lane per pose)
+// accumulate in registers and add the between parts of their pose.
+__device__ double Linearize(const BatchLmDev& d, const Ws& w, int64_t pose0, int n, int s, int lane) {
+  const size_t N = size_t(d.nmax);
+  const double* V = w.vals + size_t(s) * 7 * N;
+  double* Hd = w.Hd + size_t(s) * 36 * N;
+  double* Ho = w.Ho + size_t(s) * 36 * N;
+  double* g = w.g + size_t(s) * 6 * N;
+  double err = 0.0;
+  for (int k = lane; k + 1 < n; k += 32) {
+    const int64_t gp = pose0 + k;
+    double* own = w.bwa + size_t(k) * 27;       // pose k's part: H lower (21) + rhs (6)
+    double* cr = w.carry + size_t(k + 1) * 27;  // pose k+1's part
+    double* ho = Ho + size_t(k + 1) * 36;       // block (k+1, k)
+    for (int i = 0; i < 27; ++i) own[i] = cr[i] = 0.0;
+    for (int i = 0; i < 36; ++i) ho[i] = 0.0;
+    for (int64_t f = d.bw_ptr[gp]; f < d.bw_ptr[gp + 1]; ++f) {
+      const int rev = d.bw_rev[f];
+      const double* x[2] = {V + 7 * (rev ? k + 1 : k), V + 7 * (rev ? k : k + 1)};
+      double r[6], J[72];
+      FactorEval<SFG_FACTOR_BETWEEN_POSE3, double>::Run(x, d.consts + d.bw_coff[f], r, J);
+      const int ca = rev ? 6 : 0, cb = rev ? 0 : 6;
+      for (int i = 0; i < 6; ++i) {
+        err += r[i] * r[i];
+        for (int a = 0; a < 6; ++a) {
+          const double ja = J[i * 12 + ca + a], jb = J[i * 12 + cb + a];
+          own[21 + a] += ja * r[i];
+          cr[21 + a] += jb * r[i];
+          for (int b = 0; b <= a; ++b) {
+            own[Tri(a, b)] += ja * J[i * 12 + ca + b];
+            cr[Tri(a, b)] += jb * J[i * 12 + cb + b];
+          }
+          for (int b = 0; b < 6; ++b) ho[a * 6 + b] += jb * J[i * 12 + ca + b];
+        }
+      }
+    }
+  }
+  __syncwarp();
+  for (int k = lane; k < n; k += 32) {
+    const int64_t gp = pose0 + k;
+    double h[21], gk[6];
+#pragma unroll
+    for (int i = 0; i < 21; ++i) h[i] = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) gk[i] = 0.0;
+    for (int64_t f = d.un_ptr[gp]; f < d.un_ptr[gp + 1]; ++f) {
+      const double* c = d.consts + d.un_coff[f];
+      const double* x[1] = {V + 7 * k};
+      if (d.un_kind[f] == SFG_FACTOR_RANGE_POSE3) {
+        double r[1], J[6];
+        FactorEval<SFG_FACTOR_RANGE_POSE3, double>::Run(x, c, r, J);
+        err += r[0] * r[0];
+        // the range Jacobian has no rotation part: only the translation block changes
+#pragma unroll
+        for (int a = 3; a < 6; ++a) {
+          gk[a] += J[a] * r[0];
+#pragma unroll
+          for (int b = 3; b <= a; ++b) h[Tri(a, b)] += J[a] * J[b];
+        }
+      } else {
+        double r[6], J[36];
+        FactorEval<SFG_FACTOR_PRIOR_POSE3, double>::Run(x, c, r, J);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+          err += r[i] * r[i];
+#pragma unroll
+          for (int a = 0; a < 6; ++a) {
+            gk[a] += J[i * 6 + a] * r[i];
+#pragma unroll
+            for (int b = 0; b <= a; ++b) h[Tri(a, b)] += J[i * 6 + a] * J[i * 6 + b];
+          }
+        }
+      }
+    }
+    if (k + 1 < n) {
+      const double* own = w.bwa + size_t(k) * 27;
+#pragma unroll
+      for (int i = 0; i < 21; ++i) h[i] += own[i];
+#pragma unroll
+      for (int a = 0; a < 6; ++a) gk[a] += own[21 + a];
+    }
+    if (k > 0) {
+      const double* cr = w.carry + size_t(k) * 27;
+#pragma unroll
+      for (int i = 0; i < 21; ++i) h[i] += cr[i];
+#pragma unroll
+      for (int a = 0; a < 6; ++a) gk[a] += cr[21 + a];
+    }
+    double* hd = Hd + size_t(k) * 36;
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+#pragma unroll
+      for (int b = 0; b <= a; ++b) hd[a * 6 + b] = hd[b * 6 + a] = h[Tri(a, b)];
+      g[size_t(k) * 6 + a] = gk[a];
+    }
+  }
+  __syncwarp();
+  return 0.5 * WarpSum(err);
+}
+
+// (H + D) x = g by block Cholesky; writes upd = -x.
+__device__ void FactorSolve(const BatchLmDev& d, const Ws& w, int n, int s, int lane, double* sm) {
+  const size_t N = size_t(d.nmax);
+  const double* Hd = w.Hd + size_t(s) * 36 * N;
+  const double* Ho = w.Ho + size_t(s) * 36 * N;
+  const double* g = w.g + size_t(s) * 6 * N;
+  double* sA = sm;
+  double* sC = sm + 36;
+  double* sCi = sm + 72;       // C_k^-1 (lower)
+  double* sCiPrev = sm + 108;  // C_k-1^-1
+  double* sB = sm + 144;
+  double* sInv = sm + 180;     // 1 / C_jj
+  double* sv = sm + 186;       // 6-vectors
+  double* sv2 = sm + 192;
+  for (int k = 0; k < n; ++k) {
+    // B = A_k,k-1 C_k-1^-T
+    if (k > 0) {
+      const double* O = Ho + size_t(k) * 36;
+      for (int e = lane; e < 36; e += 32) {
+        const int i = e / 6, j = e - 6 * (e / 6);
+        double acc = 0.0;
+        for (int p = 0; p <= j; ++p) acc += O[i * 6 + p] * sCiPrev[j * 6 + p];
+        sB[e] = acc;
+        w.B[size_t(k) * 36 + e] = acc;
+      }
+    }
+    __syncwarp();
+    if (lane < 21) {
+      int i = 0;
+      while (Tri(i + 1, 0) <= lane) ++i;
+      const int j = lane - Tri(i, 0);
+      double a = Hd[size_t(k) * 36 + i * 6 + j] + (i == j ? w.damp[size_t(k) * 6 + i] : 0.0);
+      if (k > 0)
+        for (int p = 0; p < 6; ++p) a -= sB[i * 6 + p] * sB[j * 6 + p];
+      sA[i * 6 + j] = a;
+    }
+    __syncwarp();
+    for (int j = 0; j < 6; ++j) {
+      if (lane == j) {
+        double t = sA[j * 6 + j];
+        for (int p = 0; p < j; ++p) t -= sC[j * 6 + p] * sC[j * 6 + p];
+        const double r = RsqrtD(t);
+        sC[j * 6 + j] = t * r;
+        sInv[j] = r;
+      }
+      __syncwarp();
+      if (lane > j && lane < 6) {
+        double t = sA[lane * 6 + j];
+        for (int p = 0; p < j; ++p) t -= sC[lane * 6 + p] * sC[j * 6 + p];
+        sC[lane * 6 + j] = t * sInv[j];
+      }
+      __syncwarp();
+    }
+    // C^-1: lane c computes column c
+    if (lane < 6) {
+      const int c = lane;
+      for (int i = 0; i < 6; ++i) {
+        double v;
+        if (i < c) v = 0.0;
+        else if (i == c) v = sInv[c];
+        else {
+          double t = 0.0;
+          for (int p = c; p < i; ++p) t += sC[i * 6 + p] * sCi[p * 6 + c];
+          v = -t * sInv[i];
+        }
+        sCi[i * 6 + c] = v;
+      }
+    }
+    __syncwarp();
+    for (int e = lane; e < 36; e += 32) {
+      w.Ci[size_t(k) * 36 + e] = sCi[e];
+      sCiPrev[e] = sCi[e];
+    }
+    __syncwarp();
+  }
+  // forward: y_k = C_k^-1 (g_k - B_k y_k-1)
+  for (int k = 0; k < n; ++k) {
+    if (lane < 6) {
+      double t = g[size_t(k) * 6 + lane];
+      if (k > 0)
+        for (int j = 0; j < 6; ++j) t -= w.B[size_t(k) * 36 + lane * 6 + j] * sv[j];
+      sv2[lane] = t;
+    }
+    __syncwarp();
+    if (lane < 6) {
+      double t = 0.0;
+      for (int j = 0; j <= lane; ++j) t += w.Ci[size_t(k) * 36 + lane * 6 + j] * sv2[j];
+      w.y[size_t(k) * 6 + lane] = t;
+    }
+    __syncwarp();
+    if (lane < 6) sv[lane] = w.y[size_t(k) * 6 + lane];
+    __syncwarp();
+  }
+  // backward: x_k = C_k^-T (y_k - B_k+1^T x_k+1)
+  for (int k = n - 1; k >= 0; --k) {
+    if (lane < 6) {
+      double t = w.y[size_t(k) * 6 + lane];
+      if (k + 1 < n)
+        for (int i = 0; i < 6; ++i) t -= w.B[size_t(k + 1) * 36 + i * 6 + lane] * sv[i];
+      sv2[lane] = t;
+    }
+    __syncwarp();
+    if (lane < 6) {
+      double t = 0.0;
+      for (int i = lane; i < 6; ++i) t += w.Ci[size_t(k) * 36 + i * 6 + lane] * sv2[i];
+      sv[lane] = t;  // read by the lanes only after the next __syncwarp
+      w.upd[size_t(k) * 6 + lane] = -t;
+    }
+    __syncwarp();
+  }
+}
+
+template <int kWarps, int kMinBlocks>
+__global__ void __launch_bounds__(32 * kWarps, kMinBlocks) BatchLmKernel(BatchLmDev d, const LmParams* pp) {
+  __shared__ LmState sst[kWarps];
+  __shared__ double sscr[kWarps][kScratch];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slot = blockIdx.x * (blockDim.x >> 5) + warp;
+  const LmParams p = *pp;
+  const Ws w = SlotWs(d, slot);
+  LmState& st = sst[warp];
+  double* sm = sscr[warp];
+  const size_t NM = size_t(d.nmax);
+  for (;;) {
+    int job = 0;
+    if (lane == 0) job = atomicAdd(d.counter, 1);
+    job = __shfl_sync(0xffffffffu, job, 0);
+    if (job >= d.nprob) break;
+    const int prob = d.order[job];
+    const int n = d.n[prob];
+    const int64_t pose0 = d.pose0[prob];
+    sfg_iteration_t* rec = d.records ? d.records + size_t(prob) * d.rec_cap : nullptr;
+    if (lane == 0) {
+      st = LmState{};
+      LmBegin(p, st, 1);
+    }
+    __syncwarp();
+    {
+      const int init = st.init_idx;
+      for (int i = lane; i < 7 * n; i += 32) w.vals[size_t(init) * 7 * NM + i] = d.values_in[pose0 * 7 + i];
+    }
+    __syncwarp();
+    {
+      const int init = st.init_idx;
+      const double e = Linearize(d, w, pose0, n, init, lane);
+      if (lane == 0) st.error[init] = e;
+    }
+    __syncwarp();
+    int go = 0;
+    if (lane == 0) go = LmFirstRecord(p, st, rec);
+    go = __shfl_sync(0xffffffffu, go, 0);
+    while (go) {
+      const int init = st.init_idx, nw = st.new_idx;
+      const double* Hd = w.Hd + size_t(init) * 36 * NM;
+      for (int i = lane; i < 6 * n; i += 32) {
+        const int k = i / 6, a = i - 6 * (i / 6);
+        w.damp[i] = LmDamping(p, st, Hd[size_t(k) * 36 + a * 7], w.maxd + i);
+      }
+      __syncwarp();
+      FactorSolve(d, w, n, init, lane, sm);
+      for (int k = lane; k < n; k += 32)
+        RetractPose3(w.vals + size_t(init) * 7 * NM + 7 * k, w.upd + 6 * k, p.epsilon,
+                     w.vals + size_t(nw) * 7 * NM + 7 * k);
+      __syncwarp();
+      const double e_new = Linearize(d, w, pose0, n, nw, lane);
+      // u.(rhs - d.u) with rhs of the Init block, and the bold-update products
+      const double* g = w.g + size_t(init) * 6 * NM;
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+      for (int i = lane; i < 6 * n; i += 32) {
+        const double u = w.upd[i];
+        s0 += u * (g[i] - w.damp[i] * u);
+        if (p.enable_bold_updates) {
+          const double l = w.last[i];
+          s1 += u * l;
+          s2 += u * u;
+          s3 += l * l;
+        }
+      }
+      double sums[4] = {WarpSum(s0), WarpSum(s1), WarpSum(s2), WarpSum(s3)};
+      int done = 0, copy = 0;
+      if (lane == 0) {
+        st.error[nw] = e_new;
+        done = LmDecide(p, st, rec, sums, &copy);
+      }
+      done = __shfl_sync(0xffffffffu, done, 0);
+      copy = __shfl_sync(0xffffffffu, copy, 0);
+      if (copy)
+        for (int i = lane; i < 6 * n; i += 32) w.last[i] = w.upd[i];
+      __syncwarp();
+      go = !done;
+    }
+    {
+      const int best = st.best_idx;
+      for (int i = lane; i < 7 * n; i += 32) d.values_out[pose0 * 7 + i] = w.vals[size_t(best) * 7 * NM + i];
+    }
+    if (lane == 0) d.st[prob] = st;
+    __syncwarp();
+  }
+}
+
+}  // namespace
+
+// Launch shapes the autotuner chooses from: warps per CTA and the register budget implied by the
+// minimum resident CTAs per SM (fewer registers: more warps in flight to hide FP64 latency).
+template <int W, int B>
+struct Shape {
+  static int MaxCtasPerSm() {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, BatchLmKernel<W, B>, 32 * W, 0) != cudaSuccess)
+      return 0;
+    return per_sm;
+  }
+  static void Launch(const BatchLmDev& d, const LmParams* p, int ctas, cudaStream_t s) {
+    BatchLmKernel<W, B><<<ctas, 32 * W, 0, s>>>(d, p);
+  }
+};
+
+int BatchShapes() { return 5; }
+
+int BatchShapeWarps(int shape) {
+  constexpr int w[5] = {8, 4, 2, 4, 2};
+  return shape >= 0 && shape < 5 ? w[shape] : 0;
+}
+
+int BatchMaxCtasPerSm(int shape) {
+  switch (shape) {
+    case 0: return Shape<8, 1>::MaxCtasPerSm();
+    case 1: return Shape<4, 4>::MaxCtasPerSm();
+    case 2: return Shape<2, 8>::MaxCtasPerSm();
+    case 3: return Shape<4, 6>::MaxCtasPerSm();
+    case 4: return Shape<2, 16>::MaxCtasPerSm();
+  }
+  return 0;
+}
+
+void LaunchBatchLm(const BatchLmDev& d, const LmParams* p, int ctas, int shape, cudaStream_t s) {
+  cudaMemsetAsync(d.counter, 0, sizeof(int), s);
+  switch (shape) {
+    case 0: Shape<8, 1>::Launch(d, p, ctas, s); break;
+    case 1: Shape<4, 4>::Launch(d, p, ctas, s); break;
+    case 2: Shape<2, 8>::Launch(d, p, ctas, s); break;
+    case 3: Shape<4, 6>::Launch(d, p, ctas, s); break;
+    case 4: Shape<2, 16>::Launch(d, p, ctas, s); break;
+  }
+}
+
+}  // namespace sfg

@@ -7,6 +7,7 @@
 #include <algorithm>
 
 #include "kernels.h"
+#include "lm_logic.cuh"
 
 namespace sfg {
 
@@ -14,12 +15,6 @@ namespace {
 
 constexpr int kDeltaParts = 64;
 constexpr int kDeltaThreads = 256;
-
-__device__ __forceinline__ unsigned long long GlobalTimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 
 // DampHessian (symforce/opt/levenberg_marquardt_solver.tcc:22-54): damping vector from the
 // undamped diagonal of the Init block's Hessian.  The Hessian itself is left untouched: the
@@ -29,24 +24,8 @@ __global__ void DampingKernel(DampDev d, const T* hess, int64_t nvals, const LmP
                               const LmState* st) {
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= d.N) return;
-  const double lambda = st->lambda;
   const double undamped = double(hess[int64_t(st->init_idx) * nvals + d.diag_off[k]]);
-  double damp = 0.0;
-  if (p->use_diagonal_damping) {
-    if (p->keep_max_diagonal_damping) {
-      double m;
-      if (!st->have_max_diagonal) {
-        m = fmax(undamped, p->diagonal_damping_min);
-      } else {
-        m = fmax(d.max_diagonal[k], undamped);
-      }
-      d.max_diagonal[k] = m;
-      damp = m * lambda;
-    } else {
-      damp = fmax(undamped, p->diagonal_damping_min) * lambda;
-    }
-  }
-  if (p->use_unit_damping) damp += lambda;
+  const double damp = LmDamping(*p, *st, undamped, d.max_diagonal + k);
   d.damping[k] = damp;
 }
 
@@ -67,22 +46,9 @@ __global__ void RetractKernel(RetractDev r, const LmParams* p, const LmState* st
       o[3] = a[3] + d[2];
       break;
     }
-    case SFG_KEY_POSE3: {  // gen/cpp/sym/ops/pose3/lie_group_ops.cc:69-102
-      const double eps = p->epsilon;
-      const double n = sqrt(eps * eps + d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-      const double c = cos(0.5 * n);
-      const double s = sin(0.5 * n) / n;
-      const double vx = s * d[0], vy = s * d[1], vz = s * d[2];
-      const double a0 = a[0], a1 = a[1], a2 = a[2], a3 = a[3];
-      o[0] = a3 * vx + a0 * c + a1 * vz - a2 * vy;
-      o[1] = a3 * vy - a0 * vz + a1 * c + a2 * vx;
-      o[2] = a3 * vz + a0 * vy - a1 * vx + a2 * c;
-      o[3] = a3 * c - a0 * vx - a1 * vy - a2 * vz;
-      o[4] = a[4] + d[3];
-      o[5] = a[5] + d[4];
-      o[6] = a[6] + d[5];
+    case SFG_KEY_POSE3:  // gen/cpp/sym/ops/pose3/lie_group_ops.cc:69-102
+      RetractPose3(a, d, p->epsilon, o);
       break;
-    }
     default: {
       const int n = r.key_type[k];  // VEC1..VEC3: the type value is the dimension
       for (int i = 0; i < n; ++i) o[i] = a[i] + d[i];
@@ -142,58 +108,14 @@ __global__ void CopyValuesKernel(const double* src, double* values, int64_t S, c
 
 // Reset (symforce/opt/levenberg_marquardt_solver.h:163-175) + Step of the first Iterate.
 __global__ void BeginKernel(const LmParams* p, LmState* st, int reset_indices) {
-  if (reset_indices) {
-    st->init_idx = 0;
-    st->new_idx = 1;
-    st->best_idx = 0;
-    st->free_idx = 2;
-  }
-  st->lambda = p->initial_lambda;
-  st->nu = p->dynamic_beta;
-  st->have_max_diagonal = 0;
-  st->have_last_update = 0;
-  st->num_records = 0;
-  st->best_index = 0;
-  st->status = 0;
-  st->failure_reason = 0;
-  st->done = 0;
-  st->device_error = 0;
-  st->max_iterations = p->iterations;
-  st->t_start = GlobalTimer();
-  // Step(): swap New and Init; iteration_ = 0
-  const int t = st->init_idx;
-  st->init_idx = st->new_idx;
-  st->new_idx = t;
-  st->iteration = 0;
+  LmBegin(*p, *st, reset_indices);
 }
 
 // First Iterate after relinearizing Init: SetBestToInit, the iteration -1 record, and the
 // INITIAL_ERROR_NOT_FINITE check (symforce/opt/levenberg_marquardt_solver.tcc:151-186).
 __global__ void FirstRecordKernel(const LmParams* p, LmState* st, sfg_iteration_t* rec,
                                   cudaGraphConditionalHandle h, int use_cond) {
-  if (st->best_idx != st->init_idx) {
-    if (st->best_idx != st->new_idx) st->free_idx = st->best_idx;
-    st->best_idx = st->init_idx;
-  }
-  const double e = st->error[st->init_idx];
-  sfg_iteration_t r{};
-  r.iteration = -1;
-  r.new_error = e;
-  r.current_lambda = st->lambda;
-  r.best_error = e;
-  r.elapsed_ms = double(GlobalTimer() - st->t_start) * 1e-6;
-  rec[0] = r;
-  st->num_records = 1;
-  int go = 1;
-  if (!isfinite(e)) {
-    st->status = SFG_STATUS_FAILED;
-    st->failure_reason = SFG_FAILURE_INITIAL_ERROR_NOT_FINITE;
-    st->done = 1;
-    go = 0;
-  } else if (st->max_iterations <= 0) {
-    st->done = 1;
-    go = 0;
-  }
+  const int go = LmFirstRecord(*p, *st, rec);
   if (use_cond) cudaGraphSetConditional(h, go);
 }
 
@@ -206,95 +128,10 @@ __global__ void DecideKernel(const LmParams* p, LmState* st, sfg_iteration_t* re
     double sums[4] = {0, 0, 0, 0};
     for (int c = 0; c < 4; ++c)
       for (int q = 0; q < nparts; ++q) sums[c] += partials[c * nparts + q];
-    const double eps = p->epsilon;
-    const int init = st->init_idx, nw = st->new_idx;
-    const double e_init = st->error[init];
-    const double e_new = st->error[nw];
-    const double relative_reduction = (e_init - e_new) / (e_init + eps);
-    const double new_error_linear = e_init + 0.5 * sums[0];
-    const double gain_ratio = (e_init - e_new) / (e_init - new_error_linear);
-    sfg_iteration_t r{};
-    r.iteration = st->iteration;
-    r.current_lambda = st->lambda;
-    r.new_error = e_new;
-    r.new_error_linear = new_error_linear;
-    r.relative_reduction = relative_reduction;
-    int status = 0, reason = 0;
-    if ((relative_reduction > -p->early_exit_min_reduction / 10 &&
-         relative_reduction < p->early_exit_min_reduction) ||
-        e_new < p->early_exit_min_absolute_error) {
-      status = SFG_STATUS_SUCCESS;
-    }
-    bool accept = relative_reduction > 0;
-    double angle = 0;
-    if (p->enable_bold_updates && st->have_last_update && !accept) {
-      angle = sums[1] / (sqrt(sums[3]) * sqrt(sums[2]));
-      accept = ((1 - angle) * (1 - angle) * e_new) <= st->error[st->best_idx];
-    }
-    if (!accept && st->lambda >= p->lambda_upper_bound) {
-      status = SFG_STATUS_FAILED;
-      reason = SFG_FAILURE_LAMBDA_OUT_OF_BOUNDS;
-    }
-    double lambda = st->lambda;
-    if (!accept) {
-      if (p->lambda_update_type == SFG_LAMBDA_UPDATE_STATIC) {
-        lambda *= p->lambda_up_factor;
-      } else {
-        lambda *= st->nu;
-        st->nu *= 2;
-      }
-      st->init_idx = nw;  // SwapNewAndInit
-      st->new_idx = init;
-    } else {
-      if (p->lambda_update_type == SFG_LAMBDA_UPDATE_STATIC) {
-        lambda *= p->lambda_down_factor;
-      } else {
-        lambda *= fmax(1.0 / p->dynamic_gamma,
-                       1.0 - (p->dynamic_beta - 1) * pow(2 * gain_ratio - 1, double(p->dynamic_p)));
-        st->nu = 2;
-      }
-      st->have_last_update = 1;
-      if (st->error[nw] <= st->error[st->best_idx]) {  // SetBestToNew
-        if (st->best_idx != nw) {
-          if (st->best_idx != init) st->free_idx = st->best_idx;
-          st->best_idx = nw;
-        }
-        st->best_index = st->num_records;
-      }
-      if (st->best_idx == st->init_idx) {  // SetInitToNotBest
-        st->init_idx = st->free_idx;
-        st->free_idx = st->best_idx;
-      }
-    }
-    lambda = fmin(fmax(lambda, p->lambda_lower_bound), p->lambda_upper_bound);
-    st->lambda = lambda;
-    if (p->use_diagonal_damping && p->keep_max_diagonal_damping) st->have_max_diagonal = 1;
-    r.update_angle_change = angle;
-    r.update_accepted = accept ? 1 : 0;
-    r.best_error = st->error[st->best_idx];
-    r.elapsed_ms = double(GlobalTimer() - st->t_start) * 1e-6;
-    records[st->num_records] = r;
-    st->num_records += 1;
-    int done = 0;
-    if (status != 0) {
-      st->status = status;
-      st->failure_reason = reason;
-      done = 1;
-    } else if (st->iteration + 1 >= st->max_iterations) {
-      st->status = SFG_STATUS_HIT_ITERATION_LIMIT;
-      st->failure_reason = 0;
-      done = 1;
-    }
-    if (st->device_error) done = 1;
-    st->done = done;
-    if (!done) {  // Step() of the next Iterate
-      const int t = st->init_idx;
-      st->init_idx = st->new_idx;
-      st->new_idx = t;
-      st->iteration += 1;
-    }
+    int copy = 0;
+    const int done = LmDecide(*p, *st, records, sums, &copy);
     if (use_cond) cudaGraphSetConditional(h, done ? 0 : 1);
-    s_copy = (accept && p->enable_bold_updates) ? 1 : 0;
+    s_copy = copy;
   }
   __syncthreads();
   if (s_copy)

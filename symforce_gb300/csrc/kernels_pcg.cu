@@ -27,6 +27,7 @@ constexpr int kB = kPrecondBlock;
 constexpr unsigned kSpinLimit = 1u << 22;
 constexpr float kDiagShift = 0.54132485f;  // ln(e - 1): softplus(kDiagShift) = 1
 constexpr int kPcgMultiThreads = 256;
+constexpr size_t kPcgStagedMax = 200 * 1024;  // shared memory of a staged one-CTA solve
 
 __device__ __forceinline__ float Softplus(float x) { return x > 20.f ? x : log1pf(expf(x)); }
 
@@ -301,55 +302,6 @@ __device__ void GridBarrier(unsigned* bar, unsigned nblocks, int* err) {
   __syncthreads();
 }
 
-struct PcgSmem {
-  double2 red[32];
-  double2 out;
-};
-
-// Sum of (a, b) over every thread of the grid, the same bits in every thread.
-__device__ double2 GridSum2(double a, double b, const PcgDev& d, int& seq, PcgSmem& sm) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  const int grid = gridDim.x;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_down_sync(0xffffffffu, a, o);
-    b += __shfl_down_sync(0xffffffffu, b, o);
-  }
-  __syncthreads();  // readers of the previous result are done
-  if (lane == 0) sm.red[warp] = make_double2(a, b);
-  __syncthreads();
-  double2* part = reinterpret_cast<double2*>(d.partials) + size_t(seq & 1) * grid;
-  if (threadIdx.x == 0) {
-    double2 t = make_double2(0.0, 0.0);
-    for (int w = 0; w < nwarp; ++w) {
-      t.x += sm.red[w].x;
-      t.y += sm.red[w].y;
-    }
-    if (grid == 1) sm.out = t;
-    else __stcg(part + blockIdx.x, t);
-  }
-  if (grid > 1) {
-    GridBarrier(d.bar, grid, d.err);
-    if (warp == 0) {
-      double2 t = make_double2(0.0, 0.0);
-      for (int q = lane; q < grid; q += 32) {
-        const double2 v = __ldcg(part + q);
-        t.x += v.x;
-        t.y += v.y;
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        t.x += __shfl_down_sync(0xffffffffu, t.x, o);
-        t.y += __shfl_down_sync(0xffffffffu, t.y, o);
-      }
-      if (lane == 0) sm.out = t;
-    }
-  }
-  __syncthreads();
-  ++seq;
-  return sm.out;
-}
-
 template <typename T>
 __device__ __forceinline__ T ApplyBlock(const T (&prow)[kB], T r, int gbase) {
   T acc = T(0);
@@ -358,106 +310,257 @@ __device__ __forceinline__ T ApplyBlock(const T (&prow)[kB], T r, int gbase) {
   return acc;
 }
 
+// Vectors that other threads wrote in this launch: shared memory (staged) or L2 (grid-wide).
+template <bool kStaged, typename V>
+__device__ __forceinline__ V LdX(const V* p) {
+  if constexpr (kStaged) return *p;
+  else return __ldcg(p);
+}
+template <bool kStaged, typename V>
+__device__ __forceinline__ void StX(V* p, V v) {
+  if constexpr (kStaged) *p = v;
+  else __stcg(p, v);
+}
+
+// Row a of group row g of S times x (group-major): the stored lower blocks of the row, and the
+// transposed stored blocks (h, g) for the neighbours h > g (addressing chosen without branching).
+template <typename Acc, bool kStaged, typename T, typename V>
+__device__ __forceinline__ Acc GroupRow(const T* Sb, const int2* gent, int e0, int e1, int a,
+                                        const V* x) {
+  Acc acc = Acc(0);
+  for (int e = e0; e < e1; ++e) {
+    const int2 en = gent[e];
+    const int tr = en.y & 1;
+    const T* row = Sb + size_t(en.x) * (kB * kB) + (tr ? a : a * kB);
+    const int step = tr ? kB : 1;
+    const V* xh = x + size_t(en.y >> 1) * kB;
+#pragma unroll
+    for (int b = 0; b < kB; ++b) acc += Acc(row[b * step]) * Acc(LdX<kStaged>(xh + b));
+  }
+  return acc;
+}
+
+struct PcgShared {
+  double2 red[32];
+  double vnorm, target, rel;
+  float rzf, alphaf, betaf, targetf;
+  double rzd, alphad, betad;
+  int iters, stop, broke, converged;
+};
+
+// The scalars of the inner iteration in the matrix precision.
 template <typename T>
+struct InnerScalars;
+template <>
+struct InnerScalars<float> {
+  __device__ static float& rz(PcgShared& s) { return s.rzf; }
+  __device__ static float& alpha(PcgShared& s) { return s.alphaf; }
+  __device__ static float& beta(PcgShared& s) { return s.betaf; }
+  __device__ static float target(const PcgShared& s) { return s.targetf; }
+  __device__ static constexpr float big() { return 1e37f; }
+};
+template <>
+struct InnerScalars<double> {
+  __device__ static double& rz(PcgShared& s) { return s.rzd; }
+  __device__ static double& alpha(PcgShared& s) { return s.alphad; }
+  __device__ static double& beta(PcgShared& s) { return s.betad; }
+  __device__ static double target(const PcgShared& s) { return s.target; }
+  __device__ static constexpr double big() { return 1e300; }
+};
+
+// Sum (a, b) over the grid: a warp tree in Acc, the CTA's warps in order (warp 0, Acc), and the CTAs
+// in order (every CTA's warp 0, in FP64, so every CTA gets the same bits).  Thread 0 of every CTA
+// then runs epi(sum_a, sum_b) (in Acc for one CTA, FP64 across CTAs), which writes the scalars the
+// threads need into shared memory; they are visible to all threads on return.
+template <typename Acc, typename Epi>
+__device__ __forceinline__ void GridReduce(Acc a, Acc b, const PcgDev& d, int& seq, PcgShared& sm,
+                                           Epi epi) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int grid = gridDim.x;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  Acc* red = reinterpret_cast<Acc*>(sm.red);
+  __syncthreads();  // every thread has read the previous scalars
+  if (lane == 0) {
+    red[2 * warp] = a;
+    red[2 * warp + 1] = b;
+  }
+  __syncthreads();
+  double2* part = reinterpret_cast<double2*>(d.partials) + size_t(seq & 1) * grid;
+  if (warp == 0) {
+    Acc ta = lane < nwarp ? red[2 * lane] : Acc(0);
+    Acc tb = lane < nwarp ? red[2 * lane + 1] : Acc(0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      ta += __shfl_down_sync(0xffffffffu, ta, o);
+      tb += __shfl_down_sync(0xffffffffu, tb, o);
+    }
+    if (lane == 0) {
+      if (grid == 1) epi(ta, tb);
+      else __stcg(part + blockIdx.x, make_double2(double(ta), double(tb)));
+    }
+  }
+  if (grid > 1) {
+    GridBarrier(d.bar, grid, d.err);
+    if (warp == 0) {
+      double ta = 0.0, tb = 0.0;
+      for (int q = lane; q < grid; q += 32) {
+        const double2 v = __ldcg(part + q);
+        ta += v.x;
+        tb += v.y;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        ta += __shfl_down_sync(0xffffffffu, ta, o);
+        tb += __shfl_down_sync(0xffffffffu, tb, o);
+      }
+      if (lane == 0) epi(Acc(ta), Acc(tb));
+    }
+  }
+  __syncthreads();
+  ++seq;
+}
+
+// Inner products accumulate in the matrix precision T (FP32 in the mixed form); the FP64 residual
+// passes and the stopping decisions use FP64.
+template <typename T, bool kStaged>
 __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
-  __shared__ PcgSmem sm;
+  extern __shared__ __align__(16) unsigned char pcg_smem[];
+  __shared__ PcgShared sm;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / kB;  // 0..2: camera block of the lane; 3: idle lanes 27..31
   const int a = lane - sub * kB;
+  const int ng = d.pd.ng;
   const int g = (blockIdx.x * (blockDim.x >> 5) + warp) * 3 + sub;
-  const bool in_group = sub < 3 && g < d.pd.ng;
+  const bool in_group = sub < 3 && g < ng;
   const int s = in_group ? d.pd.gidx[size_t(g) * kB + a] : -1;
   const bool own = s >= 0;
   const int gbase = sub < 3 ? sub * kB : 0;
-  const T* S = static_cast<const T*>(d.S);
+  const size_t gi = size_t(in_group ? g : 0) * kB + a;
+  const int e0 = in_group ? d.gptr[g] : 0, e1 = in_group ? d.gptr[g + 1] : 0;
+  const T* Sb;
+  const int2* gent;
+  T* zv;
+  double* ygv;
+  if constexpr (kStaged) {
+    const int nent = d.gptr[ng];
+    double* sy = reinterpret_cast<double*>(pcg_smem);
+    int2* se = reinterpret_cast<int2*>(sy + size_t(ng) * kB);
+    T* sS = reinterpret_cast<T*>(se + nent);
+    T* sz = sS + size_t(d.nbl) * kB * kB;
+    const T* gS = static_cast<const T*>(d.Sb);
+    for (size_t i = threadIdx.x; i < size_t(d.nbl) * kB * kB; i += blockDim.x) sS[i] = gS[i];
+    for (int i = threadIdx.x; i < nent; i += blockDim.x) se[i] = d.gent[i];
+    for (int i = threadIdx.x; i < ng * kB; i += blockDim.x) {
+      sz[i] = T(0);
+      sy[i] = 0.0;
+    }
+    Sb = sS;
+    gent = se;
+    zv = sz;
+    ygv = sy;
+  } else {
+    Sb = static_cast<const T*>(d.Sb);
+    gent = d.gent;
+    zv = static_cast<T*>(d.z);
+    ygv = d.yg;
+  }
+  if (threadIdx.x == 0) {
+    sm.iters = 0;
+    sm.converged = 0;
+    sm.broke = 0;
+    sm.rel = 0.0;
+  }
   const T* v = static_cast<const T*>(d.v);
   const T* P = static_cast<const T*>(d.P);
-  T* zg = static_cast<T*>(d.z);
   T prow[kB];
 #pragma unroll
   for (int b = 0; b < kB; ++b) prow[b] = own ? P[(size_t(g) * kB + a) * kB + b] : T(0);
-  const int64_t q0 = own ? d.m.row_ptr[s] : 0, q1 = own ? d.m.row_ptr[s + 1] : 0;
   int seq = 0;
   const double vs = own ? double(v[s]) : 0.0;
-  const double vnorm = sqrt(GridSum2(vs * vs, 0.0, d, seq, sm).x);
-  bool converged = !(vnorm > 0.0);  // zero rhs: y = 0
-  double rel = 0.0;
+  GridReduce<double>(vs * vs, 0.0, d, seq, sm, [&](double x, double) {
+    sm.vnorm = sqrt(x);
+    sm.converged = sm.vnorm > 0.0 ? 0 : 1;  // zero rhs: y = 0
+  });
+  const double vnorm = sm.vnorm;
   double y64 = 0.0;
-  int iters = 0, outer = 0;
-  bool broke = false;
-  while (!converged) {
+  int outer = 0;
+  while (!sm.converged) {
     double r64 = vs;
-    if (outer > 0 && own) {
-      double acc = 0.0;
-      for (int64_t q = q0; q < q1; ++q) {
-        const T* aa = S + d.m.seg_base[q];
-        const int stride = d.m.seg_stride[q], n = d.m.seg_len[q];
-        const double* yy = d.y + d.m.seg_x[q];
-        for (int c = 0; c < n; ++c) acc += double(aa[int64_t(c) * stride]) * __ldcg(yy + c);
-      }
-      r64 = vs - acc;
-    }
-    const double rr64 = GridSum2(r64 * r64, 0.0, d, seq, sm).x;
-    rel = sqrt(rr64) / vnorm;
-    if (rel <= d.tol) {
-      converged = true;
-      break;
-    }
-    if (outer >= d.max_outer || iters >= d.max_iters || broke || !(rel == rel)) break;
+    if (outer > 0 && in_group) r64 = vs - GroupRow<double, kStaged>(Sb, gent, e0, e1, a, ygv);
+    GridReduce<double>(r64 * r64, 0.0, d, seq, sm, [&](double x, double) {
+      sm.rel = sqrt(x) / vnorm;
+      sm.converged = sm.rel <= d.tol ? 1 : 0;
+      sm.stop = (sm.converged || outer >= d.max_outer || sm.iters >= d.max_iters || sm.broke ||
+                 !(sm.rel == sm.rel)) ? 1 : 0;
+      sm.target = fmax(0.5 * d.tol * vnorm, d.inner_floor * sqrt(x));
+      sm.targetf = float(sm.target);
+    });
+    if (sm.stop) break;
     ++outer;
-    // inner PCG on S dx = r (x0 = 0), in the matrix precision; the product uses w = S z and
+    // inner PCG on S dx = r (x0 = 0) in the matrix precision; the product uses w = S z and
     // q = w + beta q so that one grid reduction separates the product from the update
+    using Sc = InnerScalars<T>;
     T r = T(r64);
     T zz = ApplyBlock(prow, r, gbase);
-    if (own) __stcg(zg + s, zz);
-    double rz = GridSum2(double(r) * double(zz), 0.0, d, seq, sm).x;
-    const double target = fmax(0.5 * d.tol * vnorm, d.inner_floor * sqrt(rr64));
-    T p = T(0), qv = T(0), dx = T(0);
-    double beta = 0.0;
+    if (in_group) StX<kStaged>(zv + gi, zz);
+    GridReduce<T>(r * zz, T(0), d, seq, sm, [&](T x, T) { Sc::rz(sm) = x; });
+    T p = T(0), qv = T(0), dx = T(0), beta = T(0);
     for (;;) {
-      T w = T(0);
-      for (int64_t q = q0; q < q1; ++q) {
-        const T* aa = S + d.m.seg_base[q];
-        const int stride = d.m.seg_stride[q], n = d.m.seg_len[q];
-        const T* zz_in = zg + d.m.seg_x[q];
-        for (int c = 0; c < n; ++c) w += aa[int64_t(c) * stride] * __ldcg(zz_in + c);
-      }
-      p = zz + T(beta) * p;
-      qv = w + T(beta) * qv;
-      const double pq = GridSum2(double(p) * double(qv), 0.0, d, seq, sm).x;
-      if (!(pq > 0.0) || !(pq < 1e300) || !(fabs(rz) < 1e300)) {
-        broke = true;
-        break;
-      }
-      const double alpha = rz / pq;
-      dx += T(alpha) * p;
-      r -= T(alpha) * qv;
+      const T w = in_group ? GroupRow<T, kStaged>(Sb, gent, e0, e1, a, zv) : T(0);
+      p = zz + beta * p;
+      qv = w + beta * qv;
+      GridReduce<T>(p * qv, T(0), d, seq, sm, [&](T pq, T) {
+        const T rz = Sc::rz(sm);
+        if (!(pq > T(0)) || !(pq < Sc::big()) || !(fabs(rz) < Sc::big())) sm.broke = 1;
+        else Sc::alpha(sm) = rz / pq;
+      });
+      if (sm.broke) break;
+      const T alpha = Sc::alpha(sm);
+      dx += alpha * p;
+      r -= alpha * qv;
       zz = ApplyBlock(prow, r, gbase);
-      if (own) __stcg(zg + s, zz);
-      const double2 sums = GridSum2(double(r) * double(zz), double(r) * double(r), d, seq, sm);
-      ++iters;
-      if (sqrt(sums.y) <= target || iters >= d.max_iters) break;
-      beta = sums.x / rz;
-      rz = sums.x;
+      if (in_group) StX<kStaged>(zv + gi, zz);
+      GridReduce<T>(r * zz, r * r, d, seq, sm, [&](T rz, T rr) {
+        sm.iters += 1;
+        sm.stop = (sqrt(rr) <= Sc::target(sm) || sm.iters >= d.max_iters) ? 1 : 0;
+        Sc::beta(sm) = rz / Sc::rz(sm);
+        Sc::rz(sm) = rz;
+      });
+      if (sm.stop) break;
+      beta = Sc::beta(sm);
     }
     y64 += double(dx);
-    if (own) __stcg(d.y + s, y64);
+    if (in_group) StX<kStaged>(ygv + gi, y64);
     if (gridDim.x > 1) GridBarrier(d.bar, gridDim.x, d.err);
     else __syncthreads();
   }
   if (own) __stcg(d.y + s, y64);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     PcgState* ps = d.ps;
-    ps->converged = converged ? 1 : 0;
-    ps->need_fallback = converged ? 0 : 1;
-    ps->iterations = iters;
+    const int conv = sm.converged;
+    ps->converged = conv;
+    ps->need_fallback = conv ? 0 : 1;
+    ps->iterations = sm.iters;
     ps->outer = outer;
-    ps->rel_residual = rel;
-    ps->total_iterations += iters;
+    ps->rel_residual = sm.rel;
+    ps->total_iterations += sm.iters;
     ps->solves += 1;
-    ps->fallbacks += converged ? 0 : 1;
-    ps->max_iterations = max(ps->max_iterations, iters);
-    ps->max_rel_residual = fmax(ps->max_rel_residual, rel);
+    ps->fallbacks += conv ? 0 : 1;
+    ps->max_iterations = max(ps->max_iterations, sm.iters);
+    ps->max_rel_residual = fmax(ps->max_rel_residual, sm.rel);
+  }
+}
+
+template <typename T>
+__global__ void GroupBlocksKernel(const int64_t* off, int64_t n, const T* S, T* Sb) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t o = off[i];
+    Sb[i] = o >= 0 ? S[o] : T(0);
   }
 }
 
@@ -518,7 +621,7 @@ void PcgShape(int ng, int num_sms, int* grid, int* threads) {
 template <typename T>
 int PcgMaxResidentCtas(int threads, int num_sms) {
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, PcgKernel<T>, threads, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, PcgKernel<T, false>, threads, 0) != cudaSuccess)
     return 0;
   return per_sm * num_sms;
 }
@@ -526,9 +629,39 @@ template int PcgMaxResidentCtas<double>(int, int);
 template int PcgMaxResidentCtas<float>(int, int);
 
 template <typename T>
+size_t PcgStagedSmem(int ng, int nbl, int nent) {
+  const size_t bytes = size_t(ng) * kB * 8 + size_t(nent) * 8 + size_t(nbl) * kB * kB * sizeof(T) +
+                       size_t(ng) * kB * sizeof(T);
+  return bytes > kPcgStagedMax ? 0 : bytes;
+}
+template size_t PcgStagedSmem<double>(int, int, int);
+template size_t PcgStagedSmem<float>(int, int, int);
+
+template <typename T>
+void ConfigurePcg() {
+  cudaFuncSetAttribute(PcgKernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPcgStagedMax));
+}
+template void ConfigurePcg<double>();
+template void ConfigurePcg<float>();
+
+template <typename T>
+void LaunchGroupBlocks(const int64_t* off, int64_t n, const void* S, void* Sb, cudaStream_t s) {
+  const int threads = 256;
+  const int grid = int(std::min<int64_t>((n + threads - 1) / threads, 4096));
+  GroupBlocksKernel<T><<<std::max(grid, 1), threads, 0, s>>>(off, n, static_cast<const T*>(S),
+                                                            static_cast<T*>(Sb));
+}
+template void LaunchGroupBlocks<double>(const int64_t*, int64_t, const void*, void*, cudaStream_t);
+template void LaunchGroupBlocks<float>(const int64_t*, int64_t, const void*, void*, cudaStream_t);
+
+template <typename T>
 cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s) {
   if (grid == 1) {
-    PcgKernel<T><<<1, threads, 0, s>>>(d);
+    if (d.staged) {
+      PcgKernel<T, true><<<1, threads, size_t(d.staged), s>>>(d);
+    } else {
+      PcgKernel<T, false><<<1, threads, 0, s>>>(d);
+    }
     return cudaGetLastError();
   }
   const cudaError_t e = cudaMemsetAsync(d.bar, 0, 2 * sizeof(unsigned), s);
@@ -543,8 +676,10 @@ cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, PcgKernel<T>, d);
+  return cudaLaunchKernelEx(&cfg, PcgKernel<T, false>, d);
 }
+template cudaError_t LaunchPcg<double>(const PcgDev&, int, int, cudaStream_t);
+template cudaError_t LaunchPcg<float>(const PcgDev&, int, int, cudaStream_t);
 
 void LaunchPcgBegin(PcgState* ps, cudaStream_t s) { cudaMemsetAsync(ps, 0, sizeof(PcgState), s); }
 
@@ -560,7 +695,4 @@ template void LaunchCollectSamples<double>(const PrecondDev&, const float*, cons
 template void LaunchCollectSamples<float>(const PrecondDev&, const float*, const float*, const void*,
                                           const double*, float*, int, PcgState*, const LmState*,
                                           cudaStream_t);
-template cudaError_t LaunchPcg<double>(const PcgDev&, int, int, cudaStream_t);
-template cudaError_t LaunchPcg<float>(const PcgDev&, int, int, cudaStream_t);
-
 }  // namespace sfg

@@ -52,6 +52,11 @@ struct PrecondLayout {
   std::vector<float> degree;          // [ng] neighbouring blocks
   std::vector<int32_t> scalar_group;  // [nB]
   std::vector<int64_t> sdiag_off;     // [nB]
+  // 9 x 9 group blocks of S (lower: column group <= row group), row-major, 81 entries each
+  std::vector<int32_t> blk_row, blk_col;
+  std::vector<int64_t> blk_off;       // [nblocks][81] S value offset; -1 padding, -2 zero
+  std::vector<int32_t> gptr;          // [ng + 1] entries of each group row
+  std::vector<int32_t> gent;          // [entries][2] {stored block, neighbour << 1 | transposed}
 };
 PrecondLayout BuildPrecondLayout(const HostProblem& P, const SchurLayout& SL);
 

@@ -113,21 +113,38 @@ def infer(features: np.ndarray, weights: np.ndarray, device: int = 0) -> np.ndar
     return z
 
 
+def time_to_cost(stats, target: float, rel: float = 1e-6) -> float | None:
+    """Device time (ms) of the first LM record whose best error is within `rel` of `target`."""
+    for r in stats.iterations:
+        if r.best_error <= target * (1 + rel):
+            return r.elapsed_ms
+    return None
+
+
 def compare(problem: A.ProblemArrays, weights: np.ndarray, params: A.OptimizerParams,
-            precision: int = A.SFG_PRECISION_MIXED) -> dict:
-    """Block-Jacobi PCG versus the learned preconditioner on one problem: PCG iterations, fallbacks,
-    LM iterations, device time and final cost."""
+            precision: int = A.SFG_PRECISION_MIXED, target: float | None = None,
+            forms=("block_jacobi", "learned"), **form_overrides) -> dict:
+    """Block-Jacobi PCG versus the learned preconditioner (and optionally the exact "plain" /
+    "mixed" Schur forms) on one problem: PCG iterations, fallbacks, LM iterations, device time,
+    final cost and, given the oracle's cost, the time to reach it within 1e-6."""
+    solvers = {"block_jacobi": (A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI, precision),
+               "learned": (A.SFG_LINEAR_SOLVER_PCG_LEARNED, precision),
+               "plain": (A.SFG_LINEAR_SOLVER_SCHUR, A.SFG_PRECISION_FP64),
+               "mixed": (A.SFG_LINEAR_SOLVER_SCHUR, A.SFG_PRECISION_MIXED)}
     out = {}
-    for name, solver in (("block_jacobi", A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI),
-                         ("learned", A.SFG_LINEAR_SOLVER_PCG_LEARNED)):
-        opt = Optimizer(problem, params, A.default_form_params(precision=precision, linear_solver=solver),
+    for name in forms:
+        solver, prec = solvers[name]
+        opt = Optimizer(problem, params, A.default_form_params(precision=prec, linear_solver=solver,
+                                                               **form_overrides),
                         weights=weights if solver == A.SFG_LINEAR_SOLVER_PCG_LEARNED else None)
         opt.optimize(problem.values)  # warm-up (graph build)
         _, st = opt.optimize(problem.values)
         ps = opt.pcg_stats()
         out[name] = dict(pcg_iterations=int(ps["iterations"]), solves=int(ps["solves"]),
                          fallbacks=int(ps["fallbacks"]), lm_iterations=len(st.iterations) - 1,
-                         device_ms=st.device_ms, best_error=st.best_error)
+                         device_ms=round(st.device_ms, 3), best_error=st.best_error)
+        if target is not None:
+            out[name]["time_to_cost_ms"] = time_to_cost(st, target)
         opt.close()
     return out
 
@@ -146,6 +163,9 @@ def main(argv=None) -> None:
     e = sub.add_parser("evaluate")
     e.add_argument("--weights", default=str(WEIGHTS))
     e.add_argument("--seeds", default="0,1,2")
+    e.add_argument("--pcg-tol", type=float, default=1e-8)
+    e.add_argument("--pcg-max-iters", type=int, default=500)
+    e.add_argument("--forms", default="block_jacobi,learned")
     args = ap.parse_args(argv)
     if args.cmd == "train":
         t0 = time.perf_counter()
@@ -166,7 +186,13 @@ def main(argv=None) -> None:
         w = load_weights(args.weights)
         for seed in [int(s) for s in args.seeds.split(",")]:
             p = synth.bundle_adjustment(50, 7800, 32000, seed=seed)
-            print(json.dumps(dict(seed=seed, **compare(p, w, ba_params(100)))))
+            # the exact FP64 Schur form's converged cost is the target (it matches the oracle's)
+            ref = Optimizer(p, ba_params(100), A.default_form_params(linear_solver=A.SFG_LINEAR_SOLVER_SCHUR))
+            target = ref.optimize(p.values)[1].best_error
+            ref.close()
+            r = compare(p, w, ba_params(100), target=target, forms=tuple(args.forms.split(",")),
+                        pcg_tol=args.pcg_tol, pcg_max_iters=args.pcg_max_iters)
+            print(json.dumps(dict(seed=seed, pcg_tol=args.pcg_tol, **r)))
 
 
 if __name__ == "__main__":

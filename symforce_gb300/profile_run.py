@@ -18,13 +18,19 @@ from .optimizer import Optimizer
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="ba_50_7800")
-    ap.add_argument("--form", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--form", default="plain", choices=["plain", "mixed", "jacobi", "learned"])
+    ap.add_argument("--pcg-tol", type=float, default=1e-8)
     ap.add_argument("--runs", type=int, default=2)
     args = ap.parse_args()
     w = workloads.get(args.workload)
     p = w.problem()
     prec = A.SFG_PRECISION_FP64 if args.form == "plain" else A.SFG_PRECISION_MIXED
-    opt = Optimizer(p, w.params(), w.form(prec))
+    form = w.form(prec)
+    if args.form in ("jacobi", "learned"):
+        form.linear_solver = (A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI if args.form == "jacobi"
+                              else A.SFG_LINEAR_SOLVER_PCG_LEARNED)
+        form.pcg_tol = args.pcg_tol
+    opt = Optimizer(p, w.params(), form)
     for _ in range(args.runs):
         _, stats = opt.optimize(p.values)
         print(f"{args.workload} {args.form}: {len(stats.iterations)} records, best {stats.best_error:.10g}, "

@@ -120,6 +120,98 @@ def robot_2d(num_poses: int = 1000, num_landmarks: int = 20, bearings_per_pose: 
 
 
 # ---------------------------------------------------------------------------------------------
+# Config 3: batches of independent 3D localization problems
+# ---------------------------------------------------------------------------------------------
+def _pose3_draws(n: int, L: int, seed: int) -> dict:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    d = dict(q0=rng.normal(size=4), t0=rng.uniform(-20, 20, size=3))
+    d["rot_inc"] = rng.normal(0, 0.1, size=(n - 1, 3))
+    d["jitter"] = rng.normal(0, 0.1, size=(n - 1, 3))
+    d["landmarks"] = rng.uniform(-20, 20, size=(L, 3))
+    d["n_rot"] = rng.normal(0, 0.05, size=(n - 1, 3))
+    d["n_t"] = rng.normal(0, 0.1, size=(n - 1, 3))
+    d["n_range"] = rng.normal(0, 0.1, size=(n, L))
+    return d
+
+
+def _pose3_build(sizes, lms, seeds) -> list:
+    """The problems of pose3_chain for every (n, L, seed), with the sequential trajectory and dead
+    reckoning recursions evaluated for all problems at once."""
+    eps = A.DEFAULT_EPSILON
+    P = len(sizes)
+    nmax = int(max(sizes))
+    draws = [_pose3_draws(int(sizes[i]), int(lms[i]), int(seeds[i])) for i in range(P)]
+    pad = lambda key: np.stack([np.concatenate([d[key], np.zeros((nmax - 1 - d[key].shape[0], 3))], 0)
+                                for d in draws], 0)
+    rot_inc, jitter, n_rot, n_t = pad("rot_inc"), pad("jitter"), pad("n_rot"), pad("n_t")
+    q = np.zeros((P, nmax, 4))
+    t = np.zeros((P, nmax, 3))
+    q0 = np.stack([d["q0"] for d in draws])
+    q[:, 0] = q0 / np.linalg.norm(q0, axis=1, keepdims=True)
+    t[:, 0] = np.stack([d["t0"] for d in draws])
+    fwd = np.array([1.0, 0.0, 0.0])
+    for k in range(1, nmax):
+        q[:, k] = quat_mul(q[:, k - 1], quat_exp(rot_inc[:, k - 1]))
+        t[:, k] = t[:, k - 1] + quat_rotate(q[:, k - 1], fwd) + jitter[:, k - 1]
+    qa_inv = q[:, :-1] * np.array([-1, -1, -1, 1.0])
+    q_meas = quat_mul(quat_mul(qa_inv, q[:, 1:]), quat_exp(n_rot))
+    t_meas = quat_rotate(qa_inv, t[:, 1:] - t[:, :-1]) + n_t
+    qi = np.zeros_like(q)
+    ti = np.zeros_like(t)
+    qi[:, 0], ti[:, 0] = q[:, 0], t[:, 0]
+    for k in range(1, nmax):
+        qi[:, k] = quat_mul(qi[:, k - 1], q_meas[:, k - 1])
+        ti[:, k] = ti[:, k - 1] + quat_rotate(qi[:, k - 1], t_meas[:, k - 1])
+    s_between = np.array([1 / 0.05] * 3 + [1 / 0.1] * 3)
+    s_prior = np.array([1 / 0.1] * 3 + [1 / 1.0] * 3)
+    out = []
+    for i, d in enumerate(draws):
+        n, L = int(sizes[i]), int(lms[i])
+        bw_consts = np.concatenate([q_meas[i, :n - 1], t_meas[i, :n - 1], np.tile(s_between, (n - 1, 1)),
+                                    np.full((n - 1, 1), eps)], 1)
+        bw_keys = np.stack([np.arange(n - 1), np.arange(1, n)], -1)
+        lm = d["landmarks"]
+        rng_d = np.linalg.norm(t[i, :n, None, :] - lm[None, :, :], axis=-1) + d["n_range"]
+        r_keys = np.repeat(np.arange(n), L)
+        r_consts = np.concatenate([np.tile(lm, (n, 1)), rng_d.reshape(-1, 1), np.full((n * L, 1), 1 / 0.1),
+                                   np.full((n * L, 1), eps)], 1)
+        p_consts = np.concatenate([q[i, 0], t[i, 0], s_prior, [eps]])[None, :]
+        values = np.concatenate([qi[i, :n], ti[i, :n]], 1).reshape(-1)
+        out.append(A.ProblemArrays(
+            key_types=[A.SFG_KEY_POSE3] * n,
+            batches=[A.Batch(A.SFG_FACTOR_PRIOR_POSE3, np.zeros((1, 1)), p_consts),
+                     A.Batch(A.SFG_FACTOR_BETWEEN_POSE3, bw_keys, bw_consts),
+                     A.Batch(A.SFG_FACTOR_RANGE_POSE3, r_keys[:, None], r_consts)],
+            values=values,
+            name=f"pose3_chain_{n}_{L}",
+            meta=dict(seed=int(seeds[i]), num_poses=n, num_landmarks=L),
+        ))
+    return out
+
+
+def pose3_chain(num_poses: int, num_landmarks: int, seed: int) -> A.ProblemArrays:
+    """One 3D localization problem: a Pose3 random walk (1 m forward steps in the body frame with
+    N(0, 0.1) m jitter, N(0, 0.1) rad rotation increments) starting uniformly in a 40 m cube,
+    between factors on consecutive poses (noise and sqrt_info diag(1/0.05 x3, 1/0.1 x3)), a range
+    factor from every pose to every landmark (landmarks ~U in the 40 m cube, sigma 0.1 m), and a
+    weak prior on the first pose (sigma 0.1 rad / 1 m) that fixes the global rotation, which ranges
+    and relative poses leave unobservable.  Initial values are dead reckoning: the prior pose
+    composed with the measured relative poses."""
+    return _pose3_build([num_poses], [num_landmarks], [seed])[0]
+
+
+def pose3_chains(num_problems: int = 4096, seed: int = 0, min_poses: int = 5, max_poses: int = 200,
+                 min_landmarks: int = 10, max_landmarks: int = 50) -> list:
+    """Independent 3D localization problems of uneven size: problem i has U{5..200} poses and
+    U{10..50} landmarks drawn from the batch seed, and its own seed (seed * 1_000_003 + i);
+    problem i equals pose3_chain(n_i, L_i, seed * 1_000_003 + i)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sizes = rng.integers(min_poses, max_poses + 1, size=num_problems)
+    lms = rng.integers(min_landmarks, max_landmarks + 1, size=num_problems)
+    return _pose3_build(sizes, lms, [seed * 1_000_003 + i for i in range(num_problems)])
+
+
+# ---------------------------------------------------------------------------------------------
 # Configs 1/2/4: bundle adjustment
 # ---------------------------------------------------------------------------------------------
 def bundle_adjustment(num_cameras: int = 50, num_points: int = 7800,
