@@ -1,14 +1,19 @@
 #!/usr/bin/env python3
-"""Benchmark: bundle-adjustment time to the FP64-oracle cost on one GB300 (plain FP64 form).
+"""Benchmark: bundle-adjustment time to the FP64-oracle cost on one GB300.
 
-Workload (one step = one full Optimizer::Optimize call): the 50-camera / 7,800-point / ~32k
-observation synthetic bundle adjustment with Cauchy-whitened Snavely reprojection factors, Schur
-elimination of the points and a device multifrontal LDL^T of the reduced camera system, DYNAMIC
-lambda, 50 iterations.  Metric: milliseconds until the best cost is within 1e-6 (relative) of the
-CPU oracle's final cost (committed in tests/golden/oracle_costs.json), read from the per-iteration
-device timestamps of the run; lower is better.
+Headline (one step = one full Optimizer::Optimize call): the 50-camera / 7,800-point / ~32k
+observation synthetic bundle adjustment with Cauchy-whitened Snavely reprojection factors, plain FP64
+form (Schur elimination of the points and a device multifrontal LDL^T of the reduced camera system),
+DYNAMIC lambda.  Metric: milliseconds until the best cost is within 1e-6 (relative) of the CPU
+oracle's final cost (committed in tests/golden/oracle_costs.json), read from the per-iteration
+device timestamps of the run; lower is better.  The same line reports:
+  forms    - mixed precision, block-Jacobi PCG and learned-preconditioner PCG on the same workload;
+  scale    - every form on the 1,000-camera / 200k-point / ~1.2M-observation workload;
+  batched  - 4,096 independent Pose3-chain problems in one persistent launch (problems/s);
+  roofline - the linearization stage against the measured HBM copy bandwidth.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--no-scale] [--no-batched] [--no-cpu-baseline]
 
 `--impl reference` times the CPU restatement of the reference's sym::Optimizer (the reference
 itself cannot be compiled here: its Eigen / METIS dependencies are absent) on the host cores.
@@ -192,6 +197,27 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# The forms beside the plain FP64 drop-in.  "pcg_learned" is the learned-preconditioned
+# mixed-precision solve (FP32 linearization / Schur, PCG with the trained camera-block network, exact
+# LDL^T as fallback, FP64 cost and gain ratio).
+FORMS = {
+    "plain": (A.SFG_PRECISION_FP64, A.SFG_LINEAR_SOLVER_SCHUR),
+    "mixed": (A.SFG_PRECISION_MIXED, A.SFG_LINEAR_SOLVER_SCHUR),
+    "pcg_block_jacobi": (A.SFG_PRECISION_MIXED, A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI),
+    "pcg_learned": (A.SFG_PRECISION_MIXED, A.SFG_LINEAR_SOLVER_PCG_LEARNED),
+}
+SCALE_WORKLOAD = "ba_1000_200k"
+BATCH_PROBLEMS = 4096
+
+
+def _make_form(w, name: str, device: int) -> A.FormParams:
+    prec, solver = FORMS[name]
+    form = w.form(prec)
+    form.linear_solver = solver
+    form.device = device
+    return form
+
+
 def _time_form(opt, vin_np, vout_np, flush, steps, warmup, target, target9):
     """Warm up, then time `steps` full optimize calls through the public API (pinned host values in
     and out).  Returns per-step e2e ms, device ms, time-to-target ms, launches and the last stats."""
@@ -222,6 +248,121 @@ def _time_form(opt, vin_np, vout_np, flush, steps, warmup, target, target9):
     return out
 
 
+def _med(x):
+    return round(statistics.median(x), 4)
+
+
+def _form_summary(r: dict, opt, oracle_cost: float) -> dict:
+    st = r["stats"]
+    out = {
+        "time_to_cost_ms": _med(r["ttc"]),
+        "time_to_cost_1e-9_ms": _med(r["ttc9"]),
+        "solve_ms": _med(r["dev"]),
+        "e2e_ms": _med(r["e2e"]),
+        "lm_iterations": len(st.iterations) - 1,
+        "status": st.status,
+        "final_cost_rel_err_vs_oracle": (st.best_error - oracle_cost) / oracle_cost,
+    }
+    if opt.form.linear_solver in (A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI, A.SFG_LINEAR_SOLVER_PCG_LEARNED):
+        ps = opt.pcg_stats()
+        out["pcg"] = {"solves": ps["solves"], "fallbacks": ps["fallbacks"],
+                      "iterations_per_solve": round(ps["iterations"] / max(ps["solves"], 1), 1),
+                      "max_rel_residual": ps["max_rel_residual"]}
+    return out
+
+
+def _scale_section(device: int, flush) -> dict:
+    """The 1,000-camera / 200k-point / ~1.2M-observation workload: every form once after one
+    warm-up call, time to the FP64 oracle's cost (the CPU oracle's committed cost when present,
+    else the plain FP64 form's own best cost, which the oracle pins at the smaller sizes)."""
+    w = workloads.get(SCALE_WORKLOAD)
+    problem = w.problem()
+    params = w.params()
+    costs = json.loads((ROOT / "tests" / "golden" / "oracle_costs.json").read_text())
+    vin = problem.values.copy()
+    res, launches, create_s = {}, 0, {}
+    from symforce_gb300.optimizer import Optimizer
+    for name in FORMS:
+        t0 = time.perf_counter()
+        opt = Optimizer(problem, params, _make_form(w, name, device))
+        create_s[name] = round(time.perf_counter() - t0, 2)
+        r = _time_form(opt, vin, None, flush, 1, 1, -1.0, -1.0)
+        launches += sum(r["launches"])
+        res[name] = (r, opt)
+    if SCALE_WORKLOAD in costs:
+        oracle_cost, kind = costs[SCALE_WORKLOAD]["best_error"], "CPU oracle (Schur path)"
+    else:
+        oracle_cost, kind = res["plain"][0]["stats"].best_error, "plain FP64 GPU form"
+    target = oracle_cost * (1 + TOL)
+    out = {"workload": SCALE_WORKLOAD, "num_cameras": problem.meta["num_cameras"],
+           "num_points": problem.meta["num_points"],
+           "num_observations": problem.meta["num_observations"], "lm_iteration_cap": params.iterations,
+           "oracle_cost": oracle_cost, "oracle": kind, "target_rel": TOL, "forms": {},
+           "host_analysis_s": create_s}
+    for name, (r, opt) in res.items():
+        st = r["stats"]
+        r["ttc"] = [next((x.elapsed_ms for x in st.iterations if x.best_error <= target), float("nan"))]
+        out["forms"][name] = _form_summary(r, opt, oracle_cost)
+        opt.close()
+    plain_t = out["forms"]["plain"]["time_to_cost_ms"]
+    for name in FORMS:
+        t = out["forms"][name]["time_to_cost_ms"]
+        out["forms"][name]["speedup_vs_plain"] = round(plain_t / t, 3) if t == t and t > 0 else None
+    return out, launches
+
+
+def _batched_section(device: int, steps: int, cpu_budget_s: float) -> dict:
+    """4,096 independent Pose3-chain problems in one persistent launch (device time per batch and
+    problems/s), next to the CPU oracle on a bounded sample of the same problems, one optimizer per
+    host thread."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from symforce_gb300 import synth
+    from symforce_gb300.batch import BatchOptimizer
+    problems = synth.pose3_chains(BATCH_PROBLEMS, seed=0)
+    params = A.default_optimizer_params(iterations=50)
+    form = A.default_form_params()
+    form.device = device
+    t0 = time.perf_counter()
+    opt = BatchOptimizer(problems, params, form)
+    create_s = time.perf_counter() - t0
+    v0 = opt.initial_values()
+    opt.set_values(v0)
+    shape = opt.autotune()
+    opt.optimize(v0)  # warm-up (graph build)
+    dev, e2e = [], []
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        res = opt.optimize(v0)
+        vals = opt.get_values()
+        e2e.append((time.perf_counter() - t0) * 1e3)
+        dev.append(res.device_ms)
+    del vals
+    ms = statistics.median(dev)
+    out = {"workload": f"pose3_chains_{BATCH_PROBLEMS}", "problems": BATCH_PROBLEMS,
+           "poses": int(sum(p.meta.get("num_poses", len(p.key_types)) for p in problems)),
+           "batch_ms": round(ms, 3), "problems_per_s": round(BATCH_PROBLEMS / (ms * 1e-3), 1),
+           "e2e_ms": round(statistics.median(e2e), 3), "autotuned_shape": list(shape),
+           "host_create_s": round(create_s, 2),
+           "status_success": int((res.status == A.SFG_STATUS_SUCCESS).sum()),
+           "lm_iterations_mean": round(float(res.num_iterations.mean()), 2)}
+    opt.close()
+    # CPU oracle: one optimizer per thread (ctypes releases the GIL), bounded sample
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib as O
+    threads = os.cpu_count() or 1
+    done, t0 = 0, time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        while time.perf_counter() - t0 < cpu_budget_s and done < BATCH_PROBLEMS:
+            chunk = problems[done:done + 4 * threads]
+            list(ex.map(lambda p: O.optimize(p, params), chunk))
+            done += len(chunk)
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"problems_per_s": round(done / cpu_s, 1), "cores": threads, "kind": "port",
+                           "sample": f"the first {done} of the {BATCH_PROBLEMS} problems"}
+    return out, len(dev) + 2
+
+
 def run_gb300(args) -> None:
     world, rank, local = _dist_init()
     import torch
@@ -239,12 +380,7 @@ def run_gb300(args) -> None:
     vin_np, vout_np = vin.numpy(), vout.numpy()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
-    forms = {}
-    opts = {}
-    for name, prec in [("plain", A.SFG_PRECISION_FP64), ("mixed", A.SFG_PRECISION_MIXED)]:
-        form = w.form(prec)
-        form.device = local
-        opts[name] = Optimizer(problem, params, form)
+    opts = {name: Optimizer(problem, params, _make_form(w, name, local)) for name in FORMS}
     # the plain form is the headline; clocks are sampled during its timed region
     clocks = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
     _barrier(world)
@@ -252,7 +388,7 @@ def run_gb300(args) -> None:
     if clocks:
         clocks.start()
     res = {}
-    for name in ["plain", "mixed"]:
+    for name in FORMS:
         res[name] = _time_form(opts[name], vin_np, vout_np, flush, args.steps, args.warmup, target, target9)
     torch.cuda.synchronize()
     _barrier(world)
@@ -261,18 +397,10 @@ def run_gb300(args) -> None:
     value = _allreduce_max(statistics.median(plain["ttc"]), world)
     ms_step = _allreduce_max(statistics.median(plain["dev"]), world)
     e2e_ms = _allreduce_max(statistics.median(plain["e2e"]), world)
-    for name in ["plain", "mixed"]:
-        r = res[name]
-        st = r["stats"]
-        forms[name] = {
-            "time_to_cost_ms": round(statistics.median(r["ttc"]), 4),
-            "time_to_cost_1e-9_ms": round(statistics.median(r["ttc9"]), 4),
-            "solve_ms": round(statistics.median(r["dev"]), 4),
-            "e2e_ms": round(statistics.median(r["e2e"]), 4),
-            "lm_iterations": len(st.iterations) - 1,
-            "status": st.status,
-            "final_cost_rel_err_vs_oracle": (st.best_error - oracle["best_error"]) / oracle["best_error"],
-        }
+    forms = {name: _form_summary(res[name], opts[name], oracle["best_error"]) for name in FORMS}
+    for name in FORMS:
+        t = forms[name]["time_to_cost_ms"]
+        forms[name]["speedup_vs_plain"] = round(forms["plain"]["time_to_cost_ms"] / t, 3) if t == t else None
     # live roofline of the plain form's linearization stage (CUDA events on the library's stream)
     opt = opts["plain"]
     lin = opt.time_stage(A.SFG_STAGE_LINEARIZE, reps=50)
@@ -284,12 +412,30 @@ def run_gb300(args) -> None:
             t = opts[fname].time_stage(sid, reps=20)
             stages[fname][name] = {"ms": round(t["ms"], 5),
                                    "gfma_s": round(t["fmas"] / t["ms"] / 1e6, 2)}
+    for o in opts.values():
+        o.close()
     peaks, peak_kind = _measured_peaks()
     achieved = lin["bytes"] / (lin["ms"] * 1e-3) / 1e9
     traffic = None
     tp = ROOT / "profiles" / "traffic.json"
     if tp.exists():
         traffic = json.loads(tp.read_text()).get(f"linearize_{WORKLOAD}")
+    launches = int(sum(sum(r["launches"]) for r in res.values()))
+    scale = batched = None
+    # the secondary sections report an error in the line instead of losing the headline
+    if not args.no_scale:
+        try:
+            scale, n = _scale_section(local, flush)
+            launches += n
+        except Exception as e:  # noqa: BLE001
+            scale = {"error": f"{type(e).__name__}: {e}"}
+    if not args.no_batched:
+        try:
+            batched, n = _batched_section(local, min(args.steps, 5),
+                                          cpu_budget_s=10.0 if rank == 0 else 0.0)
+            launches += n
+        except Exception as e:  # noqa: BLE001
+            batched = {"error": f"{type(e).__name__}: {e}"}
     if rank != 0:
         return
     cpu = None
@@ -322,10 +468,12 @@ def run_gb300(args) -> None:
                      "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes": lin["bytes"], "ms_per_launch": round(lin["ms"], 5)},
         "stages_ms_per_launch": stages,
+        "scale": scale,
+        "batched": batched,
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": 8 * S + 8 * 24,
                 "d2h_bytes_per_step": 8 * S + 64 * len(plain["stats"].iterations)},
-        "gpu_launches": int(sum(plain["launches"]) + sum(res["mixed"]["launches"])),
+        "gpu_launches": launches,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
@@ -338,6 +486,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-scale", action="store_true", help="skip the 1,000-camera workload")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched Pose3 chains")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

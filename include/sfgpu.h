@@ -272,7 +272,12 @@ int32_t sfg_pcg_step_error(sfg_handle* h, double* rel_step_error, int32_t* itera
  * A training sample is 114 floats: the 96 inputs, g_hat = C^-1 D^-1/2 v_g and
  * x_hat = C^T D^1/2 y_g for the block's part v_g of the reduced rhs and y_g of the exact solution;
  * its loss is |L L^T g_hat - x_hat|^2 / (|x_hat|^2 + 1e-30) (the error of P_g v_g against y_g
- * in the S_gg norm, relative), averaged over samples. */
+ * in the S_gg norm, relative) plus kaporin * (tr(L L^T) - log det(L L^T) - 9) / 9, averaged over
+ * samples.  The second term is >= 0 and zero only at L = I: it is the block's share of Kaporin's
+ * condition number (tr(K)/n) / det(K)^(1/n) of the preconditioned system K = P^1/2 S P^1/2, which
+ * bounds the CG iteration count and which block Jacobi minimizes over all block-diagonal
+ * preconditioners, so kaporin > 0 lets the network leave block Jacobi only where the first term
+ * pays for it. */
 #define SFG_PRECOND_BLOCK 9
 #define SFG_PRECOND_FEATURES 96
 #define SFG_PRECOND_HIDDEN 256
@@ -292,7 +297,7 @@ typedef struct sfg_train_params_t {
   float beta1, beta2, eps;
   uint64_t seed;        /* shuffling seed */
   int32_t device;
-  int32_t _pad;
+  float kaporin;        /* weight of the Kaporin term of the loss (0: none) */
 } sfg_train_params_t;
 /* Train the network on the GPU (Adam, hand-written forward / backward kernels).  weights holds the
  * initial weights and receives the trained ones; loss_curve (optional) receives the batch loss of
@@ -301,8 +306,8 @@ int32_t sfg_precond_train(const float* samples, int64_t n, const sfg_train_param
                           float* weights, float* loss_curve);
 /* Mean loss over n samples and its gradient with respect to the weights (one forward + backward on
  * the GPU). */
-int32_t sfg_precond_loss_grad(const float* samples, int64_t n, const float* weights, double* loss,
-                              float* grad, int32_t device);
+int32_t sfg_precond_loss_grad(const float* samples, int64_t n, const float* weights, float kaporin,
+                              double* loss, float* grad, int32_t device);
 /* Network outputs z (45 per input row of 96 features). */
 int32_t sfg_precond_infer(const float* features, int64_t n, const float* weights, float* out,
                           int32_t device);

@@ -58,8 +58,9 @@ def factor_from_outputs(z: np.ndarray) -> np.ndarray:
     return L
 
 
-def loss_grad(w: np.ndarray, samples: np.ndarray):
-    """Mean of |L L^T g_hat - x_hat|^2 / (|x_hat|^2 + 1e-30) and its gradient w.r.t. the weights."""
+def loss_grad(w: np.ndarray, samples: np.ndarray, kaporin: float = 0.0):
+    """Mean of |L L^T g_hat - x_hat|^2 / (|x_hat|^2 + 1e-30) + kaporin (tr(L L^T) - log det(L L^T) - 9) / 9
+    and its gradient w.r.t. the weights."""
     S = np.asarray(samples, dtype=np.float64)
     n = S.shape[0]
     X, gh, xh = S[:, :FEATURES], S[:, FEATURES:FEATURES + BLOCK], S[:, FEATURES + BLOCK:]
@@ -73,11 +74,14 @@ def loss_grad(w: np.ndarray, samples: np.ndarray):
     M = L @ np.transpose(L, (0, 2, 1))
     u = np.einsum("nij,nj->ni", M, gh) - xh
     s = np.sum(xh * xh, axis=1) + 1e-30
-    per = np.sum(u * u, axis=1) / s
+    diag = np.diagonal(L, axis1=1, axis2=2)
+    kap = (np.sum(L * L, axis=(1, 2)) - 2.0 * np.sum(np.log(diag), axis=1) - BLOCK) / BLOCK
+    per = np.sum(u * u, axis=1) / s + kaporin * kap
     loss = per.mean()
-    # d/dL = (G + G^T) L, G = 2 u g^T / (s n)
+    # d/dL = (G + G^T) L, G = 2 u g^T / (s n); Kaporin term: kaporin (2 L - 2 diag(1/L_ii)) / (9 n)
     G = 2.0 * u[:, :, None] * gh[:, None, :] / (s * n)[:, None, None]
-    dL = (G + np.transpose(G, (0, 2, 1))) @ L
+    dL = np.tril((G + np.transpose(G, (0, 2, 1))) @ L)
+    dL += kaporin * 2.0 / (BLOCK * n) * (L - np.einsum("ni,ij->nij", 1.0 / diag, np.eye(BLOCK)))
     dZ = np.zeros_like(Z)
     for t, (i, j) in enumerate(TRI):
         if i == j:

@@ -202,7 +202,7 @@ class TrainParamsC(C.Structure):
         ("eps", C.c_float),
         ("seed", C.c_uint64),
         ("device", C.c_int32),
-        ("_pad", C.c_int32),
+        ("kaporin", C.c_float),
     ]
 
 

@@ -52,7 +52,7 @@ struct Workspace {
 
 // Mean loss of n sample rows (row stride kSampleFloats) into *loss_sum and its gradient into g.
 void ForwardBackward(const Workspace& ws, float* weights, float* grad, const float* rows, int n,
-                     double* loss_sum, cudaStream_t s) {
+                     float kaporin, double* loss_sum, cudaStream_t s) {
   const NetPtrs w = Split(weights);
   const NetPtrs g = Split(grad);
   const int F = kPrecondFeatures, H = kPrecondHidden, O = kPrecondTri;
@@ -60,7 +60,7 @@ void ForwardBackward(const Workspace& ws, float* weights, float* grad, const flo
   LaunchGemm(n, H, F, rows, ld, 1, w.W1, H, 1, ws.H1, H, kEpiBiasRelu, w.b1, nullptr, 0, s);
   LaunchGemm(n, H, H, ws.H1, H, 1, w.W2, H, 1, ws.H2, H, kEpiBiasRelu, w.b2, nullptr, 0, s);
   LaunchGemm(n, O, H, ws.H2, H, 1, w.W3, O, 1, ws.Z, O, kEpiBias, w.b3, nullptr, 0, s);
-  LaunchHead(n, ws.Z, rows, ld, 1.f / float(n), ws.dZ, ws.loss, loss_sum, s);
+  LaunchHead(n, ws.Z, rows, ld, 1.f / float(n), kaporin, ws.dZ, ws.loss, loss_sum, s);
   LaunchGemm(H, O, n, ws.H2, 1, H, ws.dZ, O, 1, g.W3, O, kEpiNone, nullptr, nullptr, 0, s);
   LaunchColSum(n, O, ws.dZ, O, g.b3, s);
   LaunchGemm(n, H, O, ws.dZ, O, 1, w.W3, 1, O, ws.dH2, H, kEpiMask, nullptr, ws.H2, H, s);
@@ -119,6 +119,7 @@ int32_t sfg_precond_train(const float* samples, int64_t n, const sfg_train_param
     if (n > (int64_t(1) << 31) - 1) throw Error(SFG_ERR_INVALID_ARGUMENT, "too many samples");
     const sfg_train_params_t& p = *params;
     if (p.steps <= 0 || p.batch <= 0) throw Error(SFG_ERR_INVALID_ARGUMENT, "steps and batch must be positive");
+    if (!(p.kaporin >= 0.f)) throw Error(SFG_ERR_INVALID_ARGUMENT, "kaporin must be >= 0");
     sfg::UseDevice(p.device);
     const int B = int(std::min<int64_t>(p.batch, n));
     sfg::DeviceArena A;
@@ -156,7 +157,7 @@ int32_t sfg_precond_train(const float* samples, int64_t n, const sfg_train_param
       }
       sfg::LaunchGather(B, d_samples, idx + pos, rows, s);
       pos += B;
-      sfg::ForwardBackward(ws, w, g, rows, B, losses + step, s);
+      sfg::ForwardBackward(ws, w, g, rows, B, p.kaporin, losses + step, s);
       b1t *= beta1;
       b2t *= beta2;
       const double frac = p.steps > 1 ? double(step) / double(p.steps - 1) : 0.0;
@@ -174,8 +175,8 @@ int32_t sfg_precond_train(const float* samples, int64_t n, const sfg_train_param
   });
 }
 
-int32_t sfg_precond_loss_grad(const float* samples, int64_t n, const float* weights, double* loss,
-                              float* grad, int32_t device) {
+int32_t sfg_precond_loss_grad(const float* samples, int64_t n, const float* weights, float kaporin,
+                              double* loss, float* grad, int32_t device) {
   return sfg::GuardL([&] {
     if (!samples || !weights || n <= 0) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument or no samples");
     if (n > (int64_t(1) << 24)) throw Error(SFG_ERR_INVALID_ARGUMENT, "too many samples for one pass");
@@ -192,7 +193,7 @@ int32_t sfg_precond_loss_grad(const float* samples, int64_t n, const float* weig
     double* l = A.Zeros<double>(1);
     sfg::Workspace ws;
     ws.Init(A, int(n));
-    sfg::ForwardBackward(ws, w, g, rows, int(n), l, s);
+    sfg::ForwardBackward(ws, w, g, rows, int(n), kaporin, l, s);
     SFG_CUDA(cudaGetLastError());
     SFG_CUDA(cudaStreamSynchronize(s));
     if (loss) SFG_CUDA(cudaMemcpy(loss, l, 8, cudaMemcpyDeviceToHost));

@@ -314,8 +314,8 @@ void LaunchGemm(int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs,
 void LaunchColSum(int M, int N, const float* A, int64_t lda, float* out, cudaStream_t s);
 // Loss head: per sample (row of z, g_hat / x_hat at sample + 96 / + 105 with row stride lds)
 // the loss and d loss / d z scaled by `scale`; loss_sum receives scale * sum of the losses.
-void LaunchHead(int n, const float* z, const float* samples, int64_t lds, float scale, float* dz,
-                float* loss, double* loss_sum, cudaStream_t s);
+void LaunchHead(int n, const float* z, const float* samples, int64_t lds, float scale, float kaporin,
+                float* dz, float* loss, double* loss_sum, cudaStream_t s);
 // rows[i] = samples[idx[i]] (kSampleFloats floats each).
 void LaunchGather(int n, const float* samples, const int32_t* idx, float* rows, cudaStream_t s);
 void LaunchAdam(int64_t n, float* w, const float* g, float* m, float* v, float lr, float beta1,

@@ -86,7 +86,7 @@ __global__ void ColSumKernel(int M, int N, const float* A, int64_t lda, float* o
 }
 
 __global__ void HeadKernel(int n, const float* z, const float* samples, int64_t lds, float scale,
-                           float* dz, float* loss) {
+                           float kaporin, float* dz, float* loss) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   constexpr int kB = kPrecondBlock;
@@ -129,8 +129,18 @@ __global__ void HeadKernel(int n, const float* z, const float* samples, int64_t 
     uu += u[r] * u[r];
   }
   const float inv = 1.f / (xx + 1e-30f);
-  loss[i] = uu * inv;
-  // d loss / d L = (G + G^T) L with G = 2 u g^T / s, lower triangle
+  // Kaporin term kaporin * (tr(L L^T) - log det(L L^T) - 9) / 9
+  float tr = 0.f, ld = 0.f;
+#pragma unroll
+  for (int r = 0; r < kB; ++r) {
+#pragma unroll
+    for (int c = 0; c <= r; ++c) tr += L[Tri(r, c)] * L[Tri(r, c)];
+    ld += logf(L[Tri(r, r)]);
+  }
+  loss[i] = uu * inv + kaporin * (tr - 2.f * ld - float(kB)) * (1.f / kB);
+  const float kf = 2.f * kaporin * (1.f / kB) * scale;
+  // d loss / d L = (G + G^T) L with G = 2 u g^T / s, lower triangle, plus the Kaporin term's
+  // 2 L - 2 diag(1 / L_rr), scaled
   const float f = 2.f * inv * scale;
   float* dzi = dz + int64_t(i) * kPrecondTri;
 #pragma unroll
@@ -141,6 +151,8 @@ __global__ void HeadKernel(int n, const float* z, const float* samples, int64_t 
 #pragma unroll
       for (int k = c; k < kB; ++k) s += (u[r] * g[k] + g[r] * u[k]) * L[Tri(k, c)];
       s *= f;
+      const float lrc = L[Tri(r, c)];
+      s += kf * (r == c ? lrc - 1.f / lrc : lrc);
       dzi[Tri(r, c)] = r == c ? s * sig[r] : s;
     }
 }
@@ -196,10 +208,11 @@ void LaunchColSum(int M, int N, const float* A, int64_t lda, float* out, cudaStr
   ColSumKernel<<<(N + threads - 1) / threads, threads, 0, s>>>(M, N, A, lda, out);
 }
 
-void LaunchHead(int n, const float* z, const float* samples, int64_t lds, float scale, float* dz,
-                float* loss, double* loss_sum, cudaStream_t s) {
+void LaunchHead(int n, const float* z, const float* samples, int64_t lds, float scale, float kaporin,
+                float* dz, float* loss, double* loss_sum, cudaStream_t s) {
   const int threads = 128;
-  HeadKernel<<<(n + threads - 1) / threads, threads, 0, s>>>(n, z, samples, lds, scale, dz, loss);
+  HeadKernel<<<(n + threads - 1) / threads, threads, 0, s>>>(n, z, samples, lds, scale, kaporin, dz,
+                                                             loss);
   SumKernel<<<1, 256, 0, s>>>(n, loss, scale, loss_sum);
 }
 

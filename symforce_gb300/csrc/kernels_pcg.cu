@@ -343,29 +343,8 @@ __device__ __forceinline__ Acc GroupRow(const T* Sb, const int2* gent, int e0, i
 struct PcgShared {
   double2 red[32];
   double vnorm, target, rel;
-  float rzf, alphaf, betaf, targetf;
-  double rzd, alphad, betad;
+  double rz, alpha, beta;
   int iters, stop, broke, converged;
-};
-
-// The scalars of the inner iteration in the matrix precision.
-template <typename T>
-struct InnerScalars;
-template <>
-struct InnerScalars<float> {
-  __device__ static float& rz(PcgShared& s) { return s.rzf; }
-  __device__ static float& alpha(PcgShared& s) { return s.alphaf; }
-  __device__ static float& beta(PcgShared& s) { return s.betaf; }
-  __device__ static float target(const PcgShared& s) { return s.targetf; }
-  __device__ static constexpr float big() { return 1e37f; }
-};
-template <>
-struct InnerScalars<double> {
-  __device__ static double& rz(PcgShared& s) { return s.rzd; }
-  __device__ static double& alpha(PcgShared& s) { return s.alphad; }
-  __device__ static double& beta(PcgShared& s) { return s.betad; }
-  __device__ static double target(const PcgShared& s) { return s.target; }
-  __device__ static constexpr double big() { return 1e300; }
 };
 
 // Sum (a, b) over the grid: a warp tree in Acc, the CTA's warps in order (warp 0, Acc), and the CTAs
@@ -424,8 +403,8 @@ __device__ __forceinline__ void GridReduce(Acc a, Acc b, const PcgDev& d, int& s
   ++seq;
 }
 
-// Inner products accumulate in the matrix precision T (FP32 in the mixed form); the FP64 residual
-// passes and the stopping decisions use FP64.
+// Vector arithmetic in the matrix precision T (FP32 in the mixed form); inner products, CG scalars,
+// the residual passes and the stopping decisions in FP64.
 template <typename T, bool kStaged>
 __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
   extern __shared__ __align__(16) unsigned char pcg_smem[];
@@ -497,41 +476,41 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
       sm.stop = (sm.converged || outer >= d.max_outer || sm.iters >= d.max_iters || sm.broke ||
                  !(sm.rel == sm.rel)) ? 1 : 0;
       sm.target = fmax(0.5 * d.tol * vnorm, d.inner_floor * sqrt(x));
-      sm.targetf = float(sm.target);
     });
     if (sm.stop) break;
     ++outer;
-    // inner PCG on S dx = r (x0 = 0) in the matrix precision; the product uses w = S z and
-    // q = w + beta q so that one grid reduction separates the product from the update
-    using Sc = InnerScalars<T>;
+    // inner PCG on S dx = r (x0 = 0): vectors and the products with S and P in the matrix
+    // precision T, inner products and the CG scalars in FP64 (FP32 sums of a few thousand terms
+    // lose the digits the recurrences need on these ill-conditioned systems).  The product uses
+    // w = S z and q = w + beta q so that one grid reduction separates the product from the update.
     T r = T(r64);
     T zz = ApplyBlock(prow, r, gbase);
     if (in_group) StX<kStaged>(zv + gi, zz);
-    GridReduce<T>(r * zz, T(0), d, seq, sm, [&](T x, T) { Sc::rz(sm) = x; });
+    GridReduce<double>(double(r) * double(zz), 0.0, d, seq, sm, [&](double x, double) { sm.rz = x; });
     T p = T(0), qv = T(0), dx = T(0), beta = T(0);
     for (;;) {
       const T w = in_group ? GroupRow<T, kStaged>(Sb, gent, e0, e1, a, zv) : T(0);
       p = zz + beta * p;
       qv = w + beta * qv;
-      GridReduce<T>(p * qv, T(0), d, seq, sm, [&](T pq, T) {
-        const T rz = Sc::rz(sm);
-        if (!(pq > T(0)) || !(pq < Sc::big()) || !(fabs(rz) < Sc::big())) sm.broke = 1;
-        else Sc::alpha(sm) = rz / pq;
+      GridReduce<double>(double(p) * double(qv), 0.0, d, seq, sm, [&](double pq, double) {
+        const double rz = sm.rz;
+        if (!(pq > 0.0) || !(pq < 1e300) || !(fabs(rz) < 1e300)) sm.broke = 1;
+        else sm.alpha = rz / pq;
       });
       if (sm.broke) break;
-      const T alpha = Sc::alpha(sm);
+      const T alpha = T(sm.alpha);
       dx += alpha * p;
       r -= alpha * qv;
       zz = ApplyBlock(prow, r, gbase);
       if (in_group) StX<kStaged>(zv + gi, zz);
-      GridReduce<T>(r * zz, r * r, d, seq, sm, [&](T rz, T rr) {
+      GridReduce<double>(double(r) * double(zz), double(r) * double(r), d, seq, sm, [&](double rz, double rr) {
         sm.iters += 1;
-        sm.stop = (sqrt(rr) <= Sc::target(sm) || sm.iters >= d.max_iters) ? 1 : 0;
-        Sc::beta(sm) = rz / Sc::rz(sm);
-        Sc::rz(sm) = rz;
+        sm.stop = (sqrt(rr) <= sm.target || sm.iters >= d.max_iters) ? 1 : 0;
+        sm.beta = rz / sm.rz;
+        sm.rz = rz;
       });
       if (sm.stop) break;
-      beta = Sc::beta(sm);
+      beta = T(sm.beta);
     }
     y64 += double(dx);
     if (in_group) StX<kStaged>(ygv + gi, y64);

@@ -342,32 +342,33 @@ __device__ void TaskDiag(const FactorDev& f, int s, int k, T* F, T* Linv, TileSm
   T* a = sm.a;  // a[c * TILE + r] = tile(r, c), lower part
   LoadTileT<T, TILE>(Fs, g.m, r0, r0, b, b, a);
   __syncthreads();
-  // Right-looking LDL^T in shared memory.  One thread forms each pivot's reciprocal (an FP64
-  // division is a long instruction sequence); column j is scaled during step j + 1, which does
-  // not read it.
+  // Right-looking LDL^T in shared memory, one barrier per pivot: every thread forms the pivot's
+  // reciprocal itself (same bits everywhere, no broadcast round trip), and column j is scaled
+  // during step j + 1, which does not read it.
+  T inv_prev = T(0);
   for (int j = 0; j < b; ++j) {
-    if (threadIdx.x == 0) sm.d[j] = PivotReciprocal<T>(a[j * TILE + j]);
-    __syncthreads();
-    const T inv = sm.d[j];
+    const T inv = PivotReciprocal<T>(a[j * TILE + j]);
     for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
       const int r = e % TILE, c = e / TILE;
       if (c > j && r >= c && r < b) a[c * TILE + r] -= a[j * TILE + r] * (a[j * TILE + c] * inv);
-      if (j > 0 && c == j - 1 && r > c && r < b) a[c * TILE + r] *= sm.d[j - 1];
+      if (j > 0 && c == j - 1 && r > c && r < b) a[c * TILE + r] *= inv_prev;
+    }
+    inv_prev = inv;
+    __syncthreads();
+  }
+  // Unit lower inverse by forward substitution on all columns at once: after step q, row q of Li
+  // is final and is eliminated from the rows below it (one multiply-add per entry and step, the
+  // entries of a step independent of each other).
+  T* li = sm.b;
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) li[e] = T((e % TILE) == (e / TILE) ? 1 : 0);
+  __syncthreads();
+  for (int q = 0; q + 1 < b; ++q) {
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+      const int r = e % TILE, c = e / TILE;
+      if (r > q && r < b && c <= q) li[c * TILE + r] -= a[q * TILE + r] * li[c * TILE + q];
     }
     __syncthreads();
   }
-  // unit lower inverse, one column per thread: Li(r, c) = -sum_{q=c}^{r-1} L(r, q) Li(q, c)
-  T* li = sm.b;
-  for (int c = threadIdx.x; c < TILE; c += blockDim.x) {
-    for (int r = 0; r < TILE; ++r) li[c * TILE + r] = T(r == c ? 1 : 0);
-    if (c < b)
-      for (int r = c + 1; r < b; ++r) {
-        T acc = T(0);
-        for (int q = c; q < r; ++q) acc += a[q * TILE + r] * li[c * TILE + q];
-        li[c * TILE + r] = -acc;
-      }
-  }
-  __syncthreads();
   T* Lk = Linv + f.linv_base[s] + int64_t(k) * TILE * TILE;
   for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
     const int r = e % TILE, c = e / TILE;

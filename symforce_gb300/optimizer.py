@@ -71,7 +71,8 @@ def lib() -> C.CDLL:
         L.sfg_precond_train.argtypes = [C.POINTER(C.c_float), C.c_int64, C.POINTER(A.TrainParamsC),
                                         C.POINTER(C.c_float), C.POINTER(C.c_float)]
         L.sfg_precond_loss_grad.argtypes = [C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float),
-                                            C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_int32]
+                                            C.c_float, C.POINTER(C.c_double), C.POINTER(C.c_float),
+                                            C.c_int32]
         L.sfg_precond_infer.argtypes = [C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float),
                                         C.POINTER(C.c_float), C.c_int32]
         _lib = L

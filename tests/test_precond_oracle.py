@@ -4,22 +4,25 @@ zero weights = block Jacobi, the block assembly identity P_g S_gg = I, and the P
 from __future__ import annotations
 
 import numpy as np
+import pytest
 
 import precond_cases as PC
 from oracle import precond_net as PN
 
 
-def test_loss_gradient_matches_finite_differences():
+@pytest.mark.parametrize("kaporin", [0.0, 0.7])
+def test_loss_gradient_matches_finite_differences(kaporin):
     rng = np.random.Generator(np.random.PCG64(1))
     samples = PC.oracle_samples((3,))[:12].astype(np.float64)
     w = PC.random_weights(2, out_scale=0.2).astype(np.float64)
-    loss, grad = PN.loss_grad(w, samples)
+    f = lambda x: PN.loss_grad(x, samples, kaporin)[0]  # noqa: E731
+    loss, grad = PN.loss_grad(w, samples, kaporin)
     assert np.isfinite(loss) and loss > 0
     # directional derivatives along random directions and along single coordinates of each layer
     for _ in range(4):
         d = rng.normal(size=w.size)
         h = 1e-6
-        fd = (PN.loss_grad(w + h * d, samples)[0] - PN.loss_grad(w - h * d, samples)[0]) / (2 * h)
+        fd = (f(w + h * d) - f(w - h * d)) / (2 * h)
         assert abs(fd - grad @ d) <= 1e-5 * max(1.0, abs(fd)), (fd, grad @ d)
     offs = np.cumsum([0, 96 * 256, 256, 256 * 256, 256, 256 * 45, 45])
     for a, b in zip(offs[:-1], offs[1:]):
@@ -27,8 +30,22 @@ def test_loss_gradient_matches_finite_differences():
         e = np.zeros(w.size)
         e[i] = 1.0
         h = 1e-6
-        fd = (PN.loss_grad(w + h * e, samples)[0] - PN.loss_grad(w - h * e, samples)[0]) / (2 * h)
+        fd = (f(w + h * e) - f(w - h * e)) / (2 * h)
         assert abs(fd - grad[i]) <= 1e-5 * max(1e-3, abs(fd)), (i, fd, grad[i])
+
+
+def test_kaporin_term_is_zero_only_at_block_jacobi():
+    """The Kaporin term is tr(M) - log det(M) - 9 over 9 for M = L L^T: zero outputs (L = I, block
+    Jacobi) give exactly zero and zero gradient; any other output raises it."""
+    samples = PC.oracle_samples((3,))[:8].astype(np.float64)
+    w = PC.random_weights(4, out_scale=0.2).astype(np.float64)
+    w_bj = w.copy()
+    w_bj[-(256 * 45 + 45):] = 0.0
+    l0, g0 = PN.loss_grad(w_bj, samples, 0.0)
+    l1, g1 = PN.loss_grad(w_bj, samples, 3.0)
+    assert l1 == pytest.approx(l0, rel=1e-12)
+    np.testing.assert_allclose(g1, g0, rtol=0, atol=1e-12 * max(1.0, np.abs(g0).max()))
+    assert PN.loss_grad(w, samples, 3.0)[0] > PN.loss_grad(w, samples, 0.0)[0]
 
 
 def test_zero_output_layer_is_block_jacobi():
