@@ -468,30 +468,7 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
   int* err_word = &h->st->device_error;
   if (h->schur) {
     const SchurLayout& S = h->SL;
-    SchurDev& d = h->sd;
-    d.npoints = S.npoints;
-    d.nB = int(S.nB);
-    d.c_toff = S.c_toff;
-    d.pt_diag = A.Upload(S.pt_diag);
-    d.pt_eptr = A.Upload(S.pt_eptr);
-    d.pt_ekey_toff = A.Upload(S.pt_ekey_toff);
-    d.pt_ekey_dim = A.Upload(S.pt_ekey_dim);
-    d.pt_eoff = A.Upload(S.pt_eoff);
-    d.pt_woff = A.Upload(S.pt_woff);
-    d.nsblocks = int(S.Spat.nblocks());
-    d.sb_ptr = A.Upload(S.sb_ptr);
-    d.sb_eoff = A.Upload(S.sb_eoff);
-    d.sb_woff = A.Upload(S.sb_woff);
-    d.sb_hoff = A.Upload(S.sb_hoff);
-    d.sb_soff = A.Upload(S.sb_soff);
-    d.sb_dk = A.Upload(S.sb_dk);
-    d.sb_dl = A.Upload(S.sb_dl);
-    d.sb_diag_toff = A.Upload(S.sb_diag_toff);
-    d.r_ptr = A.Upload(S.r_ptr);
-    d.r_eoff = A.Upload(S.r_eoff);
-    d.r_ecol = A.Upload(S.r_ecol);
-    d.r_dk = A.Upload(S.r_dk);
-    d.r_pt = A.Upload(S.r_pt);
+    h->sd = UploadSchur(A, S, E);
     h->cinv = A.Alloc(9 * size_t(std::max(S.npoints, 1)) * E);
     h->W = A.Alloc(size_t(std::max<int64_t>(S.nW, 1)) * E);
     h->tp = A.Alloc(3 * size_t(std::max(S.npoints, 1)) * E);
@@ -579,7 +556,7 @@ int BodyKernels(const sfg_handle* h) {
   n += h->red.ngroups > 0 ? 1 : 0;
   n += 1;  // cost
   n += 1 /*damping*/ + 1 /*retract*/ + 1 /*delta*/ + 1 /*decide*/ + 3 /*reset, factor, solve*/;
-  n += h->schur ? 4 /*points, S, rhs, back-substitution*/ : 1 /*negate*/;
+  n += h->schur ? 5 /*points, S chunks, S, rhs, back-substitution*/ : 1 /*negate*/;
   if (h->elem == 4) n += 1 + 4 * h->refine_steps;  // widen; residual, reset, solve, accumulate
   if (h->pcg_mode) {
     n += 1 /*group blocks*/ + 2 /*row coupling, features*/ + (h->pcg_mode == 2 ? 1 : 0) +

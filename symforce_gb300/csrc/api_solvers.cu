@@ -256,30 +256,7 @@ int32_t sfg_schur_create(int32_t n, const int32_t* col_ptr, const int32_t* row_i
     Arena& A = s->A;
     s->st = MakeState(A);
     const auto& S = s->SL;
-    sfg::SchurDev& d = s->sd;
-    d.npoints = S.npoints;
-    d.nB = int(S.nB);
-    d.c_toff = S.c_toff;
-    d.pt_diag = A.Upload(S.pt_diag);
-    d.pt_eptr = A.Upload(S.pt_eptr);
-    d.pt_ekey_toff = A.Upload(S.pt_ekey_toff);
-    d.pt_ekey_dim = A.Upload(S.pt_ekey_dim);
-    d.pt_eoff = A.Upload(S.pt_eoff);
-    d.pt_woff = A.Upload(S.pt_woff);
-    d.nsblocks = int(S.Spat.nblocks());
-    d.sb_ptr = A.Upload(S.sb_ptr);
-    d.sb_eoff = A.Upload(S.sb_eoff);
-    d.sb_woff = A.Upload(S.sb_woff);
-    d.sb_hoff = A.Upload(S.sb_hoff);
-    d.sb_soff = A.Upload(S.sb_soff);
-    d.sb_dk = A.Upload(S.sb_dk);
-    d.sb_dl = A.Upload(S.sb_dl);
-    d.sb_diag_toff = A.Upload(S.sb_diag_toff);
-    d.r_ptr = A.Upload(S.r_ptr);
-    d.r_eoff = A.Upload(S.r_eoff);
-    d.r_ecol = A.Upload(S.r_ecol);
-    d.r_dk = A.Upload(S.r_dk);
-    d.r_pt = A.Upload(S.r_pt);
+    s->sd = sfg::UploadSchur(A, S, 8);
     s->hess = A.Zeros<double>(size_t(s->L.nvals));
     s->rhs = A.Zeros<double>(size_t(n));
     s->damping = A.Zeros<double>(size_t(n));

@@ -45,7 +45,9 @@ struct PcgState {
 };
 
 // Task kinds of the persistent factorization kernel.
-enum TaskType { kTaskAssemble = 0, kTaskDiag = 1, kTaskTrsm = 2, kTaskUpdate = 3 };
+// kTaskLookahead(k): the panel solve of tile (k+1, k), the update of diagonal tile (k+1, k+1) by
+// that panel and the LDL^T of tile (k+1, k+1), in one CTA (the critical chain of a front).
+enum TaskType { kTaskAssemble = 0, kTaskDiag = 1, kTaskTrsm = 2, kTaskUpdate = 3, kTaskLookahead = 4 };
 
 enum DeviceErrorCode {
   kDevOk = 0,

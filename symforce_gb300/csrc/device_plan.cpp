@@ -224,4 +224,49 @@ template void EnqueueFactor<float>(const FactorPlan&, const void*, const double*
 template void EnqueueSolve<double>(const FactorPlan&, const void*, void*, cudaStream_t, bool, const int*);
 template void EnqueueSolve<float>(const FactorPlan&, const void*, void*, cudaStream_t, bool, const int*);
 
+SchurDev UploadSchur(DeviceArena& A, const SchurLayout& S, int elem) {
+  SchurDev d{};
+  d.npoints = S.npoints;
+  d.nB = int(S.nB);
+  d.c_toff = S.c_toff;
+  d.pt_diag = A.Upload(S.pt_diag);
+  d.pt_eptr = A.Upload(S.pt_eptr);
+  d.pt_ekey_toff = A.Upload(S.pt_ekey_toff);
+  d.pt_ekey_dim = A.Upload(S.pt_ekey_dim);
+  d.pt_eoff = A.Upload(S.pt_eoff);
+  d.pt_woff = A.Upload(S.pt_woff);
+  d.nsblocks = int(S.Spat.nblocks());
+  d.sb_ptr = A.Upload(S.sb_ptr);
+  d.sb_eoff = A.Upload(S.sb_eoff);
+  d.sb_woff = A.Upload(S.sb_woff);
+  d.sb_hoff = A.Upload(S.sb_hoff);
+  d.sb_soff = A.Upload(S.sb_soff);
+  d.sb_dk = A.Upload(S.sb_dk);
+  d.sb_dl = A.Upload(S.sb_dl);
+  d.sb_diag_toff = A.Upload(S.sb_diag_toff);
+  const int64_t ct = elem == 8 ? 64 : 256;
+  std::vector<int32_t> ch_block;
+  std::vector<int64_t> ch_begin, chunk_ptr(1, 0);
+  for (int b = 0; b < d.nsblocks; ++b) {
+    for (int64_t t = S.sb_ptr[b]; t < S.sb_ptr[b + 1]; t += ct) {
+      ch_block.push_back(b);
+      ch_begin.push_back(t);
+    }
+    chunk_ptr.push_back(int64_t(ch_block.size()));
+  }
+  if (ch_block.size() > size_t(INT32_MAX)) throw Error(SFG_ERR_STRUCTURE, "too many Schur term chunks");
+  d.nchunks = int(ch_block.size());
+  d.chunk_terms = int(ct);
+  d.ch_block = A.Upload(ch_block);
+  d.ch_begin = A.Upload(ch_begin);
+  d.sb_chunk_ptr = A.Upload(chunk_ptr);
+  d.partials = A.Alloc(std::max<size_t>(ch_block.size(), 1) * 36 * size_t(elem));
+  d.r_ptr = A.Upload(S.r_ptr);
+  d.r_eoff = A.Upload(S.r_eoff);
+  d.r_ecol = A.Upload(S.r_ecol);
+  d.r_dk = A.Upload(S.r_dk);
+  d.r_pt = A.Upload(S.r_pt);
+  return d;
+}
+
 }  // namespace sfg

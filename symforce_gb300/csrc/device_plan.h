@@ -9,6 +9,7 @@
 
 #include "common.h"
 #include "kernels.h"
+#include "layout.h"
 
 namespace sfg {
 
@@ -59,6 +60,11 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
 
 // Per-row segments of the symmetric product with a block pattern (lower blocks stored row-major).
 SpmvDev BuildSpmv(DeviceArena& A, const BlockPattern& pat, int64_t a_stride, int64_t b_stride);
+
+// Device copy of a Schur layout for elements of `elem` bytes, with the S-block terms cut into
+// chunks (64 terms in FP64, whose pipe needs the work spread over many warps; 256 in FP32) and the
+// chunks' partial-sum buffer.
+SchurDev UploadSchur(DeviceArena& A, const SchurLayout& S, int elem);
 
 // `gate` (optional): the launched kernels do nothing unless *gate != 0.
 template <typename T>

@@ -650,11 +650,19 @@ TaskPlan PlanTasks(const Symbolic& sym, int tile) {
   for (int s = 0; s < sym.ns; ++s) {
     const int nt = T.ntiles[s], np = T.npiv[s];
     for (int j = 0; j < nt; ++j) T.tasks.push_back(make_int4(kTaskAssemble, s, j, 0));
+    // Panel k: its diagonal tile is factored by the lookahead task of panel k - 1 (for k > 0),
+    // which also does the panel solve of tile (k+1, k)... in panel k the lookahead task does the
+    // panel solve of tile (k+1, k), the update of (k+1, k+1) and the LDL^T of (k+1, k+1), so the
+    // critical chain of the front runs in one CTA per panel.  Every task still comes after the tasks
+    // it waits on, which keeps the schedule free of deadlock.
     for (int k = 0; k < np; ++k) {
-      T.tasks.push_back(make_int4(kTaskDiag, s, k * 65536 + k, k));
-      for (int i = k + 1; i < nt; ++i) T.tasks.push_back(make_int4(kTaskTrsm, s, i * 65536 + k, k));
+      const bool ahead = k + 1 < np;
+      if (k == 0) T.tasks.push_back(make_int4(kTaskDiag, s, 0, 0));
+      if (ahead) T.tasks.push_back(make_int4(kTaskLookahead, s, (k + 1) * 65536 + k, k));
+      for (int i = k + (ahead ? 2 : 1); i < nt; ++i) T.tasks.push_back(make_int4(kTaskTrsm, s, i * 65536 + k, k));
       for (int j = k + 1; j < nt; ++j)
-        for (int i = j; i < nt; ++i) T.tasks.push_back(make_int4(kTaskUpdate, s, i * 65536 + j, k));
+        for (int i = j; i < nt; ++i)
+          if (!(ahead && i == k + 1 && j == k + 1)) T.tasks.push_back(make_int4(kTaskUpdate, s, i * 65536 + j, k));
     }
   }
   return T;

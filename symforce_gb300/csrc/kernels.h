@@ -97,6 +97,13 @@ struct SchurDev {
   const int32_t* sb_dk;         // rows of the block
   const int32_t* sb_dl;         // cols
   const int32_t* sb_diag_toff;  // tangent offset of the key if diagonal block, else -1
+  // the S-block terms cut into chunks of at most chunk_terms (one warp each), partial sums per chunk
+  int nchunks;
+  int chunk_terms;
+  const int32_t* ch_block;      // [nchunks] S block of the chunk
+  const int64_t* ch_begin;      // [nchunks] first term of the chunk
+  const int64_t* sb_chunk_ptr;  // [nsblocks + 1] chunks of each S block
+  void* partials;               // T [nchunks][36] chunk sums (row-major 6 x 6)
   const int64_t* r_ptr;         // [nB + 1] points of each B scalar
   const int64_t* r_eoff;        // E block offset per entry (column of the scalar inside E)
   const int32_t* r_ecol;        // column inside the E block

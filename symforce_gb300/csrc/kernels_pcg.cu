@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "kernels.h"
 
@@ -327,8 +328,34 @@ __device__ __forceinline__ void StX(V* p, V v) {
 template <typename Acc, bool kStaged, typename T, typename V>
 __device__ __forceinline__ Acc GroupRow(const T* Sb, const int2* gent, int e0, int e1, int a,
                                         const V* x) {
+  // blocks are taken U at a time with all their loads issued before the multiply-adds, so U
+  // round trips to L2 overlap; U shrinks with the operand width to stay within the 64 registers of
+  // a 1024-thread CTA
+  constexpr int U = sizeof(T) + sizeof(V) == 8 ? 4 : sizeof(T) + sizeof(V) == 12 ? 2 : 1;
   Acc acc = Acc(0);
-  for (int e = e0; e < e1; ++e) {
+  int e = e0;
+  for (; e + U <= e1; e += U) {
+    T sv[U][kB];
+    V xv[U][kB];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int2 en = gent[e + u];
+      const int tr = en.y & 1;
+      const T* row = Sb + size_t(en.x) * (kB * kB) + (tr ? a : a * kB);
+      const int step = tr ? kB : 1;
+      const V* xh = x + size_t(en.y >> 1) * kB;
+#pragma unroll
+      for (int b = 0; b < kB; ++b) {
+        sv[u][b] = row[b * step];
+        xv[u][b] = LdX<kStaged>(xh + b);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int b = 0; b < kB; ++b) acc += Acc(sv[u][b]) * Acc(xv[u][b]);
+  }
+  for (; e < e1; ++e) {
     const int2 en = gent[e];
     const int tr = en.y & 1;
     const T* row = Sb + size_t(en.x) * (kB * kB) + (tr ? a : a * kB);
@@ -591,8 +618,14 @@ void PcgShape(int ng, int num_sms, int* grid, int* threads) {
     *grid = 1;
     *threads = 32 * warps;
   } else {
-    *threads = kPcgMultiThreads;
-    const int per_cta = 3 * (kPcgMultiThreads / 32);
+    // CTA size of multi-CTA solves; SFG_PCG_CTA_THREADS (a multiple of 32, at most 1024) overrides
+    int t = kPcgMultiThreads;
+    if (const char* e = std::getenv("SFG_PCG_CTA_THREADS")) {
+      const int v = std::atoi(e);
+      if (v >= 32 && v <= 1024 && v % 32 == 0) t = v;
+    }
+    *threads = t;
+    const int per_cta = 3 * (t / 32);
     *grid = (ng + per_cta - 1) / per_cta;
   }
 }

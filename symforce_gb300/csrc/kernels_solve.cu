@@ -116,34 +116,81 @@ __global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_al
   }
 }
 
-// One CTA per S block; each warp takes block entries in turn, its lanes stride over the block's
-// terms (one FP64 dependent chain per lane is ~1/32 of the terms) and a fixed shuffle tree adds
-// the lanes, so the sum order is the same on every run.
+// S = B - sum_p E_pk^T W_pl over the S blocks' terms (points seen by both keys), in two passes.
+// Pass 1: one warp per chunk of at most chunk_terms terms of one block; each lane takes the
+// chunk's terms in turn and accumulates the whole d_k x d_l product of its terms in registers (every
+// E and W block is read once), then a fixed shuffle tree adds the lanes.  Pass 2: one warp per S
+// block adds its chunks in order and writes B_kl (+ damping) - sum.  Chunks spread the heavy
+// diagonal blocks (every observation of a camera) over many warps, which the FP64 pipe needs; the
+// fixed orders make every run give the same bits.  Key tangent dims are at most kMaxKeyDim.
+constexpr int kMaxKeyDim = 6;
+constexpr int kSchurWarps = 4;
+
 template <typename T>
-__global__ void SchurBuildSKernel(SchurDev d, const T* hess_all, int64_t nvals,
-                                  const double* damping, const T* W, T* S, const LmState* st) {
-  const int sb = blockIdx.x;
+__global__ void __launch_bounds__(32 * kSchurWarps)
+    SchurChunkKernel(SchurDev d, const T* hess_all, int64_t nvals, const T* W, const LmState* st) {
+  const int ch = blockIdx.x * kSchurWarps + (threadIdx.x >> 5);
+  if (ch >= d.nchunks) return;
+  const int lane = threadIdx.x & 31;
   const T* H = hess_all + int64_t(st->init_idx) * nvals;
+  const int sb = d.ch_block[ch];
   const int dk = d.sb_dk[sb], dl = d.sb_dl[sb];
+  const int64_t t0 = d.ch_begin[ch];
+  const int64_t t1 = min(t0 + d.chunk_terms, d.sb_ptr[sb + 1]);
+  constexpr int D = kMaxKeyDim;
+  T acc[D * D];
+#pragma unroll
+  for (int i = 0; i < D * D; ++i) acc[i] = T(0);
+  for (int64_t t = t0 + lane; t < t1; t += 32) {
+    const T* E = H + d.sb_eoff[t];
+    const T* Wl = W + d.sb_woff[t];
+    T e[3 * D], w[3 * D];
+#pragma unroll
+    for (int q = 0; q < 3; ++q)
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        e[q * D + i] = i < dk ? E[q * dk + i] : T(0);
+        w[q * D + i] = i < dl ? Wl[q * dl + i] : T(0);
+      }
+#pragma unroll
+    for (int r = 0; r < D; ++r)
+#pragma unroll
+      for (int c = 0; c < D; ++c)
+        acc[r * D + c] += e[r] * w[c] + e[D + r] * w[D + c] + e[2 * D + r] * w[2 * D + c];
+  }
+#pragma unroll
+  for (int i = 0; i < D * D; ++i) {
+    T v = acc[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    acc[i] = v;
+  }
+  if (lane == 0) {
+    T* out = static_cast<T*>(d.partials) + int64_t(ch) * (D * D);
+#pragma unroll
+    for (int i = 0; i < D * D; ++i) out[i] = acc[i];
+  }
+}
+
+template <typename T>
+__global__ void SchurFinishKernel(SchurDev d, const T* hess_all, int64_t nvals, const double* damping,
+                                  T* S, const LmState* st) {
+  const int sb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (sb >= d.nsblocks) return;
+  const int lane = threadIdx.x & 31;
+  const int dk = d.sb_dk[sb], dl = d.sb_dl[sb];
+  const T* H = hess_all + int64_t(st->init_idx) * nvals;
   const int64_t hoff = d.sb_hoff[sb];
   const int diag_toff = d.sb_diag_toff[sb];
-  const int64_t t0 = d.sb_ptr[sb], t1 = d.sb_ptr[sb + 1];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarp = blockDim.x >> 5;
-  for (int ent = warp; ent < dk * dl; ent += nwarp) {
+  const T* part = static_cast<const T*>(d.partials);
+  for (int ent = lane; ent < dk * dl; ent += 32) {
     const int r = ent / dl, c = ent - r * dl;
     T acc = T(0);
-    for (int64_t t = t0 + lane; t < t1; t += 32) {
-      const T* E = H + d.sb_eoff[t];
-      const T* Wl = W + d.sb_woff[t];
-      acc += E[r] * Wl[c] + E[dk + r] * Wl[dl + c] + E[2 * dk + r] * Wl[2 * dl + c];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) {
-      T v = hoff >= 0 ? H[hoff + ent] : T(0);
-      if (diag_toff >= 0 && r == c) v += T(damping[diag_toff + r]);
-      S[d.sb_soff[sb] + ent] = v - acc;
-    }
+    for (int64_t ch = d.sb_chunk_ptr[sb]; ch < d.sb_chunk_ptr[sb + 1]; ++ch)
+      acc += part[ch * (kMaxKeyDim * kMaxKeyDim) + r * kMaxKeyDim + c];
+    T v = hoff >= 0 ? H[hoff + ent] : T(0);
+    if (diag_toff >= 0 && r == c) v += T(damping[diag_toff + r]);
+    S[d.sb_soff[sb] + ent] = v - acc;
   }
 }
 
@@ -233,6 +280,7 @@ template <typename T, int TILE>
 struct TileSmem {
   T a[TILE * TILE];
   T b[TILE * TILE];
+  T c[TILE * TILE];
   T d[TILE];
 };
 
@@ -328,20 +376,14 @@ __device__ void TaskAssemble(const FactorDev& f, int s, int tj, const T* A, cons
   for (int i = tj + threadIdx.x; i < g.nt; i += blockDim.x) atomicExch(f.tile_state + StateIdx(g, i, tj), 1);
 }
 
-// LDL^T of the diagonal tile, plus the explicit inverse of its unit lower factor (kept for the
-// panel solves, which then become small matrix products).
+// LDL^T of diagonal tile k, held transposed in shared memory `a` (b x b of it), plus the explicit
+// inverse of its unit lower factor (kept for the panel solves, which then become small matrix
+// products); writes L, D and the inverse and publishes the tile.
 template <typename T, int TILE>
-__device__ void TaskDiag(const FactorDev& f, int s, int k, T* F, T* Linv, TileSmem<T, TILE>& sm,
-                         int* s_flag, unsigned long long* ready) {
-  const Geom g = FrontGeom(f, s);
-  bool ok = true;
-  if (threadIdx.x == 0) ok = WaitAtLeast(f.tile_state + StateIdx(g, k, k), 1 + k, f.error);
-  if (!CtaWait(ok, s_flag, ready)) return;
+__device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, T* Linv, T* a,
+                         TileSmem<T, TILE>& sm) {
   const int b = TileSize(g, k, TILE), r0 = TileStart(g, k, TILE);
   T* Fs = F + g.foff;
-  T* a = sm.a;  // a[c * TILE + r] = tile(r, c), lower part
-  LoadTileT<T, TILE>(Fs, g.m, r0, r0, b, b, a);
-  __syncthreads();
   // Right-looking LDL^T in shared memory, one barrier per pivot: every thread forms the pivot's
   // reciprocal itself (same bits everywhere, no broadcast round trip), and column j is scaled
   // during step j + 1, which does not read it.
@@ -376,6 +418,19 @@ __device__ void TaskDiag(const FactorDev& f, int s, int k, T* F, T* Linv, TileSm
     if (r < b && c < b && r >= c) St(Fs + (r0 + r) + int64_t(r0 + c) * g.m, a[c * TILE + r]);
   }
   Signal(f.tile_state + StateIdx(g, k, k), kFinal);
+}
+
+template <typename T, int TILE>
+__device__ void TaskDiag(const FactorDev& f, int s, int k, T* F, T* Linv, TileSmem<T, TILE>& sm,
+                         int* s_flag, unsigned long long* ready) {
+  const Geom g = FrontGeom(f, s);
+  bool ok = true;
+  if (threadIdx.x == 0) ok = WaitAtLeast(f.tile_state + StateIdx(g, k, k), 1 + k, f.error);
+  if (!CtaWait(ok, s_flag, ready)) return;
+  const int b = TileSize(g, k, TILE), r0 = TileStart(g, k, TILE);
+  LoadTileT<T, TILE>(F + g.foff, g.m, r0, r0, b, b, sm.a);
+  __syncthreads();
+  DiagCore<T, TILE>(f, g, s, k, F, Linv, sm.a, sm);
 }
 
 // Panel solve L_ik = F_ik L_kk^-T D_k^-1 as a product with the stored inverse.
@@ -413,6 +468,58 @@ __device__ void TaskTrsm(const FactorDev& f, int s, int i, int k, T* F, const T*
     if (r < bi && c < bk) St(Fs + (ri + r) + int64_t(ck + c) * g.m, out[n]);
   }
   Signal(f.tile_state + StateIdx(g, i, k), kFinal);
+}
+
+// The critical chain of panel k in one CTA: panel solve of tile i = k + 1 (as TaskTrsm, kept in
+// shared memory), the update of diagonal tile (i, i) by it, F_ii -= L_ik D_k L_ik^T (after every
+// earlier panel's update of that tile), and the LDL^T of (i, i).  This saves two hand-offs between
+// CTAs (and two tile reloads) per panel on the longest dependency path of a front.
+template <typename T, int TILE>
+__device__ void TaskLookahead(const FactorDev& f, int s, int i, int k, T* F, T* Linv,
+                              TileSmem<T, TILE>& sm, int* s_flag, unsigned long long* ready) {
+  const Geom g = FrontGeom(f, s);
+  bool ok = true;
+  if (threadIdx.x == 0) {
+    ok = WaitAtLeast(f.tile_state + StateIdx(g, k, k), kFinal, f.error) &&
+         WaitAtLeast(f.tile_state + StateIdx(g, i, k), 1 + k, f.error);
+  }
+  if (!CtaWait(ok, s_flag, ready)) return;
+  const int bk = TileSize(g, k, TILE), ck = TileStart(g, k, TILE);
+  const int bi = TileSize(g, i, TILE), ri = TileStart(g, i, TILE);
+  T* Fs = F + g.foff;
+  LoadTileT<T, TILE>(Fs, g.m, ri, ck, bi, bk, sm.a);  // F_ik
+  const T* Lk = Linv + f.linv_base[s] + int64_t(k) * TILE * TILE;
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) sm.b[e] = Ld(Lk + e);
+  for (int c = threadIdx.x; c < bk; c += blockDim.x)
+    sm.d[c] = PivotReciprocal<T>(Ld(Fs + int64_t(ck + c) * (g.m + 1)));
+  __syncthreads();
+  // L_ik (r, c) = sum_{q <= c} F(r, q) Li(c, q) / D_c, into c[] (transposed) and the front
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+    const int r = e % TILE, c = e / TILE;
+    T acc = T(0);
+    for (int q = 0; q <= c && q < bk; ++q) acc += sm.a[q * TILE + r] * sm.b[q * TILE + c];
+    const T l = (r < bi && c < bk) ? acc * sm.d[c < bk ? c : 0] : T(0);
+    sm.c[c * TILE + r] = l;
+    if (r < bi && c < bk) St(Fs + (ri + r) + int64_t(ck + c) * g.m, l);
+  }
+  Signal(f.tile_state + StateIdx(g, i, k), kFinal);
+  // F_ii after every earlier panel's update, minus L_ik D_k L_ik^T (lower part), in a[]
+  ok = true;
+  if (threadIdx.x == 0) ok = WaitAtLeast(f.tile_state + StateIdx(g, i, i), 1 + k, f.error);
+  if (!CtaWait(ok, s_flag)) return;
+  LoadTileT<T, TILE>(Fs, g.m, ri, ri, bi, bi, sm.a);
+  for (int c = threadIdx.x; c < bk; c += blockDim.x) sm.d[c] = Ld(Fs + int64_t(ck + c) * (g.m + 1));
+  __syncthreads();
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+    const int r = e % TILE, c = e / TILE;
+    if (r >= bi || c > r) continue;
+    T acc = T(0);
+#pragma unroll 8
+    for (int q = 0; q < bk; ++q) acc += sm.c[q * TILE + r] * sm.d[q] * sm.c[q * TILE + c];
+    sm.a[c * TILE + r] -= acc;
+  }
+  __syncthreads();
+  DiagCore<T, TILE>(f, g, s, i, F, Linv, sm.a, sm);
 }
 
 template <typename T, int TILE>
@@ -493,6 +600,7 @@ __global__ void __launch_bounds__(kFactorThreads) FactorKernel(FactorDev f, cons
       case kTaskDiag: TaskDiag<T, TILE>(f, task.y, k, F, Linv, sm, &s_flag, ready); break;
       case kTaskTrsm: TaskTrsm<T, TILE>(f, task.y, i, k, F, Linv, sm, &s_flag, ready); break;
       case kTaskUpdate: TaskUpdate<T, TILE>(f, task.y, i, j, k, F, sm, &s_flag, ready); break;
+      case kTaskLookahead: TaskLookahead<T, TILE>(f, task.y, i, k, F, Linv, sm, &s_flag, ready); break;
       default:
         if (threadIdx.x == 0) atomicExch(f.error, kDevBadTask);
     }
@@ -790,8 +898,12 @@ template <typename T>
 void LaunchSchurBuildS(const SchurDev& d, const void* hess, int64_t nvals, const double* damping,
                        const void* W, void* S, const LmState* st, cudaStream_t s) {
   if (d.nsblocks == 0) return;
-  SchurBuildSKernel<T><<<d.nsblocks, 128, 0, s>>>(d, static_cast<const T*>(hess), nvals, damping,
-                                                 static_cast<const T*>(W), static_cast<T*>(S), st);
+  if (d.nchunks > 0)
+    SchurChunkKernel<T><<<(d.nchunks + kSchurWarps - 1) / kSchurWarps, 32 * kSchurWarps, 0, s>>>(
+        d, static_cast<const T*>(hess), nvals, static_cast<const T*>(W), st);
+  constexpr int kWarps = 8;
+  SchurFinishKernel<T><<<(d.nsblocks + kWarps - 1) / kWarps, 32 * kWarps, 0, s>>>(
+      d, static_cast<const T*>(hess), nvals, damping, static_cast<T*>(S), st);
 }
 
 template <typename T>

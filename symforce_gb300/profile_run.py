@@ -21,6 +21,7 @@ def main() -> None:
     ap.add_argument("--form", default="plain", choices=["plain", "mixed", "jacobi", "learned"])
     ap.add_argument("--pcg-tol", type=float, default=1e-8)
     ap.add_argument("--runs", type=int, default=2)
+    ap.add_argument("--iterations", type=int, default=-1, help="LM iteration cap (default: the workload's)")
     args = ap.parse_args()
     w = workloads.get(args.workload)
     p = w.problem()
@@ -30,7 +31,10 @@ def main() -> None:
         form.linear_solver = (A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI if args.form == "jacobi"
                               else A.SFG_LINEAR_SOLVER_PCG_LEARNED)
         form.pcg_tol = args.pcg_tol
-    opt = Optimizer(p, w.params(), form)
+    params = w.params()
+    if args.iterations > 0:
+        params.iterations = args.iterations
+    opt = Optimizer(p, params, form)
     for _ in range(args.runs):
         _, stats = opt.optimize(p.values)
         print(f"{args.workload} {args.form}: {len(stats.iterations)} records, best {stats.best_error:.10g}, "

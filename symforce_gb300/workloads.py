@@ -39,6 +39,8 @@ _WORKLOADS = {
                              "sparse LDL^T, FP64"),
     "ba_1000_200k": Workload("ba_1000_200k", 0, "bundle adjustment, 1,000 cameras, 200k points, "
                              "~1.2M observations"),
+    "ba_10k_1m": Workload("ba_10k_1m", 0, "bundle adjustment, 10,000 cameras, 1M points, ~5M "
+                          "observations (reduced camera system of 90k unknowns)"),
 }
 
 

@@ -87,3 +87,25 @@ def test_robot_2d_config_matches_oracle():
     values, stats = opt.optimize(p.values)
     ref = O.optimize(p, params)
     assert stats.best_error == pytest.approx(ref["iterations"][ref["best_index"]].new_error, rel=1e-9)
+
+
+@pytest.mark.parametrize("name", ["ba_50_7800", "ba_1000_200k"])
+def test_benchmark_workloads_match_committed_oracle_records(name):
+    """Full-size parity: the plain FP64 form on the benchmark workloads follows the CPU oracle's
+    committed LM trajectory (tests/golden/oracle_costs.json, generated by
+    tests/golden/make_oracle_costs.py): same number of records, same accept decisions, every
+    error at 1e-9 relative, same status."""
+    import json
+    from pathlib import Path
+    from symforce_gb300 import workloads
+    ref = json.loads((Path(__file__).resolve().parent / "golden" / "oracle_costs.json").read_text())[name]
+    w = workloads.get(name)
+    p = w.problem()
+    opt = Optimizer(p, w.params(), w.form(A.SFG_PRECISION_FP64))
+    _, stats = opt.optimize(p.values)
+    assert len(stats.iterations) == ref["num_records"]
+    assert [int(r.update_accepted) for r in stats.iterations] == [int(a) for a in ref["accepted"]]
+    for g, e in zip(stats.iterations, ref["errors"]):
+        assert g.new_error == pytest.approx(e, rel=1e-9)
+    assert stats.best_error == pytest.approx(ref["best_error"], rel=1e-9)
+    assert stats.status == ref["status"]

@@ -110,13 +110,19 @@ def test_learned_form_reaches_oracle_cost_on_benchmark_workload():
     p = wl.problem()
     ref = json.loads((ROOT / "tests" / "golden" / "oracle_costs.json").read_text())["ba_50_7800"]["best_error"]
     for precision in (A.SFG_PRECISION_FP64, A.SFG_PRECISION_MIXED):
-        opt = Optimizer(p, wl.params(), A.default_form_params(precision=precision,
-                                                            linear_solver=A.SFG_LINEAR_SOLVER_PCG_LEARNED))
+        # the oracle stops on the reference's early-exit rule (relative reduction < 1e-6); the mixed
+        # form's LM path differs, and by the same rule it can stop up to ~1e-6 above the oracle's
+        # cost, so it runs on (relative reduction < 1e-9, as the benchmark does for every form but
+        # the plain one)
+        params = wl.params()
+        if precision == A.SFG_PRECISION_MIXED:
+            params.early_exit_min_reduction = 1e-9
+        opt = Optimizer(p, params, A.default_form_params(precision=precision,
+                                                        linear_solver=A.SFG_LINEAR_SOLVER_PCG_LEARNED))
         _, stats = opt.optimize(p.values)
         best = min(r.best_error for r in stats.iterations)
-        # "reaches the oracle's cost": at or below it within 1e-6.  The oracle stops on the early-exit
-        # rule (relative reduction < 1e-6), so a form whose LM path differs by rounding may stop a
-        # little lower on the same minimum (seen: -1.9e-6 relative); a different minimum would be far off.
+        # "reaches the oracle's cost": at or below it within 1e-6 (below is possible: the oracle
+        # stopped on its early-exit rule); a different minimum would be far off
         assert best <= ref * (1 + 1e-6), (precision, best, ref)
         assert best >= ref * (1 - 1e-5), (precision, best, ref)
         ps = opt.pcg_stats()
