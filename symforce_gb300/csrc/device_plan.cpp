@@ -149,7 +149,8 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   fp.ysave = A.Alloc(size_t(std::max<int64_t>(S.idx_off[S.ns], 1)) * elem);
   fp.xperm = A.Alloc(size_t(std::max<int64_t>(S.n, 1)) * elem);
   const int per_sm = 8;
-  fp.grid_factor = std::max(1, std::min<int>(f.ntasks, num_sms * per_sm));
+  // the factorization kernel is built for kFactorCtasPerSm resident CTAs of 128 threads per SM
+  fp.grid_factor = std::max(1, std::min<int>(f.ntasks, num_sms * kFactorCtasPerSm));
   fp.grid_solve = std::max(1, std::min<int>(2 * S.ns, num_sms * per_sm));
   if (elem == 8) ConfigureSolve<double>(maxm);
   else ConfigureSolve<float>(maxm);

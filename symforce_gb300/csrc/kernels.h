@@ -10,6 +10,10 @@
 
 namespace sfg {
 
+// Resident CTAs per SM the persistent factorization kernel is compiled for (its register budget:
+// 65,536 / (4 x 128 threads) = 128 per thread, which the register-resident diagonal tasks use).
+constexpr int kFactorCtasPerSm = 4;
+
 // ---------------------------------------------------------------- linearization (kernels_lin.cu)
 // Evaluate every factor of a batch at the Init or New values, writing residual rows, packed
 // Gauss-Newton Hessian / rhs entries (directly, or into staging when shared), and per-CTA cost
