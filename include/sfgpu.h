@@ -191,7 +191,7 @@ typedef struct sfg_form_params_t {
   int32_t ordering;       /* SFG_ORDERING_* (block level) */
   int32_t device;         /* CUDA device ordinal */
   double epsilon;         /* the Optimizer's epsilon (symforce/opt/optimizer.h:90-94); default 10 * DBL_EPSILON */
-  int32_t refine_steps;   /* MIXED: FP64 iterative-refinement steps per linear solve (default 2) */
+  int32_t refine_steps;   /* MIXED: FP64 iterative-refinement steps per linear solve (default 1) */
   int32_t pcg_max_iters;  /* PCG forms: iteration cap of one reduced-system solve (default 500) */
   double pcg_tol;         /* PCG forms: FP64 relative residual target (default 1e-8) */
 } sfg_form_params_t;

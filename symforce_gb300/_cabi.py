@@ -213,7 +213,7 @@ def default_form_params(**overrides) -> FormParams:
         ordering=SFG_ORDERING_NESTED_DISSECTION,
         device=0,
         epsilon=DEFAULT_EPSILON,
-        refine_steps=2,
+        refine_steps=1,
         pcg_max_iters=500,
         pcg_tol=1e-8,
     )

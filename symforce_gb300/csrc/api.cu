@@ -619,7 +619,7 @@ void sfg_default_form_params(sfg_form_params_t* o) {
   o->ordering = SFG_ORDERING_NESTED_DISSECTION;
   o->device = 0;
   o->epsilon = 10 * DBL_EPSILON;
-  o->refine_steps = 2;
+  o->refine_steps = 1;
   o->pcg_max_iters = 500;
   o->pcg_tol = 1e-8;
 }

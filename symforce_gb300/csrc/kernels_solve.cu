@@ -662,6 +662,10 @@ __global__ void __launch_bounds__(kFactorThreads, kFactorCtasPerSm) FactorKernel
 // a front costs one synchronization per panel rather than one per column.
 // ---------------------------------------------------------------------------------------------
 constexpr int kSolvePanel = 32;
+// Threads of a solve task: the rows below a panel are updated one row per thread, each row a chain
+// of kSolvePanel dependent multiply-adds after one round of L2 loads, so more threads shorten the
+// panel step of a wide front (256: a 450-wide front needs at most two rows per thread).
+constexpr int kSolveThreads = 256;
 
 template <typename T>
 __device__ void ForwardFront(const FactorDev& f, const Geom& g, const T* Fs, T* xs) {
@@ -726,7 +730,7 @@ __device__ void BackwardFront(const FactorDev& f, const Geom& g, const T* Fs, T*
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kFactorThreads) SolveKernel(FactorDev f, const T* F, const T* b,
+__global__ void __launch_bounds__(kSolveThreads) SolveKernel(FactorDev f, const T* F, const T* b,
                                                               T* ycon, T* ysave, T* xperm, T* x) {
   extern __shared__ unsigned char smem_raw[];
   T* xs = reinterpret_cast<T*>(smem_raw);
@@ -983,7 +987,7 @@ void LaunchSolve(const FactorDev& f, const void* F, const void* b, void* ycon, v
                  void* xperm, void* x, int grid, cudaStream_t s) {
   // dynamic shared memory: the largest front's scalars
   const size_t smem = size_t(f.max_m) * sizeof(T);
-  SolveKernel<T><<<grid, kFactorThreads, smem, s>>>(
+  SolveKernel<T><<<grid, kSolveThreads, smem, s>>>(
       f, static_cast<const T*>(F), static_cast<const T*>(b), static_cast<T*>(ycon),
       static_cast<T*>(ysave), static_cast<T*>(xperm), static_cast<T*>(x));
 }
