@@ -372,6 +372,12 @@ int32_t sfg_schur_factorize(sfg_schur* s, const double* values);
 int32_t sfg_schur_solve(sfg_schur* s, const double* b, double* x, int32_t nrhs);
 int32_t sfg_schur_destroy(sfg_schur* s);
 
+/* Self-test of the device wait caps (no counterpart in the reference): one CTA waits, with the
+ * capped dependency wait of the persistent kernels, for a flag that nothing sets.  The cap ends
+ * the wait without a fault; *device_status receives the device error word (1: a wait hit its cap)
+ * and *ms (optional) the kernel's duration.  The device stays usable afterwards. */
+int32_t sfg_selftest_wait_cap(int32_t device, int32_t* device_status, double* ms);
+
 /* -------------------------------- dense solve without allocation ----------------------------
  * No counterpart in the reference.  Solves A x = b for a dense symmetric positive definite n x n
  * matrix (LDL^T, unit L, no pivoting; only the lower triangle of A is read) for callers that

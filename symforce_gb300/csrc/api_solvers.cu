@@ -327,4 +327,41 @@ int32_t sfg_schur_destroy(sfg_schur* s) {
   return SFG_OK;
 }
 
+int32_t sfg_selftest_wait_cap(int32_t device, int32_t* device_status, double* ms) {
+  return Guard([&] {
+    if (!device_status) throw Error(SFG_ERR_INVALID_ARGUMENT, "device_status is null");
+    SelectDevice(device);
+    int* buf = nullptr;  // [0]: the flag nothing sets, [1]: the error word
+    SFG_CUDA(cudaMalloc(&buf, 2 * sizeof(int)));
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&] {
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+      if (st) cudaStreamDestroy(st);
+      cudaFree(buf);
+    };
+    try {
+      SFG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+      SFG_CUDA(cudaEventCreate(&e0));
+      SFG_CUDA(cudaEventCreate(&e1));
+      SFG_CUDA(cudaMemsetAsync(buf, 0, 2 * sizeof(int), st));
+      SFG_CUDA(cudaEventRecord(e0, st));
+      SFG_CUDA(sfg::LaunchWaitCapSelfTest(buf, buf + 1, st));
+      SFG_CUDA(cudaEventRecord(e1, st));
+      SFG_CUDA(cudaStreamSynchronize(st));
+      int err = 0;
+      SFG_CUDA(cudaMemcpy(&err, buf + 1, sizeof(int), cudaMemcpyDeviceToHost));
+      float t = 0.f;
+      SFG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+      *device_status = err;
+      if (ms) *ms = double(t);
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
+  });
+}
+
 }  // extern "C"

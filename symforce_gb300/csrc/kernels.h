@@ -198,6 +198,8 @@ template <typename T>
 void LaunchSolve(const FactorDev& f, const void* F, const void* b, void* ycon, void* ysave,
                  void* xperm, void* x, int grid, cudaStream_t s);
 int FactorThreads();
+// One CTA waits (capped) for *flag >= 1 while nothing sets it; the cap sets *err.
+cudaError_t LaunchWaitCapSelfTest(const int* flag, int* err, cudaStream_t s);
 void LaunchResetFactorState(int* tile_state, int nstates, int* front_flags, int nflags,
                             int* counters, cudaStream_t s, const int* gate = nullptr);
 template <typename T>

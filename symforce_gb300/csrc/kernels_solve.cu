@@ -923,6 +923,19 @@ template void LaunchAccumulate<float>(const void*, double*, int64_t, cudaStream_
 
 int FactorThreads() { return kFactorThreads; }
 
+namespace {
+// Self-test of the capped dependency wait: thread 0 waits for a flag that nothing sets, with the
+// same wait the persistent kernels use; the cap ends the wait and sets the error word.
+__global__ void WaitCapSelfTestKernel(const int* flag, int* err) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) (void)WaitAtLeast(flag, 1, err);
+}
+}  // namespace
+
+cudaError_t LaunchWaitCapSelfTest(const int* flag, int* err, cudaStream_t s) {
+  WaitCapSelfTestKernel<<<1, 32, 0, s>>>(flag, err);
+  return cudaGetLastError();
+}
+
 template <typename T>
 void ConfigureSolve(int max_m) {
   const size_t smem = size_t(max_m) * sizeof(T);

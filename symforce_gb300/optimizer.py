@@ -211,6 +211,33 @@ class Optimizer:
         _check(lib().sfg_hessian_lower(self._h, C.byref(nnz), A.iptr(colptr), A.iptr(rowidx), A.dptr(hv)))
         return dict(residual=res, rhs=rhs, error=err.value, colptr=colptr, rowidx=rowidx, hvals=hv)
 
+    def compute_covariances(self, values: np.ndarray, num_keys: int) -> dict:
+        """Optimizer::ComputeCovariances with a block-diagonal C (symforce/opt/optimizer.tcc:176-199,
+        symforce/opt/internal/covariance_utils.h:116-140): the marginal covariance of the first
+        `num_keys` keys of the key order at `values`.  The trailing block C of the undamped Hessian
+        is damped by the optimizer's epsilon, the reduced system S = B - E C^-1 E^T is factored on
+        the GPU (SparseSchurSolver: point inverses, S, LDL^T) and S^-1 = (H^-1)_BB is formed by one
+        solve with the identity on B as right-hand sides.  Returns {key index: covariance block}."""
+        if not 0 < num_keys < len(self.problem.key_types):
+            raise ValueError("num_keys must leave a non-empty trailing block to eliminate")
+        dims = [A.KEY_DIMS[int(t)][1] for t in self.problem.key_types]
+        offs = np.concatenate([[0], np.cumsum(dims)])
+        block_dim = int(offs[num_keys])
+        n = int(offs[-1])
+        lin = self.linearize(values)
+        colptr, rowidx, hv = lin["colptr"], lin["rowidx"], lin["hvals"].copy()
+        for j in range(block_dim, n):  # damp the diagonal of C
+            q = np.searchsorted(rowidx[colptr[j]:colptr[j + 1]], j) + colptr[j]
+            if q >= colptr[j + 1] or rowidx[q] != j:
+                raise SfgError(A.SFG_ERR_STRUCTURE, f"Hessian column {j} has no diagonal entry")
+            hv[q] += self.form.epsilon
+        solver = SparseSchur(n, colptr, rowidx, n - block_dim, device=self.form.device)
+        solver.factorize(hv)
+        rhs = np.zeros((n, block_dim))
+        rhs[:block_dim, :block_dim] = np.eye(block_dim)
+        cov = solver.solve(rhs)[:block_dim]
+        return {k: cov[offs[k]:offs[k + 1], offs[k]:offs[k + 1]].copy() for k in range(num_keys)}
+
     def permutation(self) -> np.ndarray:
         n = self.form.linear_solver in A.SCHUR_SOLVERS
         size = self.tangent_dim - (3 * self.problem.num_schur_keys if n else 0)

@@ -109,3 +109,32 @@ def test_benchmark_workloads_match_committed_oracle_records(name):
         assert g.new_error == pytest.approx(e, rel=1e-9)
     assert stats.best_error == pytest.approx(ref["best_error"], rel=1e-9)
     assert stats.status == ref["status"]
+
+
+def test_compute_covariances_matches_dense_inverse():
+    """Optimizer::ComputeCovariances (Schur over the points, C damped by epsilon): per-key marginal
+    covariances of the camera keys equal the diagonal blocks of the dense inverse of the damped
+    Hessian (oracle linearization)."""
+    p = synth.bundle_adjustment(num_cameras=6, num_points=150, num_observations=600, seed=9)
+    # priors on two camera poses remove the similarity gauge, so the Hessian is invertible
+    prior = [np.concatenate([p.values[7 * c:7 * c + 7], np.full(6, 10.0), [A.DEFAULT_EPSILON]]) for c in (0, 1)]
+    p.batches.append(A.Batch(A.SFG_FACTOR_PRIOR_POSE3, np.array([[0], [1]]), np.array(prior)))
+    opt = Optimizer(p, A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC, iterations=15),
+                    A.default_form_params(linear_solver=A.SFG_LINEAR_SOLVER_SCHUR))
+    best, _ = opt.optimize(p.values)
+    nk = 2 * 6  # poses and intrinsics lead the key order
+    cov = opt.compute_covariances(best, nk)
+    o = O.linearize(p, best)
+    N = o["rhs"].size
+    H = np.zeros((N, N))
+    for j in range(N):
+        for q in range(o["colptr"][j], o["colptr"][j + 1]):
+            H[o["rowidx"][q], j] = H[j, o["rowidx"][q]] = o["hvals"][q]
+    bd = 6 * 6 + 6 * 3
+    H[np.arange(bd, N), np.arange(bd, N)] += A.DEFAULT_EPSILON
+    ref = np.linalg.inv(H)[:bd, :bd]
+    offs = np.concatenate([[0], np.cumsum([6] * 6 + [3] * 6)])
+    for k in range(nk):
+        blk = ref[offs[k]:offs[k + 1], offs[k]:offs[k + 1]]
+        np.testing.assert_allclose(cov[k], blk, rtol=1e-6, atol=1e-9 * np.abs(blk).max())
+        np.testing.assert_allclose(cov[k], cov[k].T, rtol=0, atol=1e-12 * np.abs(blk).max())
