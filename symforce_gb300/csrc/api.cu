@@ -497,16 +497,11 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
     if (!h->ydbl) h->ydbl = A.Zeros<double>(size_t(nB));
     EnsurePrecond(h);
     h->net = A.Zeros<float>(kPrecondParams);  // zero weights: L = I, block Jacobi
-    PcgShape(h->pd.ng, h->num_sms, &h->pcg_grid, &h->pcg_threads);
-    if (h->pcg_grid > 1) {
-      const int cap = E == 8 ? PcgMaxResidentCtas<double>(h->pcg_threads, h->num_sms)
-                             : PcgMaxResidentCtas<float>(h->pcg_threads, h->num_sms);
-      if (h->pcg_grid > cap)
-        throw Error(SFG_ERR_STRUCTURE, "the reduced system has " + std::to_string(h->pd.ng) +
-                                           " camera blocks, more than one PCG launch can hold (" +
-                                           std::to_string(cap) + " CTAs)");
-    }
+    int split = 1;
+    if (E == 8) PcgShape<double>(h->pd.ng, h->num_sms, &h->pcg_grid, &h->pcg_threads, &split);
+    else PcgShape<float>(h->pd.ng, h->num_sms, &h->pcg_grid, &h->pcg_threads, &split);
     PcgDev& c = h->pcg;
+    c.split = split;
     const PrecondLayout& PL = h->PL;
     c.pd = h->pd;
     c.gptr = A.Upload(PL.gptr);

@@ -266,6 +266,7 @@ struct PcgDev {
   double tol;               // FP64 relative residual target
   double inner_floor;       // smallest relative reduction asked of one inner solve
   int max_iters, max_outer;
+  int split;                // lanes per row of a multi-CTA launch (1 or 3)
 };
 // Gather the 9 x 9 group blocks of S: Sb[q][e] = S[off[q][e]] (0 where off < 0).
 template <typename T>
@@ -276,11 +277,10 @@ size_t PcgStagedSmem(int ng, int nbl, int nent);
 // Opt the staged PCG kernel into its shared memory (once per device).
 template <typename T>
 void ConfigurePcg();
-// Grid shape of the PCG kernel for ng blocks (cooperative when grid > 1).
-void PcgShape(int ng, int num_sms, int* grid, int* threads);
-// CTAs of the PCG kernel that fit on the device at once (a cooperative launch needs all of them).
+// Launch shape of the PCG kernel for ng camera blocks: grid (cooperative when > 1, all CTAs
+// resident), threads and lanes per row (1 or 3); throws if the CTAs do not fit on the device.
 template <typename T>
-int PcgMaxResidentCtas(int threads, int num_sms);
+void PcgShape(int ng, int num_sms, int* grid, int* threads, int* split);
 template <typename T>
 cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s);
 void LaunchPcgBegin(PcgState* ps, cudaStream_t s);

@@ -17,7 +17,9 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <string>
 
+#include "common.h"
 #include "kernels.h"
 
 namespace sfg {
@@ -326,20 +328,20 @@ __device__ __forceinline__ void StX(V* p, V v) {
 // Row a of group row g of S times x (group-major): the stored lower blocks of the row, and the
 // transposed stored blocks (h, g) for the neighbours h > g (addressing chosen without branching).
 template <typename Acc, bool kStaged, typename T, typename V>
-__device__ __forceinline__ Acc GroupRow(const T* Sb, const int2* gent, int e0, int e1, int a,
-                                        const V* x) {
-  // blocks are taken U at a time with all their loads issued before the multiply-adds, so U
-  // round trips to L2 overlap; U shrinks with the operand width to stay within the 64 registers of
-  // a 1024-thread CTA
+__device__ __forceinline__ Acc GroupRow(const T* Sb, const int2* gent, int e0, int e1, int stride,
+                                        int a, const V* x) {
+  // entries e0, e0 + stride, ... of the row; blocks are taken U at a time with all their loads
+  // issued before the multiply-adds, so U round trips to L2 overlap; U shrinks with the operand
+  // width to stay within the 64 registers of a 1024-thread CTA
   constexpr int U = sizeof(T) + sizeof(V) == 8 ? 4 : sizeof(T) + sizeof(V) == 12 ? 2 : 1;
   Acc acc = Acc(0);
   int e = e0;
-  for (; e + U <= e1; e += U) {
+  for (; e + (U - 1) * stride < e1; e += U * stride) {
     T sv[U][kB];
     V xv[U][kB];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      const int2 en = gent[e + u];
+      const int2 en = gent[e + u * stride];
       const int tr = en.y & 1;
       const T* row = Sb + size_t(en.x) * (kB * kB) + (tr ? a : a * kB);
       const int step = tr ? kB : 1;
@@ -355,7 +357,7 @@ __device__ __forceinline__ Acc GroupRow(const T* Sb, const int2* gent, int e0, i
 #pragma unroll
       for (int b = 0; b < kB; ++b) acc += Acc(sv[u][b]) * Acc(xv[u][b]);
   }
-  for (; e < e1; ++e) {
+  for (; e < e1; e += stride) {
     const int2 en = gent[e];
     const int tr = en.y & 1;
     const T* row = Sb + size_t(en.x) * (kB * kB) + (tr ? a : a * kB);
@@ -365,6 +367,20 @@ __device__ __forceinline__ Acc GroupRow(const T* Sb, const int2* gent, int e0, i
     for (int b = 0; b < kB; ++b) acc += Acc(row[b * step]) * Acc(LdX<kStaged>(xh + b));
   }
   return acc;
+}
+
+// Sum of a row's partial products over the SPLIT lanes that share the row (lanes a, a + 9, a + 18),
+// added in the same order in every one of them, so all hold the same bits.
+template <int SPLIT, typename V>
+__device__ __forceinline__ V CombineSplit(V x, int a) {
+  if constexpr (SPLIT == 1) {
+    return x;
+  } else {
+    const V t0 = __shfl_sync(0xffffffffu, x, a);
+    const V t1 = __shfl_sync(0xffffffffu, x, a + kB);
+    const V t2 = __shfl_sync(0xffffffffu, x, a + 2 * kB);
+    return (t0 + t1) + t2;
+  }
 }
 
 struct PcgShared {
@@ -432,21 +448,30 @@ __device__ __forceinline__ void GridReduce(Acc a, Acc b, const PcgDev& d, int& s
 
 // Vector arithmetic in the matrix precision T (FP32 in the mixed form); inner products, CG scalars,
 // the residual passes and the stopping decisions in FP64.
-template <typename T, bool kStaged>
+// SPLIT 1: three camera blocks per warp (lanes 9 q + a, row a of block q).  SPLIT 3: one camera
+// block per warp and three lanes per row (lanes 9 q + a for q = 0..2), each taking every third
+// entry of the row's product with S, so a row waits on a third of the L2 round trips; the vectors
+// are kept in all three lanes (same bits) and only lane a reduces and stores.
+template <typename T, bool kStaged, int SPLIT>
 __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
+  static_assert(SPLIT == 1 || SPLIT == 3, "one or three lanes per row");
   extern __shared__ __align__(16) unsigned char pcg_smem[];
   __shared__ PcgShared sm;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int sub = lane / kB;  // 0..2: camera block of the lane; 3: idle lanes 27..31
-  const int a = lane - sub * kB;
+  const int slot = lane / kB;  // 0..2; 3: idle lanes 27..31
+  const int a = lane - slot * kB;
   const int ng = d.pd.ng;
-  const int g = (blockIdx.x * (blockDim.x >> 5) + warp) * 3 + sub;
-  const bool in_group = sub < 3 && g < ng;
+  const int sub = SPLIT == 1 ? slot : 0;    // camera block of the lane within the warp
+  const int split = SPLIT == 1 ? 0 : slot;  // entry phase of the lane within its row
+  const int g = (blockIdx.x * (blockDim.x >> 5) + warp) * (3 / SPLIT) + sub;
+  const bool in_group = slot < 3 && g < ng;
   const int s = in_group ? d.pd.gidx[size_t(g) * kB + a] : -1;
-  const bool own = s >= 0;
-  const int gbase = sub < 3 ? sub * kB : 0;
+  const bool row_ok = s >= 0;
+  const bool own = row_ok && split == 0;  // reduces and stores the row
+  const bool store = in_group && split == 0;
+  const int gbase = slot < 3 ? slot * kB : 0;
   const size_t gi = size_t(in_group ? g : 0) * kB + a;
-  const int e0 = in_group ? d.gptr[g] : 0, e1 = in_group ? d.gptr[g + 1] : 0;
+  const int e0 = in_group ? d.gptr[g] + split : 0, e1 = in_group ? d.gptr[g + 1] : 0;
   const T* Sb;
   const int2* gent;
   T* zv;
@@ -484,10 +509,10 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
   const T* P = static_cast<const T*>(d.P);
   T prow[kB];
 #pragma unroll
-  for (int b = 0; b < kB; ++b) prow[b] = own ? P[(size_t(g) * kB + a) * kB + b] : T(0);
+  for (int b = 0; b < kB; ++b) prow[b] = row_ok ? P[(size_t(g) * kB + a) * kB + b] : T(0);
   int seq = 0;
-  const double vs = own ? double(v[s]) : 0.0;
-  GridReduce<double>(vs * vs, 0.0, d, seq, sm, [&](double x, double) {
+  const double vs = row_ok ? double(v[s]) : 0.0;
+  GridReduce<double>(own ? vs * vs : 0.0, 0.0, d, seq, sm, [&](double x, double) {
     sm.vnorm = sqrt(x);
     sm.converged = sm.vnorm > 0.0 ? 0 : 1;  // zero rhs: y = 0
   });
@@ -496,8 +521,12 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
   int outer = 0;
   while (!sm.converged) {
     double r64 = vs;
-    if (outer > 0 && in_group) r64 = vs - GroupRow<double, kStaged>(Sb, gent, e0, e1, a, ygv);
-    GridReduce<double>(r64 * r64, 0.0, d, seq, sm, [&](double x, double) {
+    if (outer > 0) {
+      const double sy = CombineSplit<SPLIT>(
+          in_group ? GroupRow<double, kStaged>(Sb, gent, e0, e1, SPLIT, a, ygv) : 0.0, a);
+      if (in_group) r64 = vs - sy;
+    }
+    GridReduce<double>(own ? r64 * r64 : 0.0, 0.0, d, seq, sm, [&](double x, double) {
       sm.rel = sqrt(x) / vnorm;
       sm.converged = sm.rel <= d.tol ? 1 : 0;
       sm.stop = (sm.converged || outer >= d.max_outer || sm.iters >= d.max_iters || sm.broke ||
@@ -512,14 +541,15 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
     // w = S z and q = w + beta q so that one grid reduction separates the product from the update.
     T r = T(r64);
     T zz = ApplyBlock(prow, r, gbase);
-    if (in_group) StX<kStaged>(zv + gi, zz);
-    GridReduce<double>(double(r) * double(zz), 0.0, d, seq, sm, [&](double x, double) { sm.rz = x; });
+    if (store) StX<kStaged>(zv + gi, zz);
+    GridReduce<double>(own ? double(r) * double(zz) : 0.0, 0.0, d, seq, sm,
+                       [&](double x, double) { sm.rz = x; });
     T p = T(0), qv = T(0), dx = T(0), beta = T(0);
     for (;;) {
-      const T w = in_group ? GroupRow<T, kStaged>(Sb, gent, e0, e1, a, zv) : T(0);
+      const T w = CombineSplit<SPLIT>(in_group ? GroupRow<T, kStaged>(Sb, gent, e0, e1, SPLIT, a, zv) : T(0), a);
       p = zz + beta * p;
       qv = w + beta * qv;
-      GridReduce<double>(double(p) * double(qv), 0.0, d, seq, sm, [&](double pq, double) {
+      GridReduce<double>(own ? double(p) * double(qv) : 0.0, 0.0, d, seq, sm, [&](double pq, double) {
         const double rz = sm.rz;
         if (!(pq > 0.0) || !(pq < 1e300) || !(fabs(rz) < 1e300)) sm.broke = 1;
         else sm.alpha = rz / pq;
@@ -529,8 +559,9 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
       dx += alpha * p;
       r -= alpha * qv;
       zz = ApplyBlock(prow, r, gbase);
-      if (in_group) StX<kStaged>(zv + gi, zz);
-      GridReduce<double>(double(r) * double(zz), double(r) * double(r), d, seq, sm, [&](double rz, double rr) {
+      if (store) StX<kStaged>(zv + gi, zz);
+      GridReduce<double>(own ? double(r) * double(zz) : 0.0, own ? double(r) * double(r) : 0.0, d, seq, sm,
+                         [&](double rz, double rr) {
         sm.iters += 1;
         sm.stop = (sqrt(rr) <= sm.target || sm.iters >= d.max_iters) ? 1 : 0;
         sm.beta = rz / sm.rz;
@@ -540,7 +571,7 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
       beta = T(sm.beta);
     }
     y64 += double(dx);
-    if (in_group) StX<kStaged>(ygv + gi, y64);
+    if (store) StX<kStaged>(ygv + gi, y64);
     if (gridDim.x > 1) GridBarrier(d.bar, gridDim.x, d.err);
     else __syncthreads();
   }
@@ -611,34 +642,48 @@ void LaunchCollectSamples(const PrecondDev& pd, const float* feats, const float*
       pd, feats, fac, static_cast<const T*>(v), y, samples, max_systems, st);
 }
 
-void PcgShape(int ng, int num_sms, int* grid, int* threads) {
-  (void)num_sms;
-  const int warps = std::max(1, (ng + 2) / 3);
-  if (warps <= 32) {
-    *grid = 1;
-    *threads = 32 * warps;
-  } else {
-    // CTA size of multi-CTA solves; SFG_PCG_CTA_THREADS (a multiple of 32, at most 1024) overrides
-    int t = kPcgMultiThreads;
-    if (const char* e = std::getenv("SFG_PCG_CTA_THREADS")) {
-      const int v = std::atoi(e);
-      if (v >= 32 && v <= 1024 && v % 32 == 0) t = v;
-    }
-    *threads = t;
-    const int per_cta = 3 * (t / 32);
-    *grid = (ng + per_cta - 1) / per_cta;
-  }
-}
-
-template <typename T>
+template <typename T, int SPLIT>
 int PcgMaxResidentCtas(int threads, int num_sms) {
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, PcgKernel<T, false>, threads, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, PcgKernel<T, false, SPLIT>, threads, 0) !=
+      cudaSuccess)
     return 0;
   return per_sm * num_sms;
 }
-template int PcgMaxResidentCtas<double>(int, int);
-template int PcgMaxResidentCtas<float>(int, int);
+
+template <typename T>
+void PcgShape(int ng, int num_sms, int* grid, int* threads, int* split) {
+  *split = 1;
+  const int warps = std::max(1, (ng + 2) / 3);
+  if (warps <= 32) {  // one CTA, three camera blocks per warp (staged in shared memory if it fits)
+    *grid = 1;
+    *threads = 32 * warps;
+    return;
+  }
+  // CTA size of multi-CTA solves; SFG_PCG_CTA_THREADS (a multiple of 32, at most 1024) overrides
+  int t = kPcgMultiThreads;
+  if (const char* e = std::getenv("SFG_PCG_CTA_THREADS")) {
+    const int v = std::atoi(e);
+    if (v >= 32 && v <= 1024 && v % 32 == 0) t = v;
+  }
+  *threads = t;
+  // three lanes per row when one warp per camera block still fits on the device at once
+  const int grid3 = (ng + t / 32 - 1) / (t / 32);
+  if (grid3 <= PcgMaxResidentCtas<T, 3>(t, num_sms)) {
+    *split = 3;
+    *grid = grid3;
+    return;
+  }
+  const int per_cta = 3 * (t / 32);
+  *grid = (ng + per_cta - 1) / per_cta;
+  const int cap = PcgMaxResidentCtas<T, 1>(t, num_sms);
+  if (*grid > cap)
+    throw Error(SFG_ERR_STRUCTURE, "the reduced system has " + std::to_string(ng) +
+                                       " camera blocks, more than one PCG launch can hold (" +
+                                       std::to_string(cap) + " CTAs)");
+}
+template void PcgShape<double>(int, int, int*, int*, int*);
+template void PcgShape<float>(int, int, int*, int*, int*);
 
 template <typename T>
 size_t PcgStagedSmem(int ng, int nbl, int nent) {
@@ -651,7 +696,7 @@ template size_t PcgStagedSmem<float>(int, int, int);
 
 template <typename T>
 void ConfigurePcg() {
-  cudaFuncSetAttribute(PcgKernel<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPcgStagedMax));
+  cudaFuncSetAttribute(PcgKernel<T, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPcgStagedMax));
 }
 template void ConfigurePcg<double>();
 template void ConfigurePcg<float>();
@@ -670,9 +715,9 @@ template <typename T>
 cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s) {
   if (grid == 1) {
     if (d.staged) {
-      PcgKernel<T, true><<<1, threads, size_t(d.staged), s>>>(d);
+      PcgKernel<T, true, 1><<<1, threads, size_t(d.staged), s>>>(d);
     } else {
-      PcgKernel<T, false><<<1, threads, 0, s>>>(d);
+      PcgKernel<T, false, 1><<<1, threads, 0, s>>>(d);
     }
     return cudaGetLastError();
   }
@@ -688,7 +733,8 @@ cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, PcgKernel<T, false>, d);
+  if (d.split == 3) return cudaLaunchKernelEx(&cfg, PcgKernel<T, false, 3>, d);
+  return cudaLaunchKernelEx(&cfg, PcgKernel<T, false, 1>, d);
 }
 template cudaError_t LaunchPcg<double>(const PcgDev&, int, int, cudaStream_t);
 template cudaError_t LaunchPcg<float>(const PcgDev&, int, int, cudaStream_t);
