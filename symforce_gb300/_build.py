@@ -21,7 +21,7 @@ LIB = OUT_DIR / "libsfgpu.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["kernels_lin.cu", "kernels_lm.cu", "kernels_solve.cu", "kernels_pcg.cu",
-                "kernels_mlp.cu", "kernels_batch.cu", "api.cu", "api_solvers.cu", "api_noalloc.cu",
+                "kernels_mlp.cu", "kernels_batch.cu", "kernels_tc.cu", "api.cu", "api_solvers.cu", "api_noalloc.cu",
                 "api_learned.cu", "api_batch.cu"]
 HOST_SOURCES = ["host_structure.cpp", "host_layout.cpp", "host_pcg.cpp", "device_plan.cpp"]
 

@@ -101,6 +101,7 @@ struct sfg_handle {
   float* feats = nullptr;
   float* fac = nullptr;
   float* zout = nullptr;
+  float *mlp_h1 = nullptr, *mlp_h2 = nullptr;  // hidden activations of the network's inference
   void* Pblk = nullptr;
   int64_t* blk_off = nullptr;  // [nbl][81] S offsets of the group blocks
   void* Sb = nullptr;          // [nbl][81] group blocks of S
@@ -173,7 +174,9 @@ template <typename T>
 void EnqueuePrecond(sfg_handle* h, cudaStream_t s) {
   LaunchGroupBlocks<T>(h->blk_off, int64_t(h->pcg.nbl) * kPrecondBlock * kPrecondBlock, h->S, h->Sb, s);
   LaunchPrecondFeatures<T>(h->pd, h->spmv, h->S, h->rho, h->feats, h->fac, s);
-  if (h->pcg_mode == 2) LaunchMlpInfer(h->feats, kPrecondFeatures, h->pd.ng, h->net, h->zout, s);
+  if (h->pcg_mode == 2)
+    SFG_CUDA(LaunchMlpInferTc(h->feats, kPrecondFeatures, h->pd.ng, h->net, h->mlp_h1, h->mlp_h2, h->zout,
+                              &h->st->device_error, s));
   LaunchPrecondAssemble<T>(h->pd.ng, h->fac, h->pcg_mode == 2 ? h->zout : nullptr, h->Pblk, s);
 }
 
@@ -372,6 +375,8 @@ void EnsurePrecond(sfg_handle* h) {
   h->feats = A.Zeros<float>(ng * kPrecondFeatures);
   h->fac = A.Zeros<float>(ng * kPrecondFac);
   h->zout = A.Zeros<float>(ng * kPrecondTri);
+  h->mlp_h1 = A.Zeros<float>(ng * kPrecondHidden);
+  h->mlp_h2 = A.Zeros<float>(ng * kPrecondHidden);
   h->Pblk = A.Alloc(ng * kPrecondBlock * kPrecondBlock * h->elem);
   if (!h->ps) h->ps = A.Zeros<PcgState>(1);
   h->have_precond = true;

@@ -214,9 +214,15 @@ int32_t sfg_precond_infer(const float* features, int64_t n, const float* weights
     float* w = static_cast<float*>(A.Alloc(sfg::kPrecondParams * 4));
     SFG_CUDA(cudaMemcpy(w, weights, sfg::kPrecondParams * 4, cudaMemcpyHostToDevice));
     float* z = static_cast<float*>(A.Alloc(size_t(n) * sfg::kPrecondTri * 4));
-    sfg::LaunchMlpInfer(x, sfg::kPrecondFeatures, n, w, z, s);
-    SFG_CUDA(cudaGetLastError());
+    float* h1 = static_cast<float*>(A.Alloc(size_t(n) * sfg::kPrecondHidden * 4));
+    float* h2 = static_cast<float*>(A.Alloc(size_t(n) * sfg::kPrecondHidden * 4));
+    int* err = A.Zeros<int>(1);
+    if (n > (int64_t(1) << 30)) throw Error(SFG_ERR_INVALID_ARGUMENT, "too many inputs for one pass");
+    SFG_CUDA(sfg::LaunchMlpInferTc(x, sfg::kPrecondFeatures, n, w, h1, h2, z, err, s));
     SFG_CUDA(cudaStreamSynchronize(s));
+    int e = 0;
+    SFG_CUDA(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) throw Error(SFG_ERR_DEVICE_STATUS, "tensor-core inference: a wait hit its cap");
     SFG_CUDA(cudaMemcpy(out, z, size_t(n) * sfg::kPrecondTri * 4, cudaMemcpyDeviceToHost));
   });
 }

@@ -236,9 +236,11 @@ void LaunchPrecondFeatures(const PrecondDev& pd, const SpmvDev& m, const void* S
 // Preconditioner blocks P_g (T, [ng][81]) from the factors and the network outputs (null: L = I).
 template <typename T>
 void LaunchPrecondAssemble(int ng, const float* fac, const float* z, void* P, cudaStream_t s);
-// Network forward pass for inference: z[n][45] from x[n][96] (row stride ldx floats).
-void LaunchMlpInfer(const float* x, int64_t ldx, int64_t n, const float* weights, float* z,
-                    cudaStream_t s);
+// The network's inference pass on the tensor cores (tcgen05, TF32 with a three-pass split for FP32
+// accuracy): z[n][45] from x[n][96] (row stride ldx floats), 96 -> 256 -> 256 -> 45 with ReLU;
+// h1, h2: [n][256] scratch; a capped wait that gives up sets *err.
+cudaError_t LaunchMlpInferTc(const float* x, int64_t ldx, int64_t n, const float* weights, float* h1, float* h2,
+                             float* z, int* err, cudaStream_t s);
 // Training samples of one system: [ng][114] at samples + slot * ng * 114, slot = the LM record
 // index of the iteration, skipped when slot >= max_systems.
 template <typename T>

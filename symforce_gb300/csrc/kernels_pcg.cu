@@ -12,7 +12,7 @@
 //    order over CTAs in every CTA), so every CTA takes the same branch and runs are reproducible.
 //    Multi-CTA solves use a grid barrier (cooperative launch: all CTAs resident) whose waits are
 //    capped; a cap hit sets the device error word.
-//  - The network's inference pass (96 -> 256 -> 256 -> 45, ReLU) for all camera blocks.
+//  (The network's inference pass runs on the tensor cores: kernels_tc.cu.)
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -210,69 +210,6 @@ __global__ void CollectSamplesKernel(PrecondDev pd, const float* feats, const fl
     for (int k = i; k < kB; ++k) s += fc[Tri(k, i)] * yd[k];
     out[kPrecondFeatures + i] = gh[i];
     out[kPrecondFeatures + kB + i] = s;
-  }
-}
-
-// ---------------------------------------------------------------------------------------------
-// Network inference: 16 blocks per CTA, one hidden unit per thread.
-// ---------------------------------------------------------------------------------------------
-constexpr int kMlpRows = 16;
-
-__global__ void __launch_bounds__(kPrecondHidden) MlpInferKernel(const float* x, int64_t ldx, int64_t n,
-                                                               const float* W, float* z) {
-  __shared__ float xs[kMlpRows][kPrecondFeatures];
-  __shared__ float h1[kMlpRows][kPrecondHidden];
-  __shared__ float h2[kMlpRows][kPrecondHidden];
-  const int64_t row0 = int64_t(blockIdx.x) * kMlpRows;
-  const int t = threadIdx.x;
-  for (int i = t; i < kMlpRows * kPrecondFeatures; i += blockDim.x) {
-    const int r = i / kPrecondFeatures, c = i - r * kPrecondFeatures;
-    xs[r][c] = row0 + r < n ? x[(row0 + r) * ldx + c] : 0.f;
-  }
-  __syncthreads();
-  const float* W1 = W;
-  const float* b1 = W1 + kPrecondFeatures * kPrecondHidden;
-  const float* W2 = b1 + kPrecondHidden;
-  const float* b2 = W2 + kPrecondHidden * kPrecondHidden;
-  const float* W3 = b2 + kPrecondHidden;
-  const float* b3 = W3 + kPrecondHidden * kPrecondTri;
-  float acc[kMlpRows];
-#pragma unroll
-  for (int r = 0; r < kMlpRows; ++r) acc[r] = b1[t];
-  for (int k = 0; k < kPrecondFeatures; ++k) {
-    const float w = __ldg(W1 + k * kPrecondHidden + t);
-#pragma unroll
-    for (int r = 0; r < kMlpRows; ++r) acc[r] = fmaf(xs[r][k], w, acc[r]);
-  }
-#pragma unroll
-  for (int r = 0; r < kMlpRows; ++r) h1[r][t] = fmaxf(acc[r], 0.f);
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < kMlpRows; ++r) acc[r] = b2[t];
-  for (int k = 0; k < kPrecondHidden; ++k) {
-    const float w = __ldg(W2 + k * kPrecondHidden + t);
-#pragma unroll
-    for (int r = 0; r < kMlpRows; ++r) acc[r] = fmaf(h1[r][k], w, acc[r]);
-  }
-#pragma unroll
-  for (int r = 0; r < kMlpRows; ++r) h2[r][t] = fmaxf(acc[r], 0.f);
-  __syncthreads();
-  constexpr int kGroups = kMlpRows / 4;
-  if (t < kPrecondTri * kGroups) {
-    const int o = t % kPrecondTri, rg = t / kPrecondTri;
-    float a4[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) a4[i] = b3[o];
-    for (int k = 0; k < kPrecondHidden; ++k) {
-      const float w = __ldg(W3 + k * kPrecondTri + o);
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a4[i] = fmaf(h2[rg * 4 + i][k], w, a4[i]);
-    }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int64_t r = row0 + rg * 4 + i;
-      if (r < n) z[r * kPrecondTri + o] = a4[i];
-    }
   }
 }
 
@@ -622,13 +559,6 @@ void LaunchPrecondAssemble(int ng, const float* fac, const float* z, void* P, cu
   if (ng == 0) return;
   const int threads = 64;
   PrecondAssembleKernel<T><<<(ng + threads - 1) / threads, threads, 0, s>>>(ng, fac, z, static_cast<T*>(P));
-}
-
-void LaunchMlpInfer(const float* x, int64_t ldx, int64_t n, const float* weights, float* z,
-                    cudaStream_t s) {
-  if (n == 0) return;
-  const int64_t grid = (n + kMlpRows - 1) / kMlpRows;
-  MlpInferKernel<<<unsigned(grid), kPrecondHidden, 0, s>>>(x, ldx, n, weights, z);
 }
 
 template <typename T>

@@ -1,0 +1,319 @@
+// Tensor-core (tcgen05, TF32) GEMM with bias / ReLU epilogue for the preconditioner network's
+// inference pass: out[M x N] = act(A[M x K] W[K x N] + bias).
+//
+//  - One CTA of 128 threads per 128-row x NP-column tile (NP = 128 for the hidden layers, 48 for the
+//    45 outputs); the accumulator lives in tensor memory (TMEM, 128 lanes x NP FP32 columns,
+//    allocated per CTA).
+//  - K is consumed in chunks of 32: the threads stage the A and W chunks in shared memory in the
+//    canonical K-major layout without swizzle (8-row x 16-byte core matrices; leading byte offset
+//    = next core matrix along K, stride byte offset = next 8-row group), one elected thread issues
+//    the MMAs (M = 128, N = NP, K = 8 each) and commits them to an mbarrier that the CTA waits on
+//    before restaging.
+//  - FP32 accuracy on the TF32 tensor pipe by the three-pass split x = hi + lo (hi: the top 11
+//    significand bits, lo = x - hi): A W ~ A_hi W_hi + A_hi W_lo + A_lo W_hi, relative error ~2^-20.
+//  - Epilogue: tcgen05.ld of 16 columns at a time (warp w reads TMEM lanes 32 w .. 32 w + 31, one row
+//    per thread), bias, ReLU, store.
+//  - Every mbarrier wait is capped; a cap hit sets the error word, and the CTA still waits (capped)
+//    for its MMAs and frees its TMEM before returning.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.h"
+
+namespace sfg {
+
+namespace {
+
+constexpr int kTcRows = 128;   // M of the MMA and rows per CTA
+constexpr int kTcKc = 32;      // K per staged chunk (four MMAs of K = 8)
+constexpr int kTcThreads = 128;
+constexpr unsigned kTcSpin = 1u << 24;
+
+__device__ __forceinline__ uint32_t SmemAddr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Byte offset of element (row, k) of a [rows x kTcKc] K-major operand chunk: core matrices of
+// 8 rows x 4 FP32, 128 bytes each, consecutive along K (LBO = 128 B), 8-row groups kTcKc / 4 core
+// matrices apart (SBO = 1024 B).
+__device__ __forceinline__ uint32_t ChunkOffset(int row, int k) {
+  return uint32_t((row >> 3) * 1024 + (k >> 2) * 128 + (row & 7) * 16 + (k & 3) * 4);
+}
+
+// Shared-memory matrix descriptor: start address, LBO and SBO in 16-byte units, descriptor version 1,
+// no swizzle.
+__device__ __forceinline__ uint64_t SmemDesc(uint32_t addr) {
+  constexpr uint64_t kLbo = 128 >> 4, kSbo = 1024 >> 4;
+  return uint64_t((addr & 0x3FFFF) >> 4) | (kLbo << 16) | (kSbo << 32) | (uint64_t(1) << 46);
+}
+
+// Instruction descriptor of kind::tf32: FP32 accumulator, TF32 A and B, both K-major, N and M.
+__device__ __forceinline__ uint32_t InstrDesc(int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(kTcRows >> 4) << 24);
+}
+
+__device__ __forceinline__ float TfHi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+
+__device__ __forceinline__ void MbarInit(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(SmemAddr(bar)) : "memory");
+}
+
+// Waits for the completion of the given phase; false if the cap was hit.
+__device__ __forceinline__ bool MbarWait(uint64_t* bar, uint32_t phase) {
+  const uint32_t addr = SmemAddr(bar);
+  for (unsigned it = 0; it < kTcSpin; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void MmaTf32(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void MmaCommit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(SmemAddr(bar))
+               : "memory");
+}
+
+template <int NP, bool kRelu>
+__global__ void __launch_bounds__(kTcThreads) TcGemmKernel(const float* A, int64_t lda, int M, int K,
+                                                           const float* W, int ldw, const float* bias,
+                                                           int N, float* out, int64_t ldo, int vec4,
+                                                           int* err) {
+  static_assert(NP % 16 == 0 && NP >= 16 && NP <= 256, "N of a kind::tf32 MMA with M = 128");
+  constexpr int kCols = NP <= 32 ? 32 : NP <= 64 ? 64 : NP <= 128 ? 128 : 256;  // TMEM columns
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  unsigned char* a_hi = tc_smem;
+  unsigned char* a_lo = a_hi + kTcRows * kTcKc * 4;
+  unsigned char* b_hi = a_lo + kTcRows * kTcKc * 4;
+  unsigned char* b_lo = b_hi + NP * kTcKc * 4;
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int s_fail;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int row0 = blockIdx.x * kTcRows;
+  const int n0 = blockIdx.y * NP;  // this CTA's columns n0 .. n0 + NP of the output
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(SmemAddr(&tmem_base)),
+                 "r"(kCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    MbarInit(&bar);
+    s_fail = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t d_tmem = tmem_base;
+  const uint32_t idesc = InstrDesc(NP);
+
+  // Software pipeline over the K chunks: the global loads of chunk c + 1 go out (into registers)
+  // while the MMAs of chunk c run; the registers are written to shared memory once those MMAs have
+  // released it.
+  constexpr int kAPer = kTcRows * (kTcKc / 4) / kTcThreads;  // 8 float4 per thread
+  constexpr int kBPer = (NP + kTcThreads - 1) / kTcThreads;
+  float4 av[kAPer];
+  float bv[kBPer][kTcKc];
+  auto load_chunk = [&](int k0) {
+    // A: four consecutive k of one row per thread and step (eight threads cover a row's 32 k), so
+    // a warp reads four full 128-byte rows per load
+#pragma unroll
+    for (int i = 0; i < kAPer; ++i) {
+      const int idx = tid + i * kTcThreads;
+      const int r = idx >> 3, k4 = (idx & 7) * 4, gr = row0 + r, gk = k0 + k4;
+      if (vec4 && gr < M && gk + 3 < K) {
+        av[i] = __ldg(reinterpret_cast<const float4*>(A + int64_t(gr) * lda + gk));
+      } else {
+        const float* ap = A + int64_t(gr) * lda + gk;
+        av[i].x = (gr < M && gk < K) ? __ldg(ap) : 0.f;
+        av[i].y = (gr < M && gk + 1 < K) ? __ldg(ap + 1) : 0.f;
+        av[i].z = (gr < M && gk + 2 < K) ? __ldg(ap + 2) : 0.f;
+        av[i].w = (gr < M && gk + 3 < K) ? __ldg(ap + 3) : 0.f;
+      }
+    }
+    // W^T: row n of the operand is column n0 + n of W (consecutive threads, consecutive n)
+#pragma unroll
+    for (int j = 0; j < kBPer; ++j) {
+      const int n = tid + j * kTcThreads, gn = n0 + n;
+#pragma unroll
+      for (int k = 0; k < kTcKc; ++k) {
+        const int gk = k0 + k;
+        bv[j][k] = (n < NP && gn < N && gk < K) ? __ldg(W + int64_t(gk) * ldw + gn) : 0.f;
+      }
+    }
+  };
+  auto store_chunk = [&]() {
+#pragma unroll
+    for (int i = 0; i < kAPer; ++i) {
+      const int idx = tid + i * kTcThreads;
+      const int r = idx >> 3, k4 = (idx & 7) * 4;
+      float4 hi4, lo4;
+      hi4.x = TfHi(av[i].x);
+      hi4.y = TfHi(av[i].y);
+      hi4.z = TfHi(av[i].z);
+      hi4.w = TfHi(av[i].w);
+      lo4.x = av[i].x - hi4.x;
+      lo4.y = av[i].y - hi4.y;
+      lo4.z = av[i].z - hi4.z;
+      lo4.w = av[i].w - hi4.w;
+      const uint32_t o = ChunkOffset(r, k4);
+      *reinterpret_cast<float4*>(a_hi + o) = hi4;
+      *reinterpret_cast<float4*>(a_lo + o) = lo4;
+    }
+#pragma unroll
+    for (int j = 0; j < kBPer; ++j) {
+      const int n = tid + j * kTcThreads;
+      if (n >= NP) continue;
+#pragma unroll
+      for (int k4 = 0; k4 < kTcKc; k4 += 4) {
+        float4 hi4, lo4;
+        hi4.x = TfHi(bv[j][k4]);
+        hi4.y = TfHi(bv[j][k4 + 1]);
+        hi4.z = TfHi(bv[j][k4 + 2]);
+        hi4.w = TfHi(bv[j][k4 + 3]);
+        lo4.x = bv[j][k4] - hi4.x;
+        lo4.y = bv[j][k4 + 1] - hi4.y;
+        lo4.z = bv[j][k4 + 2] - hi4.z;
+        lo4.w = bv[j][k4 + 3] - hi4.w;
+        const uint32_t o = ChunkOffset(n, k4);
+        *reinterpret_cast<float4*>(b_hi + o) = hi4;
+        *reinterpret_cast<float4*>(b_lo + o) = lo4;
+      }
+    }
+  };
+
+  uint32_t phase = 0;
+  bool issued = false;
+  if (K > 0) load_chunk(0);
+  for (int k0 = 0; k0 < K; k0 += kTcKc) {
+    if (issued) {
+      // the MMAs of the previous chunk must have read shared memory before it is restaged
+      if (!MbarWait(&bar, phase)) {
+        if (lane == 0) atomicExch(err, kDevSpinTimeout);
+        s_fail = 1;
+      }
+      phase ^= 1u;
+      __syncthreads();
+      if (s_fail) break;
+    }
+    store_chunk();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int j = 0; j < kTcKc / 8; ++j) {  // K = 8 per MMA: two core matrices along K
+        const uint32_t off = uint32_t(j * 256);
+        const uint32_t acc0 = (k0 > 0 || j > 0) ? 1u : 0u;
+        MmaTf32(d_tmem, SmemDesc(SmemAddr(a_hi) + off), SmemDesc(SmemAddr(b_hi) + off), idesc, acc0);
+        MmaTf32(d_tmem, SmemDesc(SmemAddr(a_hi) + off), SmemDesc(SmemAddr(b_lo) + off), idesc, 1u);
+        MmaTf32(d_tmem, SmemDesc(SmemAddr(a_lo) + off), SmemDesc(SmemAddr(b_hi) + off), idesc, 1u);
+      }
+      MmaCommit(&bar);
+    }
+    issued = true;
+    if (k0 + kTcKc < K) load_chunk(k0 + kTcKc);  // overlaps the MMAs just issued
+  }
+  // the last chunk's MMAs complete the accumulator
+  if (issued && !s_fail) {
+    if (!MbarWait(&bar, phase)) {
+      if (lane == 0) atomicExch(err, kDevSpinTimeout);
+      s_fail = 1;
+    }
+    phase ^= 1u;
+    __syncthreads();
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (issued && !s_fail) {
+    // epilogue: row tid of the tile, 16 columns per TMEM load
+    const int gr = row0 + tid;
+#pragma unroll 1
+    for (int c0 = 0; c0 < NP; c0 += 16) {
+      uint32_t v[16];
+      const uint32_t taddr = d_tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+          "%14, %15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (gr < M) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int c = n0 + c0 + i;
+          if (c < N) {
+            float y = __uint_as_float(v[i]) + bias[c];
+            if (kRelu) y = fmaxf(y, 0.f);
+            out[int64_t(gr) * ldo + c] = y;
+          }
+        }
+      }
+    }
+  } else if (issued) {
+    // a wait gave up: give the MMAs a second (capped) chance to finish before the TMEM is freed
+    (void)MbarWait(&bar, phase ^ 1u);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(d_tmem), "r"(kCols) : "memory");
+}
+
+template <int NP, bool kRelu>
+size_t TcSmem() {
+  return size_t(kTcRows) * kTcKc * 4 * 2 + size_t(NP) * kTcKc * 4 * 2;
+}
+
+template <int NP, bool kRelu>
+cudaError_t LaunchTc(const float* A, int64_t lda, int M, int K, const float* W, int ldw, const float* bias,
+                     int N, float* out, int64_t ldo, int* err, cudaStream_t s) {
+  const size_t smem = TcSmem<NP, kRelu>();
+  const cudaError_t e = cudaFuncSetAttribute(TcGemmKernel<NP, kRelu>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(smem));
+  if (e != cudaSuccess) return e;
+  const int vec4 = (lda % 4 == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0) ? 1 : 0;
+  const dim3 grid((M + kTcRows - 1) / kTcRows, (N + NP - 1) / NP);
+  TcGemmKernel<NP, kRelu><<<grid, kTcThreads, smem, s>>>(A, lda, M, K, W, ldw, bias, N, out, ldo, vec4, err);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t LaunchMlpInferTc(const float* x, int64_t ldx, int64_t n, const float* weights, float* h1, float* h2,
+                             float* z, int* err, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const int F = kPrecondFeatures, H = kPrecondHidden, O = kPrecondTri;
+  const float* W1 = weights;
+  const float* b1 = W1 + F * H;
+  const float* W2 = b1 + H;
+  const float* b2 = W2 + H * H;
+  const float* W3 = b2 + H;
+  const float* b3 = W3 + H * O;
+  const int m = int(n);
+  // hidden layers: two CTAs of 128 output columns per 128-row tile
+  cudaError_t e = LaunchTc<128, true>(x, ldx, m, F, W1, H, b1, H, h1, H, err, s);
+  if (e != cudaSuccess) return e;
+  e = LaunchTc<128, true>(h1, H, m, H, W2, H, b2, H, h2, H, err, s);
+  if (e != cudaSuccess) return e;
+  return LaunchTc<48, false>(h2, H, m, H, W3, O, b3, O, z, O, err, s);
+}
+
+}  // namespace sfg
