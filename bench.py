@@ -241,12 +241,15 @@ def _time_form(opt, vin_np, vout_np, flush, steps, warmup, target, target9):
         flush.zero_()  # L2 flush: 256 MB > 129 MB L2
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        _, stats = opt.optimize(vin_np, out=vout_np)
+        vals, stats = opt.optimize(vin_np, out=vout_np)
         t1 = time.perf_counter()
         recs = stats.iterations
         ttc = next((r.elapsed_ms for r in recs if r.best_error <= target), float("nan"))
         ttc9 = next((r.elapsed_ms for r in recs if r.best_error <= target9), float("nan"))
+        last_values[0] = vals
         return (t1 - t0) * 1e3, stats, ttc, ttc9
+
+    last_values = [None]
 
     for _ in range(warmup):
         step()
@@ -259,7 +262,50 @@ def _time_form(opt, vin_np, vout_np, flush, steps, warmup, target, target9):
         out["ttc9"].append(ttc9)
         out["launches"].append(stats.kernel_launches)
         out["stats"] = stats
+    out["values"] = np.array(last_values[0], copy=True)
     return out
+
+
+def _quat_to_rot(q: np.ndarray) -> np.ndarray:
+    """Rotation matrices of [n, 4] unit quaternions [x, y, z, w]."""
+    x, y, z, w = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    return np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
+                     np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
+                     np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1)], 1)
+
+
+def _state_errors(problem, x: np.ndarray, ref: np.ndarray) -> dict:
+    """Per-state differences of a bundle-adjustment solution from a reference one, after the
+    similarity transform (scale, rotation, translation of the world) that best maps its points onto
+    the reference's (Umeyama): the cost is invariant to that 7-dof gauge, so solutions from different
+    LM paths differ by it.  Camera rotation angle (rad), camera centre and point position (m),
+    relative focal length, and the gauge scale."""
+    nc = int(problem.meta["num_cameras"])
+    cam, cam_r = x[:7 * nc].reshape(nc, 7), ref[:7 * nc].reshape(nc, 7)
+    pts, pts_r = x[10 * nc:].reshape(-1, 3), ref[10 * nc:].reshape(-1, 3)
+    mu, mu_r = pts.mean(0), pts_r.mean(0)
+    a, b = pts - mu, pts_r - mu_r
+    U, D, Vt = np.linalg.svd(b.T @ a / len(a))
+    sgn = np.diag([1.0, 1.0, np.sign(np.linalg.det(U @ Vt))])
+    R = U @ sgn @ Vt                                   # world rotation: x -> reference
+    scale = float(np.trace(np.diag(D) @ sgn) / (a * a).sum(1).mean())
+    t = mu_r - scale * R @ mu
+    pts_al = scale * pts @ R.T + t
+    Rc, Rc_r = _quat_to_rot(cam[:, :4]), _quat_to_rot(cam_r[:, :4])   # camera-from-world
+    centres = -np.einsum("nji,nj->ni", Rc, cam[:, 4:])                # world position of a camera
+    centres_r = -np.einsum("nji,nj->ni", Rc_r, cam_r[:, 4:])
+    centres_al = scale * centres @ R.T + t
+    Rc_al = Rc @ R.T                                                 # camera-from-reference-world
+    dR = np.einsum("nij,nkj->nik", Rc_al, Rc_r)
+    sin = 0.5 * np.linalg.norm(np.stack([dR[:, 2, 1] - dR[:, 1, 2], dR[:, 0, 2] - dR[:, 2, 0],
+                                         dR[:, 1, 0] - dR[:, 0, 1]], -1), axis=1)
+    ang = np.arctan2(sin, (np.trace(dR, axis1=1, axis2=2) - 1) / 2)
+    intr, intr_r = x[7 * nc:10 * nc].reshape(nc, 3), ref[7 * nc:10 * nc].reshape(nc, 3)
+    return {"rotation_rad": float(ang.max()),
+            "camera_centre_m": float(np.linalg.norm(centres_al - centres_r, axis=1).max()),
+            "point_m": float(np.linalg.norm(pts_al - pts_r, axis=1).max()),
+            "focal_rel": float((np.abs(intr[:, 0] - intr_r[:, 0]) / np.abs(intr_r[:, 0])).max()),
+            "gauge_scale": scale}
 
 
 def _med(x):
@@ -318,6 +364,8 @@ def _scale_section(device: int, flush, workload: str = SCALE_WORKLOAD) -> dict:
         st = r["stats"]
         r["ttc"] = [next((x.elapsed_ms for x in st.iterations if x.best_error <= target), float("nan"))]
         out["forms"][name] = _form_summary(r, opt, oracle_cost)
+        out["forms"][name]["max_state_err_vs_plain"] = _state_errors(problem, r["values"],
+                                                                     res["plain"][0]["values"])
         opt.close()
     plain_t = out["forms"]["plain"]["time_to_cost_ms"]
     for name in FORMS:
@@ -414,6 +462,9 @@ def run_gb300(args) -> None:
     ms_step = _allreduce_max(statistics.median(plain["dev"]), world)
     e2e_ms = _allreduce_max(statistics.median(plain["e2e"]), world)
     forms = {name: _form_summary(res[name], opts[name], oracle["best_error"]) for name in FORMS}
+    for name in FORMS:
+        forms[name]["max_state_err_vs_plain"] = _state_errors(problem, res[name]["values"],
+                                                              res["plain"]["values"])
     for name in FORMS:
         t = forms[name]["time_to_cost_ms"]
         forms[name]["speedup_vs_plain"] = round(forms["plain"]["time_to_cost_ms"] / t, 3) if t == t else None

@@ -3,6 +3,7 @@
 #include "device_plan.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <array>
 #include <unordered_map>
 
@@ -245,7 +246,11 @@ SchurDev UploadSchur(DeviceArena& A, const SchurLayout& S, int elem) {
   d.sb_dk = A.Upload(S.sb_dk);
   d.sb_dl = A.Upload(S.sb_dl);
   d.sb_diag_toff = A.Upload(S.sb_diag_toff);
-  const int64_t ct = elem == 8 ? 64 : 256;
+  int64_t ct = elem == 8 ? 128 : 256;
+  if (const char* e = std::getenv("SFG_SCHUR_CHUNK")) {  // tuning override: terms per chunk
+    const long v = std::atol(e);
+    if (v >= 1 && v <= (1 << 20)) ct = v;
+  }
   std::vector<int32_t> ch_block;
   std::vector<int64_t> ch_begin, chunk_ptr(1, 0);
   for (int b = 0; b < d.nsblocks; ++b) {

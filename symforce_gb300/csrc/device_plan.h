@@ -62,8 +62,8 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
 SpmvDev BuildSpmv(DeviceArena& A, const BlockPattern& pat, int64_t a_stride, int64_t b_stride);
 
 // Device copy of a Schur layout for elements of `elem` bytes, with the S-block terms cut into
-// chunks (64 terms in FP64, whose pipe needs the work spread over many warps; 256 in FP32) and the
-// chunks' partial-sum buffer.
+// chunks (128 terms in FP64, 256 in FP32: measured best on GB300 across the 50- and 1,000-camera
+// workloads) and the chunks' partial-sum buffer.
 SchurDev UploadSchur(DeviceArena& A, const SchurLayout& S, int elem);
 
 // `gate` (optional): the launched kernels do nothing unless *gate != 0.

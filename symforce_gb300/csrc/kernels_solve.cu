@@ -126,17 +126,46 @@ __global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_al
 constexpr int kMaxKeyDim = 6;
 constexpr int kSchurWarps = 4;
 
+// The products of one chunk for a block of DK x DL (compile-time sizes: only the block's entries are
+// accumulated, which matters on the FP64 pipe), written as a 6 x 6 row-major partial.
+template <typename T, int DK, int DL>
+__device__ __forceinline__ void ChunkTerms(const SchurDev& d, const T* H, const T* W, int64_t t0,
+                                           int64_t t1, int lane, T* out) {
+  T acc[DK * DL];
+#pragma unroll
+  for (int i = 0; i < DK * DL; ++i) acc[i] = T(0);
+  for (int64_t t = t0 + lane; t < t1; t += 32) {
+    const T* E = H + d.sb_eoff[t];
+    const T* Wl = W + d.sb_woff[t];
+    T e[3 * DK], w[3 * DL];
+#pragma unroll
+    for (int i = 0; i < 3 * DK; ++i) e[i] = E[i];
+#pragma unroll
+    for (int i = 0; i < 3 * DL; ++i) w[i] = Wl[i];
+#pragma unroll
+    for (int r = 0; r < DK; ++r)
+#pragma unroll
+      for (int c = 0; c < DL; ++c)
+        acc[r * DL + c] += e[r] * w[c] + e[DK + r] * w[DL + c] + e[2 * DK + r] * w[2 * DL + c];
+  }
+#pragma unroll
+  for (int i = 0; i < DK * DL; ++i) {
+    T v = acc[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    acc[i] = v;
+  }
+  if (lane == 0)
+#pragma unroll
+    for (int r = 0; r < DK; ++r)
+#pragma unroll
+      for (int c = 0; c < DL; ++c) out[r * kMaxKeyDim + c] = acc[r * DL + c];
+}
+
+// Any other key sizes (up to kMaxKeyDim): runtime bounds inside the 6 x 6 accumulator.
 template <typename T>
-__global__ void __launch_bounds__(32 * kSchurWarps)
-    SchurChunkKernel(SchurDev d, const T* hess_all, int64_t nvals, const T* W, const LmState* st) {
-  const int ch = blockIdx.x * kSchurWarps + (threadIdx.x >> 5);
-  if (ch >= d.nchunks) return;
-  const int lane = threadIdx.x & 31;
-  const T* H = hess_all + int64_t(st->init_idx) * nvals;
-  const int sb = d.ch_block[ch];
-  const int dk = d.sb_dk[sb], dl = d.sb_dl[sb];
-  const int64_t t0 = d.ch_begin[ch];
-  const int64_t t1 = min(t0 + d.chunk_terms, d.sb_ptr[sb + 1]);
+__device__ __forceinline__ void ChunkTermsAny(const SchurDev& d, const T* H, const T* W, int dk, int dl,
+                                              int64_t t0, int64_t t1, int lane, T* out) {
   constexpr int D = kMaxKeyDim;
   T acc[D * D];
 #pragma unroll
@@ -165,10 +194,30 @@ __global__ void __launch_bounds__(32 * kSchurWarps)
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     acc[i] = v;
   }
-  if (lane == 0) {
-    T* out = static_cast<T*>(d.partials) + int64_t(ch) * (D * D);
+  if (lane == 0)
 #pragma unroll
     for (int i = 0; i < D * D; ++i) out[i] = acc[i];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kSchurWarps)
+    SchurChunkKernel(SchurDev d, const T* hess_all, int64_t nvals, const T* W, const LmState* st) {
+  const int ch = blockIdx.x * kSchurWarps + (threadIdx.x >> 5);
+  if (ch >= d.nchunks) return;
+  const int lane = threadIdx.x & 31;
+  const T* H = hess_all + int64_t(st->init_idx) * nvals;
+  const int sb = d.ch_block[ch];
+  const int dk = d.sb_dk[sb], dl = d.sb_dl[sb];
+  const int64_t t0 = d.ch_begin[ch];
+  const int64_t t1 = min(t0 + d.chunk_terms, d.sb_ptr[sb + 1]);
+  T* out = static_cast<T*>(d.partials) + int64_t(ch) * (kMaxKeyDim * kMaxKeyDim);
+  // one case per chunk (warp-uniform): the key sizes of bundle adjustment and 2D / 3D poses
+  switch (dk * 8 + dl) {
+    case 6 * 8 + 6: ChunkTerms<T, 6, 6>(d, H, W, t0, t1, lane, out); break;
+    case 3 * 8 + 6: ChunkTerms<T, 3, 6>(d, H, W, t0, t1, lane, out); break;
+    case 6 * 8 + 3: ChunkTerms<T, 6, 3>(d, H, W, t0, t1, lane, out); break;
+    case 3 * 8 + 3: ChunkTerms<T, 3, 3>(d, H, W, t0, t1, lane, out); break;
+    default: ChunkTermsAny<T>(d, H, W, dk, dl, t0, t1, lane, out);
   }
 }
 
