@@ -25,8 +25,8 @@ extern thread_local std::string g_last_error;
 namespace {
 
 constexpr int kMaxN = 512;                       // largest system this entry point accepts
-constexpr int kTile = 16;                        // the FP64 tile of the factorization kernel
-constexpr int kMaxTiles = kMaxN / kTile;         // 32
+constexpr int kTile = sfg::kFactorTileF64;       // the FP64 tile of the factorization kernel
+constexpr int kMaxTiles = kMaxN / kTile;
 constexpr int kMaxStates = kMaxTiles * (kMaxTiles + 1) / 2;
 constexpr int kMaxTasks = kMaxTiles * (kMaxTiles + 1) * (kMaxTiles + 2) / 6 + kMaxTiles;
 

@@ -26,7 +26,7 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   fp.elem = elem;
   fp.sym = Analyze(pat, ordering);
   const Symbolic& S = fp.sym;
-  const int tile = elem == 8 ? 16 : 32;
+  const int tile = elem == 8 ? kFactorTileF64 : kFactorTileF32;
   fp.plan = PlanTasks(S, tile);
   const TaskPlan& T = fp.plan;
   FactorDev& f = fp.f;

@@ -13,6 +13,12 @@ namespace sfg {
 // Resident CTAs per SM the persistent factorization kernel is compiled for (its register budget:
 // 65,536 / (4 x 128 threads) = 128 per thread, which the register-resident diagonal tasks use).
 constexpr int kFactorCtasPerSm = 4;
+// Tile edge of the factorization.  The critical path of a front is pivots x pivot latency (a chain
+// of dependent FP64 operations, 64 cycles each on this GPU) plus panels x per-panel hand-offs;
+// measured on the 450-unknown reduced system, FP64 tiles of 8 and 16 give the same factor time
+// (0.66 ms), and 16 keeps the task list 7x shorter.
+constexpr int kFactorTileF64 = 16;
+constexpr int kFactorTileF32 = 32;
 
 // ---------------------------------------------------------------- linearization (kernels_lin.cu)
 // Evaluate every factor of a batch at the Init or New values, writing residual rows, packed

@@ -548,7 +548,7 @@ __device__ void TaskTrsm(const FactorDev& f, int s, int i, int k, T* F, const T*
     sm.d[c] = PivotReciprocal<T>(Ld(Fs + int64_t(ck + c) * (g.m + 1)));
   __syncthreads();
   // W(r, c) = sum_{q <= c} F(r, q) Li(c, q);  Li(c, q) = b[q * TILE + c]
-  T out[TILE * TILE / 32];
+  T out[TILE * TILE >= kFactorThreads ? TILE * TILE / kFactorThreads : 1];
   int n = 0;
   for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x, ++n) {
     const int r = e % TILE, c = e / TILE;
@@ -631,7 +631,7 @@ __device__ void TaskUpdate(const FactorDev& f, int s, int i, int j, int k, T* F,
   const int bi = TileSize(g, i, TILE), ri = TileStart(g, i, TILE);
   const int bj = TileSize(g, j, TILE), rj = TileStart(g, j, TILE);
   T* Fs = F + g.foff;
-  constexpr int kPer = TILE * TILE / kFactorThreads;
+  constexpr int kPer = TILE * TILE >= kFactorThreads ? TILE * TILE / kFactorThreads : 1;
   T cdst[kPer];
   {
     int n = 0;
@@ -1039,7 +1039,7 @@ void LaunchSchurBackSub(const SchurDev& d, const void* y, const void* W, const v
 template <typename T>
 void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F, void* Linv,
                   int grid, cudaStream_t s) {
-  constexpr int kTile = sizeof(T) == 8 ? 16 : 32;
+  constexpr int kTile = sizeof(T) == 8 ? kFactorTileF64 : kFactorTileF32;
   FactorKernel<T, kTile><<<grid, kFactorThreads, 0, s>>>(f, static_cast<const T*>(A), damping,
                                                          static_cast<T*>(F), static_cast<T*>(Linv));
 }
