@@ -38,8 +38,10 @@ NetPtrs Split(float* w) {
 struct Workspace {
   int cap = 0;
   float *H1, *H2, *Z, *dZ, *dH2, *dH1, *loss;
+  int* err;  // set by a tensor-core GEMM whose capped wait gave up
   void Init(DeviceArena& A, int n) {
     cap = n;
+    err = A.Zeros<int>(1);
     H1 = static_cast<float*>(A.Alloc(size_t(n) * kPrecondHidden * 4));
     H2 = static_cast<float*>(A.Alloc(size_t(n) * kPrecondHidden * 4));
     Z = static_cast<float*>(A.Alloc(size_t(n) * kPrecondTri * 4));
@@ -57,17 +59,18 @@ void ForwardBackward(const Workspace& ws, float* weights, float* grad, const flo
   const NetPtrs g = Split(grad);
   const int F = kPrecondFeatures, H = kPrecondHidden, O = kPrecondTri;
   const int64_t ld = kSampleFloats;
-  LaunchGemm(n, H, F, rows, ld, 1, w.W1, H, 1, ws.H1, H, kEpiBiasRelu, w.b1, nullptr, 0, s);
-  LaunchGemm(n, H, H, ws.H1, H, 1, w.W2, H, 1, ws.H2, H, kEpiBiasRelu, w.b2, nullptr, 0, s);
-  LaunchGemm(n, O, H, ws.H2, H, 1, w.W3, O, 1, ws.Z, O, kEpiBias, w.b3, nullptr, 0, s);
+  // every product on the tensor cores (tcgen05, TF32 with the three-pass FP32 split)
+  SFG_CUDA(LaunchGemmTc(n, H, F, rows, ld, 1, w.W1, H, 1, ws.H1, H, kEpiBiasRelu, w.b1, nullptr, 0, ws.err, s));
+  SFG_CUDA(LaunchGemmTc(n, H, H, ws.H1, H, 1, w.W2, H, 1, ws.H2, H, kEpiBiasRelu, w.b2, nullptr, 0, ws.err, s));
+  SFG_CUDA(LaunchGemmTc(n, O, H, ws.H2, H, 1, w.W3, O, 1, ws.Z, O, kEpiBias, w.b3, nullptr, 0, ws.err, s));
   LaunchHead(n, ws.Z, rows, ld, 1.f / float(n), kaporin, ws.dZ, ws.loss, loss_sum, s);
-  LaunchGemm(H, O, n, ws.H2, 1, H, ws.dZ, O, 1, g.W3, O, kEpiNone, nullptr, nullptr, 0, s);
+  SFG_CUDA(LaunchGemmTc(H, O, n, ws.H2, 1, H, ws.dZ, O, 1, g.W3, O, kEpiNone, nullptr, nullptr, 0, ws.err, s));
   LaunchColSum(n, O, ws.dZ, O, g.b3, s);
-  LaunchGemm(n, H, O, ws.dZ, O, 1, w.W3, 1, O, ws.dH2, H, kEpiMask, nullptr, ws.H2, H, s);
-  LaunchGemm(H, H, n, ws.H1, 1, H, ws.dH2, H, 1, g.W2, H, kEpiNone, nullptr, nullptr, 0, s);
+  SFG_CUDA(LaunchGemmTc(n, H, O, ws.dZ, O, 1, w.W3, 1, O, ws.dH2, H, kEpiMask, nullptr, ws.H2, H, ws.err, s));
+  SFG_CUDA(LaunchGemmTc(H, H, n, ws.H1, 1, H, ws.dH2, H, 1, g.W2, H, kEpiNone, nullptr, nullptr, 0, ws.err, s));
   LaunchColSum(n, H, ws.dH2, H, g.b2, s);
-  LaunchGemm(n, H, H, ws.dH2, H, 1, w.W2, 1, H, ws.dH1, H, kEpiMask, nullptr, ws.H1, H, s);
-  LaunchGemm(F, H, n, rows, 1, ld, ws.dH1, H, 1, g.W1, H, kEpiNone, nullptr, nullptr, 0, s);
+  SFG_CUDA(LaunchGemmTc(n, H, H, ws.dH2, H, 1, w.W2, 1, H, ws.dH1, H, kEpiMask, nullptr, ws.H1, H, ws.err, s));
+  SFG_CUDA(LaunchGemmTc(F, H, n, rows, 1, ld, ws.dH1, H, 1, g.W1, H, kEpiNone, nullptr, nullptr, 0, ws.err, s));
   LaunchColSum(n, H, ws.dH1, H, g.b1, s);
 }
 
@@ -86,6 +89,12 @@ int32_t GuardL(F&& fn) {
     g_last_error = e.what();
     return SFG_ERR_INVALID_ARGUMENT;
   }
+}
+
+void CheckErr(const int* err) {
+  int e = 0;
+  SFG_CUDA(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) throw Error(SFG_ERR_DEVICE_STATUS, "tensor-core GEMM: a wait hit its cap");
 }
 
 void UseDevice(int device) {
@@ -166,6 +175,7 @@ int32_t sfg_precond_train(const float* samples, int64_t n, const sfg_train_param
     }
     SFG_CUDA(cudaGetLastError());
     SFG_CUDA(cudaStreamSynchronize(s));
+    sfg::CheckErr(ws.err);
     SFG_CUDA(cudaMemcpy(weights, w, P * 4, cudaMemcpyDeviceToHost));
     if (loss_curve) {
       std::vector<double> l(p.steps);
@@ -196,6 +206,7 @@ int32_t sfg_precond_loss_grad(const float* samples, int64_t n, const float* weig
     sfg::ForwardBackward(ws, w, g, rows, int(n), kaporin, l, s);
     SFG_CUDA(cudaGetLastError());
     SFG_CUDA(cudaStreamSynchronize(s));
+    sfg::CheckErr(ws.err);
     if (loss) SFG_CUDA(cudaMemcpy(loss, l, 8, cudaMemcpyDeviceToHost));
     if (grad) SFG_CUDA(cudaMemcpy(grad, g, P * 4, cudaMemcpyDeviceToHost));
   });

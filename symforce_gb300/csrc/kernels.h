@@ -325,12 +325,14 @@ int BatchMaxCtasPerSm(int shape);
 void LaunchBatchLm(const BatchLmDev& d, const LmParams* p, int ctas, int shape, cudaStream_t s);
 
 // ---------------------------------------------------------------- network training (kernels_mlp.cu)
-// C[m][n] = sum_k A(m, k) B(k, n) (+ bias[n]) then ReLU, or times (mask[m][n] > 0); A(m, k) at
-// A[m * a_rs + k * a_cs], B(k, n) at B[k * b_rs + n * b_cs], C row-major with leading dim ldc.
+// Epilogues of the network's GEMMs: C = A B, + bias[n], ReLU(+ bias[n]), or times (mask[m][n] > 0).
 enum GemmEpilogue { kEpiNone = 0, kEpiBiasRelu = 1, kEpiBias = 2, kEpiMask = 3 };
-void LaunchGemm(int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs, const float* B,
-                int64_t b_rs, int64_t b_cs, float* C, int64_t ldc, int epilogue, const float* bias,
-                const float* mask, int64_t ldmask, cudaStream_t s);
+// C[M x N] = epilogue(A B) on the tensor cores (kernels_tc.cu); element (m, k) of A at
+// A[m a_rs + k a_cs], (k, n) of B at B[k b_rs + n b_cs], C row-major with leading dimension ldc;
+// a capped wait that gives up sets *err.
+cudaError_t LaunchGemmTc(int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs, const float* B,
+                         int64_t b_rs, int64_t b_cs, float* C, int64_t ldc, int epilogue, const float* bias,
+                         const float* mask, int64_t ldmask, int* err, cudaStream_t s);
 // out[n] = sum_m A[m][n] (fixed order).
 void LaunchColSum(int M, int N, const float* A, int64_t lda, float* out, cudaStream_t s);
 // Loss head: per sample (row of z, g_hat / x_hat at sample + 96 / + 105 with row stride lds)

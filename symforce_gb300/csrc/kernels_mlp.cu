@@ -1,7 +1,8 @@
-// Training kernels of the camera-block preconditioner network: a tiled FP32 GEMM with fused
-// bias / ReLU / ReLU-mask epilogues, column sums for bias gradients, the loss head (factor L from
-// the outputs, P = L L^T applied to g_hat against x_hat) with its analytic gradient, batch gather
-// and Adam.  Every reduction runs in a fixed order, so training is bit-reproducible.
+// Training kernels of the camera-block preconditioner network besides its GEMMs (which run on the
+// tensor cores, kernels_tc.cu): column sums for bias gradients, the loss head (factor L from the
+// outputs, P = L L^T applied to g_hat against x_hat, plus the Kaporin term) with its analytic
+// gradient, batch gather and Adam.  Every reduction runs in a fixed order, so training is
+// bit-reproducible.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -12,70 +13,9 @@ namespace sfg {
 
 namespace {
 
-constexpr int kTileM = 64, kTileN = 64, kTileK = 16;
 constexpr float kDiagShift = 0.54132485f;  // ln(e - 1)
 
 __device__ __forceinline__ int Tri(int i, int j) { return i * (i + 1) / 2 + j; }
-
-__global__ void __launch_bounds__(256) GemmKernel(int M, int N, int K, const float* A, int64_t a_rs,
-                                                  int64_t a_cs, const float* B, int64_t b_rs,
-                                                  int64_t b_cs, float* C, int64_t ldc, int epi,
-                                                  const float* bias, const float* mask,
-                                                  int64_t ldmask) {
-  __shared__ float As[kTileK][kTileM + 4];
-  __shared__ float Bs[kTileK][kTileN + 4];
-  const int tid = threadIdx.x;
-  const int ty = tid / 16, tx = tid % 16;
-  const int m0 = blockIdx.y * kTileM, n0 = blockIdx.x * kTileN;
-  float acc[4][4];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
-  for (int k0 = 0; k0 < K; k0 += kTileK) {
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int idx = tid + e * 256;  // 0..1023
-      // A tile: 64 rows x 16 k
-      const int am = idx / kTileK, ak = idx % kTileK;
-      const int gm = m0 + am, gk = k0 + ak;
-      As[ak][am] = (gm < M && gk < K) ? A[int64_t(gm) * a_rs + int64_t(gk) * a_cs] : 0.f;
-      // B tile: 16 k x 64 cols
-      const int bk = idx / kTileN, bn = idx % kTileN;
-      const int gk2 = k0 + bk, gn = n0 + bn;
-      Bs[bk][bn] = (gk2 < K && gn < N) ? B[int64_t(gk2) * b_rs + int64_t(gn) * b_cs] : 0.f;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < kTileK; ++k) {
-      float a[4], b[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[k][ty * 4 + i];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) b[j] = Bs[k][tx * 4 + j];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int gm = m0 + ty * 4 + i;
-    if (gm >= M) continue;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int gn = n0 + tx * 4 + j;
-      if (gn >= N) continue;
-      float v = acc[i][j];
-      if (epi == kEpiBiasRelu) v = fmaxf(v + bias[gn], 0.f);
-      else if (epi == kEpiBias) v += bias[gn];
-      else if (epi == kEpiMask) v = mask[int64_t(gm) * ldmask + gn] > 0.f ? v : 0.f;
-      C[int64_t(gm) * ldc + gn] = v;
-    }
-  }
-}
 
 __global__ void ColSumKernel(int M, int N, const float* A, int64_t lda, float* out) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -193,15 +133,6 @@ __global__ void AdamKernel(int64_t n, float* w, const float* g, float* m, float*
 }
 
 }  // namespace
-
-void LaunchGemm(int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs, const float* B,
-                int64_t b_rs, int64_t b_cs, float* C, int64_t ldc, int epilogue, const float* bias,
-                const float* mask, int64_t ldmask, cudaStream_t s) {
-  if (M == 0 || N == 0) return;
-  const dim3 grid((N + kTileN - 1) / kTileN, (M + kTileM - 1) / kTileM);
-  GemmKernel<<<grid, 256, 0, s>>>(M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, epilogue, bias,
-                                  mask, ldmask);
-}
 
 void LaunchColSum(int M, int N, const float* A, int64_t lda, float* out, cudaStream_t s) {
   const int threads = 128;

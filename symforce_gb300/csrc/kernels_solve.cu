@@ -716,6 +716,22 @@ constexpr int kSolvePanel = 32;
 // panel step of a wide front (256: a 450-wide front needs at most two rows per thread).
 constexpr int kSolveThreads = 256;
 
+// sum_{c = c0}^{c1 - 1} a[c * stride] x[c] with four independent accumulation chains (a dependent
+// FP64 multiply-add costs 64 cycles on this GPU), added in a fixed order.
+template <typename T>
+__device__ __forceinline__ T RowDot(const T* a, int64_t stride, const T* x, int c0, int c1) {
+  T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+  int c = c0;
+  for (; c + 4 <= c1; c += 4) {
+    s0 += Ld(a + int64_t(c) * stride) * x[c];
+    s1 += Ld(a + int64_t(c + 1) * stride) * x[c + 1];
+    s2 += Ld(a + int64_t(c + 2) * stride) * x[c + 2];
+    s3 += Ld(a + int64_t(c + 3) * stride) * x[c + 3];
+  }
+  for (; c < c1; ++c) s0 += Ld(a + int64_t(c) * stride) * x[c];
+  return (s0 + s1) + (s2 + s3);
+}
+
 template <typename T>
 __device__ void ForwardFront(const FactorDev& f, const Geom& g, const T* Fs, T* xs) {
   const int m = g.m;
@@ -737,11 +753,7 @@ __device__ void ForwardFront(const FactorDev& f, const Geom& g, const T* Fs, T* 
       if (r < p1) xs[r] = xr;
     }
     __syncthreads();
-    for (int r = p1 + threadIdx.x; r < m; r += blockDim.x) {
-      T acc = T(0);
-      for (int c = p0; c < p1; ++c) acc += Ld(Fs + r + int64_t(c) * m) * xs[c];
-      xs[r] -= acc;
-    }
+    for (int r = p1 + threadIdx.x; r < m; r += blockDim.x) xs[r] -= RowDot(Fs + r, int64_t(m), xs, p0, p1);
     __syncthreads();
   }
 }
@@ -768,12 +780,7 @@ __device__ void BackwardFront(const FactorDev& f, const Geom& g, const T* Fs, T*
       if (r < p1) xs[r] = xr;
     }
     __syncthreads();
-    for (int r = threadIdx.x; r < p0; r += blockDim.x) {
-      T acc = T(0);
-      const T* col = Fs + int64_t(r) * m;
-      for (int c = p0; c < p1; ++c) acc += Ld(col + c) * xs[c];
-      xs[r] -= acc;
-    }
+    for (int r = threadIdx.x; r < p0; r += blockDim.x) xs[r] -= RowDot(Fs + int64_t(r) * m, int64_t(1), xs, p0, p1);
     __syncthreads();
   }
 }
@@ -837,10 +844,8 @@ __global__ void __launch_bounds__(kSolveThreads) SolveKernel(FactorDev f, const 
         for (int r = threadIdx.x; r < h; r += blockDim.x) xa[r] = Ld(xperm + idx[g.w + r]);
         __syncthreads();
         for (int q = threadIdx.x; q < g.w; q += blockDim.x) {
-          T z = Ld(ysave + f.idx_off[s] + q) / Ld(Fs + int64_t(q) * (g.m + 1));
-          const T* col = Fs + int64_t(q) * g.m + g.w;
-          for (int r = 0; r < h; ++r) z -= Ld(col + r) * xa[r];
-          xs[q] = z;
+          const T z = Ld(ysave + f.idx_off[s] + q) / Ld(Fs + int64_t(q) * (g.m + 1));
+          xs[q] = z - RowDot(Fs + int64_t(q) * g.m + g.w, int64_t(1), xa, 0, h);
         }
         __syncthreads();
         BackwardFront<T>(f, g, Fs, xs);

@@ -1,5 +1,7 @@
-// Tensor-core (tcgen05, TF32) GEMM with bias / ReLU epilogue for the preconditioner network's
-// inference pass: out[M x N] = act(A[M x K] W[K x N] + bias).
+// Tensor-core (tcgen05, TF32) GEMM of the preconditioner network, inference and training:
+// out[M x N] = epilogue(A[M x K] B[K x N]) with strided operands (element (m, k) of A at
+// A[m a_rs + k a_cs], element (k, n) of B at B[k b_rs + n b_cs]) and the epilogues none, + bias,
+// ReLU(+ bias), or a ReLU mask (out = mask[m][n] > 0 ? v : 0).
 //
 //  - One CTA of 128 threads per 128-row x NP-column tile (NP = 128 for the hidden layers, 48 for the
 //    45 outputs); the accumulator lives in tensor memory (TMEM, 128 lanes x NP FP32 columns,
@@ -88,11 +90,26 @@ __device__ __forceinline__ void MmaCommit(uint64_t* bar) {
                : "memory");
 }
 
-template <int NP, bool kRelu>
-__global__ void __launch_bounds__(kTcThreads) TcGemmKernel(const float* A, int64_t lda, int M, int K,
-                                                           const float* W, int ldw, const float* bias,
-                                                           int N, float* out, int64_t ldo, int vec4,
-                                                           int* err) {
+struct TcArgs {
+  const float* A;
+  int64_t a_rs, a_cs;
+  const float* B;
+  int64_t b_rs, b_cs;
+  int M, N, K;
+  float* out;
+  int64_t ldo;
+  int epi;
+  const float* bias;
+  const float* mask;
+  int64_t ldmask;
+  int vec4;  // A rows are 16-byte aligned with unit column stride: 16-byte loads
+  int* err;
+};
+
+template <int NP>
+__global__ void __launch_bounds__(kTcThreads) TcGemmKernel(TcArgs g) {
+  const float* A = g.A;
+  const int M = g.M, K = g.K, N = g.N;
   static_assert(NP % 16 == 0 && NP >= 16 && NP <= 256, "N of a kind::tf32 MMA with M = 128");
   constexpr int kCols = NP <= 32 ? 32 : NP <= 64 ? 64 : NP <= 128 ? 128 : 256;  // TMEM columns
   extern __shared__ __align__(1024) unsigned char tc_smem[];
@@ -137,24 +154,24 @@ __global__ void __launch_bounds__(kTcThreads) TcGemmKernel(const float* A, int64
     for (int i = 0; i < kAPer; ++i) {
       const int idx = tid + i * kTcThreads;
       const int r = idx >> 3, k4 = (idx & 7) * 4, gr = row0 + r, gk = k0 + k4;
-      if (vec4 && gr < M && gk + 3 < K) {
-        av[i] = __ldg(reinterpret_cast<const float4*>(A + int64_t(gr) * lda + gk));
+      if (g.vec4 && gr < M && gk + 3 < K) {
+        av[i] = __ldg(reinterpret_cast<const float4*>(A + int64_t(gr) * g.a_rs + gk));
       } else {
-        const float* ap = A + int64_t(gr) * lda + gk;
+        const float* ap = A + int64_t(gr) * g.a_rs + int64_t(gk) * g.a_cs;
         av[i].x = (gr < M && gk < K) ? __ldg(ap) : 0.f;
-        av[i].y = (gr < M && gk + 1 < K) ? __ldg(ap + 1) : 0.f;
-        av[i].z = (gr < M && gk + 2 < K) ? __ldg(ap + 2) : 0.f;
-        av[i].w = (gr < M && gk + 3 < K) ? __ldg(ap + 3) : 0.f;
+        av[i].y = (gr < M && gk + 1 < K) ? __ldg(ap + g.a_cs) : 0.f;
+        av[i].z = (gr < M && gk + 2 < K) ? __ldg(ap + 2 * g.a_cs) : 0.f;
+        av[i].w = (gr < M && gk + 3 < K) ? __ldg(ap + 3 * g.a_cs) : 0.f;
       }
     }
-    // W^T: row n of the operand is column n0 + n of W (consecutive threads, consecutive n)
+    // B^T: row n of the operand is column n0 + n of B (consecutive threads, consecutive n)
 #pragma unroll
     for (int j = 0; j < kBPer; ++j) {
       const int n = tid + j * kTcThreads, gn = n0 + n;
 #pragma unroll
       for (int k = 0; k < kTcKc; ++k) {
         const int gk = k0 + k;
-        bv[j][k] = (n < NP && gn < N && gk < K) ? __ldg(W + int64_t(gk) * ldw + gn) : 0.f;
+        bv[j][k] = (n < NP && gn < N && gk < K) ? __ldg(g.B + int64_t(gk) * g.b_rs + int64_t(gn) * g.b_cs) : 0.f;
       }
     }
   };
@@ -205,7 +222,7 @@ __global__ void __launch_bounds__(kTcThreads) TcGemmKernel(const float* A, int64
     if (issued) {
       // the MMAs of the previous chunk must have read shared memory before it is restaged
       if (!MbarWait(&bar, phase)) {
-        if (lane == 0) atomicExch(err, kDevSpinTimeout);
+        if (lane == 0) atomicExch(g.err, kDevSpinTimeout);
         s_fail = 1;
       }
       phase ^= 1u;
@@ -233,7 +250,7 @@ __global__ void __launch_bounds__(kTcThreads) TcGemmKernel(const float* A, int64
   // the last chunk's MMAs complete the accumulator
   if (issued && !s_fail) {
     if (!MbarWait(&bar, phase)) {
-      if (lane == 0) atomicExch(err, kDevSpinTimeout);
+      if (lane == 0) atomicExch(g.err, kDevSpinTimeout);
       s_fail = 1;
     }
     phase ^= 1u;
@@ -260,9 +277,11 @@ __global__ void __launch_bounds__(kTcThreads) TcGemmKernel(const float* A, int64
         for (int i = 0; i < 16; ++i) {
           const int c = n0 + c0 + i;
           if (c < N) {
-            float y = __uint_as_float(v[i]) + bias[c];
-            if (kRelu) y = fmaxf(y, 0.f);
-            out[int64_t(gr) * ldo + c] = y;
+            float y = __uint_as_float(v[i]);
+            if (g.epi == kEpiBias || g.epi == kEpiBiasRelu) y += g.bias[c];
+            if (g.epi == kEpiBiasRelu) y = fmaxf(y, 0.f);
+            if (g.epi == kEpiMask && !(g.mask[int64_t(gr) * g.ldmask + c] > 0.f)) y = 0.f;
+            g.out[int64_t(gr) * g.ldo + c] = y;
           }
         }
       }
@@ -277,25 +296,32 @@ __global__ void __launch_bounds__(kTcThreads) TcGemmKernel(const float* A, int64
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(d_tmem), "r"(kCols) : "memory");
 }
 
-template <int NP, bool kRelu>
+template <int NP>
 size_t TcSmem() {
   return size_t(kTcRows) * kTcKc * 4 * 2 + size_t(NP) * kTcKc * 4 * 2;
 }
 
-template <int NP, bool kRelu>
-cudaError_t LaunchTc(const float* A, int64_t lda, int M, int K, const float* W, int ldw, const float* bias,
-                     int N, float* out, int64_t ldo, int* err, cudaStream_t s) {
-  const size_t smem = TcSmem<NP, kRelu>();
-  const cudaError_t e = cudaFuncSetAttribute(TcGemmKernel<NP, kRelu>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             int(smem));
+template <int NP>
+cudaError_t LaunchTc(TcArgs g, cudaStream_t s) {
+  const size_t smem = TcSmem<NP>();
+  const cudaError_t e = cudaFuncSetAttribute(TcGemmKernel<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) return e;
-  const int vec4 = (lda % 4 == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0) ? 1 : 0;
-  const dim3 grid((M + kTcRows - 1) / kTcRows, (N + NP - 1) / NP);
-  TcGemmKernel<NP, kRelu><<<grid, kTcThreads, smem, s>>>(A, lda, M, K, W, ldw, bias, N, out, ldo, vec4, err);
+  g.vec4 = (g.a_cs == 1 && g.a_rs % 4 == 0 && (reinterpret_cast<uintptr_t>(g.A) & 15) == 0) ? 1 : 0;
+  const dim3 grid((g.M + kTcRows - 1) / kTcRows, (g.N + NP - 1) / NP);
+  TcGemmKernel<NP><<<grid, kTcThreads, smem, s>>>(g);
   return cudaGetLastError();
 }
 
 }  // namespace
+
+cudaError_t LaunchGemmTc(int M, int N, int K, const float* A, int64_t a_rs, int64_t a_cs, const float* B,
+                         int64_t b_rs, int64_t b_cs, float* C, int64_t ldc, int epilogue, const float* bias,
+                         const float* mask, int64_t ldmask, int* err, cudaStream_t s) {
+  if (M == 0 || N == 0) return cudaSuccess;
+  TcArgs g{A, a_rs, a_cs, B, b_rs, b_cs, M, N, K, C, ldc, epilogue, bias, mask, ldmask, 0, err};
+  // 48 columns for the 45 outputs, otherwise tiles of 128 columns
+  return N <= 48 ? LaunchTc<48>(g, s) : LaunchTc<128>(g, s);
+}
 
 cudaError_t LaunchMlpInferTc(const float* x, int64_t ldx, int64_t n, const float* weights, float* h1, float* h2,
                              float* z, int* err, cudaStream_t s) {
@@ -308,12 +334,11 @@ cudaError_t LaunchMlpInferTc(const float* x, int64_t ldx, int64_t n, const float
   const float* W3 = b2 + H;
   const float* b3 = W3 + H * O;
   const int m = int(n);
-  // hidden layers: two CTAs of 128 output columns per 128-row tile
-  cudaError_t e = LaunchTc<128, true>(x, ldx, m, F, W1, H, b1, H, h1, H, err, s);
+  cudaError_t e = LaunchGemmTc(m, H, F, x, ldx, 1, W1, H, 1, h1, H, kEpiBiasRelu, b1, nullptr, 0, err, s);
   if (e != cudaSuccess) return e;
-  e = LaunchTc<128, true>(h1, H, m, H, W2, H, b2, H, h2, H, err, s);
+  e = LaunchGemmTc(m, H, H, h1, H, 1, W2, H, 1, h2, H, kEpiBiasRelu, b2, nullptr, 0, err, s);
   if (e != cudaSuccess) return e;
-  return LaunchTc<48, false>(h2, H, m, H, W3, O, b3, O, z, O, err, s);
+  return LaunchGemmTc(m, O, H, h2, H, 1, W3, O, 1, z, O, kEpiBias, b3, nullptr, 0, err, s);
 }
 
 }  // namespace sfg

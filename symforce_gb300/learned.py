@@ -30,7 +30,7 @@ TRAIN_SEED_BASE = 10_000  # training instances use seeds TRAIN_SEED_BASE + k, di
 # Weight of the Kaporin term of the shipped weights.  Block Jacobi minimizes Kaporin's condition
 # number over block-diagonal preconditioners, so the regression term alone (weight 0) moves the
 # network to blocks that need 15-35 % more PCG iterations than block Jacobi on held-out problems;
-# weight 10 keeps it beside block Jacobi, where it saves 0.1-2 % (the FP64 PCG comparison in
+# weight 10 keeps it beside block Jacobi, where it saves ~1 % (the FP64 PCG comparison in
 # tests/test_gpu_pcg.py).
 KAPORIN = 10.0
 
