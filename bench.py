@@ -415,14 +415,24 @@ def _batched_section(device: int, steps: int, cpu_budget_s: float) -> dict:
     import oracle_lib as O
     threads = os.cpu_count() or 1
     done, t0 = 0, time.perf_counter()
+    ref_best, ref_status = [], []
     with ThreadPoolExecutor(threads) as ex:
         while time.perf_counter() - t0 < cpu_budget_s and done < BATCH_PROBLEMS:
             chunk = problems[done:done + 4 * threads]
-            list(ex.map(lambda p: O.optimize(p, params), chunk))
+            for r in ex.map(lambda p: O.optimize(p, params), chunk):
+                ref_best.append(r["iterations"][r["best_index"]].new_error)
+                ref_status.append(r["status"])
             done += len(chunk)
     cpu_s = time.perf_counter() - t0
     out["cpu_baseline"] = {"problems_per_s": round(done / cpu_s, 1), "cores": threads, "kind": "port",
                            "sample": f"the first {done} of the {BATCH_PROBLEMS} problems"}
+    # per-problem parity on the same sample: best cost within 1e-9 and the same status
+    if done:
+        gb, rb = res.best_error[:done], np.array(ref_best)
+        rel = np.abs(gb - rb) / np.maximum(np.abs(rb), 1e-300)
+        out["parity_vs_oracle"] = {"problems": done, "within_1e-9": int((rel <= 1e-9).sum()),
+                                   "same_status": int((res.status[:done] == np.array(ref_status)).sum()),
+                                   "max_rel_cost_diff": float(rel.max())}
     return out, len(dev) + 2
 
 
