@@ -259,6 +259,11 @@ int32_t sfg_get_pcg_stats(sfg_handle* h, sfg_pcg_stats_t* out);
 int32_t sfg_pcg_step_error(sfg_handle* h, double* rel_step_error, int32_t* iterations,
                            double* rel_residual);
 
+/* MIXED form: FP32 diagonal tiles of the factorization that had a near-singular pivot (one that kept
+ * less than 1/4096 of its diagonal entry, or was not positive) and were factored again in FP64
+ * from their input, counted over the handle's life (no counterpart in the reference). */
+int32_t sfg_fp64_diag_tiles(sfg_handle* h, int64_t* count);
+
 /* -------------------------------- learned preconditioner -------------------------------------
  * No counterpart in the reference.  One network per camera block: input = the camera's 9 x 9
  * reduced-system block scaled to unit diagonal (81 values, row-major), log(1 + rho_r) for its 9

@@ -943,6 +943,19 @@ int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_pe
   });
 }
 
+int32_t sfg_fp64_diag_tiles(sfg_handle* h, int64_t* count) {
+  return Guard([&] {
+    if (!h || !count) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    int c = 0;
+    if (h->fp.f.fp64_tiles) {
+      SFG_CUDA(cudaSetDevice(h->device));
+      SFG_CUDA(cudaStreamSynchronize(h->stream));
+      SFG_CUDA(cudaMemcpy(&c, h->fp.f.fp64_tiles, sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    *count = c;
+  });
+}
+
 int32_t sfg_get_pcg_stats(sfg_handle* h, sfg_pcg_stats_t* out) {
   return Guard([&] {
     if (!h || !out) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");

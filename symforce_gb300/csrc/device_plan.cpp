@@ -138,6 +138,7 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   fp.nflags = 2 * S.ns;
   f.front_flags = A.Zeros<int>(size_t(fp.nflags));
   f.error = error_word;
+  f.fp64_tiles = A.Zeros<int>(1);
   int maxm = 1;
   for (int s = 0; s < S.ns; ++s) maxm = std::max(maxm, S.sn_m[s]);
   f.max_m = maxm;

@@ -190,6 +190,7 @@ struct FactorDev {
   int* counters;              // [0]: factor task counter, [1]: solve task counter
   int* front_flags;           // [2 * ns]: forward done, backward done
   int* error;                 // device error word
+  int* fp64_tiles;            // optional: FP32 diagonal tiles factored again in FP64 (near-singular)
   int max_m;                  // largest front (solve kernel shared memory)
   const LmState* st;          // state whose Init block the matrix / rhs are read from
   int64_t a_stride;           // per-state-block stride of the matrix values (0: fixed)

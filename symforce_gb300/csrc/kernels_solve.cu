@@ -326,8 +326,8 @@ __device__ __forceinline__ int StateIdx(const Geom& g, int i, int j) { return g.
 // Shared tiles are stored transposed (column index major, row index minor) so that the lanes of a
 // warp, which walk consecutive rows, read consecutive words.
 template <typename T, int TILE>
-struct TileSmem {
-  T a[TILE * TILE];
+struct alignas(16) TileSmem {
+  T a[TILE * TILE];  // a and b are contiguous: together they hold a double tile (FP64 redo of a tile)
   T b[TILE * TILE];
   T c[TILE * TILE];
   T d[TILE];
@@ -431,6 +431,36 @@ __device__ void TaskAssemble(const FactorDev& f, int s, int tj, const T* A, cons
 // of every front, and the two precisions take the form that measured fastest for them on one
 // GB300 SM (TILE 16 FP64: CTA-wide steps 12.6 us, one warp 18-32 us; TILE 32 FP32: one warp with
 // the rows in registers and a rolled pivot loop 12 us, CTA-wide steps 37 us).
+// CTA-wide right-looking LDL^T steps of a tile held transposed in shared memory (b x b of it), one
+// barrier per pivot: every thread forms the pivot's reciprocal itself (same bits everywhere), and
+// column j is scaled during step j + 1, which does not read it.
+template <typename D, int TILE>
+__device__ __forceinline__ void LdltStepsCta(D* a, int b) {
+  D inv_prev = D(0);
+  for (int j = 0; j < b; ++j) {
+    const D inv = PivotReciprocal<D>(a[j * TILE + j]);
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+      const int r = e % TILE, c = e / TILE;
+      if (c > j && r >= c && r < b) a[c * TILE + r] -= a[j * TILE + r] * (a[j * TILE + c] * inv);
+      if (j > 0 && c == j - 1 && r > c && r < b) a[c * TILE + r] *= inv_prev;
+    }
+    inv_prev = inv;
+    __syncthreads();
+  }
+}
+
+// A pivot of an FP32 diagonal tile that kept less than this fraction of its diagonal entry (more
+// than 12 of FP32's 24 bits cancelled), or is not positive, sends the tile to the FP64 redo.
+constexpr float kNearSingularPivot = 1.0f / 4096.0f;
+
+// LDL^T of diagonal tile k, held transposed in shared memory `a` (b x b of it), plus the explicit
+// inverse of its unit lower factor (kept for the panel solves, which then become small matrix
+// products); writes L, D and the inverse and publishes the tile.  This task is on the critical path
+// of every front, and the two precisions take the form that measured fastest for them on one
+// GB300 SM (TILE 16 FP64: CTA-wide steps 12.6 us, one warp 18-32 us; TILE 32 FP32: one warp with
+// the rows in registers and a rolled pivot loop 12 us, CTA-wide steps 37 us).  An FP32 tile with a
+// near-singular pivot is factored again in FP64 from its saved input and rounded back (counted in
+// f.fp64_tiles).
 template <typename T, int TILE>
 __device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, T* Linv, T* a,
                          TileSmem<T, TILE>& sm) {
@@ -439,20 +469,7 @@ __device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, 
   T* Fs = F + g.foff;
   T* li = sm.b;
   if constexpr (sizeof(T) == 8) {
-    // CTA-wide right-looking steps, one barrier per pivot: every thread forms the pivot's
-    // reciprocal itself (same bits everywhere), and column j is scaled during step j + 1, which
-    // does not read it
-    T inv_prev = T(0);
-    for (int j = 0; j < b; ++j) {
-      const T inv = PivotReciprocal<T>(a[j * TILE + j]);
-      for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
-        const int r = e % TILE, c = e / TILE;
-        if (c > j && r >= c && r < b) a[c * TILE + r] -= a[j * TILE + r] * (a[j * TILE + c] * inv);
-        if (j > 0 && c == j - 1 && r > c && r < b) a[c * TILE + r] *= inv_prev;
-      }
-      inv_prev = inv;
-      __syncthreads();
-    }
+    LdltStepsCta<T, TILE>(a, b);
     // unit lower inverse by forward substitution on all columns at once: after step q, row q of Li
     // is final and is eliminated from the rows below it
     for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) li[e] = T((e % TILE) == (e / TILE) ? 1 : 0);
@@ -465,17 +482,26 @@ __device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, 
       __syncthreads();
     }
   } else {
+    // the tile's input, kept for an FP64 redo
+    T* orig = sm.c;
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) orig[e] = a[e];
+    __shared__ int s_redo;
+    if (threadIdx.x == 0) s_redo = 0;
+    __syncthreads();
+    constexpr unsigned kAll = 0xffffffffu;
     // one warp, lane r holds row r in registers shifted one column left per pivot (row[c] =
     // a(r, j + c)), the multipliers reach the other rows by shuffles; a rolled pivot loop keeps the
     // code small
     if (threadIdx.x < 32) {
-      constexpr unsigned kAll = 0xffffffffu;
       const int r = threadIdx.x;
       T row[TILE];
 #pragma unroll
       for (int c = 0; c < TILE; ++c) row[c] = (r < b && c <= r) ? a[c * TILE + (r < TILE ? r : 0)] : T(0);
+      bool redo = false;
       for (int j = 0; j < b; ++j) {
-        const T inv = PivotReciprocal<T>(__shfl_sync(kAll, row[0], j));
+        const T dj = __shfl_sync(kAll, row[0], j);
+        redo = redo || !(dj > kNearSingularPivot * fabsf(float(orig[j * TILE + j])));
+        const T inv = PivotReciprocal<T>(dj);
         const T lrj = row[0] * inv;
 #pragma unroll
         for (int c = 1; c < TILE; ++c) {
@@ -487,7 +513,23 @@ __device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, 
         for (int c = 0; c + 1 < TILE; ++c) row[c] = row[c + 1];
         row[TILE - 1] = T(0);
       }
-      __syncwarp();
+      if (r == 0 && redo) s_redo = 1;
+    }
+    __syncthreads();
+    if (s_redo) {
+      // FP64 redo from the saved input: the double tile occupies a and b
+      double* dt = reinterpret_cast<double*>(sm.a);
+      for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) dt[e] = double(orig[e]);
+      __syncthreads();
+      LdltStepsCta<double, TILE>(dt, b);
+      for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) orig[e] = T(dt[e]);
+      __syncthreads();
+      for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) a[e] = orig[e];
+      if (threadIdx.x == 0 && f.fp64_tiles) atomicAdd(f.fp64_tiles, 1);
+      __syncthreads();
+    }
+    if (threadIdx.x < 32) {
+      const int r = threadIdx.x;
       T lrow[TILE];
 #pragma unroll
       for (int c = 0; c < TILE; ++c) lrow[c] = T(c == r ? 1 : 0);

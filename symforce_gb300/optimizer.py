@@ -50,6 +50,7 @@ def lib() -> C.CDLL:
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.sfg_storage_dim.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                       C.POINTER(C.c_int64)]
+        L.sfg_fp64_diag_tiles.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
         L.sfg_ldlt_create.argtypes = [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
                                       C.c_int32, C.POINTER(C.c_void_p)]
         L.sfg_ldlt_factorize.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
@@ -131,6 +132,12 @@ class Optimizer:
         s = A.PcgStatsC()
         _check(lib().sfg_get_pcg_stats(self._h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in A.PcgStatsC._fields_}
+
+    def fp64_diag_tiles(self) -> int:
+        """Mixed form: FP32 diagonal tiles factored again in FP64 (near-singular pivots) so far."""
+        n = C.c_int64()
+        _check(lib().sfg_fp64_diag_tiles(self._h, C.byref(n)))
+        return n.value
 
     def pcg_step_error(self) -> dict:
         """The exact LDL^T as judge of one PCG step at the last accepted state."""
