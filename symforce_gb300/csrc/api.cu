@@ -432,12 +432,15 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
     BatchDev d{};
     d.count = B.count;
     d.nent = h->L.maps[b].nent;
+    // structure-of-arrays in the layout's device order of the factors
+    const std::vector<int32_t>& order = h->L.maps[b].order;
     std::vector<int32_t> keys(size_t(B.count) * B.nk);
     for (int f = 0; f < B.count; ++f)
-      for (int k = 0; k < B.nk; ++k) keys[size_t(k) * B.count + f] = B.keys[size_t(f) * B.nk + k];
+      for (int k = 0; k < B.nk; ++k) keys[size_t(k) * B.count + f] = B.keys[size_t(order[f]) * B.nk + k];
     std::vector<double> consts(size_t(B.count) * B.nc);
     for (int f = 0; f < B.count; ++f)
-      for (int c = 0; c < B.nc; ++c) consts[size_t(c) * B.count + f] = B.consts[size_t(f) * B.nc + c];
+      for (int c = 0; c < B.nc; ++c)
+        consts[size_t(c) * B.count + f] = B.consts[size_t(order[f]) * B.nc + c];
     d.keys = A.Upload(keys);
     d.consts = A.Upload(consts);
     d.dest = A.Upload(h->L.maps[b].dest);
@@ -768,9 +771,19 @@ int32_t sfg_linearize(sfg_handle* h, double* residual, double* rhs, double* erro
     SFG_CUDA(cudaStreamSynchronize(s));
     SFG_CUDA(cudaGetLastError());
     h->last_linearized_block = blk;
-    if (residual)
-      SFG_CUDA(cudaMemcpy(residual, h->residual + size_t(blk) * h->P.M, sizeof(double) * h->P.M,
+    if (residual) {
+      // the device holds each batch's residuals in its device factor order
+      std::vector<double> dev(size_t(h->P.M));
+      SFG_CUDA(cudaMemcpy(dev.data(), h->residual + size_t(blk) * h->P.M, sizeof(double) * h->P.M,
                           cudaMemcpyDeviceToHost));
+      for (size_t b = 0; b < h->P.batches.size(); ++b) {
+        const sfg::HostBatch& B = h->P.batches[b];
+        const std::vector<int32_t>& order = h->L.maps[b].order;
+        for (int f = 0; f < B.count; ++f)
+          for (int i = 0; i < B.rdim; ++i)
+            residual[B.roff + int64_t(order[f]) * B.rdim + i] = dev[B.roff + int64_t(f) * B.rdim + i];
+      }
+    }
     if (rhs) {
       if (h->elem == 8) {
         SFG_CUDA(cudaMemcpy(rhs, static_cast<double*>(h->rhs) + size_t(blk) * h->P.N,

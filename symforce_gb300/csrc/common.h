@@ -56,6 +56,12 @@ inline FactorSpec Spec(int kind) {
   throw Error(SFG_ERR_INVALID_ARGUMENT, "unknown factor kind " + std::to_string(kind));
 }
 
+// Leading key slots whose J^T J / J^T r entries a warp of the linearization kernel sums before
+// storing, when all 32 of its factors share those keys (the factors of such a kind are ordered by
+// these keys on the device).  Snavely reprojection: the camera's pose and calibration, seen by
+// hundreds of observations each.  The factor traits of the kernel carry the same number.
+constexpr int MergedKeySlots(int kind) { return kind == SFG_FACTOR_SNAVELY_REPROJECTION ? 2 : 0; }
+
 // ---------------------------------------------------------------------------------------------
 // Host problem
 // ---------------------------------------------------------------------------------------------

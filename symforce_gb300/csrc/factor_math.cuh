@@ -19,41 +19,43 @@ namespace sfg {
 
 #define SFG_HD __host__ __device__ __forceinline__
 
+// NK keys, NC constants, RD residual rows, TD tangent columns; KT / KS the tangent and storage
+// size of key slot k; MK the leading key slots whose entries a warp sums (MergedKeySlots).
 template <int KIND>
 struct FactorTraits;
 template <>
 struct FactorTraits<SFG_FACTOR_BEARING_POSE2> {
-  static constexpr int NK = 1, NC = 5, RD = 1, TD = 3;
+  static constexpr int NK = 1, NC = 5, RD = 1, TD = 3, MK = 0;
   static constexpr SFG_HD int KT(int k) { return k == 0 ? 3 : (k == 1 ? 0 : 0); }
   static constexpr SFG_HD int KS(int k) { return k == 0 ? 4 : (k == 1 ? 0 : 0); }
 };
 template <>
 struct FactorTraits<SFG_FACTOR_ODOMETRY_POSE2> {
-  static constexpr int NK = 2, NC = 3, RD = 1, TD = 6;
+  static constexpr int NK = 2, NC = 3, RD = 1, TD = 6, MK = 0;
   static constexpr SFG_HD int KT(int k) { return k == 0 ? 3 : (k == 1 ? 3 : 0); }
   static constexpr SFG_HD int KS(int k) { return k == 0 ? 4 : (k == 1 ? 4 : 0); }
 };
 template <>
 struct FactorTraits<SFG_FACTOR_SNAVELY_REPROJECTION> {
-  static constexpr int NK = 3, NC = 4, RD = 2, TD = 12;
+  static constexpr int NK = 3, NC = 4, RD = 2, TD = 12, MK = 2;
   static constexpr SFG_HD int KT(int k) { return k == 0 ? 6 : (k == 1 ? 3 : 3); }
   static constexpr SFG_HD int KS(int k) { return k == 0 ? 7 : (k == 1 ? 3 : 3); }
 };
 template <>
 struct FactorTraits<SFG_FACTOR_BETWEEN_POSE3> {
-  static constexpr int NK = 2, NC = 14, RD = 6, TD = 12;
+  static constexpr int NK = 2, NC = 14, RD = 6, TD = 12, MK = 0;
   static constexpr SFG_HD int KT(int k) { return k == 0 ? 6 : (k == 1 ? 6 : 0); }
   static constexpr SFG_HD int KS(int k) { return k == 0 ? 7 : (k == 1 ? 7 : 0); }
 };
 template <>
 struct FactorTraits<SFG_FACTOR_PRIOR_POSE3> {
-  static constexpr int NK = 1, NC = 14, RD = 6, TD = 6;
+  static constexpr int NK = 1, NC = 14, RD = 6, TD = 6, MK = 0;
   static constexpr SFG_HD int KT(int k) { return k == 0 ? 6 : (k == 1 ? 0 : 0); }
   static constexpr SFG_HD int KS(int k) { return k == 0 ? 7 : (k == 1 ? 0 : 0); }
 };
 template <>
 struct FactorTraits<SFG_FACTOR_RANGE_POSE3> {
-  static constexpr int NK = 1, NC = 6, RD = 1, TD = 6;
+  static constexpr int NK = 1, NC = 6, RD = 1, TD = 6, MK = 0;
   static constexpr SFG_HD int KT(int k) { return k == 0 ? 6 : (k == 1 ? 0 : 0); }
   static constexpr SFG_HD int KS(int k) { return k == 0 ? 7 : (k == 1 ? 0 : 0); }
 };

@@ -6,6 +6,13 @@
 // its packed J^T J / J^T r goes.  Entries with a single contributor are written in place by the
 // linearization kernel; shared entries get staging slots grouped per destination in factor order
 // and are summed by a second kernel, which makes the result independent of thread scheduling.
+//
+// Factors of a kind with merged key slots (MergedKeySlots: the camera of a reprojection factor)
+// are put in device order by those keys.  A warp of 32 consecutive device factors that all share
+// them sums the entries among those keys across its lanes (a shuffle reduce-scatter) and makes one
+// contribution per entry, at the sink index of its first factor; every other entry stays one
+// contribution per factor.  The staged work of a camera block falls from one slot per observation
+// to one per warp.
 #include <algorithm>
 #include <numeric>
 
@@ -32,7 +39,44 @@ LinLayout BuildLinLayout(const HostProblem& P) {
     const int64_t blk = L.H.Find(k, k);
     for (int r = 0; r < P.tdim[k]; ++r) L.diag_off[P.toff[k] + r] = L.H.boff[blk] + r * P.tdim[k] + r;
   }
-  // slot (H value index or nvals + tangent index) of every factor entry
+  // device order of every batch and the warps that merge their leading key slots
+  std::vector<std::vector<int32_t>> order(P.batches.size());
+  std::vector<std::vector<char>> warp_merged(P.batches.size());
+  std::vector<int> merged_dims(P.batches.size(), 0);
+  for (size_t bi = 0; bi < P.batches.size(); ++bi) {
+    const auto& B = P.batches[bi];
+    const int ms = MergedKeySlots(B.kind);
+    auto& ord = order[bi];
+    ord.resize(B.count);
+    std::iota(ord.begin(), ord.end(), 0);
+    if (ms == 0) continue;
+    for (int s = 0; s < ms; ++s) merged_dims[bi] += B.key_tdim[s];
+    auto key = [&](int32_t f, int s) { return B.keys[size_t(f) * B.nk + s]; };
+    std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) {
+      for (int s = 0; s < ms; ++s)
+        if (key(x, s) != key(y, s)) return key(x, s) < key(y, s);
+      return false;
+    });
+    const int nwarps = B.count / 32;  // full warps only
+    warp_merged[bi].assign(size_t(nwarps), 0);
+    for (int w = 0; w < nwarps; ++w) {
+      bool same = true;
+      for (int l = 1; l < 32 && same; ++l)
+        for (int s = 0; s < ms; ++s) same = same && key(ord[32 * w + l], s) == key(ord[32 * w], s);
+      warp_merged[bi][w] = same;
+    }
+  }
+  // Whether device factor f of batch bi contributes entry e itself (false: its warp's first
+  // factor carries the warp's sum).
+  auto contributes = [&](size_t bi, int f, int e, int nh) {
+    const int mt = merged_dims[bi];
+    if (mt == 0 || (f & 31) == 0) return true;
+    const size_t w = size_t(f) / 32;
+    if (w >= warp_merged[bi].size() || !warp_merged[bi][w]) return true;
+    const bool merged_entry = e < nh ? e < mt * (mt + 1) / 2 : e - nh < mt;
+    return !merged_entry;
+  };
+  // slot (H value index or nvals + tangent index) of every factor entry; f is the user's index
   auto entry_slot = [&](const HostBatch& B, int f, int e, int* kslot_of, int* local_of) -> int64_t {
     const int td = B.tdim;
     const int nh = td * (td + 1) / 2;
@@ -64,9 +108,11 @@ LinLayout BuildLinLayout(const HostProblem& P) {
   }
   for (size_t bi = 0; bi < P.batches.size(); ++bi) {
     const auto& B = P.batches[bi];
-    const int nent = B.tdim * (B.tdim + 1) / 2 + B.tdim;
+    const int nh = B.tdim * (B.tdim + 1) / 2;
+    const int nent = nh + B.tdim;
     for (int f = 0; f < B.count; ++f)
-      for (int e = 0; e < nent; ++e) cnt[entry_slot(B, f, e, kslot[bi].data(), local[bi].data())]++;
+      for (int e = 0; e < nent; ++e)
+        if (contributes(bi, f, e, nh)) cnt[entry_slot(B, order[bi][f], e, kslot[bi].data(), local[bi].data())]++;
   }
   for (int64_t s = 0; s < nslots; ++s)
     if (cnt[s] == 0) {
@@ -101,11 +147,18 @@ LinLayout BuildLinLayout(const HostProblem& P) {
   for (size_t bi = 0; bi < P.batches.size(); ++bi) {
     const auto& B = P.batches[bi];
     LinLayout::BatchMap M;
-    M.nent = B.tdim * (B.tdim + 1) / 2 + B.tdim;
+    const int nh = B.tdim * (B.tdim + 1) / 2;
+    M.nent = nh + B.tdim;
+    M.merged_dims = merged_dims[bi];
     M.dest.resize(size_t(M.nent) * B.count);
     for (int f = 0; f < B.count; ++f)
       for (int e = 0; e < M.nent; ++e) {
-        const int64_t s = entry_slot(B, f, e, kslot[bi].data(), local[bi].data());
+        const size_t at = size_t(e) * B.count + f;
+        if (!contributes(bi, f, e, nh)) {
+          M.dest[at] = M.dest[at - (f & 31)];  // never read: the warp's first factor stores
+          continue;
+        }
+        const int64_t s = entry_slot(B, order[bi][f], e, kslot[bi].data(), local[bi].data());
         int64_t d;
         if (cnt[s] == 1) {
           d = s;
@@ -113,8 +166,9 @@ LinLayout BuildLinLayout(const HostProblem& P) {
           d = nslots + group_base[s] + seen[s];
           seen[s]++;
         }
-        M.dest[size_t(e) * B.count + f] = int32_t(d);
+        M.dest[at] = int32_t(d);
       }
+    M.order = std::move(order[bi]);
     L.maps.push_back(std::move(M));
   }
   // CSC export

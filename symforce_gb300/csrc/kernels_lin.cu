@@ -7,6 +7,13 @@
 // factor is the only contributor to that entry, otherwise into a staging slot that a second kernel
 // sums in a fixed order (no atomics, bit-reproducible).  Keys, constants and sink indices are
 // structure-of-arrays so that a warp's loads and stores of one entry are coalesced.
+//
+// Factors are in the layout's device order: for a kind with merged key slots (a reprojection
+// factor's camera) the factors of one camera are consecutive, and a warp whose 32 factors share
+// the camera adds the camera entries of its lanes with a shuffle reduce-scatter (lane l ends with
+// the warp's sum of entry l) and stores each sum once — the warp-shuffle reduction in place of
+// 32 staged contributions.
+#include "common.h"
 #include "factor_math.cuh"
 #include "kernels.h"
 
@@ -28,22 +35,66 @@ __device__ __forceinline__ void SinkStore(int32_t idx, T v, T* hess, T* rhs, T* 
   }
 }
 
+// Lane l returns the sum over the warp's lanes of v[l]: five exchange levels, each lane keeping the
+// half of its entries whose index bit matches its own lane bit and adding the partner's copy of
+// that half (31 shuffles and adds per lane for 32 entries; a fixed order of additions).
+template <typename T>
+__device__ __forceinline__ T ReduceScatter32(T (&v)[32], int lane) {
+#pragma unroll
+  for (int w = 16; w >= 1; w >>= 1) {
+    const bool upper = (lane & w) != 0;
+#pragma unroll
+    for (int j = 0; j < w; ++j) {
+      const T keep = upper ? v[j + w] : v[j];
+      const T send = upper ? v[j] : v[j + w];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, w);
+    }
+  }
+  return v[0];
+}
+
+template <typename Tr>
+__host__ __device__ constexpr int MergedDims() {
+  int d = 0;
+  for (int k = 0; k < Tr::MK; ++k) d += Tr::KT(k);
+  return d;
+}
+
 template <int KIND, typename T>
 __global__ void __launch_bounds__(kLinBlock) LinearizeKernel(LinOut o, BatchDev b) {
   using Tr = FactorTraits<KIND>;
   constexpr int TD = Tr::TD, RD = Tr::RD, NK = Tr::NK, NC = Tr::NC;
+  constexpr int NH = TD * (TD + 1) / 2;
+  constexpr int MT = MergedDims<Tr>();      // tangent columns of the merged key slots
+  constexpr int MH = MT * (MT + 1) / 2;     // their packed lower entries (a prefix of the packing)
+  constexpr int NM = MH + MT;               // merged entries: packed prefix and rhs prefix
   __shared__ double red[kLinBlock / 32];
   const int state = o.which == 0 ? o.st->init_idx : (o.which == 1 ? o.st->new_idx : o.which - 2);
   const double* vals = o.values + int64_t(state) * o.S;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool valid = f < b.count;
+  int key[NK];
+#pragma unroll
+  for (int k = 0; k < NK; ++k) key[k] = valid ? __ldg(b.keys + int64_t(k) * b.count + f) : -1;
+  bool merged = false;
+  if constexpr (Tr::MK > 0) {
+    // every lane takes part in every shuffle (no short-circuit around them)
+    bool same = valid;
+#pragma unroll
+    for (int k = 0; k < Tr::MK; ++k) {
+      const int first = __shfl_sync(0xffffffffu, key[k], 0);
+      same = same && key[k] == first;
+    }
+    merged = __all_sync(0xffffffffu, same);
+  }
   double err = 0.0;
-  if (f < b.count) {
+  if (valid) {
     double xs[NK][7];
     const double* xp[3];
 #pragma unroll
     for (int k = 0; k < NK; ++k) {
-      const int key = __ldg(b.keys + int64_t(k) * b.count + f);
-      const double* src = vals + __ldg(o.key_soff + key);
+      const double* src = vals + __ldg(o.key_soff + key[k]);
 #pragma unroll
       for (int i = 0; i < Tr::KS(k); ++i) xs[k][i] = src[i];
       xp[k] = xs[k];
@@ -64,25 +115,72 @@ __global__ void __launch_bounds__(kLinBlock) LinearizeKernel(LinOut o, BatchDev 
     T* rhs = static_cast<T*>(o.rhs) + int64_t(state) * o.N;
     T* stage = static_cast<T*>(o.stage);
     const int32_t* dest = b.dest + f;
+    // entries this factor stores itself: all of them, or those outside the merged prefix
     int e = 0;
 #pragma unroll
     for (int a = 0; a < TD; ++a) {
 #pragma unroll
       for (int q = 0; q <= a; ++q) {
-        T h = T(0);
+        if (a >= MT || !merged) {
+          T h = T(0);
 #pragma unroll
-        for (int i = 0; i < RD; ++i) h += J[i * TD + a] * J[i * TD + q];
-        SinkStore<T>(__ldg(dest + int64_t(e) * b.count), h, hess, rhs, stage, o.nvals, o.N);
+          for (int i = 0; i < RD; ++i) h += J[i * TD + a] * J[i * TD + q];
+          SinkStore<T>(__ldg(dest + int64_t(e) * b.count), h, hess, rhs, stage, o.nvals, o.N);
+        }
         ++e;
       }
     }
 #pragma unroll
     for (int a = 0; a < TD; ++a) {
-      T g = T(0);
+      if (a >= MT || !merged) {
+        T g = T(0);
 #pragma unroll
-      for (int i = 0; i < RD; ++i) g += J[i * TD + a] * T(r[i]);
-      SinkStore<T>(__ldg(dest + int64_t(e) * b.count), g, hess, rhs, stage, o.nvals, o.N);
+        for (int i = 0; i < RD; ++i) g += J[i * TD + a] * T(r[i]);
+        SinkStore<T>(__ldg(dest + int64_t(e) * b.count), g, hess, rhs, stage, o.nvals, o.N);
+      }
       ++e;
+    }
+    if constexpr (NM > 0) {
+      if (merged) {
+        // all 32 lanes are valid factors of one camera: 32 merged entries at a time
+        const int32_t* dest0 = b.dest + (f - lane);
+#pragma unroll
+        for (int ch = 0; ch < (NM + 31) / 32; ++ch) {
+          T v[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] = T(0);
+          int m = 0;
+#pragma unroll
+          for (int a = 0; a < MT; ++a) {
+#pragma unroll
+            for (int q = 0; q <= a; ++q) {
+              if (m >= 32 * ch && m < 32 * ch + 32) {
+                T h = T(0);
+#pragma unroll
+                for (int i = 0; i < RD; ++i) h += J[i * TD + a] * J[i * TD + q];
+                v[m - 32 * ch] = h;
+              }
+              ++m;
+            }
+          }
+#pragma unroll
+          for (int a = 0; a < MT; ++a) {
+            if (m >= 32 * ch && m < 32 * ch + 32) {
+              T g = T(0);
+#pragma unroll
+              for (int i = 0; i < RD; ++i) g += J[i * TD + a] * T(r[i]);
+              v[m - 32 * ch] = g;
+            }
+            ++m;
+          }
+          const T sum = ReduceScatter32<T>(v, lane);
+          const int mm = 32 * ch + lane;
+          if (mm < NM) {
+            const int em = mm < MH ? mm : NH + (mm - MH);
+            SinkStore<T>(__ldg(dest0 + int64_t(em) * b.count), sum, hess, rhs, stage, o.nvals, o.N);
+          }
+        }
+      }
     }
   }
   // deterministic block reduction of r^2: fixed shuffle tree, then warp 0
@@ -97,21 +195,18 @@ __global__ void __launch_bounds__(kLinBlock) LinearizeKernel(LinOut o, BatchDev 
   }
 }
 
-// One warp per shared destination: lanes stride over its staged contributions (a camera block
-// collects hundreds) and a fixed shuffle tree adds them, so the order is the same on every run.
+// One thread per shared destination adds its staged contributions in slot order (a point entry
+// has one per observation; a camera entry one per warp of its observations, plus the partial
+// warps at its ends), so the order is the same on every run.
 template <typename T>
 __global__ void ReduceStageKernel(ReduceDev r, LinOut o) {
-  const int g = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= r.ngroups) return;
   const int state = o.which == 0 ? o.st->init_idx : (o.which == 1 ? o.st->new_idx : o.which - 2);
   const T* stage = static_cast<const T*>(o.stage);
-  T acc = T(0);
-  const int64_t p1 = r.ptr[g + 1];
-  for (int64_t q = r.ptr[g] + lane; q < p1; q += 32) acc += stage[q];
-#pragma unroll
-  for (int d = 16; d > 0; d >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, d);
-  if (lane != 0) return;
+  const int64_t p0 = r.ptr[g], p1 = r.ptr[g + 1];
+  T acc = stage[p0];
+  for (int64_t q = p0 + 1; q < p1; ++q) acc += stage[q];
   const int32_t d = r.dst[g];
   if (d < o.nvals) {
     static_cast<T*>(o.hess)[int64_t(state) * o.nvals + d] = acc;
@@ -133,6 +228,11 @@ __global__ void FinishCostKernel(const double* partials, int n, LmState* st, int
 }
 
 }  // namespace
+
+static_assert(FactorTraits<SFG_FACTOR_SNAVELY_REPROJECTION>::MK ==
+                  MergedKeySlots(SFG_FACTOR_SNAVELY_REPROJECTION),
+              "merged key slots of the kernel and of the host layout differ");
+static_assert(kLinBlock % 32 == 0, "merged warps are aligned to the factor index");
 
 int LinearizeBlockSize() { return kLinBlock; }
 
@@ -165,8 +265,8 @@ void LaunchLinearize(int kind, const LinOut& out, const BatchDev& b, cudaStream_
 template <typename T>
 void LaunchReduceStage(const ReduceDev& r, const LinOut& out, cudaStream_t s) {
   if (r.ngroups == 0) return;
-  const int warps = 8;
-  ReduceStageKernel<T><<<(r.ngroups + warps - 1) / warps, 32 * warps, 0, s>>>(r, out);
+  const int threads = 128;
+  ReduceStageKernel<T><<<(r.ngroups + threads - 1) / threads, threads, 0, s>>>(r, out);
 }
 
 void LaunchFinishCost(const double* partials, int npartials, LmState* st, int which,

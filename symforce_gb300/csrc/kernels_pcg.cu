@@ -365,11 +365,18 @@ __device__ __forceinline__ void GridReduce(Acc a, Acc b, const PcgDev& d, int& s
   if (grid > 1) {
     GridBarrier(d.bar, grid, d.err);
     if (warp == 0) {
+      // four partials per lane in flight at once, added in CTA order
       double ta = 0.0, tb = 0.0;
-      for (int q = lane; q < grid; q += 32) {
-        const double2 v = __ldcg(part + q);
-        ta += v.x;
-        tb += v.y;
+      for (int q0 = lane; q0 < grid; q0 += 128) {
+        double2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          v[u] = q0 + 32 * u < grid ? __ldcg(part + q0 + 32 * u) : make_double2(0.0, 0.0);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          ta += v[u].x;
+          tb += v[u].y;
+        }
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {

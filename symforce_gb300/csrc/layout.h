@@ -14,7 +14,9 @@ struct LinLayout {
   std::vector<int64_t> diag_off;   // [N] value offset of each diagonal scalar
   struct BatchMap {
     int nent = 0;                  // packed H entries + rhs entries per factor
-    std::vector<int32_t> dest;     // [nent][count] sink index
+    int merged_dims = 0;           // tangent dims of the merged key slots (0: no warp merging)
+    std::vector<int32_t> dest;     // [nent][count] sink index, device order
+    std::vector<int32_t> order;    // [count] device factor -> the user's factor index
   };
   std::vector<BatchMap> maps;
   int64_t nvals = 0, N = 0, nstage = 0;
