@@ -269,7 +269,7 @@ struct PcgDev {
   int staged;               // one CTA holding blocks, entries, z and y in shared memory: its
                             // dynamic shared memory bytes (0: blocks read from L2)
   double* partials;         // [2][grid][2] per-CTA partial sums (double buffered)
-  unsigned* bar;            // [2] grid barrier count / generation
+  unsigned* bar;            // [2] grid barrier arrival count (zeroed before each launch)
   PcgState* ps;
   int* err;                 // device error word
   double tol;               // FP64 relative residual target

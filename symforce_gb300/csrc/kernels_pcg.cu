@@ -10,8 +10,10 @@
 //    P_g is a warp-shuffle product and every thread keeps its row of P_g in registers.  Dot
 //    products are reduced in FP64 in a fixed order (warp tree, CTA order, then the same fixed
 //    order over CTAs in every CTA), so every CTA takes the same branch and runs are reproducible.
-//    Multi-CTA solves use a grid barrier (cooperative launch: all CTAs resident) whose waits are
-//    capped; a cap hit sets the device error word.
+//    Multi-CTA solves use a grid barrier (cooperative launch: all CTAs resident) on one arrival
+//    counter that only grows within a launch (zeroed before it), so a CTA waits for the counter to
+//    reach its barrier's count and nobody has to release the others; the waits are capped and a
+//    cap hit sets the device error word.
 //  (The network's inference pass runs on the tensor cores: kernels_tc.cu.)
 #include <cuda_runtime.h>
 
@@ -216,26 +218,22 @@ __global__ void CollectSamplesKernel(PrecondDev pd, const float* feats, const fl
 // ---------------------------------------------------------------------------------------------
 // PCG
 // ---------------------------------------------------------------------------------------------
-__device__ void GridBarrier(unsigned* bar, unsigned nblocks, int* err) {
+// Barrier number `epoch` (1, 2, ... within the launch; kept by thread 0 of each CTA): arrive on
+// the counter, then wait until all nblocks CTAs have arrived epoch times.
+__device__ void GridBarrier(unsigned* bar, unsigned nblocks, unsigned& epoch, int* err) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned* vgen = bar + 1;
-    const unsigned gen = *vgen;
+    const unsigned target = ++epoch * nblocks;
     __threadfence();
-    if (atomicAdd(bar, 1u) == nblocks - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      unsigned it = 0;
-      while (*vgen == gen) {
-        if (*reinterpret_cast<volatile int*>(err) != 0) break;
-        if (++it > kSpinLimit) {
-          atomicExch(err, kDevSpinTimeout);
-          break;
-        }
-        if (it > 32) __nanosleep(32);
+    atomicAdd(bar, 1u);
+    volatile unsigned* count = bar;
+    unsigned it = 0;
+    while (*count < target) {
+      if (++it > kSpinLimit) {
+        atomicExch(err, kDevSpinTimeout);
+        break;
       }
+      if ((it & 63) == 0 && *reinterpret_cast<volatile int*>(err) != 0) break;
     }
     __threadfence();
   }
@@ -325,6 +323,7 @@ struct PcgShared {
   double vnorm, target, rel;
   double rz, alpha, beta;
   int iters, stop, broke, converged;
+  unsigned epoch;  // grid barriers passed (thread 0 only)
 };
 
 // Sum (a, b) over the grid: a warp tree in Acc, the CTA's warps in order (warp 0, Acc), and the CTAs
@@ -363,7 +362,7 @@ __device__ __forceinline__ void GridReduce(Acc a, Acc b, const PcgDev& d, int& s
     }
   }
   if (grid > 1) {
-    GridBarrier(d.bar, grid, d.err);
+    GridBarrier(d.bar, grid, sm.epoch, d.err);
     if (warp == 0) {
       // four partials per lane in flight at once, added in CTA order
       double ta = 0.0, tb = 0.0;
@@ -444,6 +443,7 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
     ygv = d.yg;
   }
   if (threadIdx.x == 0) {
+    sm.epoch = 0;
     sm.iters = 0;
     sm.converged = 0;
     sm.broke = 0;
@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
     }
     y64 += double(dx);
     if (store) StX<kStaged>(ygv + gi, y64);
-    if (gridDim.x > 1) GridBarrier(d.bar, gridDim.x, d.err);
+    if (gridDim.x > 1) GridBarrier(d.bar, gridDim.x, sm.epoch, d.err);
     else __syncthreads();
   }
   if (own) __stcg(d.y + s, y64);

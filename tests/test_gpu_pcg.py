@@ -139,6 +139,30 @@ def test_learned_form_reaches_oracle_cost_on_benchmark_workload():
             assert ps["fallbacks"] < ps["solves"], ps
 
 
+@pytest.mark.parametrize("precision", [A.SFG_PRECISION_FP64, A.SFG_PRECISION_MIXED])
+def test_multi_cta_pcg_reaches_plain_cost(precision):
+    """300 camera blocks (100 warps): the PCG solve runs as a cooperative multi-CTA launch with grid
+    barriers and grid reductions.  It reaches the plain FP64 form's cost (itself pinned to the
+    oracle by the optimizer tests)."""
+    p = synth.bundle_adjustment(num_cameras=300, num_points=6000, num_observations=30000, seed=11)
+    params = A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC, iterations=30,
+                                        early_exit_min_reduction=1e-9)
+    plain = Optimizer(p, params, A.default_form_params(linear_solver=A.SFG_LINEAR_SOLVER_SCHUR))
+    _, plain_stats = plain.optimize(p.values)
+    ref = min(r.best_error for r in plain_stats.iterations)
+    opt = Optimizer(p, params, A.default_form_params(precision=precision,
+                                                    linear_solver=A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI))
+    _, stats = opt.optimize(p.values)
+    best = min(r.best_error for r in stats.iterations)
+    assert abs(best - ref) <= 1e-6 * ref, (best, ref)
+    ps = opt.pcg_stats()
+    assert ps["solves"] == len(stats.iterations) - 1, ps
+    if precision == A.SFG_PRECISION_FP64:
+        assert ps["fallbacks"] == 0 and ps["max_rel_residual"] <= 1e-8, ps
+    else:
+        assert ps["fallbacks"] < ps["solves"], ps
+
+
 def test_fallback_runs_exact_factorization():
     """An iteration cap of 2 makes every PCG solve miss 1e-8: the exact LDL^T takes over and the
     optimizer still reaches the oracle's cost."""
