@@ -217,7 +217,7 @@ void EnqueueSolve(const FactorPlan& fp, const void* b, void* x, cudaStream_t s, 
   FactorDev f = fp.f;
   f.gate = gate;
   if (fixed_b) f.b_stride = 0;
-  LaunchSolve<T>(f, fp.F, b, fp.ycon, fp.ysave, fp.xperm, x, fp.grid_solve, s);
+  LaunchSolve<T>(f, fp.F, fp.Linv, b, fp.ycon, fp.ysave, fp.xperm, x, fp.grid_solve, s);
 }
 
 template void EnqueueFactor<double>(const FactorPlan&, const void*, const double*, cudaStream_t,

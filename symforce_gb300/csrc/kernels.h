@@ -200,10 +200,11 @@ struct FactorDev {
 template <typename T>
 void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F, void* Linv,
                   int grid, cudaStream_t s);
-// Solve (L D L^T) x = b for b in the original scalar order; x in the original order.
+// Solve (L D L^T) x = b for b in the original scalar order; x in the original order.  Linv: the
+// inverses of the pivot tiles' unit lower factors that LaunchFactor wrote.
 template <typename T>
-void LaunchSolve(const FactorDev& f, const void* F, const void* b, void* ycon, void* ysave,
-                 void* xperm, void* x, int grid, cudaStream_t s);
+void LaunchSolve(const FactorDev& f, const void* F, const void* Linv, const void* b, void* ycon,
+                 void* ysave, void* xperm, void* x, int grid, cudaStream_t s);
 int FactorThreads();
 // One CTA waits (capped) for *flag >= 1 while nothing sets it; the cap sets *err.
 cudaError_t LaunchWaitCapSelfTest(const int* flag, int* err, cudaStream_t s);

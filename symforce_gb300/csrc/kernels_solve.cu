@@ -748,14 +748,16 @@ __global__ void __launch_bounds__(kFactorThreads, kFactorCtasPerSm) FactorKernel
 // ---------------------------------------------------------------------------------------------
 // Triangular solves: task t < ns is the forward solve of front t (postorder), task ns + q the
 // backward solve of front ns - 1 - q (reverse postorder).  Dynamic shared memory: max_m scalars.
-// The pivot columns are processed in panels of kSolvePanel: warp 0 solves the panel's triangle
-// from registers, then every thread updates its rows with the whole panel (independent loads), so
-// a front costs one synchronization per panel rather than one per column.
+// The pivot columns go in the factorization's pivot tiles.  A tile's triangle is solved with the
+// inverse of its unit lower factor that the factorization kept (a product whose rows are
+// independent: four-chain dot products instead of a chain of TILE dependent multiply-adds), by
+// warp 0, which also updated the tile's rows in the step before (so a warp barrier orders them);
+// then every thread updates its rows with the tile (independent loads).  One CTA barrier per tile.
+// Warp 0 loads the next tile's inverse row while the current tile's update runs.
 // ---------------------------------------------------------------------------------------------
-constexpr int kSolvePanel = 32;
-// Threads of a solve task: the rows below a panel are updated one row per thread, each row a chain
-// of kSolvePanel dependent multiply-adds after one round of L2 loads, so more threads shorten the
-// panel step of a wide front (256: a 450-wide front needs at most two rows per thread).
+// Threads of a solve task: the rows below a tile are updated one row per thread, each row a few
+// dependent multiply-add chains after one round of L2 loads, so more threads shorten the step of a
+// wide front (256: a 450-wide front needs at most two rows per thread).
 constexpr int kSolveThreads = 256;
 
 // sum_{c = c0}^{c1 - 1} a[c * stride] x[c] with four independent accumulation chains (a dependent
@@ -774,62 +776,135 @@ __device__ __forceinline__ T RowDot(const T* a, int64_t stride, const T* x, int 
   return (s0 + s1) + (s2 + s3);
 }
 
-template <typename T>
-__device__ void ForwardFront(const FactorDev& f, const Geom& g, const T* Fs, T* xs) {
-  const int m = g.m;
-  const int lane = threadIdx.x & 31;
-  for (int p0 = 0; p0 < g.w; p0 += kSolvePanel) {
-    const int p1 = min(p0 + kSolvePanel, g.w);
-    if (threadIdx.x < 32) {
-      const int r = p0 + lane;
-      T lrow[kSolvePanel];
+// sum_{c < n} v[c] x[c] over a register row, four chains, fixed order (x is read below n only)
+template <typename T, int TILE>
+__device__ __forceinline__ T RegDot(const T (&v)[TILE], const T* x, int n) {
+  T s[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
-      for (int c = 0; c < kSolvePanel; ++c)
-        lrow[c] = (r < p1 && p0 + c < r) ? Ld(Fs + r + int64_t(p0 + c) * m) : T(0);
-      T xr = r < p1 ? xs[r] : T(0);
+  for (int c = 0; c < TILE; ++c)
+    if (c < n) s[c & 3] += v[c] * x[c];
+  return (s[0] + s[1]) + (s[2] + s[3]);
+}
+
+// Row `lane` of the inverse of pivot tile k (forward: row of L^-1, entries c <= lane) or column
+// `lane` (backward: row of L^-T, entries c >= lane); zeros outside the tile's b rows.  The inverse
+// is stored with (r, c) at c * TILE + r.
+template <typename T, int TILE, bool kTransposed>
+__device__ __forceinline__ void LoadInvRow(const T* Li, int k, int b, int lane, T (&v)[TILE]) {
+  const T* L = Li + int64_t(k) * TILE * TILE;
 #pragma unroll
-      for (int c = 0; c < kSolvePanel; ++c) {
-        const T xc = __shfl_sync(0xffffffffu, xr, c);
-        if (p0 + c < r) xr -= lrow[c] * xc;
-      }
-      if (r < p1) xs[r] = xr;
-    }
-    __syncthreads();
-    for (int r = p1 + threadIdx.x; r < m; r += blockDim.x) xs[r] -= RowDot(Fs + r, int64_t(m), xs, p0, p1);
-    __syncthreads();
+  for (int c = 0; c < TILE; ++c) {
+    const bool in = lane < b && c < b && (kTransposed ? c >= lane : c <= lane);
+    v[c] = in ? Ld(kTransposed ? L + lane * TILE + c : L + c * TILE + lane) : T(0);
   }
 }
 
-template <typename T>
-__device__ void BackwardFront(const FactorDev& f, const Geom& g, const T* Fs, T* xs) {
-  const int m = g.m;
-  const int lane = threadIdx.x & 31;
-  const int npan = (g.w + kSolvePanel - 1) / kSolvePanel;
-  for (int pp = npan - 1; pp >= 0; --pp) {
-    const int p0 = pp * kSolvePanel, p1 = min(p0 + kSolvePanel, g.w);
-    if (threadIdx.x < 32) {
-      const int r = p0 + lane;  // row of L^T = column of L
-      T lcol[kSolvePanel];      // L[c][r] for c in (r, p1)
+// Pivot tiles go in steps of SUP = 32 / TILE tiles (two FP64 tiles of 16, one FP32 tile of 32), one
+// per TILE lanes of warp 0, so that a step spans 32 columns.  Within a step, the lanes of a later
+// tile first subtract the earlier tile's contribution (its rows of L, loaded ahead like the inverse
+// rows), then apply their tile's inverse.
+template <typename T, int TILE>
+__device__ void ForwardFront(const Geom& g, const T* Fs, const T* Li, T* xs) {
+  constexpr int SUP = 32 / TILE;
+  static_assert(SUP * TILE == 32 && SUP <= 2, "a step is warp 0: one or two pivot tiles");
+  const int m = g.m, t = threadIdx.x;
+  const int grp = (t & 31) / TILE, lr = (t & 31) % TILE;
+  T inv[TILE], lft[TILE];
+  // inverse row of tile k0 + grp; for the second tile, its row lr against the first tile's columns
+  auto prefetch = [&](int k0) {
+    const int k = k0 + grp, pk = k * TILE;
+    const int b = k < g.np ? min(TILE, g.w - pk) : 0;
+    LoadInvRow<T, TILE, false>(Li, k < g.np ? k : 0, b, lr, inv);
 #pragma unroll
-      for (int c = 0; c < kSolvePanel; ++c)
-        lcol[c] = (r < p1 && p0 + c > r && p0 + c < p1) ? Ld(Fs + (p0 + c) + int64_t(r) * m) : T(0);
-      T xr = r < p1 ? xs[r] : T(0);
+    for (int c = 0; c < TILE; ++c)
+      lft[c] = (grp > 0 && lr < b) ? Ld(Fs + (pk + lr) + int64_t(k0 * TILE + c) * m) : T(0);
+  };
+  if (t < 32) prefetch(0);
+  for (int k0 = 0; k0 < g.np; k0 += SUP) {
+    const int p0 = k0 * TILE, p2 = min(p0 + SUP * TILE, g.w);
+    if (t < 32) {
+      // the step's rows were last updated by warp 0 (or before the caller's CTA barrier)
+      __syncwarp();
 #pragma unroll
-      for (int c = kSolvePanel - 1; c >= 0; --c) {
-        const T xc = __shfl_sync(0xffffffffu, xr, c);
-        if (p0 + c > r) xr -= lcol[c] * xc;
+      for (int j = 0; j < SUP; ++j) {
+        const int pj = p0 + j * TILE, bj = min(TILE, p2 - pj);  // bj <= 0: no such tile
+        T y = T(0);
+        if (j > 0) {
+          if (grp == j && lr < bj) xs[pj + lr] -= RegDot<T, TILE>(lft, xs + p0, TILE);
+          __syncwarp();
+        }
+        if (grp == j && lr < bj) y = RegDot<T, TILE>(inv, xs + pj, bj);
+        __syncwarp();
+        if (grp == j && lr < bj) xs[pj + lr] = y;
+        __syncwarp();
       }
-      if (r < p1) xs[r] = xr;
+      if (k0 + SUP < g.np) prefetch(k0 + SUP);
     }
     __syncthreads();
-    for (int r = threadIdx.x; r < p0; r += blockDim.x) xs[r] -= RowDot(Fs + int64_t(r) * m, int64_t(1), xs, p0, p1);
-    __syncthreads();
+    // thread i updates rows p2 + i, p2 + i + blockDim, ...: the next step's rows fall to warp 0
+    for (int r = p2 + t; r < m; r += blockDim.x) xs[r] -= RowDot(Fs + r, int64_t(m), xs, p0, p2);
   }
+  __syncthreads();
+}
+
+template <typename T, int TILE>
+__device__ void BackwardFront(const Geom& g, const T* Fs, const T* Li, T* xs) {
+  constexpr int SUP = 32 / TILE;
+  const int m = g.m, t = threadIdx.x;
+  const int grp = (t & 31) / TILE, lr = (t & 31) % TILE;
+  T inv[TILE], lft[TILE];
+  // row lr of the inverse transposed of tile k0 + grp; for the first tile of a two-tile step, its
+  // column lr of L against the second tile's rows (the entries of L^T row lr)
+  auto prefetch = [&](int k0) {
+    const int k = k0 + grp, pk = k * TILE;
+    const int b = k < g.np ? min(TILE, g.w - pk) : 0;
+    LoadInvRow<T, TILE, true>(Li, k < g.np ? k : 0, b, lr, inv);
+    const int k1 = k0 + 1, b1 = k1 < g.np ? min(TILE, g.w - k1 * TILE) : 0;
+#pragma unroll
+    for (int c = 0; c < TILE; ++c)
+      lft[c] = (SUP > 1 && grp == 0 && lr < b && c < b1) ? Ld(Fs + (k1 * TILE + c) + int64_t(pk + lr) * m)
+                                                          : T(0);
+  };
+  const int last = g.np > 0 ? ((g.np - 1) / SUP) * SUP : 0;
+  if (t < 32 && g.np > 0) prefetch(last);
+  for (int k0 = last; k0 >= 0 && g.np > 0; k0 -= SUP) {
+    const int p0 = k0 * TILE, p2 = min(p0 + SUP * TILE, g.w);
+    if (t < 32) {
+      __syncwarp();
+#pragma unroll
+      for (int jj = SUP - 1; jj >= 0; --jj) {
+        const int pj = p0 + jj * TILE, bj = min(TILE, p2 - pj);
+        if (bj > 0) {
+          T y = T(0);
+          if (jj < SUP - 1) {
+            const int pn = pj + TILE;  // the later tile of the step, solved just before
+            if (grp == jj && lr < bj) xs[pj + lr] -= RegDot<T, TILE>(lft, xs + pn, p2 - pn);
+            __syncwarp();
+          }
+          if (grp == jj && lr < bj) y = RegDot<T, TILE>(inv, xs + pj, bj);
+          __syncwarp();
+          if (grp == jj && lr < bj) xs[pj + lr] = y;
+          __syncwarp();
+        }
+      }
+      if (k0 - SUP >= 0) prefetch(k0 - SUP);
+    }
+    __syncthreads();
+    // thread i updates rows p0 - 1 - i, ...: the previous step's rows fall to warp 0
+    for (int i = t; i < p0; i += blockDim.x) {
+      const int r = p0 - 1 - i;
+      xs[r] -= RowDot(Fs + int64_t(r) * m, int64_t(1), xs, p0, p2);
+    }
+  }
+  __syncthreads();
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kSolveThreads) SolveKernel(FactorDev f, const T* F, const T* b,
-                                                              T* ycon, T* ysave, T* xperm, T* x) {
+__global__ void __launch_bounds__(kSolveThreads) SolveKernel(FactorDev f, const T* F, const T* Linv,
+                                                              const T* b, T* ycon, T* ysave, T* xperm,
+                                                              T* x) {
+  constexpr int kTile = sizeof(T) == 8 ? kFactorTileF64 : kFactorTileF32;
+  static_assert(kTile <= 32 && kSolveThreads >= 32, "warp 0 holds a tile's rows");
   extern __shared__ unsigned char smem_raw[];
   T* xs = reinterpret_cast<T*>(smem_raw);
   __shared__ int s_task, s_ok, s_flag;
@@ -865,7 +940,7 @@ __global__ void __launch_bounds__(kSolveThreads) SolveKernel(FactorDev f, const 
           for (int r = threadIdx.x; r < hc; r += blockDim.x) xs[rel[r]] += Ld(ycon + f.rel_off[c] + r);
           __syncthreads();
         }
-        ForwardFront<T>(f, g, Fs, xs);
+        ForwardFront<T, kTile>(g, Fs, Linv + f.linv_base[s], xs);
         for (int q = threadIdx.x; q < g.w; q += blockDim.x) St(ysave + f.idx_off[s] + q, xs[q]);
         for (int r = threadIdx.x; r < g.m - g.w; r += blockDim.x) St(ycon + f.rel_off[s] + r, xs[g.w + r]);
         Signal(fwd_done + s, 1);
@@ -890,7 +965,7 @@ __global__ void __launch_bounds__(kSolveThreads) SolveKernel(FactorDev f, const 
           xs[q] = z - RowDot(Fs + int64_t(q) * g.m + g.w, int64_t(1), xa, 0, h);
         }
         __syncthreads();
-        BackwardFront<T>(f, g, Fs, xs);
+        BackwardFront<T, kTile>(g, Fs, Linv + f.linv_base[s], xs);
         for (int q = threadIdx.x; q < g.w; q += blockDim.x) {
           St(xperm + idx[q], xs[q]);
           x[f.scalar_old[idx[q]]] = xs[q];
@@ -1092,13 +1167,13 @@ void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void
 }
 
 template <typename T>
-void LaunchSolve(const FactorDev& f, const void* F, const void* b, void* ycon, void* ysave,
-                 void* xperm, void* x, int grid, cudaStream_t s) {
+void LaunchSolve(const FactorDev& f, const void* F, const void* Linv, const void* b, void* ycon,
+                 void* ysave, void* xperm, void* x, int grid, cudaStream_t s) {
   // dynamic shared memory: the largest front's scalars
   const size_t smem = size_t(f.max_m) * sizeof(T);
   SolveKernel<T><<<grid, kSolveThreads, smem, s>>>(
-      f, static_cast<const T*>(F), static_cast<const T*>(b), static_cast<T*>(ycon),
-      static_cast<T*>(ysave), static_cast<T*>(xperm), static_cast<T*>(x));
+      f, static_cast<const T*>(F), static_cast<const T*>(Linv), static_cast<const T*>(b),
+      static_cast<T*>(ycon), static_cast<T*>(ysave), static_cast<T*>(xperm), static_cast<T*>(x));
 }
 
 template void LaunchSchurPoints<double>(const SchurDev&, const void*, const void*, int64_t, int64_t,
@@ -1121,9 +1196,9 @@ template void LaunchFactor<double>(const FactorDev&, const void*, const double*,
                                    cudaStream_t);
 template void LaunchFactor<float>(const FactorDev&, const void*, const double*, void*, void*, int,
                                   cudaStream_t);
-template void LaunchSolve<double>(const FactorDev&, const void*, const void*, void*, void*, void*,
-                                  void*, int, cudaStream_t);
-template void LaunchSolve<float>(const FactorDev&, const void*, const void*, void*, void*, void*,
-                                 void*, int, cudaStream_t);
+template void LaunchSolve<double>(const FactorDev&, const void*, const void*, const void*, void*, void*,
+                                  void*, void*, int, cudaStream_t);
+template void LaunchSolve<float>(const FactorDev&, const void*, const void*, const void*, void*, void*,
+                                 void*, void*, int, cudaStream_t);
 
 }  // namespace sfg
