@@ -76,24 +76,30 @@ LinLayout BuildLinLayout(const HostProblem& P) {
     const bool merged_entry = e < nh ? e < mt * (mt + 1) / 2 : e - nh < mt;
     return !merged_entry;
   };
-  // slot (H value index or nvals + tangent index) of every factor entry; f is the user's index
-  auto entry_slot = [&](const HostBatch& B, int f, int e, int* kslot_of, int* local_of) -> int64_t {
-    const int td = B.tdim;
-    const int nh = td * (td + 1) / 2;
-    const int32_t* keys = &B.keys[size_t(f) * B.nk];
-    if (e >= nh) {
-      const int a = e - nh;
-      return L.nvals + P.toff[keys[kslot_of[a]]] + local_of[a];
-    }
-    // packed lower index e -> (a, b), a >= b
-    int a = 0;
-    while ((a + 1) * (a + 2) / 2 <= e) ++a;
-    const int b = e - a * (a + 1) / 2;
-    const int ka = keys[kslot_of[a]], kb = keys[kslot_of[b]];
-    const int ra = local_of[a], rb = local_of[b];
-    if (ka == kb) return L.H.boff[L.H.Find(ka, ka)] + int64_t(ra) * P.tdim[ka] + rb;
-    if (ka > kb) return L.H.boff[L.H.Find(ka, kb)] + int64_t(ra) * P.tdim[kb] + rb;
-    return L.H.boff[L.H.Find(kb, ka)] + int64_t(rb) * P.tdim[ka] + ra;
+  // Slots (H value index or nvals + tangent index) of all entries of the user's factor f: the
+  // factor's key blocks are looked up once, each entry adds its offset inside the block.
+  auto factor_slots = [&](const HostBatch& B, int f, const int* kslot_of, const int* local_of,
+                          int64_t* out) {
+    const int td = B.tdim, nk = B.nk;
+    const int32_t* keys = &B.keys[size_t(f) * nk];
+    int64_t bo[3][3];
+    bool swapped[3][3];
+    for (int sa = 0; sa < nk; ++sa)
+      for (int sb = 0; sb <= sa; ++sb) {
+        const int ka = keys[sa], kb = keys[sb];
+        swapped[sa][sb] = ka < kb;
+        bo[sa][sb] = L.H.boff[ka >= kb ? L.H.Find(ka, kb) : L.H.Find(kb, ka)];
+      }
+    int e = 0;
+    for (int a = 0; a < td; ++a)
+      for (int b = 0; b <= a; ++b, ++e) {
+        const int sa = kslot_of[a], sb = kslot_of[b];
+        const int ra = local_of[a], rb = local_of[b];
+        if (sa == sb) out[e] = bo[sa][sa] + int64_t(ra) * P.tdim[keys[sa]] + rb;
+        else if (!swapped[sa][sb]) out[e] = bo[sa][sb] + int64_t(ra) * P.tdim[keys[sb]] + rb;
+        else out[e] = bo[sa][sb] + int64_t(rb) * P.tdim[keys[sa]] + ra;
+      }
+    for (int a = 0; a < td; ++a, ++e) out[e] = L.nvals + P.toff[keys[kslot_of[a]]] + local_of[a];
   };
   const int64_t nslots = L.nvals + P.N;
   std::vector<int32_t> cnt(nslots, 0);
@@ -110,9 +116,12 @@ LinLayout BuildLinLayout(const HostProblem& P) {
     const auto& B = P.batches[bi];
     const int nh = B.tdim * (B.tdim + 1) / 2;
     const int nent = nh + B.tdim;
-    for (int f = 0; f < B.count; ++f)
+    std::vector<int64_t> slots(nent);
+    for (int f = 0; f < B.count; ++f) {
+      factor_slots(B, order[bi][f], kslot[bi].data(), local[bi].data(), slots.data());
       for (int e = 0; e < nent; ++e)
-        if (contributes(bi, f, e, nh)) cnt[entry_slot(B, order[bi][f], e, kslot[bi].data(), local[bi].data())]++;
+        if (contributes(bi, f, e, nh)) cnt[slots[e]]++;
+    }
   }
   for (int64_t s = 0; s < nslots; ++s)
     if (cnt[s] == 0) {
@@ -151,28 +160,49 @@ LinLayout BuildLinLayout(const HostProblem& P) {
     M.nent = nh + B.tdim;
     M.merged_dims = merged_dims[bi];
     M.dest.resize(size_t(M.nent) * B.count);
-    for (int f = 0; f < B.count; ++f)
-      for (int e = 0; e < M.nent; ++e) {
-        const size_t at = size_t(e) * B.count + f;
-        if (!contributes(bi, f, e, nh)) {
-          M.dest[at] = M.dest[at - (f & 31)];  // never read: the warp's first factor stores
-          continue;
+    // factors in runs of 32 (a warp): sink indices in factor order, then written entry-major
+    constexpr int kRun = 32;
+    std::vector<int64_t> slots(M.nent);
+    std::vector<int32_t> run(size_t(kRun) * M.nent);
+    for (int f0 = 0; f0 < B.count; f0 += kRun) {
+      const int nf = std::min(kRun, B.count - f0);
+      for (int j = 0; j < nf; ++j) {
+        const int f = f0 + j;
+        factor_slots(B, order[bi][f], kslot[bi].data(), local[bi].data(), slots.data());
+        for (int e = 0; e < M.nent; ++e) {
+          int32_t& out = run[size_t(e) * kRun + j];
+          if (!contributes(bi, f, e, nh)) {
+            out = run[size_t(e) * kRun];  // never read: the warp's first factor stores
+            continue;
+          }
+          const int64_t s = slots[e];
+          if (cnt[s] == 1) {
+            out = int32_t(s);
+          } else {
+            out = int32_t(nslots + group_base[s] + seen[s]);
+            seen[s]++;
+          }
         }
-        const int64_t s = entry_slot(B, order[bi][f], e, kslot[bi].data(), local[bi].data());
-        int64_t d;
-        if (cnt[s] == 1) {
-          d = s;
-        } else {
-          d = nslots + group_base[s] + seen[s];
-          seen[s]++;
-        }
-        M.dest[at] = int32_t(d);
       }
+      for (int e = 0; e < M.nent; ++e)
+        std::copy(run.begin() + size_t(e) * kRun, run.begin() + size_t(e) * kRun + nf,
+                  M.dest.begin() + size_t(e) * B.count + f0);
+    }
     M.order = std::move(order[bi]);
     L.maps.push_back(std::move(M));
   }
   // CSC export
   L.csc_colptr.assign(P.N + 1, 0);
+  {
+    int64_t nnz = 0;
+    for (int kc = 0; kc < P.nkeys; ++kc)
+      for (int64_t q = L.H.colptr[kc]; q < L.H.colptr[kc + 1]; ++q) {
+        const int64_t dr = P.tdim[L.H.rows[q]], dc = P.tdim[kc];
+        nnz += L.H.rows[q] == kc ? dc * (dc + 1) / 2 : dr * dc;
+      }
+    L.csc_rowidx.reserve(size_t(nnz));
+    L.csc_src.reserve(size_t(nnz));
+  }
   for (int kc = 0; kc < P.nkeys; ++kc)
     for (int cc = 0; cc < P.tdim[kc]; ++cc) {
       const int64_t col = P.toff[kc] + cc;
@@ -223,36 +253,77 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L) {
     }
     S.pt_eptr.push_back(int64_t(S.pt_eoff.size()));
   }
-  // reduced pattern
+  // points of every B key, in point order, with the offset of the point's E block for the key
+  std::vector<int64_t> kp_ptr(size_t(S.nB_keys) + 1, 0);
+  for (int p = 0; p < S.npoints; ++p)
+    for (const auto& e : pe[p]) kp_ptr[size_t(e.first) + 1]++;
+  for (int k = 0; k < S.nB_keys; ++k) kp_ptr[k + 1] += kp_ptr[k];
+  std::vector<int32_t> kp(static_cast<size_t>(kp_ptr[S.nB_keys]));
+  std::vector<int64_t> kp_eoff(kp.size());
+  {
+    std::vector<int64_t> fill(kp_ptr.begin(), kp_ptr.end() - 1);
+    for (int p = 0; p < S.npoints; ++p)
+      for (const auto& e : pe[p]) {
+        const int64_t q = fill[e.first]++;
+        kp[q] = p;
+        kp_eoff[q] = e.second;
+      }
+  }
+  // reduced pattern: the B-B blocks of H and every pair of B keys that share a point, found per
+  // column key through its points (a stamp per row key keeps each pair once)
   std::vector<std::pair<int, int>> pairs;
   for (int j = 0; j < S.nB_keys; ++j)
     for (int64_t q = L.H.colptr[j]; q < L.H.colptr[j + 1]; ++q)
       if (L.H.rows[q] < S.nB_keys) pairs.push_back({L.H.rows[q], j});
-  for (int p = 0; p < S.npoints; ++p)
-    for (size_t a = 0; a < pe[p].size(); ++a)
-      for (size_t b = 0; b <= a; ++b) pairs.push_back({pe[p][a].first, pe[p][b].first});
+  {
+    std::vector<int> stamp(size_t(S.nB_keys), -1);
+    for (int kb = 0; kb < S.nB_keys; ++kb)
+      for (int64_t q = kp_ptr[kb]; q < kp_ptr[kb + 1]; ++q)
+        for (const auto& e : pe[kp[q]])
+          if (e.first >= kb && stamp[e.first] != kb) {
+            stamp[e.first] = kb;
+            pairs.push_back({e.first, kb});
+          }
+  }
   std::vector<int> bdims(P.tdim.begin(), P.tdim.begin() + S.nB_keys);
   S.Spat = MakePattern(bdims, pairs);
   const int64_t nsb = S.Spat.nblocks();
-  std::vector<std::vector<std::pair<int64_t, int64_t>>> terms(nsb);
-  for (int p = 0; p < S.npoints; ++p) {
-    const int64_t e0 = S.pt_eptr[p];
-    for (size_t a = 0; a < pe[p].size(); ++a)
-      for (size_t b = 0; b <= a; ++b) {
-        // pe sorted ascending: a >= b => key_a >= key_b
-        const int64_t blk = S.Spat.Find(pe[p][a].first, pe[p][b].first);
-        terms[blk].push_back({S.pt_eoff[e0 + a], S.pt_woff[e0 + b]});
-      }
+  // terms of every S block in point order (a counting sort by block over the terms in the order
+  // points and their E pairs are visited)
+  int64_t nterms = 0;
+  for (int p = 0; p < S.npoints; ++p) nterms += int64_t(pe[p].size()) * (pe[p].size() + 1) / 2;
+  std::vector<int32_t> tblk(static_cast<size_t>(nterms));
+  S.sb_ptr.assign(size_t(nsb) + 1, 0);
+  {
+    int64_t t = 0;
+    for (int p = 0; p < S.npoints; ++p)
+      for (size_t a = 0; a < pe[p].size(); ++a)
+        for (size_t b = 0; b <= a; ++b) {
+          // pe sorted ascending: a >= b => key_a >= key_b
+          const int64_t blk = S.Spat.Find(pe[p][a].first, pe[p][b].first);
+          tblk[t++] = int32_t(blk);
+          S.sb_ptr[blk + 1]++;
+        }
   }
-  S.sb_ptr.push_back(0);
+  for (int64_t q = 0; q < nsb; ++q) S.sb_ptr[q + 1] += S.sb_ptr[q];
+  S.sb_eoff.resize(size_t(nterms));
+  S.sb_woff.resize(size_t(nterms));
+  {
+    std::vector<int64_t> fill(S.sb_ptr.begin(), S.sb_ptr.end() - 1);
+    int64_t t = 0;
+    for (int p = 0; p < S.npoints; ++p) {
+      const int64_t e0 = S.pt_eptr[p];
+      for (size_t a = 0; a < pe[p].size(); ++a)
+        for (size_t b = 0; b <= a; ++b) {
+          const int64_t k = fill[tblk[t++]]++;
+          S.sb_eoff[k] = S.pt_eoff[e0 + a];
+          S.sb_woff[k] = S.pt_woff[e0 + b];
+        }
+    }
+  }
   for (int j = 0; j < S.nB_keys; ++j)
     for (int64_t q = S.Spat.colptr[j]; q < S.Spat.colptr[j + 1]; ++q) {
       const int i = S.Spat.rows[q];
-      for (auto& t : terms[q]) {
-        S.sb_eoff.push_back(t.first);
-        S.sb_woff.push_back(t.second);
-      }
-      S.sb_ptr.push_back(int64_t(S.sb_eoff.size()));
       const int64_t hb = L.H.Find(i, j);
       S.sb_hoff.push_back(hb >= 0 ? L.H.boff[hb] : -1);
       S.sb_soff.push_back(S.Spat.boff[q]);
@@ -260,30 +331,28 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L) {
       S.sb_dl.push_back(P.tdim[j]);
       S.sb_diag_toff.push_back(i == j ? int32_t(P.toff[i]) : -1);
     }
-  // reduced rhs lists
-  std::vector<std::vector<int64_t>> rl(S.nB);  // per B scalar: indices into (eoff, col, dk, pt)
+  // reduced rhs lists: per B scalar, the points that see its key in point order
   S.r_ptr.assign(S.nB + 1, 0);
-  std::vector<int64_t> cntr(S.nB, 0);
-  for (int p = 0; p < S.npoints; ++p)
-    for (auto& e : pe[p])
-      for (int c = 0; c < P.tdim[e.first]; ++c) cntr[P.toff[e.first] + c]++;
-  for (int64_t i = 0; i < S.nB; ++i) S.r_ptr[i + 1] = S.r_ptr[i] + cntr[i];
+  for (int k = 0; k < S.nB_keys; ++k)
+    for (int c = 0; c < P.tdim[k]; ++c) {
+      const int64_t i = P.toff[k] + c;
+      S.r_ptr[i + 1] = S.r_ptr[i] + (kp_ptr[k + 1] - kp_ptr[k]);
+    }
   const int64_t nr = S.r_ptr[S.nB];
   S.r_eoff.resize(nr);
   S.r_ecol.resize(nr);
   S.r_dk.resize(nr);
   S.r_pt.resize(nr);
-  std::vector<int64_t> fill(S.r_ptr.begin(), S.r_ptr.end() - 1);
-  for (int p = 0; p < S.npoints; ++p)
-    for (auto& e : pe[p])
-      for (int c = 0; c < P.tdim[e.first]; ++c) {
-        const int64_t i = P.toff[e.first] + c;
-        const int64_t q = fill[i]++;
-        S.r_eoff[q] = e.second;
+  for (int k = 0; k < S.nB_keys; ++k)
+    for (int c = 0; c < P.tdim[k]; ++c) {
+      int64_t q = S.r_ptr[P.toff[k] + c];
+      for (int64_t u = kp_ptr[k]; u < kp_ptr[k + 1]; ++u, ++q) {
+        S.r_eoff[q] = kp_eoff[u];
         S.r_ecol[q] = c;
-        S.r_dk[q] = P.tdim[e.first];
-        S.r_pt[q] = p;
+        S.r_dk[q] = P.tdim[k];
+        S.r_pt[q] = kp[u];
       }
+    }
   return S;
 }
 
