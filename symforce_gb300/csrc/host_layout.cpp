@@ -33,6 +33,29 @@ LinLayout BuildLinLayout(const HostProblem& P) {
         }
   L.H = MakePattern(P.tdim, std::move(pairs));
   L.nvals = L.H.nvals();
+  // row-major index of the stored blocks, so that a block is found in the shorter of its row and
+  // its column (a point's row holds a few camera blocks; a camera's column, every point it sees)
+  std::vector<int64_t> hr_ptr(size_t(L.H.nb) + 1, 0);
+  for (int64_t q = 0; q < L.H.nblocks(); ++q) hr_ptr[size_t(L.H.rows[q]) + 1]++;
+  for (int i = 0; i < L.H.nb; ++i) hr_ptr[i + 1] += hr_ptr[i];
+  std::vector<int32_t> hr_col(static_cast<size_t>(L.H.nblocks()));
+  std::vector<int64_t> hr_blk(hr_col.size());
+  {
+    std::vector<int64_t> fill(hr_ptr.begin(), hr_ptr.end() - 1);
+    for (int j = 0; j < L.H.nb; ++j)
+      for (int64_t q = L.H.colptr[j]; q < L.H.colptr[j + 1]; ++q) {
+        const int64_t at = fill[L.H.rows[q]]++;
+        hr_col[at] = j;  // ascending: columns are visited in order
+        hr_blk[at] = q;
+      }
+  }
+  auto find_block = [&](int i, int j) -> int64_t {  // i >= j, the block must exist
+    if (hr_ptr[i + 1] - hr_ptr[i] < L.H.colptr[j + 1] - L.H.colptr[j]) {
+      const auto b = hr_col.begin() + hr_ptr[i], e = hr_col.begin() + hr_ptr[i + 1];
+      return hr_blk[std::lower_bound(b, e, j) - hr_col.begin()];
+    }
+    return L.H.Find(i, j);
+  };
   L.N = P.N;
   L.diag_off.resize(P.N);
   for (int k = 0; k < P.nkeys; ++k) {
@@ -66,15 +89,20 @@ LinLayout BuildLinLayout(const HostProblem& P) {
       warp_merged[bi][w] = same;
     }
   }
-  // Whether device factor f of batch bi contributes entry e itself (false: its warp's first
-  // factor carries the warp's sum).
-  auto contributes = [&](size_t bi, int f, int e, int nh) {
-    const int mt = merged_dims[bi];
-    if (mt == 0 || (f & 31) == 0) return true;
+  // Device factor f of batch bi is a later factor of a merged warp: its merged entries are carried
+  // by the warp's first factor, and it contributes only the others.
+  auto merged_tail = [&](size_t bi, int f) {
+    if (merged_dims[bi] == 0 || (f & 31) == 0) return false;
     const size_t w = size_t(f) / 32;
-    if (w >= warp_merged[bi].size() || !warp_merged[bi][w]) return true;
-    const bool merged_entry = e < nh ? e < mt * (mt + 1) / 2 : e - nh < mt;
-    return !merged_entry;
+    return w < warp_merged[bi].size() && warp_merged[bi][w] != 0;
+  };
+  // the merged entries of a batch's packing: the packed prefix and the rhs prefix of its merged
+  // key slots
+  auto merged_entries = [&](size_t bi, int nh, int nent) {
+    const int mt = merged_dims[bi];
+    std::vector<char> m(size_t(nent), 0);
+    for (int e = 0; e < nent; ++e) m[e] = e < nh ? e < mt * (mt + 1) / 2 : e - nh < mt;
+    return m;
   };
   // Slots (H value index or nvals + tangent index) of all entries of the user's factor f: the
   // factor's key blocks are looked up once, each entry adds its offset inside the block.
@@ -88,7 +116,7 @@ LinLayout BuildLinLayout(const HostProblem& P) {
       for (int sb = 0; sb <= sa; ++sb) {
         const int ka = keys[sa], kb = keys[sb];
         swapped[sa][sb] = ka < kb;
-        bo[sa][sb] = L.H.boff[ka >= kb ? L.H.Find(ka, kb) : L.H.Find(kb, ka)];
+        bo[sa][sb] = L.H.boff[ka >= kb ? find_block(ka, kb) : find_block(kb, ka)];
       }
     int e = 0;
     for (int a = 0; a < td; ++a)
@@ -117,10 +145,15 @@ LinLayout BuildLinLayout(const HostProblem& P) {
     const int nh = B.tdim * (B.tdim + 1) / 2;
     const int nent = nh + B.tdim;
     std::vector<int64_t> slots(nent);
+    const std::vector<char> merged = merged_entries(bi, nh, nent);
     for (int f = 0; f < B.count; ++f) {
       factor_slots(B, order[bi][f], kslot[bi].data(), local[bi].data(), slots.data());
-      for (int e = 0; e < nent; ++e)
-        if (contributes(bi, f, e, nh)) cnt[slots[e]]++;
+      if (merged_tail(bi, f)) {
+        for (int e = 0; e < nent; ++e)
+          if (!merged[e]) cnt[slots[e]]++;
+      } else {
+        for (int e = 0; e < nent; ++e) cnt[slots[e]]++;
+      }
     }
   }
   for (int64_t s = 0; s < nslots; ++s)
@@ -140,19 +173,21 @@ LinLayout BuildLinLayout(const HostProblem& P) {
       }();
       if (!upper_of_diag) throw Error(SFG_ERR_STRUCTURE, "Hessian entry without a contributor");
     }
-  // staging groups in slot order
-  std::vector<int64_t> group_base(nslots, -1);
+  // staging groups in slot order; next_sink[s]: the sink index the next contribution to slot s
+  // gets (its staging slots in turn), or -1 when the slot has one contributor and is written in
+  // place (one array, so a contribution costs one random access)
+  std::vector<int64_t> next_sink(nslots, -1);
   L.red_ptr.push_back(0);
   for (int64_t s = 0; s < nslots; ++s)
     if (cnt[s] > 1) {
-      group_base[s] = L.red_ptr.back();
+      next_sink[s] = nslots + L.red_ptr.back();
       L.red_dst.push_back(int32_t(s));
       L.red_ptr.push_back(L.red_ptr.back() + cnt[s]);
     }
   L.nstage = L.red_ptr.back();
   if (nslots + L.nstage >= (int64_t(1) << 31))
     throw Error(SFG_ERR_STRUCTURE, "problem too large for 32-bit sink indices");
-  std::vector<int32_t> seen(nslots, 0);
+  std::vector<int32_t>().swap(cnt);
   for (size_t bi = 0; bi < P.batches.size(); ++bi) {
     const auto& B = P.batches[bi];
     LinLayout::BatchMap M;
@@ -164,24 +199,22 @@ LinLayout BuildLinLayout(const HostProblem& P) {
     constexpr int kRun = 32;
     std::vector<int64_t> slots(M.nent);
     std::vector<int32_t> run(size_t(kRun) * M.nent);
+    const std::vector<char> merged = merged_entries(bi, nh, M.nent);
     for (int f0 = 0; f0 < B.count; f0 += kRun) {
       const int nf = std::min(kRun, B.count - f0);
       for (int j = 0; j < nf; ++j) {
         const int f = f0 + j;
         factor_slots(B, order[bi][f], kslot[bi].data(), local[bi].data(), slots.data());
+        const bool tail = merged_tail(bi, f);
         for (int e = 0; e < M.nent; ++e) {
           int32_t& out = run[size_t(e) * kRun + j];
-          if (!contributes(bi, f, e, nh)) {
+          if (tail && merged[e]) {
             out = run[size_t(e) * kRun];  // never read: the warp's first factor stores
             continue;
           }
           const int64_t s = slots[e];
-          if (cnt[s] == 1) {
-            out = int32_t(s);
-          } else {
-            out = int32_t(nslots + group_base[s] + seen[s]);
-            seen[s]++;
-          }
+          int64_t& nx = next_sink[s];
+          out = int32_t(nx < 0 ? s : nx++);
         }
       }
       for (int e = 0; e < M.nent; ++e)
