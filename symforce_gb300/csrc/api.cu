@@ -806,6 +806,7 @@ int32_t sfg_hessian_lower(sfg_handle* h, int64_t* nnz, int32_t* col_ptr, int32_t
                           double* values) {
   return Guard([&] {
     if (!h || !nnz) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    sfg::BuildCscExport(h->L, h->P);
     const auto& L = h->L;
     *nnz = int64_t(L.csc_rowidx.size());
     if (col_ptr) std::copy(L.csc_colptr.begin(), L.csc_colptr.end(), col_ptr);
@@ -859,7 +860,7 @@ int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_pe
         };
         int64_t consts = 0;
         for (const auto& b : P.batches) consts += int64_t(b.count) * b.nc;
-        bytes = 8.0 * double(P.S + consts + P.M + int64_t(h->L.csc_rowidx.size()) + P.N);
+        bytes = 8.0 * double(P.S + consts + P.M + h->L.nnz_lower + P.N);
         for (const auto& b : P.batches) {
           const double td = b.tdim, rd = b.rdim;
           fma += double(b.count) * (rd * td * (td + 1) / 2 + rd * td);

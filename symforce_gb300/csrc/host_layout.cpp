@@ -176,17 +176,19 @@ LinLayout BuildLinLayout(const HostProblem& P) {
   // staging groups in slot order; next_sink[s]: the sink index the next contribution to slot s
   // gets (its staging slots in turn), or -1 when the slot has one contributor and is written in
   // place (one array, so a contribution costs one random access)
-  std::vector<int64_t> next_sink(nslots, -1);
+  constexpr int64_t kSinkLimit = int64_t(1) << 31;
+  if (nslots >= kSinkLimit) throw Error(SFG_ERR_STRUCTURE, "problem too large for 32-bit sink indices");
+  std::vector<int32_t> next_sink(nslots, -1);
   L.red_ptr.push_back(0);
   for (int64_t s = 0; s < nslots; ++s)
     if (cnt[s] > 1) {
-      next_sink[s] = nslots + L.red_ptr.back();
+      if (nslots + L.red_ptr.back() + cnt[s] >= kSinkLimit)
+        throw Error(SFG_ERR_STRUCTURE, "problem too large for 32-bit sink indices");
+      next_sink[s] = int32_t(nslots + L.red_ptr.back());
       L.red_dst.push_back(int32_t(s));
       L.red_ptr.push_back(L.red_ptr.back() + cnt[s]);
     }
   L.nstage = L.red_ptr.back();
-  if (nslots + L.nstage >= (int64_t(1) << 31))
-    throw Error(SFG_ERR_STRUCTURE, "problem too large for 32-bit sink indices");
   std::vector<int32_t>().swap(cnt);
   for (size_t bi = 0; bi < P.batches.size(); ++bi) {
     const auto& B = P.batches[bi];
@@ -213,8 +215,8 @@ LinLayout BuildLinLayout(const HostProblem& P) {
             continue;
           }
           const int64_t s = slots[e];
-          int64_t& nx = next_sink[s];
-          out = int32_t(nx < 0 ? s : nx++);
+          int32_t& nx = next_sink[s];
+          out = nx < 0 ? int32_t(s) : nx++;
         }
       }
       for (int e = 0; e < M.nent; ++e)
@@ -224,18 +226,20 @@ LinLayout BuildLinLayout(const HostProblem& P) {
     M.order = std::move(order[bi]);
     L.maps.push_back(std::move(M));
   }
-  // CSC export
+  // scalar entries of the CSC lower layout: full off-diagonal blocks, lower diagonal blocks
+  for (int kc = 0; kc < P.nkeys; ++kc)
+    for (int64_t q = L.H.colptr[kc]; q < L.H.colptr[kc + 1]; ++q) {
+      const int64_t dr = P.tdim[L.H.rows[q]], dc = P.tdim[kc];
+      L.nnz_lower += L.H.rows[q] == kc ? dc * (dc + 1) / 2 : dr * dc;
+    }
+  return L;
+}
+
+void BuildCscExport(LinLayout& L, const HostProblem& P) {
+  if (!L.csc_colptr.empty()) return;
   L.csc_colptr.assign(P.N + 1, 0);
-  {
-    int64_t nnz = 0;
-    for (int kc = 0; kc < P.nkeys; ++kc)
-      for (int64_t q = L.H.colptr[kc]; q < L.H.colptr[kc + 1]; ++q) {
-        const int64_t dr = P.tdim[L.H.rows[q]], dc = P.tdim[kc];
-        nnz += L.H.rows[q] == kc ? dc * (dc + 1) / 2 : dr * dc;
-      }
-    L.csc_rowidx.reserve(size_t(nnz));
-    L.csc_src.reserve(size_t(nnz));
-  }
+  L.csc_rowidx.reserve(size_t(L.nnz_lower));
+  L.csc_src.reserve(size_t(L.nnz_lower));
   for (int kc = 0; kc < P.nkeys; ++kc)
     for (int cc = 0; cc < P.tdim[kc]; ++cc) {
       const int64_t col = P.toff[kc] + cc;
@@ -248,7 +252,6 @@ LinLayout BuildLinLayout(const HostProblem& P) {
       }
       L.csc_colptr[col + 1] = int32_t(L.csc_rowidx.size());
     }
-  return L;
 }
 
 SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L) {

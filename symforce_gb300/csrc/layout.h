@@ -23,12 +23,16 @@ struct LinLayout {
   // groups of staged contributions: destination and [ptr, ptr+1) range of staging slots
   std::vector<int32_t> red_dst;
   std::vector<int64_t> red_ptr;
-  // reference CSC lower layout (symforce/opt/linearizer.cc:324-353): values come from csc_src
+  int64_t nnz_lower = 0;            // scalar entries of the reference CSC lower layout
+  // reference CSC lower layout (symforce/opt/linearizer.cc:324-353): values come from csc_src;
+  // built on first use (BuildCscExport), it is as large as the Hessian itself
   std::vector<int32_t> csc_colptr, csc_rowidx;
   std::vector<int64_t> csc_src;
 };
 
 LinLayout BuildLinLayout(const HostProblem& P);
+// Fill L's CSC export arrays (once; a no-op when they exist).
+void BuildCscExport(LinLayout& L, const HostProblem& P);
 
 struct SchurLayout {
   int nB_keys = 0, npoints = 0;
