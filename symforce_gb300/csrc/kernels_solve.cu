@@ -63,6 +63,30 @@ __device__ __forceinline__ void St(T* p, T v) { __stcg(p, v); }
 // ---------------------------------------------------------------------------------------------
 // Schur complement kernels
 // ---------------------------------------------------------------------------------------------
+// W = C^-1 E for one 3 x DK block E (row-major); cm = C^-1 entries (00, 10, 20, 11, 21, 22).
+template <typename T, int DK>
+__device__ __forceinline__ void PointW(const T* E, T* Wp, const T (&cm)[6]) {
+  T e[3 * DK];
+#pragma unroll
+  for (int i = 0; i < 3 * DK; ++i) e[i] = E[i];
+#pragma unroll
+  for (int c = 0; c < DK; ++c) {
+    const T e0 = e[c], e1 = e[DK + c], e2 = e[2 * DK + c];
+    Wp[c] = cm[0] * e0 + cm[1] * e1 + cm[2] * e2;
+    Wp[DK + c] = cm[1] * e0 + cm[3] * e1 + cm[4] * e2;
+    Wp[2 * DK + c] = cm[2] * e0 + cm[4] * e1 + cm[5] * e2;
+  }
+}
+template <typename T>
+__device__ __forceinline__ void PointWAny(const T* E, T* Wp, int dk, const T (&cm)[6]) {
+  for (int c = 0; c < dk; ++c) {
+    const T e0 = E[c], e1 = E[dk + c], e2 = E[2 * dk + c];
+    Wp[c] = cm[0] * e0 + cm[1] * e1 + cm[2] * e2;
+    Wp[dk + c] = cm[1] * e0 + cm[3] * e1 + cm[4] * e2;
+    Wp[2 * dk + c] = cm[2] * e0 + cm[4] * e1 + cm[5] * e2;
+  }
+}
+
 template <typename T>
 __global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_all, int64_t nvals,
                                   int64_t N, const double* damping, T* cinv, T* W, T* tp,
@@ -103,16 +127,15 @@ __global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_al
   t[0] = c00 * g0 + c10 * g1 + c20 * g2;
   t[1] = c10 * g0 + c11 * g1 + c21 * g2;
   t[2] = c20 * g0 + c21 * g1 + c22 * g2;
+  const T cm[6] = {c00, c10, c20, c11, c21, c22};
   for (int64_t e = d.pt_eptr[p]; e < d.pt_eptr[p + 1]; ++e) {
     const int dk = d.pt_ekey_dim[e];
     const T* E = H + d.pt_eoff[e];
     T* Wp = W + d.pt_woff[e];
-    for (int c = 0; c < dk; ++c) {
-      const T e0 = E[c], e1 = E[dk + c], e2 = E[2 * dk + c];
-      Wp[c] = c00 * e0 + c10 * e1 + c20 * e2;
-      Wp[dk + c] = c10 * e0 + c11 * e1 + c21 * e2;
-      Wp[2 * dk + c] = c20 * e0 + c21 * e1 + c22 * e2;
-    }
+    // the block's loads all issued before its stores (one memory latency per E block)
+    if (dk == 6) PointW<T, 6>(E, Wp, cm);
+    else if (dk == 3) PointW<T, 3>(E, Wp, cm);
+    else PointWAny<T>(E, Wp, dk, cm);
   }
 }
 
@@ -252,16 +275,63 @@ __global__ void SchurRhsKernel(SchurDev d, const T* hess_all, int64_t nvals, con
   if (i >= d.nB) return;
   const T* H = hess_all + int64_t(st->init_idx) * nvals;
   const T* g = rhs_all + int64_t(st->init_idx) * N;
-  T acc = T(0);
-  for (int64_t q = d.r_ptr[i] + lane; q < d.r_ptr[i + 1]; q += 32) {
+  // two entries per lane in flight (their index loads, then their operand loads), added in order
+  auto term = [&](int64_t q, T (&et)[6]) {
     const int dk = d.r_dk[q];
     const T* E = H + d.r_eoff[q] + d.r_ecol[q];
     const T* t = tp + 3 * int64_t(d.r_pt[q]);
-    acc += E[0] * t[0] + E[dk] * t[1] + E[2 * dk] * t[2];
+    et[0] = E[0];
+    et[1] = E[dk];
+    et[2] = E[2 * dk];
+    et[3] = t[0];
+    et[4] = t[1];
+    et[5] = t[2];
+  };
+  T acc = T(0);
+  const int64_t q1 = d.r_ptr[i + 1];
+  int64_t q = d.r_ptr[i] + lane;
+  for (; q + 32 < q1; q += 64) {
+    T a[6], b[6];
+    term(q, a);
+    term(q + 32, b);
+    acc += a[0] * a[3] + a[1] * a[4] + a[2] * a[5];
+    acc += b[0] * b[3] + b[1] * b[4] + b[2] * b[5];
+  }
+  if (q < q1) {
+    T a[6];
+    term(q, a);
+    acc += a[0] * a[3] + a[1] * a[4] + a[2] * a[5];
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if (lane == 0) v[i] = g[i] - acc;
+}
+
+// s = W y for one 3 x DK block (all loads issued first; the sums in column order).
+template <typename T, int DK>
+__device__ __forceinline__ void BlockTimes(const T* Wp, const double* yk, T (&s)[3]) {
+  T w[3 * DK], yv[DK];
+#pragma unroll
+  for (int i = 0; i < 3 * DK; ++i) w[i] = Wp[i];
+#pragma unroll
+  for (int c = 0; c < DK; ++c) yv[c] = T(yk[c]);
+  s[0] = s[1] = s[2] = T(0);
+#pragma unroll
+  for (int c = 0; c < DK; ++c) {
+    s[0] += w[c] * yv[c];
+    s[1] += w[DK + c] * yv[c];
+    s[2] += w[2 * DK + c] * yv[c];
+  }
+}
+template <typename T>
+__device__ __forceinline__ void BlockTimesAny(const T* Wp, const double* yk, int dk, T (&s)[3]) {
+  s[0] = s[1] = s[2] = T(0);
+  for (int c = 0; c < dk; ++c) {
+    const T yc = T(yk[c]);
+    s[0] += Wp[c] * yc;
+    s[1] += Wp[dk + c] * yc;
+    s[2] += Wp[2 * dk + c] * yc;
+  }
 }
 
 // Point back-substitution z_p = t_p - sum_k W_pk y_k, and update = -[y; z].
@@ -276,16 +346,13 @@ __global__ void SchurBackSubKernel(SchurDev d, const double* y, const T* W, cons
       const int dk = d.pt_ekey_dim[e];
       const T* Wp = W + d.pt_woff[e];
       const double* yk = y + d.pt_ekey_toff[e];
-      T s0 = T(0), s1 = T(0), s2 = T(0);
-      for (int c = 0; c < dk; ++c) {
-        const T yc = T(yk[c]);
-        s0 += Wp[c] * yc;
-        s1 += Wp[dk + c] * yc;
-        s2 += Wp[2 * dk + c] * yc;
-      }
-      z0 -= s0;
-      z1 -= s1;
-      z2 -= s2;
+      T s[3];
+      if (dk == 6) BlockTimes<T, 6>(Wp, yk, s);
+      else if (dk == 3) BlockTimes<T, 3>(Wp, yk, s);
+      else BlockTimesAny<T>(Wp, yk, dk, s);
+      z0 -= s[0];
+      z1 -= s[1];
+      z2 -= s[2];
     }
     double* u = update + d.c_toff + 3 * int64_t(p);
     u[0] = -double(z0);
