@@ -559,7 +559,7 @@ int BodyKernels(const sfg_handle* h) {
   n += h->red.ngroups > 0 ? 1 : 0;
   n += 1;  // cost
   n += 1 /*damping*/ + 1 /*retract*/ + 1 /*delta*/ + 1 /*decide*/ + 3 /*reset, factor, solve*/;
-  n += h->schur ? 5 /*points, S chunks, S, rhs, back-substitution*/ : 1 /*negate*/;
+  n += h->schur ? 6 /*points, W, S chunks, S, rhs, back-substitution*/ : 1 /*negate*/;
   if (h->elem == 4) n += 1 + 4 * h->refine_steps;  // widen; residual, reset, solve, accumulate
   if (h->pcg_mode) {
     n += 1 /*group blocks*/ + 2 /*row coupling, features*/ + (h->pcg_mode == 2 ? 1 : 0) +

@@ -237,6 +237,8 @@ SchurDev UploadSchur(DeviceArena& A, const SchurLayout& S, int elem) {
   d.pt_ekey_toff = A.Upload(S.pt_ekey_toff);
   d.pt_ekey_dim = A.Upload(S.pt_ekey_dim);
   d.pt_eoff = A.Upload(S.pt_eoff);
+  d.nE = int64_t(S.pt_eoff.size());
+  d.pt_of_e = A.Upload(S.pt_of_e);
   d.pt_woff = A.Upload(S.pt_woff);
   d.nsblocks = int(S.Spat.nblocks());
   d.sb_ptr = A.Upload(S.sb_ptr);

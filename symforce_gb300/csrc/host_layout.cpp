@@ -283,6 +283,7 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L) {
     for (auto& e : pe[p]) {
       S.pt_eoff.push_back(e.second);
       S.pt_woff.push_back(S.nW);
+      S.pt_of_e.push_back(p);
       S.pt_ekey_toff.push_back(int32_t(P.toff[e.first]));
       S.pt_ekey_dim.push_back(P.tdim[e.first]);
       S.nW += 3 * P.tdim[e.first];

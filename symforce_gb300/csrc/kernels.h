@@ -98,6 +98,8 @@ struct SchurDev {
   const int32_t* pt_ekey_dim;   // dim of that key
   const int64_t* pt_eoff;       // H value offset of E block (3 x d_k, row-major)
   const int64_t* pt_woff;       // W value offset (3 x d_k)
+  int64_t nE;                   // E blocks (pt_eptr[npoints])
+  const int32_t* pt_of_e;       // [nE] point of each E block
   int nsblocks;
   const int64_t* sb_ptr;        // [nsblocks + 1] terms of each S block
   const int64_t* sb_eoff;       // E_pk offset per term

@@ -87,9 +87,10 @@ __device__ __forceinline__ void PointWAny(const T* E, T* Wp, int dk, const T (&c
   }
 }
 
+// One thread per point: C^-1 of the damped 3 x 3 block (by its Cholesky factor) and t = C^-1 g.
 template <typename T>
 __global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_all, int64_t nvals,
-                                  int64_t N, const double* damping, T* cinv, T* W, T* tp,
+                                  int64_t N, const double* damping, T* cinv, T* tp,
                                   const LmState* st) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= d.npoints) return;
@@ -127,16 +128,24 @@ __global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_al
   t[0] = c00 * g0 + c10 * g1 + c20 * g2;
   t[1] = c10 * g0 + c11 * g1 + c21 * g2;
   t[2] = c20 * g0 + c21 * g1 + c22 * g2;
-  const T cm[6] = {c00, c10, c20, c11, c21, c22};
-  for (int64_t e = d.pt_eptr[p]; e < d.pt_eptr[p + 1]; ++e) {
-    const int dk = d.pt_ekey_dim[e];
-    const T* E = H + d.pt_eoff[e];
-    T* Wp = W + d.pt_woff[e];
-    // the block's loads all issued before its stores (one memory latency per E block)
-    if (dk == 6) PointW<T, 6>(E, Wp, cm);
-    else if (dk == 3) PointW<T, 3>(E, Wp, cm);
-    else PointWAny<T>(E, Wp, dk, cm);
-  }
+}
+
+// One thread per E block (the blocks of a point are consecutive, so neighbouring threads share its
+// C^-1): W = C^-1 E, the block's loads all issued before its stores.
+template <typename T>
+__global__ void SchurWKernel(SchurDev d, const T* hess_all, int64_t nvals, const T* cinv, T* W,
+                             const LmState* st) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= d.nE) return;
+  const T* H = hess_all + int64_t(st->init_idx) * nvals;
+  const T* ci = cinv + 9 * int64_t(d.pt_of_e[e]);
+  const T cm[6] = {ci[0], ci[1], ci[2], ci[4], ci[5], ci[8]};
+  const int dk = d.pt_ekey_dim[e];
+  const T* E = H + d.pt_eoff[e];
+  T* Wp = W + d.pt_woff[e];
+  if (dk == 6) PointW<T, 6>(E, Wp, cm);
+  else if (dk == 3) PointW<T, 3>(E, Wp, cm);
+  else PointWAny<T>(E, Wp, dk, cm);
 }
 
 // S = B - sum_p E_pk^T W_pl over the S blocks' terms (points seen by both keys), in two passes.
@@ -1191,7 +1200,10 @@ void LaunchSchurPoints(const SchurDev& d, const void* hess, const void* rhs, int
   const int threads = 128;
   SchurPointsKernel<T><<<(d.npoints + threads - 1) / threads, threads, 0, s>>>(
       d, static_cast<const T*>(hess), static_cast<const T*>(rhs), nvals, N, damping,
-      static_cast<T*>(cinv), static_cast<T*>(W), static_cast<T*>(tp), st);
+      static_cast<T*>(cinv), static_cast<T*>(tp), st);
+  if (d.nE > 0)
+    SchurWKernel<T><<<int((d.nE + threads - 1) / threads), threads, 0, s>>>(
+        d, static_cast<const T*>(hess), nvals, static_cast<const T*>(cinv), static_cast<T*>(W), st);
 }
 
 template <typename T>

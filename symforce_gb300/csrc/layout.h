@@ -39,6 +39,7 @@ struct SchurLayout {
   int64_t nB = 0, c_toff = 0;
   std::vector<int64_t> pt_diag, pt_eptr, pt_eoff, pt_woff;
   std::vector<int32_t> pt_ekey_toff, pt_ekey_dim;
+  std::vector<int32_t> pt_of_e;    // point of each E block
   int64_t nW = 0;
   BlockPattern Spat;               // pattern of the reduced system over B keys
   std::vector<int64_t> sb_ptr, sb_eoff, sb_woff, sb_hoff, sb_soff;
