@@ -1,0 +1,147 @@
+"""The linearization's host scatter plan, checked on the CPU against an independent count.
+
+The plan (symforce_gb300/csrc/host_layout.cpp, the block analogue of
+Linearizer::BuildInitialLinearization, symforce/opt/linearizer.cc:148-356) gives every factor
+entry a sink index: a Hessian / rhs value written in place, or a staging slot summed later; a warp
+of 32 reprojection factors of one camera sums its camera entries and stores them once.  Here the
+device's scatter is replayed in numpy with every factor entry worth 1 (a merged warp's sum worth
+32): each in-place value and each staging slot must be written exactly once, and after the staged
+sums every Hessian / rhs value must equal the number of factors that touch it, counted directly
+from the factors' keys and the block pattern (no use of the plan)."""
+
+from __future__ import annotations
+
+import ctypes as C
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from symforce_gb300 import _cabi as A
+from symforce_gb300 import synth
+
+ROOT = Path(__file__).resolve().parents[1]
+CSRC = ROOT / "symforce_gb300" / "csrc"
+MERGED_KEY_SLOTS = {A.SFG_FACTOR_SNAVELY_REPROJECTION: 2}  # MergedKeySlots in common.h
+
+
+@pytest.fixture(scope="module")
+def shim(tmp_path_factory):
+    gxx = shutil.which("g++")
+    cuda_inc = Path("/usr/local/cuda/include")
+    if gxx is None or not (cuda_inc / "cuda_runtime.h").exists():
+        pytest.skip("g++ or the CUDA headers are not available")
+    out = tmp_path_factory.mktemp("shim") / "libhostshim.so"
+    srcs = [ROOT / "tests" / "host_layout_shim.cpp"] + [CSRC / f for f in
+                                                        ("host_structure.cpp", "host_layout.cpp")]
+    subprocess.run([gxx, "-O1", "-std=c++17", "-shared", "-fPIC", f"-I{cuda_inc}", f"-I{ROOT / 'include'}",
+                    f"-I{CSRC}", *map(str, srcs), "-o", str(out)], check=True)
+    lib = C.CDLL(str(out))
+    lib.shim_build.argtypes = [C.POINTER(A.ProblemC)]
+    return lib
+
+
+def _arr(n, dtype):
+    return np.zeros(int(n), dtype=dtype)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _expected_counts(p: A.ProblemArrays, colptr, rows, boff, toff, nvals, N):
+    """Contributions of every Hessian value and rhs entry, from the keys and the block pattern."""
+    tdim = np.array([A.KEY_DIMS[int(t)][1] for t in p.key_types])
+    block = {}
+    for j in range(len(colptr) - 1):
+        for q in range(colptr[j], colptr[j + 1]):
+            block[(int(rows[q]), j)] = int(boff[q])
+    cnt = np.zeros(nvals + N, dtype=np.int64)
+    for b in p.batches:
+        for keys in np.asarray(b.keys):
+            cols = [(int(k), r) for k in keys for r in range(tdim[k])]
+            for a, (ka, ra) in enumerate(cols):
+                for (kb, rb) in cols[:a + 1]:
+                    if ka == kb:
+                        cnt[block[(ka, ka)] + ra * tdim[ka] + rb] += 1
+                    elif ka > kb:
+                        cnt[block[(ka, kb)] + ra * tdim[kb] + rb] += 1
+                    else:
+                        cnt[block[(kb, ka)] + rb * tdim[ka] + ra] += 1
+                cnt[nvals + toff[ka] + ra] += 1
+    return cnt
+
+
+def _replay(lib, p: A.ProblemArrays):
+    c = p.to_c()
+    assert lib.shim_build(C.byref(c)) == 0
+    sizes = _arr(7, np.int64)
+    lib.shim_sizes(_ptr(sizes))
+    nvals, N, nstage, ngroups, nbatches, nblocks, nkeys = (int(x) for x in sizes)
+    colptr, rows, boff, toff = _arr(nkeys + 1, np.int64), _arr(nblocks, np.int32), _arr(nblocks, np.int64), \
+        _arr(nkeys + 1, np.int64)
+    lib.shim_pattern(_ptr(colptr), _ptr(rows), _ptr(boff), _ptr(toff))
+    red_dst, red_ptr = _arr(ngroups, np.int32), _arr(ngroups + 1, np.int64)
+    lib.shim_groups(_ptr(red_dst), _ptr(red_ptr))
+    tdim = np.array([A.KEY_DIMS[int(t)][1] for t in p.key_types])
+
+    value = np.zeros(nvals + N, dtype=np.int64)
+    writes = np.zeros(nvals + N, dtype=np.int64)
+    stage = np.zeros(nstage, dtype=np.int64)
+    stage_writes = np.zeros(nstage, dtype=np.int64)
+    merged_warps = 0
+    for bi, b in enumerate(p.batches):
+        info = _arr(3, np.int32)
+        lib.shim_batch(bi, _ptr(info))
+        nent, mt, count = (int(x) for x in info)
+        dest, order = _arr(nent * count, np.int32), _arr(count, np.int32)
+        lib.shim_batch_arrays(bi, _ptr(dest), _ptr(order))
+        dest = dest.reshape(nent, count)
+        assert sorted(order.tolist()) == list(range(count))
+        keys = np.asarray(b.keys)[order]  # device order
+        ms = MERGED_KEY_SLOTS.get(b.kind, 0)
+        assert mt == sum(tdim[keys[0, s]] for s in range(ms)) if count else True
+        td = sum(tdim[k] for k in keys[0]) if count else 0
+        nh = td * (td + 1) // 2
+        merged_entry = np.array([(e < mt * (mt + 1) // 2) if e < nh else (e - nh < mt) for e in range(nent)])
+        for f in range(count):
+            w0 = f - f % 32
+            merged = (ms > 0 and w0 + 32 <= count
+                      and all((keys[w0:w0 + 32, s] == keys[w0, s]).all() for s in range(ms)))
+            if merged and f == w0:
+                merged_warps += 1
+            for e in range(nent):
+                v = 1
+                if merged and merged_entry[e]:
+                    if f != w0:
+                        continue
+                    v = 32
+                d = int(dest[e, f])
+                if d < nvals + N:
+                    value[d] += v
+                    writes[d] += 1
+                else:
+                    stage[d - nvals - N] += v
+                    stage_writes[d - nvals - N] += 1
+    assert (writes <= 1).all(), "a value written in place by two contributions"
+    assert (stage_writes == 1).all(), "a staging slot not written exactly once"
+    for g in range(ngroups):
+        s = int(red_dst[g])
+        assert writes[s] == 0, "a staged destination also written in place"
+        value[s] = stage[red_ptr[g]:red_ptr[g + 1]].sum()
+    expected = _expected_counts(p, colptr, rows, boff, toff, nvals, N)
+    np.testing.assert_array_equal(value, expected)
+    return merged_warps
+
+
+def test_reprojection_plan_with_merged_warps(shim):
+    # ~100 observations per camera: whole warps of one camera (merged) and mixed warps at the ends
+    p = synth.bundle_adjustment(num_cameras=6, num_points=150, num_observations=620, seed=2)
+    assert _replay(shim, p) > 0
+
+
+def test_plans_without_merging(shim):
+    assert _replay(shim, synth.robot_2d(num_poses=60, num_landmarks=8, seed=3)) == 0
+    assert _replay(shim, synth.pose3_chain(num_poses=40, num_landmarks=12, seed=4)) == 0
