@@ -9,6 +9,12 @@
 namespace {
 sfg::HostProblem g_problem;
 sfg::LinLayout g_layout;
+sfg::SchurLayout g_schur;
+
+template <typename V, typename O>
+void Put(const std::vector<V>& v, O* out) {
+  std::copy(v.begin(), v.end(), out);
+}
 }  // namespace
 
 extern "C" {
@@ -61,6 +67,65 @@ void shim_pattern(int64_t* colptr, int32_t* rows, int64_t* boff, int64_t* toff) 
   std::copy(H.rows.begin(), H.rows.end(), rows);
   std::copy(H.boff.begin(), H.boff.end() - 1, boff);
   std::copy(g_problem.toff.begin(), g_problem.toff.end(), toff);
+}
+
+// The Schur plan of the problem built last (points = the trailing num_schur keys); 0 on success.
+int shim_build_schur() {
+  try {
+    g_schur = sfg::BuildSchurLayout(g_problem, g_layout);
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// nB_keys, npoints, nB, c_toff, E blocks, S blocks, terms, rhs entries, S values
+void shim_schur_sizes(int64_t* out) {
+  const auto& S = g_schur;
+  out[0] = S.nB_keys;
+  out[1] = S.npoints;
+  out[2] = S.nB;
+  out[3] = S.c_toff;
+  out[4] = int64_t(S.pt_eoff.size());
+  out[5] = S.Spat.nblocks();
+  out[6] = int64_t(S.sb_eoff.size());
+  out[7] = int64_t(S.r_eoff.size());
+  out[8] = S.Spat.nvals();
+}
+
+// 64-bit arrays: 0 pt_diag, 1 pt_eptr, 2 pt_eoff, 3 pt_woff, 4 sb_ptr, 5 sb_eoff, 6 sb_woff,
+// 7 sb_hoff, 8 sb_soff, 9 r_ptr, 10 r_eoff, 11 Spat colptr, 12 Spat boff
+void shim_schur_i64(int which, int64_t* out) {
+  const auto& S = g_schur;
+  switch (which) {
+    case 0: Put(S.pt_diag, out); break;
+    case 1: Put(S.pt_eptr, out); break;
+    case 2: Put(S.pt_eoff, out); break;
+    case 3: Put(S.pt_woff, out); break;
+    case 4: Put(S.sb_ptr, out); break;
+    case 5: Put(S.sb_eoff, out); break;
+    case 6: Put(S.sb_woff, out); break;
+    case 7: Put(S.sb_hoff, out); break;
+    case 8: Put(S.sb_soff, out); break;
+    case 9: Put(S.r_ptr, out); break;
+    case 10: Put(S.r_eoff, out); break;
+    case 11: Put(S.Spat.colptr, out); break;
+    case 12: std::copy(S.Spat.boff.begin(), S.Spat.boff.end() - 1, out); break;
+  }
+}
+
+// 32-bit arrays: 0 pt_ekey_dim, 1 sb_dk, 2 sb_dl, 3 r_ecol, 4 r_dk, 5 r_pt, 6 Spat rows
+void shim_schur_i32(int which, int32_t* out) {
+  const auto& S = g_schur;
+  switch (which) {
+    case 0: Put(S.pt_ekey_dim, out); break;
+    case 1: Put(S.sb_dk, out); break;
+    case 2: Put(S.sb_dl, out); break;
+    case 3: Put(S.r_ecol, out); break;
+    case 4: Put(S.r_dk, out); break;
+    case 5: Put(S.r_pt, out); break;
+    case 6: Put(S.Spat.rows, out); break;
+  }
 }
 
 }  // extern "C"

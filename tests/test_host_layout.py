@@ -1,4 +1,5 @@
-"""The linearization's host scatter plan, checked on the CPU against an independent count.
+"""The host plans of the hot path, checked on the CPU: the linearization's scatter plan against an
+independent count, and the Schur plan against a dense Schur complement.
 
 The plan (symforce_gb300/csrc/host_layout.cpp, the block analogue of
 Linearizer::BuildInitialLinearization, symforce/opt/linearizer.cc:148-356) gives every factor
@@ -7,7 +8,8 @@ of 32 reprojection factors of one camera sums its camera entries and stores them
 device's scatter is replayed in numpy with every factor entry worth 1 (a merged warp's sum worth
 32): each in-place value and each staging slot must be written exactly once, and after the staged
 sums every Hessian / rhs value must equal the number of factors that touch it, counted directly
-from the factors' keys and the block pattern (no use of the plan)."""
+from the factors' keys and the block pattern (no use of the plan).  The library's host sources are
+compiled with g++ beside a small shim (tests/host_layout_shim.cpp) that hands the plans out."""
 
 from __future__ import annotations
 
@@ -145,3 +147,99 @@ def test_reprojection_plan_with_merged_warps(shim):
 def test_plans_without_merging(shim):
     assert _replay(shim, synth.robot_2d(num_poses=60, num_landmarks=8, seed=3)) == 0
     assert _replay(shim, synth.pose3_chain(num_poses=40, num_landmarks=12, seed=4)) == 0
+
+
+def _schur_arrays(lib):
+    sizes = _arr(9, np.int64)
+    lib.shim_schur_sizes(_ptr(sizes))
+    nbk, npts, nB, c_toff, nE, nsb, nterms, nr, nS = (int(x) for x in sizes)
+    n64 = {0: npts, 1: npts + 1, 2: nE, 3: nE, 4: nsb + 1, 5: nterms, 6: nterms, 7: nsb, 8: nsb,
+           9: nB + 1, 10: nr, 11: nbk + 1, 12: nsb}
+    n32 = {0: nE, 1: nsb, 2: nsb, 3: nr, 4: nr, 5: nr, 6: nsb}
+    a64, a32 = {}, {}
+    for k, n in n64.items():
+        a64[k] = _arr(n, np.int64)
+        lib.shim_schur_i64(k, _ptr(a64[k]))
+    for k, n in n32.items():
+        a32[k] = _arr(n, np.int32)
+        lib.shim_schur_i32(k, _ptr(a32[k]))
+    return (nbk, npts, nB, c_toff, nS), a64, a32
+
+
+def test_schur_plan_matches_dense_schur_complement(shim):
+    """The Schur plan (point C blocks, per-S-block term lists, reduced-rhs lists) replayed in numpy
+    on random block values gives S = B - E^T C^-1 E and v = g_B - E^T C^-1 g_C of the dense matrix
+    (symforce/opt/sparse_schur_solver.tcc:15-170)."""
+    p = synth.bundle_adjustment(num_cameras=5, num_points=60, num_observations=240, seed=7)
+    c = p.to_c()
+    assert shim.shim_build(C.byref(c)) == 0 and shim.shim_build_schur() == 0
+    sizes = _arr(7, np.int64)
+    shim.shim_sizes(_ptr(sizes))
+    nvals, N, _, _, _, nblocks, nkeys = (int(x) for x in sizes)
+    colptr, rows, boff, toff = _arr(nkeys + 1, np.int64), _arr(nblocks, np.int32), _arr(nblocks, np.int64), \
+        _arr(nkeys + 1, np.int64)
+    shim.shim_pattern(_ptr(colptr), _ptr(rows), _ptr(boff), _ptr(toff))
+    tdim = np.diff(toff)
+    rng = np.random.default_rng(1)
+    vals = rng.normal(size=nvals)
+    H = np.zeros((N, N))
+    for j in range(nkeys):
+        for q in range(colptr[j], colptr[j + 1]):
+            i = int(rows[q])
+            blk = vals[boff[q]:boff[q] + tdim[i] * tdim[j]].reshape(tdim[i], tdim[j])
+            if i == j:  # symmetric diagonal blocks, stored full
+                blk = np.tril(blk) + np.tril(blk, -1).T + 12.0 * np.eye(tdim[i])
+                vals[boff[q]:boff[q] + tdim[i] * tdim[j]] = blk.ravel()
+            H[toff[i]:toff[i] + tdim[i], toff[j]:toff[j] + tdim[j]] = blk
+            H[toff[j]:toff[j] + tdim[j], toff[i]:toff[i] + tdim[i]] = blk.T
+    g = rng.normal(size=N)
+
+    (nbk, npts, nB, c_toff, nS), a64, a32 = _schur_arrays(shim)
+    assert nB == toff[nbk] and c_toff == nB
+    # replay: C^-1 and t per point, W per E block, S blocks from their terms, v from its lists
+    cinv = [np.linalg.inv(vals[a64[0][q]:a64[0][q] + 9].reshape(3, 3)) for q in range(npts)]
+    t = np.array([cinv[q] @ g[c_toff + 3 * q:c_toff + 3 * q + 3] for q in range(npts)])
+    Wv = np.zeros(int(max(a64[3][e] + 3 * a32[0][e] for e in range(len(a64[3])))))
+    for q in range(npts):
+        for e in range(a64[1][q], a64[1][q + 1]):
+            dk = int(a32[0][e])
+            E = vals[a64[2][e]:a64[2][e] + 3 * dk].reshape(3, dk)
+            Wv[a64[3][e]:a64[3][e] + 3 * dk] = (cinv[q] @ E).ravel()
+    Sv = np.zeros(nS)
+    for q in range(len(a64[7])):
+        dk, dl = int(a32[1][q]), int(a32[2][q])
+        acc = np.zeros((dk, dl))
+        for u in range(a64[4][q], a64[4][q + 1]):
+            E = vals[a64[5][u]:a64[5][u] + 3 * dk].reshape(3, dk)
+            W = Wv[a64[6][u]:a64[6][u] + 3 * dl].reshape(3, dl)
+            acc += E.T @ W
+        B = vals[a64[7][q]:a64[7][q] + dk * dl].reshape(dk, dl) if a64[7][q] >= 0 else 0.0
+        Sv[a64[8][q]:a64[8][q] + dk * dl] = (B - acc).ravel()
+    v = g[:nB].copy()
+    for i in range(nB):
+        for u in range(a64[9][i], a64[9][i + 1]):
+            dk, col, pt = int(a32[4][u]), int(a32[3][u]), int(a32[5][u])
+            E = vals[a64[10][u] + col + dk * np.arange(3)]
+            v[i] -= E @ t[pt]
+    # dense reference
+    Cinv = np.linalg.inv(H[nB:, nB:])
+    Sd = H[:nB, :nB] - H[:nB, nB:] @ Cinv @ H[nB:, :nB]
+    vd = g[:nB] - H[:nB, nB:] @ Cinv @ g[nB:]
+    np.testing.assert_allclose(v, vd, rtol=1e-10, atol=1e-10)
+    scol, srow, sboff = a64[11], a32[6], a64[12]
+    checked = 0
+    for j in range(nbk):
+        for q in range(scol[j], scol[j + 1]):
+            i = int(srow[q])
+            blk = Sv[sboff[q]:sboff[q] + tdim[i] * tdim[j]].reshape(tdim[i], tdim[j])
+            ref = Sd[toff[i]:toff[i] + tdim[i], toff[j]:toff[j] + tdim[j]]
+            np.testing.assert_allclose(blk, ref, rtol=1e-10, atol=1e-10)
+            checked += 1
+    assert checked == len(a64[7])
+    # every nonzero of the dense lower S lies in a stored block
+    mask = np.zeros((nB, nB), dtype=bool)
+    for j in range(nbk):
+        for q in range(scol[j], scol[j + 1]):
+            i = int(srow[q])
+            mask[toff[i]:toff[i] + tdim[i], toff[j]:toff[j] + tdim[j]] = True
+    assert np.abs(np.tril(Sd)[~mask]).max(initial=0.0) < 1e-12
