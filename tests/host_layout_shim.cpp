@@ -10,6 +10,8 @@ namespace {
 sfg::HostProblem g_problem;
 sfg::LinLayout g_layout;
 sfg::SchurLayout g_schur;
+sfg::Symbolic g_sym;
+sfg::TaskPlan g_plan;
 
 template <typename V, typename O>
 void Put(const std::vector<V>& v, O* out) {
@@ -125,6 +127,51 @@ void shim_schur_i32(int which, int32_t* out) {
     case 4: Put(S.r_dk, out); break;
     case 5: Put(S.r_pt, out); break;
     case 6: Put(S.Spat.rows, out); break;
+  }
+}
+
+// Symbolic factorization and tile task plan of the Hessian pattern (which 0) or of the reduced
+// system of the Schur plan (which 1), nested-dissection ordering; 0 on success.
+int shim_build_factor_plan(int which, int tile) {
+  try {
+    g_sym = sfg::Analyze(which == 0 ? g_layout.H : g_schur.Spat, SFG_ORDERING_NESTED_DISSECTION);
+    g_plan = sfg::PlanTasks(g_sym, tile);
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// fronts, tasks, children in all
+void shim_factor_sizes(int64_t* out) {
+  out[0] = g_sym.ns;
+  out[1] = int64_t(g_plan.tasks.size());
+  int64_t nc = 0;
+  for (const auto& c : g_sym.sn_children) nc += int64_t(c.size());
+  out[2] = nc;
+}
+
+// tasks [ntasks][4] = {type, front, i << 16 | j, k}; per front: pivot tiles, tiles, parent, pivot
+// width, front size; children of every front (child_ptr [ns + 1], child_list)
+void shim_factor_arrays(int32_t* tasks, int32_t* npiv, int32_t* ntiles, int32_t* parent, int32_t* w,
+                        int32_t* m, int32_t* child_ptr, int32_t* child_list) {
+  for (size_t t = 0; t < g_plan.tasks.size(); ++t) {
+    const int4 v = g_plan.tasks[t];
+    tasks[4 * t] = v.x;
+    tasks[4 * t + 1] = v.y;
+    tasks[4 * t + 2] = v.z;
+    tasks[4 * t + 3] = v.w;
+  }
+  Put(g_plan.npiv, npiv);
+  Put(g_plan.ntiles, ntiles);
+  Put(g_sym.sn_parent, parent);
+  Put(g_sym.sn_w, w);
+  Put(g_sym.sn_m, m);
+  child_ptr[0] = 0;
+  int32_t q = 0;
+  for (int s = 0; s < g_sym.ns; ++s) {
+    for (int c : g_sym.sn_children[s]) child_list[q++] = c;
+    child_ptr[s + 1] = q;
   }
 }
 
