@@ -161,4 +161,19 @@ struct TaskPlan {
 };
 TaskPlan PlanTasks(const Symbolic& sym, int tile);
 
+// Flattened per-(front, tile column) assembly lists, extend-add rounds and solve maps of a
+// symbolic factorization and its task plan, as the device kernels read them.
+struct FactorMaps {
+  std::vector<int64_t> a_ptr, a_src;   // [slots + 1]; source value of each assembled entry
+  std::vector<int32_t> a_dst, a_damp;  // front position (r + c m); damping index or -1
+  std::vector<int64_t> e_rptr;         // [slots + 1] rounds of each slot
+  std::vector<int64_t> e_round;        // [rounds + 1] entries of each round
+  std::vector<int64_t> e_src;          // child front entry (front pool index)
+  std::vector<int32_t> e_dst;          // parent front position
+  std::vector<int64_t> linv_base;      // [ns + 1] pivot-tile inverses of each front
+  std::vector<int32_t> child_ptr, child_list;
+  std::vector<int32_t> scalar_old;     // [n] original scalar of each new scalar
+};
+FactorMaps BuildFactorMaps(const Symbolic& S, const TaskPlan& T, const BlockPattern& pat);
+
 }  // namespace sfg

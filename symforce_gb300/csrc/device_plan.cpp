@@ -40,99 +40,28 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   f.tile_base = A.Upload(T.tile_base);
   f.npiv = A.Upload(T.npiv);
   f.ntiles = A.Upload(T.ntiles);
-  // ---- flattened assembly per (front, tile column)
-  const std::vector<int32_t>& col_base = T.asm_col_base;
-  const int nslots = col_base[S.ns];
-  std::vector<std::vector<int64_t>> asrc(nslots);
-  std::vector<std::vector<int32_t>> adst(nslots), adamp(nslots);
-  std::vector<std::vector<std::pair<int64_t, int32_t>>> ea(nslots);  // (src, dst) in child order
-  for (int s = 0; s < S.ns; ++s) {
-    const int w = S.sn_w[s], m = S.sn_m[s], np = T.npiv[s];
-    auto col_tile = [&](int c) { return c < w ? c / tile : np + (c - w) / tile; };
-    for (int64_t q = S.asm_off[s]; q < S.asm_off[s + 1]; ++q) {
-      const auto& a = S.asms[q];
-      for (int r = 0; r < a.di; ++r)
-        for (int c = 0; c < a.dj; ++c) {
-          if (a.diag && r < c) continue;
-          const int fr = a.transpose ? a.row0 + c : a.row0 + r;
-          const int fc = a.transpose ? a.col0 + r : a.col0 + c;
-          const int slot = col_base[s] + col_tile(fc);
-          asrc[slot].push_back(a.src + int64_t(r) * a.dj + c);
-          adst[slot].push_back(int32_t(fr + int64_t(fc) * m));
-          adamp[slot].push_back(a.diag && r == c ? int32_t(pat.off[a.oi] + r) : -1);
-        }
-    }
-    for (int c : S.sn_children[s]) {
-      const int hc = S.sn_h[c], wc = S.sn_w[c], mc = S.sn_m[c];
-      const int32_t* rel = S.rel.data() + S.rel_off[c];
-      for (int qc = 0; qc < hc; ++qc) {
-        const int slot = col_base[s] + col_tile(rel[qc]);
-        for (int r = qc; r < hc; ++r)
-          ea[slot].push_back({S.sn_foff[c] + (wc + r) + int64_t(wc + qc) * mc,
-                              int32_t(rel[r] + int64_t(rel[qc]) * m)});
-      }
-    }
-  }
-  std::vector<int64_t> a_ptr(nslots + 1, 0), a_src;
-  std::vector<int32_t> a_dst, a_damp;
-  std::vector<int64_t> e_rptr(nslots + 1, 0), e_round, e_src;
-  std::vector<int32_t> e_dst;
-  for (int q = 0; q < nslots; ++q) {
-    a_src.insert(a_src.end(), asrc[q].begin(), asrc[q].end());
-    a_dst.insert(a_dst.end(), adst[q].begin(), adst[q].end());
-    a_damp.insert(a_damp.end(), adamp[q].begin(), adamp[q].end());
-    a_ptr[q + 1] = int64_t(a_src.size());
-    // rounds: the k-th occurrence of a destination goes to round k (children keep their order)
-    std::unordered_map<int32_t, int> seen;
-    std::vector<int> round(ea[q].size());
-    int nround = 0;
-    for (size_t e = 0; e < ea[q].size(); ++e) {
-      round[e] = seen[ea[q][e].second]++;
-      nround = std::max(nround, round[e] + 1);
-    }
-    for (int rd = 0; rd < nround; ++rd) {
-      e_round.push_back(int64_t(e_src.size()));
-      for (size_t e = 0; e < ea[q].size(); ++e)
-        if (round[e] == rd) {
-          e_src.push_back(ea[q][e].first);
-          e_dst.push_back(ea[q][e].second);
-        }
-    }
-    e_rptr[q + 1] = int64_t(e_round.size());
-  }
-  e_round.push_back(int64_t(e_src.size()));
-  f.col_base = A.Upload(col_base);
-  f.a_ptr = A.Upload(a_ptr);
-  f.a_src = A.Upload(a_src);
-  f.a_dst = A.Upload(a_dst);
-  f.a_damp = A.Upload(a_damp);
-  f.e_rptr = A.Upload(e_rptr);
-  f.e_round = A.Upload(e_round);
-  f.e_src = A.Upload(e_src);
-  f.e_dst = A.Upload(e_dst);
-  std::vector<int64_t> linv_base(S.ns + 1, 0);
-  for (int s = 0; s < S.ns; ++s) linv_base[s + 1] = linv_base[s] + int64_t(T.npiv[s]) * tile * tile;
+  // ---- flattened assembly per (front, tile column), tree and solve maps
+  const FactorMaps M = BuildFactorMaps(S, T, pat);
+  const std::vector<int64_t>& linv_base = M.linv_base;
+  f.col_base = A.Upload(T.asm_col_base);
+  f.a_ptr = A.Upload(M.a_ptr);
+  f.a_src = A.Upload(M.a_src);
+  f.a_dst = A.Upload(M.a_dst);
+  f.a_damp = A.Upload(M.a_damp);
+  f.e_rptr = A.Upload(M.e_rptr);
+  f.e_round = A.Upload(M.e_round);
+  f.e_src = A.Upload(M.e_src);
+  f.e_dst = A.Upload(M.e_dst);
   f.linv_base = A.Upload(linv_base);
   f.trace = trace ? A.Zeros<unsigned long long>(4 * T.tasks.size()) : nullptr;
-  // ---- tree, solve maps
   f.rel_off = A.Upload(S.rel_off);
   f.rel = A.Upload(S.rel);
-  std::vector<int32_t> cptr(S.ns + 1, 0), clist;
-  for (int s = 0; s < S.ns; ++s) {
-    for (int c : S.sn_children[s]) clist.push_back(c);
-    cptr[s + 1] = int32_t(clist.size());
-  }
-  f.child_ptr = A.Upload(cptr);
-  f.child_list = A.Upload(clist);
+  f.child_ptr = A.Upload(M.child_ptr);
+  f.child_list = A.Upload(M.child_list);
   f.parent = A.Upload(S.sn_parent);
   f.idx_off = A.Upload(S.idx_off);
   f.idx = A.Upload(S.idx);
-  std::vector<int32_t> scalar_old(S.n);
-  for (int q = 0; q < S.nb; ++q) {
-    const int old = S.border[q];
-    for (int t = 0; t < pat.dim[old]; ++t) scalar_old[S.pstart[q] + t] = int32_t(pat.off[old] + t);
-  }
-  f.scalar_old = A.Upload(scalar_old);
+  f.scalar_old = A.Upload(M.scalar_old);
   f.tile_state = A.Zeros<int>(size_t(T.nstates));
   f.counters = A.Zeros<int>(2);
   fp.nflags = 2 * S.ns;

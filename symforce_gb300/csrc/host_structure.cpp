@@ -16,6 +16,7 @@
 #include <numeric>
 #include <queue>
 #include <set>
+#include <unordered_map>
 
 #include "common.h"
 
@@ -666,6 +667,82 @@ TaskPlan PlanTasks(const Symbolic& sym, int tile) {
     }
   }
   return T;
+}
+
+FactorMaps BuildFactorMaps(const Symbolic& S, const TaskPlan& T, const BlockPattern& pat) {
+  FactorMaps M;
+  const int tile = T.tile;
+  const std::vector<int32_t>& col_base = T.asm_col_base;
+  const int nslots = col_base[S.ns];
+  std::vector<std::vector<int64_t>> asrc(nslots);
+  std::vector<std::vector<int32_t>> adst(nslots), adamp(nslots);
+  std::vector<std::vector<std::pair<int64_t, int32_t>>> ea(nslots);  // (src, dst) in child order
+  for (int s = 0; s < S.ns; ++s) {
+    const int w = S.sn_w[s], m = S.sn_m[s], np = T.npiv[s];
+    auto col_tile = [&](int c) { return c < w ? c / tile : np + (c - w) / tile; };
+    for (int64_t q = S.asm_off[s]; q < S.asm_off[s + 1]; ++q) {
+      const auto& a = S.asms[q];
+      for (int r = 0; r < a.di; ++r)
+        for (int c = 0; c < a.dj; ++c) {
+          if (a.diag && r < c) continue;
+          const int fr = a.transpose ? a.row0 + c : a.row0 + r;
+          const int fc = a.transpose ? a.col0 + r : a.col0 + c;
+          const int slot = col_base[s] + col_tile(fc);
+          asrc[slot].push_back(a.src + int64_t(r) * a.dj + c);
+          adst[slot].push_back(int32_t(fr + int64_t(fc) * m));
+          adamp[slot].push_back(a.diag && r == c ? int32_t(pat.off[a.oi] + r) : -1);
+        }
+    }
+    for (int c : S.sn_children[s]) {
+      const int hc = S.sn_h[c], wc = S.sn_w[c], mc = S.sn_m[c];
+      const int32_t* rel = S.rel.data() + S.rel_off[c];
+      for (int qc = 0; qc < hc; ++qc) {
+        const int slot = col_base[s] + col_tile(rel[qc]);
+        for (int r = qc; r < hc; ++r)
+          ea[slot].push_back({S.sn_foff[c] + (wc + r) + int64_t(wc + qc) * mc,
+                              int32_t(rel[r] + int64_t(rel[qc]) * m)});
+      }
+    }
+  }
+  M.a_ptr.assign(nslots + 1, 0);
+  M.e_rptr.assign(nslots + 1, 0);
+  for (int q = 0; q < nslots; ++q) {
+    M.a_src.insert(M.a_src.end(), asrc[q].begin(), asrc[q].end());
+    M.a_dst.insert(M.a_dst.end(), adst[q].begin(), adst[q].end());
+    M.a_damp.insert(M.a_damp.end(), adamp[q].begin(), adamp[q].end());
+    M.a_ptr[q + 1] = int64_t(M.a_src.size());
+    // rounds: the k-th occurrence of a destination goes to round k (children keep their order)
+    std::unordered_map<int32_t, int> seen;
+    std::vector<int> round(ea[q].size());
+    int nround = 0;
+    for (size_t e = 0; e < ea[q].size(); ++e) {
+      round[e] = seen[ea[q][e].second]++;
+      nround = std::max(nround, round[e] + 1);
+    }
+    for (int rd = 0; rd < nround; ++rd) {
+      M.e_round.push_back(int64_t(M.e_src.size()));
+      for (size_t e = 0; e < ea[q].size(); ++e)
+        if (round[e] == rd) {
+          M.e_src.push_back(ea[q][e].first);
+          M.e_dst.push_back(ea[q][e].second);
+        }
+    }
+    M.e_rptr[q + 1] = int64_t(M.e_round.size());
+  }
+  M.e_round.push_back(int64_t(M.e_src.size()));
+  M.linv_base.assign(S.ns + 1, 0);
+  for (int s = 0; s < S.ns; ++s) M.linv_base[s + 1] = M.linv_base[s] + int64_t(T.npiv[s]) * tile * tile;
+  M.child_ptr.assign(S.ns + 1, 0);
+  for (int s = 0; s < S.ns; ++s) {
+    for (int c : S.sn_children[s]) M.child_list.push_back(c);
+    M.child_ptr[s + 1] = int32_t(M.child_list.size());
+  }
+  M.scalar_old.assign(S.n, 0);
+  for (int q = 0; q < S.nb; ++q) {
+    const int old = S.border[q];
+    for (int t = 0; t < pat.dim[old]; ++t) M.scalar_old[S.pstart[q] + t] = int32_t(pat.off[old] + t);
+  }
+  return M;
 }
 
 }  // namespace sfg

@@ -12,6 +12,7 @@ sfg::LinLayout g_layout;
 sfg::SchurLayout g_schur;
 sfg::Symbolic g_sym;
 sfg::TaskPlan g_plan;
+sfg::FactorMaps g_maps;
 
 template <typename V, typename O>
 void Put(const std::vector<V>& v, O* out) {
@@ -136,6 +137,7 @@ int shim_build_factor_plan(int which, int tile) {
   try {
     g_sym = sfg::Analyze(which == 0 ? g_layout.H : g_schur.Spat, SFG_ORDERING_NESTED_DISSECTION);
     g_plan = sfg::PlanTasks(g_sym, tile);
+    g_maps = sfg::BuildFactorMaps(g_sym, g_plan, which == 0 ? g_layout.H : g_schur.Spat);
     return 0;
   } catch (...) {
     return 1;
@@ -172,6 +174,51 @@ void shim_factor_arrays(int32_t* tasks, int32_t* npiv, int32_t* ntiles, int32_t*
   for (int s = 0; s < g_sym.ns; ++s) {
     for (int c : g_sym.sn_children[s]) child_list[q++] = c;
     child_ptr[s + 1] = q;
+  }
+}
+
+// sizes of the maps arrays: 0 a_ptr, 1 a_src, 2 e_rptr, 3 e_round, 4 e_src, 5 idx_off, 6 idx,
+// 7 rel_off, 8 rel, 9 sn_foff, 10 scalar_old, 11 col_base; 12 front pool entries, 13 n
+void shim_maps_sizes(int64_t* out) {
+  out[0] = int64_t(g_maps.a_ptr.size());
+  out[1] = int64_t(g_maps.a_src.size());
+  out[2] = int64_t(g_maps.e_rptr.size());
+  out[3] = int64_t(g_maps.e_round.size());
+  out[4] = int64_t(g_maps.e_src.size());
+  out[5] = int64_t(g_sym.idx_off.size());
+  out[6] = int64_t(g_sym.idx.size());
+  out[7] = int64_t(g_sym.rel_off.size());
+  out[8] = int64_t(g_sym.rel.size());
+  out[9] = int64_t(g_sym.sn_foff.size());
+  out[10] = int64_t(g_maps.scalar_old.size());
+  out[11] = int64_t(g_plan.asm_col_base.size());
+  out[12] = g_sym.front_pool;
+  out[13] = g_sym.n;
+}
+
+// 64-bit: 0 a_ptr, 1 a_src, 2 e_rptr, 3 e_round, 4 e_src, 5 idx_off, 7 rel_off, 9 sn_foff;
+// 32-bit: 21 a_dst, 22 a_damp, 24 e_dst, 26 idx, 28 rel, 30 scalar_old, 31 col_base
+void shim_maps_i64(int which, int64_t* out) {
+  switch (which) {
+    case 0: Put(g_maps.a_ptr, out); break;
+    case 1: Put(g_maps.a_src, out); break;
+    case 2: Put(g_maps.e_rptr, out); break;
+    case 3: Put(g_maps.e_round, out); break;
+    case 4: Put(g_maps.e_src, out); break;
+    case 5: Put(g_sym.idx_off, out); break;
+    case 7: Put(g_sym.rel_off, out); break;
+    case 9: Put(g_sym.sn_foff, out); break;
+  }
+}
+void shim_maps_i32(int which, int32_t* out) {
+  switch (which) {
+    case 21: Put(g_maps.a_dst, out); break;
+    case 22: Put(g_maps.a_damp, out); break;
+    case 24: Put(g_maps.e_dst, out); break;
+    case 26: Put(g_sym.idx, out); break;
+    case 28: Put(g_sym.rel, out); break;
+    case 30: Put(g_maps.scalar_old, out); break;
+    case 31: Put(g_plan.asm_col_base, out); break;
   }
 }
 

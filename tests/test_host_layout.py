@@ -328,3 +328,136 @@ def test_factor_task_plan_is_deadlock_free(shim, tile):
     c2 = r.to_c()
     assert shim.shim_build(C.byref(c2)) == 0
     _replay_tasks(*_factor_plan(shim, 0, tile), tile)
+
+
+def _maps(lib):
+    sizes = _arr(14, np.int64)
+    lib.shim_maps_sizes(_ptr(sizes))
+    n64 = {0: 0, 1: 1, 2: 2, 3: 3, 4: 4, 5: 5, 7: 7, 9: 9}
+    n32 = {21: 1, 22: 1, 24: 4, 26: 6, 28: 8, 30: 10, 31: 11}
+    out = {}
+    for k, sz in n64.items():
+        out[k] = _arr(sizes[sz], np.int64)
+        lib.shim_maps_i64(k, _ptr(out[k]))
+    for k, sz in n32.items():
+        out[k] = _arr(sizes[sz], np.int32)
+        lib.shim_maps_i32(k, _ptr(out[k]))
+    return out, int(sizes[12]), int(sizes[13])
+
+
+def _dense_from_pattern(colptr, rows, boff, off, rng):
+    """Random diagonally dominant symmetric values on a block pattern (lower blocks row-major,
+    diagonal blocks stored full) and the dense matrix they stand for."""
+    dims = np.diff(off)
+    vals = np.zeros(max(int(boff[q] + dims[rows[q]] * dims[j]) for j in range(len(colptr) - 1)
+                        for q in range(colptr[j], colptr[j + 1])))
+    n = int(off[-1])
+    A = np.zeros((n, n))
+    for j in range(len(colptr) - 1):
+        for q in range(colptr[j], colptr[j + 1]):
+            i = int(rows[q])
+            blk = rng.normal(size=(dims[i], dims[j]))
+            if i == j:
+                blk = np.tril(blk) + np.tril(blk, -1).T
+            vals[boff[q]:boff[q] + blk.size] = blk.ravel()
+            A[off[i]:off[i] + dims[i], off[j]:off[j] + dims[j]] = blk
+            A[off[j]:off[j] + dims[j], off[i]:off[i] + dims[i]] = blk.T
+    shift = np.abs(A).sum(axis=1) + 1.0  # dominance through the damping
+    return vals, A, shift
+
+
+def _replay_numeric(plan, mp, pool, n, vals, damping, b):
+    """The multifrontal LDL^T and solve of the device, replayed in numpy from the host maps: each
+    front assembled from the matrix values (+ damping on the diagonal) and its children's update
+    blocks, its pivot columns factored, then the forward and backward solves by front."""
+    tasks, npiv, ntiles, parent, w, m, cptr, clist = plan
+    col_base, a_ptr, a_src, a_dst, a_damp = mp[31], mp[0], mp[1], mp[21], mp[22]
+    e_rptr, e_round, e_src, e_dst = mp[2], mp[3], mp[4], mp[24]
+    idx_off, idx, rel_off, rel, foff, scalar_old = mp[5], mp[26], mp[7], mp[28], mp[9], mp[30]
+    F = np.zeros(pool)
+    ns = len(w)
+    fronts = []
+    for s in range(ns):
+        ms, ws, base = int(m[s]), int(w[s]), int(foff[s])
+        for slot in range(col_base[s], col_base[s + 1]):
+            for e in range(a_ptr[slot], a_ptr[slot + 1]):
+                v = vals[a_src[e]] + (damping[a_damp[e]] if a_damp[e] >= 0 else 0.0)
+                F[base + a_dst[e]] = v
+            for rd in range(e_rptr[slot], e_rptr[slot + 1]):
+                for e in range(e_round[rd], e_round[rd + 1]):
+                    F[base + e_dst[e]] += F[e_src[e]]
+        Fm = F[base:base + ms * ms].reshape(ms, ms).T.copy()  # column-major front
+        Fm = np.tril(Fm) + np.tril(Fm, -1).T
+        for j in range(ws):
+            col = Fm[j + 1:, j].copy()
+            lj = col / Fm[j, j]
+            Fm[j + 1:, j + 1:] -= np.outer(lj, col)
+            Fm[j + 1:, j] = lj
+        F[base:base + ms * ms] = Fm.T.ravel()
+        fronts.append(Fm)
+    ycon, ysave, xperm, x = np.zeros(rel_off[-1]), np.zeros(idx_off[-1]), np.zeros(n), np.zeros(n)
+    for s in range(ns):
+        ms, ws = int(m[s]), int(w[s])
+        ids = idx[idx_off[s]:idx_off[s] + ms]
+        xs = np.zeros(ms)
+        xs[:ws] = b[scalar_old[ids[:ws]]]
+        for c in clist[cptr[s]:cptr[s + 1]]:
+            hc = int(m[c] - w[c])
+            xs[rel[rel_off[c]:rel_off[c] + hc]] += ycon[rel_off[c]:rel_off[c] + hc]
+        L = np.tril(fronts[s][:ws, :ws], -1) + np.eye(ws)
+        y = np.linalg.solve(L, xs[:ws])
+        xs[ws:] -= fronts[s][ws:, :ws] @ y
+        ysave[idx_off[s]:idx_off[s] + ws] = y
+        ycon[rel_off[s]:rel_off[s] + ms - ws] = xs[ws:]
+    for s in reversed(range(ns)):
+        ms, ws = int(m[s]), int(w[s])
+        ids = idx[idx_off[s]:idx_off[s] + ms]
+        L = np.tril(fronts[s][:ws, :ws], -1) + np.eye(ws)
+        z = ysave[idx_off[s]:idx_off[s] + ws] / np.diag(fronts[s])[:ws] - fronts[s][ws:, :ws].T @ xperm[ids[ws:]]
+        xp = np.linalg.solve(L.T, z)
+        xperm[ids[:ws]] = xp
+        x[scalar_old[ids[:ws]]] = xp
+    return x
+
+
+def test_factor_maps_solve_the_system(shim):
+    """The assembly lists, extend-add rounds and solve maps of the factorization plan, replayed in
+    numpy on random values, solve (A + diag(damping)) x = b as a dense solve does (the reduced BA
+    system with several fronts, and a 2D localization Hessian)."""
+    rng = np.random.default_rng(3)
+
+    def reduced_ba():
+        p = synth.bundle_adjustment(num_cameras=80, num_points=2000, num_observations=8000, seed=5)
+        c = p.to_c()
+        assert shim.shim_build(C.byref(c)) == 0 and shim.shim_build_schur() == 0
+        (nbk, _, _, _, _), a64, a32 = _schur_arrays(shim)
+        sizes = _arr(7, np.int64)
+        shim.shim_sizes(_ptr(sizes))
+        nkeys, nblocks = int(sizes[6]), int(sizes[5])
+        hcol, hrows, hboff, toff = _arr(nkeys + 1, np.int64), _arr(nblocks, np.int32), _arr(nblocks, np.int64), \
+            _arr(nkeys + 1, np.int64)
+        shim.shim_pattern(_ptr(hcol), _ptr(hrows), _ptr(hboff), _ptr(toff))
+        return 1, a64[11], a32[6], a64[12], toff[:nbk + 1]
+
+    def localization_hessian():
+        c = synth.robot_2d(num_poses=200, num_landmarks=10, seed=8).to_c()
+        assert shim.shim_build(C.byref(c)) == 0
+        sizes = _arr(7, np.int64)
+        shim.shim_sizes(_ptr(sizes))
+        nkeys, nblocks = int(sizes[6]), int(sizes[5])
+        colptr, rows, boff, off = _arr(nkeys + 1, np.int64), _arr(nblocks, np.int32), _arr(nblocks, np.int64), \
+            _arr(nkeys + 1, np.int64)
+        shim.shim_pattern(_ptr(colptr), _ptr(rows), _ptr(boff), _ptr(off))
+        return 0, colptr, rows, boff, off
+
+    for case in (reduced_ba, localization_hessian):
+        which, colptr, rows, boff, off = case()
+        for tile in (16, 32):
+            plan = _factor_plan(shim, which, tile)
+            mp, pool, n = _maps(shim)
+            assert n == int(off[-1])
+            vals, A, shift = _dense_from_pattern(colptr, rows, boff, off, rng)
+            b = rng.normal(size=n)
+            x = _replay_numeric(plan, mp, pool, n, vals, shift, b)
+            ref = np.linalg.solve(A + np.diag(shift), b)
+            np.testing.assert_allclose(x, ref, rtol=1e-9, atol=1e-12)
