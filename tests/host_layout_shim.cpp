@@ -13,6 +13,7 @@ sfg::SchurLayout g_schur;
 sfg::Symbolic g_sym;
 sfg::TaskPlan g_plan;
 sfg::FactorMaps g_maps;
+sfg::PrecondLayout g_pre;
 
 template <typename V, typename O>
 void Put(const std::vector<V>& v, O* out) {
@@ -220,6 +221,30 @@ void shim_maps_i32(int which, int32_t* out) {
     case 30: Put(g_maps.scalar_old, out); break;
     case 31: Put(g_plan.asm_col_base, out); break;
   }
+}
+
+// Camera blocks of the reduced system (the PCG forms) of the Schur plan built last; 0 on success.
+int shim_build_precond() {
+  try {
+    g_pre = sfg::BuildPrecondLayout(g_problem, g_schur);
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
+// camera blocks, stored 9 x 9 group blocks, group-row entries
+void shim_precond_sizes(int64_t* out) {
+  out[0] = g_pre.ng;
+  out[1] = int64_t(g_pre.blk_row.size());
+  out[2] = int64_t(g_pre.gent.size() / 2);
+}
+
+void shim_precond_arrays(int32_t* gidx, int64_t* blk_off, int32_t* gptr, int32_t* gent) {
+  Put(g_pre.gidx, gidx);
+  Put(g_pre.blk_off, blk_off);
+  Put(g_pre.gptr, gptr);
+  Put(g_pre.gent, gent);
 }
 
 }  // extern "C"

@@ -37,7 +37,7 @@ def shim(tmp_path_factory):
         pytest.skip("g++ or the CUDA headers are not available")
     out = tmp_path_factory.mktemp("shim") / "libhostshim.so"
     srcs = [ROOT / "tests" / "host_layout_shim.cpp"] + [CSRC / f for f in
-                                                        ("host_structure.cpp", "host_layout.cpp")]
+                                                        ("host_structure.cpp", "host_layout.cpp", "host_pcg.cpp")]
     subprocess.run([gxx, "-O1", "-std=c++17", "-shared", "-fPIC", f"-I{cuda_inc}", f"-I{ROOT / 'include'}",
                     f"-I{CSRC}", *map(str, srcs), "-o", str(out)], check=True)
     lib = C.CDLL(str(out))
@@ -461,3 +461,59 @@ def test_factor_maps_solve_the_system(shim):
             x = _replay_numeric(plan, mp, pool, n, vals, shift, b)
             ref = np.linalg.solve(A + np.diag(shift), b)
             np.testing.assert_allclose(x, ref, rtol=1e-9, atol=1e-12)
+
+
+def test_camera_block_rows_give_the_reduced_system_product(shim):
+    """The PCG camera-block layout (symforce_gb300/csrc/host_pcg.cpp): 9 x 9 group blocks gathered
+    from S and each group row's entries (stored block, neighbour, transposed) give S x as the dense
+    product does, and never read the upper triangle of a diagonal key block (not kept current on
+    the device; NaN here)."""
+    p = synth.bundle_adjustment(num_cameras=40, num_points=900, num_observations=3600, seed=9)
+    c = p.to_c()
+    assert shim.shim_build(C.byref(c)) == 0 and shim.shim_build_schur() == 0
+    assert shim.shim_build_precond() == 0
+    (nbk, _, nB, _, nS), a64, a32 = _schur_arrays(shim)
+    sizes = _arr(7, np.int64)
+    shim.shim_sizes(_ptr(sizes))
+    nkeys, nblocks = int(sizes[6]), int(sizes[5])
+    hcol, hrows, hboff, toff = _arr(nkeys + 1, np.int64), _arr(nblocks, np.int32), _arr(nblocks, np.int64), \
+        _arr(nkeys + 1, np.int64)
+    shim.shim_pattern(_ptr(hcol), _ptr(hrows), _ptr(hboff), _ptr(toff))
+    dims = np.diff(toff[:nbk + 1])
+    scol, srow, sboff = a64[11], a32[6], a64[12]
+    rng = np.random.default_rng(4)
+    Sv = np.zeros(nS)
+    Sd = np.zeros((nB, nB))
+    for j in range(nbk):
+        for q in range(scol[j], scol[j + 1]):
+            i = int(srow[q])
+            blk = rng.normal(size=(dims[i], dims[j]))
+            if i == j:
+                blk = np.tril(blk) + np.tril(blk, -1).T
+                stored = blk.copy()
+                stored[np.triu_indices(dims[i], 1)] = np.nan
+            else:
+                stored = blk
+            Sv[sboff[q]:sboff[q] + blk.size] = stored.ravel()
+            Sd[toff[i]:toff[i] + dims[i], toff[j]:toff[j] + dims[j]] = blk
+            Sd[toff[j]:toff[j] + dims[j], toff[i]:toff[i] + dims[i]] = blk.T
+    ps = _arr(3, np.int64)
+    shim.shim_precond_sizes(_ptr(ps))
+    ng, nbl, nent = (int(x) for x in ps)
+    gidx, blk_off = _arr(ng * 9, np.int32), _arr(nbl * 81, np.int64)
+    gptr, gent = _arr(ng + 1, np.int32), _arr(2 * nent, np.int32)
+    shim.shim_precond_arrays(_ptr(gidx), _ptr(blk_off), _ptr(gptr), _ptr(gent))
+    gidx = gidx.reshape(ng, 9)
+    assert sorted(gidx[gidx >= 0].tolist()) == list(range(nB))  # every scalar in one block
+    Sb = np.where(blk_off >= 0, Sv[np.maximum(blk_off, 0)], 0.0).reshape(nbl, 9, 9)
+    x = rng.normal(size=nB)
+    xg = np.where(gidx >= 0, x[np.maximum(gidx, 0)], 0.0)
+    y = np.zeros((ng, 9))
+    for g in range(ng):
+        for e in range(gptr[g], gptr[g + 1]):
+            blk, nb = int(gent[2 * e]), int(gent[2 * e + 1])
+            B = Sb[blk].T if nb & 1 else Sb[blk]
+            y[g] += B @ xg[nb >> 1]
+    ref = Sd @ x
+    ok = gidx >= 0
+    np.testing.assert_allclose(y[ok], ref[gidx[ok]], rtol=1e-12, atol=1e-12)
