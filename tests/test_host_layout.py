@@ -517,3 +517,48 @@ def test_camera_block_rows_give_the_reduced_system_product(shim):
     ref = Sd @ x
     ok = gidx >= 0
     np.testing.assert_allclose(y[ok], ref[gidx[ok]], rtol=1e-12, atol=1e-12)
+
+
+def _random_pose3_graph(rng, nposes, nbetween, nrange):
+    """A Pose3 factor graph of random structure (between factors on random pairs, a prior on every
+    pose, range factors on random poses): several components, uneven degrees."""
+    kt = [A.SFG_KEY_POSE3] * nposes
+    pairs = []
+    while len(pairs) < nbetween:
+        i, j = rng.integers(0, nposes, size=2)
+        if i != j:
+            pairs.append((int(i), int(j)))
+    batches = [A.Batch(A.SFG_FACTOR_BETWEEN_POSE3, np.array(pairs, dtype=np.int32),
+                       np.zeros((nbetween, A.FACTOR_DIMS[A.SFG_FACTOR_BETWEEN_POSE3][1]))),
+               A.Batch(A.SFG_FACTOR_PRIOR_POSE3, np.arange(nposes, dtype=np.int32)[:, None],
+                       np.zeros((nposes, A.FACTOR_DIMS[A.SFG_FACTOR_PRIOR_POSE3][1]))),
+               A.Batch(A.SFG_FACTOR_RANGE_POSE3, rng.integers(0, nposes, size=(nrange, 1)).astype(np.int32),
+                       np.zeros((nrange, A.FACTOR_DIMS[A.SFG_FACTOR_RANGE_POSE3][1])))]
+    values = np.tile(np.array([0, 0, 0, 1, 0, 0, 0], dtype=np.float64), nposes)
+    return A.ProblemArrays(key_types=kt, batches=batches, values=values)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_plans_of_random_factor_graphs(shim, seed):
+    """Random Pose3 graphs: the scatter plan replays to the factor counts, the task list replays
+    without a blocked wait and the factorization maps solve the system, at both tile sizes."""
+    rng = np.random.default_rng(100 + seed)
+    p = _random_pose3_graph(rng, nposes=int(rng.integers(20, 90)), nbetween=int(rng.integers(30, 200)),
+                            nrange=int(rng.integers(0, 60)))
+    _replay(shim, p)
+    c = p.to_c()
+    assert shim.shim_build(C.byref(c)) == 0
+    sizes = _arr(7, np.int64)
+    shim.shim_sizes(_ptr(sizes))
+    nkeys, nblocks = int(sizes[6]), int(sizes[5])
+    colptr, rows, boff, off = _arr(nkeys + 1, np.int64), _arr(nblocks, np.int32), _arr(nblocks, np.int64), \
+        _arr(nkeys + 1, np.int64)
+    shim.shim_pattern(_ptr(colptr), _ptr(rows), _ptr(boff), _ptr(off))
+    for tile in (16, 32):
+        plan = _factor_plan(shim, 0, tile)
+        _replay_tasks(*plan, tile)
+        mp, pool, n = _maps(shim)
+        vals, Ad, shift = _dense_from_pattern(colptr, rows, boff, off, rng)
+        b = rng.normal(size=n)
+        x = _replay_numeric(plan, mp, pool, n, vals, shift, b)
+        np.testing.assert_allclose(x, np.linalg.solve(Ad + np.diag(shift), b), rtol=1e-9, atol=1e-12)
