@@ -12,10 +12,11 @@ from pathlib import Path
 
 import numpy as np
 import pytest
-import sympy as sp
 
-from symforce_gb300 import _cabi as A
-from symforce_gb300 import codegen
+sp = pytest.importorskip("sympy")
+
+from symforce_gb300 import _cabi as A  # noqa: E402
+from symforce_gb300 import codegen  # noqa: E402
 
 ROOT = Path(__file__).resolve().parents[1]
 CSRC = ROOT / "symforce_gb300" / "csrc"
