@@ -54,11 +54,33 @@ def odometry_pose2_residual(keys, c):
     return sp.Matrix([c[2] * (sp.sqrt(dx * dx + dy * dy + c[1]) - c[0])])
 
 
+def snavely_residual(keys, c):
+    """The bundle-adjustment reprojection with Cauchy whitening (symforce/examples/
+    bundle_adjustment_in_the_large/bundle_adjustment_in_the_large.py:18-63, symforce/opt/
+    noise_models.py:318-428 at alpha -> 0); consts: pixel (2), eps, delta."""
+    cam, intr, X = keys
+    qx, qy, qz, qw = cam[0], cam[1], cam[2], cam[3]
+    R = sp.Matrix([[1 - 2 * (qy * qy + qz * qz), 2 * (qx * qy - qz * qw), 2 * (qx * qz + qy * qw)],
+                   [2 * (qx * qy + qz * qw), 1 - 2 * (qx * qx + qz * qz), 2 * (qy * qz - qx * qw)],
+                   [2 * (qx * qz - qy * qw), 2 * (qy * qz + qx * qw), 1 - 2 * (qx * qx + qy * qy)]])
+    pc = R * sp.Matrix(X[0:3, 0]) + sp.Matrix(cam[4:7, 0])
+    u, v = -pc[0] / pc[2], -pc[1] / pc[2]
+    r2 = u * u + v * v
+    g = 1 + intr[1] * r2 + intr[2] * r2 * r2
+    e0, e1 = intr[0] * g * u - c[0], intr[0] * g * v - c[1]
+    n2 = e0 * e0 + e1 * e1 + c[2]
+    rho2 = 2 * c[3] ** 2 * sp.log(1 + n2 / (2 * c[3] ** 2))
+    s = sp.sqrt(rho2) / sp.sqrt(n2)
+    return sp.Matrix([s * e0, s * e1])
+
+
 CASES = {
     # name: (kind, key types, consts, residual)
     "range": (A.SFG_FACTOR_RANGE_POSE3, [A.SFG_KEY_POSE3], 6, codegen.range_pose3_residual),
     "prior": (A.SFG_FACTOR_PRIOR_POSE3, [A.SFG_KEY_POSE3], 14, prior_pose3_residual),
     "odometry": (A.SFG_FACTOR_ODOMETRY_POSE2, [A.SFG_KEY_POSE2] * 2, 3, odometry_pose2_residual),
+    "snavely": (A.SFG_FACTOR_SNAVELY_REPROJECTION, [A.SFG_KEY_POSE3, A.SFG_KEY_VEC3, A.SFG_KEY_VEC3], 4,
+                snavely_residual),
 }
 
 
@@ -107,6 +129,21 @@ def _inputs(name, rng):
         prior_q = np.array(_qmul(list(x0[:4]), list(dq)), dtype=float)
         c = np.concatenate([prior_q, x0[4:] + rng.normal(size=3) * 0.1, 1 / (0.05 + rng.random(6)), [1e-9]])
         x = [x0]
+    elif name == "snavely":
+        q = _quat(rng)
+        X = rng.uniform(-5, 5, size=3)
+        qx, qy, qz, qw = q
+        R = np.array([[1 - 2 * (qy * qy + qz * qz), 2 * (qx * qy - qz * qw), 2 * (qx * qz + qy * qw)],
+                      [2 * (qx * qy + qz * qw), 1 - 2 * (qx * qx + qz * qz), 2 * (qy * qz - qx * qw)],
+                      [2 * (qx * qz - qy * qw), 2 * (qy * qz + qx * qw), 1 - 2 * (qx * qx + qy * qy)]])
+        t = -R @ X + np.array([rng.normal(), rng.normal(), -20.0])  # the point 20 m in front
+        intr = np.array([rng.uniform(400, 600), rng.normal() * 1e-3, rng.normal() * 1e-3])
+        pc = R @ X + t
+        uv = -pc[:2] / pc[2]
+        g = 1 + intr[1] * uv @ uv + intr[2] * (uv @ uv) ** 2
+        pix = intr[0] * g * uv + rng.normal(size=2) * 3
+        x = [np.concatenate([q, t]), intr, X]
+        c = np.array([pix[0], pix[1], 1e-9, 1.0])
     else:
         x = []
         for _ in range(2):
