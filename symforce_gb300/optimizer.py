@@ -101,6 +101,14 @@ class OptimizationStats:
         return self.iterations[self.best_index].new_error
 
 
+def csc_lower_to_dense(colptr: np.ndarray, rowidx: np.ndarray, vals: np.ndarray, n: int) -> np.ndarray:
+    """The dense lower triangle (upper part zero) of a compressed-column lower matrix."""
+    H = np.zeros((n, n))
+    cols = np.repeat(np.arange(n), np.diff(np.asarray(colptr, dtype=np.int64)))
+    H[np.asarray(rowidx, dtype=np.int64), cols] = vals
+    return H
+
+
 class Optimizer:
     """GPU Levenberg-Marquardt optimizer for one problem structure (create once, optimize many)."""
 
@@ -217,6 +225,16 @@ class Optimizer:
         hv = np.zeros(nnz.value)
         _check(lib().sfg_hessian_lower(self._h, C.byref(nnz), A.iptr(colptr), A.iptr(rowidx), A.dptr(hv)))
         return dict(residual=res, rhs=rhs, error=err.value, colptr=colptr, rowidx=rowidx, hvals=hv)
+
+    def linearize_dense(self, values: np.ndarray | None = None) -> dict:
+        """DenseLinearizer's linearization (symforce/opt/dense_linearizer.h, DenseLinearization in
+        symforce/opt/linearization.h:27-73): residual, dense hessian_lower (lower triangle filled,
+        upper zero), rhs and error, from the device linearization.  The Jacobian is not formed on the
+        device (the kernels accumulate J^T J per factor), so include_jacobians has no counterpart."""
+        lin = self.linearize(values)
+        return dict(residual=lin["residual"], rhs=lin["rhs"], error=lin["error"],
+                    hessian_lower=csc_lower_to_dense(lin["colptr"], lin["rowidx"], lin["hvals"],
+                                                     self.tangent_dim))
 
     def compute_covariances(self, values: np.ndarray, num_keys: int) -> dict:
         """Optimizer::ComputeCovariances with a block-diagonal C (symforce/opt/optimizer.tcc:176-199,

@@ -84,3 +84,16 @@ def test_create_without_device_fails_loudly():
 def test_graft_entry_build_imports():
     import __graft_entry__ as g
     g.build()
+
+
+def test_csc_lower_to_dense_matches_scipy():
+    """The DenseLinearizer adapter's conversion of the exported CSC hessian_lower."""
+    sparse = pytest.importorskip("scipy.sparse")
+    from symforce_gb300.optimizer import csc_lower_to_dense
+
+    M = sparse.random(40, 40, density=0.2, random_state=1, format="csc")
+    L = sparse.tril(M + M.T + sparse.eye(40), format="csc")
+    L.sort_indices()
+    H = csc_lower_to_dense(L.indptr, L.indices, L.data, 40)
+    np.testing.assert_array_equal(H, L.toarray())
+    assert np.count_nonzero(np.triu(H, 1)) == 0
