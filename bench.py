@@ -15,6 +15,15 @@ device timestamps of the run; lower is better.  The same line reports:
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--no-scale] [--no-batched] [--no-cpu-baseline]
 
+Profiling mode (no JSON line; the command the ncu summaries under profiles/ give):
+
+    SFG_EAGER=1 python bench.py --profile-workload ba_50_7800 --profile-form plain --profile-runs 2
+                                [--profile-iterations N]
+
+runs `--profile-runs` optimize calls of one form on one workload and prints one line per call.
+SFG_EAGER=1 launches each kernel on its own (profilers do not attribute the kernels inside graphs
+with conditional nodes).
+
 `--impl reference` times the CPU restatement of the reference's sym::Optimizer (the reference
 itself cannot be compiled here: its Eigen / METIS dependencies are absent) on the host cores.
 """
@@ -556,6 +565,23 @@ def run_gb300(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_profile(args) -> None:
+    """A few optimize calls of one form on one workload, for profilers."""
+    from symforce_gb300.optimizer import Optimizer
+    w = workloads.get(args.profile_workload)
+    p = w.problem()
+    params = w.params()
+    if args.profile_iterations > 0:
+        params.iterations = args.profile_iterations
+    opt = Optimizer(p, _form_params(params, args.profile_form), _make_form(w, args.profile_form, 0))
+    for _ in range(args.profile_runs):
+        _, stats = opt.optimize(p.values)
+        print(f"{args.profile_workload} {args.profile_form}: {len(stats.iterations)} records, best "
+              f"{stats.best_error:.10g}, {stats.device_ms:.3f} ms, {stats.kernel_launches} kernels",
+              flush=True)
+    opt.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -567,8 +593,16 @@ def main() -> None:
     ap.add_argument("--scale-workload", default=SCALE_WORKLOAD,
                     help="large workload of the scale section (ba_1000_200k or ba_10k_1m)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched Pose3 chains")
+    ap.add_argument("--profile-workload", default=None,
+                    help="profiling mode: run --profile-runs optimize calls of one form on this workload")
+    ap.add_argument("--profile-form", default="plain", choices=list(FORMS))
+    ap.add_argument("--profile-runs", type=int, default=2)
+    ap.add_argument("--profile-iterations", type=int, default=-1,
+                    help="LM iteration cap in profiling mode (default: the workload's)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_workload:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

@@ -35,7 +35,8 @@ enum {
   SFG_ERR_STRUCTURE = 4,        /* structure not supported (e.g. Schur block C not block diagonal) */
   SFG_ERR_DEVICE_STATUS = 5,    /* a device loop hit its hard cap or saw non-finite values */
   SFG_ERR_OUT_OF_MEMORY = 6,
-  SFG_ERR_CAPACITY = 7          /* a caller-provided output buffer is too small */
+  SFG_ERR_CAPACITY = 7,         /* a caller-provided output buffer is too small */
+  SFG_ERR_NUMERICAL = 8         /* sfg_dense_ldlt_solve_noalloc: a zero or non-finite pivot */
 };
 
 /* Optimization status and LM failure reasons: same integer values as the reference LCM enums
@@ -394,9 +395,11 @@ int32_t sfg_selftest_wait_cap(int32_t device, int32_t* device_status, double* ms
  * held on every GPU that loads the library until the process exits): n may be at most 512, larger
  * n is rejected with SFG_ERR_INVALID_ARGUMENT.  The call allocates nothing.  Its first call on a
  * device looks up the arrays' device addresses (cudaGetSymbolAddress), so make that first call
- * before any stream capture.  The call returns when the solve has finished on `stream`.  Every
- * call shares the same arrays, so calls that overlap on the GPU (other threads, other streams)
- * race; each call reinitializes everything it reads. */
+ * before any stream capture.  The call is synchronous: it copies the device status word to the
+ * host and waits for `stream` (cudaStreamSynchronize) before it returns.  A zero or non-finite
+ * pivot D (A singular, or not factorizable without pivoting) or a non-finite x returns
+ * SFG_ERR_NUMERICAL.  Every call shares the same arrays, so calls that overlap on the GPU (other
+ * threads, other streams) race; each call reinitializes everything it reads. */
 int32_t sfg_dense_ldlt_solve_noalloc(int32_t n, const double* A, int64_t lda, const double* b,
                                      double* x, void* stream);
 

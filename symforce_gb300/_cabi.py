@@ -13,6 +13,8 @@ import numpy as np
 
 # status codes / enums (include/sfgpu.h)
 SFG_OK = 0
+(SFG_ERR_INVALID_ARGUMENT, SFG_ERR_CUDA, SFG_ERR_NO_DEVICE, SFG_ERR_STRUCTURE, SFG_ERR_DEVICE_STATUS,
+ SFG_ERR_OUT_OF_MEMORY, SFG_ERR_CAPACITY, SFG_ERR_NUMERICAL) = range(1, 9)
 SFG_STATUS_INVALID, SFG_STATUS_SUCCESS, SFG_STATUS_HIT_ITERATION_LIMIT, SFG_STATUS_FAILED = 0, 1, 2, 3
 SFG_FAILURE_INVALID, SFG_FAILURE_LAMBDA_OUT_OF_BOUNDS, SFG_FAILURE_INITIAL_ERROR_NOT_FINITE = 0, 1, 2
 SFG_LAMBDA_UPDATE_STATIC, SFG_LAMBDA_UPDATE_DYNAMIC = 1, 2

@@ -144,6 +144,19 @@ __global__ void PrepareKernel(int n, const double* A, int64_t lda) {
   }
 }
 
+// After the solve: a zero or non-finite pivot (D, on the front's diagonal) or a non-finite solution
+// entry marks the factorization as failed (error word 3; the capped waits use 1 and 2).  The
+// unpivoted LDL^T then divided by zero or carried an overflow into x.
+constexpr int kNoAllocBadPivot = 3;
+__global__ void CheckPivotsKernel(int n, const double* x) {
+  bool bad = false;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const double d = g_front[q + int64_t(q) * n];
+    bad = bad || d == 0.0 || !isfinite(d) || !isfinite(x[q]);
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0 && g_meta.error == 0) g_meta.error = kNoAllocBadPivot;
+}
+
 int TaskCount(int nt) {
   int t = 0;
   for (int k = 0; k < nt; ++k) t += 1 + (nt - k - 1) + (nt - k - 1) * (nt - k) / 2;
@@ -225,19 +238,25 @@ extern "C" int32_t sfg_dense_ldlt_solve_noalloc(int32_t n, const double* A, int6
                             std::max(1, std::min(ntasks, sms * 8)), st);
   sfg::LaunchSolve<double>(f, s->front, s->linv, b, s->vec + 2 * kMaxN, s->vec, s->vec + kMaxN, x,
                            std::max(1, std::min(2, sms)), st);
+  CheckPivotsKernel<<<1, 256, 0, st>>>(n, x);
   rc = cudaGetLastError();
   if (rc != cudaSuccess) {
     sfg::g_last_error = std::string("sfg_dense_ldlt_solve_noalloc launch: ") + cudaGetErrorString(rc);
     return SFG_ERR_CUDA;
   }
-  // The call returns after the solve has finished, so that a capped dependency wait in the
-  // factorization can be reported as a status.
+  // The call is synchronous: it copies the device status word to the host and waits for `stream`
+  // before it returns, so that a capped dependency wait or a failed pivot is reported as a status.
   int err = 0;
   rc = cudaMemcpyAsync(&err, &m->error, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (rc == cudaSuccess) rc = cudaStreamSynchronize(st);
   if (rc != cudaSuccess) {
     sfg::g_last_error = std::string("sfg_dense_ldlt_solve_noalloc: ") + cudaGetErrorString(rc);
     return SFG_ERR_CUDA;
+  }
+  if (err == kNoAllocBadPivot) {
+    sfg::g_last_error = "sfg_dense_ldlt_solve_noalloc: zero or non-finite pivot (A is singular or "
+                        "not factorizable without pivoting)";
+    return SFG_ERR_NUMERICAL;
   }
   if (err != 0) {
     sfg::g_last_error = "sfg_dense_ldlt_solve_noalloc: a device wait hit its cap";

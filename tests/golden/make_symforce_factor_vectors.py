@@ -1,7 +1,6 @@
 """Generate tests/golden/factor_vectors.json from the reference's own symbolic factor definitions.
 
-Imports symforce (sympy back end) from the reference checkout given as argv[1] (default: the
-reference path used when the fixtures were made), builds each residual exactly as the reference
+Imports symforce (sympy back end) from the reference checkout given as argv[1] (required), builds each residual exactly as the reference
 defines it, differentiates it with symforce's tangent-space Jacobian helper (the same helper the
 reference's `with_linearization` codegen uses), and evaluates residual and Jacobian at seeded random
 inputs with 60-digit arithmetic.  Run once from the repository root; the JSON is committed and the
@@ -19,7 +18,9 @@ from pathlib import Path
 
 import numpy as np
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) < 2:
+    sys.exit("usage: make_symforce_factor_vectors.py /path/to/symforce  (the reference checkout)")
+REF = Path(sys.argv[1])
 sys.path.insert(0, str(REF))
 sys.path.insert(0, str(REF / "gen" / "python"))
 

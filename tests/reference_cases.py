@@ -84,3 +84,10 @@ def pose_smoothing(initial_values: np.ndarray, num_keys: int = 10) -> A.ProblemA
 
 POSE_SMOOTHING_PARAMS = dict(iterations=50, early_exit_min_reduction=0.0001)
 POSE_SMOOTHING_EXPECTED = dict(last_iteration=12, lambda_approx=(0.0039, 1e-1), error_approx=(7.801, 1e-3))
+
+# "Test dynamic lambda update" and "The best linearization can be filled out without debug_stats"
+# (test/symforce_optimizer_test.cc:461-506): DefaultOptimizerParams with DYNAMIC lambda updates on the
+# pose-smoothing problem; SUCCESS with failure reason INVALID after 27 records, and the best
+# linearization has 66 residual rows, a 60 x 60 lower Hessian with 534 stored entries and 60 rhs rows.
+DYNAMIC_LAMBDA_EXPECTED = dict(num_records=27, residual_rows=66, hessian_dim=60, hessian_nnz=534,
+                               rhs_rows=60)

@@ -52,6 +52,37 @@ def test_pose_smoothing_known_answers():
     assert stats.status == A.SFG_STATUS_SUCCESS
 
 
+def test_pose_smoothing_dynamic_lambda_known_answers():
+    """test/symforce_optimizer_test.cc:461-506 on the GPU: SUCCESS / INVALID after 27 records, every
+    record as the oracle's (accept flags exact, lambda and error at 1e-9), and the linearization at
+    the best values has 66 residual rows and a 60 x 60 lower Hessian with 534 stored entries, all
+    finite."""
+    p = R.pose_smoothing(O.pose_smoothing_initial_values())
+    params = A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC)
+    opt = Optimizer(p, params)
+    values, stats = opt.optimize(p.values)
+    E = R.DYNAMIC_LAMBDA_EXPECTED
+    assert stats.status == A.SFG_STATUS_SUCCESS
+    assert stats.failure_reason == A.SFG_FAILURE_INVALID
+    assert len(stats.iterations) == E["num_records"]
+    ref = O.optimize(p, params)
+    assert len(ref["iterations"]) == len(stats.iterations)
+    for g, o in zip(stats.iterations, ref["iterations"]):
+        assert g.iteration == o.iteration and g.update_accepted == o.update_accepted
+        assert g.current_lambda == pytest.approx(o.current_lambda, rel=1e-9)
+        assert g.new_error == pytest.approx(o.new_error, rel=1e-9)
+    assert stats.best_index == ref["best_index"]
+    lin = opt.linearize(values)
+    assert lin["residual"].size == E["residual_rows"] and np.isfinite(lin["residual"]).all()
+    assert lin["rhs"].size == E["rhs_rows"] and np.isfinite(lin["rhs"]).all()
+    assert lin["colptr"].size == E["hessian_dim"] + 1
+    assert lin["hvals"].size == E["hessian_nnz"] and np.isfinite(lin["hvals"]).all()
+    o = O.linearize(p, values)
+    np.testing.assert_array_equal(lin["colptr"], o["colptr"])
+    np.testing.assert_array_equal(lin["rowidx"], o["rowidx"])
+    np.testing.assert_allclose(lin["hvals"], o["hvals"], rtol=1e-9, atol=1e-12 * np.abs(o["hvals"]).max())
+
+
 def test_linearization_matches_oracle_ba_small():
     p = synth.bundle_adjustment(num_cameras=8, num_points=120, num_observations=500, seed=3)
     opt = Optimizer(p, form=A.default_form_params(linear_solver=A.SFG_LINEAR_SOLVER_SCHUR))
@@ -89,9 +120,11 @@ def test_robot_2d_config_matches_oracle():
     assert stats.best_error == pytest.approx(ref["iterations"][ref["best_index"]].new_error, rel=1e-9)
 
 
-@pytest.mark.parametrize("name", ["ba_50_7800", "ba_1000_200k"])
+@pytest.mark.parametrize("name", ["robot2d_1000", "ba_50_7800", "ba_1000_200k"])
 def test_benchmark_workloads_match_committed_oracle_records(name):
-    """Full-size parity: the plain FP64 form on the benchmark workloads follows the CPU oracle's
+    """Full-size parity: the plain FP64 form on the benchmark workloads (2D localization with 1,000
+    Pose2 and 50 iterations, sparse LDL^T; the 50- and 1,000-camera bundle adjustments, Schur) follows
+    the CPU oracle's
     committed LM trajectory (tests/golden/oracle_costs.json, generated by
     tests/golden/make_oracle_costs.py): same number of records, same accept decisions, every
     error at 1e-9 relative, same status."""

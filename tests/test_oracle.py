@@ -43,6 +43,24 @@ def test_pose_smoothing_known_answers():
     assert r["status"] == A.SFG_STATUS_SUCCESS
 
 
+def test_pose_smoothing_dynamic_lambda_known_answers():
+    """test/symforce_optimizer_test.cc:461-506: DYNAMIC lambda on the pose-smoothing problem with
+    otherwise default parameters gives SUCCESS / INVALID after 27 records, and the best
+    linearization has 66 residual rows and a 60 x 60 lower Hessian with 534 stored entries."""
+    p = R.pose_smoothing(O.pose_smoothing_initial_values())
+    params = A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC)
+    r = O.optimize(p, params)
+    E = R.DYNAMIC_LAMBDA_EXPECTED
+    assert r["status"] == A.SFG_STATUS_SUCCESS
+    assert r["failure_reason"] == A.SFG_FAILURE_INVALID
+    assert len(r["iterations"]) == E["num_records"]
+    lin = O.linearize(p, r["values"])
+    assert lin["residual"].size == E["residual_rows"] and np.isfinite(lin["residual"]).all()
+    assert lin["rhs"].size == E["rhs_rows"] and np.isfinite(lin["rhs"]).all()
+    assert lin["colptr"].size == E["hessian_dim"] + 1
+    assert lin["hvals"].size == E["hessian_nnz"] and np.isfinite(lin["hvals"]).all()
+
+
 def test_pose_smoothing_hessian_is_jtj():
     """H == lower(J^T J) (test/symforce_optimizer_test.cc:170-175), built from per-factor jets."""
     p = R.pose_smoothing(O.pose_smoothing_initial_values())

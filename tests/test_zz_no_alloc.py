@@ -39,7 +39,8 @@ def _reference_solve(Ad, b):
     return s.solve(b)
 
 
-def _noalloc(Ad, b):
+def _noalloc(Ad, b, stream=None, expect=0):
+    """One call through the C ABI; `stream` is a torch.cuda.Stream (None: the default stream)."""
     torch = pytest.importorskip("torch")
     L = lib()
     f = L.sfg_dense_ldlt_solve_noalloc
@@ -49,8 +50,9 @@ def _noalloc(Ad, b):
     db = torch.from_numpy(b.copy()).cuda()
     dx = torch.zeros(n, dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
-    rc = f(n, dA.data_ptr(), n, db.data_ptr(), dx.data_ptr(), None)
-    assert rc == 0, L.sfg_last_error().decode()
+    rc = f(n, dA.data_ptr(), n, db.data_ptr(), dx.data_ptr(),
+           None if stream is None else stream.cuda_stream)
+    assert rc == expect, L.sfg_last_error().decode()
     torch.cuda.synchronize()
     return dx.cpu().numpy()
 
@@ -62,6 +64,30 @@ def test_noalloc_matches_allocating_solver_two_calls():
         x = _noalloc(Ad, b)
         np.testing.assert_allclose(x, x_ref, rtol=1e-10, atol=1e-12)
         np.testing.assert_allclose(Ad @ x, b, rtol=1e-9, atol=1e-9)
+
+
+def test_noalloc_smaller_after_larger_and_on_a_stream():
+    """The shared scratch keeps the last call's contents: a smaller system after a larger one must
+    not read the larger one's tile states, tasks or front entries; and a caller's own stream works
+    like the default stream."""
+    torch = pytest.importorskip("torch")
+    stream = torch.cuda.Stream()
+    for n, seed, st in [(512, 3, None), (17, 4, None), (300, 5, stream), (16, 6, stream), (1, 7, None)]:
+        Ad, b = _spd(n, seed)
+        x_ref = _reference_solve(Ad, b)
+        x = _noalloc(Ad, b, stream=st)
+        np.testing.assert_allclose(x, x_ref, rtol=1e-10, atol=1e-12)
+
+
+def test_noalloc_reports_a_zero_pivot():
+    """A singular A (a zero row and column) gives SFG_ERR_NUMERICAL, not silent inf / NaN, and the
+    next call on a regular system is unaffected."""
+    Ad, b = _spd(40, 8)
+    Ad[5, :] = 0.0
+    Ad[:, 5] = 0.0
+    _noalloc(Ad, b, expect=A.SFG_ERR_NUMERICAL)
+    Ad, b = _spd(40, 9)
+    np.testing.assert_allclose(_noalloc(Ad, b), _reference_solve(Ad, b), rtol=1e-10, atol=1e-12)
 
 
 def test_noalloc_rejects_oversize():
