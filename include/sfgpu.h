@@ -52,13 +52,17 @@ enum { SFG_LAMBDA_UPDATE_INVALID = 0, SFG_LAMBDA_UPDATE_STATIC = 1, SFG_LAMBDA_U
 
 /* ---------------------------------------------------------------------------------------------
  * Variable (key) types.  Storage / tangent layouts are the reference's:
- *   VEC1..VEC3: storage = tangent = n scalars, Retract is +=   (symforce/opt/values.cc:303-309)
+ *   VEC1..VEC6: storage = tangent = n scalars, Retract is +=   (symforce/opt/values.cc:303-309,
+ *               gen/cpp/sym/ops/matrix/lie_group_ops.h)
  *   POSE2: storage [re, im, x, y], tangent [theta, x, y]        (gen/cpp/sym/ops/pose2/lie_group_ops.cc:58-82)
  *   POSE3: storage [qx, qy, qz, qw, x, y, z], tangent [w(3), t(3)]
  *          Retract q <- q * exp(w) with eps-regularised norm, t <- t + dt
  *                                                               (gen/cpp/sym/ops/pose3/lie_group_ops.cc:69-102)
+ *   ROT3:  storage [qx, qy, qz, qw], tangent [w(3)], Retract q <- q * exp(w) as POSE3's rotation
+ *                                                               (gen/cpp/sym/ops/rot3/lie_group_ops.cc)
  * ------------------------------------------------------------------------------------------- */
-enum { SFG_KEY_VEC1 = 1, SFG_KEY_VEC2 = 2, SFG_KEY_VEC3 = 3, SFG_KEY_POSE2 = 4, SFG_KEY_POSE3 = 5 };
+enum { SFG_KEY_VEC1 = 1, SFG_KEY_VEC2 = 2, SFG_KEY_VEC3 = 3, SFG_KEY_POSE2 = 4, SFG_KEY_POSE3 = 5,
+       SFG_KEY_ROT3 = 6, SFG_KEY_VEC4 = 7, SFG_KEY_VEC5 = 8, SFG_KEY_VEC6 = 9 };
 
 /* ---------------------------------------------------------------------------------------------
  * Typed factor kinds.  The reference stores a factor as a type-erased std::function
@@ -86,6 +90,21 @@ enum { SFG_KEY_VEC1 = 1, SFG_KEY_VEC2 = 2, SFG_KEY_VEC3 = 3, SFG_KEY_POSE2 = 4, 
  *  RANGE_POSE3        keys [pose3]                consts [lx, ly, lz, range, sqrt_info, epsilon]
  *      r = sqrt_info * (sqrt(|t - l|^2 + eps) - range)   (no reference counterpart; written in the
  *      same style as the odometry factor)
+ *
+ * Kinds generated from symbolic residuals (symforce_gb300/factor_defs.py, compiled from the
+ * generated functors in symforce_gb300/csrc/generated_factors.cuh):
+ *  PRIOR_ROT3         keys [rot3]                 consts [prior q (4), sqrt_info_diag (3), epsilon]
+ *      r = diag(s) * local_coordinates(prior, value)  (symforce/codegen/geo_factors_codegen.py:75-86)
+ *  BETWEEN_ROT3       keys [rot3 a, rot3 b]       consts [a_T_b q (4), sqrt_info_diag (3), epsilon]
+ *      r = diag(s) * local_coordinates(a_T_b, a^-1 * b) (symforce/codegen/geo_factors_codegen.py:53-72)
+ *  BARRON_VEC5        keys [vec5 x]               consts [y (5), mu, epsilon]
+ *      r_i = Barron whitening of x_i - y_i with alpha = 2 - 1 / (1 - mu + eps), delta 1
+ *      (symforce/opt/noise_models.py:318-428; the factor of test/symforce_gnc_codegen_test.py:24-31).
+ *      mu is the graduated non-convexity parameter (sfg_set_factor_consts changes it).
+ *  LINEAR_VEC5        keys [vec5 x]               consts [J (9 x 5 row-major), b (9)]
+ *      r = J x + b     (test/symforce_levenberg_marquardt_test.cc:17-88)
+ *  LINEAR_SCALAR2     keys [vec1 x, vec1 y]       consts [J (2 x 2 row-major), b (2)]
+ *      r = J [x, y] + b   (test/symforce_linearizer_test.cc:16-43)
  * ------------------------------------------------------------------------------------------- */
 enum {
   SFG_FACTOR_BEARING_POSE2 = 1,
@@ -93,7 +112,12 @@ enum {
   SFG_FACTOR_SNAVELY_REPROJECTION = 3,
   SFG_FACTOR_BETWEEN_POSE3 = 4,
   SFG_FACTOR_PRIOR_POSE3 = 5,
-  SFG_FACTOR_RANGE_POSE3 = 6
+  SFG_FACTOR_RANGE_POSE3 = 6,
+  SFG_FACTOR_PRIOR_ROT3 = 7,
+  SFG_FACTOR_BETWEEN_ROT3 = 8,
+  SFG_FACTOR_BARRON_VEC5 = 9,
+  SFG_FACTOR_LINEAR_VEC5 = 10,
+  SFG_FACTOR_LINEAR_SCALAR2 = 11
 };
 
 typedef struct sfg_factor_batch_t {
@@ -222,6 +246,21 @@ int32_t sfg_set_values(sfg_handle* h, const double* storage, int64_t n);
  * means params->iterations.  Values stay on the device until sfg_get_values. */
 int32_t sfg_optimize(sfg_handle* h, const sfg_optimizer_params_t* params, int32_t num_iterations,
                      sfg_stats_t* stats);
+/* The loop of GncOptimizer::OptimizeContinue (symforce/opt/gnc_optimizer.h:113-121): ResetState on
+ * the values the last call left (its best values), keeping lambda, nu and the iteration counter
+ * (symforce/opt/levenberg_marquardt_solver.h:176-183); relax_damping != 0 applies
+ * RelaxDampingToInitial first (lambda = min(lambda, initial_lambda), nu = dynamic beta, :170-174).
+ * Runs at most num_iterations more iterations.  `stats` receives only the new records (there is no
+ * iteration -1 record), num_iterations their count, and best_index the index among them of the
+ * last new best, or -1 when none improved on the state the call started from.  Requires a prior
+ * sfg_optimize on the handle. */
+int32_t sfg_optimize_continue(sfg_handle* h, const sfg_optimizer_params_t* params,
+                              int32_t num_iterations, int32_t relax_damping, sfg_stats_t* stats);
+/* Replace the constants of one factor batch (layout as in sfg_problem_t, the caller's factor
+ * order): the cost function changes, e.g. the convexity parameter mu of BARRON_VEC5 that a
+ * graduated non-convexity schedule steps (the reference keeps it as a Values entry the factors
+ * read, symforce/opt/gnc_optimizer.h:85-88). */
+int32_t sfg_set_factor_consts(sfg_handle* h, int32_t batch, const double* consts, int64_t n);
 /* GetBestValues (symforce/opt/levenberg_marquardt_solver.h:178-182). */
 int32_t sfg_get_values(sfg_handle* h, double* storage, int64_t n);
 /* Linearize the problem at the current values and return residual (M), rhs (N) and error; the

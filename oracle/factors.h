@@ -206,4 +206,77 @@ void RangePose3Residual(const S* x, const double* c, S* r) {
   r[0] = c[4] * (sqrt(dx * dx + dy * dy + dz * dz + c[5]) - c[3]);
 }
 
+// ---------------------------------------------------------------------------------------------
+// The factors the library generates from symbolic definitions (restated here by hand, so that the
+// oracle checks the generated code independently).
+// ---------------------------------------------------------------------------------------------
+
+// Rot3 storage [x, y, z, w], tangent w: gen/cpp/sym/ops/rot3/lie_group_ops.cc, q <- q * exp(w)
+// with |w| = sqrt(eps^2 + w.w) (the rotation part of RetractPose3).
+template <typename S>
+void RetractRot3(const double* a, const S* d, double eps, S* out) {
+  const S n = sqrt(eps * eps + d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  const S c = cos(0.5 * n);
+  const S s = sin(0.5 * n) / n;
+  const S vx = s * d[0], vy = s * d[1], vz = s * d[2];
+  out[0] = a[3] * vx + a[0] * c + a[1] * vz - a[2] * vy;
+  out[1] = a[3] * vy - a[0] * vz + a[1] * c + a[2] * vx;
+  out[2] = a[3] * vz + a[0] * vy - a[1] * vx + a[2] * c;
+  out[3] = a[3] * c - a[0] * vx - a[1] * vy - a[2] * vz;
+}
+
+// prior_factor for Rot3 (symforce/codegen/geo_factors_codegen.py:74-86): diag(s) Log(prior^-1 x);
+// consts [prior q (4), s (3), eps].
+template <typename S>
+void PriorRot3Residual(const S* x, const double* c, S* r) {
+  const double qp_inv[4] = {-c[0], -c[1], -c[2], c[3]};
+  S qe[4];
+  QuatMul(qp_inv, x, qe);
+  S w[3];
+  QuatLog(qe, c[7], w);
+  for (int i = 0; i < 3; ++i) r[i] = c[4 + i] * w[i];
+}
+
+// between_factor for Rot3 (symforce/codegen/geo_factors_codegen.py:53-71):
+// diag(s) Log(a_T_b^-1 a^-1 b); consts [a_T_b q (4), s (3), eps].
+template <typename S>
+void BetweenRot3Residual(const S* a, const S* b, const double* c, S* r) {
+  const S qa_inv[4] = {-a[0], -a[1], -a[2], a[3]};
+  S q[4];
+  QuatMul(qa_inv, b, q);
+  const double qm_inv[4] = {-c[0], -c[1], -c[2], c[3]};
+  S qe[4];
+  QuatMul(qm_inv, q, qe);
+  S w[3];
+  QuatLog(qe, c[7], w);
+  for (int i = 0; i < 3; ++i) r[i] = c[4 + i] * w[i];
+}
+
+// BarronNoiseModel.whiten of x - y (symforce/opt/noise_models.py:318-428) with delta 1,
+// scalar_information 1, x_epsilon = alpha_epsilon = eps and alpha = 2 - 1 / (1 - mu + eps)
+// (compute_alpha_from_mu): the factor of test/symforce_gnc_codegen_test.py:24-31;
+// consts [y (5), mu, eps].
+template <typename S>
+void BarronVec5Residual(const S* x, const double* c, S* r) {
+  const double mu = c[5], eps = c[6];
+  const double alpha = 2.0 - 1.0 / (1.0 - mu + eps);
+  const double b = std::fabs(alpha - 2.0) + eps;
+  const double d = alpha + (alpha >= 0 ? eps : -eps);
+  for (int i = 0; i < 5; ++i) {
+    const S e = x[i] - c[i];
+    const S barron = (b / d) * (pow(e * e / b + 1.0, d / 2.0) - 1.0);
+    r[i] = sqrt(2.0 * barron + eps) - std::sqrt(eps);
+  }
+}
+
+// r = J x + b (J rows x cols, row-major, then b) over the concatenated key storage.
+template <typename S>
+void LinearResidual(const S* x, const double* c, int rows, int cols, S* r) {
+  for (int i = 0; i < rows; ++i) {
+    S acc = S(c[rows * cols + i]);
+    for (int j = 0; j < cols; ++j) acc = acc + c[i * cols + j] * x[j];
+    r[i] = acc;
+  }
+}
+
 }  // namespace oracle

@@ -113,6 +113,11 @@ inline Jet<N> atan2(const Jet<N>& y, const Jet<N>& x) {
   for (int i = 0; i < N; ++i) r.v[i] = (x.a * y.v[i] - y.a * x.v[i]) / d;
   return r;
 }
+// x^e for a constant exponent e.
+template <int N>
+inline Jet<N> pow(const Jet<N>& x, double e) {
+  return Chain(x, std::pow(x.a, e), e * std::pow(x.a, e - 1.0));
+}
 // min(x, c) with a constant c: derivative follows the selected branch.
 template <int N>
 inline Jet<N> fmin(const Jet<N>& x, double c) { return x.a < c ? x : Jet<N>(c); }

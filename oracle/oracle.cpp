@@ -49,6 +49,10 @@ inline void KeyDims(int type, int* sdim, int* tdim) {
     case SFG_KEY_VEC3: *sdim = 3; *tdim = 3; return;
     case SFG_KEY_POSE2: *sdim = 4; *tdim = 3; return;
     case SFG_KEY_POSE3: *sdim = 7; *tdim = 6; return;
+    case SFG_KEY_ROT3: *sdim = 4; *tdim = 3; return;
+    case SFG_KEY_VEC4: *sdim = 4; *tdim = 4; return;
+    case SFG_KEY_VEC5: *sdim = 5; *tdim = 5; return;
+    case SFG_KEY_VEC6: *sdim = 6; *tdim = 6; return;
   }
   throw std::invalid_argument("unknown key type " + std::to_string(type));
 }
@@ -66,6 +70,11 @@ inline FactorSpec Spec(int kind) {
     case SFG_FACTOR_BETWEEN_POSE3: return {2, 14, 6, {SFG_KEY_POSE3, SFG_KEY_POSE3, 0}};
     case SFG_FACTOR_PRIOR_POSE3: return {1, 14, 6, {SFG_KEY_POSE3, 0, 0}};
     case SFG_FACTOR_RANGE_POSE3: return {1, 6, 1, {SFG_KEY_POSE3, 0, 0}};
+    case SFG_FACTOR_PRIOR_ROT3: return {1, 8, 3, {SFG_KEY_ROT3, 0, 0}};
+    case SFG_FACTOR_BETWEEN_ROT3: return {2, 8, 3, {SFG_KEY_ROT3, SFG_KEY_ROT3, 0}};
+    case SFG_FACTOR_BARRON_VEC5: return {1, 7, 5, {SFG_KEY_VEC5, 0, 0}};
+    case SFG_FACTOR_LINEAR_VEC5: return {1, 54, 9, {SFG_KEY_VEC5, 0, 0}};
+    case SFG_FACTOR_LINEAR_SCALAR2: return {2, 6, 2, {SFG_KEY_VEC1, SFG_KEY_VEC1, 0}};
   }
   throw std::invalid_argument("unknown factor kind " + std::to_string(kind));
 }
@@ -172,11 +181,15 @@ void LinearizeFactorT(const Problem& P, const Factor& F, const double* values, d
       Jet<NT> d[6];
       for (int i = 0; i < 6; ++i) d[i] = Jet<NT>::Seed(0.0, F.koff[j] + i);
       RetractPose3(values + k.soff, d, retract_eps, xs[j]);
+    } else if (k.type == SFG_KEY_ROT3) {
+      Jet<NT> d[3];
+      for (int i = 0; i < 3; ++i) d[i] = Jet<NT>::Seed(0.0, F.koff[j] + i);
+      RetractRot3(values + k.soff, d, retract_eps, xs[j]);
     } else {
       RetractKeyJet<NT>(k, values + k.soff, F.koff[j], xs[j]);
     }
   }
-  Jet<NT> r[6];
+  Jet<NT> r[9];
   switch (F.kind) {
     case SFG_FACTOR_BEARING_POSE2: BearingResidual(xs[0], F.c, r); break;
     case SFG_FACTOR_ODOMETRY_POSE2: OdometryResidual(xs[0], xs[1], F.c, r); break;
@@ -184,6 +197,15 @@ void LinearizeFactorT(const Problem& P, const Factor& F, const double* values, d
     case SFG_FACTOR_BETWEEN_POSE3: BetweenPose3Residual(xs[0], xs[1], F.c, r); break;
     case SFG_FACTOR_PRIOR_POSE3: PriorPose3Residual(xs[0], F.c, r); break;
     case SFG_FACTOR_RANGE_POSE3: RangePose3Residual(xs[0], F.c, r); break;
+    case SFG_FACTOR_PRIOR_ROT3: PriorRot3Residual(xs[0], F.c, r); break;
+    case SFG_FACTOR_BETWEEN_ROT3: BetweenRot3Residual(xs[0], xs[1], F.c, r); break;
+    case SFG_FACTOR_BARRON_VEC5: BarronVec5Residual(xs[0], F.c, r); break;
+    case SFG_FACTOR_LINEAR_VEC5: LinearResidual(xs[0], F.c, 9, 5, r); break;
+    case SFG_FACTOR_LINEAR_SCALAR2: {
+      const Jet<NT> xy[2] = {xs[0][0], xs[1][0]};
+      LinearResidual(xy, F.c, 2, 2, r);
+      break;
+    }
   }
   for (int i = 0; i < F.rdim; ++i) {
     res[i] = r[i].a;
@@ -194,6 +216,8 @@ void LinearizeFactorT(const Problem& P, const Factor& F, const double* values, d
 void LinearizeFactor(const Problem& P, const Factor& F, const double* values, double* res,
                      double* J, double retract_eps) {
   switch (F.tdim) {
+    case 2: LinearizeFactorT<2>(P, F, values, res, J, retract_eps); return;
+    case 5: LinearizeFactorT<5>(P, F, values, res, J, retract_eps); return;
     case 3: LinearizeFactorT<3>(P, F, values, res, J, retract_eps); return;
     case 6: LinearizeFactorT<6>(P, F, values, res, J, retract_eps); return;
     case 12: LinearizeFactorT<12>(P, F, values, res, J, retract_eps); return;
@@ -289,7 +313,7 @@ struct Linearizer {
     lin.residual.assign(P->M, 0.0);
     lin.rhs.assign(P->N, 0.0);
     lin.hvals.assign(H.rowidx.size(), 0.0);
-    double res[6], J[6 * 12];
+    double res[9], J[9 * 12];  // residual rows <= 9, tangent columns <= 12
     for (size_t f = 0; f < P->factors.size(); ++f) {
       const Factor& F = P->factors[f];
       LinearizeFactor(*P, F, values.data(), res, J, retract_eps);
@@ -705,6 +729,7 @@ void RetractValues(const Problem& P, const std::vector<double>& in, const double
     switch (k.type) {
       case SFG_KEY_POSE2: RetractPose2(a, d, o); break;
       case SFG_KEY_POSE3: RetractPose3(a, d, eps, o); break;
+      case SFG_KEY_ROT3: RetractRot3(a, d, eps, o); break;
       default:
         for (int i = 0; i < k.tdim; ++i) o[i] = a[i] + d[i];
     }
@@ -741,9 +766,16 @@ struct LinearSolverChoice {
   int ordering = SFG_ORDERING_MIN_DEGREE;
 };
 
+// State that OptimizeContinue keeps across calls (symforce/opt/gnc_optimizer.h:113-121): lambda,
+// nu and the iteration counter (ResetState, symforce/opt/levenberg_marquardt_solver.h:176-183).
+struct LmCarry {
+  double lambda = 0, nu = 0;
+  int iteration = -1;
+};
+
 LmResult Optimize(const Problem& P, const std::vector<double>& values0,
                   const sfg_optimizer_params_t& p, int num_iterations, double epsilon,
-                  LinearSolverChoice ls) {
+                  LinearSolverChoice ls, LmCarry* carry = nullptr, bool continue_state = false) {
   using Clock = std::chrono::steady_clock;
   const auto t_start = Clock::now();
   double t_lin = 0, t_sol = 0;
@@ -761,10 +793,15 @@ LmResult Optimize(const Problem& P, const std::vector<double>& values0,
   int init_idx = 0, new_idx = 1, best_idx = 0, free_idx = 2;
   bool best_valid = false;
   (void)best_valid;
-  // Reset(values)
+  // Reset(values), or ResetState(values) when continuing
   double lambda = p.initial_lambda;
   double nu = p.dynamic_lambda_update_beta;
   int iteration = -1;
+  if (continue_state && carry) {
+    lambda = carry->lambda;
+    nu = carry->nu;
+    iteration = carry->iteration;
+  }
   bool have_max_diagonal = false, have_last_update = false;
   blocks[new_idx].values = values0;
   for (auto& b : blocks) {
@@ -778,6 +815,7 @@ LmResult Optimize(const Problem& P, const std::vector<double>& values0,
   std::vector<double> max_diagonal, damping(N), undamped(N), update(N), last_update;
 
   LmResult R;
+  if (continue_state) R.best_index = -1;
   auto relinearize = [&](StateBlock& b) {
     const auto t0 = Clock::now();
     linz.Relinearize(b.values, b.lin);
@@ -949,6 +987,11 @@ LmResult Optimize(const Problem& P, const std::vector<double>& values0,
     R.failure_reason = 0;
   }
   R.best_values = blocks[best_idx].values;
+  if (carry) {
+    carry->lambda = lambda;
+    carry->nu = nu;
+    carry->iteration = iteration;
+  }
   R.seconds = std::chrono::duration<double>(Clock::now() - t_start).count();
   R.seconds_linearize = t_lin;
   R.seconds_solve = t_sol;
@@ -1066,6 +1109,40 @@ int orc_optimize(const sfg_problem_t* prob, const double* values_in,
   });
 }
 
+// orc_optimize with the state OptimizeContinue keeps: carry = {lambda, nu, iteration}.  mode 0 runs
+// a fresh optimization and writes the carry out; mode 1 continues from the carry (no iteration -1
+// record, best_index -1 unless a record improves) and writes it back.
+int orc_optimize_carry(const sfg_problem_t* prob, const double* values_in,
+                       const sfg_optimizer_params_t* params, int32_t num_iterations, double epsilon,
+                       int32_t linear_solver, int32_t ordering, double* values_out,
+                       sfg_iteration_t* iters, int32_t capacity, int32_t* num_iters,
+                       int32_t* best_index, int32_t* status, int32_t* failure_reason, double* carry,
+                       int32_t mode) {
+  return Guard([&] {
+    using namespace oracle;
+    Problem P = BuildProblem(prob);
+    std::vector<double> v(values_in, values_in + P.S);
+    LinearSolverChoice ls;
+    ls.kind = linear_solver;
+    ls.ordering = ordering;
+    LmCarry c;
+    c.lambda = carry[0];
+    c.nu = carry[1];
+    c.iteration = int(carry[2]);
+    LmResult R = Optimize(P, v, *params, num_iterations, epsilon, ls, &c, mode == 1);
+    if (int(R.iters.size()) > capacity) throw std::runtime_error("iteration buffer too small");
+    std::copy(R.iters.begin(), R.iters.end(), iters);
+    *num_iters = int32_t(R.iters.size());
+    *best_index = R.best_index;
+    *status = R.status;
+    *failure_reason = R.failure_reason;
+    std::copy(R.best_values.begin(), R.best_values.end(), values_out);
+    carry[0] = c.lambda;
+    carry[1] = c.nu;
+    carry[2] = double(c.iteration);
+  });
+}
+
 // SparseCholeskySolver on a lower CSC matrix; ordering SFG_ORDERING_NATURAL / MIN_DEGREE, or an
 // explicit `order` (order[new] = old) when non-null.  Returns x and D (in the permuted order).
 int orc_ldlt_solve(int64_t n, const int64_t* col_ptr, const int32_t* row_idx, const double* vals,
@@ -1109,6 +1186,7 @@ int orc_retract(int32_t key_type, const double* storage, const double* delta, do
     switch (key_type) {
       case SFG_KEY_POSE2: RetractPose2(storage, delta, out); break;
       case SFG_KEY_POSE3: RetractPose3(storage, delta, epsilon, out); break;
+      case SFG_KEY_ROT3: RetractRot3(storage, delta, epsilon, out); break;
       default: {
         int sd, td;
         KeyDims(key_type, &sd, &td);
@@ -1131,6 +1209,36 @@ int orc_pose_smoothing_initial_values(int32_t num_keys, double epsilon, double* 
       double d[6];
       for (int k = 0; k < 6; ++k) d[k] = 0.4 * dist(gen);
       oracle::RetractPose3(identity, d, epsilon, out + 7 * i);
+    }
+  });
+}
+
+// sym::Random<Eigen::Matrix<double, dim, 1>>(gen) called num_vectors times in a row on
+// std::mt19937(seed): each call draws `dim` std::normal_distribution<double> samples in order from a
+// fresh distribution (gen/cpp/sym/ops/matrix/storage_ops.h:212-218; a matrix is filled in its
+// column-major coefficient order).  out: num_vectors x dim.
+int orc_mt19937_normal_vectors(uint32_t seed, int32_t num_vectors, int32_t dim, double* out) {
+  return Guard([&] {
+    std::mt19937 gen(seed);
+    for (int i = 0; i < num_vectors; ++i) {
+      std::normal_distribution<double> dist{};
+      for (int k = 0; k < dim; ++k) out[int64_t(i) * dim + k] = dist(gen);
+    }
+  });
+}
+
+// Initial values of the reference's Rot3 smoothing test (test/symforce_optimizer_test.cc:232-236):
+// identity.Retract(0.4 * sym::Random<Vector3d>(std::mt19937(42)), epsilon) for num_keys keys,
+// storage [x, y, z, w] each.
+int orc_rot3_smoothing_initial_values(int32_t num_keys, double epsilon, double* out) {
+  return Guard([&] {
+    std::mt19937 gen(42);
+    const double identity[4] = {0, 0, 0, 1};
+    for (int i = 0; i < num_keys; ++i) {
+      std::normal_distribution<double> dist{};
+      double d[3];
+      for (int k = 0; k < 3; ++k) d[k] = 0.4 * dist(gen);
+      oracle::RetractRot3(identity, d, epsilon, out + 4 * i);
     }
   });
 }

@@ -20,12 +20,17 @@ SFG_FAILURE_INVALID, SFG_FAILURE_LAMBDA_OUT_OF_BOUNDS, SFG_FAILURE_INITIAL_ERROR
 SFG_LAMBDA_UPDATE_STATIC, SFG_LAMBDA_UPDATE_DYNAMIC = 1, 2
 
 SFG_KEY_VEC1, SFG_KEY_VEC2, SFG_KEY_VEC3, SFG_KEY_POSE2, SFG_KEY_POSE3 = 1, 2, 3, 4, 5
+SFG_KEY_ROT3, SFG_KEY_VEC4, SFG_KEY_VEC5, SFG_KEY_VEC6 = 6, 7, 8, 9
 KEY_DIMS = {  # storage, tangent
     SFG_KEY_VEC1: (1, 1),
     SFG_KEY_VEC2: (2, 2),
     SFG_KEY_VEC3: (3, 3),
     SFG_KEY_POSE2: (4, 3),
     SFG_KEY_POSE3: (7, 6),
+    SFG_KEY_ROT3: (4, 3),
+    SFG_KEY_VEC4: (4, 4),
+    SFG_KEY_VEC5: (5, 5),
+    SFG_KEY_VEC6: (6, 6),
 }
 
 SFG_FACTOR_BEARING_POSE2 = 1
@@ -34,6 +39,12 @@ SFG_FACTOR_SNAVELY_REPROJECTION = 3
 SFG_FACTOR_BETWEEN_POSE3 = 4
 SFG_FACTOR_PRIOR_POSE3 = 5
 SFG_FACTOR_RANGE_POSE3 = 6
+# kinds generated from symbolic definitions (symforce_gb300/factor_defs.py)
+SFG_FACTOR_PRIOR_ROT3 = 7
+SFG_FACTOR_BETWEEN_ROT3 = 8
+SFG_FACTOR_BARRON_VEC5 = 9
+SFG_FACTOR_LINEAR_VEC5 = 10
+SFG_FACTOR_LINEAR_SCALAR2 = 11
 FACTOR_DIMS = {  # num_keys, num_consts, residual_dim, key types
     SFG_FACTOR_BEARING_POSE2: (1, 5, 1, (SFG_KEY_POSE2,)),
     SFG_FACTOR_ODOMETRY_POSE2: (2, 3, 1, (SFG_KEY_POSE2, SFG_KEY_POSE2)),
@@ -41,6 +52,11 @@ FACTOR_DIMS = {  # num_keys, num_consts, residual_dim, key types
     SFG_FACTOR_BETWEEN_POSE3: (2, 14, 6, (SFG_KEY_POSE3, SFG_KEY_POSE3)),
     SFG_FACTOR_PRIOR_POSE3: (1, 14, 6, (SFG_KEY_POSE3,)),
     SFG_FACTOR_RANGE_POSE3: (1, 6, 1, (SFG_KEY_POSE3,)),
+    SFG_FACTOR_PRIOR_ROT3: (1, 8, 3, (SFG_KEY_ROT3,)),
+    SFG_FACTOR_BETWEEN_ROT3: (2, 8, 3, (SFG_KEY_ROT3, SFG_KEY_ROT3)),
+    SFG_FACTOR_BARRON_VEC5: (1, 7, 5, (SFG_KEY_VEC5,)),
+    SFG_FACTOR_LINEAR_VEC5: (1, 54, 9, (SFG_KEY_VEC5,)),
+    SFG_FACTOR_LINEAR_SCALAR2: (2, 6, 2, (SFG_KEY_VEC1, SFG_KEY_VEC1)),
 }
 
 SFG_PRECISION_FP64, SFG_PRECISION_MIXED = 0, 1

@@ -25,6 +25,7 @@ forwards to the generated struct, and a case in `LaunchLinearize` (kernels_lin.c
 
 from __future__ import annotations
 
+from pathlib import Path
 from typing import Callable, List, Sequence
 
 import sympy as sp
@@ -39,6 +40,13 @@ def _key_symbols(k: int, key_type: int):
 
 def _retract_first_order(key_type: int, x: sp.Matrix, d: sp.Matrix) -> sp.Matrix:
     """x ⊞ δ to first order in δ (enough for the Jacobian at δ = 0)."""
+    if key_type == A.SFG_KEY_ROT3:
+        qx, qy, qz, qw = x[0], x[1], x[2], x[3]
+        hx, hy, hz = d[0] / 2, d[1] / 2, d[2] / 2
+        return sp.Matrix([qw * hx + qx + qy * hz - qz * hy,
+                          qw * hy - qx * hz + qy + qz * hx,
+                          qw * hz + qx * hy - qy * hx + qz,
+                          qw - qx * hx - qy * hy - qz * hz])
     if key_type == A.SFG_KEY_POSE3:
         qx, qy, qz, qw = x[0], x[1], x[2], x[3]
         # q ⊗ [ω / 2, 1]
@@ -88,6 +96,13 @@ def factor_source(name: str, key_types: Sequence[int], num_consts: int,
 
     kt = ", ".join(str(v) for v in tdims)
     ks = ", ".join(str(A.KEY_DIMS[t][0]) for t in key_types)
+
+    def slot_fn(fn, dims):
+        expr = "0"
+        for k in reversed(range(len(dims))):
+            expr = f"(k == {k} ? {dims[k]} : {expr})"
+        return f"  static constexpr SFG_HD int {fn}(int k) {{ return {expr}; }}"
+
     lines = [
         f"// Generated by symforce_gb300.codegen from a sympy residual: {rd} residual rows, tangent",
         f"// dimension {td}; residual in FP64, Jacobian (row-major) in T.",
@@ -95,6 +110,8 @@ def factor_source(name: str, key_types: Sequence[int], num_consts: int,
         f"  static constexpr int NK = {len(key_types)}, NC = {num_consts}, RD = {rd}, TD = {td}, MK = 0;",
         f"  static constexpr int kTangent[NK] = {{{kt}}};",
         f"  static constexpr int kStorage[NK] = {{{ks}}};",
+        slot_fn("KT", tdims),
+        slot_fn("KS", [A.KEY_DIMS[t][0] for t in key_types]),
         "  template <typename T>",
         "  static SFG_HD void Run(const double* const* x, const double* c, double* r, T* J) {",
     ]
@@ -117,5 +134,39 @@ def range_pose3_residual(keys, c):
     return sp.Matrix([c[4] * (sp.sqrt(d.dot(d) + c[5]) - c[3])])
 
 
+def write_generated(csrc: Path | None = None) -> tuple[Path, Path]:
+    """Write generated_factors.cuh (device functors) and generated_factor_specs.h (the kinds'
+    dimensions, for host code) from the definitions in factor_defs.GENERATED."""
+    from . import factor_defs
+    csrc = csrc or Path(__file__).resolve().parent / "csrc"
+    head = ["// Generated by `python -m symforce_gb300.codegen --write` from the sympy residuals in",
+            "// symforce_gb300/factor_defs.py; do not edit by hand."]
+    dev = head + ["#pragma once", "", "namespace sfg {", ""]
+    specs = head + ["#pragma once", "",
+                    "// X(kind, num_keys, num_consts, residual_dim, key type 0, key type 1, key type 2, struct)",
+                    "#define SFG_GENERATED_FACTORS(X) \\"]
+    rows = []
+    for fd in factor_defs.GENERATED:
+        dev.append(f"// {fd.enum}: {fd.doc}")
+        dev.append(factor_source(fd.name, list(fd.key_types), fd.num_consts, fd.residual))
+        kts = list(fd.key_types) + [0] * (3 - len(fd.key_types))
+        xs = [_key_symbols(k, t) for k, t in enumerate(fd.key_types)]
+        cs = list(sp.symbols(f"c0:{fd.num_consts}", real=True))
+        rd = sp.Matrix(fd.residual(xs, cs)).shape[0]
+        rows.append(f"  X({fd.enum}, {len(fd.key_types)}, {fd.num_consts}, {rd}, {kts[0]}, {kts[1]}, {kts[2]}, "
+                    f"{fd.name})")
+    dev += ["}  // namespace sfg", ""]
+    specs += [r + " \\" for r in rows[:-1]] + [rows[-1], ""]
+    p_dev, p_spec = csrc / "generated_factors.cuh", csrc / "generated_factor_specs.h"
+    p_dev.write_text("\n".join(dev))
+    p_spec.write_text("\n".join(specs))
+    return p_dev, p_spec
+
+
 if __name__ == "__main__":
-    print(factor_source("GenRangePose3", [A.SFG_KEY_POSE3], 6, range_pose3_residual))
+    import sys
+    if "--write" in sys.argv:
+        for p in write_generated():
+            print("wrote", p)
+    else:
+        print(factor_source("GenRangePose3", [A.SFG_KEY_POSE3], 6, range_pose3_residual))

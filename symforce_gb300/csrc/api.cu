@@ -116,6 +116,7 @@ struct sfg_handle {
   cudaGraphExec_t exec = nullptr;
   bool have_graph = false;
   bool values_set = false;
+  bool optimized = false;   // an sfg_optimize call has run (sfg_optimize_continue needs one)
   int last_linearized_block = -1;
 
   ~sfg_handle() {
@@ -335,6 +336,8 @@ void ToLmParams(const sfg_optimizer_params_t& p, int iterations, double eps, LmP
   o->keep_max_diagonal_damping = p.keep_max_diagonal_damping;
   o->enable_bold_updates = p.enable_bold_updates;
   o->iterations = iterations;
+  o->continue_state = 0;
+  o->relax_damping = 0;
 }
 
 template <typename F>
@@ -686,8 +689,52 @@ int32_t sfg_set_values(sfg_handle* h, const double* storage, int64_t n) {
   });
 }
 
+namespace sfg {
+namespace {
+int32_t OptimizeImpl(sfg_handle* h, const sfg_optimizer_params_t* params, int32_t num_iterations,
+                     sfg_stats_t* stats, int continue_state, int relax_damping);
+}
+}  // namespace sfg
+
 int32_t sfg_optimize(sfg_handle* h, const sfg_optimizer_params_t* params, int32_t num_iterations,
                      sfg_stats_t* stats) {
+  return sfg::OptimizeImpl(h, params, num_iterations, stats, 0, 0);
+}
+
+int32_t sfg_optimize_continue(sfg_handle* h, const sfg_optimizer_params_t* params,
+                              int32_t num_iterations, int32_t relax_damping, sfg_stats_t* stats) {
+  return Guard([&] {
+    if (!h) throw Error(SFG_ERR_INVALID_ARGUMENT, "null handle");
+    if (!h->optimized) throw Error(SFG_ERR_INVALID_ARGUMENT, "sfg_optimize_continue needs a prior sfg_optimize");
+    const int32_t rc = sfg::OptimizeImpl(h, params, num_iterations, stats, 1, relax_damping ? 1 : 0);
+    if (rc != SFG_OK) throw Error(rc, sfg::g_last_error);
+  });
+}
+
+int32_t sfg_set_factor_consts(sfg_handle* h, int32_t batch, const double* consts, int64_t n) {
+  return Guard([&] {
+    if (!h || !consts) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (batch < 0 || batch >= int32_t(h->P.batches.size()))
+      throw Error(SFG_ERR_INVALID_ARGUMENT, "batch index out of range");
+    sfg::HostBatch& B = h->P.batches[size_t(batch)];
+    if (n != int64_t(B.count) * B.nc) throw Error(SFG_ERR_INVALID_ARGUMENT, "consts size mismatch");
+    B.consts.assign(consts, consts + n);
+    const std::vector<int32_t>& order = h->L.maps[size_t(batch)].order;
+    std::vector<double> soa(static_cast<size_t>(n));
+    for (int f = 0; f < B.count; ++f)
+      for (int c = 0; c < B.nc; ++c) soa[size_t(c) * B.count + f] = consts[size_t(order[f]) * B.nc + c];
+    SFG_CUDA(cudaSetDevice(h->device));
+    if (n > 0)
+      SFG_CUDA(cudaMemcpyAsync(const_cast<double*>(h->batches[size_t(batch)].consts), soa.data(),
+                               sizeof(double) * size_t(n), cudaMemcpyHostToDevice, h->stream));
+    SFG_CUDA(cudaStreamSynchronize(h->stream));
+  });
+}
+
+namespace sfg {
+namespace {
+int32_t OptimizeImpl(sfg_handle* h, const sfg_optimizer_params_t* params, int32_t num_iterations,
+                     sfg_stats_t* stats, int continue_state, int relax_damping) {
   return Guard([&] {
     if (!h || !params) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
     if (!h->values_set) throw Error(SFG_ERR_INVALID_ARGUMENT, "sfg_set_values was not called");
@@ -704,6 +751,8 @@ int32_t sfg_optimize(sfg_handle* h, const sfg_optimizer_params_t* params, int32_
     }
     sfg::LmParams lp;
     sfg::ToLmParams(*params, iters, h->epsilon, &lp);
+    lp.continue_state = continue_state;
+    lp.relax_damping = relax_damping;
     SFG_CUDA(cudaMemcpyAsync(h->params, &lp, sizeof(lp), cudaMemcpyHostToDevice, h->stream));
     cudaEvent_t e0, e1;
     SFG_CUDA(cudaEventCreate(&e0));
@@ -728,8 +777,8 @@ int32_t sfg_optimize(sfg_handle* h, const sfg_optimizer_params_t* params, int32_
       throw Error(SFG_ERR_DEVICE_STATUS, "device loop hit its cap (code " + std::to_string(st.device_error) + ")");
     if (stats) {
       stats->device_ms = double(ms);
-      stats->kernel_launches =
-          sfg::PrologueKernels(h) + std::max(st.num_records - 1, 0) * sfg::BodyKernels(h);
+      stats->kernel_launches = sfg::PrologueKernels(h) +
+                               std::max(st.num_records - (continue_state ? 0 : 1), 0) * sfg::BodyKernels(h);
       stats->num_iterations = st.num_records;
       stats->best_index = st.best_index;
       stats->status = st.status;
@@ -741,8 +790,11 @@ int32_t sfg_optimize(sfg_handle* h, const sfg_optimizer_params_t* params, int32_
                             cudaMemcpyDeviceToHost));
       }
     }
+    h->optimized = true;
   });
 }
+}  // namespace
+}  // namespace sfg
 
 int32_t sfg_get_values(sfg_handle* h, double* storage, int64_t n) {
   return Guard([&] {

@@ -238,7 +238,7 @@ void RunGraph(sfg_batch* b) {
 }
 
 double Optimize(sfg_batch* b, const sfg_optimizer_params_t& params, int iters) {
-  LmParams lp;
+  LmParams lp{};
   ToParams(params, iters, b->epsilon, &lp);
   EnsureRecords(b, iters + 1);
   EnsureWorkspace(b, b->ctas, b->shape);

@@ -11,6 +11,7 @@
 
 #include "../../include/sfgpu.h"
 #include "device.cuh"
+#include "generated_factor_specs.h"
 
 namespace sfg {
 
@@ -35,6 +36,10 @@ inline void KeyDims(int type, int* sdim, int* tdim) {
     case SFG_KEY_VEC3: *sdim = 3; *tdim = 3; return;
     case SFG_KEY_POSE2: *sdim = 4; *tdim = 3; return;
     case SFG_KEY_POSE3: *sdim = 7; *tdim = 6; return;
+    case SFG_KEY_ROT3: *sdim = 4; *tdim = 3; return;
+    case SFG_KEY_VEC4: *sdim = 4; *tdim = 4; return;
+    case SFG_KEY_VEC5: *sdim = 5; *tdim = 5; return;
+    case SFG_KEY_VEC6: *sdim = 6; *tdim = 6; return;
   }
   throw Error(SFG_ERR_INVALID_ARGUMENT, "unknown key type " + std::to_string(type));
 }
@@ -52,6 +57,10 @@ inline FactorSpec Spec(int kind) {
     case SFG_FACTOR_BETWEEN_POSE3: return {2, 14, 6, {SFG_KEY_POSE3, SFG_KEY_POSE3, 0}};
     case SFG_FACTOR_PRIOR_POSE3: return {1, 14, 6, {SFG_KEY_POSE3, 0, 0}};
     case SFG_FACTOR_RANGE_POSE3: return {1, 6, 1, {SFG_KEY_POSE3, 0, 0}};
+#define SFG_GENERATED_SPEC(KIND, NKEYS, NCONSTS, RDIM, K0, K1, K2, G) \
+    case KIND: return {NKEYS, NCONSTS, RDIM, {K0, K1, K2}};
+    SFG_GENERATED_FACTORS(SFG_GENERATED_SPEC)
+#undef SFG_GENERATED_SPEC
   }
   throw Error(SFG_ERR_INVALID_ARGUMENT, "unknown factor kind " + std::to_string(kind));
 }

@@ -66,6 +66,11 @@ struct LmParams {
   int use_diagonal_damping, use_unit_damping, keep_max_diagonal_damping;
   int enable_bold_updates;
   int iterations;
+  // 1: continue an optimization (OptimizeContinue of symforce/opt/gnc_optimizer.h:113-121):
+  // ResetState on the current values, keeping lambda, nu and the iteration counter, and write no
+  // iteration -1 record; relax_damping additionally applies RelaxDampingToInitial first
+  // (symforce/opt/levenberg_marquardt_solver.h:170-174)
+  int continue_state, relax_damping;
 };
 
 // One factor batch as seen by the linearization kernel.

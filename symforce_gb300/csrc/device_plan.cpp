@@ -81,7 +81,11 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   fp.xperm = A.Alloc(size_t(std::max<int64_t>(S.n, 1)) * elem);
   const int per_sm = 8;
   // the factorization kernel is built for kFactorCtasPerSm resident CTAs of 128 threads per SM
-  fp.grid_factor = std::max(1, std::min<int>(f.ntasks, num_sms * kFactorCtasPerSm));
+  // SFG_FACTOR_CTAS_PER_SM (1..kFactorCtasPerSm) narrows the grid for launch-shape measurements
+  int factor_per_sm = kFactorCtasPerSm;
+  if (const char* e = std::getenv("SFG_FACTOR_CTAS_PER_SM"))
+    factor_per_sm = std::max(1, std::min(kFactorCtasPerSm, std::atoi(e)));
+  fp.grid_factor = std::max(1, std::min<int>(f.ntasks, num_sms * factor_per_sm));
   fp.grid_solve = std::max(1, std::min<int>(2 * S.ns, num_sms * per_sm));
   if (elem == 8) ConfigureSolve<double>(maxm);
   else ConfigureSolve<float>(maxm);

@@ -127,6 +127,20 @@ SFG_HD void QuatLogWithJacobian(const T* q, double eps, T* w, T* dw) {
   }
 }
 
+// Rot3 retraction (gen/cpp/sym/ops/rot3/lie_group_ops.cc): q <- q * exp(w) with the
+// eps-regularised norm, as the rotation part of RetractPose3 below.  a, o: [qx, qy, qz, qw].
+SFG_HD void RetractRot3(const double* a, const double* d, double eps, double* o) {
+  const double n = sqrt(eps * eps + d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  const double c = cos(0.5 * n);
+  const double s = sin(0.5 * n) / n;
+  const double vx = s * d[0], vy = s * d[1], vz = s * d[2];
+  const double a0 = a[0], a1 = a[1], a2 = a[2], a3 = a[3];
+  o[0] = a3 * vx + a0 * c + a1 * vz - a2 * vy;
+  o[1] = a3 * vy - a0 * vz + a1 * c + a2 * vx;
+  o[2] = a3 * vz + a0 * vy - a1 * vx + a2 * c;
+  o[3] = a3 * c - a0 * vx - a1 * vy - a2 * vz;
+}
+
 // Pose3 retraction (gen/cpp/sym/ops/pose3/lie_group_ops.cc:69-102): q <- q * exp(w) with the
 // eps-regularised norm, t <- t + dt.  a, o: storage [qx, qy, qz, qw, x, y, z]; d: tangent [w, dt].
 SFG_HD void RetractPose3(const double* a, const double* d, double eps, double* o) {
@@ -397,5 +411,29 @@ struct FactorEval<SFG_FACTOR_RANGE_POSE3, T> {
     J[5] = T(s * dz);
   }
 };
+
+// ---------------------------------------------------------------------------------------------
+// Factor kinds generated from symbolic residuals (symforce_gb300/factor_defs.py, emitted by
+// symforce_gb300/codegen.py): traits and evaluation forward to the generated structs.
+// ---------------------------------------------------------------------------------------------
+}  // namespace sfg
+#include "generated_factor_specs.h"
+#include "generated_factors.cuh"
+namespace sfg {
+#define SFG_GENERATED_KIND(KIND, NKEYS, NCONSTS, RDIM, K0, K1, K2, G)                              \
+  template <>                                                                                      \
+  struct FactorTraits<KIND> {                                                                      \
+    static constexpr int NK = G::NK, NC = G::NC, RD = G::RD, TD = G::TD, MK = 0;                   \
+    static constexpr SFG_HD int KT(int k) { return G::KT(k); }                                     \
+    static constexpr SFG_HD int KS(int k) { return G::KS(k); }                                     \
+  };                                                                                               \
+  template <typename T>                                                                            \
+  struct FactorEval<KIND, T> {                                                                     \
+    static SFG_HD void Run(const double* const* x, const double* c, double* r, T* J) {             \
+      G::template Run<T>(x, c, r, J);                                                              \
+    }                                                                                              \
+  };
+SFG_GENERATED_FACTORS(SFG_GENERATED_KIND)
+#undef SFG_GENERATED_KIND
 
 }  // namespace sfg

@@ -259,6 +259,12 @@ void LaunchLinearize(int kind, const LinOut& out, const BatchDev& b, cudaStream_
     case SFG_FACTOR_RANGE_POSE3:
       LinearizeKernel<SFG_FACTOR_RANGE_POSE3, T><<<grid, kLinBlock, 0, s>>>(out, b);
       break;
+#define SFG_GENERATED_CASE(KIND, NKEYS, NCONSTS, RDIM, K0, K1, K2, G) \
+    case KIND:                                                         \
+      LinearizeKernel<KIND, T><<<grid, kLinBlock, 0, s>>>(out, b);     \
+      break;
+      SFG_GENERATED_FACTORS(SFG_GENERATED_CASE)
+#undef SFG_GENERATED_CASE
   }
 }
 

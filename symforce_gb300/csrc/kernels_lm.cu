@@ -49,8 +49,12 @@ __global__ void RetractKernel(RetractDev r, const LmParams* p, const LmState* st
     case SFG_KEY_POSE3:  // gen/cpp/sym/ops/pose3/lie_group_ops.cc:69-102
       RetractPose3(a, d, p->epsilon, o);
       break;
+    case SFG_KEY_ROT3:  // gen/cpp/sym/ops/rot3/lie_group_ops.cc: the rotation part of the above
+      RetractRot3(a, d, p->epsilon, o);
+      break;
     default: {
-      const int n = r.key_type[k];  // VEC1..VEC3: the type value is the dimension
+      const int t = r.key_type[k];  // VEC1..VEC3 = 1..3, VEC4..VEC6 = 7..9
+      const int n = t <= SFG_KEY_VEC3 ? t : t - SFG_KEY_VEC4 + 4;
       for (int i = 0; i < n; ++i) o[i] = a[i] + d[i];
     }
   }

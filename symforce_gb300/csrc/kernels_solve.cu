@@ -406,6 +406,7 @@ struct alignas(16) TileSmem {
   T a[TILE * TILE];  // a and b are contiguous: together they hold a double tile (FP64 redo of a tile)
   T b[TILE * TILE];
   T c[TILE * TILE];
+  T w[TILE * TILE];  // L D of the look-ahead's panel tile
   T d[TILE];
 };
 
@@ -525,6 +526,38 @@ __device__ __forceinline__ void LdltStepsCta(D* a, int b) {
   }
 }
 
+// LDL^T of a 16 x 16 FP64 tile and the inverse of its unit lower factor, by one warp with the rows
+// in registers (Gauss-Jordan on [A | I]).  Lane r < 16 holds row r of the tile (v[c] = A(r, c); only
+// c <= r is read), lane 16 + r row r of the identity.  Pivot j applies one row operation to both
+// halves, row_r -= L(r, j) row_j for r > j: the tile's lanes update their columns c > j with the
+// pivot column A(c, j) (the trailing block stays symmetric), the identity's lanes their columns
+// c <= j with row j of their half, which ends as L^-1 (row operations give L^-1 A = D L^T on the
+// left and L^-1 on the right).  On return lane r < 16 holds L(r, c) for c < r and D(r) at c = r,
+// lane 16 + r row r of L^-1.  Rows at or beyond the tile's size must be identity rows.  One
+// shuffle per column and pivot serves both halves (the sender picks what its half is asked for),
+// and the pivot's reciprocal is formed once per pivot for the whole warp.
+__device__ __forceinline__ void WarpLdltInv16(double (&v)[16], int lane) {
+  constexpr unsigned kAll = 0xffffffffu;
+  const bool top = lane < 16;
+  const int r = lane & 15;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const double dj = __shfl_sync(kAll, v[j], j);
+    const double inv = PivotReciprocal<double>(dj);
+    const double l = v[j] * inv;               // L(r, j) on the tile's lanes r > j
+    const double m = __shfl_sync(kAll, l, r);  // the identity's lanes take their row's multiplier
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      if (c == j) continue;
+      const double send = top ? v[j] : v[c];
+      const double p = __shfl_sync(kAll, send, top ? c : 16 + j);
+      if (r > j && (top ? c > j : c < j)) v[c] = fma(-m, p, v[c]);
+    }
+    // column j: L(r, j) on the tile's lanes; the identity's row j has 1 there, so row r gets -m
+    if (r > j) v[j] = top ? l : -m;
+  }
+}
+
 // A pivot of an FP32 diagonal tile that kept less than this fraction of its diagonal entry (more
 // than 12 of FP32's 24 bits cancelled), or is not positive, sends the tile to the FP64 redo.
 constexpr float kNearSingularPivot = 1.0f / 4096.0f;
@@ -545,18 +578,34 @@ __device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, 
   T* Fs = F + g.foff;
   T* li = sm.b;
   if constexpr (sizeof(T) == 8) {
-    LdltStepsCta<T, TILE>(a, b);
-    // unit lower inverse by forward substitution on all columns at once: after step q, row q of Li
-    // is final and is eliminated from the rows below it
-    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) li[e] = T((e % TILE) == (e / TILE) ? 1 : 0);
-    __syncthreads();
-    for (int q = 0; q + 1 < b; ++q) {
-      for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
-        const int r = e % TILE, c = e / TILE;
-        if (r > q && r < b && c <= q) li[c * TILE + r] -= a[q * TILE + r] * li[c * TILE + q];
+    static_assert(sizeof(T) != 8 || TILE == 16, "the FP64 warp elimination is written for 16 x 16 tiles");
+    // one warp: the tile and the identity eliminated together (L, D and L^-1), written straight
+    // from registers; the other warps go on to the signal
+    if (threadIdx.x < 32) {
+      const int lane = threadIdx.x, r = lane & 15;
+      const bool top = lane < 16;
+      double v[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        double x = c == r ? 1.0 : 0.0;
+        if (top && r < b && c < b && c <= r) x = double(a[c * TILE + r]);
+        v[c] = x;
       }
-      __syncthreads();
+      WarpLdltInv16(v, lane);
+      T* Lk = Linv + f.linv_base[s] + int64_t(k) * TILE * TILE;
+      if (top) {
+        if (r < b) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c)
+            if (c <= r) St(Fs + (r0 + r) + int64_t(r0 + c) * g.m, T(v[c]));
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) St(Lk + c * TILE + r, T(c <= r ? v[c] : 0.0));
+      }
     }
+    Signal(f.tile_state + StateIdx(g, k, k), kFinal);
+    return;
   } else {
     // the tile's input, kept for an FP64 redo
     T* orig = sm.c;
@@ -645,6 +694,21 @@ __device__ void TaskDiag(const FactorDev& f, int s, int k, T* F, T* Linv, TileSm
   DiagCore<T, TILE>(f, g, s, k, F, Linv, sm.a, sm);
 }
 
+// sum_{q < n} x[q * TILE + r] y[q * TILE + c] over two tiles held transposed in shared memory, with
+// two accumulation chains (a dependent FP64 multiply-add costs 64 cycles on this GPU) added at
+// the end in a fixed order.
+template <typename T, int TILE>
+__device__ __forceinline__ T PanelDot(const T* x, const T* y, int r, int c, int n) {
+  T s0 = T(0), s1 = T(0);
+  int q = 0;
+  for (; q + 2 <= n; q += 2) {
+    s0 = fma(x[q * TILE + r], y[q * TILE + c], s0);
+    s1 = fma(x[(q + 1) * TILE + r], y[(q + 1) * TILE + c], s1);
+  }
+  if (q < n) s0 = fma(x[q * TILE + r], y[q * TILE + c], s0);
+  return s0 + s1;
+}
+
 // Panel solve L_ik = F_ik L_kk^-T D_k^-1 as a product with the stored inverse.
 template <typename T, int TILE>
 __device__ void TaskTrsm(const FactorDev& f, int s, int i, int k, T* F, const T* Linv,
@@ -665,14 +729,12 @@ __device__ void TaskTrsm(const FactorDev& f, int s, int i, int k, T* F, const T*
   for (int c = threadIdx.x; c < bk; c += blockDim.x)
     sm.d[c] = PivotReciprocal<T>(Ld(Fs + int64_t(ck + c) * (g.m + 1)));
   __syncthreads();
-  // W(r, c) = sum_{q <= c} F(r, q) Li(c, q);  Li(c, q) = b[q * TILE + c]
+  // W(r, c) = sum_{q <= c} F(r, q) Li(c, q);  Li(c, q) = b[q * TILE + c]; two accumulation chains
   T out[TILE * TILE >= kFactorThreads ? TILE * TILE / kFactorThreads : 1];
   int n = 0;
   for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x, ++n) {
     const int r = e % TILE, c = e / TILE;
-    T acc = T(0);
-    for (int q = 0; q <= c && q < bk; ++q) acc += sm.a[q * TILE + r] * sm.b[q * TILE + c];
-    out[n] = acc * sm.d[c < bk ? c : 0];
+    out[n] = PanelDot<T, TILE>(sm.a, sm.b, r, c, min(c + 1, bk)) * sm.d[c < bk ? c : 0];
   }
   n = 0;
   for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x, ++n) {
@@ -705,13 +767,15 @@ __device__ void TaskLookahead(const FactorDev& f, int s, int i, int k, T* F, T* 
   for (int c = threadIdx.x; c < bk; c += blockDim.x)
     sm.d[c] = PivotReciprocal<T>(Ld(Fs + int64_t(ck + c) * (g.m + 1)));
   __syncthreads();
-  // L_ik (r, c) = sum_{q <= c} F(r, q) Li(c, q) / D_c, into c[] (transposed) and the front
+  // L_ik (r, c) = sum_{q <= c} F(r, q) Li(c, q) / D_c, into c[] (transposed) and the front, and
+  // L_ik D into w[]
   for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
     const int r = e % TILE, c = e / TILE;
-    T acc = T(0);
-    for (int q = 0; q <= c && q < bk; ++q) acc += sm.a[q * TILE + r] * sm.b[q * TILE + c];
-    const T l = (r < bi && c < bk) ? acc * sm.d[c < bk ? c : 0] : T(0);
+    const T acc = PanelDot<T, TILE>(sm.a, sm.b, r, c, min(c + 1, bk));
+    const T inv = sm.d[c < bk ? c : 0];
+    const T l = (r < bi && c < bk) ? acc * inv : T(0);
     sm.c[c * TILE + r] = l;
+    sm.w[c * TILE + r] = (r < bi && c < bk) ? acc : T(0);  // F Li^T = L D
     if (r < bi && c < bk) St(Fs + (ri + r) + int64_t(ck + c) * g.m, l);
   }
   Signal(f.tile_state + StateIdx(g, i, k), kFinal);
@@ -720,15 +784,11 @@ __device__ void TaskLookahead(const FactorDev& f, int s, int i, int k, T* F, T* 
   if (threadIdx.x == 0) ok = WaitAtLeast(f.tile_state + StateIdx(g, i, i), 1 + k, f.error);
   if (!CtaWait(ok, s_flag)) return;
   LoadTileT<T, TILE>(Fs, g.m, ri, ri, bi, bi, sm.a);
-  for (int c = threadIdx.x; c < bk; c += blockDim.x) sm.d[c] = Ld(Fs + int64_t(ck + c) * (g.m + 1));
   __syncthreads();
   for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
     const int r = e % TILE, c = e / TILE;
     if (r >= bi || c > r) continue;
-    T acc = T(0);
-#pragma unroll 8
-    for (int q = 0; q < bk; ++q) acc += sm.c[q * TILE + r] * sm.d[q] * sm.c[q * TILE + c];
-    sm.a[c * TILE + r] -= acc;
+    sm.a[c * TILE + r] -= PanelDot<T, TILE>(sm.w, sm.c, r, c, bk);
   }
   __syncthreads();
   DiagCore<T, TILE>(f, g, s, i, F, Linv, sm.a, sm);
@@ -772,10 +832,7 @@ __device__ void TaskUpdate(const FactorDev& f, int s, int i, int j, int k, T* F,
     for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x, ++n) {
       const int r = e % TILE, c = e / TILE;
       if (r >= bi || c >= bj || (i == j && r < c)) continue;
-      T acc = T(0);
-#pragma unroll 8
-      for (int q = 0; q < bk; ++q) acc += sm.a[q * TILE + r] * sm.b[q * TILE + c];
-      St(Fs + (ri + r) + int64_t(rj + c) * g.m, cdst[n] - acc);
+      St(Fs + (ri + r) + int64_t(rj + c) * g.m, cdst[n] - PanelDot<T, TILE>(sm.a, sm.b, r, c, bk));
     }
   }
   Signal(f.tile_state + StateIdx(g, i, j), 2 + k);

@@ -24,6 +24,29 @@ __device__ __forceinline__ unsigned long long LmGlobalTimer() {
 
 // Reset (symforce/opt/levenberg_marquardt_solver.h:163-175) + Step of the first Iterate.
 __device__ __forceinline__ void LmBegin(const LmParams& p, LmState& st, int reset_indices) {
+  if (p.continue_state) {
+    // ResetState (symforce/opt/levenberg_marquardt_solver.h:176-183): lambda, nu and the iteration
+    // counter carry over; the caller's values become New and every linearization is reset
+    if (p.relax_damping) {
+      st.lambda = fmin(st.lambda, p.initial_lambda);
+      st.nu = p.dynamic_beta;
+    }
+    st.have_max_diagonal = 0;
+    st.have_last_update = 0;
+    st.num_records = 0;
+    st.best_index = -1;
+    st.status = 0;
+    st.failure_reason = 0;
+    st.done = 0;
+    st.device_error = 0;
+    st.t_start = LmGlobalTimer();
+    const int t = st.init_idx;
+    st.init_idx = st.new_idx;
+    st.new_idx = t;
+    st.iteration += 1;
+    st.max_iterations = st.iteration + p.iterations;
+    return;
+  }
   if (reset_indices) {
     st.init_idx = 0;
     st.new_idx = 1;
@@ -58,6 +81,15 @@ __device__ __forceinline__ int LmFirstRecord(const LmParams& p, LmState& st, sfg
     st.best_idx = st.init_idx;
   }
   const double e = st.error[st.init_idx];
+  if (p.continue_state) {
+    // the iteration -1 record and the initial-error check belong to iteration 0 only
+    // (symforce/opt/levenberg_marquardt_solver.tcc:157-186)
+    if (st.iteration >= st.max_iterations) {
+      st.done = 1;
+      return 0;
+    }
+    return 1;
+  }
   sfg_iteration_t r{};
   r.iteration = -1;
   r.new_error = e;

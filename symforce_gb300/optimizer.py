@@ -41,6 +41,9 @@ def lib() -> C.CDLL:
         L.sfg_set_values.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int64]
         L.sfg_get_values.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_int64]
         L.sfg_optimize.argtypes = [C.c_void_p, C.POINTER(A.OptimizerParams), C.c_int32, C.POINTER(A.StatsC)]
+        L.sfg_optimize_continue.argtypes = [C.c_void_p, C.POINTER(A.OptimizerParams), C.c_int32, C.c_int32,
+                                            C.POINTER(A.StatsC)]
+        L.sfg_set_factor_consts.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int64]
         L.sfg_linearize.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                     C.POINTER(C.c_double)]
         L.sfg_hessian_lower.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
@@ -204,6 +207,25 @@ class Optimizer:
         _check(lib().sfg_get_values(self._h, A.dptr(out), out.size))
         return out, stats
 
+    def optimize_continue(self, num_iterations: int, params: A.OptimizerParams | None = None,
+                          relax_damping: bool = True) -> OptimizationStats:
+        """The loop of GncOptimizer::OptimizeContinue (symforce/opt/gnc_optimizer.h:113-121): ResetState
+        on the best values of the last call (lambda, nu and the iteration counter carry over), with
+        RelaxDampingToInitial first when `relax_damping`.  Returns only the new records; best_index is
+        -1 when none of them improved on the starting state."""
+        p = params or self.params
+        cap = num_iterations + 1
+        recs = (A.IterationC * cap)()
+        st = A.StatsC(recs, cap, 0, 0, 0, 0, 0, 0.0)
+        _check(lib().sfg_optimize_continue(self._h, C.byref(p), num_iterations, int(relax_damping), C.byref(st)))
+        return OptimizationStats([recs[i] for i in range(st.num_iterations)], st.best_index, st.status,
+                                 st.failure_reason, st.kernel_launches, st.device_ms)
+
+    def set_factor_consts(self, batch: int, consts: np.ndarray) -> None:
+        """Replace the constants of one factor batch (the caller's factor order)."""
+        c = np.ascontiguousarray(consts, dtype=np.float64)
+        _check(lib().sfg_set_factor_consts(self._h, batch, A.dptr(c), c.size))
+
     def time_stage(self, stage: int, reps: int = 20) -> dict:
         """CUDA-event time of one stage of the LM iteration (after an optimize call)."""
         ms, by, fm = C.c_double(), C.c_double(), C.c_double()
@@ -269,6 +291,50 @@ class Optimizer:
         perm = np.zeros(size, dtype=np.int32)
         _check(lib().sfg_permutation(self._h, A.iptr(perm), size))
         return perm
+
+
+class GncOptimizer:
+    """sym::GncOptimizer<Optimizer> (symforce/opt/gnc_optimizer.h:22-110) over the device loop.
+
+    The reference keeps mu as a Values entry that the robust factors read; here it is a constant of
+    the factors that take it, named by (batch index, constant index) pairs in `mu_slots`, which the
+    schedule rewrites on the device (sfg_set_factor_consts) before every stage."""
+
+    def __init__(self, problem: A.ProblemArrays, params: A.OptimizerParams, gnc_params,
+                 mu_slots, form: A.FormParams | None = None):
+        self.problem = problem
+        self.params = params
+        self.gnc_params = gnc_params
+        self.mu_slots = list(mu_slots)
+        self.optimizer = Optimizer(problem, params, form)
+        self._consts = {b: np.array(problem.batches[b].consts, dtype=np.float64, copy=True)
+                        for b, _ in self.mu_slots}
+
+    def _set_mu(self, mu: float) -> None:
+        for b, ci in self.mu_slots:
+            self._consts[b][:, ci] = mu
+        for b in self._consts:
+            self.optimizer.set_factor_consts(b, self._consts[b])
+
+    def optimize(self, values: np.ndarray, num_iterations: int = -1):
+        """GncOptimizer::Optimize: returns (best values, OptimizationStats) with the records of every
+        stage, and the final mu in stats.mu."""
+        from . import gnc
+
+        def run(p, n, cont, relax):
+            if not cont:
+                _, st = self.optimizer.optimize(values, num_iterations=n, params=p)
+            else:
+                st = self.optimizer.optimize_continue(n, params=p, relax_damping=relax)
+            return st.iterations, st.best_index, st.status, st.failure_reason
+
+        r = gnc.run_gnc(self.params, self.gnc_params, self._set_mu, run, num_iterations)
+        stats = OptimizationStats(r["iterations"], r["best_index"], r["status"], r["failure_reason"])
+        stats.mu = r["mu"]
+        return self.optimizer.get_values(), stats
+
+    def close(self) -> None:
+        self.optimizer.close()
 
 
 class SparseLdlt:

@@ -201,6 +201,49 @@ for k in range(4):
     r, J = evaluate(res, [v], subs)
     vectors.append(dict(kind=5, key_types=[5], storage=sv_, consts=sp + sq + [e_val], residual=r, jacobian=J))
 
+# ---- kinds the library generates from symbolic definitions: between / prior Rot3
+# (geo_factors_codegen.py:53-86 with sf.Rot3), diagonal sqrt_info
+for k in range(3):
+    a, b, m = sf.Rot3.symbolic("a"), sf.Rot3.symbolic("b"), sf.Rot3.symbolic("m")
+    s = sf.V3.symbolic("s")
+    eps = sf.Symbol("eps")
+    res = geo_factors_codegen.between_factor(a, b, m, sf.Matrix.diag(s.to_flat_list()), eps)
+    sa, sb, sm = rand_quat(), rand_quat(), rand_quat()
+    sv = list(rng.uniform(1, 20, size=3))
+    e_val = 1e-10
+    subs = {**subs_for(a, sa), **subs_for(b, sb), **subs_for(m, sm), **dict(zip(s.to_flat_list(), sv)),
+            eps: e_val}
+    r, J = evaluate(res, [a, b], subs)
+    vectors.append(dict(kind=8, key_types=[6, 6], storage=sa + sb, consts=sm + sv + [e_val], residual=r,
+                        jacobian=J))
+for k in range(3):
+    v, p = sf.Rot3.symbolic("v"), sf.Rot3.symbolic("p")
+    s = sf.V3.symbolic("s")
+    eps = sf.Symbol("eps")
+    res = geo_factors_codegen.prior_factor(v, p, sf.Matrix.diag(s.to_flat_list()), eps)
+    sv_, sp_ = rand_quat(), rand_quat()
+    sq = list(rng.uniform(1, 20, size=3))
+    e_val = 1e-10
+    subs = {**subs_for(v, sv_), **subs_for(p, sp_), **dict(zip(s.to_flat_list(), sq)), eps: e_val}
+    r, J = evaluate(res, [v], subs)
+    vectors.append(dict(kind=7, key_types=[6], storage=sv_, consts=sp_ + sq + [e_val], residual=r, jacobian=J))
+
+# ---- the GNC test factor (test/symforce_gnc_codegen_test.py:24-31): Barron whitening of x - y with
+# alpha from the convexity parameter mu (noise_models.py BarronNoiseModel.compute_alpha_from_mu)
+for mu_val in (0.0, 0.33, 0.66, 0.99):
+    x, y = sf.V5.symbolic("x"), sf.V5.symbolic("y")
+    mu, eps = sf.symbols("mu eps")
+    alpha = BarronNoiseModel.compute_alpha_from_mu(mu, eps)
+    nm = BarronNoiseModel(alpha=alpha, delta=1, scalar_information=1, x_epsilon=eps)
+    res = nm.whiten(x - y)
+    xv = list(rng.normal(0, 1, size=5))
+    yv = list(rng.normal(0, 1, size=5) + (10.0 if mu_val > 0.5 else 0.0))
+    e_val = 2.220446049250313e-15
+    subs = {**subs_for(x, xv), **subs_for(y, yv), mu: mu_val, eps: e_val}
+    r, J = evaluate(res, [x], subs)
+    vectors.append(dict(kind=9, key_types=[8], storage=xv, consts=yv + [mu_val, e_val], residual=r,
+                        jacobian=J))
+
 OUT.write_text(json.dumps(dict(generator="tests/golden/make_symforce_factor_vectors.py",
                                digits=DIGITS, vectors=vectors), indent=1))
 print(f"wrote {len(vectors)} vectors to {OUT}")

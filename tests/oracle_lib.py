@@ -136,3 +136,60 @@ def pose_smoothing_initial_values(num_keys=10, epsilon=A.DEFAULT_EPSILON):
     _check(lib().orc_pose_smoothing_initial_values(C.c_int32(num_keys), C.c_double(epsilon),
                                                    A.dptr(out)))
     return out
+
+
+def optimize_carry(problem: A.ProblemArrays, params, num_iterations, carry, continue_state,
+                   epsilon=A.DEFAULT_EPSILON, values=None):
+    """orc_optimize_carry: a fresh run (continue_state False) or OptimizeContinue from `carry`
+    ([lambda, nu, iteration], updated in place)."""
+    pc = problem.to_c()
+    v = problem.values if values is None else np.ascontiguousarray(values, dtype=np.float64)
+    out = np.zeros_like(v)
+    cap = num_iterations + 2
+    iters = (A.IterationC * cap)()
+    n, best, status, reason = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+    _check(lib().orc_optimize_carry(C.byref(pc), A.dptr(v), C.byref(params), C.c_int32(num_iterations),
+                                    C.c_double(epsilon), C.c_int32(A.SFG_LINEAR_SOLVER_SPARSE_LDLT),
+                                    C.c_int32(A.SFG_ORDERING_MIN_DEGREE), A.dptr(out), iters,
+                                    C.c_int32(cap), C.byref(n), C.byref(best), C.byref(status),
+                                    C.byref(reason), A.dptr(carry), C.c_int32(1 if continue_state else 0)))
+    return dict(values=out, iterations=[iters[i] for i in range(n.value)], best_index=best.value,
+                status=status.value, failure_reason=reason.value)
+
+
+def gnc_optimize(problem: A.ProblemArrays, params, gnc_params, mu_slots, epsilon=A.DEFAULT_EPSILON,
+                 num_iterations=-1):
+    """The GNC schedule (symforce_gb300.gnc.run_gnc) over the oracle's LM loop."""
+    from symforce_gb300 import gnc
+    state = dict(values=problem.values.copy(), carry=np.zeros(3))
+    consts = {b: np.array(problem.batches[b].consts, dtype=np.float64, copy=True) for b, _ in mu_slots}
+
+    def set_mu(mu):
+        for b, ci in mu_slots:
+            consts[b][:, ci] = mu
+            problem.batches[b].consts = consts[b]
+
+    def run(p, n, cont, relax):
+        if relax:
+            state["carry"][0] = min(state["carry"][0], p.initial_lambda)
+            state["carry"][1] = p.dynamic_lambda_update_beta
+        r = optimize_carry(problem, p, n, state["carry"], cont, epsilon=epsilon, values=state["values"])
+        state["values"] = r["values"]
+        return r["iterations"], r["best_index"], r["status"], r["failure_reason"]
+
+    r = gnc.run_gnc(params, gnc_params, set_mu, run, num_iterations)
+    r["values"] = state["values"]
+    return r
+
+
+def mt19937_normal_vectors(seed, num_vectors, dim):
+    out = np.zeros((num_vectors, dim))
+    _check(lib().orc_mt19937_normal_vectors(C.c_uint32(seed), C.c_int32(num_vectors), C.c_int32(dim),
+                                            A.dptr(out)))
+    return out
+
+
+def rot3_smoothing_initial_values(num_keys=10, epsilon=A.DEFAULT_EPSILON):
+    out = np.zeros(4 * num_keys)
+    _check(lib().orc_rot3_smoothing_initial_values(C.c_int32(num_keys), C.c_double(epsilon), A.dptr(out)))
+    return out

@@ -91,3 +91,110 @@ POSE_SMOOTHING_EXPECTED = dict(last_iteration=12, lambda_approx=(0.0039, 1e-1), 
 # linearization has 66 residual rows, a 60 x 60 lower Hessian with 534 stored entries and 60 rhs rows.
 DYNAMIC_LAMBDA_EXPECTED = dict(num_records=27, residual_rows=66, hessian_dim=60, hessian_nnz=534,
                                rhs_rows=60)
+
+
+def rot3_smoothing(initial_values: np.ndarray, num_keys: int = 10) -> A.ProblemArrays:
+    """"Test Rotation smoothing" (test/symforce_optimizer_test.cc:183-261): Rot3 priors at the first
+    (identity, sigma 0.1 rad) and last key (yaw pi, sigma 0.1 rad), identity between factors
+    (sigma 0.5 rad) in a chain, factor epsilon 1e-15; generated PRIOR_ROT3 / BETWEEN_ROT3 kinds."""
+    eps = 1e-15
+    prior_start = [0.0, 0.0, 0.0, 1.0]
+    prior_last = list(ypr_quaternion(math.pi, 0, 0))
+    prior_consts = [prior_start + [1 / 0.1] * 3 + [eps], prior_last + [1 / 0.1] * 3 + [eps]]
+    between_consts = [[0.0, 0.0, 0.0, 1.0] + [1 / 0.5] * 3 + [eps] for _ in range(num_keys - 1)]
+    return A.ProblemArrays(
+        key_types=[A.SFG_KEY_ROT3] * num_keys,
+        batches=[A.Batch(A.SFG_FACTOR_PRIOR_ROT3, [[0], [num_keys - 1]], prior_consts),
+                 A.Batch(A.SFG_FACTOR_BETWEEN_ROT3, [[i, i + 1] for i in range(num_keys - 1)], between_consts)],
+        values=initial_values,
+        name="rot3_smoothing",
+    )
+
+
+ROT3_SMOOTHING_PARAMS = dict(iterations=50, early_exit_min_reduction=0.0001)
+ROT3_SMOOTHING_EXPECTED = dict(last_iteration=6, lambda_approx=(2.4e-4, 1e-1), error_approx=(2.174, 1e-3))
+
+
+def linear_problem(J: np.ndarray) -> A.ProblemArrays:
+    """"Converges for a linear problem in one iteration" (test/symforce_levenberg_marquardt_test.cc:
+    17-88): r = J x for a random 9 x 5 J, x initialised to 100 * ones."""
+    return A.ProblemArrays(
+        key_types=[A.SFG_KEY_VEC5],
+        batches=[A.Batch(A.SFG_FACTOR_LINEAR_VEC5, [[0]], [np.concatenate([J.ravel(), np.zeros(9)])])],
+        values=np.full(5, 100.0),
+        name="linear_problem",
+    )
+
+
+def linear_problem_params() -> A.OptimizerParams:
+    """The test's optimizer_params_t{} (value-initialised) with the fields it sets: one iteration of
+    undamped Gauss-Newton (no diagonal or unit damping), STATIC lambda."""
+    p = A.default_optimizer_params()
+    for f, _ in A.OptimizerParams._fields_:
+        setattr(p, f, 0)
+    p.debug_stats = 1
+    p.initial_lambda = 1.0
+    p.lambda_update_type = A.SFG_LAMBDA_UPDATE_STATIC
+    p.lambda_up_factor = 3.0
+    p.lambda_down_factor = 1.0 / 3.0
+    p.lambda_lower_bound = 0.0
+    p.lambda_upper_bound = 0.0
+    p.iterations = 1
+    p.use_diagonal_damping = 0
+    p.use_unit_damping = 0
+    return p
+
+
+LINEAR_PROBLEM_EPSILON = 1e-10
+
+
+def gnc_problem(y: np.ndarray) -> A.ProblemArrays:
+    """"Test GNC" (test/symforce_gnc_test.cc:22-76): x in R^5 (initialised to ones) pulled towards 20
+    samples y_i by Barron-whitened factors whose convexity parameter mu is a constant of the
+    generated BARRON_VEC5 kind (constant 5); factor epsilon kDefaultEpsilon."""
+    n = y.shape[0]
+    eps = A.DEFAULT_EPSILON
+    consts = np.concatenate([y, np.zeros((n, 1)), np.full((n, 1), eps)], axis=1)
+    return A.ProblemArrays(
+        key_types=[A.SFG_KEY_VEC5],
+        batches=[A.Batch(A.SFG_FACTOR_BARRON_VEC5, [[0]] * n, consts)],
+        values=np.ones(5),
+        name="gnc",
+    )
+
+
+def gnc_samples(draws: np.ndarray, n_outliers: int = 3) -> np.ndarray:
+    """y_i = 10 + 0.1 r_i for the first n_outliers samples, 0.1 r_i after (symforce_gnc_test.cc:34-42)."""
+    y = 0.1 * draws
+    y[:n_outliers] += 10.0
+    return y
+
+
+GNC_OPTIMIZER_EPSILON = 1e-12
+GNC_MU_SLOTS = [(0, 5)]
+GNC_EXPECTED = dict(num_records=9)
+
+
+def gnc_params():
+    from symforce_gb300.gnc import GncParams
+    return GncParams(gnc_update_min_reduction=1e-3, mu_initial=0.0, mu_step=0.33, mu_max=0.99)
+
+
+def linearizer_problem(factor_order: str, key_order: str) -> A.ProblemArrays:
+    """test/symforce_linearizer_test.cc:16-127: two linear factors J1 = diag(1, 2) and J2 = diag(3, 4)
+    on scalar keys x = 10, y = -20, in either factor order and either key order (the reference's
+    dense and sparse factors have the same math; both are the LINEAR_SCALAR2 kind here)."""
+    J1 = [1.0, 0.0, 0.0, 2.0]
+    J2 = [3.0, 0.0, 0.0, 4.0]
+    xy = {"x": 10.0, "y": -20.0}
+    order = list(key_order)  # e.g. "xy" or "yx"
+    idx = {k: i for i, k in enumerate(order)}
+    factors = [J1, J2] if factor_order == "dense_sparse" else [J2, J1]
+    keys = [[idx["x"], idx["y"]]] * 2
+    consts = [J + [0.0, 0.0] for J in factors]
+    return A.ProblemArrays(
+        key_types=[A.SFG_KEY_VEC1, A.SFG_KEY_VEC1],
+        batches=[A.Batch(A.SFG_FACTOR_LINEAR_SCALAR2, keys, consts)],
+        values=np.array([xy[k] for k in order]),
+        name="linearizer",
+    )

@@ -170,3 +170,79 @@ def test_generated_functor_matches_library_factor(lib, name):
             out[which] = (r, J)
         np.testing.assert_allclose(out["gen"][0], out["ref"][0], rtol=1e-10, atol=1e-12)
         np.testing.assert_allclose(out["gen"][1], out["ref"][1], rtol=1e-8, atol=1e-9)
+
+
+# ---- the generated factor kinds the library registers (symforce_gb300/factor_defs.py) ----------
+
+def test_committed_generated_headers_are_current(tmp_path):
+    """generated_factors.cuh / generated_factor_specs.h are what the generator writes from
+    factor_defs.py today."""
+    p_dev, p_spec = codegen.write_generated(tmp_path)
+    assert p_dev.read_text() == (CSRC / "generated_factors.cuh").read_text()
+    assert p_spec.read_text() == (CSRC / "generated_factor_specs.h").read_text()
+
+
+@pytest.fixture(scope="module")
+def genlib(tmp_path_factory):
+    gxx = shutil.which("g++")
+    cuda_inc = Path("/usr/local/cuda/include")
+    if gxx is None or not (cuda_inc / "cuda_runtime.h").exists():
+        pytest.skip("g++ or the CUDA headers are not available")
+    src = ['#include <cmath>', '#include "factor_math.cuh"', 'extern "C" {']
+    from symforce_gb300 import factor_defs
+    for fd in factor_defs.GENERATED:
+        nk = len(fd.key_types)
+        src.append(f"void eval_{fd.kind}(const double* const* x, const double* c, double* r, double* J) "
+                   f"{{ sfg::FactorEval<{fd.kind}, double>::Run(x, c, r, J); }}")
+    src.append("}")
+    d = tmp_path_factory.mktemp("genkinds")
+    (d / "gen.cpp").write_text("\n".join(src))
+    out = d / "libgenkinds.so"
+    subprocess.run([gxx, "-O1", "-std=c++17", "-shared", "-fPIC", f"-I{cuda_inc}", f"-I{ROOT / 'include'}",
+                    f"-I{CSRC}", str(d / "gen.cpp"), "-o", str(out)], check=True)
+    return C.CDLL(str(out))
+
+
+def _golden_generated():
+    import json
+    from symforce_gb300 import factor_defs
+    kinds = {fd.kind for fd in factor_defs.GENERATED}
+    vecs = json.loads((ROOT / "tests" / "golden" / "factor_vectors.json").read_text())["vectors"]
+    return [v for v in vecs if v["kind"] in kinds]
+
+
+@pytest.mark.parametrize("vec", _golden_generated(), ids=lambda v: f"kind{v['kind']}")
+def test_generated_kind_matches_symforce_symbolic(genlib, vec):
+    """The registered generated kinds (compiled here with g++) against the golden vectors evaluated
+    from the reference's own symbolic definitions."""
+    kind = vec["kind"]
+    nk, _, rd, kt = A.FACTOR_DIMS[kind]
+    td = sum(A.KEY_DIMS[t][1] for t in kt)
+    st = np.array(vec["storage"])
+    offs = np.cumsum([0] + [A.KEY_DIMS[t][0] for t in kt])
+    keys = [np.ascontiguousarray(st[offs[k]:offs[k + 1]]) for k in range(nk)]
+    xp = (C.c_void_p * nk)(*[k.ctypes.data_as(C.c_void_p) for k in keys])
+    c = np.array(vec["consts"])
+    r, J = np.zeros(rd), np.zeros(rd * td)
+    getattr(genlib, f"eval_{kind}")(xp, c.ctypes.data_as(C.c_void_p), r.ctypes.data_as(C.c_void_p),
+                                   J.ctypes.data_as(C.c_void_p))
+    np.testing.assert_allclose(r, vec["residual"], rtol=1e-10, atol=1e-12)
+    Jg = np.array(vec["jacobian"])
+    np.testing.assert_allclose(J.reshape(rd, td), Jg, rtol=1e-8, atol=1e-9 * max(1.0, np.abs(Jg).max()))
+
+
+def test_generated_linear_kinds_against_numpy(genlib):
+    """LINEAR_VEC5 / LINEAR_SCALAR2: residual J x + b and Jacobian J."""
+    rng = np.random.default_rng(4)
+    for kind, rows, cols, kt in [(A.SFG_FACTOR_LINEAR_VEC5, 9, 5, [5]), (A.SFG_FACTOR_LINEAR_SCALAR2, 2, 2, [1, 1])]:
+        Jm = rng.normal(size=(rows, cols))
+        b = rng.normal(size=rows)
+        x = rng.normal(size=cols)
+        keys = [np.ascontiguousarray(x)] if len(kt) == 1 else [np.ascontiguousarray(x[:1]), np.ascontiguousarray(x[1:])]
+        xp = (C.c_void_p * len(keys))(*[k.ctypes.data_as(C.c_void_p) for k in keys])
+        c = np.concatenate([Jm.ravel(), b])
+        r, J = np.zeros(rows), np.zeros(rows * cols)
+        getattr(genlib, f"eval_{kind}")(xp, c.ctypes.data_as(C.c_void_p), r.ctypes.data_as(C.c_void_p),
+                                       J.ctypes.data_as(C.c_void_p))
+        np.testing.assert_allclose(r, Jm @ x + b, rtol=1e-13, atol=1e-13)
+        np.testing.assert_allclose(J.reshape(rows, cols), Jm, rtol=0, atol=0)

@@ -164,3 +164,68 @@ def test_ba_oracle_fixture_is_reproducible():
     w = workloads.get("robot2d_1000")
     r = O.optimize(w.problem(), w.params())
     assert r["iterations"][r["best_index"]].new_error == pytest.approx(fx["robot2d_1000"]["best_error"], rel=1e-12)
+
+
+def test_rot3_smoothing_known_answers():
+    """test/symforce_optimizer_test.cc:183-261 (generated Rot3 prior / between kinds): last
+    iteration 6, lambda ~2.4e-4, error ~2.174, SUCCESS, and H == lower(J^T J)."""
+    p = R.rot3_smoothing(O.rot3_smoothing_initial_values())
+    r = O.optimize(p, A.default_optimizer_params(**R.ROT3_SMOOTHING_PARAMS))
+    last = r["iterations"][-1]
+    E = R.ROT3_SMOOTHING_EXPECTED
+    assert last.iteration == E["last_iteration"]
+    assert last.current_lambda == pytest.approx(E["lambda_approx"][0], rel=E["lambda_approx"][1])
+    assert last.new_error == pytest.approx(E["error_approx"][0], rel=E["error_approx"][1])
+    assert r["status"] == A.SFG_STATUS_SUCCESS
+
+
+def _linear_J():
+    # sym::Random<Eigen::Matrix<double, 9, 5>>(std::mt19937(12345)): column-major coefficient order
+    return O.mt19937_normal_vectors(12345, 1, 45)[0].reshape(5, 9).T
+
+
+def test_linear_problem_converges_in_one_iteration():
+    """test/symforce_levenberg_marquardt_test.cc:17-88: initial error > 1e4, after one undamped
+    Gauss-Newton iteration the error is below 1e-8 and |x| < 1e-4."""
+    p = R.linear_problem(_linear_J())
+    r = O.optimize(p, R.linear_problem_params(), epsilon=R.LINEAR_PROBLEM_EPSILON)
+    assert r["iterations"][0].new_error > 1e4
+    assert len(r["iterations"]) == 2
+    assert r["iterations"][-1].new_error < 1e-8
+    assert np.linalg.norm(r["values"]) < 1e-4
+
+
+def test_gnc_known_answers():
+    """test/symforce_gnc_test.cc:22-76: 9 records in all, |x| < 0.1, five times closer to zero than
+    the plain optimization at mu = 0, SUCCESS."""
+    y = R.gnc_samples(O.mt19937_normal_vectors(42, 20, 5))
+    p = R.gnc_problem(y)
+    params = A.default_optimizer_params()
+    r = O.gnc_optimize(p, params, R.gnc_params(), R.GNC_MU_SLOTS, epsilon=R.GNC_OPTIMIZER_EPSILON)
+    assert len(r["iterations"]) == R.GNC_EXPECTED["num_records"]
+    assert r["status"] == A.SFG_STATUS_SUCCESS
+    x = r["values"]
+    assert np.linalg.norm(x) < 0.1
+    plain = O.optimize(R.gnc_problem(y), params)
+    assert np.linalg.norm(x) * 5 < np.linalg.norm(plain["values"])
+
+
+@pytest.mark.parametrize("factor_order", ["dense_sparse", "sparse_dense"])
+def test_linearizer_consistency(factor_order):
+    """test/symforce_linearizer_test.cc:51-127: J^T J == H and J^T r == rhs exactly in either factor
+    order, and the key order permutes the Jacobian's columns."""
+    J = np.vstack([np.diag([1.0, 2.0]), np.diag([3.0, 4.0])])
+    if factor_order == "sparse_dense":
+        J = np.vstack([J[2:], J[:2]])
+    for key_order in ("xy", "yx"):
+        p = R.linearizer_problem(factor_order, key_order)
+        lin = O.linearize(p)
+        Jk = J if key_order == "xy" else J[:, ::-1]
+        H = np.zeros((2, 2))
+        for c in range(2):
+            for q in range(lin["colptr"][c], lin["colptr"][c + 1]):
+                H[lin["rowidx"][q], c] = lin["hvals"][q]
+        H = np.tril(H) + np.tril(H, -1).T
+        np.testing.assert_array_equal(H, Jk.T @ Jk)
+        np.testing.assert_array_equal(lin["rhs"], Jk.T @ lin["residual"])
+        np.testing.assert_array_equal(lin["residual"], Jk @ p.values)
