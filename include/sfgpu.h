@@ -269,6 +269,13 @@ int32_t sfg_get_values(sfg_handle* h, double* storage, int64_t n);
 int32_t sfg_linearize(sfg_handle* h, double* residual, double* rhs, double* error);
 int32_t sfg_hessian_lower(sfg_handle* h, int64_t* nnz, int32_t* col_ptr, int32_t* row_idx,
                           double* values);
+/* OptimizationStats::cholesky_factor_sparsity (symforce/opt/optimization_stats.h:53-58, filled at
+ * symforce/opt/levenberg_marquardt_solver.tcc:209-211): the unit lower factor of the handle's
+ * exact factorization (the full damped Hessian, or the reduced camera system of the Schur forms)
+ * as a compressed-column strict-lower matrix in the solver's ordering, with the values of the last
+ * factorization; query and capacity convention as sfg_ldlt_lower. */
+int32_t sfg_factor_lower(sfg_handle* h, int64_t* nnz, int32_t* col_ptr, int32_t* row_idx,
+                         double* values);
 /* The block ordering used by the linear solver, as new position of every state scalar. */
 int32_t sfg_permutation(sfg_handle* h, int32_t* perm, int64_t n);
 /* Time `reps` back-to-back launches of one stage of the iteration on the handle's stream with CUDA
@@ -404,6 +411,12 @@ int32_t sfg_ldlt_factorize(sfg_ldlt* s, const double* values);
 int32_t sfg_ldlt_solve(sfg_ldlt* s, const double* b, double* x, int32_t nrhs);
 int32_t sfg_ldlt_diagonal(sfg_ldlt* s, double* d);        /* D() in the solver's ordering */
 int32_t sfg_ldlt_permutation(sfg_ldlt* s, int32_t* perm);  /* Permutation(): new index of old i */
+/* L() (symforce/opt/sparse_cholesky/sparse_cholesky_solver.h:128-131; read by
+ * symforce/opt/levenberg_marquardt_solver.tcc:209-211): the unit lower factor as a compressed-column
+ * strict-lower n x n matrix in the solver's ordering, the supernodal pattern (explicit zeros
+ * included).  Call with col_ptr, row_idx and values all null to query *nnz; otherwise *nnz is the
+ * capacity on entry and the count on return; any of the three arrays may be null. */
+int32_t sfg_ldlt_lower(sfg_ldlt* s, int64_t* nnz, int32_t* col_ptr, int32_t* row_idx, double* values);
 int32_t sfg_ldlt_destroy(sfg_ldlt* s);
 
 /* -------------------------------- SparseSchurSolver ----------------------------------------

@@ -796,6 +796,32 @@ int32_t OptimizeImpl(sfg_handle* h, const sfg_optimizer_params_t* params, int32_
 }  // namespace
 }  // namespace sfg
 
+int32_t sfg_factor_lower(sfg_handle* h, int64_t* nnz, int32_t* col_ptr, int32_t* row_idx, double* values) {
+  return Guard([&] {
+    if (!h || !nnz) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (!h->fp.F) throw Error(SFG_ERR_STRUCTURE, "this form has no sparse factorization");
+    SFG_CUDA(cudaSetDevice(h->device));
+    SFG_CUDA(cudaStreamSynchronize(h->stream));
+    std::vector<unsigned char> F;
+    if (values) {
+      F.resize(size_t(h->fp.sym.front_pool) * h->fp.elem);
+      SFG_CUDA(cudaMemcpy(F.data(), h->fp.F, F.size(), cudaMemcpyDeviceToHost));
+    }
+    std::vector<int32_t> cp, ri;
+    std::vector<double> v;
+    sfg::FactorLowerCsc(h->fp, values ? F.data() : nullptr, cp, ri, values ? &v : nullptr);
+    if (!col_ptr && !row_idx && !values) {
+      *nnz = int64_t(ri.size());
+      return;
+    }
+    if (*nnz < int64_t(ri.size())) throw Error(SFG_ERR_CAPACITY, "nnz capacity too small");
+    *nnz = int64_t(ri.size());
+    if (col_ptr) std::copy(cp.begin(), cp.end(), col_ptr);
+    if (row_idx) std::copy(ri.begin(), ri.end(), row_idx);
+    if (values) std::copy(v.begin(), v.end(), values);
+  });
+}
+
 int32_t sfg_get_values(sfg_handle* h, double* storage, int64_t n) {
   return Guard([&] {
     if (!h || !storage) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");

@@ -194,6 +194,31 @@ int32_t sfg_ldlt_diagonal(sfg_ldlt* s, double* d) {
   });
 }
 
+int32_t sfg_ldlt_lower(sfg_ldlt* s, int64_t* nnz, int32_t* col_ptr, int32_t* row_idx, double* values) {
+  return Guard([&] {
+    if (!s || !nnz) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    if (!s->factored) throw Error(SFG_ERR_INVALID_ARGUMENT, "factorize first");
+    SFG_CUDA(cudaSetDevice(s->device));
+    std::vector<double> F;
+    if (values) {
+      F.resize(size_t(s->plan.sym.front_pool));
+      SFG_CUDA(cudaMemcpy(F.data(), s->plan.F, sizeof(double) * F.size(), cudaMemcpyDeviceToHost));
+    }
+    std::vector<int32_t> cp, ri;
+    std::vector<double> v;
+    sfg::FactorLowerCsc(s->plan, values ? F.data() : nullptr, cp, ri, values ? &v : nullptr);
+    if (!col_ptr && !row_idx && !values) {
+      *nnz = int64_t(ri.size());
+      return;
+    }
+    if (*nnz < int64_t(ri.size())) throw Error(SFG_ERR_CAPACITY, "nnz capacity too small");
+    *nnz = int64_t(ri.size());
+    if (col_ptr) std::copy(cp.begin(), cp.end(), col_ptr);
+    if (row_idx) std::copy(ri.begin(), ri.end(), row_idx);
+    if (values) std::copy(v.begin(), v.end(), values);
+  });
+}
+
 int32_t sfg_ldlt_permutation(sfg_ldlt* s, int32_t* perm) {
   return Guard([&] {
     if (!s || !perm) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");

@@ -91,6 +91,40 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   else ConfigureSolve<float>(maxm);
 }
 
+void FactorLowerCsc(const FactorPlan& fp, const void* front, std::vector<int32_t>& col_ptr,
+                    std::vector<int32_t>& row_idx, std::vector<double>* values) {
+  const Symbolic& S = fp.sym;
+  const int64_t n = S.n;
+  std::vector<std::vector<std::pair<int32_t, double>>> cols(static_cast<size_t>(n));
+  for (int s = 0; s < S.ns; ++s) {
+    const int w = S.sn_w[s], m = S.sn_m[s];
+    const int32_t* idx = S.idx.data() + S.idx_off[s];
+    for (int q = 0; q < w; ++q) {
+      auto& col = cols[size_t(idx[q])];
+      for (int r = q + 1; r < m; ++r) {
+        double v = 0.0;
+        if (front) {
+          const int64_t at = S.sn_foff[s] + r + int64_t(q) * m;
+          v = fp.elem == 8 ? static_cast<const double*>(front)[at] : double(static_cast<const float*>(front)[at]);
+        }
+        col.push_back({idx[r], v});
+      }
+    }
+  }
+  col_ptr.assign(size_t(n) + 1, 0);
+  row_idx.clear();
+  if (values) values->clear();
+  for (int64_t c = 0; c < n; ++c) {
+    auto& col = cols[size_t(c)];
+    std::sort(col.begin(), col.end());
+    for (const auto& e : col) {
+      row_idx.push_back(e.first);
+      if (values) values->push_back(e.second);
+    }
+    col_ptr[size_t(c) + 1] = int32_t(row_idx.size());
+  }
+}
+
 SpmvDev BuildSpmv(DeviceArena& A, const BlockPattern& pat, int64_t a_stride, int64_t b_stride) {
   const int64_t n = pat.off[pat.nb];
   std::vector<std::vector<std::array<int64_t, 4>>> rows(n);  // base, stride, len, x

@@ -58,6 +58,14 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
                      size_t elem, int* error_word, const LmState* st, int64_t a_stride,
                      int64_t b_stride, int num_sms, bool trace);
 
+// The unit lower factor of a factorization plan as a compressed-column strict-lower matrix in the
+// solver's ordering (the L() of SparseCholeskySolver, symforce/opt/sparse_cholesky/
+// sparse_cholesky_solver.h:128-131): the supernodal pattern (every entry below the diagonal of a
+// front's pivot columns, explicit zeros included).  With `front` (the front pool on the host, FP64
+// or FP32 per elem) the values are gathered too.
+void FactorLowerCsc(const FactorPlan& fp, const void* front, std::vector<int32_t>& col_ptr,
+                    std::vector<int32_t>& row_idx, std::vector<double>* values);
+
 // Per-row segments of the symmetric product with a block pattern (lower blocks stored row-major).
 SpmvDev BuildSpmv(DeviceArena& A, const BlockPattern& pat, int64_t a_stride, int64_t b_stride);
 

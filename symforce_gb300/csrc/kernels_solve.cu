@@ -407,6 +407,7 @@ struct alignas(16) TileSmem {
   T b[TILE * TILE];
   T c[TILE * TILE];
   T w[TILE * TILE];  // L D of the look-ahead's panel tile
+  T e[sizeof(T) == 8 ? TILE * TILE : 1];  // FP64 look-ahead: the diagonal tile
   T d[TILE];
 };
 
@@ -526,36 +527,135 @@ __device__ __forceinline__ void LdltStepsCta(D* a, int b) {
   }
 }
 
-// LDL^T of a 16 x 16 FP64 tile and the inverse of its unit lower factor, by one warp with the rows
-// in registers (Gauss-Jordan on [A | I]).  Lane r < 16 holds row r of the tile (v[c] = A(r, c); only
-// c <= r is read), lane 16 + r row r of the identity.  Pivot j applies one row operation to both
-// halves, row_r -= L(r, j) row_j for r > j: the tile's lanes update their columns c > j with the
-// pivot column A(c, j) (the trailing block stays symmetric), the identity's lanes their columns
-// c <= j with row j of their half, which ends as L^-1 (row operations give L^-1 A = D L^T on the
-// left and L^-1 on the right).  On return lane r < 16 holds L(r, c) for c < r and D(r) at c = r,
-// lane 16 + r row r of L^-1.  Rows at or beyond the tile's size must be identity rows.  One
-// shuffle per column and pivot serves both halves (the sender picks what its half is asked for),
-// and the pivot's reciprocal is formed once per pivot for the whole warp.
-__device__ __forceinline__ void WarpLdltInv16(double (&v)[16], int lane) {
-  constexpr unsigned kAll = 0xffffffffu;
-  const bool top = lane < 16;
-  const int r = lane & 15;
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const double dj = __shfl_sync(kAll, v[j], j);
-    const double inv = PivotReciprocal<double>(dj);
-    const double l = v[j] * inv;               // L(r, j) on the tile's lanes r > j
-    const double m = __shfl_sync(kAll, l, r);  // the identity's lanes take their row's multiplier
-#pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      if (c == j) continue;
-      const double send = top ? v[j] : v[c];
-      const double p = __shfl_sync(kAll, send, top ? c : 16 + j);
-      if (r > j && (top ? c > j : c < j)) v[c] = fma(-m, p, v[c]);
-    }
-    // column j: L(r, j) on the tile's lanes; the identity's row j has 1 there, so row r gets -m
-    if (r > j) v[j] = top ? l : -m;
+// ---- FP64 tiles (16 x 16).  On this GPU a warp issues an FP64 instruction about once per 64
+// cycles on its own SM sub-partition (a one-warp elimination of a tile measured 20 us against 12.6
+// us for the same work spread over four warps), so FP64 tile work is spread over all four warps of
+// the CTA (one per sub-partition) with as few FP64 instructions per warp and step as possible.
+
+// Lower entries of a 16 x 16 tile in column-major order: entry e -> (r, c), r >= c.
+__device__ __forceinline__ void LowerEntry16(int e, int* r, int* c) {
+  int cc = 0, start = 0;
+  while (cc < 15 && e >= start + (16 - cc)) {
+    start += 16 - cc;
+    ++cc;
   }
+  *c = cc;
+  *r = cc + (e - start);
+}
+
+// Right-looking LDL^T of the b x b leading part of a 16 x 16 FP64 tile held transposed in shared
+// memory (a[c * 16 + r] = A(r, c), lower part used): on return column j below the diagonal holds
+// L(:, j) and the diagonal D.  Warp 0 forms each pivot's reciprocal; warps 1-3 own the 136 lower
+// entries (at most two per thread) in registers, form the products A(r, j) A(c, j) while warp 0
+// works on the reciprocal, then apply one multiply-add per entry once it is published.  Two CTA
+// barriers per pivot.
+__device__ void DiagLdltF64(double* a, int b, double* s_inv) {
+  const int t = threadIdx.x;
+  int r0 = 0, c0 = 16, r1 = 0, c1 = 16;  // c = 16: no entry
+  double v0 = 0.0, v1 = 0.0;
+  if (t >= 32) {
+    const int e = t - 32;
+    LowerEntry16(e, &r0, &c0);
+    if (r0 >= b) c0 = 16;
+    if (e + 96 < 136) {
+      LowerEntry16(e + 96, &r1, &c1);
+      if (r1 >= b) c1 = 16;
+    }
+    if (c0 < 16) v0 = a[c0 * 16 + r0];
+    if (c1 < 16) v1 = a[c1 * 16 + r1];
+  }
+  for (int j = 0; j < b; ++j) {
+    double p0 = 0.0, p1 = 0.0;
+    if (t < 32) {
+      const double inv = PivotReciprocal<double>(a[j * 16 + j]);
+      if (t == 0) *s_inv = inv;
+    } else {
+      if (c0 < 16 && c0 > j) p0 = a[j * 16 + r0] * a[j * 16 + c0];
+      if (c1 < 16 && c1 > j) p1 = a[j * 16 + r1] * a[j * 16 + c1];
+    }
+    __syncthreads();
+    if (t >= 32) {
+      const double inv = *s_inv;
+      if (c0 < 16) {
+        if (c0 > j) {
+          v0 = fma(-p0, inv, v0);
+          a[c0 * 16 + r0] = v0;
+        } else if (c0 == j && r0 > j) {
+          v0 *= inv;  // L(r, j)
+          a[c0 * 16 + r0] = v0;
+        }
+      }
+      if (c1 < 16) {
+        if (c1 > j) {
+          v1 = fma(-p1, inv, v1);
+          a[c1 * 16 + r1] = v1;
+        } else if (c1 == j && r1 > j) {
+          v1 *= inv;
+          a[c1 * 16 + r1] = v1;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Inverse of the unit lower factor held in `a` (strict lower part of the b x b leading block, as
+// DiagLdltF64 leaves it) into li (transposed like the tiles; identity outside the block), by forward
+// substitution on all columns at once: one entry (r > c) per thread, one multiply-add per step.
+__device__ void UnitLowerInverseF64(const double* a, int b, double* li) {
+  const int t = threadIdx.x;
+  for (int e = t; e < 256; e += blockDim.x) li[e] = (e % 17 == 0) ? 1.0 : 0.0;
+  // strict lower entries (120): e -> (r, c) with r > c, column-major
+  int r = 0, c = 16;
+  if (t < 120) {
+    int cc = 0, start = 0;
+    while (cc < 14 && t >= start + (15 - cc)) {
+      start += 15 - cc;
+      ++cc;
+    }
+    c = cc;
+    r = cc + 1 + (t - start);
+    if (r >= b) c = 16;
+  }
+  __syncthreads();
+  double v = 0.0;
+  for (int q = 0; q + 1 < b; ++q) {
+    // Li(r, c) -= L(r, q) Li(q, c) for r > q >= c; row q of Li is final after step q - 1
+    if (c < 16 && r > q && c <= q) {
+      v = (c == q) ? -a[q * 16 + r] : fma(-a[q * 16 + r], li[c * 16 + q], v);
+      li[c * 16 + r] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// Panel solve X = F L^-T D^-1 of a 16 x 16 FP64 tile by forward substitution (no inverse on the
+// critical path): Y L^T = F row by row, then X = Y D^-1.  f: F transposed in shared memory, l: the
+// diagonal tile's unit lower factor (transposed, strict lower part), dinv: D^-1 (bk entries).
+// Thread t takes row r = t / 8 and columns g = t % 8 and g + 8 in registers; the eight threads of a
+// row are lanes of one warp, and step q takes y_q from its owner by a shuffle.  Writes X into x_out
+// and Y = X D into y_out (transposed, zero outside bi x bk).
+__device__ void PanelSolveSubstF64(const double* f, const double* l, const double* dinv, int bi, int bk,
+                                   double* x_out, double* y_out) {
+  constexpr unsigned kAll = 0xffffffffu;
+  const int t = threadIdx.x;
+  const int r = t >> 3, g = t & 7;
+  const int lane = t & 31, base = lane & ~7;
+  double y0 = (r < bi && g < bk) ? f[g * 16 + r] : 0.0;
+  double y1 = (r < bi && g + 8 < bk) ? f[(g + 8) * 16 + r] : 0.0;
+#pragma unroll
+  for (int q = 0; q < 15; ++q) {
+    const double yq = __shfl_sync(kAll, q < 8 ? y0 : y1, base + (q & 7));
+    if (q < bk) {
+      if (g > q && g < bk) y0 = fma(-yq, l[q * 16 + g], y0);
+      if (g + 8 > q && g + 8 < bk) y1 = fma(-yq, l[q * 16 + g + 8], y1);
+    }
+  }
+  const bool in0 = r < bi && g < bk, in1 = r < bi && g + 8 < bk;
+  y_out[g * 16 + r] = in0 ? y0 : 0.0;
+  y_out[(g + 8) * 16 + r] = in1 ? y1 : 0.0;
+  x_out[g * 16 + r] = in0 ? y0 * dinv[g] : 0.0;
+  x_out[(g + 8) * 16 + r] = in1 ? y1 * dinv[g + 8] : 0.0;
 }
 
 // A pivot of an FP32 diagonal tile that kept less than this fraction of its diagonal entry (more
@@ -578,33 +678,19 @@ __device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, 
   T* Fs = F + g.foff;
   T* li = sm.b;
   if constexpr (sizeof(T) == 8) {
-    static_assert(sizeof(T) != 8 || TILE == 16, "the FP64 warp elimination is written for 16 x 16 tiles");
-    // one warp: the tile and the identity eliminated together (L, D and L^-1), written straight
-    // from registers; the other warps go on to the signal
-    if (threadIdx.x < 32) {
-      const int lane = threadIdx.x, r = lane & 15;
-      const bool top = lane < 16;
-      double v[16];
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        double x = c == r ? 1.0 : 0.0;
-        if (top && r < b && c < b && c <= r) x = double(a[c * TILE + r]);
-        v[c] = x;
-      }
-      WarpLdltInv16(v, lane);
-      T* Lk = Linv + f.linv_base[s] + int64_t(k) * TILE * TILE;
-      if (top) {
-        if (r < b) {
-#pragma unroll
-          for (int c = 0; c < 16; ++c)
-            if (c <= r) St(Fs + (r0 + r) + int64_t(r0 + c) * g.m, T(v[c]));
-        }
-      } else {
-#pragma unroll
-        for (int c = 0; c < 16; ++c) St(Lk + c * TILE + r, T(c <= r ? v[c] : 0.0));
-      }
+    static_assert(sizeof(T) != 8 || TILE == 16, "the FP64 tile kernels are written for 16 x 16 tiles");
+    __shared__ double s_inv;
+    DiagLdltF64(a, b, &s_inv);
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+      const int r = e % TILE, c = e / TILE;
+      if (r < b && c < b && r >= c) St(Fs + (r0 + r) + int64_t(r0 + c) * g.m, a[c * TILE + r]);
     }
     Signal(f.tile_state + StateIdx(g, k, k), kFinal);
+    // the inverse of L is for the triangular solves only (the FP64 panel solves substitute), so
+    // it is formed after the tile is published, off the front's critical chain
+    UnitLowerInverseF64(a, b, li);
+    T* Lk = Linv + f.linv_base[s] + int64_t(k) * TILE * TILE;
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) St(Lk + e, li[e]);
     return;
   } else {
     // the tile's input, kept for an FP64 redo
@@ -724,6 +810,20 @@ __device__ void TaskTrsm(const FactorDev& f, int s, int i, int k, T* F, const T*
   const int bi = TileSize(g, i, TILE), ri = TileStart(g, i, TILE);
   T* Fs = F + g.foff;
   LoadTileT<T, TILE>(Fs, g.m, ri, ck, bi, bk, sm.a);  // F_ik
+  if constexpr (sizeof(T) == 8) {
+    LoadTileT<T, TILE>(Fs, g.m, ck, ck, bk, bk, sm.b);  // L_kk (strict lower) and D_k
+    __syncthreads();
+    for (int c = threadIdx.x; c < bk; c += blockDim.x) sm.d[c] = PivotReciprocal<T>(sm.b[c * TILE + c]);
+    __syncthreads();
+    PanelSolveSubstF64(sm.a, sm.b, sm.d, bi, bk, sm.c, sm.w);
+    __syncthreads();
+    for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+      const int r = e % TILE, c = e / TILE;
+      if (r < bi && c < bk) St(Fs + (ri + r) + int64_t(ck + c) * g.m, sm.c[c * TILE + r]);
+    }
+    Signal(f.tile_state + StateIdx(g, i, k), kFinal);
+    return;
+  }
   const T* Lk = Linv + f.linv_base[s] + int64_t(k) * TILE * TILE;
   for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) sm.b[e] = Ld(Lk + e);
   for (int c = threadIdx.x; c < bk; c += blockDim.x)
@@ -748,9 +848,53 @@ __device__ void TaskTrsm(const FactorDev& f, int s, int i, int k, T* F, const T*
 // shared memory), the update of diagonal tile (i, i) by it, F_ii -= L_ik D_k L_ik^T (after every
 // earlier panel's update of that tile), and the LDL^T of (i, i).  This saves two hand-offs between
 // CTAs (and two tile reloads) per panel on the longest dependency path of a front.
+// FP64 look-ahead: the three tiles it reads are waited for and loaded in one round (the diagonal
+// tile (i, i) is normally ready long before), the panel solve substitutes against L_kk, and the
+// diagonal tile is factored by the CTA-wide kernel.
+template <typename T, int TILE>
+__device__ void LookaheadF64(const FactorDev& f, int s, int i, int k, T* F, T* Linv, TileSmem<T, TILE>& sm,
+                             int* s_flag, unsigned long long* ready) {
+  const Geom g = FrontGeom(f, s);
+  bool ok = true;
+  if (threadIdx.x == 0) {
+    ok = WaitAtLeast(f.tile_state + StateIdx(g, k, k), kFinal, f.error) &&
+         WaitAtLeast(f.tile_state + StateIdx(g, i, k), 1 + k, f.error) &&
+         WaitAtLeast(f.tile_state + StateIdx(g, i, i), 1 + k, f.error);
+  }
+  if (!CtaWait(ok, s_flag, ready)) return;
+  const int bk = TileSize(g, k, TILE), ck = TileStart(g, k, TILE);
+  const int bi = TileSize(g, i, TILE), ri = TileStart(g, i, TILE);
+  T* Fs = F + g.foff;
+  LoadTileT<T, TILE>(Fs, g.m, ri, ck, bi, bk, sm.a);  // F_ik
+  LoadTileT<T, TILE>(Fs, g.m, ck, ck, bk, bk, sm.b);  // L_kk and D_k
+  LoadTileT<T, TILE>(Fs, g.m, ri, ri, bi, bi, sm.e);  // F_ii
+  __syncthreads();
+  for (int c = threadIdx.x; c < bk; c += blockDim.x) sm.d[c] = PivotReciprocal<T>(sm.b[c * TILE + c]);
+  __syncthreads();
+  PanelSolveSubstF64(sm.a, sm.b, sm.d, bi, bk, sm.c, sm.w);
+  __syncthreads();
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+    const int r = e % TILE, c = e / TILE;
+    if (r < bi && c < bk) St(Fs + (ri + r) + int64_t(ck + c) * g.m, sm.c[c * TILE + r]);
+  }
+  Signal(f.tile_state + StateIdx(g, i, k), kFinal);
+  // F_ii -= Y X^T (Y = X D), lower part
+  for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
+    const int r = e % TILE, c = e / TILE;
+    if (r >= bi || c > r) continue;
+    sm.e[c * TILE + r] -= PanelDot<T, TILE>(sm.w, sm.c, r, c, bk);
+  }
+  __syncthreads();
+  DiagCore<T, TILE>(f, g, s, i, F, Linv, sm.e, sm);
+}
+
 template <typename T, int TILE>
 __device__ void TaskLookahead(const FactorDev& f, int s, int i, int k, T* F, T* Linv,
                               TileSmem<T, TILE>& sm, int* s_flag, unsigned long long* ready) {
+  if constexpr (sizeof(T) == 8) {
+    LookaheadF64<T, TILE>(f, s, i, k, F, Linv, sm, s_flag, ready);
+    return;
+  }
   const Geom g = FrontGeom(f, s);
   bool ok = true;
   if (threadIdx.x == 0) {

@@ -61,6 +61,10 @@ def lib() -> C.CDLL:
         L.sfg_ldlt_diagonal.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.sfg_ldlt_permutation.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.sfg_ldlt_destroy.argtypes = [C.c_void_p]
+        L.sfg_ldlt_lower.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        L.sfg_factor_lower.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_int32), C.POINTER(C.c_double)]
         L.sfg_schur_create.argtypes = [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int32,
                                        C.c_int32, C.POINTER(C.c_void_p)]
         L.sfg_schur_factorize.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
@@ -98,10 +102,28 @@ class OptimizationStats:
     failure_reason: int = 0
     kernel_launches: int = 0
     device_ms: float = 0.0
+    best_linearization: dict | None = None       # populate_best_linearization
+    linear_solver_ordering: np.ndarray | None = None  # debug_stats
+    cholesky_factor_sparsity: dict | None = None  # debug_stats
 
     @property
     def best_error(self) -> float:
         return self.iterations[self.best_index].new_error
+
+
+def _lower_csc(fn, handle, n: int, with_values: bool = True) -> dict:
+    """Two-phase query of a compressed-column strict-lower factor (sfg_ldlt_lower /
+    sfg_factor_lower)."""
+    nnz = C.c_int64()
+    _check(fn(handle, C.byref(nnz), None, None, None))
+    colptr = np.zeros(n + 1, dtype=np.int32)
+    rowidx = np.zeros(nnz.value, dtype=np.int32)
+    vals = np.zeros(nnz.value) if with_values else None
+    _check(fn(handle, C.byref(nnz), A.iptr(colptr), A.iptr(rowidx), A.dptr(vals) if with_values else None))
+    out = dict(colptr=colptr, rowidx=rowidx, shape=(n, n))
+    if with_values:
+        out["values"] = vals
+    return out
 
 
 def csc_lower_to_dense(colptr: np.ndarray, rowidx: np.ndarray, vals: np.ndarray, n: int) -> np.ndarray:
@@ -190,9 +212,14 @@ class Optimizer:
 
     def optimize(self, values: np.ndarray | None = None, num_iterations: int = -1,
                  params: A.OptimizerParams | None = None,
-                 out: np.ndarray | None = None) -> tuple[np.ndarray, OptimizationStats]:
-        """Optimizer::Optimize: returns (best values, stats).  `out` (float64, storage size), if
-        given, receives the best values (e.g. a pinned buffer)."""
+                 out: np.ndarray | None = None,
+                 populate_best_linearization: bool = False) -> tuple[np.ndarray, OptimizationStats]:
+        """Optimizer::Optimize(values, num_iterations, populate_best_linearization, stats): returns
+        (best values, stats).  `out` (float64, storage size), if given, receives the best values
+        (e.g. a pinned buffer).  With populate_best_linearization the stats carry the linearization
+        at the best values (symforce/opt/internal/optimizer_utils.h:69-75); with params.debug_stats
+        the linear solver's ordering and the sparsity of its factor L
+        (symforce/opt/levenberg_marquardt_solver.tcc:209-211)."""
         if values is not None:
             self.set_values(values)
         p = params or self.params
@@ -205,7 +232,22 @@ class Optimizer:
         if out is None:
             out = np.zeros(self.storage_dim)
         _check(lib().sfg_get_values(self._h, A.dptr(out), out.size))
+        if populate_best_linearization:
+            lin = self.linearize(out)
+            stats.best_linearization = dict(residual=lin["residual"], rhs=lin["rhs"], error=lin["error"],
+                                            hessian_lower=dict(colptr=lin["colptr"], rowidx=lin["rowidx"],
+                                                               values=lin["hvals"]))
+        if p.debug_stats and self.form.linear_solver in (A.SFG_LINEAR_SOLVER_SPARSE_LDLT,
+                                                          A.SFG_LINEAR_SOLVER_SCHUR):
+            stats.linear_solver_ordering = self.permutation()
+            stats.cholesky_factor_sparsity = self.factor_lower(with_values=False)
         return out, stats
+
+    def factor_lower(self, with_values: bool = True) -> dict:
+        """The unit lower factor L of the last exact factorization (strict lower CSC, solver order)."""
+        n = self.tangent_dim - (3 * self.problem.num_schur_keys
+                                if self.form.linear_solver in A.SCHUR_SOLVERS else 0)
+        return _lower_csc(lib().sfg_factor_lower, self._h, n, with_values)
 
     def optimize_continue(self, num_iterations: int, params: A.OptimizerParams | None = None,
                           relax_damping: bool = True) -> OptimizationStats:
@@ -369,6 +411,10 @@ class SparseLdlt:
         p = np.zeros(self.n, dtype=np.int32)
         _check(lib().sfg_ldlt_permutation(self._h, A.iptr(p)))
         return p
+
+    def lower(self) -> dict:
+        """L(): the unit lower factor (strict lower CSC in the solver's ordering) with its values."""
+        return _lower_csc(lib().sfg_ldlt_lower, self._h, self.n)
 
     def __del__(self) -> None:
         try:

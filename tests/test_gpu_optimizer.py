@@ -83,6 +83,29 @@ def test_pose_smoothing_dynamic_lambda_known_answers():
     np.testing.assert_allclose(lin["hvals"], o["hvals"], rtol=1e-9, atol=1e-12 * np.abs(o["hvals"]).max())
 
 
+def test_debug_stats_and_best_linearization():
+    """populate_best_linearization and debug_stats (symforce/opt/optimization_stats.h:34-58): the
+    best linearization equals the oracle's at the best values; the ordering is a permutation and
+    the factor's sparsity is a strict-lower CSC of the right size."""
+    p = synth.bundle_adjustment(num_cameras=6, num_points=80, num_observations=320, seed=4)
+    params = A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC, iterations=10,
+                                        debug_stats=1)
+    opt = Optimizer(p, params, A.default_form_params(linear_solver=A.SFG_LINEAR_SOLVER_SCHUR))
+    values, stats = opt.optimize(p.values, populate_best_linearization=True)
+    bl = stats.best_linearization
+    o = O.linearize(p, values)
+    np.testing.assert_allclose(bl["residual"], o["residual"], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(bl["hessian_lower"]["values"], o["hvals"], rtol=1e-9,
+                               atol=1e-12 * np.abs(o["hvals"]).max())
+    assert bl["error"] == pytest.approx(stats.best_error, rel=1e-12)
+    n = 6 * 9
+    assert sorted(stats.linear_solver_ordering.tolist()) == list(range(n))
+    sp = stats.cholesky_factor_sparsity
+    assert sp["shape"] == (n, n) and sp["colptr"].size == n + 1
+    for c in range(n):
+        assert (sp["rowidx"][sp["colptr"][c]:sp["colptr"][c + 1]] > c).all()
+
+
 def test_linearization_matches_oracle_ba_small():
     p = synth.bundle_adjustment(num_cameras=8, num_points=120, num_observations=500, seed=3)
     opt = Optimizer(p, form=A.default_form_params(linear_solver=A.SFG_LINEAR_SOLVER_SCHUR))

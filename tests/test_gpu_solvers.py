@@ -158,3 +158,30 @@ def test_schur_against_dense():
     s.factorize(v2)
     x2 = s.solve(b)
     np.testing.assert_allclose(x2, np.linalg.solve(H2, b), rtol=1e-10, atol=1e-12 * np.abs(x2).max())
+
+
+@pytest.mark.parametrize("ordering", ORDERINGS)
+def test_ldlt_lower_reconstructs_permuted_matrix(ordering):
+    """L() with D() and Permutation(): P A P^T == (I + L) D (I + L)^T, the contract the reference's
+    debug stats read (symforce/opt/levenberg_marquardt_solver.tcc:209-211)."""
+    n = 120
+    rng = np.random.default_rng(11 + ordering)
+    Ad = _random_symmetric(n, rng)
+    Ad = Ad @ Ad.T / n + np.eye(n)
+    Ad[np.abs(Ad) < 0.3] = 0.0
+    Ad = 0.5 * (Ad + Ad.T) + 2.0 * np.eye(n)
+    cp, ri, v = _csc_lower(Ad)
+    s = SparseLdlt(n, cp, ri, ordering=ordering)
+    s.factorize(v)
+    low = s.lower()
+    assert low["colptr"][0] == 0 and low["colptr"][-1] == low["rowidx"].size
+    Ld = np.eye(n)
+    for c in range(n):
+        rows = low["rowidx"][low["colptr"][c]:low["colptr"][c + 1]]
+        assert (rows > c).all() and (np.diff(rows) > 0).all()
+        Ld[rows, c] = low["values"][low["colptr"][c]:low["colptr"][c + 1]]
+    perm = s.permutation()
+    P = np.zeros((n, n))
+    P[perm, np.arange(n)] = 1.0
+    np.testing.assert_allclose(Ld @ np.diag(s.diagonal()) @ Ld.T, P @ Ad @ P.T, rtol=1e-10,
+                               atol=1e-11 * np.abs(Ad).max())

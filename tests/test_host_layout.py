@@ -291,6 +291,8 @@ def _replay_tasks(tasks, npiv, ntiles, parent, w, m, cptr, clist, tile):
             need(s, i, k, 1 + k, "panel")
             st[i, k] = FINAL
             if ty == LOOKAHEAD:
+                # the FP64 look-ahead waits for this one at its start, the FP32 one after its panel
+                # solve; (i, i) does not depend on (i, k), so the replay is the same for both
                 assert i == k + 1
                 need(s, i, i, 1 + k, "lookahead diag")
                 st[i, i] = FINAL
