@@ -50,6 +50,7 @@ def _stale() -> bool:
 
 def build(force: bool = False, verbose: bool = False) -> Path:
     if not force and not _stale():
+        build_python_binding(verbose)
         return LIB
     nvcc = _nvcc()
     BUILD_DIR.mkdir(exist_ok=True)
@@ -78,7 +79,35 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_python_binding(verbose)
     return LIB
+
+
+def python_binding_path() -> Path:
+    import sysconfig
+    return PKG / ("_cc_sym_gpu" + (sysconfig.get_config_var("EXT_SUFFIX") or ".so"))
+
+
+def build_python_binding(verbose: bool = False) -> Path:
+    """The compiled cc_sym-shaped binding (csrc/py_cc_sym.cpp, CPython C API) next to the package,
+    linked against lib/libsfgpu.so."""
+    import sysconfig
+    out = python_binding_path()
+    src = CSRC / "py_cc_sym.cpp"
+    if out.exists() and out.stat().st_mtime > max(src.stat().st_mtime, LIB.stat().st_mtime):
+        return out
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("no C++ compiler for the Python binding")
+    cmd = [cxx, "-O2", "-std=c++17", "-shared", "-fPIC", f"-I{sysconfig.get_paths()['include']}", f"-I{INCLUDE}",
+           str(src), f"-L{OUT_DIR}", "-lsfgpu", "-Wl,-rpath,$ORIGIN/lib", "-o", str(out) + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"binding build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if verbose and r.stderr:
+        print(r.stderr)
+    os.replace(str(out) + ".tmp", out)
+    return out
 
 
 if __name__ == "__main__":

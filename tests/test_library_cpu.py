@@ -125,3 +125,19 @@ def test_cpp_adapters_compile_and_link(tmp_path):
     r = subprocess.run([str(exe)], capture_output=True, text=True, env={"CUDA_VISIBLE_DEVICES": ""})
     assert r.returncode != 0
     assert "no CUDA device" in r.stderr + r.stdout
+
+
+def test_cc_sym_binding_builds_and_fails_loudly_without_device():
+    """The compiled cc_sym-shaped binding (symforce/pybind/cc_optimizer.cc:29-170) imports, reports
+    DefaultOptimizerParams, and refuses to construct an Optimizer without a GPU."""
+    from symforce_gb300 import cc_sym
+    d = cc_sym.default_optimizer_params()
+    p = A.default_optimizer_params()
+    for k, v in d.items():
+        assert getattr(p, k) == pytest.approx(v), k
+    prob = synth.robot_2d(num_poses=20, num_landmarks=5, seed=1)
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    with pytest.raises(RuntimeError, match="sfgpu error 3"):
+        cc_sym.Optimizer(d, prob)
