@@ -50,6 +50,7 @@ from symforce_gb300 import workloads  # noqa: E402
 
 METRIC = "BA time to FP64-oracle cost (rel 1e-6): plain vs mixed/learned; linearize GB/s"
 WORKLOAD = "ba_50_7800"
+FP64_PEAK_GFLOPS = 1208.0  # FP64 FMA throughput measured on GB300 (profiles/gb300_fp64_latency.md)
 TOL = 1e-6
 
 
@@ -144,10 +145,13 @@ def _barrier(world: int) -> None:
         dist.barrier()
 
 
-def _cpu_solve(problem, params, max_iterations: int) -> dict:
-    """The oracle port (CPU restatement of the reference optimizer), single-threaded."""
+def _cpu_solve(problem, params, max_iterations: int, variant: str = "o3") -> dict:
+    """The oracle port (CPU restatement of the reference optimizer), single-threaded; `variant`
+    picks its build: "o3" (the timed baseline), "o3_fast" (-O3 -ffast-math), "o2" (the parity
+    build the tests use)."""
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_lib as O
+    O.use_variant(variant)
     p = A.default_optimizer_params()
     for f, _ in A.OptimizerParams._fields_:
         setattr(p, f, getattr(params, f))
@@ -195,7 +199,8 @@ def run_reference(args) -> None:
         "ms_per_step": round(ms_step, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
         "config": {"workload": WORKLOAD, "form": "plain FP64, CPU restatement of sym::Optimizer "
-                   "(up-looking sparse LDL^T on the full Hessian, block minimum-degree ordering)",
+                   "(up-looking sparse LDL^T on the full Hessian, block minimum-degree ordering), "
+                   "built g++ -O3",
                    "cores": 1},
         "cpu_baseline": {"value": round(value, 3), "unit": "ms", "cores": 1, "kind": "port",
                          "sample": sample},
@@ -491,6 +496,7 @@ def run_gb300(args) -> None:
     opt = opts["plain"]
     lin = opt.time_stage(A.SFG_STAGE_LINEARIZE, reps=50)
     stages = {}
+    factor_fmas = {}
     for fname in ["plain", "mixed"]:
         stages[fname] = {}
         for name, sid in [("linearize", A.SFG_STAGE_LINEARIZE), ("schur", A.SFG_STAGE_SCHUR),
@@ -498,6 +504,8 @@ def run_gb300(args) -> None:
             t = opts[fname].time_stage(sid, reps=20)
             stages[fname][name] = {"ms": round(t["ms"], 5),
                                    "gfma_s": round(t["fmas"] / t["ms"] / 1e6, 2)}
+            if name == "factor":
+                factor_fmas[fname] = t
     for o in opts.values():
         o.close()
     peaks, peak_kind = _measured_peaks()
@@ -526,12 +534,16 @@ def run_gb300(args) -> None:
         return
     cpu = None
     if not args.no_cpu_baseline:
-        t0 = time.perf_counter()
-        r = _cpu_solve(problem, params, params.iterations)
-        cpu_s = time.perf_counter() - t0
-        frac = next((i for i, e in enumerate(r["iterations"]) if e.best_error <= target),
-                    len(r["iterations"]) - 1) / max(len(r["iterations"]) - 1, 1)
-        cpu = {"value": round(cpu_s * 1e3 * frac, 3), "unit": "ms", "cores": 1, "kind": "port",
+        timed = {}
+        for variant in ("o3", "o3_fast", "o2"):
+            t0 = time.perf_counter()
+            r = _cpu_solve(problem, params, params.iterations, variant)
+            cpu_s = time.perf_counter() - t0
+            frac = next((i for i, e in enumerate(r["iterations"]) if e.best_error <= target),
+                        len(r["iterations"]) - 1) / max(len(r["iterations"]) - 1, 1)
+            timed[variant] = round(cpu_s * 1e3 * frac, 3)
+        cpu = {"value": timed["o3"], "unit": "ms", "cores": 1, "kind": "port", "build": "g++ -O3",
+               "variants_ms": {"-O3 -ffast-math": timed["o3_fast"], "-O2 (the parity build)": timed["o2"]},
                "sample": "one full solve (to convergence) of the same workload on one host core "
                          "(CPU restatement of sym::Optimizer, full-Hessian sparse LDL^T)"}
     line = {
@@ -554,6 +566,16 @@ def run_gb300(args) -> None:
                      "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes": lin["bytes"], "ms_per_launch": round(lin["ms"], 5)},
         "stages_ms_per_launch": stages,
+        # the kernel that sets the plain form's time: the FP64 multifrontal LDL^T of the reduced
+        # camera system, flops from the symbolic factor (2 per multiply-add) against the FP64 rate
+        # measured on this GPU (profiles/gb300_fp64_latency.md; MEASURED_PEAKS.json has no FP64 entry)
+        "roofline_factor": {
+            "kernel": "FactorKernel<double, 16> (persistent tile-task LDL^T)", "bound": "fp64",
+            "achieved": round(2 * factor_fmas["plain"]["fmas"] / (factor_fmas["plain"]["ms"] * 1e-3) / 1e9, 2),
+            "peak": FP64_PEAK_GFLOPS, "unit": "GFLOP/s", "peak_kind": "measured (FP64 FMA loop, all SMs)",
+            "frac": round(2 * factor_fmas["plain"]["fmas"] / (factor_fmas["plain"]["ms"] * 1e-3) / 1e9
+                          / FP64_PEAK_GFLOPS, 5),
+            "multiply_adds": factor_fmas["plain"]["fmas"], "ms_per_launch": round(factor_fmas["plain"]["ms"], 5)},
         "scale": scale,
         "batched": batched,
         "cpu_baseline": cpu,

@@ -17,21 +17,37 @@ from symforce_gb300 import _cabi as A
 ROOT = Path(__file__).resolve().parents[1]
 ORACLE_DIR = ROOT / "oracle"
 LIB_PATH = ORACLE_DIR / "_build" / "liboracle.so"
+# timed CPU baselines (bench.py): the same source at -O3, and at -O3 -ffast-math
+VARIANTS = {"o2": "liboracle.so", "o3": "liboracle_o3.so", "o3_fast": "liboracle_o3_fast.so"}
 
 _lib = None
 
 
+def use_variant(name: str) -> None:
+    """Load another build of the oracle (VARIANTS) for the calls that follow (bench timing only)."""
+    global _lib
+    path = ORACLE_DIR / "_build" / VARIANTS[name]
+    if not path.exists():
+        build()
+    L = C.CDLL(str(path))
+    L.orc_last_error.restype = C.c_char_p
+    _lib = L
+
+
 def build() -> Path:
-    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], check=True)
+    subprocess.run(["make", "-s", "-j3", "-C", str(ORACLE_DIR)], check=True)
     return LIB_PATH
 
 
 def lib() -> C.CDLL:
+    """The oracle library; SFG_ORACLE_VARIANT (o2 | o3 | o3_fast) picks the build (default o2, the
+    parity reference)."""
     global _lib
     if _lib is None:
-        if not LIB_PATH.exists() or os.environ.get("SFG_REBUILD_ORACLE"):
+        path = ORACLE_DIR / "_build" / VARIANTS[os.environ.get("SFG_ORACLE_VARIANT", "o2")]
+        if not path.exists() or os.environ.get("SFG_REBUILD_ORACLE"):
             build()
-        L = C.CDLL(str(LIB_PATH))
+        L = C.CDLL(str(path))
         L.orc_last_error.restype = C.c_char_p
         _lib = L
     return _lib
