@@ -696,29 +696,29 @@ __device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, 
     if (threadIdx.x == 0) s_redo = 0;
     __syncthreads();
     constexpr unsigned kAll = 0xffffffffu;
-    // one warp, lane r holds row r in registers shifted one column left per pivot (row[c] =
-    // a(r, j + c)), the multipliers reach the other rows by shuffles; a rolled pivot loop keeps the
-    // code small
+    // one warp, lane r holds row r in registers; the pivot loop is unrolled so that every register
+    // index is static (FP32 issues at full rate from one warp, unlike FP64), and the multipliers
+    // reach the other rows by shuffles
     if (threadIdx.x < 32) {
       const int r = threadIdx.x;
       T row[TILE];
 #pragma unroll
       for (int c = 0; c < TILE; ++c) row[c] = (r < b && c <= r) ? a[c * TILE + (r < TILE ? r : 0)] : T(0);
       bool redo = false;
-      for (int j = 0; j < b; ++j) {
-        const T dj = __shfl_sync(kAll, row[0], j);
-        redo = redo || !(dj > kNearSingularPivot * fabsf(float(orig[j * TILE + j])));
-        const T inv = PivotReciprocal<T>(dj);
-        const T lrj = row[0] * inv;
 #pragma unroll
-        for (int c = 1; c < TILE; ++c) {
-          const T lcj = __shfl_sync(kAll, lrj, (j + c) & 31);
-          if (r >= j + c) row[c] -= row[0] * lcj;
+      for (int j = 0; j < TILE; ++j) {
+        if (j < b) {
+          const T dj = __shfl_sync(kAll, row[j], j);
+          redo = redo || !(dj > kNearSingularPivot * fabsf(float(orig[j * TILE + j])));
+          const T inv = PivotReciprocal<T>(dj);
+          const T lrj = row[j] * inv;
+#pragma unroll
+          for (int c = j + 1; c < TILE; ++c) {
+            const T lcj = __shfl_sync(kAll, lrj, c);
+            if (r >= c) row[c] -= row[j] * lcj;
+          }
+          if (r < b && r >= j) a[j * TILE + r] = r > j ? lrj : row[j];  // L(r, j), or d_j on the diagonal
         }
-        if (r < b && r >= j) a[j * TILE + r] = r > j ? lrj : row[0];  // L(r, j), or d_j on the diagonal
-#pragma unroll
-        for (int c = 0; c + 1 < TILE; ++c) row[c] = row[c + 1];
-        row[TILE - 1] = T(0);
       }
       if (r == 0 && redo) s_redo = 1;
     }
