@@ -545,54 +545,58 @@ __device__ __forceinline__ void LowerEntry16(int e, int* r, int* c) {
 
 // Right-looking LDL^T of the b x b leading part of a 16 x 16 FP64 tile held transposed in shared
 // memory (a[c * 16 + r] = A(r, c), lower part used): on return column j below the diagonal holds
-// L(:, j) and the diagonal D; dinv (16 entries, shared) receives D^-1.  The 136 lower entries are
-// spread over the four warps (at most two per thread, in registers).  Every warp forms the pivot's
-// reciprocal itself (each on its own sub-partition, in parallel) while its threads form the
-// products A(r, j) A(c, j), then applies one multiply-add per entry: one CTA barrier per pivot.
-// Column j is scaled to L(:, j) during pivot j + 1, when nothing reads it any more.
-__device__ void DiagLdltF64(double* a, int b, double* dinv) {
+// L(:, j) and the diagonal D.  Warp 0 forms each pivot's reciprocal; warps 1-3 own the 136 lower
+// entries (at most two per thread) in registers, form the products A(r, j) A(c, j) while warp 0
+// works on the reciprocal, then apply one multiply-add per entry once it is published.  Two CTA
+// barriers per pivot.
+__device__ void DiagLdltF64(double* a, int b, double* s_inv) {
   const int t = threadIdx.x;
   int r0 = 0, c0 = 16, r1 = 0, c1 = 16;  // c = 16: no entry
   double v0 = 0.0, v1 = 0.0;
-  LowerEntry16(t, &r0, &c0);
-  if (r0 >= b) c0 = 16;
-  if (t + 128 < 136) {
-    LowerEntry16(t + 128, &r1, &c1);
-    if (r1 >= b) c1 = 16;
+  if (t >= 32) {
+    const int e = t - 32;
+    LowerEntry16(e, &r0, &c0);
+    if (r0 >= b) c0 = 16;
+    if (e + 96 < 136) {
+      LowerEntry16(e + 96, &r1, &c1);
+      if (r1 >= b) c1 = 16;
+    }
+    if (c0 < 16) v0 = a[c0 * 16 + r0];
+    if (c1 < 16) v1 = a[c1 * 16 + r1];
   }
-  if (c0 < 16) v0 = a[c0 * 16 + r0];
-  if (c1 < 16) v1 = a[c1 * 16 + r1];
-  double inv_prev = 0.0;
-  for (int j = 0; j <= b; ++j) {
-    // column j - 1 becomes L(:, j - 1)
-    if (j > 0) {
-      if (c0 == j - 1 && r0 > c0) {
-        v0 *= inv_prev;
-        a[c0 * 16 + r0] = v0;
+  for (int j = 0; j < b; ++j) {
+    double p0 = 0.0, p1 = 0.0;
+    if (t < 32) {
+      const double inv = PivotReciprocal<double>(a[j * 16 + j]);
+      if (t == 0) *s_inv = inv;
+    } else {
+      if (c0 < 16 && c0 > j) p0 = a[j * 16 + r0] * a[j * 16 + c0];
+      if (c1 < 16 && c1 > j) p1 = a[j * 16 + r1] * a[j * 16 + c1];
+    }
+    __syncthreads();
+    if (t >= 32) {
+      const double inv = *s_inv;
+      if (c0 < 16) {
+        if (c0 > j) {
+          v0 = fma(-p0, inv, v0);
+          a[c0 * 16 + r0] = v0;
+        } else if (c0 == j && r0 > j) {
+          v0 *= inv;  // L(r, j)
+          a[c0 * 16 + r0] = v0;
+        }
       }
-      if (c1 == j - 1 && r1 > c1) {
-        v1 *= inv_prev;
-        a[c1 * 16 + r1] = v1;
+      if (c1 < 16) {
+        if (c1 > j) {
+          v1 = fma(-p1, inv, v1);
+          a[c1 * 16 + r1] = v1;
+        } else if (c1 == j && r1 > j) {
+          v1 *= inv;
+          a[c1 * 16 + r1] = v1;
+        }
       }
     }
-    if (j == b) break;
-    const bool act0 = c0 < 16 && c0 > j, act1 = c1 < 16 && c1 > j;
-    const double p0 = act0 ? a[j * 16 + r0] * a[j * 16 + c0] : 0.0;
-    const double p1 = act1 ? a[j * 16 + r1] * a[j * 16 + c1] : 0.0;
-    const double inv = PivotReciprocal<double>(a[j * 16 + j]);
-    if (t == j) dinv[j] = inv;
-    if (act0) {
-      v0 = fma(-p0, inv, v0);
-      a[c0 * 16 + r0] = v0;
-    }
-    if (act1) {
-      v1 = fma(-p1, inv, v1);
-      a[c1 * 16 + r1] = v1;
-    }
-    inv_prev = inv;
     __syncthreads();
   }
-  __syncthreads();
 }
 
 // Inverse of the unit lower factor held in `a` (strict lower part of the b x b leading block, as
@@ -675,8 +679,8 @@ __device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, 
   T* li = sm.b;
   if constexpr (sizeof(T) == 8) {
     static_assert(sizeof(T) != 8 || TILE == 16, "the FP64 tile kernels are written for 16 x 16 tiles");
-    __shared__ double s_dinv[16];
-    DiagLdltF64(a, b, s_dinv);
+    __shared__ double s_inv;
+    DiagLdltF64(a, b, &s_inv);
     for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
       const int r = e % TILE, c = e / TILE;
       if (r < b && c < b && r >= c) St(Fs + (r0 + r) + int64_t(r0 + c) * g.m, a[c * TILE + r]);
