@@ -1018,7 +1018,7 @@ int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_pe
     if (stage == SFG_STAGE_FACTOR && h->fp.f.trace) {
       if (const char* path = std::getenv("SFG_TRACE_FACTOR_FILE")) {
         const auto& tasks = h->fp.plan.tasks;
-        std::vector<unsigned long long> tr(4 * tasks.size());
+        std::vector<unsigned long long> tr(8 * tasks.size());
         SFG_CUDA(cudaMemcpy(tr.data(), h->fp.f.trace, tr.size() * 8, cudaMemcpyDeviceToHost));
         if (FILE* fo = std::fopen(path, "wb")) {
           const int64_t n = int64_t(tasks.size());

@@ -53,7 +53,7 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   f.e_src = A.Upload(M.e_src);
   f.e_dst = A.Upload(M.e_dst);
   f.linv_base = A.Upload(linv_base);
-  f.trace = trace ? A.Zeros<unsigned long long>(4 * T.tasks.size()) : nullptr;
+  f.trace = trace ? A.Zeros<unsigned long long>(8 * T.tasks.size()) : nullptr;  // start, ready, end, SM, 4 phase stamps
   f.rel_off = A.Upload(S.rel_off);
   f.rel = A.Upload(S.rel);
   f.child_ptr = A.Upload(M.child_ptr);

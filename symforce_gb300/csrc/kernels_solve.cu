@@ -412,20 +412,28 @@ struct alignas(16) TileSmem {
 };
 
 // Reciprocal for the pivot chain.  FP64 division is a long dependent instruction sequence on this
-// GPU (FP64 issues at a small fraction of the FP32 rate), so doubles use the Newton-Raphson
-// iteration y <- y + y (1 - x y) from an FP32 seed: two steps take the seed's ~24 correct bits to
-// full double precision (the error squares at each step).
+// GPU (~560 cycles measured; every dependent FP64 operation costs ~64), so doubles take the
+// hardware's approximate FP64 reciprocal (rcp.approx.ftz.f64, ~18 cycles) and two Newton-Raphson
+// steps y <- y + y (1 - x y), whose error squares at each step.  Inputs whose reciprocal leaves the
+// normal range (the approximation flushes subnormals) take the IEEE division.
 template <typename T>
 __device__ __forceinline__ T PivotReciprocal(T x) { return T(1) / x; }
 template <>
 __device__ __forceinline__ double PivotReciprocal<double>(double x) {
-  const float xf = float(x);
-  if (!(fabsf(xf) > 1e-30f && fabsf(xf) < 1e30f)) return 1.0 / x;  // seed out of FP32 range
-  double y = double(1.0f / xf);
+  const int ex = __double2hiint(x) & 0x7FF00000;  // biased exponent field
+  if (ex < 0x00200000 || ex >= 0x7FD00000) return 1.0 / x;
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
   double e = fma(-x, y, 1.0);
   y = fma(y, e, y);
   e = fma(-x, y, 1.0);
   return fma(y, e, y);
+}
+
+// Per-phase clock stamps of a traced task (SFG_TRACE_FACTOR): `ready` is the task's trace record
+// + 1; phase i goes to record slot 4 + i.
+__device__ __forceinline__ void Stamp(unsigned long long* ready, int i) {
+  if (ready && threadIdx.x == 0) ready[3 + i] = Clock64Global();
 }
 
 // Broadcast of thread 0's wait result.
@@ -672,7 +680,7 @@ constexpr float kNearSingularPivot = 1.0f / 4096.0f;
 // f.fp64_tiles).
 template <typename T, int TILE>
 __device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, T* Linv, T* a,
-                         TileSmem<T, TILE>& sm) {
+                         TileSmem<T, TILE>& sm, unsigned long long* tr = nullptr) {
   static_assert(TILE <= 32, "one lane per tile row");
   const int b = TileSize(g, k, TILE), r0 = TileStart(g, k, TILE);
   T* Fs = F + g.foff;
@@ -681,6 +689,7 @@ __device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, 
     static_assert(sizeof(T) != 8 || TILE == 16, "the FP64 tile kernels are written for 16 x 16 tiles");
     __shared__ double s_inv;
     DiagLdltF64(a, b, &s_inv);
+    Stamp(tr, 3);
     for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
       const int r = e % TILE, c = e / TILE;
       if (r < b && c < b && r >= c) St(Fs + (r0 + r) + int64_t(r0 + c) * g.m, a[c * TILE + r]);
@@ -727,6 +736,7 @@ __device__ void DiagCore(const FactorDev& f, const Geom& g, int s, int k, T* F, 
       if (r == 0 && redo) s_redo = 1;
     }
     __syncthreads();
+    Stamp(tr, 3);
     if (s_redo) {
       // FP64 redo from the saved input: the double tile occupies a and b
       double* dt = reinterpret_cast<double*>(sm.a);
@@ -777,7 +787,8 @@ __device__ void TaskDiag(const FactorDev& f, int s, int k, T* F, T* Linv, TileSm
   const int b = TileSize(g, k, TILE), r0 = TileStart(g, k, TILE);
   LoadTileT<T, TILE>(F + g.foff, g.m, r0, r0, b, b, sm.a);
   __syncthreads();
-  DiagCore<T, TILE>(f, g, s, k, F, Linv, sm.a, sm);
+  Stamp(ready, 0);
+  DiagCore<T, TILE>(f, g, s, k, F, Linv, sm.a, sm, ready);
 }
 
 // sum_{q < n} x[q * TILE + r] y[q * TILE + c] over two tiles held transposed in shared memory, with
@@ -871,6 +882,7 @@ __device__ void LookaheadF64(const FactorDev& f, int s, int i, int k, T* F, T* L
   __syncthreads();
   for (int c = threadIdx.x; c < bk; c += blockDim.x) sm.d[c] = PivotReciprocal<T>(sm.b[c * TILE + c]);
   __syncthreads();
+  Stamp(ready, 0);
   PanelSolveSubstF64(sm.a, sm.b, sm.d, bi, bk, sm.c, sm.w);
   __syncthreads();
   for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
@@ -878,6 +890,7 @@ __device__ void LookaheadF64(const FactorDev& f, int s, int i, int k, T* F, T* L
     if (r < bi && c < bk) St(Fs + (ri + r) + int64_t(ck + c) * g.m, sm.c[c * TILE + r]);
   }
   Signal(f.tile_state + StateIdx(g, i, k), kFinal);
+  Stamp(ready, 1);
   // F_ii -= Y X^T (Y = X D), lower part
   for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
     const int r = e % TILE, c = e / TILE;
@@ -885,7 +898,8 @@ __device__ void LookaheadF64(const FactorDev& f, int s, int i, int k, T* F, T* L
     sm.e[c * TILE + r] -= PanelDot<T, TILE>(sm.w, sm.c, r, c, bk);
   }
   __syncthreads();
-  DiagCore<T, TILE>(f, g, s, i, F, Linv, sm.e, sm);
+  Stamp(ready, 2);
+  DiagCore<T, TILE>(f, g, s, i, F, Linv, sm.e, sm, ready);
 }
 
 template <typename T, int TILE>
@@ -911,6 +925,7 @@ __device__ void TaskLookahead(const FactorDev& f, int s, int i, int k, T* F, T* 
   for (int c = threadIdx.x; c < bk; c += blockDim.x)
     sm.d[c] = PivotReciprocal<T>(Ld(Fs + int64_t(ck + c) * (g.m + 1)));
   __syncthreads();
+  Stamp(ready, 0);
   // L_ik (r, c) = sum_{q <= c} F(r, q) Li(c, q) / D_c, into c[] (transposed) and the front, and
   // L_ik D into w[]
   for (int e = threadIdx.x; e < TILE * TILE; e += blockDim.x) {
@@ -923,6 +938,7 @@ __device__ void TaskLookahead(const FactorDev& f, int s, int i, int k, T* F, T* 
     if (r < bi && c < bk) St(Fs + (ri + r) + int64_t(ck + c) * g.m, l);
   }
   Signal(f.tile_state + StateIdx(g, i, k), kFinal);
+  Stamp(ready, 1);
   // F_ii after every earlier panel's update, minus L_ik D_k L_ik^T (lower part), in a[]
   ok = true;
   if (threadIdx.x == 0) ok = WaitAtLeast(f.tile_state + StateIdx(g, i, i), 1 + k, f.error);
@@ -935,7 +951,8 @@ __device__ void TaskLookahead(const FactorDev& f, int s, int i, int k, T* F, T* 
     sm.a[c * TILE + r] -= PanelDot<T, TILE>(sm.w, sm.c, r, c, bk);
   }
   __syncthreads();
-  DiagCore<T, TILE>(f, g, s, i, F, Linv, sm.a, sm);
+  Stamp(ready, 2);
+  DiagCore<T, TILE>(f, g, s, i, F, Linv, sm.a, sm, ready);
 }
 
 template <typename T, int TILE>
@@ -1003,10 +1020,10 @@ __global__ void __launch_bounds__(kFactorThreads, kFactorCtasPerSm) FactorKernel
     if (t >= f.ntasks) return;
     const int4 task = f.tasks[t];
     const int i = task.z >> 16, j = task.z & 0xffff, k = task.w;
-    unsigned long long* ready = f.trace ? f.trace + 4 * int64_t(t) + 1 : nullptr;
+    unsigned long long* ready = f.trace ? f.trace + 8 * int64_t(t) + 1 : nullptr;
     if (f.trace && threadIdx.x == 0) {
-      f.trace[4 * int64_t(t)] = Clock64Global();
-      f.trace[4 * int64_t(t) + 3] = SmId();
+      f.trace[8 * int64_t(t)] = Clock64Global();
+      f.trace[8 * int64_t(t) + 3] = SmId();
     }
     switch (task.x) {
       case kTaskAssemble: TaskAssemble<T, TILE>(f, task.y, j, A, damping, F, &s_flag, ready); break;
@@ -1018,7 +1035,7 @@ __global__ void __launch_bounds__(kFactorThreads, kFactorCtasPerSm) FactorKernel
         if (threadIdx.x == 0) atomicExch(f.error, kDevBadTask);
     }
     __syncthreads();
-    if (f.trace && threadIdx.x == 0) f.trace[4 * int64_t(t) + 2] = Clock64Global();
+    if (f.trace && threadIdx.x == 0) f.trace[8 * int64_t(t) + 2] = Clock64Global();
   }
 }
 
