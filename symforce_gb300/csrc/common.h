@@ -168,7 +168,7 @@ struct TaskPlan {
   std::vector<int64_t> asm_col_off;   // per (front, tile column)
   std::vector<int32_t> asm_col_list;
 };
-TaskPlan PlanTasks(const Symbolic& sym, int tile);
+TaskPlan PlanTasks(const Symbolic& sym, int tile, bool separate_inverse);
 
 // Flattened per-(front, tile column) assembly lists, extend-add rounds and solve maps of a
 // symbolic factorization and its task plan, as the device kernels read them.

@@ -46,8 +46,20 @@ struct PcgState {
 
 // Task kinds of the persistent factorization kernel.
 // kTaskLookahead(k): the panel solve of tile (k+1, k), the update of diagonal tile (k+1, k+1) by
-// that panel and the LDL^T of tile (k+1, k+1), in one CTA (the critical chain of a front).
-enum TaskType { kTaskAssemble = 0, kTaskDiag = 1, kTaskTrsm = 2, kTaskUpdate = 3, kTaskLookahead = 4 };
+// that panel and the LDL^T of tile (k+1, k+1), in one CTA.
+// kTaskChain: the whole critical chain of a front in one CTA: the LDL^T of tile (0, 0), then every
+// look-ahead step k = 0 .. np - 2 in turn, the factor of tile (k, k) kept in shared memory.
+// kTaskInverse(k): the inverse of tile (k, k)'s unit lower factor, for the triangular solves (FP64
+// chains leave it out of the chain).
+enum TaskType {
+  kTaskAssemble = 0,
+  kTaskDiag = 1,
+  kTaskTrsm = 2,
+  kTaskUpdate = 3,
+  kTaskLookahead = 4,
+  kTaskChain = 5,
+  kTaskInverse = 6
+};
 
 enum DeviceErrorCode {
   kDevOk = 0,

@@ -27,7 +27,8 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   fp.sym = Analyze(pat, ordering);
   const Symbolic& S = fp.sym;
   const int tile = elem == 8 ? kFactorTileF64 : kFactorTileF32;
-  fp.plan = PlanTasks(S, tile);
+  // FP64 chains leave the inverses of their diagonal factors to separate tasks
+  fp.plan = PlanTasks(S, tile, elem == 8);
   const TaskPlan& T = fp.plan;
   FactorDev& f = fp.f;
   f.ns = S.ns;
@@ -64,8 +65,11 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   f.scalar_old = A.Upload(M.scalar_old);
   f.tile_state = A.Zeros<int>(size_t(T.nstates));
   f.counters = A.Zeros<int>(2);
-  fp.nflags = 2 * S.ns;
+  fp.nflags = 2 * S.ns + kSmFlagSlots + 1;
   f.front_flags = A.Zeros<int>(size_t(fp.nflags));
+  f.sm_flags = f.front_flags + 2 * S.ns;
+  // chains may take at most half of the SMs for themselves
+  f.iso_limit = std::max(1, num_sms / 2);
   f.error = error_word;
   f.fp64_tiles = A.Zeros<int>(1);
   int maxm = 1;

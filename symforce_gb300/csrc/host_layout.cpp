@@ -104,94 +104,121 @@ LinLayout BuildLinLayout(const HostProblem& P) {
     for (int e = 0; e < nent; ++e) m[e] = e < nh ? e < mt * (mt + 1) / 2 : e - nh < mt;
     return m;
   };
-  // Slots (H value index or nvals + tangent index) of all entries of the user's factor f: the
-  // factor's key blocks are looked up once, each entry adds its offset inside the block.
-  auto factor_slots = [&](const HostBatch& B, int f, const int* kslot_of, const int* local_of,
-                          int64_t* out) {
-    const int td = B.tdim, nk = B.nk;
-    const int32_t* keys = &B.keys[size_t(f) * nk];
-    int64_t bo[3][3];
-    bool swapped[3][3];
-    for (int sa = 0; sa < nk; ++sa)
-      for (int sb = 0; sb <= sa; ++sb) {
-        const int ka = keys[sa], kb = keys[sb];
-        swapped[sa][sb] = ka < kb;
-        bo[sa][sb] = L.H.boff[ka >= kb ? find_block(ka, kb) : find_block(kb, ka)];
-      }
-    int e = 0;
-    for (int a = 0; a < td; ++a)
-      for (int b = 0; b <= a; ++b, ++e) {
-        const int sa = kslot_of[a], sb = kslot_of[b];
-        const int ra = local_of[a], rb = local_of[b];
-        if (sa == sb) out[e] = bo[sa][sa] + int64_t(ra) * P.tdim[keys[sa]] + rb;
-        else if (!swapped[sa][sb]) out[e] = bo[sa][sb] + int64_t(ra) * P.tdim[keys[sb]] + rb;
-        else out[e] = bo[sa][sb] + int64_t(rb) * P.tdim[keys[sa]] + ra;
-      }
-    for (int a = 0; a < td; ++a, ++e) out[e] = L.nvals + P.toff[keys[kslot_of[a]]] + local_of[a];
+  // Packed entries by key-slot pair: a factor's keys are distinct (ParseProblem), so the entries
+  // of one pair of its key slots fill one stored block (the lower triangle of a diagonal block, a
+  // whole off-diagonal block), and every value of a block has the same contributors.  The counts
+  // and the staging ranks below are therefore kept per block, and an entry's slot is its block's
+  // offset plus its place inside the block, stored (max key, min key) row-major.
+  struct EntryPlace {
+    std::vector<int32_t> pair;    // key-slot pair sa * (sa + 1) / 2 + sb (sa >= sb) of entry e < nh
+    std::vector<int32_t> off;     // place in the block stored as (key of sa, key of sb)
+    std::vector<int32_t> off_sw;  // place in the block stored as (key of sb, key of sa)
+    std::vector<int32_t> lidx;    // diagonal pair (sa == sb): rank of the entry in the lower
+                                  // triangle (row-major); -1 for other pairs
+    std::vector<int32_t> rslot, rloc;  // rhs entry: key slot and row inside the key
   };
+  std::vector<EntryPlace> places(P.batches.size());
+  for (size_t bi = 0; bi < P.batches.size(); ++bi) {
+    const auto& B = P.batches[bi];
+    std::vector<int> ks, lo;
+    for (int sl = 0; sl < B.nk; ++sl)
+      for (int r = 0; r < B.key_tdim[sl]; ++r) {
+        ks.push_back(sl);
+        lo.push_back(r);
+      }
+    EntryPlace& E = places[bi];
+    for (int a = 0; a < B.tdim; ++a)
+      for (int b = 0; b <= a; ++b) {
+        const int sa = ks[a], sb = ks[b], ra = lo[a], rb = lo[b];
+        E.pair.push_back(sa * (sa + 1) / 2 + sb);
+        E.off.push_back(ra * B.key_tdim[sb] + rb);
+        E.off_sw.push_back(rb * B.key_tdim[sa] + ra);
+        E.lidx.push_back(sa == sb ? ra * (ra + 1) / 2 + rb : -1);
+      }
+    for (int a = 0; a < B.tdim; ++a) {
+      E.rslot.push_back(ks[a]);
+      E.rloc.push_back(lo[a]);
+    }
+  }
+  // the stored block of each key-slot pair of the user's factor f (swapped: stored as (kb, ka))
+  auto factor_blocks = [&](const HostBatch& B, int f, int64_t* blk, char* swapped) {
+    const int32_t* keys = &B.keys[size_t(f) * B.nk];
+    for (int sa = 0; sa < B.nk; ++sa)
+      for (int sb = 0; sb <= sa; ++sb) {
+        const int ka = keys[sa], kb = keys[sb], pr = sa * (sa + 1) / 2 + sb;
+        swapped[pr] = ka < kb;
+        blk[pr] = ka >= kb ? find_block(ka, kb) : find_block(kb, ka);
+      }
+  };
+  constexpr int kMaxPairs = 6;  // factors have at most three keys
   const int64_t nslots = L.nvals + P.N;
-  std::vector<int32_t> cnt(nslots, 0);
-  std::vector<std::vector<int>> kslot(P.batches.size()), local(P.batches.size());
+  std::vector<int32_t> cnt_blk(static_cast<size_t>(L.H.nblocks()), 0), cnt_key(P.nkeys, 0);
   for (size_t bi = 0; bi < P.batches.size(); ++bi) {
     const auto& B = P.batches[bi];
-    for (int s = 0; s < B.nk; ++s)
-      for (int r = 0; r < B.key_tdim[s]; ++r) {
-        kslot[bi].push_back(s);
-        local[bi].push_back(r);
-      }
-  }
-  for (size_t bi = 0; bi < P.batches.size(); ++bi) {
-    const auto& B = P.batches[bi];
-    const int nh = B.tdim * (B.tdim + 1) / 2;
-    const int nent = nh + B.tdim;
-    std::vector<int64_t> slots(nent);
-    const std::vector<char> merged = merged_entries(bi, nh, nent);
+    if (B.nk * (B.nk + 1) / 2 > kMaxPairs) throw Error(SFG_ERR_STRUCTURE, "factor with more than three keys");
+    const int ms = MergedKeySlots(B.kind);
+    int64_t blk[kMaxPairs];
+    char swapped[kMaxPairs];
     for (int f = 0; f < B.count; ++f) {
-      factor_slots(B, order[bi][f], kslot[bi].data(), local[bi].data(), slots.data());
-      if (merged_tail(bi, f)) {
-        for (int e = 0; e < nent; ++e)
-          if (!merged[e]) cnt[slots[e]]++;
-      } else {
-        for (int e = 0; e < nent; ++e) cnt[slots[e]]++;
+      const int uf = order[bi][f];
+      factor_blocks(B, uf, blk, swapped);
+      const bool tail = merged_tail(bi, f);
+      for (int sa = 0; sa < B.nk; ++sa) {
+        if (tail && sa < ms) continue;  // carried by the warp's first factor
+        for (int sb = 0; sb <= sa; ++sb) cnt_blk[blk[sa * (sa + 1) / 2 + sb]]++;
+        cnt_key[B.keys[size_t(uf) * B.nk + sa]]++;
       }
     }
   }
-  for (int64_t s = 0; s < nslots; ++s)
-    if (cnt[s] == 0) {
-      // every stored value must receive at least one contribution (the reference sets explicit
-      // zeros from the first linearization; the block pattern never has untouched entries except
-      // the strictly upper part of diagonal blocks, which is not a slot)
-      const bool upper_of_diag = [&] {
-        if (s >= L.nvals) return false;
-        const auto it = std::upper_bound(L.H.boff.begin(), L.H.boff.end(), s) - 1;
-        const int64_t blk = it - L.H.boff.begin();
-        int j = int(std::upper_bound(L.H.colptr.begin(), L.H.colptr.end(), blk) - L.H.colptr.begin()) - 1;
-        const int i = L.H.rows[blk];
-        if (i != j) return false;
-        const int64_t o = s - L.H.boff[blk];
-        return (o % P.tdim[i]) > (o / P.tdim[i]);
-      }();
-      if (!upper_of_diag) throw Error(SFG_ERR_STRUCTURE, "Hessian entry without a contributor");
-    }
-  // staging groups in slot order; next_sink[s]: the sink index the next contribution to slot s
-  // gets (its staging slots in turn), or -1 when the slot has one contributor and is written in
-  // place (one array, so a contribution costs one random access)
+  // Every stored value must receive at least one contribution (the reference sets explicit zeros
+  // from the first linearization; the block pattern never has untouched entries except the strict
+  // upper part of diagonal blocks, which is not a slot).
+  for (int64_t q = 0; q < L.H.nblocks(); ++q)
+    if (cnt_blk[q] == 0) throw Error(SFG_ERR_STRUCTURE, "Hessian entry without a contributor");
+  for (int k = 0; k < P.nkeys; ++k)
+    if (cnt_key[k] == 0) throw Error(SFG_ERR_STRUCTURE, "Hessian entry without a contributor");
+  // Staging groups in slot order: every slot of a block (the lower triangle of a diagonal block)
+  // with more than one contributor gets as many consecutive staging slots as its block has
+  // contributors.  base_blk / base_key: the first staging slot of the block's (the key's rhs's)
+  // first slot, or -1 when its slots have one contributor each and are written in place.
   constexpr int64_t kSinkLimit = int64_t(1) << 31;
   if (nslots >= kSinkLimit) throw Error(SFG_ERR_STRUCTURE, "problem too large for 32-bit sink indices");
-  std::vector<int32_t> next_sink(nslots, -1);
+  std::vector<int32_t> base_blk(cnt_blk.size(), -1), base_key(P.nkeys, -1);
   L.red_ptr.push_back(0);
-  for (int64_t s = 0; s < nslots; ++s)
-    if (cnt[s] > 1) {
-      if (nslots + L.red_ptr.back() + cnt[s] >= kSinkLimit)
-        throw Error(SFG_ERR_STRUCTURE, "problem too large for 32-bit sink indices");
-      next_sink[s] = int32_t(nslots + L.red_ptr.back());
-      L.red_dst.push_back(int32_t(s));
-      L.red_ptr.push_back(L.red_ptr.back() + cnt[s]);
+  auto stage = [&](int64_t slot, int32_t c) {
+    if (nslots + L.red_ptr.back() + c >= kSinkLimit)
+      throw Error(SFG_ERR_STRUCTURE, "problem too large for 32-bit sink indices");
+    L.red_dst.push_back(int32_t(slot));
+    L.red_ptr.push_back(L.red_ptr.back() + c);
+  };
+  for (int kc = 0; kc < P.nkeys; ++kc)
+    for (int64_t q = L.H.colptr[kc]; q < L.H.colptr[kc + 1]; ++q) {
+      const int32_t c = cnt_blk[q];
+      if (c <= 1) continue;
+      base_blk[q] = int32_t(nslots + L.red_ptr.back());
+      const int dc = P.tdim[kc], dr = P.tdim[L.H.rows[q]];
+      const bool diag = L.H.rows[q] == kc;
+      for (int r = 0; r < dr; ++r)
+        for (int cc = 0; cc < (diag ? r + 1 : dc); ++cc) stage(L.H.boff[q] + int64_t(r) * dc + cc, c);
     }
+  for (int k = 0; k < P.nkeys; ++k) {
+    const int32_t c = cnt_key[k];
+    if (c <= 1) continue;
+    base_key[k] = int32_t(nslots + L.red_ptr.back());
+    for (int r = 0; r < P.tdim[k]; ++r) stage(L.nvals + P.toff[k] + r, c);
+  }
   L.nstage = L.red_ptr.back();
-  std::vector<int32_t>().swap(cnt);
+  // Sink of the contribution of rank k (device factor order) in its block: the slot itself for a
+  // single contributor, else base + (place of the slot among the block's slots) * count + k.
+  std::vector<int32_t> count_blk(cnt_blk), count_key(cnt_key);
+  std::fill(cnt_blk.begin(), cnt_blk.end(), 0);
+  std::fill(cnt_key.begin(), cnt_key.end(), 0);
+  std::vector<int32_t>& rank_blk = cnt_blk;
+  std::vector<int32_t>& rank_key = cnt_key;
   for (size_t bi = 0; bi < P.batches.size(); ++bi) {
     const auto& B = P.batches[bi];
+    const EntryPlace& E = places[bi];
+    const int ms = MergedKeySlots(B.kind);
     LinLayout::BatchMap M;
     const int nh = B.tdim * (B.tdim + 1) / 2;
     M.nent = nh + B.tdim;
@@ -199,24 +226,50 @@ LinLayout BuildLinLayout(const HostProblem& P) {
     M.dest.resize(size_t(M.nent) * B.count);
     // factors in runs of 32 (a warp): sink indices in factor order, then written entry-major
     constexpr int kRun = 32;
-    std::vector<int64_t> slots(M.nent);
     std::vector<int32_t> run(size_t(kRun) * M.nent);
     const std::vector<char> merged = merged_entries(bi, nh, M.nent);
+    int64_t blk[kMaxPairs], base[kMaxPairs];
+    char swapped[kMaxPairs];
+    int32_t rank[kMaxPairs], sbase[kMaxPairs], scount[kMaxPairs];
+    int32_t rank_rhs[3], rbase[3], rcount[3];
     for (int f0 = 0; f0 < B.count; f0 += kRun) {
       const int nf = std::min(kRun, B.count - f0);
       for (int j = 0; j < nf; ++j) {
-        const int f = f0 + j;
-        factor_slots(B, order[bi][f], kslot[bi].data(), local[bi].data(), slots.data());
+        const int f = f0 + j, uf = order[bi][f];
+        const int32_t* keys = &B.keys[size_t(uf) * B.nk];
+        factor_blocks(B, uf, blk, swapped);
         const bool tail = merged_tail(bi, f);
+        for (int sa = 0; sa < B.nk; ++sa) {
+          const bool skip = tail && sa < ms;
+          for (int sb = 0; sb <= sa; ++sb) {
+            const int pr = sa * (sa + 1) / 2 + sb;
+            const int64_t q = blk[pr];
+            base[pr] = L.H.boff[q];
+            sbase[pr] = base_blk[q];
+            scount[pr] = count_blk[q];
+            rank[pr] = skip ? 0 : rank_blk[q]++;
+          }
+          const int kk = keys[sa];
+          rbase[sa] = base_key[kk];
+          rcount[sa] = count_key[kk];
+          rank_rhs[sa] = skip ? 0 : rank_key[kk]++;
+        }
         for (int e = 0; e < M.nent; ++e) {
           int32_t& out = run[size_t(e) * kRun + j];
           if (tail && merged[e]) {
             out = run[size_t(e) * kRun];  // never read: the warp's first factor stores
             continue;
           }
-          const int64_t s = slots[e];
-          int32_t& nx = next_sink[s];
-          out = nx < 0 ? int32_t(s) : nx++;
+          if (e < nh) {
+            const int pr = E.pair[e];
+            const int32_t o = swapped[pr] ? E.off_sw[e] : E.off[e];
+            if (sbase[pr] < 0) out = int32_t(base[pr] + o);
+            else out = sbase[pr] + (E.lidx[e] >= 0 ? E.lidx[e] : o) * scount[pr] + rank[pr];
+          } else {
+            const int a = e - nh, sl = E.rslot[a];
+            out = rbase[sl] < 0 ? int32_t(L.nvals + P.toff[keys[sl]] + E.rloc[a])
+                                : rbase[sl] + E.rloc[a] * rcount[sl] + rank_rhs[sl];
+          }
         }
       }
       for (int e = 0; e < M.nent; ++e)

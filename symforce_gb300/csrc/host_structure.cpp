@@ -609,7 +609,7 @@ Symbolic Analyze(const BlockPattern& A, int ordering) {
   return S;
 }
 
-TaskPlan PlanTasks(const Symbolic& sym, int tile) {
+TaskPlan PlanTasks(const Symbolic& sym, int tile, bool separate_inverse) {
   TaskPlan T;
   T.tile = tile;
   T.tile_base.assign(sym.ns + 1, 0);
@@ -648,24 +648,78 @@ TaskPlan PlanTasks(const Symbolic& sym, int tile) {
     T.asm_col_off[q + 1] = T.asm_col_off[q] + int64_t(percol[q].size());
     T.asm_col_list.insert(T.asm_col_list.end(), percol[q].begin(), percol[q].end());
   }
+  // Tasks are generated front by front in postorder, each front panel by panel; every task comes
+  // after the tasks it waits on.  The critical chain of a front (the LDL^T of tile (0, 0), then for
+  // every panel k < np - 1 the panel solve of tile (k+1, k), the update of (k+1, k+1) by it and
+  // the LDL^T of (k+1, k+1)) is one chain task, which stays in its CTA for the front's whole
+  // factorization; the other panel solves and trailing updates follow in panel order.  A
+  // single-panel front has a plain diagonal task.
+  //
+  // The list is then ordered by each task's start time in an as-soon-as-possible schedule with
+  // unbounded CTAs and nominal durations (a topological order, since every task starts after the
+  // tasks it waits on end): the kernel's CTAs claim tasks in list order, and in front order they
+  // would claim thousands of one front's updates that wait on its chain while the independent
+  // fronts beside it wait to be claimed.
+  //
+  // Deadlock freedom: a task only waits on tasks that start earlier, so on tasks earlier in the
+  // list, claimed by running CTAs; chain step k waits only on tasks that end before the step
+  // starts, and every task that waits on step k starts after the step starts, so those tasks are
+  // claimed before any CTA can be held by a task waiting on step k: the chain always advances.
+  struct Timed {
+    double key;
+    int4 task;
+  };
+  std::vector<Timed> timed;
+  // nominal durations (microseconds; only the order matters)
+  constexpr double kAsm = 5, kDiag = 5, kStep = 10, kTrsm = 4, kUpd = 5, kInv = 3;
+  std::vector<double> front_done(sym.ns, 0.0);
   for (int s = 0; s < sym.ns; ++s) {
     const int nt = T.ntiles[s], np = T.npiv[s];
-    for (int j = 0; j < nt; ++j) T.tasks.push_back(make_int4(kTaskAssemble, s, j, 0));
-    // Panel k: its diagonal tile is factored by the lookahead task of panel k - 1 (for k > 0),
-    // which also does the panel solve of tile (k+1, k)... in panel k the lookahead task does the
-    // panel solve of tile (k+1, k), the update of (k+1, k+1) and the LDL^T of (k+1, k+1), so the
-    // critical chain of the front runs in one CTA per panel.  Every task still comes after the tasks
-    // it waits on, which keeps the schedule free of deadlock.
+    // ver: time tile (i, j) reached its latest version so far; fin: time it became final
+    std::vector<double> ver(size_t(nt) * nt, 0.0), fin(size_t(nt) * nt, 0.0);
+    auto V = [&](int i, int j) -> double& { return ver[size_t(i) * nt + j]; };
+    auto Fn = [&](int i, int j) -> double& { return fin[size_t(i) * nt + j]; };
+    double t0 = 0.0, done = 0.0;
+    for (int c : sym.sn_children[s]) t0 = std::max(t0, front_done[c]);
+    auto add = [&](double start, double dur, int4 task) {
+      timed.push_back({start, task});
+      done = std::max(done, start + dur);
+      return start + dur;
+    };
+    for (int j = 0; j < nt; ++j) {
+      const double e = add(t0, kAsm, make_int4(kTaskAssemble, s, j, 0));
+      for (int i = j; i < nt; ++i) V(i, j) = e;
+    }
+    if (np == 1) {
+      Fn(0, 0) = add(V(0, 0), kDiag, make_int4(kTaskDiag, s, 0, 0));
+    } else {
+      // the chain task sits at its first step; its later steps are timed here, not listed
+      Fn(0, 0) = add(V(0, 0), kDiag, make_int4(kTaskChain, s, 0, 0));
+    }
     for (int k = 0; k < np; ++k) {
       const bool ahead = k + 1 < np;
-      if (k == 0) T.tasks.push_back(make_int4(kTaskDiag, s, 0, 0));
-      if (ahead) T.tasks.push_back(make_int4(kTaskLookahead, s, (k + 1) * 65536 + k, k));
-      for (int i = k + (ahead ? 2 : 1); i < nt; ++i) T.tasks.push_back(make_int4(kTaskTrsm, s, i * 65536 + k, k));
+      if (ahead) {
+        const double st = std::max({Fn(k, k), V(k + 1, k), V(k + 1, k + 1)});
+        Fn(k + 1, k) = st + kStep / 2;  // the panel tile is published halfway through the step
+        Fn(k + 1, k + 1) = st + kStep;
+        done = std::max(done, st + kStep);
+      }
+      for (int i = k + (ahead ? 2 : 1); i < nt; ++i)
+        Fn(i, k) = add(std::max(Fn(k, k), V(i, k)), kTrsm, make_int4(kTaskTrsm, s, i * 65536 + k, k));
       for (int j = k + 1; j < nt; ++j)
-        for (int i = j; i < nt; ++i)
-          if (!(ahead && i == k + 1 && j == k + 1)) T.tasks.push_back(make_int4(kTaskUpdate, s, i * 65536 + j, k));
+        for (int i = j; i < nt; ++i) {
+          if (ahead && i == k + 1 && j == k + 1) continue;  // chain step k
+          V(i, j) = add(std::max({Fn(i, k), Fn(j, k), V(i, j)}), kUpd, make_int4(kTaskUpdate, s, i * 65536 + j, k));
+        }
     }
+    // the inverses of the chain's diagonal factors, for the triangular solves only
+    if (separate_inverse && np > 1)
+      for (int k = 0; k < np; ++k) add(Fn(k, k), kInv, make_int4(kTaskInverse, s, k * 65536 + k, k));
+    front_done[s] = done;
   }
+  std::stable_sort(timed.begin(), timed.end(), [](const Timed& a, const Timed& b) { return a.key < b.key; });
+  T.tasks.reserve(timed.size());
+  for (const Timed& x : timed) T.tasks.push_back(x.task);
   return T;
 }
 

@@ -198,7 +198,12 @@ struct FactorDev {
   int64_t a_stride;           // per-state-block stride of the matrix values (0: fixed)
   int64_t b_stride;           // per-state-block stride of the rhs (0: fixed)
   const int* gate;            // optional: the kernels return at once unless *gate != 0
+  // optional: [kSmFlagSlots] per-SM flags (1: the SM is given to a chain task; its other CTAs
+  // leave the kernel) followed by the count of SMs so given, at most iso_limit
+  int* sm_flags = nullptr;
+  int iso_limit = 0;
 };
+constexpr int kSmFlagSlots = 512;
 template <typename T>
 void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F, void* Linv,
                   int grid, cudaStream_t s);

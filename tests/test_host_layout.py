@@ -246,7 +246,7 @@ def test_schur_plan_matches_dense_schur_complement(shim):
 
 
 # tile task types of the persistent factorization (device.cuh TaskType)
-ASSEMBLE, DIAG, TRSM, UPDATE, LOOKAHEAD = 0, 1, 2, 3, 4
+ASSEMBLE, DIAG, TRSM, UPDATE, LOOKAHEAD, CHAIN, INVERSE = 0, 1, 2, 3, 4, 5, 6
 FINAL = 1 << 30
 
 
@@ -264,19 +264,57 @@ def _factor_plan(lib, which, tile):
 
 def _replay_tasks(tasks, npiv, ntiles, parent, w, m, cptr, clist, tile):
     """Run the task list in its own order on the tile-state machine of the factorization kernel
-    (kernels_solve.cu: TaskAssemble, TaskDiag, TaskTrsm, TaskLookahead, TaskUpdate): every wait
-    must already hold when its task comes up.  The kernel's CTAs claim tasks in list order, so a
-    task only ever waits on tasks claimed before it, which then always finish: no deadlock."""
+    (kernels_solve.cu: TaskAssemble, TaskDiag, TaskTrsm, TaskLookahead, TaskUpdate, TaskChain,
+    TaskInverse): every wait must already hold when its task comes up.  The kernel's CTAs claim
+    tasks in list order, so a task only ever waits on tasks claimed before it, which then always
+    finish.  A chain task stays in its CTA for the front's whole factorization: its steps are run
+    here as soon as their waits hold (the chain's CTA advances by itself), and a later task that
+    waits on a step that cannot have run yet fails the replay; every chain must end up complete.
+    So no task waits on a step that waits on an unclaimed task: no deadlock.  (A CTA claims its
+    next task when it starts one, except under a chain task, whose CTA would otherwise hold a task
+    the chain waits on.)"""
     ns = len(npiv)
     state = [np.zeros((int(ntiles[s]), int(ntiles[s])), dtype=np.int64) for s in range(ns)]
+    chains = {}  # front -> next chain step (-1: the diagonal tile (0, 0))
 
     def need(s, i, j, v, what):
         assert state[s][i, j] >= v, f"front {s}: {what} waits on tile ({i}, {j}) >= {v}, has {state[s][i, j]}"
 
+    def advance_chains():
+        for s in list(chains):
+            st, nps = state[s], int(npiv[s])
+            while True:
+                k = chains[s]
+                if k < 0:
+                    if st[0, 0] < 1:
+                        break
+                    st[0, 0] = FINAL
+                else:
+                    # step k: the panel solve of (k+1, k), the update of (k+1, k+1) by it and its
+                    # LDL^T
+                    i = k + 1
+                    assert st[k, k] == FINAL
+                    if st[i, k] < 1 + k or st[i, i] < 1 + k:
+                        break
+                    st[i, k] = FINAL
+                    st[i, i] = FINAL
+                chains[s] = k + 1
+                if chains[s] + 1 >= nps:
+                    del chains[s]
+                    break
+
     for ty, s, z, k in tasks:
+        advance_chains()
         i, j = int(z) >> 16, int(z) & 0xFFFF
         st = state[s]
-        if ty == ASSEMBLE:
+        if ty == CHAIN:
+            assert int(npiv[s]) > 1 and s not in chains
+            chains[s] = -1
+            advance_chains()
+        elif ty == INVERSE:
+            assert i == j == k
+            need(s, k, k, FINAL, "inverse")
+        elif ty == ASSEMBLE:
             for c in clist[cptr[s]:cptr[s + 1]]:
                 npc, ntc = int(npiv[c]), int(ntiles[c])
                 for a in range(npc, ntc):
@@ -303,6 +341,8 @@ def _replay_tasks(tasks, npiv, ntiles, parent, w, m, cptr, clist, tile):
             st[i, j] = 2 + k
         else:
             raise AssertionError(f"unknown task type {ty}")
+    advance_chains()
+    assert not chains, f"chains left unfinished: {chains}"
     # every front fully factored: pivot and panel tiles final, the update block through all panels
     for s in range(ns):
         nps, nts = int(npiv[s]), int(ntiles[s])
