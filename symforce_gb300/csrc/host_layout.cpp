@@ -13,8 +13,14 @@
 // contribution per entry, at the sink index of its first factor; every other entry stays one
 // contribution per factor.  The staged work of a camera block falls from one slot per observation
 // to one per warp.
+//
+// Counts and staging ranks are kept per stored block (all values of a block have the same
+// contributors), and the passes whose items are independent (factors' block lookups and sink
+// indices, the Schur complement's columns) run on host threads; every array is the same as a
+// sequential pass gives.
 #include <algorithm>
 #include <numeric>
+#include <thread>
 
 #include "layout.h"
 
@@ -75,11 +81,18 @@ LinLayout BuildLinLayout(const HostProblem& P) {
     if (ms == 0) continue;
     for (int s = 0; s < ms; ++s) merged_dims[bi] += B.key_tdim[s];
     auto key = [&](int32_t f, int s) { return B.keys[size_t(f) * B.nk + s]; };
-    std::stable_sort(ord.begin(), ord.end(), [&](int32_t x, int32_t y) {
-      for (int s = 0; s < ms; ++s)
-        if (key(x, s) != key(y, s)) return key(x, s) < key(y, s);
-      return false;
-    });
+    // stable sort by the merged key slots, lexicographic: counting sorts from the last slot
+    {
+      std::vector<int32_t> tmp(ord.size());
+      std::vector<int64_t> cnt(size_t(P.nkeys) + 1);
+      for (int s = ms - 1; s >= 0; --s) {
+        std::fill(cnt.begin(), cnt.end(), 0);
+        for (int32_t f : ord) cnt[size_t(key(f, s)) + 1]++;
+        for (int k = 0; k < P.nkeys; ++k) cnt[k + 1] += cnt[k];
+        for (int32_t f : ord) tmp[size_t(cnt[key(f, s)]++)] = f;
+        ord.swap(tmp);
+      }
+    }
     const int nwarps = B.count / 32;  // full warps only
     warp_merged[bi].assign(size_t(nwarps), 0);
     for (int w = 0; w < nwarps; ++w) {
@@ -152,21 +165,64 @@ LinLayout BuildLinLayout(const HostProblem& P) {
   };
   constexpr int kMaxPairs = 6;  // factors have at most three keys
   const int64_t nslots = L.nvals + P.N;
-  std::vector<int32_t> cnt_blk(static_cast<size_t>(L.H.nblocks()), 0), cnt_key(P.nkeys, 0);
+  if (L.H.nblocks() >= (int64_t(1) << 31)) throw Error(SFG_ERR_STRUCTURE, "too many Hessian blocks");
+  const unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  // run fn(i0, i1) over [0, n) in contiguous parts on host threads
+  auto parallel = [&](int64_t n, int64_t min_part, auto&& fn) {
+    const int nt = int(std::min<int64_t>(nthreads, std::max<int64_t>(1, n / min_part)));
+    if (nt <= 1) {
+      fn(int64_t(0), n);
+      return;
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) pool.emplace_back(fn, n * t / nt, n * (t + 1) / nt);
+    for (auto& th : pool) th.join();
+  };
+  // the stored block of every key-slot pair of every factor (device order) and its orientation
+  std::vector<std::vector<int32_t>> fblk(P.batches.size());
+  std::vector<std::vector<uint8_t>> fswap(P.batches.size());
   for (size_t bi = 0; bi < P.batches.size(); ++bi) {
     const auto& B = P.batches[bi];
-    if (B.nk * (B.nk + 1) / 2 > kMaxPairs) throw Error(SFG_ERR_STRUCTURE, "factor with more than three keys");
+    const int npair = B.nk * (B.nk + 1) / 2;
+    if (npair > kMaxPairs) throw Error(SFG_ERR_STRUCTURE, "factor with more than three keys");
+    fblk[bi].resize(size_t(B.count) * npair);
+    fswap[bi].resize(B.count);
+    parallel(B.count, 4096, [&](int64_t f0, int64_t f1) {
+      int64_t blk[kMaxPairs];
+      char swapped[kMaxPairs];
+      for (int64_t f = f0; f < f1; ++f) {
+        factor_blocks(B, order[bi][f], blk, swapped);
+        uint8_t bits = 0;
+        for (int pr = 0; pr < npair; ++pr) {
+          fblk[bi][size_t(f) * npair + pr] = int32_t(blk[pr]);
+          bits |= uint8_t(swapped[pr] ? 1 : 0) << pr;
+        }
+        fswap[bi][f] = bits;
+      }
+    });
+  }
+  // Contributors per block and per key (rhs) in device factor order; the count before a factor's
+  // contribution is that contribution's rank, kept per factor for the sink pass (key-slot pairs,
+  // then the key slots' rhs).
+  std::vector<int32_t> cnt_blk(static_cast<size_t>(L.H.nblocks()), 0), cnt_key(P.nkeys, 0);
+  std::vector<std::vector<int32_t>> ranks(P.batches.size());
+  for (size_t bi = 0; bi < P.batches.size(); ++bi) {
+    const auto& B = P.batches[bi];
+    const int npair = B.nk * (B.nk + 1) / 2, nr = npair + B.nk;
     const int ms = MergedKeySlots(B.kind);
-    int64_t blk[kMaxPairs];
-    char swapped[kMaxPairs];
+    ranks[bi].resize(size_t(B.count) * nr);
     for (int f = 0; f < B.count; ++f) {
       const int uf = order[bi][f];
-      factor_blocks(B, uf, blk, swapped);
+      int32_t* rk = &ranks[bi][size_t(f) * nr];
+      const int32_t* blk = &fblk[bi][size_t(f) * npair];
       const bool tail = merged_tail(bi, f);
       for (int sa = 0; sa < B.nk; ++sa) {
-        if (tail && sa < ms) continue;  // carried by the warp's first factor
-        for (int sb = 0; sb <= sa; ++sb) cnt_blk[blk[sa * (sa + 1) / 2 + sb]]++;
-        cnt_key[B.keys[size_t(uf) * B.nk + sa]]++;
+        const bool skip = tail && sa < ms;  // carried by the warp's first factor
+        for (int sb = 0; sb <= sa; ++sb) {
+          const int pr = sa * (sa + 1) / 2 + sb;
+          rk[pr] = skip ? 0 : cnt_blk[blk[pr]]++;
+        }
+        rk[npair + sa] = skip ? 0 : cnt_key[B.keys[size_t(uf) * B.nk + sa]]++;
       }
     }
   }
@@ -210,15 +266,11 @@ LinLayout BuildLinLayout(const HostProblem& P) {
   L.nstage = L.red_ptr.back();
   // Sink of the contribution of rank k (device factor order) in its block: the slot itself for a
   // single contributor, else base + (place of the slot among the block's slots) * count + k.
-  std::vector<int32_t> count_blk(cnt_blk), count_key(cnt_key);
-  std::fill(cnt_blk.begin(), cnt_blk.end(), 0);
-  std::fill(cnt_key.begin(), cnt_key.end(), 0);
-  std::vector<int32_t>& rank_blk = cnt_blk;
-  std::vector<int32_t>& rank_key = cnt_key;
+  // Factors are independent here, so runs of them are spread over host threads.
   for (size_t bi = 0; bi < P.batches.size(); ++bi) {
     const auto& B = P.batches[bi];
     const EntryPlace& E = places[bi];
-    const int ms = MergedKeySlots(B.kind);
+    const int npair = B.nk * (B.nk + 1) / 2, nr = npair + B.nk;
     LinLayout::BatchMap M;
     const int nh = B.tdim * (B.tdim + 1) / 2;
     M.nent = nh + B.tdim;
@@ -226,56 +278,56 @@ LinLayout BuildLinLayout(const HostProblem& P) {
     M.dest.resize(size_t(M.nent) * B.count);
     // factors in runs of 32 (a warp): sink indices in factor order, then written entry-major
     constexpr int kRun = 32;
-    std::vector<int32_t> run(size_t(kRun) * M.nent);
     const std::vector<char> merged = merged_entries(bi, nh, M.nent);
-    int64_t blk[kMaxPairs], base[kMaxPairs];
-    char swapped[kMaxPairs];
-    int32_t rank[kMaxPairs], sbase[kMaxPairs], scount[kMaxPairs];
-    int32_t rank_rhs[3], rbase[3], rcount[3];
-    for (int f0 = 0; f0 < B.count; f0 += kRun) {
-      const int nf = std::min(kRun, B.count - f0);
-      for (int j = 0; j < nf; ++j) {
-        const int f = f0 + j, uf = order[bi][f];
-        const int32_t* keys = &B.keys[size_t(uf) * B.nk];
-        factor_blocks(B, uf, blk, swapped);
-        const bool tail = merged_tail(bi, f);
-        for (int sa = 0; sa < B.nk; ++sa) {
-          const bool skip = tail && sa < ms;
-          for (int sb = 0; sb <= sa; ++sb) {
-            const int pr = sa * (sa + 1) / 2 + sb;
-            const int64_t q = blk[pr];
-            base[pr] = L.H.boff[q];
-            sbase[pr] = base_blk[q];
-            scount[pr] = count_blk[q];
-            rank[pr] = skip ? 0 : rank_blk[q]++;
+    const int nruns = (B.count + kRun - 1) / kRun;
+    auto work = [&](int64_t run0, int64_t run1) {
+      std::vector<int32_t> run(size_t(kRun) * M.nent);
+      int64_t base[kMaxPairs];
+      char swapped[kMaxPairs];
+      int32_t sbase[kMaxPairs], scount[kMaxPairs], rbase[3], rcount[3];
+      for (int64_t ru = run0; ru < run1; ++ru) {
+        const int f0 = int(ru) * kRun, nf = std::min(kRun, B.count - f0);
+        for (int j = 0; j < nf; ++j) {
+          const int f = f0 + j, uf = order[bi][f];
+          const int32_t* keys = &B.keys[size_t(uf) * B.nk];
+          const int32_t* rk = &ranks[bi][size_t(f) * nr];
+          const int32_t* blk = &fblk[bi][size_t(f) * npair];
+          const uint8_t bits = fswap[bi][f];
+          const bool tail = merged_tail(bi, f);
+          for (int pr = 0; pr < npair; ++pr) {
+            base[pr] = L.H.boff[blk[pr]];
+            sbase[pr] = base_blk[blk[pr]];
+            scount[pr] = cnt_blk[blk[pr]];
+            swapped[pr] = (bits >> pr) & 1;
           }
-          const int kk = keys[sa];
-          rbase[sa] = base_key[kk];
-          rcount[sa] = count_key[kk];
-          rank_rhs[sa] = skip ? 0 : rank_key[kk]++;
+          for (int sa = 0; sa < B.nk; ++sa) {
+            rbase[sa] = base_key[keys[sa]];
+            rcount[sa] = cnt_key[keys[sa]];
+          }
+          for (int e = 0; e < M.nent; ++e) {
+            int32_t& out = run[size_t(e) * kRun + j];
+            if (tail && merged[e]) {
+              out = run[size_t(e) * kRun];  // never read: the warp's first factor stores
+              continue;
+            }
+            if (e < nh) {
+              const int pr = E.pair[e];
+              const int32_t o = swapped[pr] ? E.off_sw[e] : E.off[e];
+              if (sbase[pr] < 0) out = int32_t(base[pr] + o);
+              else out = sbase[pr] + (E.lidx[e] >= 0 ? E.lidx[e] : o) * scount[pr] + rk[pr];
+            } else {
+              const int a = e - nh, sl = E.rslot[a];
+              out = rbase[sl] < 0 ? int32_t(L.nvals + P.toff[keys[sl]] + E.rloc[a])
+                                  : rbase[sl] + E.rloc[a] * rcount[sl] + rk[npair + sl];
+            }
+          }
         }
-        for (int e = 0; e < M.nent; ++e) {
-          int32_t& out = run[size_t(e) * kRun + j];
-          if (tail && merged[e]) {
-            out = run[size_t(e) * kRun];  // never read: the warp's first factor stores
-            continue;
-          }
-          if (e < nh) {
-            const int pr = E.pair[e];
-            const int32_t o = swapped[pr] ? E.off_sw[e] : E.off[e];
-            if (sbase[pr] < 0) out = int32_t(base[pr] + o);
-            else out = sbase[pr] + (E.lidx[e] >= 0 ? E.lidx[e] : o) * scount[pr] + rank[pr];
-          } else {
-            const int a = e - nh, sl = E.rslot[a];
-            out = rbase[sl] < 0 ? int32_t(L.nvals + P.toff[keys[sl]] + E.rloc[a])
-                                : rbase[sl] + E.rloc[a] * rcount[sl] + rank_rhs[sl];
-          }
-        }
+        for (int e = 0; e < M.nent; ++e)
+          std::copy(run.begin() + size_t(e) * kRun, run.begin() + size_t(e) * kRun + nf,
+                    M.dest.begin() + size_t(e) * B.count + f0);
       }
-      for (int e = 0; e < M.nent; ++e)
-        std::copy(run.begin() + size_t(e) * kRun, run.begin() + size_t(e) * kRun + nf,
-                  M.dest.begin() + size_t(e) * B.count + f0);
-    }
+    };
+    parallel(nruns, 64, work);
     M.order = std::move(order[bi]);
     L.maps.push_back(std::move(M));
   }
@@ -315,8 +367,20 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L) {
   S.c_toff = S.nB;
   for (int k = S.nB_keys; k < P.nkeys; ++k)
     if (P.tdim[k] != 3) throw Error(SFG_ERR_STRUCTURE, "Schur keys must be 3-dimensional");
-  // E lists per point, sorted by B key
-  std::vector<std::vector<std::pair<int, int64_t>>> pe(S.npoints);
+  const unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  // run fn(i0, i1) over [0, n) in contiguous parts on host threads
+  auto parallel = [&](int64_t n, int64_t min_part, auto&& fn) {
+    const int nt = int(std::min<int64_t>(nthreads, std::max<int64_t>(1, n / min_part)));
+    if (nt <= 1) {
+      fn(int64_t(0), n);
+      return;
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) pool.emplace_back(fn, n * t / nt, n * (t + 1) / nt);
+    for (auto& th : pool) th.join();
+  };
+  // E lists per point (compressed rows), sorted by B key: the points' rows of the B columns of H
+  std::vector<int64_t> pe_ptr(size_t(S.npoints) + 1, 0);
   for (int j = 0; j < P.nkeys; ++j)
     for (int64_t q = L.H.colptr[j]; q < L.H.colptr[j + 1]; ++q) {
       const int i = L.H.rows[q];
@@ -327,36 +391,57 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L) {
                       "Submatrix C of A is not block diagonal, cannot use a Schur complement solver");
         continue;
       }
-      pe[i - S.nB_keys].push_back({j, L.H.boff[q]});
+      pe_ptr[size_t(i - S.nB_keys) + 1]++;
     }
-  S.pt_eptr.push_back(0);
+  for (int p = 0; p < S.npoints; ++p) pe_ptr[p + 1] += pe_ptr[p];
+  const int64_t ne = pe_ptr[S.npoints];
+  std::vector<int32_t> pe_key(static_cast<size_t>(ne));
+  std::vector<int64_t> pe_boff(static_cast<size_t>(ne));
+  {
+    std::vector<int64_t> fill(pe_ptr.begin(), pe_ptr.end() - 1);
+    for (int j = 0; j < S.nB_keys; ++j)  // ascending B keys: each point's list comes out sorted
+      for (int64_t q = L.H.colptr[j]; q < L.H.colptr[j + 1]; ++q) {
+        const int i = L.H.rows[q];
+        if (i < S.nB_keys) continue;
+        const int64_t at = fill[i - S.nB_keys]++;
+        pe_key[at] = j;
+        pe_boff[at] = L.H.boff[q];
+      }
+  }
+  S.pt_diag.resize(S.npoints);
+  S.pt_eptr.assign(pe_ptr.begin(), pe_ptr.end());
+  S.pt_eoff.resize(ne);
+  S.pt_woff.resize(ne);
+  S.pt_of_e.resize(ne);
+  S.pt_ekey_toff.resize(ne);
+  S.pt_ekey_dim.resize(ne);
   for (int p = 0; p < S.npoints; ++p) {
     const int kp = S.nB_keys + p;
-    S.pt_diag.push_back(L.H.boff[L.H.Find(kp, kp)]);
-    for (auto& e : pe[p]) {
-      S.pt_eoff.push_back(e.second);
-      S.pt_woff.push_back(S.nW);
-      S.pt_of_e.push_back(p);
-      S.pt_ekey_toff.push_back(int32_t(P.toff[e.first]));
-      S.pt_ekey_dim.push_back(P.tdim[e.first]);
-      S.nW += 3 * P.tdim[e.first];
+    S.pt_diag[p] = L.H.boff[L.H.Find(kp, kp)];
+    for (int64_t e = pe_ptr[p]; e < pe_ptr[p + 1]; ++e) {
+      S.pt_eoff[e] = pe_boff[e];
+      S.pt_woff[e] = S.nW;
+      S.pt_of_e[e] = p;
+      S.pt_ekey_toff[e] = int32_t(P.toff[pe_key[e]]);
+      S.pt_ekey_dim[e] = P.tdim[pe_key[e]];
+      S.nW += 3 * P.tdim[pe_key[e]];
     }
-    S.pt_eptr.push_back(int64_t(S.pt_eoff.size()));
   }
-  // points of every B key, in point order, with the offset of the point's E block for the key
+  // points of every B key, in point order, with the offset of the point's E block for the key and
+  // the key's place in the point's list
   std::vector<int64_t> kp_ptr(size_t(S.nB_keys) + 1, 0);
-  for (int p = 0; p < S.npoints; ++p)
-    for (const auto& e : pe[p]) kp_ptr[size_t(e.first) + 1]++;
+  for (int64_t e = 0; e < ne; ++e) kp_ptr[size_t(pe_key[e]) + 1]++;
   for (int k = 0; k < S.nB_keys; ++k) kp_ptr[k + 1] += kp_ptr[k];
-  std::vector<int32_t> kp(static_cast<size_t>(kp_ptr[S.nB_keys]));
+  std::vector<int32_t> kp(static_cast<size_t>(kp_ptr[S.nB_keys])), kp_pos(kp.size());
   std::vector<int64_t> kp_eoff(kp.size());
   {
     std::vector<int64_t> fill(kp_ptr.begin(), kp_ptr.end() - 1);
     for (int p = 0; p < S.npoints; ++p)
-      for (const auto& e : pe[p]) {
-        const int64_t q = fill[e.first]++;
+      for (int64_t e = pe_ptr[p]; e < pe_ptr[p + 1]; ++e) {
+        const int64_t q = fill[pe_key[e]]++;
         kp[q] = p;
-        kp_eoff[q] = e.second;
+        kp_pos[q] = int32_t(e - pe_ptr[p]);
+        kp_eoff[q] = pe_boff[e];
       }
   }
   // reduced pattern: the B-B blocks of H and every pair of B keys that share a point, found per
@@ -366,61 +451,91 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L) {
     for (int64_t q = L.H.colptr[j]; q < L.H.colptr[j + 1]; ++q)
       if (L.H.rows[q] < S.nB_keys) pairs.push_back({L.H.rows[q], j});
   {
-    std::vector<int> stamp(size_t(S.nB_keys), -1);
-    for (int kb = 0; kb < S.nB_keys; ++kb)
-      for (int64_t q = kp_ptr[kb]; q < kp_ptr[kb + 1]; ++q)
-        for (const auto& e : pe[kp[q]])
-          if (e.first >= kb && stamp[e.first] != kb) {
-            stamp[e.first] = kb;
-            pairs.push_back({e.first, kb});
+    std::vector<std::vector<std::pair<int, int>>> found(nthreads);
+    std::vector<int64_t> part_start;
+    {
+      const int nt = int(std::min<int64_t>(nthreads, std::max<int64_t>(1, S.nB_keys / 16)));
+      for (int t = 0; t <= nt; ++t) part_start.push_back(int64_t(S.nB_keys) * t / nt);
+    }
+    const int nparts = int(part_start.size()) - 1;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nparts; ++t)
+      pool.emplace_back([&, t] {
+        std::vector<int> stamp(size_t(S.nB_keys), -1);
+        for (int kb = int(part_start[t]); kb < int(part_start[t + 1]); ++kb)
+          for (int64_t q = kp_ptr[kb]; q < kp_ptr[kb + 1]; ++q) {
+            const int p = kp[q];
+            for (int64_t e = pe_ptr[p]; e < pe_ptr[p + 1]; ++e) {
+              const int ka = pe_key[e];
+              if (ka >= kb && stamp[ka] != kb) {
+                stamp[ka] = kb;
+                found[t].push_back({ka, kb});
+              }
+            }
           }
+      });
+    for (auto& th : pool) th.join();
+    for (int t = 0; t < nparts; ++t) pairs.insert(pairs.end(), found[t].begin(), found[t].end());
   }
   std::vector<int> bdims(P.tdim.begin(), P.tdim.begin() + S.nB_keys);
   S.Spat = MakePattern(bdims, pairs);
   const int64_t nsb = S.Spat.nblocks();
-  // terms of every S block in point order (a counting sort by block over the terms in the order
-  // points and their E pairs are visited)
-  int64_t nterms = 0;
-  for (int p = 0; p < S.npoints; ++p) nterms += int64_t(pe[p].size()) * (pe[p].size() + 1) / 2;
-  std::vector<int32_t> tblk(static_cast<size_t>(nterms));
-  S.sb_ptr.assign(size_t(nsb) + 1, 0);
-  {
-    int64_t t = 0;
-    for (int p = 0; p < S.npoints; ++p)
-      for (size_t a = 0; a < pe[p].size(); ++a)
-        for (size_t b = 0; b <= a; ++b) {
-          // pe sorted ascending: a >= b => key_a >= key_b
-          const int64_t blk = S.Spat.Find(pe[p][a].first, pe[p][b].first);
-          tblk[t++] = int32_t(blk);
-          S.sb_ptr[blk + 1]++;
+  // Terms of every S block in point order.  The blocks of column key kb take their terms from the
+  // points that see kb (in point order, so each block's terms come out in point order), one term
+  // per E pair (a >= b) of the point with kb at b; a dense row map per column finds the blocks.
+  // Columns are independent (disjoint blocks): counted, then filled, in parallel.
+  auto for_columns = [&](auto&& fn) {
+    const int nt = int(std::min<int64_t>(nthreads, std::max(1, S.nB_keys / 16)));
+    auto part = [&](int t) {
+      std::vector<int64_t> row_blk(size_t(S.nB_keys), -1);
+      for (int kb = int(int64_t(S.nB_keys) * t / nt); kb < int(int64_t(S.nB_keys) * (t + 1) / nt); ++kb) {
+        for (int64_t q = S.Spat.colptr[kb]; q < S.Spat.colptr[kb + 1]; ++q) row_blk[S.Spat.rows[q]] = q;
+        for (int64_t u = kp_ptr[kb]; u < kp_ptr[kb + 1]; ++u) {
+          const int p = kp[u], b = kp_pos[u];
+          const int64_t e0 = pe_ptr[p], n = pe_ptr[p + 1] - e0;
+          for (int64_t a = b; a < n; ++a) fn(row_blk[pe_key[e0 + a]], e0 + a, e0 + b);  // pair in the pattern
         }
-  }
+      }
+    };
+    if (nt <= 1) {
+      part(0);
+    } else {
+      std::vector<std::thread> pool;
+      for (int t = 0; t < nt; ++t) pool.emplace_back(part, t);
+      for (auto& th : pool) th.join();
+    }
+  };
+  S.sb_ptr.assign(size_t(nsb) + 1, 0);
+  for_columns([&](int64_t blk, int64_t, int64_t) { S.sb_ptr[blk + 1]++; });
   for (int64_t q = 0; q < nsb; ++q) S.sb_ptr[q + 1] += S.sb_ptr[q];
+  const int64_t nterms = S.sb_ptr[nsb];
   S.sb_eoff.resize(size_t(nterms));
   S.sb_woff.resize(size_t(nterms));
   {
     std::vector<int64_t> fill(S.sb_ptr.begin(), S.sb_ptr.end() - 1);
-    int64_t t = 0;
-    for (int p = 0; p < S.npoints; ++p) {
-      const int64_t e0 = S.pt_eptr[p];
-      for (size_t a = 0; a < pe[p].size(); ++a)
-        for (size_t b = 0; b <= a; ++b) {
-          const int64_t k = fill[tblk[t++]]++;
-          S.sb_eoff[k] = S.pt_eoff[e0 + a];
-          S.sb_woff[k] = S.pt_woff[e0 + b];
-        }
-    }
+    for_columns([&](int64_t blk, int64_t ea, int64_t eb) {
+      const int64_t k = fill[blk]++;
+      S.sb_eoff[k] = S.pt_eoff[ea];
+      S.sb_woff[k] = S.pt_woff[eb];
+    });
   }
-  for (int j = 0; j < S.nB_keys; ++j)
-    for (int64_t q = S.Spat.colptr[j]; q < S.Spat.colptr[j + 1]; ++q) {
-      const int i = S.Spat.rows[q];
-      const int64_t hb = L.H.Find(i, j);
-      S.sb_hoff.push_back(hb >= 0 ? L.H.boff[hb] : -1);
-      S.sb_soff.push_back(S.Spat.boff[q]);
-      S.sb_dk.push_back(P.tdim[i]);
-      S.sb_dl.push_back(P.tdim[j]);
-      S.sb_diag_toff.push_back(i == j ? int32_t(P.toff[i]) : -1);
-    }
+  S.sb_hoff.resize(size_t(nsb));
+  S.sb_soff.resize(size_t(nsb));
+  S.sb_dk.resize(size_t(nsb));
+  S.sb_dl.resize(size_t(nsb));
+  S.sb_diag_toff.resize(size_t(nsb));
+  parallel(S.nB_keys, 16, [&](int64_t j0, int64_t j1) {
+    for (int j = int(j0); j < int(j1); ++j)
+      for (int64_t q = S.Spat.colptr[j]; q < S.Spat.colptr[j + 1]; ++q) {
+        const int i = S.Spat.rows[q];
+        const int64_t hb = L.H.Find(i, j);
+        S.sb_hoff[q] = hb >= 0 ? L.H.boff[hb] : -1;
+        S.sb_soff[q] = S.Spat.boff[q];
+        S.sb_dk[q] = P.tdim[i];
+        S.sb_dl[q] = P.tdim[j];
+        S.sb_diag_toff[q] = i == j ? int32_t(P.toff[i]) : -1;
+      }
+  });
   // reduced rhs lists: per B scalar, the points that see its key in point order
   S.r_ptr.assign(S.nB + 1, 0);
   for (int k = 0; k < S.nB_keys; ++k)
@@ -433,16 +548,18 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L) {
   S.r_ecol.resize(nr);
   S.r_dk.resize(nr);
   S.r_pt.resize(nr);
-  for (int k = 0; k < S.nB_keys; ++k)
-    for (int c = 0; c < P.tdim[k]; ++c) {
-      int64_t q = S.r_ptr[P.toff[k] + c];
-      for (int64_t u = kp_ptr[k]; u < kp_ptr[k + 1]; ++u, ++q) {
-        S.r_eoff[q] = kp_eoff[u];
-        S.r_ecol[q] = c;
-        S.r_dk[q] = P.tdim[k];
-        S.r_pt[q] = kp[u];
+  parallel(S.nB_keys, 16, [&](int64_t k0, int64_t k1) {
+    for (int k = int(k0); k < int(k1); ++k)
+      for (int c = 0; c < P.tdim[k]; ++c) {
+        int64_t q = S.r_ptr[P.toff[k] + c];
+        for (int64_t u = kp_ptr[k]; u < kp_ptr[k + 1]; ++u, ++q) {
+          S.r_eoff[q] = kp_eoff[u];
+          S.r_ecol[q] = c;
+          S.r_dk[q] = P.tdim[k];
+          S.r_pt[q] = kp[u];
+        }
       }
-    }
+  });
   return S;
 }
 

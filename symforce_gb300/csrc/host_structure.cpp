@@ -111,10 +111,18 @@ BlockPattern MakePattern(const std::vector<int>& dims, std::vector<std::pair<int
   for (int b = 0; b < P.nb; ++b) pairs.push_back({b, b});
   for (auto& pr : pairs)
     if (pr.first < pr.second) std::swap(pr.first, pr.second);
-  // sort by column then row
-  std::sort(pairs.begin(), pairs.end(), [](const auto& a, const auto& b) {
-    return a.second != b.second ? a.second < b.second : a.first < b.first;
-  });
+  // sort by column then row: a counting sort by row, then a stable one by column
+  {
+    std::vector<std::pair<int, int>> tmp(pairs.size());
+    std::vector<int64_t> cnt(size_t(P.nb) + 1, 0);
+    for (const auto& pr : pairs) cnt[size_t(pr.first) + 1]++;
+    for (int b = 0; b < P.nb; ++b) cnt[b + 1] += cnt[b];
+    for (const auto& pr : pairs) tmp[size_t(cnt[pr.first]++)] = pr;
+    std::fill(cnt.begin(), cnt.end(), 0);
+    for (const auto& pr : tmp) cnt[size_t(pr.second) + 1]++;
+    for (int b = 0; b < P.nb; ++b) cnt[b + 1] += cnt[b];
+    for (const auto& pr : tmp) pairs[size_t(cnt[pr.second]++)] = pr;
+  }
   pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
   P.colptr.assign(P.nb + 1, 0);
   P.rows.resize(pairs.size());

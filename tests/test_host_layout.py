@@ -38,7 +38,7 @@ def shim(tmp_path_factory):
     out = tmp_path_factory.mktemp("shim") / "libhostshim.so"
     srcs = [ROOT / "tests" / "host_layout_shim.cpp"] + [CSRC / f for f in
                                                         ("host_structure.cpp", "host_layout.cpp", "host_pcg.cpp")]
-    subprocess.run([gxx, "-O1", "-std=c++17", "-shared", "-fPIC", f"-I{cuda_inc}", f"-I{ROOT / 'include'}",
+    subprocess.run([gxx, "-O1", "-std=c++17", "-shared", "-fPIC", "-pthread", f"-I{cuda_inc}", f"-I{ROOT / 'include'}",
                     f"-I{CSRC}", *map(str, srcs), "-o", str(out)], check=True)
     lib = C.CDLL(str(out))
     lib.shim_build.argtypes = [C.POINTER(A.ProblemC)]
