@@ -168,7 +168,9 @@ struct TaskPlan {
   std::vector<int64_t> asm_col_off;   // per (front, tile column)
   std::vector<int32_t> asm_col_list;
 };
-TaskPlan PlanTasks(const Symbolic& sym, int tile, bool separate_inverse);
+// separate_inverse: FP64 chains leave the diagonal tiles' inverses to kTaskInverse tasks;
+// tc_updates: runs of trailing updates go to tensor-core tasks (FP32 tiles of 32).
+TaskPlan PlanTasks(const Symbolic& sym, int tile, bool separate_inverse, bool tc_updates);
 
 // Flattened per-(front, tile column) assembly lists, extend-add rounds and solve maps of a
 // symbolic factorization and its task plan, as the device kernels read them.

@@ -51,6 +51,8 @@ struct PcgState {
 // look-ahead step k = 0 .. np - 2 in turn, the factor of tile (k, k) kept in shared memory.
 // kTaskInverse(k): the inverse of tile (k, k)'s unit lower factor, for the triangular solves (FP64
 // chains leave it out of the chain).
+// kTaskUpdateTc: panel k's update of tiles (i0 .. i0 + cnt - 1, j) on the tensor cores (FP32
+// fronts); z = i0 << 16 | j, w = k | cnt << 20.
 enum TaskType {
   kTaskAssemble = 0,
   kTaskDiag = 1,
@@ -58,7 +60,8 @@ enum TaskType {
   kTaskUpdate = 3,
   kTaskLookahead = 4,
   kTaskChain = 5,
-  kTaskInverse = 6
+  kTaskInverse = 6,
+  kTaskUpdateTc = 7
 };
 
 enum DeviceErrorCode {

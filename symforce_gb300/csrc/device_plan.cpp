@@ -27,8 +27,11 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   fp.sym = Analyze(pat, ordering);
   const Symbolic& S = fp.sym;
   const int tile = elem == 8 ? kFactorTileF64 : kFactorTileF32;
-  // FP64 chains leave the inverses of their diagonal factors to separate tasks
-  fp.plan = PlanTasks(S, tile, elem == 8);
+  // FP64 chains leave the inverses of their diagonal factors to separate tasks; FP32 fronts take
+  // runs of trailing updates on the tensor cores (SFG_FACTOR_TC=0: SIMT tile updates only)
+  bool tc = elem == 4;
+  if (const char* e = std::getenv("SFG_FACTOR_TC")) tc = tc && std::atoi(e) != 0;
+  fp.plan = PlanTasks(S, tile, elem == 8, tc);
   const TaskPlan& T = fp.plan;
   FactorDev& f = fp.f;
   f.ns = S.ns;

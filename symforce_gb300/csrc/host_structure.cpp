@@ -617,7 +617,7 @@ Symbolic Analyze(const BlockPattern& A, int ordering) {
   return S;
 }
 
-TaskPlan PlanTasks(const Symbolic& sym, int tile, bool separate_inverse) {
+TaskPlan PlanTasks(const Symbolic& sym, int tile, bool separate_inverse, bool tc_updates) {
   TaskPlan T;
   T.tile = tile;
   T.tile_base.assign(sym.ns + 1, 0);
@@ -679,7 +679,7 @@ TaskPlan PlanTasks(const Symbolic& sym, int tile, bool separate_inverse) {
   };
   std::vector<Timed> timed;
   // nominal durations (microseconds; only the order matters)
-  constexpr double kAsm = 5, kDiag = 5, kStep = 10, kTrsm = 4, kUpd = 5, kInv = 3;
+  constexpr double kAsm = 5, kDiag = 5, kStep = 10, kTrsm = 4, kUpd = 5, kInv = 3, kUpdTc = 6;
   std::vector<double> front_done(sym.ns, 0.0);
   for (int s = 0; s < sym.ns; ++s) {
     const int nt = T.ntiles[s], np = T.npiv[s];
@@ -714,11 +714,43 @@ TaskPlan PlanTasks(const Symbolic& sym, int tile, bool separate_inverse) {
       }
       for (int i = k + (ahead ? 2 : 1); i < nt; ++i)
         Fn(i, k) = add(std::max(Fn(k, k), V(i, k)), kTrsm, make_int4(kTaskTrsm, s, i * 65536 + k, k));
-      for (int j = k + 1; j < nt; ++j)
-        for (int i = j; i < nt; ++i) {
-          if (ahead && i == k + 1 && j == k + 1) continue;  // chain step k
+      for (int j = k + 1; j < nt; ++j) {
+        // rows of tile column j that take panel k's update here (tile (k+1, k+1) is the chain's)
+        std::vector<int> rows;
+        for (int i = j; i < nt; ++i)
+          if (!(ahead && i == k + 1 && j == k + 1)) rows.push_back(i);
+        auto single = [&](int i) {
           V(i, j) = add(std::max({Fn(i, k), Fn(j, k), V(i, j)}), kUpd, make_int4(kTaskUpdate, s, i * 65536 + j, k));
+        };
+        if (!tc_updates) {
+          for (int i : rows) single(i);
+          continue;
         }
+        // Tensor-core tasks take runs of up to four consecutive rows.  The tiles chain step k + 1
+        // waits on, (k+2, k+1) and (k+2, k+2), stay single tasks that wait for nothing else.
+        const bool chain_next = k + 2 < np;
+        size_t q = 0;
+        while (q < rows.size()) {
+          const int i0 = rows[q];
+          if (chain_next && i0 == k + 2 && (j == k + 1 || j == k + 2)) {
+            single(i0);
+            ++q;
+            continue;
+          }
+          int cnt = 1;
+          while (cnt < 4 && q + cnt < rows.size() && rows[q + cnt] == i0 + cnt) ++cnt;
+          if (cnt == 1) {
+            single(i0);
+            ++q;
+            continue;
+          }
+          double st = std::max(Fn(j, k), 0.0);
+          for (int r = 0; r < cnt; ++r) st = std::max({st, Fn(i0 + r, k), V(i0 + r, j)});
+          const double e = add(st, kUpdTc, make_int4(kTaskUpdateTc, s, i0 * 65536 + j, k | (cnt << 20)));
+          for (int r = 0; r < cnt; ++r) V(i0 + r, j) = e;
+          q += size_t(cnt);
+        }
+      }
     }
     // the inverses of the chain's diagonal factors, for the triangular solves only
     if (separate_inverse && np > 1)

@@ -17,6 +17,7 @@
 #include <algorithm>
 
 #include "kernels.h"
+#include "tc_common.cuh"
 
 namespace sfg {
 
@@ -1116,14 +1117,161 @@ __device__ void TaskUpdate(const FactorDev& f, int s, int i, int j, int k, T* F,
   Signal(f.tile_state + StateIdx(g, i, j), 2 + k);
 }
 
+// ---- Tensor-core trailing updates (FP32 fronts).  A column of up to four row tiles i0 ..
+// i0 + cnt - 1 takes panel k's update as one product: C -= (L_ik D_k) L_jk^T, M = 128 rows (the
+// four tiles), N = 32 (tile column j), K = the panel's width, on the tcgen05 tensor cores in
+// kind::tf32 with the three-pass split x = hi + lo (A_hi B_hi + A_hi B_lo + A_lo B_hi, FP32-level
+// accuracy), the accumulator in the CTA's 32 TMEM columns.  The operands are staged by the threads
+// in the canonical K-major layout (no swizzle) in the CTA's shared tile storage; thread 0 issues the
+// twelve MMAs and commits them to an mbarrier; warp w reads TMEM lanes 32 w .. 32 w + 31 (tile
+// i0 + w) and subtracts them from the front.  The target and L_ik are waited for and staged before
+// the usually later panel tile L_jk.
+constexpr int kTcUpdRows = tc::kTcRows;                         // 4 tiles of 32
+constexpr size_t kTcUpdBytes = size_t(kTcUpdRows) * 32 * 4 * 2  // A hi / lo
+                               + size_t(32) * 32 * 4 * 2;       // B hi / lo
+constexpr int kTcUpdCols = 32;                                  // TMEM columns per CTA
+
+template <typename T, int TILE>
+__device__ void TaskUpdateTc(const FactorDev& f, int s, int i0, int cnt, int j, int k, T* F, unsigned char* smem,
+                             uint32_t tmem, uint64_t* bar, uint32_t& phase, int* s_flag,
+                             unsigned long long* ready) {
+  static_assert(TILE == 32 && sizeof(T) == 4, "tensor-core updates are for FP32 tiles of 32");
+  using namespace tc;
+  const Geom g = FrontGeom(f, s);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  bool ok = true;
+  if (tid == 0)
+    for (int q = 0; q < cnt && ok; ++q)
+      ok = WaitAtLeast(f.tile_state + StateIdx(g, i0 + q, k), kFinal, f.error) &&
+           WaitAtLeast(f.tile_state + StateIdx(g, i0 + q, j), 1 + k, f.error);
+  if (!CtaWait(ok, s_flag, ready)) return;
+  const int bk = TileSize(g, k, TILE), ck = TileStart(g, k, TILE);
+  const int bj = TileSize(g, j, TILE), rj = TileStart(g, j, TILE);
+  T* Fs = F + g.foff;
+  unsigned char* a_hi = smem;
+  unsigned char* a_lo = a_hi + kTcUpdRows * 32 * 4;
+  unsigned char* b_hi = a_lo + kTcUpdRows * 32 * 4;
+  unsigned char* b_lo = b_hi + 32 * 32 * 4;
+  // A row tid: row tid % 32 of tile i0 + warp, times D_k (lane q of the warp holds d_q)
+  {
+    const int it = i0 + warp;
+    const bool in_tile = warp < cnt && lane < TileSize(g, it < g.nt ? it : 0, TILE);
+    const float dq = lane < bk ? Ld(Fs + int64_t(ck + lane) * (g.m + 1)) : 0.f;
+    const T* arow = Fs + (in_tile ? TileStart(g, it, TILE) + lane : 0) + int64_t(ck) * g.m;
+#pragma unroll
+    for (int q4 = 0; q4 < 32; q4 += 4) {
+      float v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float d = __shfl_sync(0xffffffffu, dq, q4 + u);
+        v[u] = (in_tile && q4 + u < bk) ? Ld(arow + int64_t(q4 + u) * g.m) * d : 0.f;
+      }
+      float4 hi4, lo4;
+      hi4.x = TfHi(v[0]);
+      hi4.y = TfHi(v[1]);
+      hi4.z = TfHi(v[2]);
+      hi4.w = TfHi(v[3]);
+      lo4.x = v[0] - hi4.x;
+      lo4.y = v[1] - hi4.y;
+      lo4.z = v[2] - hi4.z;
+      lo4.w = v[3] - hi4.w;
+      const uint32_t o = ChunkOffset(tid, q4);
+      *reinterpret_cast<float4*>(a_hi + o) = hi4;
+      *reinterpret_cast<float4*>(a_lo + o) = lo4;
+    }
+  }
+  if (tid == 0) ok = WaitAtLeast(f.tile_state + StateIdx(g, j, k), kFinal, f.error);
+  if (!CtaWait(ok, s_flag)) return;
+  // B row n = row n of L_jk (the product's column n), K along the row; thread: row tid / 4, 8 k
+  {
+    const int n = tid >> 2, qb = (tid & 3) * 8;
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      v[u] = (n < bj && qb + u < bk) ? Ld(Fs + (rj + n) + int64_t(ck + qb + u) * g.m) : 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      float4 hi4, lo4;
+      hi4.x = TfHi(v[4 * h]);
+      hi4.y = TfHi(v[4 * h + 1]);
+      hi4.z = TfHi(v[4 * h + 2]);
+      hi4.w = TfHi(v[4 * h + 3]);
+      lo4.x = v[4 * h] - hi4.x;
+      lo4.y = v[4 * h + 1] - hi4.y;
+      lo4.z = v[4 * h + 2] - hi4.z;
+      lo4.w = v[4 * h + 3] - hi4.w;
+      const uint32_t o = ChunkOffset(n, qb + 4 * h);
+      *reinterpret_cast<float4*>(b_hi + o) = hi4;
+      *reinterpret_cast<float4*>(b_lo + o) = lo4;
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  if (tid == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t idesc = InstrDesc(32);
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {  // K = 8 per MMA: two core matrices along K
+      const uint32_t off = uint32_t(kk * 256);
+      MmaTf32(tmem, SmemDesc(SmemAddr(a_hi) + off), SmemDesc(SmemAddr(b_hi) + off), idesc, kk > 0 ? 1u : 0u);
+      MmaTf32(tmem, SmemDesc(SmemAddr(a_hi) + off), SmemDesc(SmemAddr(b_lo) + off), idesc, 1u);
+      MmaTf32(tmem, SmemDesc(SmemAddr(a_lo) + off), SmemDesc(SmemAddr(b_hi) + off), idesc, 1u);
+    }
+    MmaCommit(bar);
+  }
+  const bool done = __all_sync(0xffffffffu, MbarWait(bar, phase));  // warp-uniform for tcgen05.ld
+  if (!done) {
+    if (lane == 0) atomicExch(f.error, kDevSpinTimeout);
+    (void)MbarWait(bar, phase);  // a second (capped) chance before the storage is reused
+  }
+  phase ^= 1u;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (done && warp < cnt) {
+    const int it = i0 + warp, ri = TileStart(g, it, TILE), bi = TileSize(g, it, TILE);
+#pragma unroll
+    for (int c0 = 0; c0 < 32; c0 += 16) {
+      uint32_t v[16];
+      TmemLoad16(tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0), v);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int c = c0 + u;
+        if (lane < bi && c < bj && (it != j || lane >= c)) {
+          T* dst = Fs + (ri + lane) + int64_t(rj + c) * g.m;
+          St(dst, Ld(dst) - __uint_as_float(v[u]));
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    for (int q = 0; q < cnt; ++q) atomicExch(f.tile_state + StateIdx(g, i0 + q, j), 2 + k);
+  }
+}
+
 template <typename T, int TILE>
 __global__ void __launch_bounds__(kFactorThreads, kFactorCtasPerSm) FactorKernel(FactorDev f, const T* A,
                                                                const double* damping, T* F,
                                                                T* Linv) {
-  __shared__ TileSmem<T, TILE> sm;
+  // the tile storage; FP32 kernels also stage tensor-core update operands in it (one task at a time)
+  constexpr bool kTc = sizeof(T) == 4;
+  constexpr size_t kSmemBytes = (kTc && kTcUpdBytes > sizeof(TileSmem<T, TILE>)) ? kTcUpdBytes : sizeof(TileSmem<T, TILE>);
+  __shared__ __align__(1024) unsigned char smem_raw[kSmemBytes];
+  TileSmem<T, TILE>& sm = *reinterpret_cast<TileSmem<T, TILE>*>(smem_raw);
   __shared__ int s_task, s_next, s_ok, s_flag;
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_tmem;
   if (f.gate && *f.gate == 0) return;
   A += int64_t(f.st->init_idx) * f.a_stride;
+  uint32_t phase = 0;
+  if constexpr (kTc) {
+    if ((threadIdx.x >> 5) == 0) tc::TmemAlloc(&s_tmem, kTcUpdCols);
+    if (threadIdx.x == 0) tc::MbarInit(&s_bar);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
   // A chain task runs on an SM of its own where it can (its FP64 work otherwise queues behind the
   // co-resident CTAs' updates on the SM's shared FP64 pipe): its CTA flags the SM, and the SM's
   // other CTAs leave the kernel after their claimed tasks.  At most f.iso_limit SMs are flagged,
@@ -1155,9 +1303,9 @@ __global__ void __launch_bounds__(kFactorThreads, kFactorCtasPerSm) FactorKernel
     }
     __syncthreads();
     const int t = s_task;
-    if (t >= f.ntasks) return;
+    if (t >= f.ntasks) break;
     const int4 task = f.tasks[t];
-    const int i = task.z >> 16, j = task.z & 0xffff, k = task.w;
+    const int i = task.z >> 16, j = task.z & 0xffff, k = task.w & 0xfffff;
     unsigned long long* ready = f.trace ? f.trace + 8 * int64_t(t) + 1 : nullptr;
     if (f.trace && threadIdx.x == 0) {
       f.trace[8 * int64_t(t)] = Clock64Global();
@@ -1170,6 +1318,13 @@ __global__ void __launch_bounds__(kFactorThreads, kFactorCtasPerSm) FactorKernel
       case kTaskUpdate: TaskUpdate<T, TILE>(f, task.y, i, j, k, F, sm, &s_flag, ready); break;
       case kTaskChain: TaskChain<T, TILE>(f, task.y, F, Linv, sm, &s_flag, ready); break;
       case kTaskInverse: TaskInverse<T, TILE>(f, task.y, k, F, Linv, sm, &s_flag, ready); break;
+      case kTaskUpdateTc:
+        if constexpr (kTc) {
+          TaskUpdateTc<T, TILE>(f, task.y, i, task.w >> 20, j, task.w & 0xfffff, F, smem_raw, s_tmem, &s_bar,
+                                phase, &s_flag, ready);
+          break;
+        }
+        [[fallthrough]];
       default:
         if (threadIdx.x == 0) atomicExch(f.error, kDevBadTask);
     }
@@ -1179,6 +1334,11 @@ __global__ void __launch_bounds__(kFactorThreads, kFactorCtasPerSm) FactorKernel
       // after a chain, or on an SM given to a chain (this CTA then leaves)
       s_next = (s_chain_cta || !sm_flag || LoadVolatile(sm_flag) == 0) ? atomicAdd(f.counters, 1) : f.ntasks;
     }
+  }
+  if constexpr (kTc) {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) tc::TmemFree(s_tmem, kTcUpdCols);
   }
 }
 
@@ -1639,6 +1799,9 @@ template <typename T>
 void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F, void* Linv,
                   int grid, cudaStream_t s) {
   constexpr int kTile = sizeof(T) == 8 ? kFactorTileF64 : kFactorTileF32;
+  static const cudaError_t carveout = cudaFuncSetAttribute(
+      FactorKernel<T, kTile>, cudaFuncAttributePreferredSharedMemoryCarveout, int(cudaSharedmemCarveoutMaxShared));
+  (void)carveout;
   FactorKernel<T, kTile><<<grid, kFactorThreads, 0, s>>>(f, static_cast<const T*>(A), damping,
                                                          static_cast<T*>(F), static_cast<T*>(Linv));
 }

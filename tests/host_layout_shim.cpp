@@ -137,7 +137,7 @@ void shim_schur_i32(int which, int32_t* out) {
 int shim_build_factor_plan(int which, int tile) {
   try {
     g_sym = sfg::Analyze(which == 0 ? g_layout.H : g_schur.Spat, SFG_ORDERING_NESTED_DISSECTION);
-    g_plan = sfg::PlanTasks(g_sym, tile, tile == 16);  // FP64 tiles are 16 wide
+    g_plan = sfg::PlanTasks(g_sym, tile, tile == 16, tile == 32);  // FP64 tiles 16 wide, FP32 32
     g_maps = sfg::BuildFactorMaps(g_sym, g_plan, which == 0 ? g_layout.H : g_schur.Spat);
     return 0;
   } catch (...) {

@@ -246,7 +246,7 @@ def test_schur_plan_matches_dense_schur_complement(shim):
 
 
 # tile task types of the persistent factorization (device.cuh TaskType)
-ASSEMBLE, DIAG, TRSM, UPDATE, LOOKAHEAD, CHAIN, INVERSE = 0, 1, 2, 3, 4, 5, 6
+ASSEMBLE, DIAG, TRSM, UPDATE, LOOKAHEAD, CHAIN, INVERSE, UPDATE_TC = 0, 1, 2, 3, 4, 5, 6, 7
 FINAL = 1 << 30
 
 
@@ -303,9 +303,10 @@ def _replay_tasks(tasks, npiv, ntiles, parent, w, m, cptr, clist, tile):
                     del chains[s]
                     break
 
-    for ty, s, z, k in tasks:
+    for ty, s, z, kw in tasks:
         advance_chains()
         i, j = int(z) >> 16, int(z) & 0xFFFF
+        k, cnt = int(kw) & 0xFFFFF, int(kw) >> 20
         st = state[s]
         if ty == CHAIN:
             assert int(npiv[s]) > 1 and s not in chains
@@ -339,6 +340,13 @@ def _replay_tasks(tasks, npiv, ntiles, parent, w, m, cptr, clist, tile):
             need(s, j, k, FINAL, "update")
             need(s, i, j, 1 + k, "update")
             st[i, j] = 2 + k
+        elif ty == UPDATE_TC:
+            assert 2 <= cnt <= 4
+            need(s, j, k, FINAL, "tensor-core update")
+            for r in range(i, i + cnt):
+                need(s, r, k, FINAL, "tensor-core update")
+                need(s, r, j, 1 + k, "tensor-core update")
+                st[r, j] = 2 + k
         else:
             raise AssertionError(f"unknown task type {ty}")
     advance_chains()
