@@ -596,6 +596,15 @@ def run_profile(args) -> None:
     if args.profile_iterations > 0:
         params.iterations = args.profile_iterations
     opt = Optimizer(p, _form_params(params, args.profile_form), _make_form(w, args.profile_form, 0))
+    if args.profile_fronts:
+        width, size = opt.fronts()
+        edges = [0, 16, 64, 128, 256, 512, 1024, 2048, 4096, 1 << 30]
+        hist = np.histogram(size, bins=edges)[0]
+        madd = sum(int(m) ** 3 - (int(m) - int(wd)) ** 3 for wd, m in zip(width, size)) / 6
+        print(f"{args.profile_workload} {args.profile_form}: {len(size)} fronts, size max {size.max()}, median "
+              f"{int(np.median(size))}, pivot columns {int(width.sum())}; sizes: "
+              + ", ".join(f"[{edges[q]}, {edges[q + 1]}): {int(h)}" for q, h in enumerate(hist) if h)
+              + f"; dense LDL^T multiply-adds ~{madd / 1e6:.1f} M", flush=True)
     for _ in range(args.profile_runs):
         _, stats = opt.optimize(p.values)
         print(f"{args.profile_workload} {args.profile_form}: {len(stats.iterations)} records, best "
@@ -621,6 +630,8 @@ def main() -> None:
     ap.add_argument("--profile-runs", type=int, default=2)
     ap.add_argument("--profile-iterations", type=int, default=-1,
                     help="LM iteration cap in profiling mode (default: the workload's)")
+    ap.add_argument("--profile-fronts", action="store_true",
+                    help="profiling mode: print the sizes of the factorization's fronts")
     args = ap.parse_args()
     if args.profile_workload:
         run_profile(args)

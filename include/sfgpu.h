@@ -278,6 +278,10 @@ int32_t sfg_factor_lower(sfg_handle* h, int64_t* nnz, int32_t* col_ptr, int32_t*
                          double* values);
 /* The block ordering used by the linear solver, as new position of every state scalar. */
 int32_t sfg_permutation(sfg_handle* h, int32_t* perm, int64_t n);
+/* The fronts (supernodes) of the handle's exact factorization, in postorder: the pivot width and
+ * the front size of each.  *count in: the capacity of width / size (0: query); out: the number of
+ * fronts. */
+int32_t sfg_fronts(sfg_handle* h, int32_t* count, int32_t* width, int32_t* size);
 /* Time `reps` back-to-back launches of one stage of the iteration on the handle's stream with CUDA
  * events (after one warm-up launch) at the current values: SFG_STAGE_LINEARIZE (all factor
  * batches + staged reduction + cost), SFG_STAGE_SCHUR (point inverses, reduced system and rhs),

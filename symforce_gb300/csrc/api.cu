@@ -920,6 +920,21 @@ int32_t sfg_permutation(sfg_handle* h, int32_t* perm, int64_t n) {
   });
 }
 
+int32_t sfg_fronts(sfg_handle* h, int32_t* count, int32_t* width, int32_t* size) {
+  return Guard([&] {
+    if (!h || !count) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
+    const sfg::Symbolic& S = h->fp.sym;
+    const int32_t cap = *count;
+    *count = S.ns;
+    if (cap == 0) return;
+    if (cap < S.ns || !width || !size) throw Error(SFG_ERR_INVALID_ARGUMENT, "capacity too small");
+    for (int q = 0; q < S.ns; ++q) {
+      width[q] = S.sn_w[q];
+      size[q] = S.sn_m[q];
+    }
+  });
+}
+
 int32_t sfg_time_stage(sfg_handle* h, int32_t stage, int32_t reps, double* ms_per_launch,
                        double* algorithmic_bytes, double* fmas) {
   return Guard([&] {

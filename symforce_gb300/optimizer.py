@@ -49,6 +49,7 @@ def lib() -> C.CDLL:
         L.sfg_hessian_lower.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                         C.POINTER(C.c_int32), C.POINTER(C.c_double)]
         L.sfg_permutation.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.c_int64]
+        L.sfg_fronts.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.sfg_time_stage.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.sfg_storage_dim.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
@@ -333,6 +334,15 @@ class Optimizer:
         perm = np.zeros(size, dtype=np.int32)
         _check(lib().sfg_permutation(self._h, A.iptr(perm), size))
         return perm
+
+    def fronts(self) -> tuple[np.ndarray, np.ndarray]:
+        """Pivot widths and sizes of the exact factorization's fronts (supernodes), postorder."""
+        count = C.c_int32(0)
+        _check(lib().sfg_fronts(self._h, C.byref(count), None, None))
+        width = np.zeros(count.value, dtype=np.int32)
+        size = np.zeros(count.value, dtype=np.int32)
+        _check(lib().sfg_fronts(self._h, C.byref(count), A.iptr(width), A.iptr(size)))
+        return width, size
 
 
 class GncOptimizer:
