@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define SFG_ABI_VERSION 2
+#define SFG_ABI_VERSION 3
 
 /* ---------------------------------------------------------------------------------------------
  * Status codes.  Solver outcomes (SUCCESS / HIT_ITERATION_LIMIT / FAILED) are not errors: they are
@@ -219,6 +219,12 @@ typedef struct sfg_form_params_t {
   int32_t refine_steps;   /* MIXED: FP64 iterative-refinement steps per linear solve (default 1) */
   int32_t pcg_max_iters;  /* PCG forms: iteration cap of one reduced-system solve (default 500) */
   double pcg_tol;         /* PCG forms: FP64 relative residual target (default 1e-8) */
+  int32_t pcg_coarse;     /* PCG forms: 1 adds to the camera-block preconditioner a coarse
+                             correction on the 7 similarity-gauge directions of the camera poses
+                             (POSE3 keys: world translation, rotation, scale), the near-null space
+                             of a bundle-adjustment reduced system, while those directions stay
+                             near-null under the damping; 0 (default): blocks only */
+  int32_t reserved;       /* 0 */
 } sfg_form_params_t;
 
 typedef struct sfg_handle sfg_handle;

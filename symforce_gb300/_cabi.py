@@ -195,6 +195,8 @@ class FormParams(C.Structure):
         ("refine_steps", C.c_int32),
         ("pcg_max_iters", C.c_int32),
         ("pcg_tol", C.c_double),
+        ("pcg_coarse", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -234,6 +236,7 @@ def default_form_params(**overrides) -> FormParams:
         refine_steps=1,
         pcg_max_iters=500,
         pcg_tol=1e-8,
+        pcg_coarse=0,
     )
     for k, v in overrides.items():
         setattr(f, k, v)

@@ -186,6 +186,7 @@ void EnqueuePrecond(sfg_handle* h, cudaStream_t s) {
 template <typename T>
 void EnqueuePcgSolve(sfg_handle* h, cudaStream_t s, bool gated) {
   EnqueuePrecond<T>(h, s);
+  if (h->pcg.coarse) LaunchGaugeBasis<T>(h->pcg, h->values, h->P.S, h->st, s);
   SFG_CUDA(LaunchPcg<T>(h->pcg, h->pcg_grid, h->pcg_threads, s));
   const int* gate = gated ? &h->ps->need_fallback : nullptr;
   EnqueueFactor<T>(h->fp, h->S, nullptr, s, gate);
@@ -537,7 +538,16 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
         c.staged = int(smem);
       }
     }
-    c.partials = A.Zeros<double>(4 * size_t(h->pcg_grid));
+    c.partials = A.Zeros<double>(2 * size_t(kPcgReduceMax) * size_t(h->pcg_grid));
+    // the gauge coarse correction needs at least two cameras' poses (otherwise Z^T S Z is singular)
+    c.coarse = (fm.pcg_coarse != 0 && PL.gauge_rows >= 12) ? 1 : 0;
+    if (c.coarse) {
+      const size_t rows = size_t(std::max(h->pd.ng, 1)) * kPrecondBlock;
+      c.zg = A.Zeros<char>(size_t(kGaugeDim) * rows * E);
+      c.szg = A.Zeros<char>(size_t(kGaugeDim) * rows * E);
+      c.gauge_soff = A.Upload(PL.gauge_soff);
+      c.gauge_comp = A.Upload(PL.gauge_comp);
+    }
     c.bar = A.Zeros<unsigned>(2);
     c.ps = h->ps;
     c.err = err_word;
@@ -566,7 +576,7 @@ int BodyKernels(const sfg_handle* h) {
   if (h->elem == 4) n += 1 + 4 * h->refine_steps;  // widen; residual, reset, solve, accumulate
   if (h->pcg_mode) {
     n += 1 /*group blocks*/ + 2 /*row coupling, features*/ + (h->pcg_mode == 2 ? 1 : 0) +
-         1 /*assemble*/ + 1 /*PCG*/;
+         1 /*assemble*/ + 1 /*PCG*/ + (h->pcg.coarse ? 1 : 0) /*gauge basis*/;
     if (h->elem == 8) n += 1;  // widen of the fallback solution
   }
   if (h->collect_cap > 0) n += (h->pcg_mode ? 0 : 2) + 1;
@@ -628,6 +638,7 @@ void sfg_default_form_params(sfg_form_params_t* o) {
   o->refine_steps = 1;
   o->pcg_max_iters = 500;
   o->pcg_tol = 1e-8;
+  o->pcg_coarse = 0;
 }
 
 int32_t sfg_key_dims(int32_t key_type, int32_t* storage_dim, int32_t* tangent_dim) {
@@ -1097,6 +1108,7 @@ void StepError(sfg_handle* h, double* rel_step_error, int32_t* iterations, doubl
   LaunchSchurBuildS<T>(h->sd, h->hess, h->L.nvals, h->damp.damping, h->W, h->S, h->st, s);
   LaunchSchurRhs<T>(h->sd, h->hess, h->L.nvals, h->rhs, N, h->tp, h->v, h->st, s);
   EnqueuePrecond<T>(h, s);
+  if (h->pcg.coarse) LaunchGaugeBasis<T>(h->pcg, h->values, h->P.S, h->st, s);
   SFG_CUDA(LaunchPcg<T>(h->pcg, h->pcg_grid, h->pcg_threads, s));
   std::vector<double> ypcg(nB), yex(nB);
   SFG_CUDA(cudaMemcpyAsync(ypcg.data(), h->ydbl, nB * 8, cudaMemcpyDeviceToHost, s));

@@ -53,6 +53,8 @@ PrecondLayout BuildPrecondLayout(const HostProblem& P, const SchurLayout& SL) {
   L.degree.assign(L.ng, 0.f);
   L.scalar_group.assign(SL.nB, -1);
   L.sdiag_off.assign(SL.nB, -1);
+  L.gauge_soff.assign(size_t(L.ng) * kB, -1);
+  L.gauge_comp.assign(size_t(L.ng) * kB, 0);
   const BlockPattern& S = SL.Spat;
   // the reduced system keeps only the lower triangle of its diagonal key blocks up to date
   auto entry_offset = [&](int ka, int ta, int kb, int tb) -> int64_t {
@@ -76,6 +78,11 @@ PrecondLayout BuildPrecondLayout(const HostProblem& P, const SchurLayout& SL) {
       const int64_t s = S.off[dims[a].first] + dims[a].second;
       L.gidx[size_t(g) * kB + a] = int32_t(s);
       L.scalar_group[s] = g;
+      if (P.key_type[dims[a].first] == SFG_KEY_POSE3) {
+        L.gauge_soff[size_t(g) * kB + a] = P.soff[dims[a].first];
+        L.gauge_comp[size_t(g) * kB + a] = dims[a].second;
+        ++L.gauge_rows;
+      }
       for (size_t b = 0; b < dims.size(); ++b) {
         const int64_t o = entry_offset(dims[a].first, dims[a].second, dims[b].first, dims[b].second);
         L.goff[(size_t(g) * kB + a) * kB + b] = o < 0 ? -2 : o;  // -2: structurally zero

@@ -284,10 +284,23 @@ struct PcgDev {
   double inner_floor;       // smallest relative reduction asked of one inner solve
   int max_iters, max_outer;
   int split;                // lanes per row of a multi-CTA launch (1 or 3)
+  // coarse correction on the camera poses' similarity gauge (coarse != 0): basis Z and S Z by
+  // group row, column-major T [7][ng * 9] (Z from the current values, S Z by the PCG launch)
+  int coarse;
+  void* zg;
+  void* szg;
+  const int64_t* gauge_soff;  // [ng * 9] POSE3 storage offset of a pose row, -1 otherwise
+  const int32_t* gauge_comp;  // [ng * 9] tangent component of a pose row
 };
+constexpr int kGaugeDim = 7;      // world translation 3, rotation 3, scale 1
+constexpr int kPcgReduceMax = 32; // values one PCG grid reduction can carry
 // Gather the 9 x 9 group blocks of S: Sb[q][e] = S[off[q][e]] (0 where off < 0).
 template <typename T>
 void LaunchGroupBlocks(const int64_t* off, int64_t n, const void* S, void* Sb, cudaStream_t s);
+// The similarity-gauge basis Z (T [7][ng * 9]) of the camera poses at the state block init_idx of
+// `values` (storage size `S` per block).
+template <typename T>
+void LaunchGaugeBasis(const PcgDev& d, const double* values, int64_t S, const LmState* st, cudaStream_t s);
 // Shared memory of a staged (one CTA) PCG launch; 0 if the blocks do not fit.
 template <typename T>
 size_t PcgStagedSmem(int ng, int nbl, int nent);

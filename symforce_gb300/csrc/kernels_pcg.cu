@@ -32,6 +32,10 @@ constexpr int kB = kPrecondBlock;
 constexpr unsigned kSpinLimit = 1u << 22;
 constexpr float kDiagShift = 0.54132485f;  // ln(e - 1): softplus(kDiagShift) = 1
 constexpr int kPcgMultiThreads = 256;
+// gauge coarse correction: kept while tr(Z^T S Z) / tr(Z^T S_blocks Z) is at most this (a CPU study
+// of 30- and 100-camera problems: at 4e-4 the correction saved 25-45 % of the iterations, at 3e-2
+// 7-18 %, at 0.8 it cost 30 %)
+constexpr double kCoarseMaxRatio = 0.05;
 constexpr size_t kPcgStagedMax = 200 * 1024;  // shared memory of a staged one-CTA solve
 
 __device__ __forceinline__ float Softplus(float x) { return x > 20.f ? x : log1pf(expf(x)); }
@@ -304,6 +308,25 @@ __device__ __forceinline__ Acc GroupRow(const T* Sb, const int2* gent, int e0, i
   return acc;
 }
 
+// Row a of group row g of the diagonal block S_gg times x (the entry of the row's list whose
+// neighbour is g itself); entries e0, e0 + stride, ... as GroupRow.
+template <bool kStaged, typename T, typename V>
+__device__ __forceinline__ T DiagBlockRow(const T* Sb, const int2* gent, int e0, int e1, int stride, int a,
+                                          const V* x, int g) {
+  T acc = T(0);
+  for (int e = e0; e < e1; e += stride) {
+    const int2 en = gent[e];
+    if ((en.y >> 1) != g) continue;
+    const int tr = en.y & 1;
+    const T* row = Sb + size_t(en.x) * (kB * kB) + (tr ? a : a * kB);
+    const int step = tr ? kB : 1;
+    const V* xh = x + size_t(g) * kB;
+#pragma unroll
+    for (int b = 0; b < kB; ++b) acc += row[b * step] * T(LdX<kStaged>(xh + b));
+  }
+  return acc;
+}
+
 // Sum of a row's partial products over the SPLIT lanes that share the row (lanes a, a + 9, a + 18),
 // added in the same order in every one of them, so all hold the same bits.
 template <int SPLIT, typename V>
@@ -324,6 +347,11 @@ struct PcgShared {
   double rz, alpha, beta;
   int iters, stop, broke, converged;
   unsigned epoch;  // grid barriers passed (thread 0 only)
+  double E[kGaugeDim * kGaugeDim];  // coarse correction: (Z^T S Z)^-1
+  double cg[kGaugeDim];             // coarse correction of the current residual: E Z^T r
+  double sums[32];                  // results of GridReduceN
+  double trs, trd;                  // tr(Z^T S Z), tr(Z^T S_blocks Z)
+  double zsz[kGaugeDim * (kGaugeDim + 1) / 2];  // Z^T S Z, packed lower
 };
 
 // Sum (a, b) over the grid: a warp tree in Acc, the CTA's warps in order (warp 0, Acc), and the CTAs
@@ -389,17 +417,115 @@ __device__ __forceinline__ void GridReduce(Acc a, Acc b, const PcgDev& d, int& s
   ++seq;
 }
 
+// Sum of N values (N <= kPcgReduceMax) over the grid in FP64, in the fixed orders of GridReduce
+// (warp trees, the CTA's warps in order, the CTAs in order); thread 0 of every CTA then runs
+// epi(sums), whose shared-memory writes are visible to all threads on return.  red: shared scratch
+// of 32 x N doubles.
+template <int N, typename Epi>
+__device__ __forceinline__ void GridReduceN(double (&v)[N], const PcgDev& d, int& seq, PcgShared& sm,
+                                            double* red, Epi epi) {
+  static_assert(N <= kPcgReduceMax && N <= 32, "partials hold kPcgReduceMax values per CTA");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int grid = gridDim.x;
+#pragma unroll
+  for (int n = 0; n < N; ++n)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[n] += __shfl_down_sync(0xffffffffu, v[n], o);
+  __syncthreads();  // every thread has read the previous scalars
+  if (lane == 0)
+#pragma unroll
+    for (int n = 0; n < N; ++n) red[warp * N + n] = v[n];
+  __syncthreads();
+  double* part = d.partials + size_t(seq & 1) * grid * kPcgReduceMax;
+  double* sums = sm.sums;
+  if (warp == 0) {
+    // lane n < N sums value n over the CTA's warps in order
+    if (lane < N) {
+      double t = 0.0;
+      for (int w = 0; w < nwarp; ++w) t += red[w * N + lane];
+      if (grid == 1) sums[lane] = t;
+      else __stcg(part + size_t(blockIdx.x) * kPcgReduceMax + lane, t);
+    }
+    __syncwarp();
+    if (grid == 1 && lane == 0) epi(sums);
+  }
+  if (grid > 1) {
+    GridBarrier(d.bar, grid, sm.epoch, d.err);
+    if (warp == 0) {
+      // lane l takes the CTAs l, l + 32, ... (all N values each, the loads in flight together),
+      // then a warp tree per value: a fixed order, the same bits in every CTA
+      double t[N];
+#pragma unroll
+      for (int n = 0; n < N; ++n) t[n] = 0.0;
+      for (int q = lane; q < grid; q += 32)
+#pragma unroll
+        for (int n = 0; n < N; ++n) t[n] += __ldcg(part + size_t(q) * kPcgReduceMax + n);
+#pragma unroll
+      for (int n = 0; n < N; ++n) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t[n] += __shfl_down_sync(0xffffffffu, t[n], o);
+        if (lane == 0) sums[n] = t[n];
+      }
+      __syncwarp();
+      if (lane == 0) epi(sums);
+    }
+  }
+  __syncthreads();
+  ++seq;
+}
+
+// The gauge coarse correction's 7 x 7 matrix E = (Z^T S Z)^-1 from the packed lower triangle of
+// Z^T S Z (28 values), by an LDL^T and the solve of the seven unit vectors; false when Z^T S Z is
+// not positive definite (then no coarse correction: E = 0).  Thread 0 of each CTA, same bits in all.
+__device__ bool GaugeInverse(const double* g, double* E) {
+  constexpr int K = kGaugeDim;
+  double a[K][K], d[K];
+  for (int i = 0; i < K; ++i)
+    for (int j = 0; j <= i; ++j) a[i][j] = a[j][i] = g[i * (i + 1) / 2 + j];
+  // A = L D L^T (unit L below the diagonal)
+  for (int k = 0; k < K; ++k) {
+    double dk = a[k][k];
+    for (int q = 0; q < k; ++q) dk -= a[k][q] * a[k][q] * d[q];
+    if (!(dk > 1e-300 * (fabs(a[k][k]) + 1e-300)) || !(dk < 1e300)) return false;
+    d[k] = dk;
+    for (int i = k + 1; i < K; ++i) {
+      double v = a[i][k];
+      for (int q = 0; q < k; ++q) v -= a[i][q] * a[k][q] * d[q];
+      a[i][k] = v / dk;
+    }
+  }
+  for (int c = 0; c < K; ++c) {
+    double x[K];
+    for (int i = 0; i < K; ++i) {
+      double v = i == c ? 1.0 : 0.0;
+      for (int q = 0; q < i; ++q) v -= a[i][q] * x[q];
+      x[i] = v;
+    }
+    for (int i = 0; i < K; ++i) x[i] /= d[i];
+    for (int i = K - 1; i >= 0; --i)
+      for (int q = i + 1; q < K; ++q) x[i] -= a[q][i] * x[q];
+    for (int i = 0; i < K; ++i) E[i * K + c] = x[i];
+  }
+  return true;
+}
+
 // Vector arithmetic in the matrix precision T (FP32 in the mixed form); inner products, CG scalars,
 // the residual passes and the stopping decisions in FP64.
 // SPLIT 1: three camera blocks per warp (lanes 9 q + a, row a of block q).  SPLIT 3: one camera
 // block per warp and three lanes per row (lanes 9 q + a for q = 0..2), each taking every third
 // entry of the row's product with S, so a row waits on a third of the L2 round trips; the vectors
 // are kept in all three lanes (same bits) and only lane a reduces and stores.
-template <typename T, bool kStaged, int SPLIT>
+// kCoarse: the preconditioner adds a coarse correction on the camera poses' similarity gauge,
+// M^-1 r = P r + Z E Z^T r with E = (Z^T S Z)^-1 (an additive two-level preconditioner; Z from
+// LaunchGaugeBasis).  S Z is formed once per launch and kept by row, so that the product of a search
+// direction stays one pass over S: S z = S (P r) + (S Z) c, c = E Z^T r, and Z^T r rides in the
+// grid reduction that already follows the update of r.
+template <typename T, bool kStaged, int SPLIT, bool kCoarse>
 __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
   static_assert(SPLIT == 1 || SPLIT == 3, "one or three lanes per row");
   extern __shared__ __align__(16) unsigned char pcg_smem[];
   __shared__ PcgShared sm;
+  __shared__ double redn[kCoarse ? 32 * (2 + kGaugeDim) : 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int slot = lane / kB;  // 0..2; 3: idle lanes 27..31
   const int a = lane - slot * kB;
@@ -461,6 +587,54 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
     sm.converged = sm.vnorm > 0.0 ? 0 : 1;  // zero rhs: y = 0
   });
   const double vnorm = sm.vnorm;
+  const size_t nrows = size_t(ng) * kB;
+  const T* zg = static_cast<const T*>(d.zg);
+  T* szg = static_cast<T*>(d.szg);
+  if constexpr (kCoarse) {
+    // S Z by row (kept for the products), then Z^T S Z over the grid and its inverse
+    // Column j of Z^T S Z (rows i = 0 .. 6; the lower part is kept) per grid reduction, with
+    // z_j^T S_blocks z_j (the camera blocks alone).  The correction is kept only while the gauge
+    // directions are near-null next to what the blocks see, tr(Z^T S Z) <= kCoarseMaxRatio
+    // tr(Z^T S_blocks Z): with large damping they are not, and the correction costs iterations.
+    if (threadIdx.x == 0) {
+      sm.trs = 0.0;
+      sm.trd = 0.0;
+    }
+    for (int j = 0; j < kGaugeDim; ++j) {
+      const T sz = CombineSplit<SPLIT>(
+          in_group ? GroupRow<T, kStaged>(Sb, gent, e0, e1, SPLIT, a, zg + j * nrows) : T(0), a);
+      const T dz = CombineSplit<SPLIT>(
+          in_group ? DiagBlockRow<kStaged>(Sb, gent, e0, e1, SPLIT, a, zg + j * nrows, g) : T(0), a);
+      if (store) szg[j * nrows + gi] = sz;
+      const double zj = row_ok ? double(zg[j * nrows + gi]) : 0.0;
+      double zs[kGaugeDim + 1];
+#pragma unroll
+      for (int i = 0; i < kGaugeDim; ++i) zs[i] = own ? double(row_ok ? zg[i * nrows + gi] : T(0)) * double(sz) : 0.0;
+      zs[kGaugeDim] = own ? zj * double(dz) : 0.0;
+      GridReduceN<kGaugeDim + 1>(zs, d, seq, sm, redn, [&](double* gs) {
+        for (int i = j; i < kGaugeDim; ++i) sm.zsz[i * (i + 1) / 2 + j] = gs[i];
+        sm.trs += gs[j];
+        sm.trd += gs[kGaugeDim];
+        if (j == kGaugeDim - 1 &&
+            (!(sm.trs <= kCoarseMaxRatio * sm.trd) || !GaugeInverse(sm.zsz, sm.E)))
+          for (int q = 0; q < kGaugeDim * kGaugeDim; ++q) sm.E[q] = 0.0;
+      });
+    }
+  }
+  // the coarse correction c = E Z^T r from the reduced Z^T r (thread 0 of each CTA)
+  auto coarse_of = [&](const double* ztr) {
+    for (int i = 0; i < kGaugeDim; ++i) {
+      double c = 0.0;
+      for (int j = 0; j < kGaugeDim; ++j) c += sm.E[i * kGaugeDim + j] * ztr[j];
+      sm.cg[i] = c;
+    }
+  };
+  auto z_plus_coarse = [&](T zb) {  // P r + Z c of this row
+    T z = zb;
+#pragma unroll
+    for (int i = 0; i < kGaugeDim; ++i) z += (row_ok ? zg[i * nrows + gi] : T(0)) * T(sm.cg[i]);
+    return z;
+  };
   double y64 = 0.0;
   int outer = 0;
   while (!sm.converged) {
@@ -486,12 +660,31 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
     T r = T(r64);
     T zz = ApplyBlock(prow, r, gbase);
     if (store) StX<kStaged>(zv + gi, zz);
-    GridReduce<double>(own ? double(r) * double(zz) : 0.0, 0.0, d, seq, sm,
-                       [&](double x, double) { sm.rz = x; });
+    T zf = zz;  // the preconditioned residual (with the coarse correction)
+    if constexpr (kCoarse) {
+      double rv[1 + kGaugeDim];
+      rv[0] = own ? double(r) * double(zz) : 0.0;
+#pragma unroll
+      for (int i = 0; i < kGaugeDim; ++i) rv[1 + i] = own ? double(r) * double(zg[i * nrows + gi]) : 0.0;
+      GridReduceN<1 + kGaugeDim>(rv, d, seq, sm, redn, [&](double* g) {
+        coarse_of(g + 1);
+        double rz = g[0];
+        for (int i = 0; i < kGaugeDim; ++i) rz += sm.cg[i] * g[1 + i];
+        sm.rz = rz;
+      });
+      zf = z_plus_coarse(zz);
+    } else {
+      GridReduce<double>(own ? double(r) * double(zz) : 0.0, 0.0, d, seq, sm,
+                         [&](double x, double) { sm.rz = x; });
+    }
     T p = T(0), qv = T(0), dx = T(0), beta = T(0);
     for (;;) {
-      const T w = CombineSplit<SPLIT>(in_group ? GroupRow<T, kStaged>(Sb, gent, e0, e1, SPLIT, a, zv) : T(0), a);
-      p = zz + beta * p;
+      T w = CombineSplit<SPLIT>(in_group ? GroupRow<T, kStaged>(Sb, gent, e0, e1, SPLIT, a, zv) : T(0), a);
+      if constexpr (kCoarse) {
+#pragma unroll
+        for (int i = 0; i < kGaugeDim; ++i) w += (row_ok ? szg[i * nrows + gi] : T(0)) * T(sm.cg[i]);
+      }
+      p = zf + beta * p;
       qv = w + beta * qv;
       GridReduce<double>(own ? double(p) * double(qv) : 0.0, 0.0, d, seq, sm, [&](double pq, double) {
         const double rz = sm.rz;
@@ -504,13 +697,32 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
       r -= alpha * qv;
       zz = ApplyBlock(prow, r, gbase);
       if (store) StX<kStaged>(zv + gi, zz);
-      GridReduce<double>(own ? double(r) * double(zz) : 0.0, own ? double(r) * double(r) : 0.0, d, seq, sm,
-                         [&](double rz, double rr) {
-        sm.iters += 1;
-        sm.stop = (sqrt(rr) <= sm.target || sm.iters >= d.max_iters) ? 1 : 0;
-        sm.beta = rz / sm.rz;
-        sm.rz = rz;
-      });
+      if constexpr (kCoarse) {
+        double rv[2 + kGaugeDim];
+        rv[0] = own ? double(r) * double(zz) : 0.0;
+        rv[1] = own ? double(r) * double(r) : 0.0;
+#pragma unroll
+        for (int i = 0; i < kGaugeDim; ++i) rv[2 + i] = own ? double(r) * double(zg[i * nrows + gi]) : 0.0;
+        GridReduceN<2 + kGaugeDim>(rv, d, seq, sm, redn, [&](double* g) {
+          coarse_of(g + 2);
+          double rz = g[0];
+          for (int i = 0; i < kGaugeDim; ++i) rz += sm.cg[i] * g[2 + i];
+          sm.iters += 1;
+          sm.stop = (sqrt(g[1]) <= sm.target || sm.iters >= d.max_iters) ? 1 : 0;
+          sm.beta = rz / sm.rz;
+          sm.rz = rz;
+        });
+        zf = z_plus_coarse(zz);
+      } else {
+        GridReduce<double>(own ? double(r) * double(zz) : 0.0, own ? double(r) * double(r) : 0.0, d, seq, sm,
+                           [&](double rz, double rr) {
+          sm.iters += 1;
+          sm.stop = (sqrt(rr) <= sm.target || sm.iters >= d.max_iters) ? 1 : 0;
+          sm.beta = rz / sm.rz;
+          sm.rz = rz;
+        });
+        zf = zz;
+      }
       if (sm.stop) break;
       beta = T(sm.beta);
     }
@@ -534,6 +746,37 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
     ps->max_iterations = max(ps->max_iterations, sm.iters);
     ps->max_rel_residual = fmax(ps->max_rel_residual, sm.rel);
   }
+}
+
+// Z (T [7][ng * 9], column-major by group row) of the similarity gauge at the current camera
+// poses (POSE3 storage qx qy qz qw tx ty tz, tangent [rotation, translation], the pose mapping world
+// to camera coordinates): moving the world by a translation e_a moves a pose's translation by
+// -R e_a; rotating it by e_a moves a pose's rotation by -e_a; scaling it moves the translation by t
+// (the null vectors of an undamped bundle-adjustment Hessian, restricted to the cameras).
+template <typename T>
+__global__ void GaugeBasisKernel(PcgDev d, const double* values, int64_t S, const LmState* st) {
+  const int64_t rows = int64_t(d.pd.ng) * kB;
+  const int64_t row = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (row >= rows) return;
+  double z[kGaugeDim] = {0, 0, 0, 0, 0, 0, 0};
+  const int64_t so = d.gauge_soff[row];
+  if (so >= 0) {
+    const double* x = values + int64_t(st->init_idx) * S + so;
+    const double qx = x[0], qy = x[1], qz = x[2], qw = x[3];
+    const int c = d.gauge_comp[row];
+    if (c < 3) {
+      z[3 + c] = -1.0;
+    } else {
+      const int i = c - 3;  // row i of R
+      const double R[3][3] = {{1 - 2 * (qy * qy + qz * qz), 2 * (qx * qy - qw * qz), 2 * (qx * qz + qw * qy)},
+                              {2 * (qx * qy + qw * qz), 1 - 2 * (qx * qx + qz * qz), 2 * (qy * qz - qw * qx)},
+                              {2 * (qx * qz - qw * qy), 2 * (qy * qz + qw * qx), 1 - 2 * (qx * qx + qy * qy)}};
+      for (int a = 0; a < 3; ++a) z[a] = -R[i][a];
+      z[6] = x[4 + i];
+    }
+  }
+  T* zg = static_cast<T*>(d.zg);
+  for (int j = 0; j < kGaugeDim; ++j) zg[j * rows + row] = T(z[j]);
 }
 
 template <typename T>
@@ -581,11 +824,14 @@ void LaunchCollectSamples(const PrecondDev& pd, const float* feats, const float*
 
 template <typename T, int SPLIT>
 int PcgMaxResidentCtas(int threads, int num_sms) {
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, PcgKernel<T, false, SPLIT>, threads, 0) !=
-      cudaSuccess)
+  // the coarse variant uses more registers and shared memory: the smaller count of the two
+  int per_sm = 0, per_sm_c = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, PcgKernel<T, false, SPLIT, false>, threads, 0) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c, PcgKernel<T, false, SPLIT, true>, threads, 0) !=
+          cudaSuccess)
     return 0;
-  return per_sm * num_sms;
+  return std::min(per_sm, per_sm_c) * num_sms;
 }
 
 template <typename T>
@@ -633,7 +879,8 @@ template size_t PcgStagedSmem<float>(int, int, int);
 
 template <typename T>
 void ConfigurePcg() {
-  cudaFuncSetAttribute(PcgKernel<T, true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPcgStagedMax));
+  cudaFuncSetAttribute(PcgKernel<T, true, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPcgStagedMax));
+  cudaFuncSetAttribute(PcgKernel<T, true, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPcgStagedMax));
 }
 template void ConfigurePcg<double>();
 template void ConfigurePcg<float>();
@@ -648,13 +895,13 @@ void LaunchGroupBlocks(const int64_t* off, int64_t n, const void* S, void* Sb, c
 template void LaunchGroupBlocks<double>(const int64_t*, int64_t, const void*, void*, cudaStream_t);
 template void LaunchGroupBlocks<float>(const int64_t*, int64_t, const void*, void*, cudaStream_t);
 
-template <typename T>
-cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s) {
+template <typename T, bool kCoarse>
+cudaError_t LaunchPcgVariant(const PcgDev& d, int grid, int threads, cudaStream_t s) {
   if (grid == 1) {
     if (d.staged) {
-      PcgKernel<T, true, 1><<<1, threads, size_t(d.staged), s>>>(d);
+      PcgKernel<T, true, 1, kCoarse><<<1, threads, size_t(d.staged), s>>>(d);
     } else {
-      PcgKernel<T, false, 1><<<1, threads, 0, s>>>(d);
+      PcgKernel<T, false, 1, kCoarse><<<1, threads, 0, s>>>(d);
     }
     return cudaGetLastError();
   }
@@ -670,9 +917,24 @@ cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s) {
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (d.split == 3) return cudaLaunchKernelEx(&cfg, PcgKernel<T, false, 3>, d);
-  return cudaLaunchKernelEx(&cfg, PcgKernel<T, false, 1>, d);
+  if (d.split == 3) return cudaLaunchKernelEx(&cfg, PcgKernel<T, false, 3, kCoarse>, d);
+  return cudaLaunchKernelEx(&cfg, PcgKernel<T, false, 1, kCoarse>, d);
 }
+
+template <typename T>
+cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s) {
+  return d.coarse ? LaunchPcgVariant<T, true>(d, grid, threads, s) : LaunchPcgVariant<T, false>(d, grid, threads, s);
+}
+
+template <typename T>
+void LaunchGaugeBasis(const PcgDev& d, const double* values, int64_t S, const LmState* st, cudaStream_t s) {
+  const int64_t rows = int64_t(d.pd.ng) * kB;
+  if (rows == 0) return;
+  const int threads = 256;
+  GaugeBasisKernel<T><<<int((rows + threads - 1) / threads), threads, 0, s>>>(d, values, S, st);
+}
+template void LaunchGaugeBasis<double>(const PcgDev&, const double*, int64_t, const LmState*, cudaStream_t);
+template void LaunchGaugeBasis<float>(const PcgDev&, const double*, int64_t, const LmState*, cudaStream_t);
 template cudaError_t LaunchPcg<double>(const PcgDev&, int, int, cudaStream_t);
 template cudaError_t LaunchPcg<float>(const PcgDev&, int, int, cudaStream_t);
 

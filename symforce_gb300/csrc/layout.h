@@ -64,6 +64,11 @@ struct PrecondLayout {
   std::vector<int64_t> blk_off;       // [nblocks][81] S value offset; -1 padding, -2 zero
   std::vector<int32_t> gptr;          // [ng + 1] entries of each group row
   std::vector<int32_t> gent;          // [entries][2] {stored block, neighbour << 1 | transposed}
+  // similarity gauge of the camera poses: per group row, the storage offset of its POSE3 key in the
+  // values (-1: not a pose row) and its tangent component (0..2 rotation, 3..5 translation)
+  std::vector<int64_t> gauge_soff;    // [ng][9]
+  std::vector<int32_t> gauge_comp;    // [ng][9]
+  int gauge_rows = 0;                 // pose rows
 };
 PrecondLayout BuildPrecondLayout(const HostProblem& P, const SchurLayout& SL);
 

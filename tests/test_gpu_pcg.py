@@ -201,3 +201,25 @@ def test_trained_network_against_block_jacobi():
             tot[k][1] += r[k]["fallbacks"]
     assert tot["learned"][0] < tot["block_jacobi"][0], tot
     assert tot["learned"][1] <= tot["block_jacobi"][1], tot
+
+
+@pytest.mark.parametrize("precision", [A.SFG_PRECISION_FP64, A.SFG_PRECISION_MIXED])
+def test_gauge_coarse_correction_cuts_iterations(precision):
+    """The coarse correction on the camera poses' similarity gauge (pcg_coarse) against the camera
+    blocks alone, block Jacobi, multi-CTA launch: the same cost, and fewer PCG iterations in total
+    (the 7 gauge directions are the near-null space of a bundle-adjustment reduced system; damping
+    lifts them only as far as lambda does)."""
+    p = synth.bundle_adjustment(num_cameras=300, num_points=6000, num_observations=30000, seed=11)
+    params = A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC, iterations=30,
+                                        early_exit_min_reduction=1e-9)
+    out = {}
+    for coarse in (0, 1):
+        opt = Optimizer(p, params, A.default_form_params(precision=precision, pcg_coarse=coarse,
+                                                        linear_solver=A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI))
+        _, stats = opt.optimize(p.values)
+        out[coarse] = (min(r.best_error for r in stats.iterations), opt.pcg_stats())
+        opt.close()
+    (best0, ps0), (best1, ps1) = out[0], out[1]
+    assert abs(best1 - best0) <= 1e-6 * best0, (best0, best1)
+    assert ps1["fallbacks"] <= ps0["fallbacks"], (ps0, ps1)
+    assert ps1["iterations"] < ps0["iterations"], (ps0, ps1)

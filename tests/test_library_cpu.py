@@ -52,7 +52,7 @@ def test_default_params_match_reference():
     ref = A.default_optimizer_params()
     for f, _ in A.OptimizerParams._fields_:
         assert getattr(p, f) == getattr(ref, f), f
-    assert L.sfg_abi_version() == 2
+    assert L.sfg_abi_version() == 3
     f = A.FormParams()
     L.sfg_default_form_params(C.byref(f))
     for k, _ in A.FormParams._fields_:
