@@ -159,21 +159,56 @@ __global__ void SchurWKernel(SchurDev d, const T* hess_all, int64_t nvals, const
 // S = B - sum_p E_pk^T W_pl over the S blocks' terms (points seen by both keys), in two passes.
 // Pass 1: one warp per chunk of at most chunk_terms terms of one block; each lane takes the
 // chunk's terms in turn and accumulates the whole d_k x d_l product of its terms in registers (every
-// E and W block is read once), then a fixed shuffle tree adds the lanes.  Pass 2: one warp per S
-// block adds its chunks in order and writes B_kl (+ damping) - sum.  Chunks spread the heavy
-// diagonal blocks (every observation of a camera) over many warps, which the FP64 pipe needs; the
-// fixed orders make every run give the same bits.  Key tangent dims are at most kMaxKeyDim.
+// E and W block is read once; a diagonal block only its lower triangle), then a butterfly
+// reduce-scatter adds the lanes.  Pass 2: one warp per S block adds its chunks in order and writes
+// B_kl (+ damping) - sum.  Chunks spread the heavy diagonal blocks (every observation of a camera)
+// over many warps, which the FP64 pipe needs; the fixed orders make every run give the same bits.
+// Key tangent dims are at most kMaxKeyDim.
 constexpr int kMaxKeyDim = 6;
 constexpr int kSchurWarps = 4;
+
+// One exchange level of a butterfly reduce-scatter over the warp: the N values of v (entries
+// [base, base + cnt) of the original order, the rest zero padding) are halved; lanes with bit O
+// clear keep the lower ceil(N/2), the others the upper part, each adding its partner's copy of the
+// half it keeps.  Five levels (O = 16 .. 1) leave every value summed over the 32 lanes in exactly
+// one lane, for N/2 + N/4 + ... FP64 adds a lane instead of the 5 N of a shuffle tree per value.
+template <typename T, int N, int O>
+__device__ __forceinline__ void ReduceScatterLevel(T* v, int lane, int& base, int& cnt) {
+  constexpr int H = (N + 1) / 2;
+  const bool up = (lane & O) != 0;
+#pragma unroll
+  for (int i = 0; i < H; ++i) {
+    const T lo = v[i];
+    const T hi = H + i < N ? v[H + i] : T(0);
+    const T send = up ? lo : hi;
+    const T keep = up ? hi : lo;
+    v[i] = keep + __shfl_xor_sync(0xffffffffu, send, O);
+  }
+  if (up) {
+    base += H;
+    cnt = cnt > H ? cnt - H : 0;
+  } else {
+    cnt = cnt < H ? cnt : H;
+  }
+  if constexpr (O > 1) ReduceScatterLevel<T, H, O / 2>(v, lane, base, cnt);
+}
+// Values a lane holds after the five levels for N inputs.
+template <int N>
+__host__ __device__ constexpr int ReduceScatterSlots() {
+  int n = N;
+  for (int l = 0; l < 5; ++l) n = (n + 1) / 2;
+  return n;
+}
 
 // The products of one chunk for a block of DK x DL (compile-time sizes: only the block's entries are
 // accumulated, which matters on the FP64 pipe), written as a 6 x 6 row-major partial.
 template <typename T, int DK, int DL>
 __device__ __forceinline__ void ChunkTerms(const SchurDev& d, const T* H, const T* W, int64_t t0,
                                            int64_t t1, int lane, T* out) {
-  T acc[DK * DL];
+  constexpr int N = DK * DL;
+  T acc[N];
 #pragma unroll
-  for (int i = 0; i < DK * DL; ++i) acc[i] = T(0);
+  for (int i = 0; i < N; ++i) acc[i] = T(0);
   for (int64_t t = t0 + lane; t < t1; t += 32) {
     const T* E = H + d.sb_eoff[t];
     const T* Wl = W + d.sb_woff[t];
@@ -188,18 +223,51 @@ __device__ __forceinline__ void ChunkTerms(const SchurDev& d, const T* H, const 
       for (int c = 0; c < DL; ++c)
         acc[r * DL + c] += e[r] * w[c] + e[DK + r] * w[DL + c] + e[2 * DK + r] * w[2 * DL + c];
   }
+  int base = 0, cnt = N;
+  ReduceScatterLevel<T, N, 16>(acc, lane, base, cnt);
 #pragma unroll
-  for (int i = 0; i < DK * DL; ++i) {
-    T v = acc[i];
+  for (int i = 0; i < ReduceScatterSlots<N>(); ++i)
+    if (i < cnt) {
+      const int ent = base + i, r = ent / DL, c = ent - r * DL;
+      out[r * kMaxKeyDim + c] = acc[i];
+    }
+}
+
+// A diagonal block (k = l, W_pk = C_p^-1 E_pk): its D (D + 1) / 2 lower entries, row-major packed;
+// each is written to both triangles of the partial.
+template <typename T, int D>
+__device__ __forceinline__ void ChunkTermsSym(const SchurDev& d, const T* H, const T* W, int64_t t0,
+                                              int64_t t1, int lane, T* out) {
+  constexpr int N = D * (D + 1) / 2;
+  T acc[N];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    acc[i] = v;
+  for (int i = 0; i < N; ++i) acc[i] = T(0);
+  for (int64_t t = t0 + lane; t < t1; t += 32) {
+    const T* E = H + d.sb_eoff[t];
+    const T* Wl = W + d.sb_woff[t];
+    T e[3 * D], w[3 * D];
+#pragma unroll
+    for (int i = 0; i < 3 * D; ++i) e[i] = E[i];
+#pragma unroll
+    for (int i = 0; i < 3 * D; ++i) w[i] = Wl[i];
+#pragma unroll
+    for (int r = 0; r < D; ++r)
+#pragma unroll
+      for (int c = 0; c <= r; ++c)
+        acc[r * (r + 1) / 2 + c] += e[r] * w[c] + e[D + r] * w[D + c] + e[2 * D + r] * w[2 * D + c];
   }
-  if (lane == 0)
+  int base = 0, cnt = N;
+  ReduceScatterLevel<T, N, 16>(acc, lane, base, cnt);
 #pragma unroll
-    for (int r = 0; r < DK; ++r)
-#pragma unroll
-      for (int c = 0; c < DL; ++c) out[r * kMaxKeyDim + c] = acc[r * DL + c];
+  for (int i = 0; i < ReduceScatterSlots<N>(); ++i)
+    if (i < cnt) {
+      const int ent = base + i;
+      int r = 0;
+      while ((r + 1) * (r + 2) / 2 <= ent) ++r;
+      const int c = ent - r * (r + 1) / 2;
+      out[r * kMaxKeyDim + c] = acc[i];
+      out[c * kMaxKeyDim + r] = acc[i];
+    }
 }
 
 // Any other key sizes (up to kMaxKeyDim): runtime bounds inside the 6 x 6 accumulator.
@@ -207,9 +275,10 @@ template <typename T>
 __device__ __forceinline__ void ChunkTermsAny(const SchurDev& d, const T* H, const T* W, int dk, int dl,
                                               int64_t t0, int64_t t1, int lane, T* out) {
   constexpr int D = kMaxKeyDim;
-  T acc[D * D];
+  constexpr int N = D * D;
+  T acc[N];
 #pragma unroll
-  for (int i = 0; i < D * D; ++i) acc[i] = T(0);
+  for (int i = 0; i < N; ++i) acc[i] = T(0);
   for (int64_t t = t0 + lane; t < t1; t += 32) {
     const T* E = H + d.sb_eoff[t];
     const T* Wl = W + d.sb_woff[t];
@@ -227,16 +296,11 @@ __device__ __forceinline__ void ChunkTermsAny(const SchurDev& d, const T* H, con
       for (int c = 0; c < D; ++c)
         acc[r * D + c] += e[r] * w[c] + e[D + r] * w[D + c] + e[2 * D + r] * w[2 * D + c];
   }
+  int base = 0, cnt = N;
+  ReduceScatterLevel<T, N, 16>(acc, lane, base, cnt);
 #pragma unroll
-  for (int i = 0; i < D * D; ++i) {
-    T v = acc[i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    acc[i] = v;
-  }
-  if (lane == 0)
-#pragma unroll
-    for (int i = 0; i < D * D; ++i) out[i] = acc[i];
+  for (int i = 0; i < ReduceScatterSlots<N>(); ++i)
+    if (i < cnt) out[base + i] = acc[i];
 }
 
 template <typename T>
@@ -252,7 +316,12 @@ __global__ void __launch_bounds__(32 * kSchurWarps)
   const int64_t t1 = min(t0 + d.chunk_terms, d.sb_ptr[sb + 1]);
   T* out = static_cast<T*>(d.partials) + int64_t(ch) * (kMaxKeyDim * kMaxKeyDim);
   // one case per chunk (warp-uniform): the key sizes of bundle adjustment and 2D / 3D poses
-  switch (dk * 8 + dl) {
+  const bool diag = d.sb_diag_toff[sb] >= 0;
+  switch (dk * 8 + dl + (diag ? 64 : 0)) {
+    case 64 + 6 * 8 + 6: ChunkTermsSym<T, 6>(d, H, W, t0, t1, lane, out); break;
+    case 64 + 3 * 8 + 3: ChunkTermsSym<T, 3>(d, H, W, t0, t1, lane, out); break;
+    case 64 + 2 * 8 + 2: ChunkTermsSym<T, 2>(d, H, W, t0, t1, lane, out); break;
+    case 64 + 1 * 8 + 1: ChunkTermsSym<T, 1>(d, H, W, t0, t1, lane, out); break;
     case 6 * 8 + 6: ChunkTerms<T, 6, 6>(d, H, W, t0, t1, lane, out); break;
     case 3 * 8 + 6: ChunkTerms<T, 3, 6>(d, H, W, t0, t1, lane, out); break;
     case 6 * 8 + 3: ChunkTerms<T, 6, 3>(d, H, W, t0, t1, lane, out); break;
