@@ -236,7 +236,7 @@ extern "C" int32_t sfg_dense_ldlt_solve_noalloc(int32_t n, const double* A, int6
   PrepareKernel<<<1, 256, 0, st>>>(n, A, lda);
   sfg::LaunchFactor<double>(f, s->front, nullptr, s->front, s->linv,
                             std::max(1, std::min(ntasks, sms * 8)), st);
-  sfg::LaunchSolve<double>(f, s->front, s->linv, b, s->vec + 2 * kMaxN, s->vec, s->vec + kMaxN, x,
+  sfg::LaunchSolve<double>(f, s->front, s->linv, b, s->vec + 2 * kMaxN, s->vec, s->vec + kMaxN, x, nullptr,
                            std::max(1, std::min(2, sms)), st);
   CheckPivotsKernel<<<1, 256, 0, st>>>(n, x);
   rc = cudaGetLastError();

@@ -84,8 +84,51 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   fp.F = A.Alloc(size_t(S.front_pool) * elem);
   fp.Linv = A.Alloc(size_t(std::max<int64_t>(linv_base[S.ns], 1)) * elem);
   fp.ycon = A.Alloc(size_t(std::max<int64_t>(S.rel_off[S.ns], 1)) * elem);
-  fp.ysave = A.Alloc(size_t(std::max<int64_t>(S.idx_off[S.ns], 1)) * elem);
+  fp.nsave = std::max<int64_t>(S.idx_off[S.ns], 1);
+  fp.ysave = A.Alloc(size_t(2 * fp.nsave) * elem);
+  fp.xb = static_cast<char*>(fp.ysave) + size_t(fp.nsave) * elem;
   fp.xperm = A.Alloc(size_t(std::max<int64_t>(S.n, 1)) * elem);
+  // FP64 solves of fronts with more tiles than a solve CTA has warps are split over CTAs of
+  // kSolveBlockTiles pivot tiles (and, forward, CTAs of as many update tiles): one SM's FP64 pipe
+  // caps a front's solve.  FP32 solves keep one CTA per front and direction, as does
+  // SFG_SOLVE_SPLIT=0.
+  bool split = elem == 8;
+  if (const char* e = std::getenv("SFG_SOLVE_SPLIT")) split = split && std::atoi(e) != 0;
+  std::vector<int32_t> kp(size_t(S.ns), 0), ku(size_t(S.ns), 0), task_front, task_sub;
+  int64_t nsplit = 0;
+  for (int s = 0; s < S.ns; ++s) {
+    const int np = T.npiv[size_t(s)], nu = T.ntiles[size_t(s)] - np;
+    if (split && np > 0 && np + nu > SolveWarps()) {
+      kp[size_t(s)] = (np + kSolveBlockTiles - 1) / kSolveBlockTiles;
+      ku[size_t(s)] = (nu + kSolveBlockTiles - 1) / kSolveBlockTiles;
+      ++nsplit;
+    }
+  }
+  int ntasks_solve = 2 * S.ns;
+  if (nsplit > 0) {
+    for (int s = 0; s < S.ns; ++s) {
+      const int k = kp[size_t(s)] > 0 ? kp[size_t(s)] + ku[size_t(s)] : 1;
+      for (int c = 0; c < k; ++c) {
+        task_front.push_back(s);
+        task_sub.push_back(c);
+      }
+    }
+    const int nf = int(task_front.size());
+    for (int s = S.ns - 1; s >= 0; --s) {
+      const int k = kp[size_t(s)] > 0 ? kp[size_t(s)] : 1;
+      for (int c = 0; c < k; ++c) {
+        task_front.push_back(s);
+        task_sub.push_back(c);
+      }
+    }
+    f.solve_front = A.Upload(task_front);
+    f.solve_sub = A.Upload(task_sub);
+    f.solve_kp = A.Upload(kp);
+    f.solve_ku = A.Upload(ku);
+    f.solve_nf = nf;
+    f.solve_nb = int(task_front.size()) - nf;
+    ntasks_solve = int(task_front.size());
+  }
   const int per_sm = 8;
   // the factorization kernel is built for kFactorCtasPerSm resident CTAs of 128 threads per SM
   // SFG_FACTOR_CTAS_PER_SM (1..kFactorCtasPerSm) narrows the grid for launch-shape measurements
@@ -93,7 +136,7 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   if (const char* e = std::getenv("SFG_FACTOR_CTAS_PER_SM"))
     factor_per_sm = std::max(1, std::min(kFactorCtasPerSm, std::atoi(e)));
   fp.grid_factor = std::max(1, std::min<int>(f.ntasks, num_sms * factor_per_sm));
-  fp.grid_solve = std::max(1, std::min<int>(2 * S.ns, num_sms * per_sm));
+  fp.grid_solve = std::max(1, std::min<int>(ntasks_solve, num_sms * per_sm));
   if (elem == 8) ConfigureSolve<double>(maxm);
   else ConfigureSolve<float>(maxm);
 }
@@ -187,11 +230,14 @@ void EnqueueFactor(const FactorPlan& fp, const void* A, const double* damping, c
 template <typename T>
 void EnqueueSolve(const FactorPlan& fp, const void* b, void* x, cudaStream_t s, bool fixed_b,
                   const int* gate) {
-  LaunchResetFactorState(fp.f.tile_state, 0, fp.f.front_flags, fp.nflags, fp.f.counters, s, gate);
+  // split solves: the exchange values (ysave, xb) back to the unset pattern
+  const bool split = fp.f.solve_front != nullptr;
+  LaunchResetFactorState(fp.f.tile_state, 0, fp.f.front_flags, fp.nflags, fp.f.counters, s, gate,
+                         split ? fp.ysave : nullptr, split ? 2 * fp.nsave : 0, int(sizeof(T)));
   FactorDev f = fp.f;
   f.gate = gate;
   if (fixed_b) f.b_stride = 0;
-  LaunchSolve<T>(f, fp.F, fp.Linv, b, fp.ycon, fp.ysave, fp.xperm, x, fp.grid_solve, s);
+  LaunchSolve<T>(f, fp.F, fp.Linv, b, fp.ycon, fp.ysave, fp.xperm, x, fp.xb, fp.grid_solve, s);
 }
 
 template void EnqueueFactor<double>(const FactorPlan&, const void*, const double*, cudaStream_t,

@@ -49,6 +49,8 @@ struct FactorPlan {
   void* ycon = nullptr;
   void* ysave = nullptr;
   void* xperm = nullptr;
+  void* xb = nullptr;      // backward exchange values of split solves (ysave's size, right after it)
+  int64_t nsave = 0;       // scalars of ysave (and of xb)
   int nflags = 0;
 };
 

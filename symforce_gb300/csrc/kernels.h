@@ -202,21 +202,37 @@ struct FactorDev {
   // leave the kernel) followed by the count of SMs so given, at most iso_limit
   int* sm_flags = nullptr;
   int iso_limit = 0;
+  // optional: solves of wide fronts shared by several CTAs (null solve_front: one CTA per front and
+  // direction).  Tasks [0, solve_nf) are forward (fronts in order), [solve_nf, solve_nf +
+  // solve_nb) backward (fronts in reverse order); each is (front, sub-task).  Per front: solve_kp
+  // pivot-block CTAs (0: the front is solved by one CTA) and solve_ku update-row CTAs.
+  const int32_t* solve_front = nullptr;
+  const int32_t* solve_sub = nullptr;
+  const int32_t* solve_kp = nullptr;
+  const int32_t* solve_ku = nullptr;
+  int solve_nf = 0, solve_nb = 0;
 };
 constexpr int kSmFlagSlots = 512;
+// Pivot tiles of one CTA of a split front solve (one per warp).
+constexpr int kSolveBlockTiles = 4;
+// Warps of a solve CTA.
+int SolveWarps();
 template <typename T>
 void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F, void* Linv,
                   int grid, cudaStream_t s);
 // Solve (L D L^T) x = b for b in the original scalar order; x in the original order.  Linv: the
 // inverses of the pivot tiles' unit lower factors that LaunchFactor wrote.
+// xb: the backward exchange buffer (as large as ysave) of split solves, else unused.
 template <typename T>
 void LaunchSolve(const FactorDev& f, const void* F, const void* Linv, const void* b, void* ycon,
-                 void* ysave, void* xperm, void* x, int grid, cudaStream_t s);
+                 void* ysave, void* xperm, void* x, void* xb, int grid, cudaStream_t s);
 int FactorThreads();
 // One CTA waits (capped) for *flag >= 1 while nothing sets it; the cap sets *err.
 cudaError_t LaunchWaitCapSelfTest(const int* flag, int* err, cudaStream_t s);
+// `unset` (optional): n_unset values of elem bytes set to the split solves' unset pattern.
 void LaunchResetFactorState(int* tile_state, int nstates, int* front_flags, int nflags,
-                            int* counters, cudaStream_t s, const int* gate = nullptr);
+                            int* counters, cudaStream_t s, const int* gate = nullptr,
+                            void* unset = nullptr, int64_t n_unset = 0, int elem = 8);
 template <typename T>
 void LaunchNegate(const void* x, double* u, int64_t n, cudaStream_t s);
 // Opt the solve kernel into the shared memory its largest front needs (call once per device).

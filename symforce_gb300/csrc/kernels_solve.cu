@@ -533,6 +533,14 @@ __device__ __forceinline__ void Signal(int* addr, int v) {
     atomicExch(addr, v);
   }
 }
+// The same for a completion count that several CTAs add to.
+__device__ __forceinline__ void SignalAdd(int* addr) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(addr, 1);
+  }
+}
 
 // Load a b_r x b_c tile at (r0, c0) of a column-major front into smem, transposed: dst[c*TILE + r].
 template <typename T, int TILE>
@@ -1426,10 +1434,10 @@ __global__ void __launch_bounds__(kFactorThreads, kFactorCtasPerSm) FactorKernel
 constexpr int kSolveThreads = 256;
 // Dynamic shared memory of a solve CTA: the largest front's scalars, plus one warp's width of
 // slack (every read is bounded by the front; the slack only keeps a short last tile's lanes inside
-// the allocation).
+// the allocation), then one tile of received values per warp (solves shared by several CTAs).
 template <typename T>
 size_t SolveSmemBytes(int max_m) {
-  return (size_t(max_m) + 32) * sizeof(T);
+  return (size_t(max_m) + 32 + size_t(kSolveThreads / 32) * 32) * sizeof(T);
 }
 
 // sum_{c = c0}^{c1 - 1} a[c * stride] x[c] with four independent accumulation chains, added in a
@@ -1600,60 +1608,258 @@ __device__ void BackwardFront(const Geom& g, const T* Fs, const T* Li, T* xs, vo
   __syncthreads();
 }
 
+// ---------------------------------------------------------------------------------------------
+// Solves of wide fronts by several CTAs.  One CTA's FP64 pipe caps a front's solve (a 450-wide
+// front's ~100k multiply-adds per direction take ~37 us of one SM), so a front with more tiles than
+// a CTA has warps is split: pivot-block CTAs own kSolveBlockTiles consecutive pivot tiles each (one
+// per warp: the chain steps inside a block pass through shared memory), update CTAs own the
+// update-row tiles (forward only; tile np + u + ku l to CTA u).  Values a CTA needs from another
+// CTA go through global memory without flags: the exchange buffers (ysave for the forward y, xb
+// for the backward x, front-local order) hold an unset pattern — a signalling NaN, which no
+// arithmetic produces — until the owner stores the value, and a reader polls each value until it
+// is set.  The buffers are reset to the pattern before every solve launch.  Every CTA waits only on
+// CTAs with lower task numbers (forward: earlier blocks; backward: later blocks, numbered first),
+// so the persistent task order cannot deadlock.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ bool IsUnset(double v) {
+  return __double_as_longlong(v) == static_cast<long long>(0x7FF4DEAD0BADF00DULL);
+}
+__device__ __forceinline__ bool IsUnset(float v) { return __float_as_uint(v) == 0x7FA5DEADu; }
+__device__ __forceinline__ double LdRelaxed(const double* p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ float LdRelaxed(const float* p) {
+  float v;
+  asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void StRelaxed(double* p, double v) {
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" : : "l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ void StRelaxed(float* p, float v) {
+  asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" : : "l"(p), "f"(v) : "memory");
+}
+
+// First attempt at the bn values of a published tile (lane l reads value l mod TILE).
+template <typename T, int TILE>
+__device__ __forceinline__ T PeekTile(const T* p, int bn) {
+  const int l = (threadIdx.x & 31) % TILE;
+  return l < bn ? LdRelaxed(p + l) : T(0);
+}
+// Spin (capped, and given up when the error word is set) until all bn values of the tile are set,
+// starting from the PeekTile value v, then copy them to the warp's scratch (zero past bn).
+template <typename T, int TILE>
+__device__ __forceinline__ void ReceiveTile(const T* p, int bn, T v, T* scratch, int* err) {
+  const int lane = threadIdx.x & 31, l = lane % TILE;
+  const bool need = l < bn;
+  unsigned it = 0;
+  while (!__all_sync(0xffffffffu, !need || !IsUnset(v))) {
+    if (++it > kSpinLimit || ((it & 255u) == 0 && LoadVolatile(err) != 0)) {
+      if (lane == 0 && it > kSpinLimit) atomicExch(err, kDevSpinTimeout);
+      break;
+    }
+    if (need && IsUnset(v)) v = LdRelaxed(p + l);
+  }
+  if (lane < TILE) scratch[lane] = need ? v : T(0);
+  __syncwarp();
+}
+
+// Forward solve of front g by CTA `cta` of kp pivot-block CTAs and ku update CTAs (xs holds the
+// CTA's own rows: b plus the children's contributions; yx = the front's forward exchange values).
+// Warp q of pivot CTA c takes pivot tile c kSolveBlockTiles + q: it applies every earlier column
+// (received from global memory for earlier blocks, from shared memory inside its block), solves
+// the tile and stores y to shared memory and to yx.  Update CTA warps take update tiles and apply
+// every pivot column.
+template <typename T, int TILE>
+__device__ void ForwardMulti(const Geom& g, const T* Fs, const T* Li, T* xs, T* yx, T* scratch,
+                             volatile int* s_done, int cta, int kp, int ku, int* err) {
+  const int m = g.m, np = g.np, nt = g.nt;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int row = lane % TILE, part = lane / TILE;
+  if (warp >= kSolveBlockTiles) return;
+  WarpBlock<T, TILE> inv, cur, nxt;
+  if (cta < kp) {
+    const int b0 = cta * kSolveBlockTiles, i = b0 + warp;
+    if (i >= np) return;
+    const int ri = i * TILE, bi = min(TILE, g.w - ri);
+    inv.Load(Li + int64_t(i) * TILE * TILE, 1, TILE, bi, bi);
+    if (i > 0) cur.Load(Fs + ri, 1, m, bi, min(TILE, g.w));
+    T pv = b0 > 0 ? PeekTile<T, TILE>(yx, min(TILE, g.w)) : T(0);
+    for (int j = 0; j < i; ++j) {
+      const int cj = j * TILE, bj = min(TILE, g.w - cj);
+      const T* x;
+      if (j < b0) {
+        ReceiveTile<T, TILE>(yx + cj, bj, pv, scratch, err);
+        x = scratch;
+        if (j + 1 < b0) pv = PeekTile<T, TILE>(yx + cj + TILE, min(TILE, g.w - cj - TILE));
+      } else {
+        WaitPublished(s_done, j - b0 + 1, err);
+        x = xs + cj;
+      }
+      if (j + 1 < i) nxt.Load(Fs + ri + int64_t(cj + TILE) * m, 1, m, bi, min(TILE, g.w - cj - TILE));
+      const T u = cur.Dot(x);
+      if (part == 0 && row < bi) xs[ri + row] -= u;
+      cur = nxt;
+      __syncwarp();
+    }
+    const T y = inv.Dot(xs + ri);
+    __syncwarp();
+    if (part == 0 && row < bi) {
+      xs[ri + row] = y;
+      StRelaxed(yx + ri + row, y);
+    }
+    Publish(s_done, warp + 1);
+    return;
+  }
+  // update CTA: tiles np + u + ku (warp + kSolveBlockTiles r), r = 0, 1, ...
+  const int u = cta - kp, step = ku * kSolveBlockTiles;
+  const int i0 = np + u + ku * warp;
+  if (i0 >= nt) return;
+  T pv = PeekTile<T, TILE>(yx, min(TILE, g.w));
+  for (int j = 0; j < np; ++j) {
+    const int cj = j * TILE, bj = min(TILE, g.w - cj);
+    cur.Load(Fs + TileStart(g, i0, TILE) + int64_t(cj) * m, 1, m, TileSize(g, i0, TILE), bj);
+    ReceiveTile<T, TILE>(yx + cj, bj, pv, scratch, err);
+    if (j + 1 < np) pv = PeekTile<T, TILE>(yx + cj + TILE, min(TILE, g.w - cj - TILE));
+    for (int i = i0; i < nt; i += step) {
+      const int ri = TileStart(g, i, TILE), bi = TileSize(g, i, TILE);
+      if (i + step < nt) nxt.Load(Fs + TileStart(g, i + step, TILE) + int64_t(cj) * m, 1, m, TileSize(g, i + step, TILE), bj);
+      const T v = cur.Dot(scratch);
+      if (part == 0 && row < bi) xs[ri + row] -= v;
+      cur = nxt;
+    }
+    __syncwarp();
+  }
+}
+
+// Backward solve of front g's pivot columns by pivot-block CTA `blk` (xs holds its rows' z: D^-1 y
+// minus the update rows' contributions; xe = the front's backward exchange values).  Warp q takes
+// tile blk kSolveBlockTiles + q and applies L_ij^T x_i of every later tile i (received from global
+// memory for later blocks, from shared memory inside its block), then solves it.
+template <typename T, int TILE>
+__device__ void BackwardMulti(const Geom& g, const T* Fs, const T* Li, T* xs, T* xe, T* scratch,
+                              volatile int* s_done, int blk, int* err) {
+  const int m = g.m, np = g.np;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int row = lane % TILE, part = lane / TILE;
+  if (warp >= kSolveBlockTiles) return;
+  const int b0 = blk * kSolveBlockTiles, j = b0 + warp;
+  const int top = min(b0 + kSolveBlockTiles, np) - 1;  // the block's last tile, published first
+  if (j > top) return;
+  const int cj = j * TILE, bj = min(TILE, g.w - cj);
+  WarpBlock<T, TILE> inv, cur, nxt;
+  inv.Load(Li + int64_t(j) * TILE * TILE, TILE, 1, bj, bj);
+  if (j < np - 1) cur.Load(Fs + (np - 1) * TILE + int64_t(cj) * m, m, 1, bj, min(TILE, g.w - (np - 1) * TILE));
+  T pv = top < np - 1 ? PeekTile<T, TILE>(xe + (np - 1) * TILE, min(TILE, g.w - (np - 1) * TILE)) : T(0);
+  for (int i = np - 1; i > j; --i) {
+    const int ri = i * TILE, bi = min(TILE, g.w - ri);
+    const T* x;
+    if (i > top) {
+      ReceiveTile<T, TILE>(xe + ri, bi, pv, scratch, err);
+      x = scratch;
+      if (i - 1 > top) pv = PeekTile<T, TILE>(xe + ri - TILE, TILE);
+    } else {
+      WaitPublished(s_done, top - i + 1, err);
+      x = xs + ri;
+    }
+    if (i - 1 > j) nxt.Load(Fs + ri - TILE + int64_t(cj) * m, m, 1, bj, TILE);
+    const T u = cur.Dot(x);
+    if (part == 0 && row < bj) xs[cj + row] -= u;
+    cur = nxt;
+    __syncwarp();
+  }
+  const T x = inv.Dot(xs + cj);
+  __syncwarp();
+  if (part == 0 && row < bj) {
+    xs[cj + row] = x;
+    StRelaxed(xe + cj + row, x);
+  }
+  Publish(s_done, top - j + 1);
+}
+
+// Rows of a front a solve CTA owns: all of them for a one-CTA solve, else its block's pivot rows
+// (pivot CTA) or its update tiles' rows (update CTA).
+__device__ __forceinline__ bool OwnsRow(const Geom& g, int tile, int q, int cta, int kp, int ku) {
+  if (kp == 0) return true;
+  if (cta < kp) return q < g.w && q / (tile * kSolveBlockTiles) == cta;
+  return q >= g.w && ((q - g.w) / tile) % ku == cta - kp;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kSolveThreads) SolveKernel(FactorDev f, const T* F, const T* Linv,
                                                               const T* b, T* ycon, T* ysave, T* xperm,
-                                                              T* x) {
+                                                              T* x, T* xb) {
   constexpr int kTile = sizeof(T) == 8 ? kFactorTileF64 : kFactorTileF32;
   static_assert(kTile <= 32 && kSolveThreads >= 32, "warp 0 holds a tile's rows");
   extern __shared__ unsigned char smem_raw[];
   T* xs = reinterpret_cast<T*>(smem_raw);
+  T* scratch = xs + (f.max_m + 32) + (threadIdx.x >> 5) * 32;
   __shared__ int s_task, s_ok, s_flag, s_done;
   int* fwd_done = f.front_flags;
   int* bwd_done = f.front_flags + f.ns;
   if (f.gate && *f.gate == 0) return;
   b += int64_t(f.st->init_idx) * f.b_stride;
+  const bool split = f.solve_front != nullptr;
+  const int nfwd = split ? f.solve_nf : f.ns;
+  const int ntasks = split ? f.solve_nf + f.solve_nb : 2 * f.ns;
+  // CTAs that signal a front's forward / backward completion
+  auto fwd_ctas = [&](int s) { return split && f.solve_kp[s] > 0 ? f.solve_kp[s] + f.solve_ku[s] : 1; };
+  auto bwd_ctas = [&](int s) { return split && f.solve_kp[s] > 0 ? f.solve_kp[s] : 1; };
   for (;;) {
     if (threadIdx.x == 0) {
       s_ok = LoadVolatile(f.error) == 0;
-      s_task = s_ok ? atomicAdd(f.counters + 1, 1) : 2 * f.ns;
+      s_task = s_ok ? atomicAdd(f.counters + 1, 1) : ntasks;
     }
     __syncthreads();
     const int t = s_task;
-    if (t >= 2 * f.ns) return;
-    if (t < f.ns) {
-      const int s = t;
-      const Geom g = FrontGeom(f, s);
+    if (t >= ntasks) return;
+    const bool forward = t < nfwd;
+    const int s = split ? f.solve_front[t] : (forward ? t : f.ns - 1 - (t - f.ns));
+    const int sub = split ? f.solve_sub[t] : 0;
+    const int kp = split ? f.solve_kp[s] : 0, ku = split ? f.solve_ku[s] : 0;
+    const Geom g = FrontGeom(f, s);
+    if (forward) {
       bool ok = true;
       if (threadIdx.x == 0)
         for (int q = f.child_ptr[s]; q < f.child_ptr[s + 1] && ok; ++q)
-          ok = WaitAtLeast(fwd_done + f.child_list[q], 1, f.error);
+          ok = WaitAtLeast(fwd_done + f.child_list[q], fwd_ctas(f.child_list[q]), f.error);
       if (CtaWait(ok, &s_flag)) {
         const int32_t* idx = f.idx + f.idx_off[s];
         const T* Fs = F + g.foff;
         for (int q = threadIdx.x; q < g.m; q += blockDim.x)
-          xs[q] = q < g.w ? b[f.scalar_old[idx[q]]] : T(0);
+          if (OwnsRow(g, kTile, q, sub, kp, ku)) xs[q] = q < g.w ? b[f.scalar_old[idx[q]]] : T(0);
         if (threadIdx.x == 0) s_done = 0;
         __syncthreads();
         for (int q = f.child_ptr[s]; q < f.child_ptr[s + 1]; ++q) {
           const int c = f.child_list[q];
           const int hc = f.sn_m[c] - f.sn_w[c];
           const int32_t* rel = f.rel + f.rel_off[c];
-          for (int r = threadIdx.x; r < hc; r += blockDim.x) xs[rel[r]] += Ld(ycon + f.rel_off[c] + r);
+          for (int r = threadIdx.x; r < hc; r += blockDim.x)
+            if (OwnsRow(g, kTile, rel[r], sub, kp, ku)) xs[rel[r]] += Ld(ycon + f.rel_off[c] + r);
           __syncthreads();
         }
-        ForwardFront<T, kTile>(g, Fs, Linv + f.linv_base[s], xs, &s_done, f.error);
-        for (int q = threadIdx.x; q < g.w; q += blockDim.x) St(ysave + f.idx_off[s] + q, xs[q]);
-        for (int r = threadIdx.x; r < g.m - g.w; r += blockDim.x) St(ycon + f.rel_off[s] + r, xs[g.w + r]);
-        Signal(fwd_done + s, 1);
+        if (kp == 0) {
+          ForwardFront<T, kTile>(g, Fs, Linv + f.linv_base[s], xs, &s_done, f.error);
+          for (int q = threadIdx.x; q < g.w; q += blockDim.x) St(ysave + f.idx_off[s] + q, xs[q]);
+        } else if constexpr (sizeof(T) == 8) {
+          // pivot CTAs store their y in ysave as they solve
+          ForwardMulti<T, kTile>(g, Fs, Linv + f.linv_base[s], xs, ysave + f.idx_off[s], scratch,
+                                 &s_done, sub, kp, ku, f.error);
+          __syncthreads();
+        }
+        for (int r = threadIdx.x; r < g.m - g.w; r += blockDim.x)
+          if (OwnsRow(g, kTile, g.w + r, sub, kp, ku)) St(ycon + f.rel_off[s] + r, xs[g.w + r]);
+        SignalAdd(fwd_done + s);
       }
     } else {
-      const int s = f.ns - 1 - (t - f.ns);
-      const Geom g = FrontGeom(f, s);
+      const int blk = kp - 1 - sub;  // backward tasks take a front's blocks from the last one down
       bool ok = true;
       if (threadIdx.x == 0) {
         const int p = f.parent[s];
-        ok = p >= 0 ? WaitAtLeast(bwd_done + p, 1, f.error) : WaitAtLeast(fwd_done + s, 1, f.error);
+        ok = p >= 0 ? WaitAtLeast(bwd_done + p, bwd_ctas(p), f.error)
+                    : WaitAtLeast(fwd_done + s, fwd_ctas(s), f.error);
       }
       if (CtaWait(ok, &s_flag)) {
         const int32_t* idx = f.idx + f.idx_off[s];
@@ -1662,18 +1868,26 @@ __global__ void __launch_bounds__(kSolveThreads) SolveKernel(FactorDev f, const 
         T* xa = xs + g.w;
         for (int r = threadIdx.x; r < h; r += blockDim.x) xa[r] = Ld(xperm + idx[g.w + r]);
         __syncthreads();
-        for (int q = threadIdx.x; q < g.w; q += blockDim.x) {
-          const T z = Ld(ysave + f.idx_off[s] + q) / Ld(Fs + int64_t(q) * (g.m + 1));
-          xs[q] = z - RowDot(Fs + int64_t(q) * g.m + g.w, int64_t(1), xa, 0, h);
-        }
+        for (int q = threadIdx.x; q < g.w; q += blockDim.x)
+          if (OwnsRow(g, kTile, q, blk, kp, ku)) {
+            const T z = Ld(ysave + f.idx_off[s] + q) / Ld(Fs + int64_t(q) * (g.m + 1));
+            xs[q] = z - RowDot(Fs + int64_t(q) * g.m + g.w, int64_t(1), xa, 0, h);
+          }
         if (threadIdx.x == 0) s_done = 0;
         __syncthreads();
-        BackwardFront<T, kTile>(g, Fs, Linv + f.linv_base[s], xs, &s_done, f.error);
-        for (int q = threadIdx.x; q < g.w; q += blockDim.x) {
-          St(xperm + idx[q], xs[q]);
-          x[f.scalar_old[idx[q]]] = xs[q];
+        if (kp == 0) {
+          BackwardFront<T, kTile>(g, Fs, Linv + f.linv_base[s], xs, &s_done, f.error);
+        } else if constexpr (sizeof(T) == 8) {
+          BackwardMulti<T, kTile>(g, Fs, Linv + f.linv_base[s], xs, xb + f.idx_off[s], scratch,
+                                  &s_done, blk, f.error);
+          __syncthreads();
         }
-        Signal(bwd_done + s, 1);
+        for (int q = threadIdx.x; q < g.w; q += blockDim.x)
+          if (OwnsRow(g, kTile, q, blk, kp, ku)) {
+            St(xperm + idx[q], xs[q]);
+            x[f.scalar_old[idx[q]]] = xs[q];
+          }
+        SignalAdd(bwd_done + s);
       }
     }
     __syncthreads();
@@ -1727,12 +1941,17 @@ __global__ void AccumulateKernel(const T* dx, double* y, int64_t n, const int* g
 }
 
 __global__ void ResetFactorStateKernel(int* tile_state, int nstates, int* front_flags, int nflags,
-                                       int* counters, const int* gate) {
+                                       int* counters, const int* gate, unsigned* unset,
+                                       int64_t unset_words, int elem) {
   if (gate && *gate == 0) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nstates; i += gridDim.x * blockDim.x)
     tile_state[i] = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nflags; i += gridDim.x * blockDim.x)
     front_flags[i] = 0;
+  // the unset pattern of IsUnset: 0x7FF4DEAD0BADF00D (double, low word first), 0x7FA5DEAD (float)
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < unset_words;
+       i += int64_t(gridDim.x) * blockDim.x)
+    unset[i] = elem == 8 ? ((i & 1) ? 0x7FF4DEADu : 0x0BADF00Du) : 0x7FA5DEADu;
   if (blockIdx.x == 0 && threadIdx.x < 2) counters[threadIdx.x] = 0;
 }
 
@@ -1746,12 +1965,14 @@ __global__ void NegateKernel(const T* x, double* u, int64_t n) {
 }  // namespace
 
 void LaunchResetFactorState(int* tile_state, int nstates, int* front_flags, int nflags,
-                            int* counters, cudaStream_t s, const int* gate) {
+                            int* counters, cudaStream_t s, const int* gate, void* unset,
+                            int64_t n_unset, int elem) {
   const int threads = 256;
-  int grid = (std::max(nstates, nflags) + threads - 1) / threads;
-  grid = std::min(std::max(grid, 1), 1024);
+  const int64_t words = unset ? n_unset * elem / 4 : 0;
+  int64_t work = std::max<int64_t>(std::max(nstates, nflags), words);
+  const int grid = int(std::min<int64_t>(std::max<int64_t>((work + threads - 1) / threads, 1), 1024));
   ResetFactorStateKernel<<<grid, threads, 0, s>>>(tile_state, nstates, front_flags, nflags, counters,
-                                                  gate);
+                                                  gate, static_cast<unsigned*>(unset), words, elem);
 }
 
 template <typename T>
@@ -1809,6 +2030,8 @@ cudaError_t LaunchWaitCapSelfTest(const int* flag, int* err, cudaStream_t s) {
   WaitCapSelfTestKernel<<<1, 32, 0, s>>>(flag, err);
   return cudaGetLastError();
 }
+
+int SolveWarps() { return kSolveThreads / 32; }
 
 template <typename T>
 void ConfigureSolve(int max_m) {
@@ -1877,11 +2100,12 @@ void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void
 
 template <typename T>
 void LaunchSolve(const FactorDev& f, const void* F, const void* Linv, const void* b, void* ycon,
-                 void* ysave, void* xperm, void* x, int grid, cudaStream_t s) {
+                 void* ysave, void* xperm, void* x, void* xb, int grid, cudaStream_t s) {
   const size_t smem = SolveSmemBytes<T>(f.max_m);
   SolveKernel<T><<<grid, kSolveThreads, smem, s>>>(
       f, static_cast<const T*>(F), static_cast<const T*>(Linv), static_cast<const T*>(b),
-      static_cast<T*>(ycon), static_cast<T*>(ysave), static_cast<T*>(xperm), static_cast<T*>(x));
+      static_cast<T*>(ycon), static_cast<T*>(ysave), static_cast<T*>(xperm), static_cast<T*>(x),
+      static_cast<T*>(xb));
 }
 
 template void LaunchSchurPoints<double>(const SchurDev&, const void*, const void*, int64_t, int64_t,
@@ -1904,9 +2128,9 @@ template void LaunchFactor<double>(const FactorDev&, const void*, const double*,
                                    cudaStream_t);
 template void LaunchFactor<float>(const FactorDev&, const void*, const double*, void*, void*, int,
                                   cudaStream_t);
-template void LaunchSolve<double>(const FactorDev&, const void*, const void*, const void*, void*, void*,
+template void LaunchSolve<double>(const FactorDev&, const void*, const void*, const void*, void*, void*, void*,
                                   void*, void*, int, cudaStream_t);
-template void LaunchSolve<float>(const FactorDev&, const void*, const void*, const void*, void*, void*,
+template void LaunchSolve<float>(const FactorDev&, const void*, const void*, const void*, void*, void*, void*,
                                  void*, void*, int, cudaStream_t);
 
 }  // namespace sfg
