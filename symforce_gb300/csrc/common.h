@@ -172,6 +172,18 @@ struct TaskPlan {
 // tc_updates: runs of trailing updates go to tensor-core tasks (FP32 tiles of 32).
 TaskPlan PlanTasks(const Symbolic& sym, int tile, bool separate_inverse, bool tc_updates);
 
+// Split of the front triangular solves over CTAs: a front with more tiles than a solve CTA has
+// warps gets kp pivot-block CTAs of block_tiles pivot tiles and ku CTAs of as many update-row tiles
+// (kp = 0: one CTA per direction).  Tasks are (front, sub-task): forward ones in front order (a
+// front's blocks in order, then its update CTAs), then backward ones in reverse front order (a
+// front's blocks from the last one down), so that every sub-task waits only on lower task numbers.
+// Empty task lists when no front is split.
+struct SolveSplit {
+  std::vector<int32_t> kp, ku, task_front, task_sub;
+  int nf = 0;  // forward tasks
+};
+SolveSplit PlanSolveSplit(const TaskPlan& plan, int ns, int warps, int block_tiles, bool split);
+
 // Flattened per-(front, tile column) assembly lists, extend-add rounds and solve maps of a
 // symbolic factorization and its task plan, as the device kernels read them.
 struct FactorMaps {

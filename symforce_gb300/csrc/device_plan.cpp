@@ -94,40 +94,16 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
   // SFG_SOLVE_SPLIT=0.
   bool split = elem == 8;
   if (const char* e = std::getenv("SFG_SOLVE_SPLIT")) split = split && std::atoi(e) != 0;
-  std::vector<int32_t> kp(size_t(S.ns), 0), ku(size_t(S.ns), 0), task_front, task_sub;
-  int64_t nsplit = 0;
-  for (int s = 0; s < S.ns; ++s) {
-    const int np = T.npiv[size_t(s)], nu = T.ntiles[size_t(s)] - np;
-    if (split && np > 0 && np + nu > SolveWarps()) {
-      kp[size_t(s)] = (np + kSolveBlockTiles - 1) / kSolveBlockTiles;
-      ku[size_t(s)] = (nu + kSolveBlockTiles - 1) / kSolveBlockTiles;
-      ++nsplit;
-    }
-  }
+  const SolveSplit sp = PlanSolveSplit(T, S.ns, SolveWarps(), kSolveBlockTiles, split);
   int ntasks_solve = 2 * S.ns;
-  if (nsplit > 0) {
-    for (int s = 0; s < S.ns; ++s) {
-      const int k = kp[size_t(s)] > 0 ? kp[size_t(s)] + ku[size_t(s)] : 1;
-      for (int c = 0; c < k; ++c) {
-        task_front.push_back(s);
-        task_sub.push_back(c);
-      }
-    }
-    const int nf = int(task_front.size());
-    for (int s = S.ns - 1; s >= 0; --s) {
-      const int k = kp[size_t(s)] > 0 ? kp[size_t(s)] : 1;
-      for (int c = 0; c < k; ++c) {
-        task_front.push_back(s);
-        task_sub.push_back(c);
-      }
-    }
-    f.solve_front = A.Upload(task_front);
-    f.solve_sub = A.Upload(task_sub);
-    f.solve_kp = A.Upload(kp);
-    f.solve_ku = A.Upload(ku);
-    f.solve_nf = nf;
-    f.solve_nb = int(task_front.size()) - nf;
-    ntasks_solve = int(task_front.size());
+  if (!sp.task_front.empty()) {
+    f.solve_front = A.Upload(sp.task_front);
+    f.solve_sub = A.Upload(sp.task_sub);
+    f.solve_kp = A.Upload(sp.kp);
+    f.solve_ku = A.Upload(sp.ku);
+    f.solve_nf = sp.nf;
+    f.solve_nb = int(sp.task_front.size()) - sp.nf;
+    ntasks_solve = int(sp.task_front.size());
   }
   const int per_sm = 8;
   // the factorization kernel is built for kFactorCtasPerSm resident CTAs of 128 threads per SM

@@ -839,4 +839,36 @@ FactorMaps BuildFactorMaps(const Symbolic& S, const TaskPlan& T, const BlockPatt
   return M;
 }
 
+SolveSplit PlanSolveSplit(const TaskPlan& plan, int ns, int warps, int block_tiles, bool split) {
+  SolveSplit out;
+  out.kp.assign(size_t(ns), 0);
+  out.ku.assign(size_t(ns), 0);
+  bool any = false;
+  for (int s = 0; s < ns; ++s) {
+    const int np = plan.npiv[size_t(s)], nu = plan.ntiles[size_t(s)] - np;
+    if (split && np > 0 && np + nu > warps) {
+      out.kp[size_t(s)] = (np + block_tiles - 1) / block_tiles;
+      out.ku[size_t(s)] = (nu + block_tiles - 1) / block_tiles;
+      any = true;
+    }
+  }
+  if (!any) return out;
+  for (int s = 0; s < ns; ++s) {
+    const int k = out.kp[size_t(s)] > 0 ? out.kp[size_t(s)] + out.ku[size_t(s)] : 1;
+    for (int c = 0; c < k; ++c) {
+      out.task_front.push_back(s);
+      out.task_sub.push_back(c);
+    }
+  }
+  out.nf = int(out.task_front.size());
+  for (int s = ns - 1; s >= 0; --s) {
+    const int k = out.kp[size_t(s)] > 0 ? out.kp[size_t(s)] : 1;
+    for (int c = 0; c < k; ++c) {
+      out.task_front.push_back(s);
+      out.task_sub.push_back(c);
+    }
+  }
+  return out;
+}
+
 }  // namespace sfg

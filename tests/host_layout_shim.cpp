@@ -247,4 +247,19 @@ void shim_precond_arrays(int32_t* gidx, int64_t* blk_off, int32_t* gptr, int32_t
   Put(g_pre.gent, gent);
 }
 
+// Split of the front solves (block_tiles pivot tiles a CTA, `warps` warps a CTA) of the factor
+// plan built last: out = {forward tasks, all tasks}; then shim_solve_split_arrays.
+static sfg::SolveSplit g_split;
+void shim_solve_split(int warps, int block_tiles, int64_t* out) {
+  g_split = sfg::PlanSolveSplit(g_plan, g_sym.ns, warps, block_tiles, true);
+  out[0] = g_split.nf;
+  out[1] = int64_t(g_split.task_front.size());
+}
+void shim_solve_split_arrays(int32_t* kp, int32_t* ku, int32_t* task_front, int32_t* task_sub) {
+  Put(g_split.kp, kp);
+  Put(g_split.ku, ku);
+  Put(g_split.task_front, task_front);
+  Put(g_split.task_sub, task_sub);
+}
+
 }  // extern "C"

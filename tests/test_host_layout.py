@@ -612,3 +612,133 @@ def test_plans_of_random_factor_graphs(shim, seed):
         b = rng.normal(size=n)
         x = _replay_numeric(plan, mp, pool, n, vals, shift, b)
         np.testing.assert_allclose(x, np.linalg.solve(Ad + np.diag(shift), b), rtol=1e-9, atol=1e-12)
+
+
+def _replay_split_solve(fronts, kp, ku, task_front, task_sub, nf, block_tiles, tile, rng):
+    """The split front solves of SolveKernel (kernels_solve.cu: OwnsRow, ForwardMulti, BackwardMulti)
+    run in task order on random unit-lower fronts.  A value another CTA owns is read from the
+    exchange buffer, which holds NaN (the unset pattern) until its owner stores it, so a task that
+    needs a value of a later task fails the replay: every wait is on a lower task number.  Each
+    front's forward and backward results must equal dense triangular solves."""
+    P = block_tiles
+    state = {}
+    for s, (w, m) in enumerate(fronts):
+        np_, nu = -(-w // tile), -(-(m - w) // tile)
+        L = np.tril(rng.normal(size=(m, m)) * 0.2, -1) + np.eye(m)
+        state[s] = dict(w=w, m=m, np=np_, nt=np_ + nu, L=L, b=rng.normal(size=m), z=rng.normal(size=w),
+                        y=np.full(w, np.nan), upd=np.full(m - w, np.nan), xe=np.full(w, np.nan),
+                        fwd_done=0, bwd_done=0)
+
+    def owns(st, q, cta, k_p, k_u):
+        if k_p == 0:
+            return True
+        if cta < k_p:
+            return q < st["w"] and q // (tile * P) == cta
+        return q >= st["w"] and ((q - st["w"]) // tile) % k_u == cta - k_p
+
+    def tstart(st, t):
+        return t * tile if t < st["np"] else st["w"] + (t - st["np"]) * tile
+
+    def tsize(st, t):
+        return min(tile, st["w"] - t * tile) if t < st["np"] else min(tile, st["m"] - tstart(st, t))
+
+    for t in range(len(task_front)):
+        s, c = int(task_front[t]), int(task_sub[t])
+        st, k_p, k_u = state[s], int(kp[s]), int(ku[s])
+        w, m, np_, nt, L = st["w"], st["m"], st["np"], st["nt"], st["L"]
+        if t < nf:
+            assert 0 <= c < (k_p + k_u if k_p else 1)
+            xs = np.array([st["b"][q] if owns(st, q, c, k_p, k_u) else np.nan for q in range(m)])
+            if k_p == 0 or c < k_p:
+                tiles = range(np_) if k_p == 0 else range(c * P, min(c * P + P, np_))
+                for i in tiles:
+                    ri, bi = i * tile, tsize(st, i)
+                    for j in range(i):
+                        cj, bj = j * tile, tsize(st, j)
+                        # earlier blocks' values come from the exchange buffer
+                        yj = st["y"][cj:cj + bj] if (k_p == 0 or j < c * P) else xs[cj:cj + bj]
+                        assert not np.isnan(yj).any(), f"task {t} waits on an unsolved tile {j}"
+                        xs[ri:ri + bi] -= L[ri:ri + bi, cj:cj + bj] @ yj
+                    xs[ri:ri + bi] = np.linalg.solve(L[ri:ri + bi, ri:ri + bi], xs[ri:ri + bi])
+                    st["y"][ri:ri + bi] = xs[ri:ri + bi]
+                if k_p == 0:  # the one-CTA solve also forms the update rows
+                    for i in range(np_, nt):
+                        ri, bi = tstart(st, i), tsize(st, i)
+                        xs[ri:ri + bi] -= L[ri:ri + bi, :w] @ st["y"]
+            else:
+                for i in range(np_ + (c - k_p), nt, k_u):
+                    ri, bi = tstart(st, i), tsize(st, i)
+                    assert ri >= w and ri + bi <= m
+                    for j in range(np_):
+                        cj, bj = j * tile, tsize(st, j)
+                        yj = st["y"][cj:cj + bj]
+                        assert not np.isnan(yj).any(), f"task {t} waits on an unsolved tile {j}"
+                        xs[ri:ri + bi] -= L[ri:ri + bi, cj:cj + bj] @ yj
+            for q in range(w, m):
+                if owns(st, q, c, k_p, k_u):
+                    assert np.isnan(st["upd"][q - w])
+                    st["upd"][q - w] = xs[q]
+            st["fwd_done"] += 1
+        else:
+            k_b = k_p if k_p else 1
+            assert 0 <= c < k_b
+            assert st["fwd_done"] == (k_p + k_u if k_p else 1), f"front {s} backward before its forward"
+            blk = k_p - 1 - c
+            tiles = range(np_ - 1, -1, -1) if k_p == 0 else range(min(blk * P + P, np_) - 1, blk * P - 1, -1)
+            top = np_ - 1 if k_p == 0 else min(blk * P + P, np_) - 1
+            xs = st["z"].copy()
+            for j in tiles:
+                cj, bj = j * tile, tsize(st, j)
+                for i in range(np_ - 1, j, -1):
+                    ri, bi = i * tile, tsize(st, i)
+                    xi = st["xe"][ri:ri + bi] if i > top else xs[ri:ri + bi]
+                    assert not np.isnan(xi).any(), f"task {t} waits on an unsolved tile {i}"
+                    xs[cj:cj + bj] -= L[ri:ri + bi, cj:cj + bj].T @ xi
+                xs[cj:cj + bj] = np.linalg.solve(L[cj:cj + bj, cj:cj + bj].T, xs[cj:cj + bj])
+                assert np.isnan(st["xe"][cj:cj + bj]).all()
+                st["xe"][cj:cj + bj] = xs[cj:cj + bj]
+            st["bwd_done"] += 1
+    for s, st in state.items():
+        w, L = st["w"], st["L"]
+        ref = np.linalg.solve(L[:w, :w], st["b"][:w])
+        np.testing.assert_allclose(st["y"], ref, rtol=1e-9, atol=1e-11)
+        np.testing.assert_allclose(st["upd"], st["b"][w:] - L[w:, :w] @ ref, rtol=1e-9, atol=1e-11)
+        np.testing.assert_allclose(st["xe"], np.linalg.solve(L[:w, :w].T, st["z"]), rtol=1e-9, atol=1e-11)
+
+
+@pytest.mark.parametrize("warps,block_tiles", [(8, 4), (2, 1), (2, 2), (3, 3)])
+def test_split_front_solves(shim, warps, block_tiles):
+    """Fronts with more tiles than a solve CTA has warps are split over pivot-block and update-row
+    CTAs (host_structure.cpp PlanSolveSplit); the split tasks, replayed in task order, solve every
+    front as dense triangular solves do, and every wait is on an earlier task (no deadlock).  The
+    tree order holds too: a front's forward tasks come after its children's, its backward tasks
+    after its parent's.  (8, 4) is the device's split; the smaller ones split the small fronts."""
+    p = synth.bundle_adjustment(num_cameras=80, num_points=2000, num_observations=8000, seed=5)
+    c = p.to_c()
+    assert shim.shim_build(C.byref(c)) == 0 and shim.shim_build_schur() == 0
+    tile = 16
+    tasks, npiv, ntiles, parent, w, m, cptr, clist = _factor_plan(shim, 1, tile)
+    ns = len(npiv)
+    out = _arr(2, np.int64)
+    shim.shim_solve_split(warps, block_tiles, _ptr(out))
+    nf, ntot = int(out[0]), int(out[1])
+    kp, ku = _arr(ns, np.int32), _arr(ns, np.int32)
+    tf, tsub = _arr(max(ntot, 1), np.int32), _arr(max(ntot, 1), np.int32)
+    shim.shim_solve_split_arrays(*(_ptr(a) for a in (kp, ku, tf, tsub)))
+    split = [s for s in range(ns) if npiv[s] + 0 > 0 and ntiles[s] > warps]
+    assert [s for s in range(ns) if kp[s] > 0] == split
+    assert len(split) > 0 and ntot > 0
+    for s in split:
+        assert kp[s] == -(-int(npiv[s]) // block_tiles)
+        assert ku[s] == -(-(int(ntiles[s]) - int(npiv[s])) // block_tiles)
+    first_fwd = {int(s): i for i, s in reversed(list(enumerate(tf[:nf])))}
+    last_fwd = {int(s): i for i, s in enumerate(tf[:nf])}
+    first_bwd = {int(s): nf + i for i, s in reversed(list(enumerate(tf[nf:ntot])))}
+    last_bwd = {int(s): nf + i for i, s in enumerate(tf[nf:ntot])}
+    for s in range(ns):
+        for q in range(cptr[s], cptr[s + 1]):
+            assert last_fwd[int(clist[q])] < first_fwd[s]
+        if parent[s] >= 0:
+            assert last_bwd[int(parent[s])] < first_bwd[s]
+    fronts = [(int(w[s]), int(m[s])) for s in range(ns)]
+    _replay_split_solve(fronts, kp, ku, tf[:ntot], tsub[:ntot], nf, block_tiles, tile, np.random.default_rng(11))
