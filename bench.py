@@ -36,6 +36,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 from pathlib import Path
@@ -595,6 +596,12 @@ def run_profile(args) -> None:
     params = w.params()
     if args.profile_iterations > 0:
         params.iterations = args.profile_iterations
+    trace_path = None
+    if args.profile_pcg_trace:
+        # iteration trace of the PCG kernel's CTA 0 (read back after the runs)
+        trace_path = os.path.join(tempfile.mkdtemp(), "pcg_trace.bin")
+        os.environ["SFG_TRACE_PCG"] = "1"
+        os.environ["SFG_TRACE_PCG_FILE"] = trace_path
     opt = Optimizer(p, _form_params(params, args.profile_form), _make_form(w, args.profile_form, 0))
     if args.profile_fronts:
         width, size = opt.fronts()
@@ -610,6 +617,20 @@ def run_profile(args) -> None:
         print(f"{args.profile_workload} {args.profile_form}: {len(stats.iterations)} records, best "
               f"{stats.best_error:.10g}, {stats.device_ms:.3f} ms, {stats.kernel_launches} kernels",
               flush=True)
+    if trace_path:
+        opt.pcg_stats()  # writes the trace of the last solve
+        tr = np.fromfile(trace_path, dtype=np.uint64)
+        n = min(int(tr[0]), (len(tr) - 1) // 4)
+        st = tr[1:1 + 4 * n].astype(np.int64).reshape(n, 4)
+        if n > 1:
+            ph = np.empty((n - 1, 4))
+            ph[:, 0] = st[1:, 0] - st[:-1, 3]  # product with S (from the previous iteration's end)
+            ph[:, 1:] = np.diff(st[1:], axis=1)  # first reduction, preconditioner + update, second reduction
+            med = np.median(ph, axis=0) / 1e3
+            print(f"{args.profile_workload} {args.profile_form}: last solve {n} CG iterations, "
+                  f"{(st[-1, 3] - st[0, 0]) / 1e3 / (n - 1):.2f} us each (CTA 0); median us: product with S "
+                  f"{med[0]:.2f}, grid reduction p.Sp {med[1]:.2f}, update + preconditioner {med[2]:.2f}, "
+                  f"grid reduction r.z {med[3]:.2f}", flush=True)
     opt.close()
 
 
@@ -630,6 +651,8 @@ def main() -> None:
     ap.add_argument("--profile-runs", type=int, default=2)
     ap.add_argument("--profile-iterations", type=int, default=-1,
                     help="LM iteration cap in profiling mode (default: the workload's)")
+    ap.add_argument("--profile-pcg-trace", action="store_true",
+                    help="profiling mode (PCG forms): per-phase times of the last solve's CG iterations")
     ap.add_argument("--profile-fronts", action="store_true",
                     help="profiling mode: print the sizes of the factorization's fronts")
     args = ap.parse_args()

@@ -548,6 +548,10 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
       c.gauge_soff = A.Upload(PL.gauge_soff);
       c.gauge_comp = A.Upload(PL.gauge_comp);
     }
+    if (const char* tr = std::getenv("SFG_TRACE_PCG"); tr && tr[0] == '1') {
+      c.trace_cap = 4096;
+      c.trace = A.Zeros<unsigned long long>(1 + 4 * size_t(c.trace_cap));
+    }
     c.bar = A.Zeros<unsigned>(2);
     c.ps = h->ps;
     c.err = err_word;
@@ -1089,6 +1093,16 @@ int32_t sfg_get_pcg_stats(sfg_handle* h, sfg_pcg_stats_t* out) {
     out->last_iterations = ps.iterations;
     out->max_rel_residual = ps.max_rel_residual;
     out->last_rel_residual = ps.rel_residual;
+    // the iteration trace of the last solve (SFG_TRACE_PCG=1), written to SFG_TRACE_PCG_FILE
+    const char* path = std::getenv("SFG_TRACE_PCG_FILE");
+    if (h->pcg.trace && path) {
+      std::vector<unsigned long long> tr(1 + 4 * size_t(h->pcg.trace_cap));
+      SFG_CUDA(cudaMemcpy(tr.data(), h->pcg.trace, tr.size() * 8, cudaMemcpyDeviceToHost));
+      if (FILE* fo = std::fopen(path, "wb")) {
+        std::fwrite(tr.data(), 8, tr.size(), fo);
+        std::fclose(fo);
+      }
+    }
   });
 }
 

@@ -307,6 +307,11 @@ struct PcgDev {
   void* szg;
   const int64_t* gauge_soff;  // [ng * 9] POSE3 storage offset of a pose row, -1 otherwise
   const int32_t* gauge_comp;  // [ng * 9] tangent component of a pose row
+  // optional iteration trace of CTA 0 (SFG_TRACE_PCG): [0] inner iterations of the last solve,
+  // then per inner iteration (up to trace_cap) the %globaltimer after the product with S, after
+  // the first grid reduction, after the preconditioner, after the second grid reduction
+  unsigned long long* trace = nullptr;
+  int trace_cap = 0;
 };
 constexpr int kGaugeDim = 7;      // world translation 3, rotation 3, scale 1
 constexpr int kPcgReduceMax = 32; // values one PCG grid reduction can carry

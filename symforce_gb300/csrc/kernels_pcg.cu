@@ -509,6 +509,15 @@ __device__ bool GaugeInverse(const double* g, double* E) {
   return true;
 }
 
+// One stamp of the optional iteration trace (CTA 0, thread 0).
+__device__ __forceinline__ void PcgStamp(const PcgDev& d, int it, int phase) {
+  if (d.trace && blockIdx.x == 0 && threadIdx.x == 0 && it < d.trace_cap) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    d.trace[1 + 4 * size_t(it) + phase] = t;
+  }
+}
+
 // Vector arithmetic in the matrix precision T (FP32 in the mixed form); inner products, CG scalars,
 // the residual passes and the stopping decisions in FP64.
 // SPLIT 1: three camera blocks per warp (lanes 9 q + a, row a of block q).  SPLIT 3: one camera
@@ -636,7 +645,7 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
     return z;
   };
   double y64 = 0.0;
-  int outer = 0;
+  int outer = 0, traced = 0;
   while (!sm.converged) {
     double r64 = vs;
     if (outer > 0) {
@@ -680,6 +689,7 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
     T p = T(0), qv = T(0), dx = T(0), beta = T(0);
     for (;;) {
       T w = CombineSplit<SPLIT>(in_group ? GroupRow<T, kStaged>(Sb, gent, e0, e1, SPLIT, a, zv) : T(0), a);
+      PcgStamp(d, traced, 0);
       if constexpr (kCoarse) {
 #pragma unroll
         for (int i = 0; i < kGaugeDim; ++i) w += (row_ok ? szg[i * nrows + gi] : T(0)) * T(sm.cg[i]);
@@ -691,12 +701,14 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
         if (!(pq > 0.0) || !(pq < 1e300) || !(fabs(rz) < 1e300)) sm.broke = 1;
         else sm.alpha = rz / pq;
       });
+      PcgStamp(d, traced, 1);
       if (sm.broke) break;
       const T alpha = T(sm.alpha);
       dx += alpha * p;
       r -= alpha * qv;
       zz = ApplyBlock(prow, r, gbase);
       if (store) StX<kStaged>(zv + gi, zz);
+      PcgStamp(d, traced, 2);
       if constexpr (kCoarse) {
         double rv[2 + kGaugeDim];
         rv[0] = own ? double(r) * double(zz) : 0.0;
@@ -723,6 +735,7 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
         });
         zf = zz;
       }
+      PcgStamp(d, traced++, 3);
       if (sm.stop) break;
       beta = T(sm.beta);
     }
@@ -732,6 +745,7 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
     else __syncthreads();
   }
   if (own) __stcg(d.y + s, y64);
+  if (d.trace && blockIdx.x == 0 && threadIdx.x == 0) d.trace[0] = (unsigned long long)traced;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     PcgState* ps = d.ps;
     const int conv = sm.converged;
