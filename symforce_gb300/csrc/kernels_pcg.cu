@@ -224,24 +224,41 @@ __global__ void CollectSamplesKernel(PrecondDev pd, const float* feats, const fl
 // ---------------------------------------------------------------------------------------------
 // Barrier number `epoch` (1, 2, ... within the launch; kept by thread 0 of each CTA): arrive on
 // the counter, then wait until all nblocks CTAs have arrived epoch times.
+// Thread 0 only: arrive and wait.  The arrival is a release (the CTA's writes, ordered before it by
+// a CTA barrier, become visible with it) and the polls acquire, so no separate fences sit on the
+// path.
+__device__ void GridArriveWait(unsigned* bar, unsigned nblocks, unsigned& epoch, int* err) {
+  const unsigned target = ++epoch * nblocks;
+  asm volatile("red.release.gpu.global.add.u32 [%0], 1;" : : "l"(bar) : "memory");
+  unsigned it = 0, count;
+  for (;;) {
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(count) : "l"(bar) : "memory");
+    if (count >= target) break;
+    if (++it > kSpinLimit) {
+      atomicExch(err, kDevSpinTimeout);
+      break;
+    }
+    if ((it & 63) == 0 && *reinterpret_cast<volatile int*>(err) != 0) break;
+  }
+}
 __device__ void GridBarrier(unsigned* bar, unsigned nblocks, unsigned& epoch, int* err) {
   __syncthreads();
-  if (threadIdx.x == 0) {
-    const unsigned target = ++epoch * nblocks;
-    __threadfence();
-    atomicAdd(bar, 1u);
-    volatile unsigned* count = bar;
-    unsigned it = 0;
-    while (*count < target) {
-      if (++it > kSpinLimit) {
-        atomicExch(err, kDevSpinTimeout);
-        break;
-      }
-      if ((it & 63) == 0 && *reinterpret_cast<volatile int*>(err) != 0) break;
-    }
-    __threadfence();
-  }
+  if (threadIdx.x == 0) GridArriveWait(bar, nblocks, epoch, err);
   __syncthreads();
+}
+
+// 1 / x for the CG scalars: the hardware's approximate FP64 reciprocal and two Newton-Raphson
+// steps (on this GPU one FP64 division costs ~560 cycles, one dependent FP64 operation ~64);
+// inputs outside the range where the approximation is normal take the IEEE division.
+__device__ __forceinline__ double FastRecip(double x) {
+  const int ex = __double2hiint(x) & 0x7FF00000;
+  if (ex < 0x00200000 || ex >= 0x7FD00000) return 1.0 / x;
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
 }
 
 template <typename T>
@@ -343,7 +360,7 @@ __device__ __forceinline__ V CombineSplit(V x, int a) {
 
 struct PcgShared {
   double2 red[32];
-  double vnorm, target, rel;
+  double vnorm, target2, rel;
   double rz, alpha, beta;
   int iters, stop, broke, converged;
   unsigned epoch;  // grid barriers passed (thread 0 only)
@@ -379,19 +396,24 @@ __device__ __forceinline__ void GridReduce(Acc a, Acc b, const PcgDev& d, int& s
   if (warp == 0) {
     Acc ta = lane < nwarp ? red[2 * lane] : Acc(0);
     Acc tb = lane < nwarp ? red[2 * lane + 1] : Acc(0);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      ta += __shfl_down_sync(0xffffffffu, ta, o);
-      tb += __shfl_down_sync(0xffffffffu, tb, o);
+    // as many levels as the CTA has warps need (nwarp <= 2^levels)
+    for (int o = 1; o < nwarp; o <<= 1) {
+      const Acc ua = __shfl_xor_sync(0xffffffffu, ta, o);
+      const Acc ub = __shfl_xor_sync(0xffffffffu, tb, o);
+      ta += ua;  // a butterfly: every lane ends with the same bits
+      tb += ub;
     }
     if (lane == 0) {
       if (grid == 1) epi(ta, tb);
       else __stcg(part + blockIdx.x, make_double2(double(ta), double(tb)));
     }
   }
-  if (grid > 1) {
-    GridBarrier(d.bar, grid, sm.epoch, d.err);
-    if (warp == 0) {
+  if (grid > 1 && warp == 0) {
+    // thread 0 stored the partial after the CTA barrier that ordered every thread's writes before
+    // it; only warp 0 needs the others' partials
+    if (lane == 0) GridArriveWait(d.bar, grid, sm.epoch, d.err);
+    __syncwarp();
+    {
       // four partials per lane in flight at once, added in CTA order
       double ta = 0.0, tb = 0.0;
       for (int q0 = lane; q0 < grid; q0 += 128) {
@@ -405,10 +427,11 @@ __device__ __forceinline__ void GridReduce(Acc a, Acc b, const PcgDev& d, int& s
           tb += v[u].y;
         }
       }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        ta += __shfl_down_sync(0xffffffffu, ta, o);
-        tb += __shfl_down_sync(0xffffffffu, tb, o);
+      for (int o = 1; o < min(grid, 32); o <<= 1) {
+        const double ua = __shfl_xor_sync(0xffffffffu, ta, o);
+        const double ub = __shfl_xor_sync(0xffffffffu, tb, o);
+        ta += ua;
+        tb += ub;
       }
       if (lane == 0) epi(Acc(ta), Acc(tb));
     }
@@ -449,9 +472,10 @@ __device__ __forceinline__ void GridReduceN(double (&v)[N], const PcgDev& d, int
     __syncwarp();
     if (grid == 1 && lane == 0) epi(sums);
   }
-  if (grid > 1) {
-    GridBarrier(d.bar, grid, sm.epoch, d.err);
-    if (warp == 0) {
+  if (grid > 1 && warp == 0) {
+    if (lane == 0) GridArriveWait(d.bar, grid, sm.epoch, d.err);
+    __syncwarp();
+    {
       // lane l takes the CTAs l, l + 32, ... (all N values each, the loads in flight together),
       // then a warp tree per value: a fixed order, the same bits in every CTA
       double t[N];
@@ -460,12 +484,12 @@ __device__ __forceinline__ void GridReduceN(double (&v)[N], const PcgDev& d, int
       for (int q = lane; q < grid; q += 32)
 #pragma unroll
         for (int n = 0; n < N; ++n) t[n] += __ldcg(part + size_t(q) * kPcgReduceMax + n);
+      for (int o = 1; o < min(grid, 32); o <<= 1)
 #pragma unroll
-      for (int n = 0; n < N; ++n) {
+        for (int n = 0; n < N; ++n) t[n] += __shfl_xor_sync(0xffffffffu, t[n], o);
+      if (lane == 0)
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t[n] += __shfl_down_sync(0xffffffffu, t[n], o);
-        if (lane == 0) sums[n] = t[n];
-      }
+        for (int n = 0; n < N; ++n) sums[n] = t[n];
       __syncwarp();
       if (lane == 0) epi(sums);
     }
@@ -658,7 +682,8 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
       sm.converged = sm.rel <= d.tol ? 1 : 0;
       sm.stop = (sm.converged || outer >= d.max_outer || sm.iters >= d.max_iters || sm.broke ||
                  !(sm.rel == sm.rel)) ? 1 : 0;
-      sm.target = fmax(0.5 * d.tol * vnorm, d.inner_floor * sqrt(x));
+      const double target = fmax(0.5 * d.tol * vnorm, d.inner_floor * sqrt(x));
+      sm.target2 = target * target;  // the inner solves stop once |r|^2 <= target^2
     });
     if (sm.stop) break;
     ++outer;
@@ -699,7 +724,7 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
       GridReduce<double>(own ? double(p) * double(qv) : 0.0, 0.0, d, seq, sm, [&](double pq, double) {
         const double rz = sm.rz;
         if (!(pq > 0.0) || !(pq < 1e300) || !(fabs(rz) < 1e300)) sm.broke = 1;
-        else sm.alpha = rz / pq;
+        else sm.alpha = rz * FastRecip(pq);
       });
       PcgStamp(d, traced, 1);
       if (sm.broke) break;
@@ -720,8 +745,8 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
           double rz = g[0];
           for (int i = 0; i < kGaugeDim; ++i) rz += sm.cg[i] * g[2 + i];
           sm.iters += 1;
-          sm.stop = (sqrt(g[1]) <= sm.target || sm.iters >= d.max_iters) ? 1 : 0;
-          sm.beta = rz / sm.rz;
+          sm.stop = (g[1] <= sm.target2 || sm.iters >= d.max_iters) ? 1 : 0;
+          sm.beta = rz * FastRecip(sm.rz);
           sm.rz = rz;
         });
         zf = z_plus_coarse(zz);
@@ -729,8 +754,8 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
         GridReduce<double>(own ? double(r) * double(zz) : 0.0, own ? double(r) * double(r) : 0.0, d, seq, sm,
                            [&](double rz, double rr) {
           sm.iters += 1;
-          sm.stop = (sqrt(rr) <= sm.target || sm.iters >= d.max_iters) ? 1 : 0;
-          sm.beta = rz / sm.rz;
+          sm.stop = (rr <= sm.target2 || sm.iters >= d.max_iters) ? 1 : 0;
+          sm.beta = rz * FastRecip(sm.rz);
           sm.rz = rz;
         });
         zf = zz;
