@@ -100,13 +100,24 @@ int SetupScratch(int device, Scratch** out) {
 
 // Copy the lower triangle of A into the front, reset the counters, and write the task list of one
 // dense front (panels: diagonal tile, panel solves, trailing updates; no assembly tasks, since the
-// tiles start out assembled).  One block; thread 0 writes the task list.
+// tiles start out assembled).  One block per column of A (n blocks): block c copies column c's lower
+// part and, for c < nt, writes panel c's tasks from its closed-form offset in the list; block 0
+// also writes the plan's scalars.
 __global__ void PrepareKernel(int n, const double* A, int64_t lda) {
   const int nt = (n + kTile - 1) / kTile;
-  for (int64_t e = threadIdx.x; e < int64_t(n) * n; e += blockDim.x) {
-    const int r = int(e % n), c = int(e / n);
-    if (r >= c) g_front[e] = A[r + int64_t(c) * lda];
+  const int c = blockIdx.x;
+  for (int r = c + threadIdx.x; r < n; r += blockDim.x) g_front[r + int64_t(c) * n] = A[r + int64_t(c) * lda];
+  if (c < nt && threadIdx.x == 0) {
+    // tasks of the panels before k: 1 + (nt - k' - 1) + (nt - k' - 1)(nt - k') / 2 each
+    int t = 0;
+    for (int k = 0; k < c; ++k) t += 1 + (nt - k - 1) + (nt - k - 1) * (nt - k) / 2;
+    const int k = c;
+    g_tasks[t++] = make_int4(sfg::kTaskDiag, 0, k * 65536 + k, k);
+    for (int i = k + 1; i < nt; ++i) g_tasks[t++] = make_int4(sfg::kTaskTrsm, 0, i * 65536 + k, k);
+    for (int j = k + 1; j < nt; ++j)
+      for (int i = j; i < nt; ++i) g_tasks[t++] = make_int4(sfg::kTaskUpdate, 0, i * 65536 + j, k);
   }
+  if (c != 0) return;
   for (int q = threadIdx.x; q < nt * (nt + 1) / 2; q += blockDim.x) g_tile_state[q] = 1;
   for (int q = threadIdx.x; q < n; q += blockDim.x) g_ident[q] = q;
   if (threadIdx.x == 0) {
@@ -134,13 +145,6 @@ __global__ void PrepareKernel(int n, const double* A, int64_t lda) {
     m.rel_off[0] = m.rel_off[1] = 0;
     m.idx_off[0] = 0;
     m.idx_off[1] = n;
-    int t = 0;
-    for (int k = 0; k < nt; ++k) {
-      g_tasks[t++] = make_int4(sfg::kTaskDiag, 0, k * 65536 + k, k);
-      for (int i = k + 1; i < nt; ++i) g_tasks[t++] = make_int4(sfg::kTaskTrsm, 0, i * 65536 + k, k);
-      for (int j = k + 1; j < nt; ++j)
-        for (int i = j; i < nt; ++i) g_tasks[t++] = make_int4(sfg::kTaskUpdate, 0, i * 65536 + j, k);
-    }
   }
 }
 
@@ -233,7 +237,7 @@ extern "C" int32_t sfg_dense_ldlt_solve_noalloc(int32_t n, const double* A, int6
     sfg::g_last_error = "sfg_dense_ldlt_solve_noalloc: task list exceeds its scratch";
     return SFG_ERR_CAPACITY;
   }
-  PrepareKernel<<<1, 256, 0, st>>>(n, A, lda);
+  PrepareKernel<<<n, 128, 0, st>>>(n, A, lda);
   sfg::LaunchFactor<double>(f, s->front, nullptr, s->front, s->linv,
                             std::max(1, std::min(ntasks, sms * 8)), st);
   sfg::LaunchSolve<double>(f, s->front, s->linv, b, s->vec + 2 * kMaxN, s->vec, s->vec + kMaxN, x, nullptr,

@@ -194,3 +194,33 @@ def test_compute_covariances_matches_dense_inverse():
         blk = ref[offs[k]:offs[k + 1], offs[k]:offs[k + 1]]
         np.testing.assert_allclose(cov[k], blk, rtol=1e-6, atol=1e-9 * np.abs(blk).max())
         np.testing.assert_allclose(cov[k], cov[k].T, rtol=0, atol=1e-12 * np.abs(blk).max())
+
+
+@pytest.mark.parametrize("case", ["bundle_adjustment", "pose_smoothing"])
+def test_dense_linearization_matches_oracle(case):
+    """DenseLinearizer adapter (Optimizer.linearize_dense; symforce/opt/dense_linearizer.h): the
+    device's residual, dense lower Hessian (upper triangle zero), rhs and error against the CPU
+    oracle's linearization at the same values, at 1e-9."""
+    if case == "bundle_adjustment":
+        p = synth.bundle_adjustment(num_cameras=6, num_points=40, num_observations=150, seed=2)
+    else:
+        p = R.pose_smoothing(O.pose_smoothing_initial_values())
+    opt = Optimizer(p)
+    got = opt.linearize_dense(p.values)
+    ref = O.linearize(p)
+    n = len(ref["rhs"])
+    Hd = np.zeros((n, n))
+    for j in range(n):
+        for q in range(int(ref["colptr"][j]), int(ref["colptr"][j + 1])):
+            Hd[int(ref["rowidx"][q]), j] = ref["hvals"][q]
+    Hd = np.tril(Hd + np.triu(Hd, 1).T)  # the oracle stores the lower triangle; keep it lower
+    H = got["hessian_lower"]
+    assert H.shape == (n, n)
+    assert np.all(np.triu(H, 1) == 0.0)
+    scale = max(1.0, np.abs(Hd).max())
+    np.testing.assert_allclose(H, Hd, rtol=1e-9, atol=1e-9 * scale)
+    np.testing.assert_allclose(got["rhs"], ref["rhs"], rtol=1e-9, atol=1e-9 * max(1.0, np.abs(ref["rhs"]).max()))
+    np.testing.assert_allclose(got["residual"], ref["residual"], rtol=1e-9,
+                               atol=1e-12 * max(1.0, np.abs(ref["residual"]).max()))
+    assert got["error"] == pytest.approx(0.5 * float(ref["residual"] @ ref["residual"]), rel=1e-9)
+    opt.close()
