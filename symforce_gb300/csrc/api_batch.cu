@@ -1,5 +1,6 @@
-// C ABI of the batched form: many independent Pose3-chain problems solved by one persistent kernel
-// launch (kernels_batch.cu), captured in a CUDA graph, with a launch-shape autotuner.
+// C ABI of the batched form: many independent problems solved by one persistent kernel launch
+// (kernels_batch.cu), captured in a CUDA graph, with a launch-shape autotuner.  Batches of Pose3
+// chains take the block-tridiagonal path; any other batch the dense path.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -24,6 +25,7 @@ struct sfg_batch {
   int nprob = 0;
   int nmax = 0;
   int64_t total_poses = 0;
+  int64_t total_storage = 0;  // doubles of all problems' values
   std::vector<int32_t> n_host;
   std::vector<int64_t> pose0_host;
   sfg::BatchLmDev d{};
@@ -85,6 +87,9 @@ void ToParams(const sfg_optimizer_params_t& p, int iterations, double eps, LmPar
   o->iterations = iterations;
 }
 
+void CreateChain(const sfg_problem_t* problems, int32_t num_problems, sfg_batch* b);
+void CreateDense(const sfg_problem_t* problems, int32_t num_problems, sfg_batch* b);
+
 void Create(const sfg_problem_t* problems, int32_t num_problems, const sfg_form_params_t* form,
             sfg_batch* b) {
   if (!problems || num_problems <= 0) throw Error(SFG_ERR_INVALID_ARGUMENT, "no problems");
@@ -102,6 +107,17 @@ void Create(const sfg_problem_t* problems, int32_t num_problems, const sfg_form_
   b->epsilon = fm.epsilon;
   SFG_CUDA(cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, fm.device));
   b->nprob = num_problems;
+  try {
+    CreateChain(problems, num_problems, b);
+  } catch (const Error& e) {
+    if (e.code != SFG_ERR_STRUCTURE) throw;
+    CreateDense(problems, num_problems, b);
+  }
+  SFG_CUDA(cudaDeviceSynchronize());
+}
+
+// Pose3 chains (throws SFG_ERR_STRUCTURE, before allocating anything, for any other problem).
+void CreateChain(const sfg_problem_t* problems, int32_t num_problems, sfg_batch* b) {
   // validate and flatten
   std::vector<int32_t> n(num_problems);
   std::vector<int64_t> pose0(num_problems);
@@ -118,6 +134,7 @@ void Create(const sfg_problem_t* problems, int32_t num_problems, const sfg_form_
     total += P.num_keys;
   }
   b->total_poses = total;
+  b->total_storage = total * 7;
   b->nmax = *std::max_element(n.begin(), n.end());
   std::vector<std::vector<std::pair<int, int64_t>>> un(total);   // (kind, const offset)
   std::vector<std::vector<std::pair<int, int64_t>>> bw(total);   // (rev, const offset)
@@ -193,16 +210,117 @@ void Create(const sfg_problem_t* problems, int32_t num_problems, const sfg_form_
   b->params = static_cast<LmParams*>(A.Alloc(sizeof(LmParams)));
   b->n_host = n;
   b->pose0_host = pose0;
+  d.dense = 0;
+  d.ws_stride = int64_t(kBatchWsPerPose) * b->nmax;
   // launch shape until the autotuner picks one: 8 warps per CTA, as many CTAs as fit
   b->shape = 0;
-  b->ctas = std::max(1, BatchMaxCtasPerSm(b->shape)) * b->num_sms;
-  SFG_CUDA(cudaDeviceSynchronize());
+  b->ctas = std::max(1, BatchMaxCtasPerSm(b->shape, false)) * b->num_sms;
+}
+
+// Any keys and factor kinds, tangent dimension up to kBatchDenseMaxN a problem, every factor's keys
+// distinct: the dense path.
+void CreateDense(const sfg_problem_t* problems, int32_t num_problems, sfg_batch* b) {
+  std::vector<int32_t> dn_n(num_problems), dn_s(num_problems), dn_k0(num_problems), dn_nk(num_problems);
+  std::vector<int64_t> dn_s0(num_problems), f_ptr(num_problems + 1, 0), f_coff, work(num_problems);
+  std::vector<int8_t> key_type, f_kind;
+  std::vector<int32_t> key_soff, key_toff, f_key;
+  std::vector<double> consts;
+  int64_t total_s = 0;
+  int nmax_t = 1, smax = 1;
+  for (int p = 0; p < num_problems; ++p) {
+    const sfg_problem_t& P = problems[p];
+    if (P.num_keys <= 0 || !P.key_types) throw Error(SFG_ERR_INVALID_ARGUMENT, "problem without keys");
+    dn_k0[p] = int32_t(key_type.size());
+    dn_nk[p] = P.num_keys;
+    dn_s0[p] = total_s;
+    int so = 0, to = 0;
+    for (int k = 0; k < P.num_keys; ++k) {
+      int sd = 0, td = 0;
+      KeyDims(P.key_types[k], &sd, &td);
+      key_type.push_back(int8_t(P.key_types[k]));
+      key_soff.push_back(so);
+      key_toff.push_back(to);
+      so += sd;
+      to += td;
+    }
+    if (to > kBatchDenseMaxN)
+      throw Error(SFG_ERR_STRUCTURE, "batched problem " + std::to_string(p) + " has tangent dimension " +
+                                         std::to_string(to) + ", more than the batched form's " +
+                                         std::to_string(kBatchDenseMaxN));
+    dn_n[p] = to;
+    dn_s[p] = so;
+    total_s += so;
+    nmax_t = std::max(nmax_t, to);
+    smax = std::max(smax, so);
+    int64_t nf = 0;
+    for (int bi = 0; bi < P.num_batches; ++bi) {
+      const sfg_factor_batch_t& B = P.batches[bi];
+      if (B.count == 0) continue;
+      if (B.count < 0 || !B.keys || (!B.consts && Spec(B.kind).nconsts > 0))
+        throw Error(SFG_ERR_INVALID_ARGUMENT, "bad factor batch");
+      const FactorSpec spec = Spec(B.kind);
+      if (spec.nkeys > kBatchDenseKeys) throw Error(SFG_ERR_STRUCTURE, "factor with too many keys");
+      for (int f = 0; f < B.count; ++f) {
+        const int32_t* k = B.keys + size_t(f) * spec.nkeys;
+        for (int q = 0; q < spec.nkeys; ++q) {
+          if (k[q] < 0 || k[q] >= P.num_keys) throw Error(SFG_ERR_INVALID_ARGUMENT, "factor key out of range");
+          if (P.key_types[k[q]] != spec.key_types[q])
+            throw Error(SFG_ERR_INVALID_ARGUMENT, "factor key of the wrong type");
+          for (int r = 0; r < q; ++r)
+            if (k[r] == k[q]) throw Error(SFG_ERR_STRUCTURE, "batched factors take distinct keys");
+        }
+        f_kind.push_back(int8_t(B.kind));
+        for (int q = 0; q < kBatchDenseKeys; ++q) f_key.push_back(q < spec.nkeys ? dn_k0[p] + k[q] : -1);
+        f_coff.push_back(int64_t(consts.size()));
+        consts.insert(consts.end(), B.consts + size_t(f) * spec.nconsts,
+                      B.consts + size_t(f + 1) * spec.nconsts);
+        ++nf;
+      }
+    }
+    f_ptr[p + 1] = int64_t(f_kind.size());
+    work[p] = int64_t(to) * to * to / 6 + 64 * nf;  // factorization + linearization
+  }
+  std::vector<int32_t> order(num_problems);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return work[a] > work[c]; });
+  SFG_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  DeviceArena& A = b->arena;
+  BatchLmDev& d = b->d;
+  d.nprob = num_problems;
+  d.nmax = 1;
+  d.dense = 1;
+  d.nmax_t = nmax_t;
+  d.smax = smax;
+  d.ws_stride = BatchDenseWsStride(nmax_t, smax);
+  d.order = A.Upload(order);
+  d.dn_n = A.Upload(dn_n);
+  d.dn_s = A.Upload(dn_s);
+  d.dn_s0 = A.Upload(dn_s0);
+  d.dn_k0 = A.Upload(dn_k0);
+  d.dn_nk = A.Upload(dn_nk);
+  d.key_type = A.Upload(key_type);
+  d.key_soff = A.Upload(key_soff);
+  d.key_toff = A.Upload(key_toff);
+  d.f_ptr = A.Upload(f_ptr);
+  d.f_kind = A.Upload(f_kind);
+  d.f_key = A.Upload(f_key);
+  d.f_coff = A.Upload(f_coff);
+  d.consts = A.Upload(consts);
+  d.values_in = A.Zeros<double>(size_t(total_s));
+  d.values_out = A.Zeros<double>(size_t(total_s));
+  d.st = A.Zeros<LmState>(size_t(num_problems));
+  d.counter = A.Zeros<int>(1);
+  b->params = static_cast<LmParams*>(A.Alloc(sizeof(LmParams)));
+  b->nmax = 1;
+  b->total_storage = total_s;
+  b->shape = 0;
+  b->ctas = std::max(1, BatchMaxCtasPerSm(b->shape, true)) * b->num_sms;
 }
 
 void EnsureWorkspace(sfg_batch* b, int ctas, int shape) {
   const size_t slots = size_t(ctas) * BatchShapeWarps(shape);
   if (slots <= b->ws_slots) return;
-  b->d.ws = static_cast<double*>(b->arena.Alloc(slots * kBatchWsPerPose * size_t(b->nmax) * sizeof(double)));
+  b->d.ws = static_cast<double*>(b->arena.Alloc(slots * size_t(b->d.ws_stride) * sizeof(double)));
   b->ws_slots = slots;
   b->graph_shape = -1;
 }
@@ -288,14 +406,14 @@ int32_t sfg_batch_destroy(sfg_batch* b) {
 
 int32_t sfg_batch_storage_dim(const sfg_batch* b, int64_t* storage_dim) {
   if (!b || !storage_dim) return SFG_ERR_INVALID_ARGUMENT;
-  *storage_dim = b->total_poses * 7;
+  *storage_dim = b->total_storage;
   return SFG_OK;
 }
 
 int32_t sfg_batch_set_values(sfg_batch* b, const double* storage, int64_t n) {
   return sfg::GuardB([&] {
     if (!b || !storage) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
-    if (n != b->total_poses * 7) throw Error(SFG_ERR_INVALID_ARGUMENT, "values size mismatch");
+    if (n != b->total_storage) throw Error(SFG_ERR_INVALID_ARGUMENT, "values size mismatch");
     SFG_CUDA(cudaSetDevice(b->device));
     SFG_CUDA(cudaMemcpyAsync(const_cast<double*>(b->d.values_in), storage, size_t(n) * 8,
                              cudaMemcpyHostToDevice, b->stream));
@@ -307,7 +425,7 @@ int32_t sfg_batch_set_values(sfg_batch* b, const double* storage, int64_t n) {
 int32_t sfg_batch_get_values(sfg_batch* b, double* storage, int64_t n) {
   return sfg::GuardB([&] {
     if (!b || !storage) throw Error(SFG_ERR_INVALID_ARGUMENT, "null argument");
-    if (n != b->total_poses * 7) throw Error(SFG_ERR_INVALID_ARGUMENT, "values size mismatch");
+    if (n != b->total_storage) throw Error(SFG_ERR_INVALID_ARGUMENT, "values size mismatch");
     SFG_CUDA(cudaSetDevice(b->device));
     SFG_CUDA(cudaMemcpyAsync(storage, b->d.values_out, size_t(n) * 8, cudaMemcpyDeviceToHost, b->stream));
     SFG_CUDA(cudaStreamSynchronize(b->stream));
@@ -371,7 +489,7 @@ int32_t sfg_batch_autotune(sfg_batch* b, const sfg_optimizer_params_t* params, i
     double best = 1e300;
     int bs = b->shape, bc = b->ctas;
     for (int shape = 0; shape < sfg::BatchShapes(); ++shape) {
-      const int per_sm = sfg::BatchMaxCtasPerSm(shape);
+      const int per_sm = sfg::BatchMaxCtasPerSm(shape, b->d.dense != 0);
       if (per_sm <= 0) continue;
       for (int frac : {1, 2}) {  // every resident CTA, or half of them
         if (frac == 2 && per_sm < 2) continue;

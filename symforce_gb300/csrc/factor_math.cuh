@@ -158,6 +158,32 @@ SFG_HD void RetractPose3(const double* a, const double* d, double eps, double* o
   o[6] = a[6] + d[5];
 }
 
+// Values::Retract of one key of any type (symforce/opt/values.cc:315-327): storage a, tangent
+// update d, result o.
+SFG_HD void RetractKey(int type, const double* a, const double* d, double eps, double* o) {
+  switch (type) {
+    case SFG_KEY_POSE2: {  // gen/cpp/sym/ops/pose2/lie_group_ops.cc:58-82
+      const double c = cos(d[0]), s = sin(d[0]);
+      const double re = a[0], im = a[1];
+      o[0] = re * c - im * s;
+      o[1] = re * s + im * c;
+      o[2] = a[2] + d[1];
+      o[3] = a[3] + d[2];
+      break;
+    }
+    case SFG_KEY_POSE3:  // gen/cpp/sym/ops/pose3/lie_group_ops.cc:69-102
+      RetractPose3(a, d, eps, o);
+      break;
+    case SFG_KEY_ROT3:  // gen/cpp/sym/ops/rot3/lie_group_ops.cc: the rotation part of the above
+      RetractRot3(a, d, eps, o);
+      break;
+    default: {  // VEC1..VEC3 = 1..3, VEC4..VEC6 = 7..9
+      const int n = type <= SFG_KEY_VEC3 ? type : type - SFG_KEY_VEC4 + 4;
+      for (int i = 0; i < n; ++i) o[i] = a[i] + d[i];
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // Factor evaluation: x[slot] points at the key storage, c at the constants (already loaded).
 // r: residual (double), J: RD x TD row-major (T).

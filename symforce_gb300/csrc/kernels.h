@@ -358,13 +358,41 @@ struct BatchLmDev {
   LmState* st;                 // [nprob]
   sfg_iteration_t* records;    // [nprob][rec_cap] (null: none)
   int rec_cap;
-  double* ws;                  // [slots][kBatchWsPerPose * nmax]
+  double* ws;                  // [slots][ws_stride]
   int* counter;                // problem queue head (zero before launch)
+  // Dense path (dense = 1: problems of any key and factor kinds that are not Pose3 chains; the
+  // chain arrays above are then unused): problem p has dn_nk[p] keys from global key dn_k0[p],
+  // tangent dimension dn_n[p] (at most kBatchDenseMaxN), storage dn_s[p] doubles at dn_s0[p] of
+  // the values, and factors f_ptr[p] .. f_ptr[p + 1] - 1 (kind, up to kBatchDenseKeys global key
+  // indices, -1 past the factor's keys, constants offset).
+  int dense;
+  int nmax_t, smax;            // largest tangent dimension / storage of a problem
+  int64_t ws_stride;           // doubles of one workspace slot
+  const int32_t* dn_n;
+  const int32_t* dn_s;
+  const int64_t* dn_s0;
+  const int32_t* dn_k0;
+  const int32_t* dn_nk;
+  const int8_t* key_type;      // [total keys]
+  const int32_t* key_soff;     // storage offset of the key within its problem
+  const int32_t* key_toff;     // tangent offset of the key within its problem
+  const int64_t* f_ptr;        // [nprob + 1]
+  const int8_t* f_kind;
+  const int32_t* f_key;        // [factors][kBatchDenseKeys]
+  const int64_t* f_coff;
 };
+constexpr int kBatchDenseMaxN = 128;  // largest tangent dimension of a dense-path problem
+constexpr int kBatchDenseKeys = 4;    // keys of a factor
+constexpr int kBatchDenseRd = 12;     // residual rows of a factor
+constexpr int kBatchDenseTd = 16;     // tangent columns of a factor
+// Doubles of one dense-path workspace slot for problems up to n tangent / s storage dimensions.
+inline int64_t BatchDenseWsStride(int n, int s) {
+  return 3 * int64_t(s) + 4 * int64_t(n) * n + 9 * int64_t(n) + 32 * (int64_t(kBatchDenseRd) * (kBatchDenseTd + 1) + 1);
+}
 // Launch shapes (kernel instantiations): warps per CTA x register budget.
 int BatchShapes();
 int BatchShapeWarps(int shape);
-int BatchMaxCtasPerSm(int shape);
+int BatchMaxCtasPerSm(int shape, bool dense);
 void LaunchBatchLm(const BatchLmDev& d, const LmParams* p, int ctas, int shape, cudaStream_t s);
 
 // ---------------------------------------------------------------- network training (kernels_mlp.cu)

@@ -273,7 +273,264 @@ __device__ void FactorSolve(const BatchLmDev& d, const Ws& w, int n, int s, int 
   }
 }
 
-template <int kWarps, int kMinBlocks>
+// ---------------------------------------------------------------------------------------------
+// Dense path: problems of any key and factor kinds (tangent dimension up to kBatchDenseMaxN), one
+// warp per problem as above, with the Hessian dense in the slot's workspace (L2-resident).
+//   - linearize: factors in rounds of 32, one lane each (residual and Jacobian into the slot's
+//     scratch), then the warp adds the round's J^T J / J^T r entries factor by factor in factor
+//     order (lanes over a factor's entries, which fall on distinct Hessian entries because a
+//     factor's keys are distinct): the same bits on every run, no atomics;
+//   - factor: right-looking LDL^T of H + D (the lanes over the trailing lower entries of a pivot),
+//     then column-oriented unit-lower solves and D^-1;
+//   - retract every key by its type, relinearize, decide (lm_logic.cuh, as the chain path).
+// ---------------------------------------------------------------------------------------------
+struct DnWs {
+  double *vals, *H, *F, *g, *damp, *maxd, *upd, *last, *y, *Js;
+};
+constexpr int kDnJs = kBatchDenseRd * (kBatchDenseTd + 1) + 1;  // r, J, then rd and td
+
+__device__ __forceinline__ DnWs DenseWs(const BatchLmDev& d, int slot) {
+  const size_t n = size_t(d.nmax_t), sm = size_t(d.smax);
+  double* w = d.ws + size_t(slot) * size_t(d.ws_stride);
+  DnWs s;
+  s.vals = w;  w += 3 * sm;
+  s.H = w;     w += 3 * n * n;
+  s.F = w;     w += n * n;
+  s.g = w;     w += 3 * n;
+  s.damp = w;  w += n;
+  s.maxd = w;  w += n;
+  s.upd = w;   w += n;
+  s.last = w;  w += n;
+  s.y = w;     w += 2 * n;
+  s.Js = w;
+  return s;
+}
+
+template <int KIND>
+__device__ __forceinline__ void EvalKind(const double* const* x, const double* c, double* r, double* J,
+                                         int* rd, int* td) {
+  static_assert(FactorTraits<KIND>::RD <= kBatchDenseRd && FactorTraits<KIND>::TD <= kBatchDenseTd &&
+                    FactorTraits<KIND>::NK <= kBatchDenseKeys,
+                "dense batch scratch holds the factor");
+  FactorEval<KIND, double>::Run(x, c, r, J);
+  *rd = FactorTraits<KIND>::RD;
+  *td = FactorTraits<KIND>::TD;
+}
+
+// Residual r and row-major Jacobian J (rd x td) of a factor of any kind.
+__device__ void EvalAny(int kind, const double* const* x, const double* c, double* r, double* J, int* rd,
+                        int* td) {
+  *rd = 0;
+  *td = 0;
+  switch (kind) {
+    case SFG_FACTOR_BEARING_POSE2: EvalKind<SFG_FACTOR_BEARING_POSE2>(x, c, r, J, rd, td); break;
+    case SFG_FACTOR_ODOMETRY_POSE2: EvalKind<SFG_FACTOR_ODOMETRY_POSE2>(x, c, r, J, rd, td); break;
+    case SFG_FACTOR_SNAVELY_REPROJECTION: EvalKind<SFG_FACTOR_SNAVELY_REPROJECTION>(x, c, r, J, rd, td); break;
+    case SFG_FACTOR_BETWEEN_POSE3: EvalKind<SFG_FACTOR_BETWEEN_POSE3>(x, c, r, J, rd, td); break;
+    case SFG_FACTOR_PRIOR_POSE3: EvalKind<SFG_FACTOR_PRIOR_POSE3>(x, c, r, J, rd, td); break;
+    case SFG_FACTOR_RANGE_POSE3: EvalKind<SFG_FACTOR_RANGE_POSE3>(x, c, r, J, rd, td); break;
+#define SFG_DENSE_CASE(KIND, NKEYS, NCONSTS, RDIM, K0, K1, K2, G) \
+    case KIND: EvalKind<KIND>(x, c, r, J, rd, td); break;
+      SFG_GENERATED_FACTORS(SFG_DENSE_CASE)
+#undef SFG_DENSE_CASE
+  }
+}
+
+__device__ __forceinline__ int KeyTangentDim(int type) {
+  switch (type) {
+    case SFG_KEY_POSE2: return 3;
+    case SFG_KEY_POSE3: return 6;
+    case SFG_KEY_ROT3: return 3;
+    default: return type <= SFG_KEY_VEC3 ? type : type - SFG_KEY_VEC4 + 4;
+  }
+}
+
+// Row of entry e of a packed lower triangle (row-major: row i holds entries i (i + 1) / 2 ...).
+__device__ __forceinline__ int TriRow(int e) {
+  int i = int((sqrtf(8.0f * float(e) + 1.0f) - 1.0f) * 0.5f);
+  if ((i + 1) * (i + 2) / 2 <= e) ++i;
+  if (i * (i + 1) / 2 > e) --i;
+  return i;
+}
+
+// Linearize state block s of problem prob: H (lower part of an n x n row-major block), g = J^T r,
+// and 0.5 |r|^2 (returned to every lane).
+__device__ double DnLinearize(const BatchLmDev& d, const DnWs& w, int prob, int s, int lane) {
+  const int n = d.dn_n[prob];
+  const size_t nm = size_t(d.nmax_t);
+  const double* V = w.vals + size_t(s) * size_t(d.smax);
+  double* H = w.H + size_t(s) * nm * nm;
+  double* g = w.g + size_t(s) * nm;
+  for (int i = lane; i < n * n; i += 32) H[i] = 0.0;
+  for (int i = lane; i < n; i += 32) g[i] = 0.0;
+  __syncwarp();
+  double err = 0.0;
+  const int64_t f0 = d.f_ptr[prob], f1 = d.f_ptr[prob + 1];
+  for (int64_t fb = f0; fb < f1; fb += 32) {
+    const int cnt = int(f1 - fb < 32 ? f1 - fb : 32);
+    if (lane < cnt) {
+      const int64_t f = fb + lane;
+      const int32_t* fk = d.f_key + f * kBatchDenseKeys;
+      const double* x[kBatchDenseKeys];
+#pragma unroll
+      for (int q = 0; q < kBatchDenseKeys; ++q) x[q] = fk[q] >= 0 ? V + d.key_soff[fk[q]] : V;
+      double* js = w.Js + size_t(lane) * kDnJs;
+      int rd = 0, td = 0;
+      EvalAny(d.f_kind[f], x, d.consts + d.f_coff[f], js, js + kBatchDenseRd, &rd, &td);
+      for (int i = 0; i < rd; ++i) err += js[i] * js[i];
+      js[kDnJs - 1] = double(rd * 256 + td);
+    }
+    __syncwarp();
+    for (int q = 0; q < cnt; ++q) {
+      const int32_t* fk = d.f_key + (fb + q) * kBatchDenseKeys;
+      const double* js = w.Js + size_t(q) * kDnJs;
+      const int code = int(js[kDnJs - 1]), rd = code >> 8, td = code & 255;
+      const double* r = js;
+      const double* J = js + kBatchDenseRd;
+      // the factor's tangent columns on the problem's tangent vector
+      int cols[kBatchDenseTd];
+      int nc = 0;
+#pragma unroll
+      for (int k = 0; k < kBatchDenseKeys; ++k) {
+        if (fk[k] < 0) continue;
+        const int t = KeyTangentDim(d.key_type[fk[k]]), o = d.key_toff[fk[k]];
+        for (int j = 0; j < t && nc < kBatchDenseTd; ++j) cols[nc++] = o + j;
+      }
+      if (nc != td) continue;  // (the host admits only factors whose key types give td columns)
+      const int ntri = td * (td + 1) / 2;
+      for (int e = lane; e < ntri + td; e += 32) {
+        if (e < ntri) {
+          const int a = TriRow(e), b = e - a * (a + 1) / 2;
+          double v = 0.0;
+          for (int i = 0; i < rd; ++i) v += J[i * td + a] * J[i * td + b];
+          const int ga = cols[a], gb = cols[b];
+          H[size_t(max(ga, gb)) * n + min(ga, gb)] += v;
+        } else {
+          const int a = e - ntri;
+          double v = 0.0;
+          for (int i = 0; i < rd; ++i) v += J[i * td + a] * r[i];
+          g[cols[a]] += v;
+        }
+      }
+      __syncwarp();
+    }
+  }
+  return 0.5 * WarpSum(err);
+}
+
+// (H + D) x = g by LDL^T (no pivoting, as the reference's sparse LDL^T); writes upd = -x.
+__device__ void DnFactorSolve(const BatchLmDev& d, const DnWs& w, int prob, int s, int lane) {
+  const int n = d.dn_n[prob];
+  const size_t nm = size_t(d.nmax_t);
+  const double* H = w.H + size_t(s) * nm * nm;
+  const double* g = w.g + size_t(s) * nm;
+  double* F = w.F;
+  double* y = w.y;
+  double* l = w.y + nm;  // the scaled pivot column
+  for (int i = lane; i < n * n; i += 32) {
+    const int r = i / n, c = i - (i / n) * n;
+    F[i] = c <= r ? H[i] + (r == c ? w.damp[r] : 0.0) : 0.0;
+  }
+  __syncwarp();
+  for (int k = 0; k < n; ++k) {
+    const double inv = 1.0 / F[size_t(k) * n + k];
+    for (int j = k + 1 + lane; j < n; j += 32) l[j] = F[size_t(j) * n + k] * inv;
+    __syncwarp();
+    const int m = n - k - 1;
+    for (int e = lane; e < m * (m + 1) / 2; e += 32) {
+      const int ii = TriRow(e), jj = e - ii * (ii + 1) / 2;
+      const int i = k + 1 + ii, j = k + 1 + jj;
+      F[size_t(i) * n + j] -= F[size_t(i) * n + k] * l[j];
+    }
+    __syncwarp();
+    for (int j = k + 1 + lane; j < n; j += 32) F[size_t(j) * n + k] = l[j];
+    __syncwarp();
+  }
+  for (int i = lane; i < n; i += 32) y[i] = g[i];
+  __syncwarp();
+  for (int j = 0; j < n; ++j) {  // L y = g, unit L
+    const double yj = y[j];
+    for (int i = j + 1 + lane; i < n; i += 32) y[i] -= F[size_t(i) * n + j] * yj;
+    __syncwarp();
+  }
+  for (int i = lane; i < n; i += 32) y[i] /= F[size_t(i) * n + i];
+  __syncwarp();
+  for (int i = n - 1; i > 0; --i) {  // L^T x = D^-1 y
+    const double xi = y[i];
+    for (int j = lane; j < i; j += 32) y[j] -= F[size_t(i) * n + j] * xi;
+    __syncwarp();
+  }
+  for (int i = lane; i < n; i += 32) w.upd[i] = -y[i];
+  __syncwarp();
+}
+
+// One problem of the dense path, start to finish (the warp's LM loop).
+__device__ void DenseProblem(const BatchLmDev& d, const LmParams& p, const DnWs& w, LmState& st, int prob,
+                             int lane) {
+  const int n = d.dn_n[prob], S = d.dn_s[prob], nk = d.dn_nk[prob], k0 = d.dn_k0[prob];
+  const int64_t s0 = d.dn_s0[prob];
+  const size_t sm = size_t(d.smax), nm = size_t(d.nmax_t);
+  sfg_iteration_t* rec = d.records ? d.records + size_t(prob) * d.rec_cap : nullptr;
+  if (lane == 0) {
+    st = LmState{};
+    LmBegin(p, st, 1);
+  }
+  __syncwarp();
+  for (int i = lane; i < S; i += 32) w.vals[size_t(st.init_idx) * sm + i] = d.values_in[s0 + i];
+  __syncwarp();
+  {
+    const int init = st.init_idx;
+    const double e = DnLinearize(d, w, prob, init, lane);
+    if (lane == 0) st.error[init] = e;
+  }
+  __syncwarp();
+  int go = 0;
+  if (lane == 0) go = LmFirstRecord(p, st, rec);
+  go = __shfl_sync(0xffffffffu, go, 0);
+  while (go) {
+    const int init = st.init_idx, nw = st.new_idx;
+    const double* H = w.H + size_t(init) * nm * nm;
+    for (int i = lane; i < n; i += 32) w.damp[i] = LmDamping(p, st, H[size_t(i) * n + i], w.maxd + i);
+    __syncwarp();
+    DnFactorSolve(d, w, prob, init, lane);
+    for (int k = lane; k < nk; k += 32) {
+      const int kg = k0 + k;
+      RetractKey(d.key_type[kg], w.vals + size_t(init) * sm + d.key_soff[kg], w.upd + d.key_toff[kg],
+                 p.epsilon, w.vals + size_t(nw) * sm + d.key_soff[kg]);
+    }
+    __syncwarp();
+    const double e_new = DnLinearize(d, w, prob, nw, lane);
+    const double* g = w.g + size_t(init) * nm;
+    double s0s = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (int i = lane; i < n; i += 32) {
+      const double u = w.upd[i];
+      s0s += u * (g[i] - w.damp[i] * u);
+      if (p.enable_bold_updates) {
+        const double l = w.last[i];
+        s1 += u * l;
+        s2 += u * u;
+        s3 += l * l;
+      }
+    }
+    double sums[4] = {WarpSum(s0s), WarpSum(s1), WarpSum(s2), WarpSum(s3)};
+    int done = 0, copy = 0;
+    if (lane == 0) {
+      st.error[nw] = e_new;
+      done = LmDecide(p, st, rec, sums, &copy);
+    }
+    done = __shfl_sync(0xffffffffu, done, 0);
+    copy = __shfl_sync(0xffffffffu, copy, 0);
+    if (copy)
+      for (int i = lane; i < n; i += 32) w.last[i] = w.upd[i];
+    __syncwarp();
+    go = !done;
+  }
+  for (int i = lane; i < S; i += 32) d.values_out[s0 + i] = w.vals[size_t(st.best_idx) * sm + i];
+  if (lane == 0) d.st[prob] = st;
+  __syncwarp();
+}
+
+template <int kWarps, int kMinBlocks, bool kDense>
 __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) BatchLmKernel(BatchLmDev d, const LmParams* pp) {
   __shared__ LmState sst[kWarps];
   __shared__ double sscr[kWarps][kScratch];
@@ -290,6 +547,10 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) BatchLmKernel(BatchLm
     job = __shfl_sync(0xffffffffu, job, 0);
     if (job >= d.nprob) break;
     const int prob = d.order[job];
+    if constexpr (kDense) {
+      DenseProblem(d, p, DenseWs(d, slot), st, prob, lane);
+      continue;
+    }
     const int n = d.n[prob];
     const int64_t pose0 = d.pose0[prob];
     sfg_iteration_t* rec = d.records ? d.records + size_t(prob) * d.rec_cap : nullptr;
@@ -364,17 +625,20 @@ __global__ void __launch_bounds__(32 * kWarps, kMinBlocks) BatchLmKernel(BatchLm
 }  // namespace
 
 // Launch shapes the autotuner chooses from: warps per CTA and the register budget implied by the
-// minimum resident CTAs per SM (fewer registers: more warps in flight to hide FP64 latency).
+// minimum resident CTAs per SM (fewer registers: more warps in flight to hide FP64 latency); each
+// for the chain and the dense path.
 template <int W, int B>
 struct Shape {
-  static int MaxCtasPerSm() {
+  static int MaxCtasPerSm(bool dense) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, BatchLmKernel<W, B>, 32 * W, 0) != cudaSuccess)
-      return 0;
-    return per_sm;
+    const cudaError_t e =
+        dense ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, BatchLmKernel<W, B, true>, 32 * W, 0)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, BatchLmKernel<W, B, false>, 32 * W, 0);
+    return e == cudaSuccess ? per_sm : 0;
   }
   static void Launch(const BatchLmDev& d, const LmParams* p, int ctas, cudaStream_t s) {
-    BatchLmKernel<W, B><<<ctas, 32 * W, 0, s>>>(d, p);
+    if (d.dense) BatchLmKernel<W, B, true><<<ctas, 32 * W, 0, s>>>(d, p);
+    else BatchLmKernel<W, B, false><<<ctas, 32 * W, 0, s>>>(d, p);
   }
 };
 
@@ -385,13 +649,13 @@ int BatchShapeWarps(int shape) {
   return shape >= 0 && shape < 5 ? w[shape] : 0;
 }
 
-int BatchMaxCtasPerSm(int shape) {
+int BatchMaxCtasPerSm(int shape, bool dense) {
   switch (shape) {
-    case 0: return Shape<8, 1>::MaxCtasPerSm();
-    case 1: return Shape<4, 4>::MaxCtasPerSm();
-    case 2: return Shape<2, 8>::MaxCtasPerSm();
-    case 3: return Shape<4, 6>::MaxCtasPerSm();
-    case 4: return Shape<2, 16>::MaxCtasPerSm();
+    case 0: return Shape<8, 1>::MaxCtasPerSm(dense);
+    case 1: return Shape<4, 4>::MaxCtasPerSm(dense);
+    case 2: return Shape<2, 8>::MaxCtasPerSm(dense);
+    case 3: return Shape<4, 6>::MaxCtasPerSm(dense);
+    case 4: return Shape<2, 16>::MaxCtasPerSm(dense);
   }
   return 0;
 }

@@ -36,28 +36,7 @@ __global__ void RetractKernel(RetractDev r, const LmParams* p, const LmState* st
   const double* a = r.values + int64_t(st->init_idx) * r.S + r.soff[k];
   double* o = r.values + int64_t(st->new_idx) * r.S + r.soff[k];
   const double* d = r.update + r.toff[k];
-  switch (r.key_type[k]) {
-    case SFG_KEY_POSE2: {  // gen/cpp/sym/ops/pose2/lie_group_ops.cc:58-82
-      const double c = cos(d[0]), s = sin(d[0]);
-      const double re = a[0], im = a[1];
-      o[0] = re * c - im * s;
-      o[1] = re * s + im * c;
-      o[2] = a[2] + d[1];
-      o[3] = a[3] + d[2];
-      break;
-    }
-    case SFG_KEY_POSE3:  // gen/cpp/sym/ops/pose3/lie_group_ops.cc:69-102
-      RetractPose3(a, d, p->epsilon, o);
-      break;
-    case SFG_KEY_ROT3:  // gen/cpp/sym/ops/rot3/lie_group_ops.cc: the rotation part of the above
-      RetractRot3(a, d, p->epsilon, o);
-      break;
-    default: {
-      const int t = r.key_type[k];  // VEC1..VEC3 = 1..3, VEC4..VEC6 = 7..9
-      const int n = t <= SFG_KEY_VEC3 ? t : t - SFG_KEY_VEC4 + 4;
-      for (int i = 0; i < n; ++i) o[i] = a[i] + d[i];
-    }
-  }
+  RetractKey(r.key_type[k], a, d, p->epsilon, o);
 }
 
 template <typename T>
