@@ -10,6 +10,8 @@ device timestamps of the run; lower is better.  The same line reports:
   forms    - mixed precision, block-Jacobi PCG and learned-preconditioner PCG on the same workload;
   scale    - every form on the 1,000-camera / 200k-point / ~1.2M-observation workload;
   batched  - 4,096 independent Pose3-chain problems in one persistent launch (problems/s);
+  batched_dense - 4,096 small 2D localization, bundle adjustment and loop-closed Pose3 problems
+             (the batched form's dense path);
   roofline - the linearization stage against the measured HBM copy bandwidth.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
@@ -389,15 +391,16 @@ def _scale_section(device: int, flush, workload: str = SCALE_WORKLOAD) -> dict:
     return out, launches
 
 
-def _batched_section(device: int, steps: int, cpu_budget_s: float) -> dict:
-    """4,096 independent Pose3-chain problems in one persistent launch (device time per batch and
-    problems/s), next to the CPU oracle on a bounded sample of the same problems, one optimizer per
-    host thread."""
+def _batched_section(device: int, steps: int, cpu_budget_s: float, mixed: bool = False) -> dict:
+    """4,096 independent problems in one persistent launch (device time per batch and problems/s),
+    next to the CPU oracle on a bounded sample of the same problems, one optimizer per host thread:
+    Pose3 chains (the block-tridiagonal path) or, with `mixed`, small 2D localization, bundle
+    adjustment and loop-closed Pose3 problems (the dense path)."""
     from concurrent.futures import ThreadPoolExecutor
 
     from symforce_gb300 import synth
     from symforce_gb300.batch import BatchOptimizer
-    problems = synth.pose3_chains(BATCH_PROBLEMS, seed=0)
+    problems = synth.mixed_small_problems(BATCH_PROBLEMS, seed=0) if mixed else synth.pose3_chains(BATCH_PROBLEMS, seed=0)
     params = A.default_optimizer_params(iterations=50)
     form = A.default_form_params()
     form.device = device
@@ -417,8 +420,9 @@ def _batched_section(device: int, steps: int, cpu_budget_s: float) -> dict:
         dev.append(res.device_ms)
     del vals
     ms = statistics.median(dev)
-    out = {"workload": f"pose3_chains_{BATCH_PROBLEMS}", "problems": BATCH_PROBLEMS,
-           "poses": int(sum(p.meta.get("num_poses", len(p.key_types)) for p in problems)),
+    out = {"workload": f"{'mixed_small_problems' if mixed else 'pose3_chains'}_{BATCH_PROBLEMS}",
+           "problems": BATCH_PROBLEMS,
+           "keys": int(sum(len(p.key_types) for p in problems)),
            "batch_ms": round(ms, 3), "problems_per_s": round(BATCH_PROBLEMS / (ms * 1e-3), 1),
            "e2e_ms": round(statistics.median(e2e), 3), "autotuned_shape": list(shape),
            "host_create_s": round(create_s, 2),
@@ -516,7 +520,7 @@ def run_gb300(args) -> None:
     if tp.exists():
         traffic = json.loads(tp.read_text()).get(f"linearize_{WORKLOAD}")
     launches = int(sum(sum(r["launches"]) for r in res.values()))
-    scale = batched = None
+    scale = batched = batched_dense = None
     # the secondary sections report an error in the line instead of losing the headline
     if not args.no_scale:
         try:
@@ -531,6 +535,12 @@ def run_gb300(args) -> None:
             launches += n
         except Exception as e:  # noqa: BLE001
             batched = {"error": f"{type(e).__name__}: {e}"}
+        try:
+            batched_dense, n = _batched_section(local, min(args.steps, 5),
+                                                cpu_budget_s=10.0 if rank == 0 else 0.0, mixed=True)
+            launches += n
+        except Exception as e:  # noqa: BLE001
+            batched_dense = {"error": f"{type(e).__name__}: {e}"}
     if rank != 0:
         return
     cpu = None
@@ -579,6 +589,7 @@ def run_gb300(args) -> None:
             "multiply_adds": factor_fmas["plain"]["fmas"], "ms_per_launch": round(factor_fmas["plain"]["ms"], 5)},
         "scale": scale,
         "batched": batched,
+        "batched_dense": batched_dense,
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_ms, 4), "unit": "ms", "h2d_bytes_per_step": 8 * S + 8 * 24,
                 "d2h_bytes_per_step": 8 * S + 64 * len(plain["stats"].iterations)},
@@ -644,7 +655,7 @@ def main() -> None:
     ap.add_argument("--no-scale", action="store_true", help="skip the large workload")
     ap.add_argument("--scale-workload", default=SCALE_WORKLOAD,
                     help="large workload of the scale section (ba_1000_200k or ba_10k_1m)")
-    ap.add_argument("--no-batched", action="store_true", help="skip the batched Pose3 chains")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched sections")
     ap.add_argument("--profile-workload", default=None,
                     help="profiling mode: run --profile-runs optimize calls of one form on this workload")
     ap.add_argument("--profile-form", default="plain", choices=list(FORMS))

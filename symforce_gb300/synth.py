@@ -211,6 +211,67 @@ def pose3_chains(num_problems: int = 4096, seed: int = 0, min_poses: int = 5, ma
     return _pose3_build(sizes, lms, [seed * 1_000_003 + i for i in range(num_problems)])
 
 
+def loop_closed_pose3_chain(num_poses: int, num_landmarks: int, seed: int) -> A.ProblemArrays:
+    """pose3_chain with one more between factor, from the last pose back to the first (a loop
+    closure): no longer block tridiagonal."""
+    p = pose3_chain(num_poses, num_landmarks, seed)
+    bw = next(b for b in p.batches if b.kind == A.SFG_FACTOR_BETWEEN_POSE3)
+    # the closure measures the dead-reckoned relative pose last -> first (zero residual at the
+    # initial values), with the chain's noise model
+    v = p.values.reshape(num_poses, 7)
+    qa_inv = v[-1, :4] * np.array([-1, -1, -1, 1.0])
+    c = bw.consts[:1].copy()
+    c[0, :4] = quat_mul(qa_inv, v[0, :4])
+    c[0, 4:7] = quat_rotate(qa_inv, v[0, 4:7] - v[-1, 4:7])
+    loop = A.Batch(A.SFG_FACTOR_BETWEEN_POSE3, np.array([[num_poses - 1, 0]], dtype=np.int32), c)
+    return A.ProblemArrays(key_types=p.key_types, batches=list(p.batches) + [loop], values=p.values,
+                           name=f"loop_pose3_chain_{num_poses}_{num_landmarks}", meta=dict(p.meta))
+
+
+def rot3_chain(num_keys: int, seed: int) -> A.ProblemArrays:
+    """Rotation smoothing: a Rot3 random walk (N(0, 0.2) rad increments), a PRIOR_ROT3 on every key
+    measured with N(0, 0.1) rad noise (sqrt_info 1/0.1) and a BETWEEN_ROT3 on consecutive keys
+    measured with N(0, 0.05) rad noise (sqrt_info 1/0.05) (the generated factor kinds); every key
+    starts at identity."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    eps = A.DEFAULT_EPSILON
+    q = np.zeros((num_keys, 4))
+    q[0] = quat_exp(rng.normal(0, 1.0, size=3))
+    for k in range(1, num_keys):
+        q[k] = quat_mul(q[k - 1], quat_exp(rng.normal(0, 0.2, size=3)))
+    meas = quat_mul(q, quat_exp(rng.normal(0, 0.1, size=(num_keys, 3))))
+    rel = quat_mul(quat_mul(q[:-1] * np.array([-1, -1, -1, 1.0]), q[1:]),
+                   quat_exp(rng.normal(0, 0.05, size=(num_keys - 1, 3))))
+    prior = np.concatenate([meas, np.full((num_keys, 3), 1 / 0.1), np.full((num_keys, 1), eps)], 1)
+    between = np.concatenate([rel, np.full((num_keys - 1, 3), 1 / 0.05), np.full((num_keys - 1, 1), eps)], 1)
+    values = np.tile([0.0, 0.0, 0.0, 1.0], num_keys)
+    return A.ProblemArrays(
+        key_types=[A.SFG_KEY_ROT3] * num_keys,
+        batches=[A.Batch(A.SFG_FACTOR_PRIOR_ROT3, np.arange(num_keys)[:, None], prior),
+                 A.Batch(A.SFG_FACTOR_BETWEEN_ROT3, np.stack([np.arange(num_keys - 1), np.arange(1, num_keys)], -1),
+                         between)],
+        values=values, name=f"rot3_chain_{num_keys}", meta=dict(seed=seed))
+
+
+def mixed_small_problems(num_problems: int = 4096, seed: int = 0) -> list:
+    """Independent small problems of uneven size and structure for the batched form's dense path
+    (tangent dimension at most 120): in turn a 2D localization (U{5..40} Pose2 states, robot_2d), a
+    loop-closed Pose3 chain of U{5..20} poses with U{4..12} range landmarks, and a Rot3 smoothing
+    chain of U{5..40} keys; problem i has its own seed (seed * 1_000_003 + i)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(num_problems):
+        s = seed * 1_000_003 + i
+        k = i % 3
+        if k == 0:
+            out.append(robot_2d(num_poses=int(rng.integers(5, 41)), num_landmarks=6, seed=s))
+        elif k == 1:
+            out.append(loop_closed_pose3_chain(int(rng.integers(5, 21)), int(rng.integers(4, 13)), s))
+        else:
+            out.append(rot3_chain(int(rng.integers(5, 41)), s))
+    return out
+
+
 # ---------------------------------------------------------------------------------------------
 # Configs 1/2/4: bundle adjustment
 # ---------------------------------------------------------------------------------------------

@@ -78,9 +78,7 @@ def _mixed_problems():
               for c, pts in ((3, 12), (4, 25), (3, 8))]
     probs.append(R.pose_smoothing(O.pose_smoothing_initial_values()))
     probs.append(R.rot3_smoothing(O.rot3_smoothing_initial_values()))
-    ch = synth.pose3_chain(12, 10, 5)
-    loop = A.Batch(A.SFG_FACTOR_BETWEEN_POSE3, np.array([[0, 11]]), ch.batches[1].consts[:1])
-    probs.append(A.ProblemArrays(key_types=ch.key_types, batches=list(ch.batches) + [loop], values=ch.values))
+    probs.append(synth.loop_closed_pose3_chain(12, 10, 5))
     return probs
 
 
