@@ -378,11 +378,13 @@ int32_t sfg_precond_infer(const float* features, int64_t n, const float* weights
  * Many independent problems of uneven size solved by one persistent kernel launch (captured in a
  * CUDA graph): each warp runs the whole LM loop of one problem at a time (the reference would run
  * one sym::Optimizer<double> per problem, symforce/opt/optimizer.h:72-94), taking problems
- * largest first from a device queue.  Supported structure: every key POSE3; unary PRIOR_POSE3 /
- * RANGE_POSE3 factors and BETWEEN_POSE3 factors between consecutive keys, so each Hessian is block
- * tridiagonal in key order (6 x 6 blocks) and is factored by a block Cholesky recursion, in FP64.
- * Values of all problems are concatenated in problem order.  No reference counterpart for the
- * batching itself. */
+ * largest first from a device queue, in FP64.  A batch whose every problem is a Pose3 chain (every
+ * key POSE3; unary PRIOR_POSE3 / RANGE_POSE3 factors and BETWEEN_POSE3 factors between consecutive
+ * keys) has block-tridiagonal Hessians (6 x 6 blocks) factored by a block Cholesky recursion; any
+ * other batch runs the dense path: any key types and factor kinds, at most 128 tangent dimensions a
+ * problem (SFG_ERR_STRUCTURE above), every factor's keys distinct (SFG_ERR_STRUCTURE otherwise),
+ * the dense Hessian factored by LDL^T; Schur keys are solved with the rest.  Values of all
+ * problems are concatenated in problem order.  No reference counterpart for the batching itself. */
 typedef struct sfg_batch sfg_batch;
 typedef struct sfg_batch_result_t {
   int32_t num_iterations;   /* records, as optimization_stats_t.iterations.size() */
