@@ -602,6 +602,21 @@ def run_gb300(args) -> None:
 def run_profile(args) -> None:
     """A few optimize calls of one form on one workload, for profilers."""
     from symforce_gb300.optimizer import Optimizer
+    if args.profile_workload in ("pose3_chains", "mixed_small_problems"):
+        # the batched form on 1,024 problems of the bench's batched sections (one launch a run)
+        from symforce_gb300 import synth
+        from symforce_gb300.batch import BatchOptimizer
+        probs = (synth.pose3_chains(1024, seed=0) if args.profile_workload == "pose3_chains"
+                 else synth.mixed_small_problems(1024, seed=0))
+        params = A.default_optimizer_params(iterations=50 if args.profile_iterations <= 0 else args.profile_iterations)
+        opt = BatchOptimizer(probs, params)
+        v0 = opt.initial_values()
+        for _ in range(args.profile_runs):
+            res = opt.optimize(v0)
+            print(f"{args.profile_workload} batched: 1024 problems, {res.device_ms:.3f} ms, "
+                  f"{int((res.status == A.SFG_STATUS_SUCCESS).sum())} SUCCESS", flush=True)
+        opt.close()
+        return
     w = workloads.get(args.profile_workload)
     p = w.problem()
     params = w.params()
