@@ -288,6 +288,7 @@ struct DnWs {
   double *vals, *H, *F, *g, *damp, *maxd, *upd, *last, *y, *Js;
 };
 constexpr int kDnJs = kBatchDenseRd * (kBatchDenseTd + 1) + 1;  // r, J, then rd and td
+constexpr int kDnBatch = 8;  // trailing-update entries a lane keeps in flight
 
 __device__ __forceinline__ DnWs DenseWs(const BatchLmDev& d, int slot) {
   const size_t n = size_t(d.nmax_t), sm = size_t(d.smax);
@@ -398,20 +399,36 @@ __device__ double DnLinearize(const BatchLmDev& d, const DnWs& w, int prob, int 
       }
       if (nc != td) continue;  // (the host admits only factors whose key types give td columns)
       const int ntri = td * (td + 1) / 2;
-      for (int e = lane; e < ntri + td; e += 32) {
+      // the lane's entries of this factor (at most kDnFactorEntries): products first, then the
+      // read-modify-writes with their loads in flight together
+      constexpr int kDnFactorEntries = (kBatchDenseTd * (kBatchDenseTd + 1) / 2 + kBatchDenseTd + 31) / 32;
+      double val[kDnFactorEntries], old[kDnFactorEntries];
+      double* dst[kDnFactorEntries];
+#pragma unroll
+      for (int u = 0; u < kDnFactorEntries; ++u) {
+        const int e = lane + 32 * u;
+        dst[u] = nullptr;
+        val[u] = 0.0;
         if (e < ntri) {
           const int a = TriRow(e), b = e - a * (a + 1) / 2;
           double v = 0.0;
           for (int i = 0; i < rd; ++i) v += J[i * td + a] * J[i * td + b];
           const int ga = cols[a], gb = cols[b];
-          H[size_t(max(ga, gb)) * n + min(ga, gb)] += v;
-        } else {
+          dst[u] = H + size_t(max(ga, gb)) * n + min(ga, gb);
+          val[u] = v;
+        } else if (e < ntri + td) {
           const int a = e - ntri;
           double v = 0.0;
           for (int i = 0; i < rd; ++i) v += J[i * td + a] * r[i];
-          g[cols[a]] += v;
+          dst[u] = g + cols[a];
+          val[u] = v;
         }
       }
+#pragma unroll
+      for (int u = 0; u < kDnFactorEntries; ++u) old[u] = dst[u] ? *dst[u] : 0.0;
+#pragma unroll
+      for (int u = 0; u < kDnFactorEntries; ++u)
+        if (dst[u]) *dst[u] = old[u] + val[u];
       __syncwarp();
     }
   }
@@ -436,11 +453,28 @@ __device__ void DnFactorSolve(const BatchLmDev& d, const DnWs& w, int prob, int 
     const double inv = 1.0 / F[size_t(k) * n + k];
     for (int j = k + 1 + lane; j < n; j += 32) l[j] = F[size_t(j) * n + k] * inv;
     __syncwarp();
-    const int m = n - k - 1;
-    for (int e = lane; e < m * (m + 1) / 2; e += 32) {
-      const int ii = TriRow(e), jj = e - ii * (ii + 1) / 2;
-      const int i = k + 1 + ii, j = k + 1 + jj;
-      F[size_t(i) * n + j] -= F[size_t(i) * n + k] * l[j];
+    // trailing update, kDnBatch entries a lane in flight: their loads issue before any store
+    const int m = n - k - 1, cnt = m * (m + 1) / 2;
+    for (int e0 = lane; e0 < cnt; e0 += 32 * kDnBatch) {
+      double fv[kDnBatch], av[kDnBatch], bv[kDnBatch];
+      size_t at[kDnBatch];
+#pragma unroll
+      for (int u = 0; u < kDnBatch; ++u) {
+        const int e = e0 + 32 * u;
+        at[u] = 0;
+        fv[u] = av[u] = bv[u] = 0.0;
+        if (e < cnt) {
+          const int ii = TriRow(e), jj = e - ii * (ii + 1) / 2;
+          const int i = k + 1 + ii, j = k + 1 + jj;
+          at[u] = size_t(i) * n + j;
+          fv[u] = F[at[u]];
+          av[u] = F[size_t(i) * n + k];
+          bv[u] = l[j];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kDnBatch; ++u)
+        if (e0 + 32 * u < cnt) F[at[u]] = fv[u] - av[u] * bv[u];
     }
     __syncwarp();
     for (int j = k + 1 + lane; j < n; j += 32) F[size_t(j) * n + k] = l[j];
