@@ -220,7 +220,7 @@ void EnqueueIterationBody(sfg_handle* h, cudaGraphConditionalHandle cond, int us
       LaunchCollectSamples<T>(h->pd, h->feats, h->fac, h->v, ysol, h->samples, h->collect_cap, h->ps,
                               h->st, s);
     }
-    LaunchSchurBackSub<T>(h->sd, ysol, h->W, h->tp, h->update, s);
+    LaunchSchurBackSub<T>(h->sd, ysol, h->W, h->tp, h->cinv, h->update, s);
   } else {
     EnqueueFactor<T>(h->fp, h->hess, h->damp.damping, s);
     EnqueueSolve<T>(h->fp, h->rhs, h->xsol, s);
@@ -411,7 +411,7 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
   if (h->schur && h->P.num_schur == 0)
     throw Error(SFG_ERR_INVALID_ARGUMENT, "Schur and PCG solvers require num_schur_keys > 0");
   h->L = BuildLinLayout(h->P);
-  if (h->schur) h->SL = BuildSchurLayout(h->P, h->L);
+  if (h->schur) h->SL = BuildSchurLayout(h->P, h->L, /*g_at_e=*/h->elem == 4);
   SFG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   DeviceArena& A = h->arena;
   const HostProblem& P = h->P;
@@ -482,7 +482,7 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
     const SchurLayout& S = h->SL;
     h->sd = UploadSchur(A, S, E);
     h->cinv = A.Alloc(9 * size_t(std::max(S.npoints, 1)) * E);
-    h->W = A.Alloc(size_t(std::max<int64_t>(S.nW, 1)) * E);
+    h->W = A.Alloc(size_t(std::max<int64_t>(S.nG, 1)) * E);  // G = L^-1 E
     h->tp = A.Alloc(3 * size_t(std::max(S.npoints, 1)) * E);
     h->S = A.Alloc(size_t(std::max<int64_t>(S.Spat.nvals(), 1)) * E);
     h->v = A.Alloc(size_t(std::max<int64_t>(S.nB, 1)) * E);

@@ -286,7 +286,7 @@ int32_t sfg_schur_create(int32_t n, const int32_t* col_ptr, const int32_t* row_i
     s->rhs = A.Zeros<double>(size_t(n));
     s->damping = A.Zeros<double>(size_t(n));
     s->cinv = A.Zeros<double>(9 * size_t(npts));
-    s->W = A.Zeros<double>(size_t(S.nW));
+    s->W = A.Zeros<double>(size_t(std::max<int64_t>(S.nG, 1)));  // G = L^-1 E
     s->tp = A.Zeros<double>(3 * size_t(npts));
     s->S = A.Zeros<double>(size_t(S.Spat.nvals()));
     s->v = A.Zeros<double>(size_t(S.nB));
@@ -309,7 +309,7 @@ int32_t sfg_schur_factorize(sfg_schur* s, const double* values) {
     for (size_t q = 0; q < s->csc_to_val.size(); ++q) v[s->csc_to_val[q]] += values[q];
     SFG_CUDA(cudaMemcpy(s->hess, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice));
     cudaStream_t st = s->stream;
-    // C^-1 and W only depend on the matrix; the rhs-dependent t_p is recomputed in solve
+    // L^-1 and G = L^-1 E only depend on the matrix; the rhs-dependent t_p is recomputed in solve
     sfg::LaunchSchurPoints<double>(s->sd, s->hess, s->rhs, s->L.nvals, s->n, s->damping, s->cinv, s->W,
                                    s->tp, s->st, st);
     sfg::LaunchSchurBuildS<double>(s->sd, s->hess, s->L.nvals, s->damping, s->W, s->S, s->st, st);
@@ -335,7 +335,7 @@ int32_t sfg_schur_solve(sfg_schur* s, const double* b, double* x, int32_t nrhs) 
                                      s->tp, s->st, st);
       sfg::LaunchSchurRhs<double>(s->sd, s->hess, s->L.nvals, s->rhs, s->n, s->tp, s->v, s->st, st);
       sfg::EnqueueSolve<double>(p, s->v, s->y, st);
-      sfg::LaunchSchurBackSub<double>(s->sd, s->y, s->W, s->tp, s->update, st);
+      sfg::LaunchSchurBackSub<double>(s->sd, s->y, s->W, s->tp, s->cinv, s->update, st);
       SFG_CUDA(cudaMemcpyAsync(u.data(), s->update, sizeof(double) * s->n, cudaMemcpyDeviceToHost, st));
       SFG_CUDA(cudaStreamSynchronize(st));
       CheckError(s->st);

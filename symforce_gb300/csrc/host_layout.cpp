@@ -359,7 +359,7 @@ void BuildCscExport(LinLayout& L, const HostProblem& P) {
     }
 }
 
-SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L) {
+SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L, bool g_at_e) {
   SchurLayout S;
   S.nB_keys = P.nkeys - P.num_schur;
   S.npoints = P.num_schur;
@@ -505,6 +505,8 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L) {
       for (auto& th : pool) th.join();
     }
   };
+  S.g_at_e = g_at_e;
+  S.nG = g_at_e ? L.nvals : S.nW;
   S.sb_ptr.assign(size_t(nsb) + 1, 0);
   for_columns([&](int64_t blk, int64_t, int64_t) { S.sb_ptr[blk + 1]++; });
   for (int64_t q = 0; q < nsb; ++q) S.sb_ptr[q + 1] += S.sb_ptr[q];
@@ -515,8 +517,9 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L) {
     std::vector<int64_t> fill(S.sb_ptr.begin(), S.sb_ptr.end() - 1);
     for_columns([&](int64_t blk, int64_t ea, int64_t eb) {
       const int64_t k = fill[blk]++;
-      S.sb_eoff[k] = S.pt_eoff[ea];
-      S.sb_woff[k] = S.pt_woff[eb];
+      // both operands are G = L^-1 E blocks (at E's offsets or at W's)
+      S.sb_eoff[k] = g_at_e ? S.pt_eoff[ea] : S.pt_woff[ea];
+      S.sb_woff[k] = g_at_e ? S.pt_eoff[eb] : S.pt_woff[eb];
     });
   }
   S.sb_hoff.resize(size_t(nsb));

@@ -97,13 +97,13 @@ struct SchurDev {
   const int32_t* pt_ekey_toff;  // tangent offset of the B key of each E block
   const int32_t* pt_ekey_dim;   // dim of that key
   const int64_t* pt_eoff;       // H value offset of E block (3 x d_k, row-major)
-  const int64_t* pt_woff;       // W value offset (3 x d_k)
+  const int64_t* pt_woff;       // G = L^-1 E offset (3 x d_k) of each E block in the G buffer
   int64_t nE;                   // E blocks (pt_eptr[npoints])
   const int32_t* pt_of_e;       // [nE] point of each E block
   int nsblocks;
   const int64_t* sb_ptr;        // [nsblocks + 1] terms of each S block
-  const int64_t* sb_eoff;       // E_pk offset per term
-  const int64_t* sb_woff;       // W_pl offset per term
+  const int64_t* sb_eoff;       // G_pk offset (G buffer, E's layout) per term
+  const int64_t* sb_woff;       // G_pl offset (G buffer, E's layout) per term
   const int64_t* sb_hoff;       // H value offset of the B block (-1: none)
   const int64_t* sb_soff;       // S value offset of the block
   const int32_t* sb_dk;         // rows of the block
@@ -134,7 +134,7 @@ void LaunchSchurRhs(const SchurDev& d, const void* hess, int64_t nvals, const vo
                     const void* tp, void* v, const LmState* st, cudaStream_t s);
 // y: the reduced-system solution in FP64.
 template <typename T>
-void LaunchSchurBackSub(const SchurDev& d, const void* y, const void* W, const void* tp,
+void LaunchSchurBackSub(const SchurDev& d, const void* y, const void* W, const void* tp, const void* cinv,
                         double* update, cudaStream_t s);
 
 // Symmetric block-sparse matrix-vector product layout (per scalar row: segments of a stored block

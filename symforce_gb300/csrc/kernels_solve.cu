@@ -71,31 +71,33 @@ __device__ __forceinline__ void St(T* p, T v) { __stcg(p, v); }
 // ---------------------------------------------------------------------------------------------
 // Schur complement kernels
 // ---------------------------------------------------------------------------------------------
-// W = C^-1 E for one 3 x DK block E (row-major); cm = C^-1 entries (00, 10, 20, 11, 21, 22).
+// G = L^-1 E for one 3 x DK block E (row-major), li = L^-1 lower (00, 10, 11, 20, 21, 22) with
+// C = L L^T: then E_k^T C^-1 E_l = G_k^T G_l, so the S terms read one array for both operands.
 template <typename T, int DK>
-__device__ __forceinline__ void PointW(const T* E, T* Wp, const T (&cm)[6]) {
+__device__ __forceinline__ void PointG(const T* E, T* Gp, const T (&li)[6]) {
   T e[3 * DK];
 #pragma unroll
   for (int i = 0; i < 3 * DK; ++i) e[i] = E[i];
 #pragma unroll
   for (int c = 0; c < DK; ++c) {
     const T e0 = e[c], e1 = e[DK + c], e2 = e[2 * DK + c];
-    Wp[c] = cm[0] * e0 + cm[1] * e1 + cm[2] * e2;
-    Wp[DK + c] = cm[1] * e0 + cm[3] * e1 + cm[4] * e2;
-    Wp[2 * DK + c] = cm[2] * e0 + cm[4] * e1 + cm[5] * e2;
+    Gp[c] = li[0] * e0;
+    Gp[DK + c] = li[1] * e0 + li[2] * e1;
+    Gp[2 * DK + c] = li[3] * e0 + li[4] * e1 + li[5] * e2;
   }
 }
 template <typename T>
-__device__ __forceinline__ void PointWAny(const T* E, T* Wp, int dk, const T (&cm)[6]) {
+__device__ __forceinline__ void PointGAny(const T* E, T* Gp, int dk, const T (&li)[6]) {
   for (int c = 0; c < dk; ++c) {
     const T e0 = E[c], e1 = E[dk + c], e2 = E[2 * dk + c];
-    Wp[c] = cm[0] * e0 + cm[1] * e1 + cm[2] * e2;
-    Wp[dk + c] = cm[1] * e0 + cm[3] * e1 + cm[4] * e2;
-    Wp[2 * dk + c] = cm[2] * e0 + cm[4] * e1 + cm[5] * e2;
+    Gp[c] = li[0] * e0;
+    Gp[dk + c] = li[1] * e0 + li[2] * e1;
+    Gp[2 * dk + c] = li[3] * e0 + li[4] * e1 + li[5] * e2;
   }
 }
 
-// One thread per point: C^-1 of the damped 3 x 3 block (by its Cholesky factor) and t = C^-1 g.
+// One thread per point: the Cholesky factor L of the damped 3 x 3 block, its inverse (kept) and
+// t = C^-1 g.
 template <typename T>
 __global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_all, int64_t nvals,
                                   int64_t N, const double* damping, T* cinv, T* tp,
@@ -127,10 +129,10 @@ __global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_al
   const T c11 = i11 * i11 + i21 * i21;
   const T c21 = i22 * i21;
   const T c22 = i22 * i22;
-  T* ci = cinv + 9 * int64_t(p);
-  ci[0] = c00; ci[1] = c10; ci[2] = c20;
-  ci[3] = c10; ci[4] = c11; ci[5] = c21;
-  ci[6] = c20; ci[7] = c21; ci[8] = c22;
+  T* ci = cinv + 9 * int64_t(p);  // L^-1 (C = L L^T), lower, row-major packed
+  ci[0] = i00;
+  ci[1] = i10; ci[2] = i11;
+  ci[3] = i20; ci[4] = i21; ci[5] = i22;
   const T g0 = g[toff], g1 = g[toff + 1], g2 = g[toff + 2];
   T* t = tp + 3 * int64_t(p);
   t[0] = c00 * g0 + c10 * g1 + c20 * g2;
@@ -139,7 +141,8 @@ __global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_al
 }
 
 // One thread per E block (the blocks of a point are consecutive, so neighbouring threads share its
-// C^-1): W = C^-1 E, the block's loads all issued before its stores.
+// L^-1): G = L^-1 E into the G buffer (at E's offset or point-major, as the layout chose), the
+// block's loads all issued before its stores.
 template <typename T>
 __global__ void SchurWKernel(SchurDev d, const T* hess_all, int64_t nvals, const T* cinv, T* W,
                              const LmState* st) {
@@ -147,19 +150,20 @@ __global__ void SchurWKernel(SchurDev d, const T* hess_all, int64_t nvals, const
   if (e >= d.nE) return;
   const T* H = hess_all + int64_t(st->init_idx) * nvals;
   const T* ci = cinv + 9 * int64_t(d.pt_of_e[e]);
-  const T cm[6] = {ci[0], ci[1], ci[2], ci[4], ci[5], ci[8]};
+  const T li[6] = {ci[0], ci[1], ci[2], ci[3], ci[4], ci[5]};
   const int dk = d.pt_ekey_dim[e];
   const T* E = H + d.pt_eoff[e];
-  T* Wp = W + d.pt_woff[e];
-  if (dk == 6) PointW<T, 6>(E, Wp, cm);
-  else if (dk == 3) PointW<T, 3>(E, Wp, cm);
-  else PointWAny<T>(E, Wp, dk, cm);
+  T* Gp = W + d.pt_woff[e];
+  if (dk == 6) PointG<T, 6>(E, Gp, li);
+  else if (dk == 3) PointG<T, 3>(E, Gp, li);
+  else PointGAny<T>(E, Gp, dk, li);
 }
 
-// S = B - sum_p E_pk^T W_pl over the S blocks' terms (points seen by both keys), in two passes.
+// S = B - sum_p G_pk^T G_pl over the S blocks' terms (points seen by both keys), G = L_p^-1 E (the
+// G buffer; E_pk^T C_p^-1 E_pl = G_pk^T G_pl with C_p = L_p L_p^T), in two passes.
 // Pass 1: one warp per chunk of at most chunk_terms terms of one block; each lane takes the
 // chunk's terms in turn and accumulates the whole d_k x d_l product of its terms in registers (every
-// E and W block is read once; a diagonal block only its lower triangle), then a butterfly
+// G block is read once; a diagonal block only its lower triangle), then a butterfly
 // reduce-scatter adds the lanes.  Pass 2: one warp per S block adds its chunks in order and writes
 // B_kl (+ damping) - sum.  Chunks spread the heavy diagonal blocks (every observation of a camera)
 // over many warps, which the FP64 pipe needs; the fixed orders make every run give the same bits.
@@ -210,7 +214,7 @@ __device__ __forceinline__ void ChunkTerms(const SchurDev& d, const T* H, const 
 #pragma unroll
   for (int i = 0; i < N; ++i) acc[i] = T(0);
   for (int64_t t = t0 + lane; t < t1; t += 32) {
-    const T* E = H + d.sb_eoff[t];
+    const T* E = W + d.sb_eoff[t];
     const T* Wl = W + d.sb_woff[t];
     T e[3 * DK], w[3 * DL];
 #pragma unroll
@@ -243,7 +247,7 @@ __device__ __forceinline__ void ChunkTermsSym(const SchurDev& d, const T* H, con
 #pragma unroll
   for (int i = 0; i < N; ++i) acc[i] = T(0);
   for (int64_t t = t0 + lane; t < t1; t += 32) {
-    const T* E = H + d.sb_eoff[t];
+    const T* E = W + d.sb_eoff[t];
     const T* Wl = W + d.sb_woff[t];
     T e[3 * D], w[3 * D];
 #pragma unroll
@@ -280,7 +284,7 @@ __device__ __forceinline__ void ChunkTermsAny(const SchurDev& d, const T* H, con
 #pragma unroll
   for (int i = 0; i < N; ++i) acc[i] = T(0);
   for (int64_t t = t0 + lane; t < t1; t += 32) {
-    const T* E = H + d.sb_eoff[t];
+    const T* E = W + d.sb_eoff[t];
     const T* Wl = W + d.sb_woff[t];
     T e[3 * D], w[3 * D];
 #pragma unroll
@@ -420,14 +424,15 @@ __device__ __forceinline__ void BlockTimesAny(const T* Wp, const double* yk, int
   }
 }
 
-// Point back-substitution z_p = t_p - sum_k W_pk y_k, and update = -[y; z].
+// Point back-substitution z_p = t_p - C_p^-1 sum_k E_pk y_k = t_p - L_p^-T sum_k G_pk y_k, and
+// update = -[y; z].
 template <typename T>
-__global__ void SchurBackSubKernel(SchurDev d, const double* y, const T* W, const T* tp,
+__global__ void SchurBackSubKernel(SchurDev d, const double* y, const T* W, const T* tp, const T* cinv,
                                    double* update) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < d.npoints) {
     const int p = t;
-    T z0 = tp[3 * int64_t(p)], z1 = tp[3 * int64_t(p) + 1], z2 = tp[3 * int64_t(p) + 2];
+    T z0 = T(0), z1 = T(0), z2 = T(0);  // sum_k G_pk y_k
     for (int64_t e = d.pt_eptr[p]; e < d.pt_eptr[p + 1]; ++e) {
       const int dk = d.pt_ekey_dim[e];
       const T* Wp = W + d.pt_woff[e];
@@ -436,14 +441,18 @@ __global__ void SchurBackSubKernel(SchurDev d, const double* y, const T* W, cons
       if (dk == 6) BlockTimes<T, 6>(Wp, yk, s);
       else if (dk == 3) BlockTimes<T, 3>(Wp, yk, s);
       else BlockTimesAny<T>(Wp, yk, dk, s);
-      z0 -= s[0];
-      z1 -= s[1];
-      z2 -= s[2];
+      z0 += s[0];
+      z1 += s[1];
+      z2 += s[2];
     }
+    const T* li = cinv + 9 * int64_t(p);  // L^-1 lower (00, 10, 11, 20, 21, 22)
+    const T w0 = li[0] * z0 + li[1] * z1 + li[3] * z2;
+    const T w1 = li[2] * z1 + li[4] * z2;
+    const T w2 = li[5] * z2;
     double* u = update + d.c_toff + 3 * int64_t(p);
-    u[0] = -double(z0);
-    u[1] = -double(z1);
-    u[2] = -double(z2);
+    u[0] = -double(tp[3 * int64_t(p)] - w0);
+    u[1] = -double(tp[3 * int64_t(p) + 1] - w1);
+    u[2] = -double(tp[3 * int64_t(p) + 2] - w2);
   } else if (t < d.npoints + d.nB) {
     const int i = t - d.npoints;
     update[i] = -double(y[i]);
@@ -2079,12 +2088,13 @@ void LaunchSchurRhs(const SchurDev& d, const void* hess, int64_t nvals, const vo
 }
 
 template <typename T>
-void LaunchSchurBackSub(const SchurDev& d, const void* y, const void* W, const void* tp,
+void LaunchSchurBackSub(const SchurDev& d, const void* y, const void* W, const void* tp, const void* cinv,
                         double* update, cudaStream_t s) {
   const int n = d.npoints + d.nB;
   const int threads = 128;
   SchurBackSubKernel<T><<<(n + threads - 1) / threads, threads, 0, s>>>(
-      d, static_cast<const double*>(y), static_cast<const T*>(W), static_cast<const T*>(tp), update);
+      d, static_cast<const double*>(y), static_cast<const T*>(W), static_cast<const T*>(tp),
+      static_cast<const T*>(cinv), update);
 }
 
 template <typename T>
@@ -2121,9 +2131,9 @@ template void LaunchSchurRhs<double>(const SchurDev&, const void*, int64_t, cons
 template void LaunchSchurRhs<float>(const SchurDev&, const void*, int64_t, const void*, int64_t,
                                     const void*, void*, const LmState*, cudaStream_t);
 template void LaunchSchurBackSub<double>(const SchurDev&, const void*, const void*, const void*,
-                                         double*, cudaStream_t);
+                                         const void*, double*, cudaStream_t);
 template void LaunchSchurBackSub<float>(const SchurDev&, const void*, const void*, const void*,
-                                        double*, cudaStream_t);
+                                        const void*, double*, cudaStream_t);
 template void LaunchFactor<double>(const FactorDev&, const void*, const double*, void*, void*, int,
                                    cudaStream_t);
 template void LaunchFactor<float>(const FactorDev&, const void*, const double*, void*, void*, int,

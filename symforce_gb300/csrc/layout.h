@@ -42,13 +42,21 @@ struct SchurLayout {
   std::vector<int32_t> pt_of_e;    // point of each E block
   int64_t nW = 0;
   BlockPattern Spat;               // pattern of the reduced system over B keys
+  // terms of S block q: [sb_ptr[q], sb_ptr[q + 1]); each term's two blocks G_pk, G_pl
+  // (G = L_p^-1 E, L_p the Cholesky factor of the point block) at offsets sb_eoff, sb_woff of the
+  // G buffer; pt_goff: the G offset of each E block (pt_eoff or pt_woff, see BuildSchurLayout)
   std::vector<int64_t> sb_ptr, sb_eoff, sb_woff, sb_hoff, sb_soff;
+  bool g_at_e = false;
+  int64_t nG = 0;  // G buffer size
   std::vector<int32_t> sb_dk, sb_dl, sb_diag_toff;
   std::vector<int64_t> r_ptr, r_eoff;
   std::vector<int32_t> r_ecol, r_dk, r_pt;
 };
 
-SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L);
+// g_at_e: the G = L^-1 E blocks sit at E's offsets in a Hessian-sized buffer (a key's blocks
+// contiguous over its points: fewer bytes for the memory-bound FP32 S build); otherwise at their
+// W offsets (point-major, compact: the FP64 build is bound by the FP64 pipe, not by its loads).
+SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L, bool g_at_e = false);
 
 // Camera blocks of the reduced system for the PCG forms: B keys joined when they share a factor
 // (pose + intrinsics of a camera), at most 9 scalars per block, ordered by their first key.

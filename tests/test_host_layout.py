@@ -168,8 +168,8 @@ def _schur_arrays(lib):
 
 def test_schur_plan_matches_dense_schur_complement(shim):
     """The Schur plan (point C blocks, per-S-block term lists, reduced-rhs lists) replayed in numpy
-    on random block values gives S = B - E^T C^-1 E and v = g_B - E^T C^-1 g_C of the dense matrix
-    (symforce/opt/sparse_schur_solver.tcc:15-170)."""
+    on random block values gives S = B - E^T C^-1 E (as sum G_pk^T G_pl, G = L^-1 E) and
+    v = g_B - E^T C^-1 g_C of the dense matrix (symforce/opt/sparse_schur_solver.tcc:15-170)."""
     p = synth.bundle_adjustment(num_cameras=5, num_points=60, num_observations=240, seed=7)
     c = p.to_c()
     assert shim.shim_build(C.byref(c)) == 0 and shim.shim_build_schur() == 0
@@ -196,23 +196,25 @@ def test_schur_plan_matches_dense_schur_complement(shim):
 
     (nbk, npts, nB, c_toff, nS), a64, a32 = _schur_arrays(shim)
     assert nB == toff[nbk] and c_toff == nB
-    # replay: C^-1 and t per point, W per E block, S blocks from their terms, v from its lists
-    cinv = [np.linalg.inv(vals[a64[0][q]:a64[0][q] + 9].reshape(3, 3)) for q in range(npts)]
-    t = np.array([cinv[q] @ g[c_toff + 3 * q:c_toff + 3 * q + 3] for q in range(npts)])
-    Wv = np.zeros(int(max(a64[3][e] + 3 * a32[0][e] for e in range(len(a64[3])))))
+    # replay: L^-1 (C = L L^T) and t per point, G = L^-1 E per E block (at E's offset), S blocks
+    # from their terms (G_pk^T G_pl), v from its lists
+    Cs = [vals[a64[0][q]:a64[0][q] + 9].reshape(3, 3) for q in range(npts)]
+    linv = [np.linalg.inv(np.linalg.cholesky(Cq)) for Cq in Cs]
+    t = np.array([np.linalg.solve(Cs[q], g[c_toff + 3 * q:c_toff + 3 * q + 3]) for q in range(npts)])
+    Wv = np.zeros(int(max(a64[3][e] + 3 * a32[0][e] for e in range(len(a64[3])))))  # G, point-major
     for q in range(npts):
         for e in range(a64[1][q], a64[1][q + 1]):
             dk = int(a32[0][e])
             E = vals[a64[2][e]:a64[2][e] + 3 * dk].reshape(3, dk)
-            Wv[a64[3][e]:a64[3][e] + 3 * dk] = (cinv[q] @ E).ravel()
+            Wv[a64[3][e]:a64[3][e] + 3 * dk] = (linv[q] @ E).ravel()
     Sv = np.zeros(nS)
     for q in range(len(a64[7])):
         dk, dl = int(a32[1][q]), int(a32[2][q])
         acc = np.zeros((dk, dl))
         for u in range(a64[4][q], a64[4][q + 1]):
-            E = vals[a64[5][u]:a64[5][u] + 3 * dk].reshape(3, dk)
-            W = Wv[a64[6][u]:a64[6][u] + 3 * dl].reshape(3, dl)
-            acc += E.T @ W
+            Gk = Wv[a64[5][u]:a64[5][u] + 3 * dk].reshape(3, dk)
+            Gl = Wv[a64[6][u]:a64[6][u] + 3 * dl].reshape(3, dl)
+            acc += Gk.T @ Gl
         B = vals[a64[7][q]:a64[7][q] + dk * dl].reshape(dk, dl) if a64[7][q] >= 0 else 0.0
         Sv[a64[8][q]:a64[8][q] + dk * dl] = (B - acc).ravel()
     v = g[:nB].copy()
