@@ -9,13 +9,14 @@ oracle's final cost (committed in tests/golden/oracle_costs.json), read from the
 device timestamps of the run; lower is better.  The same line reports:
   forms    - mixed precision, block-Jacobi PCG and learned-preconditioner PCG on the same workload;
   scale    - every form on the 1,000-camera / 200k-point / ~1.2M-observation workload;
+  scale_10k - every form on the 10,000-camera / 1M-point / ~5M-observation workload;
   batched  - 4,096 independent Pose3-chain problems in one persistent launch (problems/s);
-  batched_dense - 4,096 small 2D localization, bundle adjustment and loop-closed Pose3 problems
+  batched_dense - 4,096 small 2D localization, loop-closed Pose3 and Rot3 smoothing problems
              (the batched form's dense path);
   roofline - the linearization stage against the measured HBM copy bandwidth.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--no-scale] [--no-batched] [--no-cpu-baseline]
+                    [--no-scale] [--no-scale-10k] [--no-batched] [--no-cpu-baseline]
 
 Profiling mode (no JSON line; the command the ncu summaries under profiles/ give):
 
@@ -224,6 +225,7 @@ FORMS = {
     "pcg_learned": (A.SFG_PRECISION_MIXED, A.SFG_LINEAR_SOLVER_PCG_LEARNED),
 }
 SCALE_WORKLOAD = "ba_1000_200k"
+SCALE_10K_WORKLOAD = "ba_10k_1m"  # the learned form's named configuration, in the default run too
 BATCH_PROBLEMS = 4096
 
 
@@ -394,8 +396,8 @@ def _scale_section(device: int, flush, workload: str = SCALE_WORKLOAD) -> dict:
 def _batched_section(device: int, steps: int, cpu_budget_s: float, mixed: bool = False) -> dict:
     """4,096 independent problems in one persistent launch (device time per batch and problems/s),
     next to the CPU oracle on a bounded sample of the same problems, one optimizer per host thread:
-    Pose3 chains (the block-tridiagonal path) or, with `mixed`, small 2D localization, bundle
-    adjustment and loop-closed Pose3 problems (the dense path)."""
+    Pose3 chains (the block-tridiagonal path) or, with `mixed`, small 2D localization,
+    loop-closed Pose3 and Rot3 smoothing problems (the dense path)."""
     from concurrent.futures import ThreadPoolExecutor
 
     from symforce_gb300 import synth
@@ -520,7 +522,7 @@ def run_gb300(args) -> None:
     if tp.exists():
         traffic = json.loads(tp.read_text()).get(f"linearize_{WORKLOAD}")
     launches = int(sum(sum(r["launches"]) for r in res.values()))
-    scale = batched = batched_dense = None
+    scale = scale_10k = batched = batched_dense = None
     # the secondary sections report an error in the line instead of losing the headline
     if not args.no_scale:
         try:
@@ -528,6 +530,12 @@ def run_gb300(args) -> None:
             launches += n
         except Exception as e:  # noqa: BLE001
             scale = {"error": f"{type(e).__name__}: {e}"}
+        if args.scale_workload != SCALE_10K_WORKLOAD and not args.no_scale_10k:
+            try:
+                scale_10k, n = _scale_section(local, flush, SCALE_10K_WORKLOAD)
+                launches += n
+            except Exception as e:  # noqa: BLE001
+                scale_10k = {"error": f"{type(e).__name__}: {e}"}
     if not args.no_batched:
         try:
             batched, n = _batched_section(local, min(args.steps, 5),
@@ -588,6 +596,7 @@ def run_gb300(args) -> None:
                           / FP64_PEAK_GFLOPS, 5),
             "multiply_adds": factor_fmas["plain"]["fmas"], "ms_per_launch": round(factor_fmas["plain"]["ms"], 5)},
         "scale": scale,
+        "scale_10k": scale_10k,
         "batched": batched,
         "batched_dense": batched_dense,
         "cpu_baseline": cpu,
@@ -670,6 +679,7 @@ def main() -> None:
     ap.add_argument("--no-scale", action="store_true", help="skip the large workload")
     ap.add_argument("--scale-workload", default=SCALE_WORKLOAD,
                     help="large workload of the scale section (ba_1000_200k or ba_10k_1m)")
+    ap.add_argument("--no-scale-10k", action="store_true", help="skip the 10,000-camera workload")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched sections")
     ap.add_argument("--profile-workload", default=None,
                     help="profiling mode: run --profile-runs optimize calls of one form on this workload")
