@@ -411,7 +411,12 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
   if (h->schur && h->P.num_schur == 0)
     throw Error(SFG_ERR_INVALID_ARGUMENT, "Schur and PCG solvers require num_schur_keys > 0");
   h->L = BuildLinLayout(h->P);
-  if (h->schur) h->SL = BuildSchurLayout(h->P, h->L, /*g_at_e=*/h->elem == 4);
+  if (h->schur) {
+    // FP32: G = L^-1 E at E's offsets; SFG_SCHUR_G_AT_E=0 / 1 overrides (layout measurements)
+    bool g_at_e = h->elem == 4;
+    if (const char* e = std::getenv("SFG_SCHUR_G_AT_E")) g_at_e = std::atoi(e) != 0;
+    h->SL = BuildSchurLayout(h->P, h->L, g_at_e);
+  }
   SFG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   DeviceArena& A = h->arena;
   const HostProblem& P = h->P;
