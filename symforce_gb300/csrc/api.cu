@@ -412,8 +412,8 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
     throw Error(SFG_ERR_INVALID_ARGUMENT, "Schur and PCG solvers require num_schur_keys > 0");
   h->L = BuildLinLayout(h->P);
   if (h->schur) {
-    // FP32: G = L^-1 E at E's offsets; SFG_SCHUR_G_AT_E=0 / 1 overrides (layout measurements)
-    bool g_at_e = h->elem == 4;
+    // G = L^-1 E at E's offsets (SFG_SCHUR_G_AT_E=0: point-major, for layout measurements)
+    bool g_at_e = true;
     if (const char* e = std::getenv("SFG_SCHUR_G_AT_E")) g_at_e = std::atoi(e) != 0;
     h->SL = BuildSchurLayout(h->P, h->L, g_at_e);
   }

@@ -276,7 +276,7 @@ int32_t sfg_schur_create(int32_t n, const int32_t* col_ptr, const int32_t* row_i
         const int64_t blk = s->L.H.Find(kr, kc);
         s->csc_to_val[q] = s->L.H.boff[blk] + int64_t(r - P.toff[kr]) * P.tdim[kc] + (c - P.toff[kc]);
       }
-    s->SL = sfg::BuildSchurLayout(P, s->L);
+    s->SL = sfg::BuildSchurLayout(P, s->L, /*g_at_e=*/true);
     SFG_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
     Arena& A = s->A;
     s->st = MakeState(A);

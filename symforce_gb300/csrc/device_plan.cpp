@@ -236,6 +236,7 @@ SchurDev UploadSchur(DeviceArena& A, const SchurLayout& S, int elem) {
   d.nE = int64_t(S.pt_eoff.size());
   d.pt_of_e = A.Upload(S.pt_of_e);
   d.pt_woff = S.g_at_e ? d.pt_eoff : A.Upload(S.pt_woff);  // where each block's G lives
+  d.e_order = S.e_order.empty() ? nullptr : A.Upload(S.e_order);
   d.nsblocks = int(S.Spat.nblocks());
   d.sb_ptr = A.Upload(S.sb_ptr);
   d.sb_eoff = A.Upload(S.sb_eoff);

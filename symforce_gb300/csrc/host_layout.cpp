@@ -397,8 +397,12 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L, bool g_at
   const int64_t ne = pe_ptr[S.npoints];
   std::vector<int32_t> pe_key(static_cast<size_t>(ne));
   std::vector<int64_t> pe_boff(static_cast<size_t>(ne));
+  // e_order (G at E's offsets): the E blocks in the order of their Hessian offsets (key-major), so
+  // that the kernel forming G = L^-1 E writes (and reads) consecutive addresses
+  if (g_at_e) S.e_order.resize(size_t(ne));
   {
     std::vector<int64_t> fill(pe_ptr.begin(), pe_ptr.end() - 1);
+    int64_t km = 0;
     for (int j = 0; j < S.nB_keys; ++j)  // ascending B keys: each point's list comes out sorted
       for (int64_t q = L.H.colptr[j]; q < L.H.colptr[j + 1]; ++q) {
         const int i = L.H.rows[q];
@@ -406,6 +410,7 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L, bool g_at
         const int64_t at = fill[i - S.nB_keys]++;
         pe_key[at] = j;
         pe_boff[at] = L.H.boff[q];
+        if (g_at_e) S.e_order[size_t(km++)] = at;
       }
   }
   S.pt_diag.resize(S.npoints);

@@ -98,6 +98,7 @@ struct SchurDev {
   const int32_t* pt_ekey_dim;   // dim of that key
   const int64_t* pt_eoff;       // H value offset of E block (3 x d_k, row-major)
   const int64_t* pt_woff;       // G = L^-1 E offset (3 x d_k) of each E block in the G buffer
+  const int64_t* e_order;       // optional: the order the G kernel takes the E blocks in (null: 0, 1, ...)
   int64_t nE;                   // E blocks (pt_eptr[npoints])
   const int32_t* pt_of_e;       // [nE] point of each E block
   int nsblocks;

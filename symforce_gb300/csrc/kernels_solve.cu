@@ -140,14 +140,15 @@ __global__ void SchurPointsKernel(SchurDev d, const T* hess_all, const T* rhs_al
   t[2] = c20 * g0 + c21 * g1 + c22 * g2;
 }
 
-// One thread per E block (the blocks of a point are consecutive, so neighbouring threads share its
-// L^-1): G = L^-1 E into the G buffer (at E's offset or point-major, as the layout chose), the
-// block's loads all issued before its stores.
+// One thread per E block: G = L^-1 E into the G buffer (at E's offset or point-major, as the layout
+// chose), the block's loads all issued before its stores; the blocks are taken in the order of
+// their G offsets (e_order), so that neighbouring threads write neighbouring addresses.
 template <typename T>
 __global__ void SchurWKernel(SchurDev d, const T* hess_all, int64_t nvals, const T* cinv, T* W,
                              const LmState* st) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= d.nE) return;
+  const int64_t q = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (q >= d.nE) return;
+  const int64_t e = d.e_order ? d.e_order[q] : q;
   const T* H = hess_all + int64_t(st->init_idx) * nvals;
   const T* ci = cinv + 9 * int64_t(d.pt_of_e[e]);
   const T li[6] = {ci[0], ci[1], ci[2], ci[3], ci[4], ci[5]};

@@ -47,15 +47,16 @@ struct SchurLayout {
   // G buffer; pt_goff: the G offset of each E block (pt_eoff or pt_woff, see BuildSchurLayout)
   std::vector<int64_t> sb_ptr, sb_eoff, sb_woff, sb_hoff, sb_soff;
   bool g_at_e = false;
-  int64_t nG = 0;  // G buffer size
+  int64_t nG = 0;                  // G buffer size
+  std::vector<int64_t> e_order;    // g_at_e: E blocks in Hessian-offset order (else empty)
   std::vector<int32_t> sb_dk, sb_dl, sb_diag_toff;
   std::vector<int64_t> r_ptr, r_eoff;
   std::vector<int32_t> r_ecol, r_dk, r_pt;
 };
 
 // g_at_e: the G = L^-1 E blocks sit at E's offsets in a Hessian-sized buffer (a key's blocks
-// contiguous over its points: fewer bytes for the memory-bound FP32 S build); otherwise at their
-// W offsets (point-major, compact: the FP64 build is bound by the FP64 pipe, not by its loads).
+// contiguous over its points, for both operands of every S term; the kernel forming G takes the
+// blocks in that order); otherwise point-major in a compact buffer.
 SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L, bool g_at_e = false);
 
 // Camera blocks of the reduced system for the PCG forms: B keys joined when they share a factor

@@ -83,6 +83,17 @@ int shim_build_schur() {
   }
 }
 
+// The same with G = L^-1 E at E's offsets (the library's default); e_order into out ([nE]).
+int shim_build_schur_g_at_e(int64_t* e_order) {
+  try {
+    g_schur = sfg::BuildSchurLayout(g_problem, g_layout, true);
+    if (e_order) Put(g_schur.e_order, e_order);
+    return 0;
+  } catch (...) {
+    return 1;
+  }
+}
+
 // nB_keys, npoints, nB, c_toff, E blocks, S blocks, terms, rhs entries, S values
 void shim_schur_sizes(int64_t* out) {
   const auto& S = g_schur;

@@ -166,7 +166,8 @@ def _schur_arrays(lib):
     return (nbk, npts, nB, c_toff, nS), a64, a32
 
 
-def test_schur_plan_matches_dense_schur_complement(shim):
+@pytest.mark.parametrize("g_at_e", [False, True])
+def test_schur_plan_matches_dense_schur_complement(shim, g_at_e):
     """The Schur plan (point C blocks, per-S-block term lists, reduced-rhs lists) replayed in numpy
     on random block values gives S = B - E^T C^-1 E (as sum G_pk^T G_pl, G = L^-1 E) and
     v = g_B - E^T C^-1 g_C of the dense matrix (symforce/opt/sparse_schur_solver.tcc:15-170)."""
@@ -176,6 +177,12 @@ def test_schur_plan_matches_dense_schur_complement(shim):
     sizes = _arr(7, np.int64)
     shim.shim_sizes(_ptr(sizes))
     nvals, N, _, _, _, nblocks, nkeys = (int(x) for x in sizes)
+    if g_at_e:  # G at E's offsets; the G kernel's order visits every E block once, offsets ascending
+        ssz = _arr(9, np.int64)
+        shim.shim_schur_sizes(_ptr(ssz))
+        order = _arr(int(ssz[4]), np.int64)
+        assert shim.shim_build_schur_g_at_e(_ptr(order)) == 0
+        assert sorted(order.tolist()) == list(range(len(order)))
     colptr, rows, boff, toff = _arr(nkeys + 1, np.int64), _arr(nblocks, np.int32), _arr(nblocks, np.int64), \
         _arr(nkeys + 1, np.int64)
     shim.shim_pattern(_ptr(colptr), _ptr(rows), _ptr(boff), _ptr(toff))
@@ -201,12 +208,15 @@ def test_schur_plan_matches_dense_schur_complement(shim):
     Cs = [vals[a64[0][q]:a64[0][q] + 9].reshape(3, 3) for q in range(npts)]
     linv = [np.linalg.inv(np.linalg.cholesky(Cq)) for Cq in Cs]
     t = np.array([np.linalg.solve(Cs[q], g[c_toff + 3 * q:c_toff + 3 * q + 3]) for q in range(npts)])
-    Wv = np.zeros(int(max(a64[3][e] + 3 * a32[0][e] for e in range(len(a64[3])))))  # G, point-major
+    goff = a64[2] if g_at_e else a64[3]  # where each block's G lives
+    if g_at_e:
+        assert np.all(np.diff(a64[2][order]) > 0)
+    Wv = np.zeros(int(max(goff[e] + 3 * a32[0][e] for e in range(len(goff)))))
     for q in range(npts):
         for e in range(a64[1][q], a64[1][q + 1]):
             dk = int(a32[0][e])
             E = vals[a64[2][e]:a64[2][e] + 3 * dk].reshape(3, dk)
-            Wv[a64[3][e]:a64[3][e] + 3 * dk] = (linv[q] @ E).ravel()
+            Wv[goff[e]:goff[e] + 3 * dk] = (linv[q] @ E).ravel()
     Sv = np.zeros(nS)
     for q in range(len(a64[7])):
         dk, dl = int(a32[1][q]), int(a32[2][q])
