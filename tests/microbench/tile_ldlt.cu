@@ -123,10 +123,104 @@ __device__ void DiagLdltFF(double* a, int b, double* s_rp) {
   __syncthreads();
 }
 
+// Fraction-free elimination two pivots per CTA barrier: for the pair (k, k + 1) with P = B(k, k),
+// Q = B(k + 1, k + 1), X = B(k + 1, k), D = P Q - X^2, every trailing entry (c >= k + 2) becomes
+// 2^-e(D) [D B(r, c) - B(r, k) u_c - B(r, k + 1) w_c], u_c = Q B(c, k) - X B(c, k + 1),
+// w_c = P B(c, k + 1) - X B(c, k): the Schur complement of the 2 x 2 block times D (the block's
+// determinant), so the stored matrix stays the true Schur complement times a product of pivot
+// mantissas.  At the end d_k = P_k / S_k, L(r, k) = B(r, k) / P_k for the first column of a pair
+// (and single pivots), and d_k+1 = D / (P S_k), L(r, k + 1) = (P B(r, k + 1) - X B(r, k)) / D for
+// the second.
+__device__ void DiagLdltFF2(double* a, int b, double* s_rp, double* s_aux) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  int r = 0, c = 16;
+  if (t < 120) {
+    int cc = 1, start = 0;
+    while (cc < 15 && t >= start + (16 - cc)) { start += 16 - cc; ++cc; }
+    c = cc; r = cc + (t - start);
+    if (r >= b) c = 16;
+  }
+  double v = (c < 16) ? a[c * 16 + r] : 0.0;
+  int k = 0;
+  for (; k + 2 < b; k += 2) {
+    const double P = a[k * 17], Q = a[(k + 1) * 17], X = a[k * 16 + k + 1];
+    const double D = fma(P, Q, -(X * X));
+    const int eD = PivotExponent(D);
+    if (c < 16 && c >= k + 2) {
+      const double ar = a[k * 16 + r], br = a[(k + 1) * 16 + r];
+      const double ac = a[k * 16 + c], bc = a[(k + 1) * 16 + c];
+      const double uc = fma(Q, ac, -(X * bc)), wc = fma(P, bc, -(X * ac));
+      double in = D * v;
+      in = fma(-ar, uc, in);
+      in = fma(-br, wc, in);
+      v = Pow2Scale(in, -eD);
+      a[c * 16 + r] = v;
+    }
+    __syncthreads();
+  }
+  if (k + 1 < b) {  // one single pivot left before the last column
+    const double p = a[k * 17];
+    const int ek = PivotExponent(p);
+    if (c < 16 && c > k) {
+      const double m = a[k * 16 + r] * a[k * 16 + c];
+      v = Pow2Scale(fma(p, v, -m), -ek);
+      a[c * 16 + r] = v;
+    }
+    __syncthreads();
+  }
+  const int npair = (b >= 3) ? (b - 1) / 2 : 0;  // pairs (0,1) .. (2 npair - 2, 2 npair - 1)
+  double dk = 0.0;
+  if (warp == 0) {
+    // event factor of column j: a pair's first column mant(D), its second 1, a single mant(P)
+    const bool first = lane < 2 * npair && (lane & 1) == 0, second = lane < 2 * npair && (lane & 1);
+    double P = lane < b ? a[lane * 17] : 1.0, Dp = 1.0;
+    if (first) {
+      const double Q = a[(lane + 1) * 17], X = a[lane * 16 + lane + 1];
+      Dp = fma(P, Q, -(X * X));
+    }
+    const double Dsec = __shfl_up_sync(0xffffffffu, Dp, 1);  // a pair's D, at its second column
+    const double Psec = __shfl_up_sync(0xffffffffu, P, 1);
+    double f = lane < b ? (first ? Pow2Scale(Dp, -PivotExponent(Dp)) : second ? 1.0 : Pow2Scale(P, -PivotExponent(P))) : 1.0;
+    double x = f;
+#pragma unroll
+    for (int off = 1; off < 16; off <<= 1) {
+      const double y = __shfl_up_sync(0xffffffffu, x, off);
+      if (lane >= off) x *= y;
+    }
+    double S = __shfl_up_sync(0xffffffffu, x, 1);  // exclusive product
+    if (lane == 0) S = 1.0;
+    const double Sprev = __shfl_up_sync(0xffffffffu, S, 1);  // the pair's scale, at its second column
+    if (second) dk = Dsec * PivotReciprocal(Psec * Sprev);
+    else dk = P * PivotReciprocal(S);
+    if (lane < 16) {
+      s_rp[lane] = lane < b ? (second ? PivotReciprocal(Dsec) : PivotReciprocal(P)) : 0.0;
+      s_aux[lane] = second ? 1.0 : 0.0;
+    }
+  }
+  __syncthreads();
+  // every L value is formed before any is stored (a pair's second column reads its first)
+  double lv = 0.0, l0 = 0.0;
+  if (c < 16 && r > c) {
+    if (s_aux[c] != 0.0) {  // second column of a pair: (P b_r - X a_r) / D
+      const double P = a[(c - 1) * 17], X = a[(c - 1) * 16 + c], ar = a[(c - 1) * 16 + r];
+      lv = fma(P, v, -(X * ar)) * s_rp[c];
+    } else {
+      lv = v * s_rp[c];
+    }
+  }
+  const int rr = t - 111;  // threads 112..126: column 0, rows 1..15
+  if (t >= 112 && t < 127 && rr < b) l0 = a[rr] * s_rp[0];
+  __syncthreads();
+  if (c < 16 && r > c) a[c * 16 + r] = lv;
+  if (t >= 112 && t < 127 && rr < b) a[rr] = l0;
+  if (warp == 0 && lane < b) a[lane * 17] = dk;
+  __syncthreads();
+}
+
 template <int V>
 __global__ void __launch_bounds__(128) BenchF64(const double* tiles, int ntiles, int b, int reps, double* out,
                                              long long* cycles) {
-  __shared__ double a[256], keep[256], s[16];
+  __shared__ double a[256], keep[256], s[16], aux[16];
   const int tile = blockIdx.x % ntiles;
   for (int e = threadIdx.x; e < 256; e += 128) keep[e] = tiles[int64_t(tile) * 256 + e];
   __syncthreads();
@@ -137,7 +231,8 @@ __global__ void __launch_bounds__(128) BenchF64(const double* tiles, int ntiles,
     const long long t0 = clock64();
     if (V == 0) DiagLdltF64(a, b, s);
     else if (V == 1) DiagLdltFF<false>(a, b, s);
-    else DiagLdltFF<true>(a, b, s);
+    else if (V == 2) DiagLdltFF<true>(a, b, s);
+    else DiagLdltFF2(a, b, s, aux);
     __syncthreads();
     total += clock64() - t0;
   }
@@ -188,13 +283,15 @@ int RunF64() {
   cudaMemcpy(d_t, tiles.data(), sizeof(double) * tiles.size(), cudaMemcpyHostToDevice);
   std::vector<double> out(tiles.size());
   std::vector<long long> cyc(608);
-  const char* names[3] = {"reciprocal, 2 barriers", "fraction-free, 1 barrier", "fraction-free, named barriers"};
+  const char* names[4] = {"reciprocal, 2 barriers", "fraction-free, 1 barrier", "fraction-free, named barriers",
+                          "fraction-free, 2 pivots a barrier"};
   for (int b : {16, 11}) {
-    for (int V = 0; V < 3; ++V) {
+    for (int V = 0; V < 4; ++V) {
       for (int grid : {1, 608}) {
         if (V == 0) BenchF64<0><<<grid, 128>>>(d_t, ntiles, b, 200, d_o, d_c);
         if (V == 1) BenchF64<1><<<grid, 128>>>(d_t, ntiles, b, 200, d_o, d_c);
         if (V == 2) BenchF64<2><<<grid, 128>>>(d_t, ntiles, b, 200, d_o, d_c);
+        if (V == 3) BenchF64<3><<<grid, 128>>>(d_t, ntiles, b, 200, d_o, d_c);
         cudaDeviceSynchronize();
         cudaMemcpy(cyc.data(), d_c, sizeof(long long) * grid, cudaMemcpyDeviceToHost);
         double mean = 0; for (int g = 0; g < grid; ++g) mean += cyc[g]; mean /= grid;
