@@ -271,6 +271,8 @@ SchurDev UploadSchur(DeviceArena& A, const SchurLayout& S, int elem) {
   d.r_eoff = A.Upload(S.r_eoff);
   d.r_ecol = A.Upload(S.r_ecol);
   d.r_dk = A.Upload(S.r_dk);
+  d.nBk = S.nB_keys;
+  d.bkey_toff = A.Upload(S.bkey_toff);
   d.r_pt = A.Upload(S.r_pt);
   return d;
 }

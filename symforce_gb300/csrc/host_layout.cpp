@@ -544,6 +544,8 @@ SchurLayout BuildSchurLayout(const HostProblem& P, const LinLayout& L, bool g_at
         S.sb_diag_toff[q] = i == j ? int32_t(P.toff[i]) : -1;
       }
   });
+  S.bkey_toff.resize(size_t(S.nB_keys) + 1);
+  for (int k = 0; k <= S.nB_keys; ++k) S.bkey_toff[size_t(k)] = int32_t(k < S.nB_keys ? P.toff[k] : S.nB);
   // reduced rhs lists: per B scalar, the points that see its key in point order
   S.r_ptr.assign(S.nB + 1, 0);
   for (int k = 0; k < S.nB_keys; ++k)

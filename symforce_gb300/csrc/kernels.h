@@ -91,6 +91,8 @@ void LaunchCopyBest(const double* values, double* dst, int64_t S, const LmState*
 struct SchurDev {
   int npoints;
   int nB;                       // scalar dimension of the reduced system
+  int nBk;                      // keys of the reduced system
+  const int32_t* bkey_toff;     // [nBk + 1] their tangent offsets
   int64_t c_toff;               // tangent offset of the first point
   const int64_t* pt_diag;       // H value offset of each point's 3x3 block
   const int64_t* pt_eptr;       // [np + 1] E blocks of each point

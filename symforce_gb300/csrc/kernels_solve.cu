@@ -398,6 +398,67 @@ __global__ void SchurRhsKernel(SchurDev d, const T* hess_all, int64_t nvals, con
   if (lane == 0) v[i] = g[i] - acc;
 }
 
+// The same per reduced-system key: one warp per key k (d_k scalars), lanes over the points that see
+// it (the list of its first scalar), each point's E_pk block read once, whole and contiguous (a
+// key's blocks lie consecutively in the Hessian values); the lanes' d_k sums are added by the
+// butterfly reduce-scatter.  v_k = g_k - sum_p E_pk^T t_p.
+template <typename T, int DK>
+__device__ __forceinline__ void RhsKeyTerms(const SchurDev& d, const T* H, const T* tp, int64_t q0,
+                                            int64_t q1, int lane, T* sum, int* base, int* cnt) {
+  constexpr int N = DK;
+  T acc[N];
+#pragma unroll
+  for (int c = 0; c < N; ++c) acc[c] = T(0);
+  for (int64_t q = q0 + lane; q < q1; q += 32) {
+    const T* E = H + d.r_eoff[q];
+    const T* t = tp + 3 * int64_t(d.r_pt[q]);
+    T e[3 * N];
+#pragma unroll
+    for (int i = 0; i < 3 * N; ++i) e[i] = E[i];
+    const T t0 = t[0], t1 = t[1], t2 = t[2];
+#pragma unroll
+    for (int c = 0; c < N; ++c) acc[c] += e[c] * t0 + e[N + c] * t1 + e[2 * N + c] * t2;
+  }
+  int b = 0, n = N;
+  ReduceScatterLevel<T, N, 16>(acc, lane, b, n);
+#pragma unroll
+  for (int i = 0; i < ReduceScatterSlots<N>(); ++i) sum[i] = acc[i];
+  *base = b;
+  *cnt = n;
+}
+
+constexpr int kRhsKeyWarpsMin = 1024;  // keys below which the rhs runs a warp per scalar
+
+template <typename T>
+__global__ void SchurRhsKeyKernel(SchurDev d, const T* hess_all, int64_t nvals, const T* rhs_all,
+                                  int64_t N, const T* tp, T* v, const LmState* st) {
+  const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (k >= d.nBk) return;
+  const T* H = hess_all + int64_t(st->init_idx) * nvals;
+  const T* g = rhs_all + int64_t(st->init_idx) * N;
+  const int i0 = d.bkey_toff[k], dk = d.bkey_toff[k + 1] - i0;
+  const int64_t q0 = d.r_ptr[i0], q1 = d.r_ptr[i0 + 1];
+  T sum[2];
+  int base = 0, cnt = 0;
+  if (dk == 6) RhsKeyTerms<T, 6>(d, H, tp, q0, q1, lane, sum, &base, &cnt);
+  else if (dk == 3) RhsKeyTerms<T, 3>(d, H, tp, q0, q1, lane, sum, &base, &cnt);
+  else {
+    // other key sizes: one lane per component, in point order
+    if (lane < dk) {
+      T acc = T(0);
+      for (int64_t q = q0; q < q1; ++q) {
+        const T* E = H + d.r_eoff[q];
+        const T* t = tp + 3 * int64_t(d.r_pt[q]);
+        acc += E[lane] * t[0] + E[dk + lane] * t[1] + E[2 * dk + lane] * t[2];
+      }
+      v[i0 + lane] = g[i0 + lane] - acc;
+    }
+    return;
+  }
+  for (int i = 0; i < cnt; ++i) v[i0 + base + i] = g[i0 + base + i] - sum[i];
+}
+
 // s = W y for one 3 x DK block (all loads issued first; the sums in column order).
 template <typename T, int DK>
 __device__ __forceinline__ void BlockTimes(const T* Wp, const double* yk, T (&s)[3]) {
@@ -2083,9 +2144,22 @@ void LaunchSchurRhs(const SchurDev& d, const void* hess, int64_t nvals, const vo
                     const void* tp, void* v, const LmState* st, cudaStream_t s) {
   if (d.nB == 0) return;
   const int warps = 4;
-  SchurRhsKernel<T><<<(d.nB + warps - 1) / warps, 32 * warps, 0, s>>>(
-      d, static_cast<const T*>(hess), nvals, static_cast<const T*>(rhs), N,
-      static_cast<const T*>(tp), static_cast<T*>(v), st);
+  // a warp per key reads every E block once but has d_k times fewer warps than a warp per scalar:
+  // it is taken when the keys alone fill the GPU (1,000 cameras: 2,000 keys; 50 cameras: 100)
+  // SFG_SCHUR_RHS_PER_SCALAR=0 / 1 overrides
+  static const int force = [] {
+    const char* e = std::getenv("SFG_SCHUR_RHS_PER_SCALAR");
+    return e ? std::atoi(e) : -1;
+  }();
+  const bool per_scalar = force >= 0 ? force != 0 : d.nBk < kRhsKeyWarpsMin;
+  if (per_scalar)
+    SchurRhsKernel<T><<<(d.nB + warps - 1) / warps, 32 * warps, 0, s>>>(
+        d, static_cast<const T*>(hess), nvals, static_cast<const T*>(rhs), N,
+        static_cast<const T*>(tp), static_cast<T*>(v), st);
+  else
+    SchurRhsKeyKernel<T><<<(d.nBk + warps - 1) / warps, 32 * warps, 0, s>>>(
+        d, static_cast<const T*>(hess), nvals, static_cast<const T*>(rhs), N,
+        static_cast<const T*>(tp), static_cast<T*>(v), st);
 }
 
 template <typename T>

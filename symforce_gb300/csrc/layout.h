@@ -50,6 +50,7 @@ struct SchurLayout {
   int64_t nG = 0;                  // G buffer size
   std::vector<int64_t> e_order;    // g_at_e: E blocks in Hessian-offset order (else empty)
   std::vector<int32_t> sb_dk, sb_dl, sb_diag_toff;
+  std::vector<int32_t> bkey_toff;  // [nB_keys + 1] tangent offsets of the reduced system's keys
   std::vector<int64_t> r_ptr, r_eoff;
   std::vector<int32_t> r_ecol, r_dk, r_pt;
 };
