@@ -106,11 +106,15 @@ void BuildFactorPlan(DeviceArena& A, FactorPlan& fp, const BlockPattern& pat, in
     ntasks_solve = int(sp.task_front.size());
   }
   const int per_sm = 8;
-  // the factorization kernel is built for kFactorCtasPerSm resident CTAs of 128 threads per SM
-  // SFG_FACTOR_CTAS_PER_SM (1..kFactorCtasPerSm) narrows the grid for launch-shape measurements
-  int factor_per_sm = kFactorCtasPerSm;
+  // the factorization kernel is built for kFactorCtasPerSm (or, FP64 plans of many fronts,
+  // kFactorCtasPerSmWide) resident CTAs of 128 threads per SM; SFG_FACTOR_WIDE=0 / 1 overrides
+  // SFG_FACTOR_CTAS_PER_SM (1..that) narrows the grid for launch-shape measurements
+  f.wide = (elem == 8 && S.ns >= kFactorWideFronts) ? 1 : 0;
+  if (const char* e = std::getenv("SFG_FACTOR_WIDE")) f.wide = (elem == 8 && std::atoi(e) != 0) ? 1 : 0;
+  const int max_per_sm = f.wide ? kFactorCtasPerSmWide : kFactorCtasPerSm;
+  int factor_per_sm = max_per_sm;
   if (const char* e = std::getenv("SFG_FACTOR_CTAS_PER_SM"))
-    factor_per_sm = std::max(1, std::min(kFactorCtasPerSm, std::atoi(e)));
+    factor_per_sm = std::max(1, std::min(max_per_sm, std::atoi(e)));
   fp.grid_factor = std::max(1, std::min<int>(f.ntasks, num_sms * factor_per_sm));
   fp.grid_solve = std::max(1, std::min<int>(ntasks_solve, num_sms * per_sm));
   if (elem == 8) ConfigureSolve<double>(maxm);

@@ -11,8 +11,13 @@
 namespace sfg {
 
 // Resident CTAs per SM the persistent factorization kernel is compiled for (its register budget:
-// 65,536 / (4 x 128 threads) = 128 per thread, which the register-resident diagonal tasks use).
+// 65,536 / (CTAs x 128 threads) a thread): 4 (128 registers; FP32, and FP64 plans of few fronts,
+// whose chains set the time), and 8 for FP64 plans of many fronts (FactorDev::wide: 64
+// registers, twice the trailing updates in flight; 1,000 cameras, 32 fronts: 3.34 -> 3.07 ms; one
+// 450-wide front: 0.343 -> 0.353 ms).
 constexpr int kFactorCtasPerSm = 4;
+constexpr int kFactorCtasPerSmWide = 8;
+constexpr int kFactorWideFronts = 8;  // FP64 plans of at least this many fronts run wide
 // Tile edge of the factorization.  The critical path of a front is pivots x pivot latency (a chain
 // of dependent FP64 operations, 64 cycles each on this GPU) plus panels x per-panel hand-offs;
 // measured on the 450-unknown reduced system, FP64 tiles of 8 and 16 give the same factor time
@@ -205,6 +210,7 @@ struct FactorDev {
   // leave the kernel) followed by the count of SMs so given, at most iso_limit
   int* sm_flags = nullptr;
   int iso_limit = 0;
+  int wide = 0;  // FP64: the build for kFactorCtasPerSmWide resident CTAs (the grid is sized to it)
   // optional: solves of wide fronts shared by several CTAs (null solve_front: one CTA per front and
   // direction).  Tasks [0, solve_nf) are forward (fronts in order), [solve_nf, solve_nf +
   // solve_nb) backward (fronts in reverse order); each is (front, sub-task).  Per front: solve_kp

@@ -1398,8 +1398,8 @@ __device__ void TaskUpdateTc(const FactorDev& f, int s, int i0, int cnt, int j, 
   }
 }
 
-template <typename T, int TILE>
-__global__ void __launch_bounds__(kFactorThreads, kFactorCtasPerSm) FactorKernel(FactorDev f, const T* A,
+template <typename T, int TILE, int MINB>
+__global__ void __launch_bounds__(kFactorThreads, MINB) FactorKernel(FactorDev f, const T* A,
                                                                const double* damping, T* F,
                                                                T* Linv) {
   // the tile storage; FP32 kernels also stage tensor-core update operands in it (one task at a time)
@@ -2176,11 +2176,25 @@ template <typename T>
 void LaunchFactor(const FactorDev& f, const void* A, const double* damping, void* F, void* Linv,
                   int grid, cudaStream_t s) {
   constexpr int kTile = sizeof(T) == 8 ? kFactorTileF64 : kFactorTileF32;
+  // FP64 plans of many fronts take the build for more resident CTAs (fewer registers a thread):
+  // more trailing updates in flight; a single front's chain runs faster with more registers
+  if constexpr (sizeof(T) == 8) {
+    if (f.wide) {
+      static const cudaError_t carveout = cudaFuncSetAttribute(
+          FactorKernel<T, kTile, kFactorCtasPerSmWide>, cudaFuncAttributePreferredSharedMemoryCarveout,
+          int(cudaSharedmemCarveoutMaxShared));
+      (void)carveout;
+      FactorKernel<T, kTile, kFactorCtasPerSmWide><<<grid, kFactorThreads, 0, s>>>(
+          f, static_cast<const T*>(A), damping, static_cast<T*>(F), static_cast<T*>(Linv));
+      return;
+    }
+  }
   static const cudaError_t carveout = cudaFuncSetAttribute(
-      FactorKernel<T, kTile>, cudaFuncAttributePreferredSharedMemoryCarveout, int(cudaSharedmemCarveoutMaxShared));
+      FactorKernel<T, kTile, kFactorCtasPerSm>, cudaFuncAttributePreferredSharedMemoryCarveout,
+      int(cudaSharedmemCarveoutMaxShared));
   (void)carveout;
-  FactorKernel<T, kTile><<<grid, kFactorThreads, 0, s>>>(f, static_cast<const T*>(A), damping,
-                                                         static_cast<T*>(F), static_cast<T*>(Linv));
+  FactorKernel<T, kTile, kFactorCtasPerSm><<<grid, kFactorThreads, 0, s>>>(
+      f, static_cast<const T*>(A), damping, static_cast<T*>(F), static_cast<T*>(Linv));
 }
 
 template <typename T>
