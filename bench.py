@@ -216,13 +216,16 @@ def run_reference(args) -> None:
 
 
 # The forms beside the plain FP64 drop-in.  "pcg_learned" is the learned-preconditioned
-# mixed-precision solve (FP32 linearization / Schur, PCG with the trained camera-block network, exact
-# LDL^T as fallback, FP64 cost and gain ratio).
+# mixed-precision solve (FP32 linearization / Schur, PCG with the trained camera-block network on the
+# band preconditioner, exact LDL^T as fallback, FP64 cost and gain ratio); "pcg_band" is the same
+# band preconditioner without the network (Lambda = I), "pcg_block_jacobi" the block-diagonal one.
+PCG_BAND = 4  # neighbouring camera blocks of a band preconditioner row (form parameter pcg_band)
 FORMS = {
-    "plain": (A.SFG_PRECISION_FP64, A.SFG_LINEAR_SOLVER_SCHUR),
-    "mixed": (A.SFG_PRECISION_MIXED, A.SFG_LINEAR_SOLVER_SCHUR),
-    "pcg_block_jacobi": (A.SFG_PRECISION_MIXED, A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI),
-    "pcg_learned": (A.SFG_PRECISION_MIXED, A.SFG_LINEAR_SOLVER_PCG_LEARNED),
+    "plain": (A.SFG_PRECISION_FP64, A.SFG_LINEAR_SOLVER_SCHUR, 0),
+    "mixed": (A.SFG_PRECISION_MIXED, A.SFG_LINEAR_SOLVER_SCHUR, 0),
+    "pcg_block_jacobi": (A.SFG_PRECISION_MIXED, A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI, 0),
+    "pcg_band": (A.SFG_PRECISION_MIXED, A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI, PCG_BAND),
+    "pcg_learned": (A.SFG_PRECISION_MIXED, A.SFG_LINEAR_SOLVER_PCG_LEARNED, PCG_BAND),
 }
 SCALE_WORKLOAD = "ba_1000_200k"
 SCALE_10K_WORKLOAD = "ba_10k_1m"  # the learned form's named configuration, in the default run too
@@ -244,9 +247,10 @@ def _form_params(params: A.OptimizerParams, name: str) -> A.OptimizerParams:
 
 
 def _make_form(w, name: str, device: int) -> A.FormParams:
-    prec, solver = FORMS[name]
+    prec, solver, band = FORMS[name]
     form = w.form(prec)
     form.linear_solver = solver
+    form.pcg_band = band
     form.device = device
     return form
 

@@ -224,7 +224,14 @@ typedef struct sfg_form_params_t {
                              (POSE3 keys: world translation, rotation, scale), the near-null space
                              of a bundle-adjustment reduced system, while those directions stay
                              near-null under the damping; 0 (default): blocks only */
-  int32_t reserved;       /* 0 */
+  int32_t pcg_band;       /* PCG forms: 0 (default): one preconditioner block per camera group
+                             (block Jacobi, or the learned blocks); k in 1..6: the factorized sparse
+                             approximate inverse M = G^T Lambda G, where block row i of G is the last
+                             block row of chol(S_JJ)^-1 over J = {i} and the groups i-k .. i-1 coupled
+                             to i in S (the Kaporin-optimal lower factor on that pattern, so that
+                             G S G^T has unit diagonal blocks), and Lambda_i = I (BLOCK_JACOBI) or the
+                             network's L L^T of group i (LEARNED); k = 0 is the block-diagonal case.
+                             Not combined with pcg_coarse. */
 } sfg_form_params_t;
 
 typedef struct sfg_handle sfg_handle;

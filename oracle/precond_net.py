@@ -167,6 +167,110 @@ def samples_of_system(S: np.ndarray, v: np.ndarray, gidx: np.ndarray, degree: np
     return out
 
 
+def band_preconditioner(S: np.ndarray, gidx: np.ndarray, band: int, z: np.ndarray | None = None,
+                        tiny: float = 1e-12, return_factor: bool = False):
+    """The band preconditioner M = G^T Lambda G (dense, n x n) of the PCG forms' pcg_band option.
+
+    Group pattern: groups l, h are coupled when S has a nonzero entry between their scalars.  Per
+    group row l: J_l = {h : l - band <= h < l, coupled to l} + {l} (ascending); A = D^-1/2 S_JJ
+    D^-1/2 (identity on padding and non-positive-diagonal rows), R R^T = A, block row l of G = the
+    last 9 rows of R^-1 times D^-1/2.  A Cholesky that meets a pivot <= tiny retries with J_l = {l};
+    if that fails too the row is D^-1/2 (Jacobi).  Lambda_l = L L^T from the network outputs z
+    (factor_from_outputs), or I.  band = 0 gives assemble()'s block-diagonal P_g.  With
+    return_factor, (M, G) with G dense in the same scalar indices."""
+    n = S.shape[0]
+    ng = gidx.shape[0]
+    valid = gidx >= 0
+    sidx = np.where(valid, gidx, 0)
+
+    def block(a, b):
+        return np.where(valid[a][:, None] & valid[b][None, :], S[np.ix_(sidx[a], sidx[b])], 0.0)
+
+    def coupled(a, b):
+        return bool(np.any(block(a, b) != 0.0))
+
+    d = np.where(valid, np.diag(S)[sidx], 0.0)
+    dis = np.where(valid & (d > 0), 1.0 / np.sqrt(np.where(d > 0, d, 1.0)), -1.0)  # -1: identity row
+    Lam = (np.broadcast_to(np.eye(BLOCK), (ng, BLOCK, BLOCK)) if z is None
+           else np.einsum("nij,nkj->nik", factor_from_outputs(z), factor_from_outputs(z)))
+
+    def chol(A):
+        m = A.shape[0]
+        R = np.zeros_like(A)
+        for j in range(m):
+            s = A[j:, j] - R[j:, :j] @ R[j, :j]
+            if not s[0] > tiny:
+                return None
+            R[j, j] = np.sqrt(s[0])
+            R[j + 1:, j] = s[1:] / R[j, j]
+        return R
+
+    G = {}  # (l, h) -> 9 x 9 block of G
+    for l in range(ng):
+        J = [h for h in range(max(0, l - band), l) if coupled(l, h)] + [l]
+        done = False
+        for Jt in (J, [l]):
+            m = len(Jt)
+            A = np.zeros((9 * m, 9 * m))
+            for i1, a in enumerate(Jt):
+                for i2, b in enumerate(Jt):
+                    A[9 * i1:9 * i1 + 9, 9 * i2:9 * i2 + 9] = block(a, b)
+            ds = np.concatenate([dis[h] for h in Jt])
+            ident = ds < 0
+            A = A * np.where(ident, 1.0, ds)[:, None] * np.where(ident, 1.0, ds)[None, :]
+            A[ident, :] = 0.0
+            A[:, ident] = 0.0
+            A[ident, ident] = 1.0
+            R = chol(A)
+            if R is None:
+                continue
+            X = np.linalg.inv(R)[-9:, :] * np.where(ident, 1.0, ds)[None, :]
+            for i, h in enumerate(Jt):
+                G[(l, h)] = X[:, 9 * i:9 * i + 9]
+            done = True
+            break
+        if not done:
+            G[(l, l)] = np.diag(np.where(d[l] > 0, 1.0 / np.sqrt(np.where(d[l] > 0, d[l], 1.0)), 1.0))
+    Mg = np.zeros((ng, BLOCK, ng, BLOCK))
+    for (l, a), Ga in G.items():
+        for (l2, b), Gb in G.items():
+            if l2 == l:
+                Mg[a, :, b, :] += Ga.T @ Lam[l] @ Gb
+    M = np.zeros((n, n))
+    for a in range(ng):
+        for b in range(ng):
+            blk = Mg[a, :, b, :][np.ix_(valid[a], valid[b])]
+            M[np.ix_(gidx[a][valid[a]], gidx[b][valid[b]])] = blk
+    if not return_factor:
+        return M
+    Gd = np.zeros((n, n))
+    for (l, h), blk in G.items():
+        Gd[np.ix_(gidx[l][valid[l]], gidx[h][valid[h]])] = blk[np.ix_(valid[l], valid[h])]
+    return M, Gd
+
+
+def pcg_dense(S: np.ndarray, v: np.ndarray, M: np.ndarray, tol: float = 1e-8, max_iters: int = 1000):
+    """CG preconditioned by the dense M in float64 (x0 = 0); returns (x, iterations, relative residual)."""
+    x = np.zeros_like(v)
+    r = v.copy()
+    zr = M @ r
+    p = zr.copy()
+    rz = r @ zr
+    vn = np.linalg.norm(v)
+    it = 0
+    while np.linalg.norm(r) > tol * vn and it < max_iters:
+        q = S @ p
+        alpha = rz / (p @ q)
+        x += alpha * p
+        r -= alpha * q
+        zr = M @ r
+        rz_new = r @ zr
+        p = zr + (rz_new / rz) * p
+        rz = rz_new
+        it += 1
+    return x, it, np.linalg.norm(v - S @ x) / vn
+
+
 def pcg(S: np.ndarray, v: np.ndarray, P: np.ndarray, gidx: np.ndarray, tol: float = 1e-8,
         max_iters: int = 1000):
     """Block-preconditioned CG in float64 (x0 = 0); returns (x, iterations, relative residual)."""

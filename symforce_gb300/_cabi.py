@@ -196,7 +196,7 @@ class FormParams(C.Structure):
         ("pcg_max_iters", C.c_int32),
         ("pcg_tol", C.c_double),
         ("pcg_coarse", C.c_int32),
-        ("reserved", C.c_int32),
+        ("pcg_band", C.c_int32),
     ]
 
 
@@ -237,6 +237,7 @@ def default_form_params(**overrides) -> FormParams:
         pcg_max_iters=500,
         pcg_tol=1e-8,
         pcg_coarse=0,
+        pcg_band=0,
     )
     for k, v in overrides.items():
         setattr(f, k, v)

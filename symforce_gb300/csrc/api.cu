@@ -108,6 +108,8 @@ struct sfg_handle {
   float* net = nullptr;
   sfg::PcgState* ps = nullptr;
   sfg::PcgDev pcg{};
+  sfg::BandDev band{};  // band preconditioner (band.band > 0)
+  void* Mband = nullptr;
   int pcg_grid = 1, pcg_threads = 32;
   int collect_cap = 0;
   float* samples = nullptr;
@@ -178,7 +180,12 @@ void EnqueuePrecond(sfg_handle* h, cudaStream_t s) {
   if (h->pcg_mode == 2)
     SFG_CUDA(LaunchMlpInferTc(h->feats, kPrecondFeatures, h->pd.ng, h->net, h->mlp_h1, h->mlp_h2, h->zout,
                               &h->st->device_error, s));
-  LaunchPrecondAssemble<T>(h->pd.ng, h->fac, h->pcg_mode == 2 ? h->zout : nullptr, h->Pblk, s);
+  if (h->band.band > 0) {
+    LaunchBandFactor<T>(h->band, h->Sb, s);
+    LaunchBandAssemble<T>(h->band, h->pcg_mode == 2 ? h->zout : nullptr, h->Mband, s);
+  } else {
+    LaunchPrecondAssemble<T>(h->pd.ng, h->fac, h->pcg_mode == 2 ? h->zout : nullptr, h->Pblk, s);
+  }
 }
 
 // Reduced-system solve of the PCG forms: PCG into ydbl; the exact factorization and solve (with
@@ -398,6 +405,10 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
   h->P = ParseProblem(problem);
   h->precision = fm.precision;
   h->elem = fm.precision == SFG_PRECISION_MIXED ? 4 : 8;
+  if (fm.pcg_band < 0 || fm.pcg_band > kPcgMaxBand)
+    throw Error(SFG_ERR_INVALID_ARGUMENT, "pcg_band must be in 0.." + std::to_string(kPcgMaxBand));
+  if (fm.pcg_band > 0 && fm.pcg_coarse != 0)
+    throw Error(SFG_ERR_INVALID_ARGUMENT, "pcg_band and pcg_coarse cannot be combined");
   if (fm.refine_steps < 0 || fm.refine_steps > 64)
     throw Error(SFG_ERR_INVALID_ARGUMENT, "refine_steps must be in 0..64");
   h->refine_steps = fm.precision == SFG_PRECISION_MIXED ? fm.refine_steps : 0;
@@ -546,6 +557,22 @@ void CreateHandle(const sfg_problem_t* problem, const sfg_form_params_t* form, s
     c.partials = A.Zeros<double>(2 * size_t(kPcgReduceMax) * size_t(h->pcg_grid));
     // the gauge coarse correction needs at least two cameras' poses (otherwise Z^T S Z is singular)
     c.coarse = (fm.pcg_coarse != 0 && PL.gauge_rows >= 12) ? 1 : 0;
+    if (fm.pcg_band > 0) {
+      const BandPattern BP = BuildBandPattern(PL, fm.pcg_band);
+      BandDev& bd = h->band;
+      bd.ng = h->pd.ng;
+      bd.band = fm.pcg_band;
+      bd.nj = A.Upload(BP.nj);
+      bd.jgrp = A.Upload(BP.jgrp);
+      bd.jblk = A.Upload(BP.jblk);
+      bd.gidx = h->pd.gidx;
+      const size_t blocks = size_t(std::max(h->pd.ng, 1)) * (fm.pcg_band + 1);
+      bd.G = A.Zeros<char>(blocks * kPrecondBlock * kPrecondBlock * E);
+      h->Mband = A.Zeros<char>(blocks * kPrecondBlock * kPrecondBlock * E);
+      c.band = fm.pcg_band;
+      c.Mb = h->Mband;
+      c.RQ = A.Zeros<char>(size_t(std::max(h->pd.ng, 1)) * kPrecondBlock * 2 * E);
+    }
     if (c.coarse) {
       const size_t rows = size_t(std::max(h->pd.ng, 1)) * kPrecondBlock;
       c.zg = A.Zeros<char>(size_t(kGaugeDim) * rows * E);
@@ -585,7 +612,8 @@ int BodyKernels(const sfg_handle* h) {
   if (h->elem == 4) n += 1 + 4 * h->refine_steps;  // widen; residual, reset, solve, accumulate
   if (h->pcg_mode) {
     n += 1 /*group blocks*/ + 2 /*row coupling, features*/ + (h->pcg_mode == 2 ? 1 : 0) +
-         1 /*assemble*/ + 1 /*PCG*/ + (h->pcg.coarse ? 1 : 0) /*gauge basis*/;
+         (h->band.band > 0 ? 2 /*band factor, band assembly*/ : 1 /*assemble*/) + 1 /*PCG*/ +
+         (h->pcg.coarse ? 1 : 0) /*gauge basis*/;
     if (h->elem == 8) n += 1;  // widen of the fallback solution
   }
   if (h->collect_cap > 0) n += (h->pcg_mode ? 0 : 2) + 1;

@@ -145,4 +145,33 @@ PrecondLayout BuildPrecondLayout(const HostProblem& P, const SchurLayout& SL) {
   return L;
 }
 
+BandPattern BuildBandPattern(const PrecondLayout& L, int band) {
+  BandPattern B;
+  B.band = band;
+  const int K1 = band + 1;
+  // stored lower group blocks by row: (column, block), ascending (blk_row is nondecreasing)
+  std::vector<std::vector<std::pair<int, int>>> lower(L.ng);
+  for (size_t q = 0; q < L.blk_row.size(); ++q) lower[L.blk_row[q]].push_back({L.blk_col[q], int(q)});
+  for (auto& r : lower) std::sort(r.begin(), r.end());
+  auto find = [&](int g, int h) {
+    auto it = std::lower_bound(lower[g].begin(), lower[g].end(), std::make_pair(h, -1));
+    return (it != lower[g].end() && it->first == h) ? it->second : -1;
+  };
+  B.nj.assign(L.ng, 0);
+  B.jgrp.assign(size_t(L.ng) * K1, -1);
+  B.jblk.assign(size_t(L.ng) * K1 * K1, -1);
+  for (int l = 0; l < L.ng; ++l) {
+    std::vector<int> J;
+    for (const auto& e : lower[l])
+      if (e.first >= l - band && e.first < l) J.push_back(e.first);
+    J.push_back(l);
+    B.nj[l] = int32_t(J.size());
+    for (size_t s1 = 0; s1 < J.size(); ++s1) {
+      B.jgrp[size_t(l) * K1 + s1] = J[s1];
+      for (size_t s2 = 0; s2 <= s1; ++s2) B.jblk[(size_t(l) * K1 + s1) * K1 + s2] = find(J[s1], J[s2]);
+    }
+  }
+  return B;
+}
+
 }  // namespace sfg

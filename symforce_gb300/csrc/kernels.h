@@ -316,6 +316,13 @@ struct PcgDev {
   void* szg;
   const int64_t* gauge_soff;  // [ng * 9] POSE3 storage offset of a pose row, -1 otherwise
   const int32_t* gauge_comp;  // [ng * 9] tangent component of a pose row
+  // factorized sparse approximate inverse over `band` neighbouring groups (band > 0): the lower
+  // band blocks of M = G^T Lambda G, T [ng][band + 1][81] (slot d: M_{g, g - d}, row-major), and
+  // the residual and product of every row, interleaved (T2 [ng][9]), that the rows of M read from
+  // the other CTAs
+  int band = 0;
+  const void* Mb = nullptr;
+  void* RQ = nullptr;
   // optional iteration trace of CTA 0 (SFG_TRACE_PCG): [0] inner iterations of the last solve,
   // then per inner iteration (up to trace_cap) the %globaltimer after the product with S, after
   // the first grid reduction, after the preconditioner, after the second grid reduction
@@ -323,6 +330,25 @@ struct PcgDev {
   int trace_cap = 0;
 };
 constexpr int kGaugeDim = 7;      // world translation 3, rotation 3, scale 1
+constexpr int kPcgMaxBand = 6;    // neighbouring groups of a band preconditioner row (9 (k + 1) <= 63)
+// Pattern of the band preconditioner: per group row l the groups J_l (ascending, the last one l
+// itself; nj[l] of them) and the stored S group block of every pair (J_l[s1], J_l[s2]), s1 >= s2,
+// at jblk[l][s1 * (band + 1) + s2] (-1: a zero block).
+struct BandDev {
+  int ng = 0, band = 0;
+  const int32_t* nj = nullptr;    // [ng]
+  const int32_t* jgrp = nullptr;  // [ng][band + 1]
+  const int32_t* jblk = nullptr;  // [ng][(band + 1)^2]
+  const int32_t* gidx = nullptr;  // [ng][9] reduced-system scalar of each group row, -1 padding
+  void* G = nullptr;              // T [ng][band + 1][81]: block (l, l - band + slot) of G
+};
+// G (block rows of the factorized approximate inverse) from the group blocks Sb of S.
+template <typename T>
+void LaunchBandFactor(const BandDev& b, const void* Sb, cudaStream_t s);
+// The band blocks of M = G^T Lambda G (Lambda_l = L L^T from the network outputs z, or I when z
+// is null) into Mb (T [ng][band + 1][81]).
+template <typename T>
+void LaunchBandAssemble(const BandDev& b, const float* z, void* Mb, cudaStream_t s);
 constexpr int kPcgReduceMax = 32; // values one PCG grid reduction can carry
 // Gather the 9 x 9 group blocks of S: Sb[q][e] = S[off[q][e]] (0 where off < 0).
 template <typename T>

@@ -185,6 +185,291 @@ __global__ void PrecondAssembleKernel(int ng, const float* fac, const float* z, 
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Band preconditioner: factorized sparse approximate inverse M = G^T Lambda G
+// ---------------------------------------------------------------------------------------------
+// Block row l of G is the last block row of R^-1, R R^T = D^-1/2 S_JJ D^-1/2 over the groups J_l
+// (ascending, l last), times D^-1/2: then G S G^T has identity diagonal blocks, and with J_l = {l}
+// it is C^-1 D^-1/2 of the block-diagonal preconditioner, so that Lambda = L L^T keeps the
+// meaning it has there.  One warp per group row, the scaled S_JJ (n = 9 |J_l|) in shared memory
+// with an odd row stride; a block Cholesky by 9 x 9 blocks (the diagonal block by rows, the panel
+// by forward substitution in registers, the trailing update with lanes over independent entries),
+// then X R = [0 I] by block columns from the right.  A pivot that is not numerically positive
+// retries with J_l = {l}; if that fails too the row is D^-1/2 (Jacobi).
+__host__ __device__ constexpr int BandLd(int band) { return 9 * (band + 1) + ((band + 1) % 2 == 0 ? 1 : 0); }
+__host__ __device__ constexpr int BandWarpElems(int band) {
+  return 9 * (band + 1) * BandLd(band) + 9 * (band + 1) + kB * 9 * (band + 1);
+}
+
+template <typename T>
+__global__ void BandFactorKernel(BandDev bd, const T* Sb) {
+  extern __shared__ __align__(16) unsigned char band_smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int l = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (l >= bd.ng) return;  // warp-uniform
+  const int LD = BandLd(bd.band), XLD = 9 * (bd.band + 1);
+  T* A = reinterpret_cast<T*>(band_smem) + size_t(warp) * BandWarpElems(bd.band);
+  T* dis = A + XLD * LD;  // D^-1/2 of the rows; negative: an identity row (padding)
+  T* X = dis + XLD;       // [9][XLD] last block row of R^-1
+  const int K1 = bd.band + 1;
+  const int nj = bd.nj[l];
+  const int32_t* jg = bd.jgrp + size_t(l) * K1;
+  const int32_t* jb = bd.jblk + size_t(l) * K1 * K1;
+  T* Gl = static_cast<T*>(bd.G) + size_t(l) * K1 * kB * kB;
+  const T tiny = T(sizeof(T) == 8 ? 1e-12 : 1e-6);
+  auto pair_of = [](int p, int& s1, int& s2) {
+    s1 = 0;
+    while ((s1 + 1) * (s1 + 2) / 2 <= p) ++s1;
+    s2 = p - s1 * (s1 + 1) / 2;
+  };
+  int s0 = -1;  // first group of J_l that the factor used (-1: none)
+  for (int attempt = 0; attempt < 2 && s0 < 0; ++attempt) {
+    const int first = attempt == 0 ? 0 : nj - 1;
+    const int m = nj - first, n = m * kB, npairs = m * (m + 1) / 2;
+    // lane p: the stored block of lower pair p (at most 28 pairs); every row's padding flag
+    int pblk = -1;
+    if (lane < npairs) {
+      int s1, s2;
+      pair_of(lane, s1, s2);
+      pblk = jb[(first + s1) * K1 + first + s2];
+    }
+    bool padr[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int r = lane + 32 * q;
+      padr[q] = r < n ? bd.gidx[size_t(jg[first + r / kB]) * kB + r % kB] < 0 : true;
+    }
+    // the raw blocks, four pairs (twelve loads a lane) in flight at a time
+    for (int p0 = 0; p0 < npairs; p0 += 4) {
+      T v[4][3];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int p = p0 + u;
+        const int blk = __shfl_sync(0xffffffffu, pblk, p);
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+          const int e = lane + 32 * t;
+          v[u][t] = (p < npairs && blk >= 0 && e < kB * kB) ? Sb[size_t(blk) * (kB * kB) + e] : T(0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int p = p0 + u;
+        if (p >= npairs) break;
+        int s1, s2;
+        pair_of(p, s1, s2);
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+          const int e = lane + 32 * t;
+          if (e < kB * kB) A[(kB * s1 + e / kB) * LD + kB * s2 + e % kB] = v[u][t];
+        }
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int r = lane + 32 * q;
+      if (r < n) {
+        const T d = A[r * LD + r];
+        dis[r] = (!padr[q] && d > T(0)) ? T(1) / sqrt(d) : T(-1);
+      }
+    }
+    __syncwarp();
+    // D^-1/2 S_JJ D^-1/2 (lower), identity rows for padding
+    for (int r = 0; r < n; ++r)
+      for (int c = lane; c <= r; c += 32) {
+        T v = A[r * LD + c];
+        if (dis[r] < T(0) || dis[c] < T(0)) v = r == c ? T(1) : T(0);
+        else v *= dis[r] * dis[c];
+        A[r * LD + c] = v;
+      }
+    __syncwarp();
+    // block Cholesky
+    bool ok = true;
+    for (int sb = 0; sb < m && ok; ++sb) {
+      T* Ass = A + kB * sb * LD + kB * sb;
+      for (int j = 0; j < kB; ++j) {  // the diagonal block, lanes over its rows
+        T v = T(0);
+        if (lane < kB && lane >= j) {
+          v = Ass[lane * LD + j];
+          for (int k = 0; k < j; ++k) v -= Ass[lane * LD + k] * Ass[j * LD + k];
+        }
+        const T piv = __shfl_sync(0xffffffffu, v, j);
+        if (!(piv > tiny)) {  // the same value in every lane: a warp-uniform exit
+          ok = false;
+          break;
+        }
+        const T ljj = sqrt(piv);
+        if (lane == j) Ass[j * LD + j] = ljj;
+        else if (lane < kB && lane > j) Ass[lane * LD + j] = v / ljj;
+        __syncwarp();
+      }
+      if (!ok) break;
+      // the panel below: L_ts = A_ts L_ss^-T, a row per lane in registers
+      for (int i = kB * (sb + 1) + lane; i < n; i += 32) {
+        T x[kB];
+#pragma unroll
+        for (int c = 0; c < kB; ++c) x[c] = A[i * LD + kB * sb + c];
+#pragma unroll
+        for (int c = 0; c < kB; ++c) {
+#pragma unroll
+          for (int k = 0; k < c; ++k) x[c] -= x[k] * Ass[c * LD + k];
+          x[c] /= Ass[c * LD + c];
+        }
+#pragma unroll
+        for (int c = 0; c < kB; ++c) A[i * LD + kB * sb + c] = x[c];
+      }
+      __syncwarp();
+      // the trailing lower blocks (t, u), sb < u <= t < m: A_tu -= L_ts L_us^T
+      const int q = m - 1 - sb;
+      const int tp = q * (q + 1) / 2;
+      for (int pr = 0; pr < tp; ++pr) {
+        int tt, uu;
+        pair_of(pr, tt, uu);
+        const int t = sb + 1 + tt, u = sb + 1 + uu;
+        for (int e = lane; e < kB * kB; e += 32) {
+          const int r = e / kB, c = e % kB;
+          if (t == u && c > r) continue;
+          const T* lt = A + (kB * t + r) * LD + kB * sb;
+          const T* lu = A + (kB * u + c) * LD + kB * sb;
+          T acc = A[(kB * t + r) * LD + kB * u + c];
+#pragma unroll
+          for (int k = 0; k < kB; ++k) acc -= lt[k] * lu[k];
+          A[(kB * t + r) * LD + kB * u + c] = acc;
+        }
+      }
+      __syncwarp();
+    }
+    if (!ok) {
+      __syncwarp();
+      continue;
+    }
+    // X R = [0 I] by block columns from the right: X_s R_ss = delta(s, m - 1) I - sum_{t > s} X_t R_ts
+    for (int sb = m - 1; sb >= 0; --sb) {
+      for (int e = lane; e < kB * kB; e += 32) {
+        const int r = e / kB, c = e % kB;
+        T b = (sb == m - 1 && r == c) ? T(1) : T(0);
+        for (int t = sb + 1; t < m; ++t) {
+          const T* xr = X + r * XLD + kB * t;
+#pragma unroll
+          for (int k = 0; k < kB; ++k) b -= xr[k] * A[(kB * t + k) * LD + kB * sb + c];
+        }
+        X[r * XLD + kB * sb + c] = b;
+      }
+      __syncwarp();
+      if (lane < kB) {  // row `lane` of X_s: x R_ss = b, from the last column down
+        const T* Ass = A + kB * sb * LD + kB * sb;
+        T x[kB];
+#pragma unroll
+        for (int c = 0; c < kB; ++c) x[c] = X[lane * XLD + kB * sb + c];
+#pragma unroll
+        for (int c = kB - 1; c >= 0; --c) {
+#pragma unroll
+          for (int k = c + 1; k < kB; ++k) x[c] -= x[k] * Ass[k * LD + c];
+          x[c] /= Ass[c * LD + c];
+        }
+#pragma unroll
+        for (int c = 0; c < kB; ++c) X[lane * XLD + kB * sb + c] = x[c];
+      }
+      __syncwarp();
+    }
+    s0 = first;
+  }
+  // block (l, l - band + slot) of G: X's columns of that group times D^-1/2
+  for (int e = lane; e < K1 * kB * kB; e += 32) {
+    const int slot = e / (kB * kB), rc = e - slot * (kB * kB), r = rc / kB, c = rc % kB;
+    const int grp = l - bd.band + slot;
+    T v = T(0);
+    if (s0 >= 0) {
+      for (int sg = s0; sg < nj; ++sg)
+        if (jg[sg] == grp) {
+          const int col = (sg - s0) * kB + c;
+          v = X[r * XLD + col] * (dis[col] < T(0) ? T(1) : dis[col]);
+        }
+    } else if (grp == l && r == c) {  // Jacobi row
+      const int blk = jb[(nj - 1) * K1 + nj - 1];
+      const T d = blk >= 0 ? Sb[size_t(blk) * (kB * kB) + r * kB + r] : T(0);
+      v = d > T(0) ? T(1) / sqrt(d) : T(1);
+    }
+    Gl[e] = v;
+  }
+}
+
+// M_{a, a - d} = sum over l = a .. min(a - d + band, ng - 1) of G_{l,a}^T Lambda_l G_{l,a-d}; one
+// warp per (a, d), four warps per CTA.  All the terms' blocks (and network outputs) are loaded into
+// shared memory at once, then added in l order.
+constexpr int kBandAsmWarps = 4;
+template <typename T>
+__global__ void BandAssembleKernel(BandDev bd, const float* z, T* Mb) {
+  constexpr int kT = kPcgMaxBand + 1;
+  __shared__ T sg[kBandAsmWarps][kT][2][kB * kB];
+  __shared__ float sz[kBandAsmWarps][kT][kPrecondTri];
+  __shared__ T stt[kBandAsmWarps][2][kB * kB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int K1 = bd.band + 1;
+  const int idx = blockIdx.x * kBandAsmWarps + warp;
+  if (idx >= bd.ng * K1) return;  // warp-uniform
+  const int a = idx / K1, b = a - idx % K1;
+  const int nterm = b >= 0 ? min(b + bd.band, bd.ng - 1) - a + 1 : 0;
+  for (int e = lane; e < nterm * 2 * kB * kB; e += 32) {
+    const int t = e / (2 * kB * kB), w = (e / (kB * kB)) & 1, x = e % (kB * kB);
+    const int l = a + t;
+    const int slot = (w ? b : a) - l + bd.band;
+    sg[warp][t][w][x] = static_cast<const T*>(bd.G)[(size_t(l) * K1 + slot) * (kB * kB) + x];
+  }
+  if (z)
+    for (int e = lane; e < nterm * kPrecondTri; e += 32)
+      sz[warp][e / kPrecondTri][e % kPrecondTri] = z[size_t(a + e / kPrecondTri) * kPrecondTri + e % kPrecondTri];
+  __syncwarp();
+  T acc[3] = {T(0), T(0), T(0)};
+  T* Lm = stt[warp][0];
+  T* tt = stt[warp][1];
+  for (int t = 0; t < nterm; ++t) {
+    const T* ga = sg[warp][t][0];
+    T* gb = sg[warp][t][1];
+    if (z) {  // gb <- L (L^T gb)
+      const float* zl = sz[warp][t];
+      for (int e = lane; e < kB * kB; e += 32) {
+        const int i = e / kB, j = e % kB;
+        Lm[e] = j > i ? T(0) : i == j ? T(Softplus(zl[Tri(i, i)] + kDiagShift)) : T(zl[Tri(i, j)]);
+      }
+      __syncwarp();
+      for (int e = lane; e < kB * kB; e += 32) {
+        const int x = e / kB, c = e % kB;
+        T s = T(0);
+        for (int y = x; y < kB; ++y) s += Lm[y * kB + x] * gb[y * kB + c];
+        tt[e] = s;
+      }
+      __syncwarp();
+      for (int e = lane; e < kB * kB; e += 32) {
+        const int x = e / kB, c = e % kB;
+        T s = T(0);
+        for (int y = 0; y <= x; ++y) s += Lm[x * kB + y] * tt[y * kB + c];
+        gb[e] = s;
+      }
+      __syncwarp();
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int e = lane + 32 * k;
+      if (e < kB * kB) {
+        const int r = e / kB, c = e % kB;
+        T s = T(0);
+#pragma unroll
+        for (int x = 0; x < kB; ++x) s += ga[x * kB + r] * gb[x * kB + c];
+        acc[k] += s;
+      }
+    }
+    __syncwarp();
+  }
+  T* out = Mb + size_t(idx) * (kB * kB);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int e = lane + 32 * k;
+    if (e < kB * kB) out[e] = acc[k];
+  }
+}
+
 // Training samples of the current system: inputs, g_hat = C^-1 D^-1/2 v_g, x_hat = C^T D^1/2 y_g.
 template <typename T>
 __global__ void CollectSamplesKernel(PrecondDev pd, const float* feats, const float* fac,
@@ -356,6 +641,49 @@ __device__ __forceinline__ V CombineSplit(V x, int a) {
     const V t2 = __shfl_sync(0xffffffffu, x, a + 2 * kB);
     return (t0 + t1) + t2;
   }
+}
+
+template <typename T> struct PairOf;
+template <> struct PairOf<float> { using type = float2; };
+template <> struct PairOf<double> { using type = double2; };
+
+// Row a of group row g of the band preconditioner M times x_h = r_h - alpha q_h (kQ) or r_h, over
+// the neighbours h = g + j, j = -band + phase, -band + phase + stride, ... <= band; (r, q) of
+// every row interleaved in rq.  M_{g,h} is the stored block (g, g - h) for h <= g and the
+// transposed block (h, h - g) above.  Lane a of the row's nine lanes (gbase + a) loads entry a of
+// x_h and the nine lanes exchange them by shuffles; three blocks at a time, every load issued
+// before the multiply-adds.  Called by all lanes of the warp with the same trip count (lanes with
+// ok_row false add nothing).
+template <bool kQ, int SPLIT, typename T>
+__device__ __forceinline__ T BandRow(const T* Mb, int band, int ng, int g, int a, int gbase, int phase,
+                                     bool ok_row, const typename PairOf<T>::type* rq, T alpha) {
+  constexpr int U = sizeof(T) == 8 ? 2 : 3;
+  const int K1 = band + 1;
+  const int per_phase = (2 * band + SPLIT) / SPLIT;  // blocks of phase 0, the most of any phase
+  const int trips = (per_phase + U - 1) / U;
+  T acc = T(0);
+  for (int t = 0; t < trips; ++t) {
+    T mv[U][kB], xe[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int j = -band + phase + (t * U + u) * SPLIT;
+      const int h = g + j;
+      const bool ok = ok_row && j <= band && h >= 0 && h < ng;
+      const int hc = ok ? h : 0;
+      const T* blk = j <= 0 ? Mb + (size_t(ok ? g : 0) * K1 + (ok ? -j : 0)) * (kB * kB) + a * kB
+                            : Mb + (size_t(hc) * K1 + (ok ? j : 0)) * (kB * kB) + a;
+      const int step = j <= 0 ? 1 : kB;
+#pragma unroll
+      for (int b = 0; b < kB; ++b) mv[u][b] = ok ? blk[b * step] : T(0);
+      const auto v = __ldcg(rq + size_t(hc) * kB + a);
+      xe[u] = ok ? (kQ ? v.x - alpha * v.y : v.x) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int b = 0; b < kB; ++b) acc += mv[u][b] * __shfl_sync(0xffffffffu, xe[u], gbase + b);
+  }
+  return acc;
 }
 
 struct PcgShared {
@@ -553,9 +881,10 @@ __device__ __forceinline__ void PcgStamp(const PcgDev& d, int it, int phase) {
 // LaunchGaugeBasis).  S Z is formed once per launch and kept by row, so that the product of a search
 // direction stays one pass over S: S z = S (P r) + (S Z) c, c = E Z^T r, and Z^T r rides in the
 // grid reduction that already follows the update of r.
-template <typename T, bool kStaged, int SPLIT, bool kCoarse>
+template <typename T, bool kStaged, int SPLIT, bool kCoarse, bool kBand>
 __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
   static_assert(SPLIT == 1 || SPLIT == 3, "one or three lanes per row");
+  static_assert(!(kCoarse && kBand), "the coarse correction goes with the block-diagonal preconditioner");
   extern __shared__ __align__(16) unsigned char pcg_smem[];
   __shared__ PcgShared sm;
   __shared__ double redn[kCoarse ? 32 * (2 + kGaugeDim) : 1];
@@ -612,7 +941,21 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
   const T* P = static_cast<const T*>(d.P);
   T prow[kB];
 #pragma unroll
-  for (int b = 0; b < kB; ++b) prow[b] = row_ok ? P[(size_t(g) * kB + a) * kB + b] : T(0);
+  for (int b = 0; b < kB; ++b) prow[b] = (!kBand && row_ok) ? P[(size_t(g) * kB + a) * kB + b] : T(0);
+  using T2 = typename PairOf<T>::type;
+  const T* Mb = static_cast<const T*>(d.Mb);
+  T2* rq = static_cast<T2*>(d.RQ);
+  // the preconditioned residual of this row: the block product in registers, or a row of the
+  // band preconditioner over the (r, q) that every row stored before the last grid reduction
+  auto precond = [&](T r, T alpha, bool with_q) -> T {
+    if constexpr (kBand) {
+      const T zb = with_q ? BandRow<true, SPLIT>(Mb, d.band, ng, g, a, gbase, split, in_group, rq, alpha)
+                          : BandRow<false, SPLIT>(Mb, d.band, ng, g, a, gbase, split, in_group, rq, alpha);
+      return CombineSplit<SPLIT>(zb, a);
+    } else {
+      return ApplyBlock(prow, r, gbase);
+    }
+  };
   int seq = 0;
   const double vs = row_ok ? double(v[s]) : 0.0;
   GridReduce<double>(own ? vs * vs : 0.0, 0.0, d, seq, sm, [&](double x, double) {
@@ -677,6 +1020,9 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
           in_group ? GroupRow<double, kStaged>(Sb, gent, e0, e1, SPLIT, a, ygv) : 0.0, a);
       if (in_group) r64 = vs - sy;
     }
+    if constexpr (kBand) {
+      if (store) __stcg(rq + gi, T2{T(r64), T(0)});
+    }
     GridReduce<double>(own ? r64 * r64 : 0.0, 0.0, d, seq, sm, [&](double x, double) {
       sm.rel = sqrt(x) / vnorm;
       sm.converged = sm.rel <= d.tol ? 1 : 0;
@@ -692,7 +1038,7 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
     // lose the digits the recurrences need on these ill-conditioned systems).  The product uses
     // w = S z and q = w + beta q so that one grid reduction separates the product from the update.
     T r = T(r64);
-    T zz = ApplyBlock(prow, r, gbase);
+    T zz = precond(r, T(0), false);
     if (store) StX<kStaged>(zv + gi, zz);
     T zf = zz;  // the preconditioned residual (with the coarse correction)
     if constexpr (kCoarse) {
@@ -721,6 +1067,9 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
       }
       p = zf + beta * p;
       qv = w + beta * qv;
+      if constexpr (kBand) {
+        if (store) __stcg(rq + gi, T2{r, qv});
+      }
       GridReduce<double>(own ? double(p) * double(qv) : 0.0, 0.0, d, seq, sm, [&](double pq, double) {
         const double rz = sm.rz;
         if (!(pq > 0.0) || !(pq < 1e300) || !(fabs(rz) < 1e300)) sm.broke = 1;
@@ -731,7 +1080,7 @@ __global__ void __launch_bounds__(1024) PcgKernel(PcgDev d) {
       const T alpha = T(sm.alpha);
       dx += alpha * p;
       r -= alpha * qv;
-      zz = ApplyBlock(prow, r, gbase);
+      zz = precond(r, alpha, true);
       if (store) StX<kStaged>(zv + gi, zz);
       PcgStamp(d, traced, 2);
       if constexpr (kCoarse) {
@@ -863,14 +1212,16 @@ void LaunchCollectSamples(const PrecondDev& pd, const float* feats, const float*
 
 template <typename T, int SPLIT>
 int PcgMaxResidentCtas(int threads, int num_sms) {
-  // the coarse variant uses more registers and shared memory: the smaller count of the two
-  int per_sm = 0, per_sm_c = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, PcgKernel<T, false, SPLIT, false>, threads, 0) !=
+  // the coarse and band variants use more registers and shared memory: the smallest count
+  int per_sm = 0, per_sm_c = 0, per_sm_b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, PcgKernel<T, false, SPLIT, false, false>, threads, 0) !=
           cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c, PcgKernel<T, false, SPLIT, true>, threads, 0) !=
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_c, PcgKernel<T, false, SPLIT, true, false>, threads, 0) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_b, PcgKernel<T, false, SPLIT, false, true>, threads, 0) !=
           cudaSuccess)
     return 0;
-  return std::min(per_sm, per_sm_c) * num_sms;
+  return std::min(std::min(per_sm, per_sm_c), per_sm_b) * num_sms;
 }
 
 template <typename T>
@@ -918,8 +1269,12 @@ template size_t PcgStagedSmem<float>(int, int, int);
 
 template <typename T>
 void ConfigurePcg() {
-  cudaFuncSetAttribute(PcgKernel<T, true, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPcgStagedMax));
-  cudaFuncSetAttribute(PcgKernel<T, true, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kPcgStagedMax));
+  cudaFuncSetAttribute(PcgKernel<T, true, 1, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       int(kPcgStagedMax));
+  cudaFuncSetAttribute(PcgKernel<T, true, 1, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       int(kPcgStagedMax));
+  cudaFuncSetAttribute(PcgKernel<T, true, 1, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       int(kPcgStagedMax));
 }
 template void ConfigurePcg<double>();
 template void ConfigurePcg<float>();
@@ -934,13 +1289,13 @@ void LaunchGroupBlocks(const int64_t* off, int64_t n, const void* S, void* Sb, c
 template void LaunchGroupBlocks<double>(const int64_t*, int64_t, const void*, void*, cudaStream_t);
 template void LaunchGroupBlocks<float>(const int64_t*, int64_t, const void*, void*, cudaStream_t);
 
-template <typename T, bool kCoarse>
+template <typename T, bool kCoarse, bool kBand>
 cudaError_t LaunchPcgVariant(const PcgDev& d, int grid, int threads, cudaStream_t s) {
   if (grid == 1) {
     if (d.staged) {
-      PcgKernel<T, true, 1, kCoarse><<<1, threads, size_t(d.staged), s>>>(d);
+      PcgKernel<T, true, 1, kCoarse, kBand><<<1, threads, size_t(d.staged), s>>>(d);
     } else {
-      PcgKernel<T, false, 1, kCoarse><<<1, threads, 0, s>>>(d);
+      PcgKernel<T, false, 1, kCoarse, kBand><<<1, threads, 0, s>>>(d);
     }
     return cudaGetLastError();
   }
@@ -956,14 +1311,37 @@ cudaError_t LaunchPcgVariant(const PcgDev& d, int grid, int threads, cudaStream_
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (d.split == 3) return cudaLaunchKernelEx(&cfg, PcgKernel<T, false, 3, kCoarse>, d);
-  return cudaLaunchKernelEx(&cfg, PcgKernel<T, false, 1, kCoarse>, d);
+  if (d.split == 3) return cudaLaunchKernelEx(&cfg, PcgKernel<T, false, 3, kCoarse, kBand>, d);
+  return cudaLaunchKernelEx(&cfg, PcgKernel<T, false, 1, kCoarse, kBand>, d);
 }
 
 template <typename T>
 cudaError_t LaunchPcg(const PcgDev& d, int grid, int threads, cudaStream_t s) {
-  return d.coarse ? LaunchPcgVariant<T, true>(d, grid, threads, s) : LaunchPcgVariant<T, false>(d, grid, threads, s);
+  if (d.band > 0) return LaunchPcgVariant<T, false, true>(d, grid, threads, s);
+  return d.coarse ? LaunchPcgVariant<T, true, false>(d, grid, threads, s)
+                  : LaunchPcgVariant<T, false, false>(d, grid, threads, s);
 }
+
+template <typename T>
+void LaunchBandFactor(const BandDev& b, const void* Sb, cudaStream_t s) {
+  if (b.ng == 0) return;
+  // warps per CTA: as many as 48 KB of shared memory holds (at most 8)
+  const size_t per_warp = size_t(BandWarpElems(b.band)) * sizeof(T);
+  const int w = int(std::max<size_t>(1, std::min<size_t>(8, (48 * 1024) / per_warp)));
+  BandFactorKernel<T><<<(b.ng + w - 1) / w, 32 * w, w * per_warp, s>>>(b, static_cast<const T*>(Sb));
+}
+
+template <typename T>
+void LaunchBandAssemble(const BandDev& b, const float* z, void* Mb, cudaStream_t s) {
+  const int n = b.ng * (b.band + 1);
+  if (n == 0) return;
+  BandAssembleKernel<T><<<(n + kBandAsmWarps - 1) / kBandAsmWarps, 32 * kBandAsmWarps, 0, s>>>(
+      b, z, static_cast<T*>(Mb));
+}
+template void LaunchBandFactor<double>(const BandDev&, const void*, cudaStream_t);
+template void LaunchBandFactor<float>(const BandDev&, const void*, cudaStream_t);
+template void LaunchBandAssemble<double>(const BandDev&, const float*, void*, cudaStream_t);
+template void LaunchBandAssemble<float>(const BandDev&, const float*, void*, cudaStream_t);
 
 template <typename T>
 void LaunchGaugeBasis(const PcgDev& d, const double* values, int64_t S, const LmState* st, cudaStream_t s) {

@@ -82,4 +82,15 @@ struct PrecondLayout {
 };
 PrecondLayout BuildPrecondLayout(const HostProblem& P, const SchurLayout& SL);
 
+// Pattern of the band preconditioner over `band` neighbouring groups: per group row l the groups
+// J_l = {h : l - band <= h < l, S_lh stored} + {l} (ascending) and the stored group block of
+// every pair (J_l[s1], J_l[s2]), s1 >= s2 (-1: structurally zero).
+struct BandPattern {
+  int band = 0;
+  std::vector<int32_t> nj;    // [ng]
+  std::vector<int32_t> jgrp;  // [ng][band + 1], -1 past nj
+  std::vector<int32_t> jblk;  // [ng][band + 1][band + 1]
+};
+BandPattern BuildBandPattern(const PrecondLayout& L, int band);
+
 }  // namespace sfg

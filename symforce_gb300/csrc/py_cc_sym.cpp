@@ -278,11 +278,11 @@ int OptimizerInit(PyOptimizer* self, PyObject* args, PyObject* kwds) {
   sfg_default_form_params(&fp);
   fp.epsilon = epsilon;
   fp.linear_solver = num_schur > 0 ? SFG_LINEAR_SOLVER_SCHUR : SFG_LINEAR_SOLVER_SPARSE_LDLT;
-  const char* form_int[] = {"precision",    "linear_solver", "ordering",  "device",
-                            "refine_steps", "pcg_max_iters", "pcg_coarse"};
-  int32_t* form_dst[] = {&fp.precision,    &fp.linear_solver, &fp.ordering,  &fp.device,
-                         &fp.refine_steps, &fp.pcg_max_iters, &fp.pcg_coarse};
-  for (int i = 0; i < 7; ++i)
+  const char* form_int[] = {"precision",    "linear_solver", "ordering",   "device",
+                            "refine_steps", "pcg_max_iters", "pcg_coarse", "pcg_band"};
+  int32_t* form_dst[] = {&fp.precision,    &fp.linear_solver, &fp.ordering,   &fp.device,
+                         &fp.refine_steps, &fp.pcg_max_iters, &fp.pcg_coarse, &fp.pcg_band};
+  for (int i = 0; i < 8; ++i)
     if (PyObject* v = Field(form, form_int[i])) {
       *form_dst[i] = int32_t(PyLong_AsLong(v));
       Py_DECREF(v);

@@ -223,3 +223,62 @@ def test_gauge_coarse_correction_cuts_iterations(precision):
     assert abs(best1 - best0) <= 1e-6 * best0, (best0, best1)
     assert ps1["fallbacks"] <= ps0["fallbacks"], (ps0, ps1)
     assert ps1["iterations"] < ps0["iterations"], (ps0, ps1)
+
+
+@pytest.mark.parametrize("band", [2, 5])
+@pytest.mark.parametrize("solver", [A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI, A.SFG_LINEAR_SOLVER_PCG_LEARNED])
+def test_band_preconditioner_iterations_match_oracle(band, solver):
+    """One FP64 PCG solve with the band preconditioner (one CTA, 16 cameras): the same iteration
+    count, within 2, as the oracle's float64 PCG with its M = G^T Lambda G on the same reduced
+    system (the first LM iteration: initial values, lambda = 1), for Lambda = I and for the
+    network's blocks (small random weights, every layer active)."""
+    p = synth.bundle_adjustment(num_cameras=16, num_points=800, num_observations=4800, seed=4)
+    params = A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC, iterations=1)
+    w = PC.random_weights(7, out_scale=0.05) if solver == A.SFG_LINEAR_SOLVER_PCG_LEARNED else None
+    opt = Optimizer(p, params, A.default_form_params(linear_solver=solver, pcg_band=band), weights=w)
+    opt.optimize(p.values, num_iterations=1)
+    ps = opt.pcg_stats()
+    S, v = PC.reduced_system(p)
+    gidx, degree = PC.camera_blocks(p)
+    z = None
+    if w is not None:
+        z = PN.forward(w.astype(np.float64), PN.block_features(S, gidx, degree)[0])
+    _, it, _ = PN.pcg_dense(S, v, PN.band_preconditioner(S, gidx, band, z), tol=0.5e-8)
+    _, it0, _ = PN.pcg_dense(S, v, PN.band_preconditioner(S, gidx, 0, z), tol=0.5e-8)
+    assert ps["solves"] == 1 and ps["fallbacks"] == 0, ps
+    assert abs(ps["iterations"] - it) <= 2, (ps, it, it0)
+    assert it < it0, (it, it0)
+
+
+@pytest.mark.parametrize("precision", [A.SFG_PRECISION_FP64, A.SFG_PRECISION_MIXED])
+def test_band_preconditioner_multi_cta_reaches_plain_cost(precision):
+    """300 cameras (a cooperative multi-CTA launch whose rows of M read the other CTAs' residuals):
+    block Jacobi and the band preconditioner over 4 neighbouring camera blocks reach the plain FP64
+    form's cost, and the band needs fewer PCG iterations in total."""
+    p = synth.bundle_adjustment(num_cameras=300, num_points=6000, num_observations=30000, seed=11)
+    params = A.default_optimizer_params(lambda_update_type=A.SFG_LAMBDA_UPDATE_DYNAMIC, iterations=30,
+                                        early_exit_min_reduction=1e-9)
+    plain = Optimizer(p, params, A.default_form_params(linear_solver=A.SFG_LINEAR_SOLVER_SCHUR))
+    _, plain_stats = plain.optimize(p.values)
+    ref = min(r.best_error for r in plain_stats.iterations)
+    its = {}
+    for band in (0, 4):
+        opt = Optimizer(p, params, A.default_form_params(precision=precision, pcg_band=band,
+                                                        linear_solver=A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI))
+        _, stats = opt.optimize(p.values)
+        best = min(r.best_error for r in stats.iterations)
+        assert abs(best - ref) <= 1e-6 * ref, (band, best, ref)
+        ps = opt.pcg_stats()
+        assert ps["solves"] == len(stats.iterations) - 1, ps
+        if precision == A.SFG_PRECISION_FP64:
+            assert ps["fallbacks"] == 0 and ps["max_rel_residual"] <= 1e-8, ps
+        its[band] = ps["iterations"] / ps["solves"]
+    assert its[4] < 0.85 * its[0], its
+
+
+def test_band_option_rejects_bad_values():
+    p = PC.small_ba(3)
+    params = A.default_optimizer_params()
+    for bad in (dict(pcg_band=-1), dict(pcg_band=7), dict(pcg_band=2, pcg_coarse=1)):
+        with pytest.raises(RuntimeError):
+            Optimizer(p, params, A.default_form_params(linear_solver=A.SFG_LINEAR_SOLVER_PCG_BLOCK_JACOBI, **bad))
