@@ -254,7 +254,8 @@ struct FactorEval<SFG_FACTOR_SNAVELY_REPROJECTION, T> {
     const double e0 = f * g * u - px;
     const double e1 = f * g * v - py;
     // whitening
-    double s = 1.0, t = 0.0;  // dw/de = s I + t e e^T
+    double s = 1.0;  // dw/de = s I + t e e^T
+    T Tt = T(0);
     if (delta > 0) {
       const double n2 = e0 * e0 + e1 * e1 + eps;
       const double n = sqrt(n2);
@@ -262,13 +263,20 @@ struct FactorEval<SFG_FACTOR_SNAVELY_REPROJECTION, T> {
       const double rho2 = 2.0 * delta * delta * log1p(uu);
       const double sq = sqrt(rho2);
       s = sq / n;
-      const double dsdn = (n2 / ((1.0 + uu) * sq) - sq) / n2;
-      t = dsdn / n;
+      // t only enters the Jacobian: in its precision (two divisions off the FP64 pipe in FP32)
+      if constexpr (sizeof(T) == 8) {
+        const double dsdn = (n2 / ((1.0 + uu) * sq) - sq) / n2;
+        Tt = T(dsdn / n);
+      } else {
+        const T fn2 = T(n2), fsq = T(sq);
+        const T dsdn = (fn2 / ((T(1) + T(uu)) * fsq) - fsq) / fn2;
+        Tt = dsdn / T(n);
+      }
     }
     r[0] = s * e0;
     r[1] = s * e1;
     // Jacobian chain in T
-    const T Ts = T(s), Tt = T(t), Te0 = T(e0), Te1 = T(e1);
+    const T Ts = T(s), Te0 = T(e0), Te1 = T(e1);
     const T W00 = Ts + Tt * Te0 * Te0, W01 = Tt * Te0 * Te1, W11 = Ts + Tt * Te1 * Te1;
     const T Tu = T(u), Tv = T(v), Tf = T(f), Tg = T(g), Tr2 = T(r2);
     const T dg = T(2) * (T(k1) + T(2) * T(k2) * Tr2);
