@@ -258,6 +258,15 @@ void shim_precond_arrays(int32_t* gidx, int64_t* blk_off, int32_t* gptr, int32_t
   Put(g_pre.gent, gent);
 }
 
+// Band preconditioner pattern over `band` neighbouring groups of the camera blocks built last:
+// nj [ng], jgrp [ng][band + 1], jblk [ng][band + 1][band + 1].
+void shim_band_pattern(int band, int32_t* nj, int32_t* jgrp, int32_t* jblk) {
+  const sfg::BandPattern B = sfg::BuildBandPattern(g_pre, band);
+  Put(B.nj, nj);
+  Put(B.jgrp, jgrp);
+  Put(B.jblk, jblk);
+}
+
 // Split of the front solves (block_tiles pivot tiles a CTA, `warps` warps a CTA) of the factor
 // plan built last: out = {forward tasks, all tasks}; then shim_solve_split_arrays.
 static sfg::SolveSplit g_split;

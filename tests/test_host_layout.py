@@ -579,6 +579,26 @@ def test_camera_block_rows_give_the_reduced_system_product(shim):
     ref = Sd @ x
     ok = gidx >= 0
     np.testing.assert_allclose(y[ok], ref[gidx[ok]], rtol=1e-12, atol=1e-12)
+    # band preconditioner pattern: J_l = the groups l - band .. l - 1 that S couples to l, then l;
+    # the stored block of every lower pair of J_l
+    lower = {}
+    for g in range(ng):
+        for e in range(gptr[g], gptr[g + 1]):
+            blk, nb = int(gent[2 * e]), int(gent[2 * e + 1])
+            if not nb & 1:
+                lower[(g, nb >> 1)] = blk
+    for band in (1, 3):
+        k1 = band + 1
+        nj, jgrp, jblk = _arr(ng, np.int32), _arr(ng * k1, np.int32), _arr(ng * k1 * k1, np.int32)
+        shim.shim_band_pattern(band, _ptr(nj), _ptr(jgrp), _ptr(jblk))
+        jgrp, jblk = jgrp.reshape(ng, k1), jblk.reshape(ng, k1, k1)
+        for g in range(ng):
+            J = [h for h in range(max(0, g - band), g) if (g, h) in lower] + [g]
+            assert nj[g] == len(J) and jgrp[g, :len(J)].tolist() == J, (band, g, J)
+            for s1 in range(len(J)):
+                for s2 in range(s1 + 1):
+                    assert jblk[g, s1, s2] == lower.get((J[s1], J[s2]), -1), (band, g, s1, s2)
+        assert int(nj.max()) > 1  # some rows do couple to earlier groups
 
 
 def _random_pose3_graph(rng, nposes, nbetween, nrange):
